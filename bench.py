@@ -1,0 +1,321 @@
+"""Benchmark: particle-steps/s of the FP64 drop-in stepsolve! on one GB300.
+
+Workload (default): 2-D dam break, plain FP64 single instance -- fluid column
+1.0 x 2.0 m at dx = 0.02 (5,000 particles, ρ = 1000, v = 0) in a 4.0 x 3.0 m
+tank with 3 lattice rows of fixed boundary particles (ptype 0), WendlandC2 2-D,
+h = 1.2√2·dx, H = 2h, cellsize (H, H), dist = H (cell list rebuilt every
+step), α = 0.01, g = 9.81, c₀ = 20√(2g), γ = 7, δ = 0.1, Δt = 1e-5.
+One bench step = stepsolve!(prob, 15): 15 SPH time steps, one CSPM period.
+Timed with CUDA events on the library's stream (the legacy default stream);
+the L2 is flushed (256 MB write) between bench steps, outside the events.
+
+--impl reference times the CPU restatement of the reference's algorithm (the
+reference itself is Julia + CUDA.jl and cannot run here) on all host cores.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+SUB = 15                    # SPH steps per bench step (one CSPM period)
+WORKLOAD = "2-D dam break, plain FP64 single instance, dx=0.02, 1.0x2.0 m column in 4.0x3.0 m tank, 3 boundary rows"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    return ap.parse_args()
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def make_case(pkg):
+    return pkg.workloads.dam_break_2d()
+
+
+def algorithmic_bytes_per_stage(case, npairs):
+    """Algorithmic HBM bytes of one fused pair-sum stage (gather form, FP64):
+    N·(8D x + 8D v + 8 ρ + 8 P + 4 ptype) read + N·(8 ρ̇ + 8D a) written
+    + 2P·4 B of neighbour indices."""
+    D, N = case.D, case.N
+    return N * (24 * D + 28) + 2 * npairs * 4
+
+
+class Clocks:
+    """nvidia-smi sampler running during the timed region."""
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_bench_{os.getpid()}.csv")
+
+    def __enter__(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}",
+                 "--query-gpu=index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+                 "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        try:
+            rows = [r.split(",") for r in open(self.path).read().strip().splitlines()]
+        except Exception:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[1])); mx.append(float(r[2]))
+                for k, nm in enumerate(names):
+                    if r[5 + k].strip().lower() == "active":
+                        reasons.add(nm)
+            except Exception:
+                continue
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline(case, seconds, threads):
+    """The oracle (C restatement of the reference's pair loops) on host cores,
+    a bounded sample of the same workload: whole bench steps until `seconds`."""
+    from oracle import oracle as orc
+    orc.set_threads(threads)
+    p = orc.default_params(case.dx, case.h, case.H, case.rho0, case.m0, case.dt, case.alpha, case.c0, case.gamma,
+                           case.delta, case.CFL, case.dist)
+    s = orc.OracleSystem(case.x, case.cellsize, case.dist, case.rho, case.ptype, p)
+    s.stepsolve(1)
+    n = 0
+    t0 = time.perf_counter()
+    while True:
+        s.stepsolve(SUB)
+        n += SUB
+        el = time.perf_counter() - t0
+        if el >= seconds:
+            break
+    return case.N * n / el, n, el
+
+
+def run_reference(args):
+    ws, rank, local = dist_env()
+    if rank != 0:
+        return 0
+    import __graft_entry__ as ge
+    wl = ge.load_package().workloads  # importing the package needs no GPU
+    from oracle import oracle as orc
+    case = wl.dam_break_2d()
+    threads = orc.max_threads()
+    orc.set_threads(threads)
+    p = orc.default_params(case.dx, case.h, case.H, case.rho0, case.m0, case.dt, case.alpha, case.c0, case.gamma,
+                           case.delta, case.CFL, case.dist)
+    s = orc.OracleSystem(case.x, case.cellsize, case.dist, case.rho, case.ptype, p)
+    for _ in range(args.warmup):
+        s.stepsolve(SUB)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        s.stepsolve(SUB)
+        times.append(time.perf_counter() - t0)
+    total = sum(times)
+    value = case.N * SUB * args.steps / total
+    out = {"metric": "particle-steps/s", "value": value, "unit": "particle-steps/s", "n_gpus": args.gpus,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+           "data": "synthetic", "impl": "reference",
+           "config": {"workload": WORKLOAD, "particles": case.N, "sph_steps_per_bench_step": SUB},
+           "cpu_baseline": {"value": value, "unit": "particle-steps/s", "cores": threads, "kind": "port",
+                            "sample": f"{args.steps} x stepsolve!(prob, {SUB}) on the full workload"},
+           "e2e": {"value": value, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out))
+    return 0
+
+
+def run_gb300(args):
+    import torch
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    else:
+        torch.cuda.set_device(0)
+    import __graft_entry__ as ge
+    g = ge.load_package()
+    L = g.load_library()
+    case = make_case(g)
+    D, N = case.D, case.N
+
+    def new_problem():
+        system = g.GPUCellList(tuple(case.x), case.cellsize, case.dist)
+        prob = g.SPHProblem(system, case.dx, case.h, case.H, g.WendlandC2(dim=D), case.rho, case.ptype, case.rho0,
+                            case.m0, case.dt, case.alpha, case.c0, case.gamma, case.delta, case.CFL)
+        return system, prob
+
+    system, prob = new_problem()
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    def barrier():
+        torch.cuda.synchronize()
+        if ws > 1:
+            import torch.distributed as dist
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    # ---------------- device-resident measurement
+    for _ in range(args.warmup):
+        prob.stepsolve(SUB)
+    L.gcsph_timing_enable(1)
+    L.gcsph_timing_reset()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    launches0 = g.launch_count()
+    barrier()
+    with Clocks(local) as clk:
+        for i in range(args.steps):
+            flush.fill_(float(i))
+            starts[i].record()
+            prob.stepsolve(SUB)
+            ends[i].record()
+        barrier()
+    launches = g.launch_count() - launches0
+    ms = sum(starts[i].elapsed_time(ends[i]) for i in range(args.steps))
+    if ws > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = ws * N * SUB * args.steps / (ms / 1e3)
+    # per-kernel-family timers
+    import ctypes as C
+    fam = {}
+    for tid in range(L.gcsph_timing_count()):
+        n_ = C.c_int64(); t_ = C.c_double()
+        L.gcsph_timing_get(tid, C.byref(n_), C.byref(t_))
+        fam[L.gcsph_timing_name(tid).decode()] = (int(n_.value), float(t_.value))
+    L.gcsph_timing_enable(0)
+    top = max(fam, key=lambda k: fam[k][1])
+    npairs = system.pairsn
+    # ---------------- end-to-end through the public API with host buffers
+    hx = torch.empty((D, N), dtype=torch.float64).pin_memory()
+    hv = torch.empty((D, N), dtype=torch.float64).pin_memory()
+    hr = torch.empty(N, dtype=torch.float64).pin_memory()
+    hx.copy_(torch.from_numpy(case.x)); hv.zero_(); hr.copy_(torch.from_numpy(case.rho))
+    system2, prob2 = new_problem()
+    h2d = d2h = (2 * D + 1) * N * 8
+    e_st = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    e_en = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+
+    def e2e_step():
+        for d in range(D):
+            system2.points[d].copy_(hx[d], non_blocking=True)
+            prob2.v[d].copy_(hv[d], non_blocking=True)
+        prob2.rho.copy_(hr, non_blocking=True)
+        prob2.stepsolve(SUB)
+        for d in range(D):
+            hx[d].copy_(system2.points[d], non_blocking=True)
+            hv[d].copy_(prob2.v[d], non_blocking=True)
+        hr.copy_(prob2.rho, non_blocking=True)
+
+    for _ in range(args.warmup):
+        e2e_step()
+    barrier()
+    for i in range(args.steps):
+        flush.fill_(float(i))
+        e_st[i].record()
+        e2e_step()
+        e_en[i].record()
+    barrier()
+    ms_e2e = sum(e_st[i].elapsed_time(e_en[i]) for i in range(args.steps))
+    if ws > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms_e2e], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_e2e = float(t.item())
+    e2e = ws * N * SUB * args.steps / (ms_e2e / 1e3)
+    if rank != 0:
+        return 0
+    # ---------------- roofline of the dominant kernel family
+    peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        peaks = json.load(open(peaks_path))
+        hbm_peak, peak_src = float(peaks["hbm_gbs"]), "measured"
+    except Exception:
+        hbm_peak, peak_src = 6800.0, "fallback"
+    nl, tms = fam[top]
+    avg_s = tms / 1e3 / max(nl, 1)
+    if top in ("stage1", "stage2"):
+        alg = algorithmic_bytes_per_stage(case, npairs)
+    else:
+        alg = None
+    achieved = (alg / avg_s / 1e9) if alg else None
+    roof = {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+            "frac": (achieved / hbm_peak) if achieved else None, "traffic": None, "peak_source": peak_src,
+            "avg_launch_us": avg_s * 1e6, "alg_bytes_per_launch": alg,
+            "note": "FP64-pipe-bound kernel; HBM fraction reported against measured copy bandwidth"}
+    cpu = None
+    if not args.no_cpu_baseline:
+        try:
+            from oracle import oracle as orc
+            v, n, el = cpu_baseline(case, args.cpu_seconds, 1)
+            cpu = {"value": v, "unit": "particle-steps/s", "cores": 1, "kind": "port",
+                   "sample": f"{n} SPH steps of the same workload in {el:.1f} s, serial oracle"}
+        except Exception as e:  # noqa: BLE001
+            cpu = {"value": None, "unit": "particle-steps/s", "cores": 0, "kind": "port", "sample": f"failed: {e}"}
+    out = {"metric": "particle-steps/s", "value": value, "unit": "particle-steps/s", "n_gpus": ws,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+           "config": {"workload": WORKLOAD, "particles": N, "pairs": npairs, "sph_steps_per_bench_step": SUB,
+                      "l2": "flushed (256 MB write) between bench steps", "parallelism": f"replicas x{ws}"},
+           "e2e": {"value": e2e, "unit": "particle-steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+           "gpu_launches": launches, "roofline": roof, "cpu_baseline": cpu, "clocks": clk.summary(),
+           "kernel_ms": {k: {"launches": v[0], "total_ms": v[1]} for k, v in fam.items() if v[0]}}
+    print(json.dumps(out))
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gb300(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

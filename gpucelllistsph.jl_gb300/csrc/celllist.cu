@@ -1,0 +1,533 @@
+// celllist.cu -- GPUCellList on sm_103a: frozen grid, counting sort of the
+// particles into cell order, and the pair set as a neighbour CSR.
+//
+// Reference behaviour restated (src/celllist.jl, src/gpukernels_cls.jl):
+//  * grid frozen at construction: cs raised to dist, MIN lowered by
+//    |(MIN+sqrt(eps))*sqrt(eps)|, CELL = ceil((MAX-MIN)/cs)   (celllist.jl:27-46)
+//  * cell of a point: ceil(Int32, clamp((x-MIN)*(1/cs), 1, CELL))
+//    (gpukernels_cls.jl:29-60); out-of-box points land in edge cells
+//  * pair set: every (i,j), i != j, whose cells are within Chebyshev distance
+//    1 and whose r^2 = (xi-xj)^2 + (yi-yj)^2 [+ (zi-zj)^2], evaluated left to
+//    right without FMA, is < dist^2 (neib_internal! + the half-stencil
+//    neib_external! launches, gpukernels_cls.jl:293-587)
+// The reference scatters pairs with per-cell threads and global atomics; here
+// each sorted particle scans the 3^D stencil as 3^(D-1) contiguous x-rows of
+// the sorted arrays and the pairs land at scanned offsets, so the emitted list
+// is deterministic (ascending sorted index).
+#include "celllist.cuh"
+
+namespace gcsph {
+
+static constexpr int TPB = 256;
+
+// ---------------------------------------------------------------------------
+// min/max reduction for the grid bounds (celllist.jl:41-43)
+// ---------------------------------------------------------------------------
+__global__ void k_minmax(const double* __restrict__ x, int64_t N, double* __restrict__ part) {
+  double mn = INFINITY, mx = -INFINITY;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x) {
+    double v = x[i];
+    mn = fmin(mn, v);
+    mx = fmax(mx, v);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    mn = fmin(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+    mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  }
+  __shared__ double smn[TPB / 32], smx[TPB / 32];
+  int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane == 0) { smn[w] = mn; smx[w] = mx; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int k = 1; k < TPB / 32; ++k) { mn = fmin(mn, smn[k]); mx = fmax(mx, smx[k]); }
+    part[2 * blockIdx.x] = mn;
+    part[2 * blockIdx.x + 1] = mx;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// binning: key, arrival slot, per-cell count (kernel_cellmap!)
+// ---------------------------------------------------------------------------
+template <int D>
+__global__ void k_cellkey(const double* __restrict__ x0, const double* __restrict__ x1, const double* __restrict__ x2,
+                          int64_t N, Grid g, int32_t* __restrict__ key, int32_t* __restrict__ slot,
+                          int32_t* __restrict__ count) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  const double* xs[3] = {x0, x1, x2};
+  int64_t lin = 0, stride = 1;
+#pragma unroll
+  for (int d = 0; d < D; ++d) {
+    double p = (xs[d][i] - g.offset[d]) * g.hinv[d];
+    double c = fmin(fmax(p, 1.0), (double)g.nc[d]);
+    int ci = (int)ceil(c);
+    lin += (int64_t)(ci - 1) * stride;
+    stride *= g.nc[d];
+  }
+  key[i] = (int32_t)lin;
+  slot[i] = atomicAdd(&count[lin], 1);
+}
+
+__global__ void k_scatter_arrival(const int32_t* __restrict__ key, const int32_t* __restrict__ slot,
+                                  const int32_t* __restrict__ cellstart, int64_t N, int32_t* __restrict__ tmp) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  tmp[cellstart[key[i]] + slot[i]] = (int32_t)i;
+}
+
+// rank of each cell member by original index: stable, history-free order.
+// Cost is sum over cells of n_c^2 integer compares (the reference's own pair
+// search is quadratic per cell too).
+__global__ void k_rank_in_cell(const int32_t* __restrict__ tmp, const int32_t* __restrict__ key,
+                               const int32_t* __restrict__ cellstart, const int32_t* __restrict__ ord, int64_t N,
+                               int32_t* __restrict__ perm) {
+  int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= N) return;
+  int32_t i = tmp[q];
+  int32_t c = key[i];
+  int32_t s = cellstart[c], e = cellstart[c + 1];
+  int32_t oi = ord ? ord[i] : i;
+  int32_t r = 0;
+  for (int32_t t = s; t < e; ++t) {
+    int32_t j = tmp[t];
+    int32_t oj = ord ? ord[j] : j;
+    r += (oj < oi);
+  }
+  perm[s + r] = i;
+}
+
+__global__ void k_apply_perm(const int32_t* __restrict__ perm, const int32_t* __restrict__ key,
+                             const int32_t* __restrict__ ord, int64_t N, int32_t* __restrict__ skey,
+                             int32_t* __restrict__ orig) {
+  int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= N) return;
+  int32_t i = perm[k];
+  skey[k] = key[i];
+  orig[k] = ord ? ord[i] : i;
+}
+
+template <int D>
+__global__ void k_gather_pos(const int32_t* __restrict__ idx, int64_t N, const double* __restrict__ a0,
+                             const double* __restrict__ a1, const double* __restrict__ a2, double* __restrict__ b0,
+                             double* __restrict__ b1, double* __restrict__ b2) {
+  int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= N) return;
+  int32_t i = idx[k];
+  b0[k] = a0[i];
+  b1[k] = a1[i];
+  if (D == 3) b2[k] = a2[i];
+}
+
+// ---------------------------------------------------------------------------
+// pair search over the 3^D stencil, as 3^(D-1) contiguous x-rows
+// ---------------------------------------------------------------------------
+template <int D>
+__device__ inline double r2_ref(double ax, double ay, double az, double bx, double by, double bz) {
+  double d0 = ax - bx;
+  double d1 = ay - by;
+  double s = d0 * d0 + d1 * d1;
+  if (D == 3) {
+    double d2 = az - bz;
+    s = s + d2 * d2;
+  }
+  return s;
+}
+
+// MODE 0: count (full, up); MODE 1: fill nbr
+template <int D, int MODE>
+__global__ void __launch_bounds__(TPB) k_pairs(const double* __restrict__ x0, const double* __restrict__ x1,
+                                               const double* __restrict__ x2, const int32_t* __restrict__ skey,
+                                               const int32_t* __restrict__ cellstart, int64_t N, Grid g,
+                                               int32_t* __restrict__ cnt_full, int32_t* __restrict__ cnt_up,
+                                               const int64_t* __restrict__ rs_full, int32_t* __restrict__ nbr) {
+  int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= N) return;
+  const int nx = g.nc[0], ny = g.nc[1], nz = D == 3 ? g.nc[2] : 1;
+  int32_t key = skey[k];
+  int cx = key % nx;
+  int t = key / nx;
+  int cy = t % ny;
+  int cz = t / ny;
+  double ax = x0[k], ay = x1[k], az = D == 3 ? x2[k] : 0.0;
+  int32_t nf = 0, nu = 0;
+  int64_t wpos = MODE == 1 ? rs_full[k] : 0;
+  const int xlo = cx > 0 ? cx - 1 : 0;
+  const int xhi = cx < nx - 1 ? cx + 1 : nx - 1;
+  for (int dz = (D == 3 ? -1 : 0); dz <= (D == 3 ? 1 : 0); ++dz) {
+    int z = cz + dz;
+    if (z < 0 || z >= nz) continue;
+    for (int dy = -1; dy <= 1; ++dy) {
+      int y = cy + dy;
+      if (y < 0 || y >= ny) continue;
+      int64_t base = (int64_t)nx * ((int64_t)y + (int64_t)ny * z);
+      int32_t m0 = cellstart[base + xlo], m1 = cellstart[base + xhi + 1];
+      for (int32_t m = m0; m < m1; ++m) {
+        if (m == k) continue;
+        double r2 = r2_ref<D>(ax, ay, az, x0[m], x1[m], D == 3 ? x2[m] : 0.0);
+        if (r2 < g.dist2) {
+          if (MODE == 0) {
+            ++nf;
+            nu += (m > k);
+          } else {
+            nbr[wpos++] = m;
+          }
+        }
+      }
+    }
+  }
+  if (MODE == 0) {
+    cnt_full[k] = nf;
+    cnt_up[k] = nu;
+  }
+}
+
+__global__ void k_emit_pairs(const int64_t* __restrict__ rs_full, const int64_t* __restrict__ rs_up,
+                             const int32_t* __restrict__ nbr, const int32_t* __restrict__ orig, int64_t N, int64_t cap,
+                             int32_t* __restrict__ pairs) {
+  int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= N) return;
+  int64_t r1 = rs_full[k + 1];
+  int64_t u0 = rs_up[k], u1 = rs_up[k + 1];
+  int64_t nu = u1 - u0;
+  int32_t ok = orig[k] + 1;
+  for (int64_t t = 0; t < nu; ++t) {
+    int64_t pos = u0 + t;
+    if (pos >= cap) break;
+    int32_t om = orig[nbr[r1 - nu + t]] + 1;
+    pairs[2 * pos] = ok < om ? ok : om;
+    pairs[2 * pos + 1] = ok < om ? om : ok;
+  }
+}
+
+// мaxpairs: n(n-1)/2 + n * (half-stencil neighbour counts), gpukernels_cls.jl:130-286
+template <int D>
+__global__ void k_maxpairs(const int32_t* __restrict__ count, Grid g, unsigned long long* __restrict__ out) {
+  int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  unsigned long long v = 0;
+  if (c < g.ncell) {
+    const int nx = g.nc[0], ny = g.nc[1], nz = D == 3 ? g.nc[2] : 1;
+    int64_t n = count[c];
+    if (n > 0) {
+      int cx = (int)(c % nx);
+      int64_t t = c / nx;
+      int cy = (int)(t % ny), cz = (int)(t / ny);
+      int64_t m = 0;
+      const int no = D == 2 ? 4 : 13;
+      const int off[13][3] = {{-1, 1, 0}, {0, 1, 0}, {1, 1, 0}, {1, 0, 0}, {-1, 1, 1}, {0, 1, 1}, {1, 1, 1},
+                              {1, 0, 1}, {0, 0, 1}, {-1, 1, -1}, {0, 1, -1}, {1, 1, -1}, {1, 0, -1}};
+      for (int o = 0; o < no; ++o) {
+        int a = cx + off[o][0], b = cy + off[o][1], z = cz + (D == 3 ? off[o][2] : 0);
+        if (a >= 0 && a < nx && b >= 0 && b < ny && z >= 0 && z < nz)
+          m += count[a + (int64_t)nx * (b + (int64_t)ny * z)];
+      }
+      v = (unsigned long long)((int64_t)((double)(n * (n - 1)) * 0.5) + m * n);
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0 && v) atomicAdd(out, v);
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+int CellCore::read_scalar(const int64_t* dev, int64_t* host) {
+  GC_CUDA(cudaMemcpyAsync(pin, dev, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+  GC_CUDA(cudaStreamSynchronize(st));
+  *host = pin[0];
+  return GCSPH_OK;
+}
+
+int CellCore::init(int D_, int64_t N_, const double* cellsize, double dist_, const double* MIN, const double* MAX,
+                   const double* const* xin, cudaStream_t s) {
+  D = D_;
+  N = N_;
+  dist = dist_;
+  st = s;
+  if (D != 2 && D != 3) return fail(GCSPH_EINVAL, "wrong dimention: D=%d (2 or 3)", D);
+  if (N < 1 || N > 0x7ffffffeLL) return fail(GCSPH_EINVAL, "N=%lld out of range", (long long)N);
+  if (!(dist > 0)) return fail(GCSPH_EINVAL, "dist must be > 0");
+  GC_CUDA(cudaMallocHost((void**)&pin, 8 * sizeof(int64_t)));
+  const double seps = 1.4901161193847656e-08;  // sqrt(eps(Float64)) = 2^-26
+  double mn[3], mx[3];
+  if (!MIN || !MAX) {
+    const int nb = 4 * 152;
+    DevBuf part;
+    int rc = part.ensure(sizeof(double) * 2 * nb, st);
+    if (rc) return rc;
+    double* hp = nullptr;
+    GC_CUDA(cudaMallocHost((void**)&hp, sizeof(double) * 2 * nb));
+    for (int d = 0; d < D; ++d) {
+      k_minmax<<<nb, TPB, 0, st>>>(xin[d], N, part.as<double>());
+      GC_LAUNCHED();
+      GC_CUDA(cudaMemcpyAsync(hp, part.p, sizeof(double) * 2 * nb, cudaMemcpyDeviceToHost, st));
+      GC_CUDA(cudaStreamSynchronize(st));
+      double a = INFINITY, b = -INFINITY;
+      for (int k = 0; k < nb; ++k) { a = fmin(a, hp[2 * k]); b = fmax(b, hp[2 * k + 1]); }
+      mn[d] = a;
+      mx[d] = b;
+    }
+    cudaFreeHost(hp);
+    part.release();
+  }
+  int64_t ncell = 1;
+  for (int d = 0; d < D; ++d) {
+    cs[d] = cellsize[d] < dist ? dist : cellsize[d];
+    double lo = MIN ? MIN[d] : mn[d];
+    double hi = MAX ? MAX[d] : mx[d];
+    lo = lo - fabs((lo + seps) * seps);
+    double c = ceil((hi - lo) / cs[d]);
+    if (!(c >= 1.0) || c > 2.0e9) return fail(GCSPH_EINVAL, "degenerate grid in dim %d (CELL=%g)", d + 1, c);
+    g.offset[d] = lo;
+    g.hinv[d] = 1.0 / cs[d];
+    g.nc[d] = (int)c;
+    ncell *= (int64_t)c;
+    if (ncell > 0x7ffffff0LL) return fail(GCSPH_EINVAL, "cell grid too large (%lld cells)", (long long)ncell);
+  }
+  for (int d = D; d < 3; ++d) { g.offset[d] = 0; g.hinv[d] = 0; g.nc[d] = 1; }
+  g.D = D;
+  g.ncell = ncell;
+  g.dist2 = dist * dist;
+  int rc;
+  if ((rc = count.ensure(sizeof(int32_t) * ncell, st))) return rc;
+  if ((rc = cellstart.ensure(sizeof(int32_t) * (ncell + 1), st))) return rc;
+  if ((rc = key.ensure(sizeof(int32_t) * N, st))) return rc;
+  if ((rc = slot.ensure(sizeof(int32_t) * N, st))) return rc;
+  if ((rc = tmp.ensure(sizeof(int32_t) * N, st))) return rc;
+  if ((rc = perm.ensure(sizeof(int32_t) * N, st))) return rc;
+  if ((rc = skey.ensure(sizeof(int32_t) * N, st))) return rc;
+  if ((rc = orig.ensure(sizeof(int32_t) * N, st))) return rc;
+  if ((rc = cnt_full.ensure(sizeof(int32_t) * N, st))) return rc;
+  if ((rc = cnt_up.ensure(sizeof(int32_t) * N, st))) return rc;
+  if ((rc = rs_full.ensure(sizeof(int64_t) * (N + 1), st))) return rc;
+  if ((rc = rs_up.ensure(sizeof(int64_t) * (N + 1), st))) return rc;
+  int64_t sc = scan_scratch_elems((ncell > N ? ncell : N) + 1);
+  if ((rc = scratch.ensure(sizeof(int64_t) * (sc + 16), st))) return rc;
+  return GCSPH_OK;
+}
+
+void CellCore::release() {
+  DevBuf* all[] = {&count, &cellstart, &key, &slot, &tmp, &perm, &skey, &orig, &cnt_full, &cnt_up, &rs_full,
+                   &rs_up, &nbr, &scratch};
+  for (DevBuf* b : all) b->release();
+  if (pin) cudaFreeHost(pin);
+  pin = nullptr;
+}
+
+int CellCore::sort(const double* const* xin, const int32_t* ord) {
+  timer_begin(T_SORT, st);
+  GC_CUDA(cudaMemsetAsync(count.p, 0, sizeof(int32_t) * g.ncell, st));
+  const double* x2 = D == 3 ? xin[2] : xin[0];
+  if (D == 2)
+    k_cellkey<2><<<nblocks(N, TPB), TPB, 0, st>>>(xin[0], xin[1], x2, N, g, key.as<int32_t>(), slot.as<int32_t>(),
+                                                   count.as<int32_t>());
+  else
+    k_cellkey<3><<<nblocks(N, TPB), TPB, 0, st>>>(xin[0], xin[1], x2, N, g, key.as<int32_t>(), slot.as<int32_t>(),
+                                                   count.as<int32_t>());
+  GC_LAUNCHED();
+  int rc = exclusive_scan_i32_to_i32(count.as<int32_t>(), cellstart.as<int32_t>(), g.ncell, scratch.as<int64_t>(), st);
+  if (rc) return rc;
+  k_scatter_arrival<<<nblocks(N, TPB), TPB, 0, st>>>(key.as<int32_t>(), slot.as<int32_t>(), cellstart.as<int32_t>(), N,
+                                                      tmp.as<int32_t>());
+  GC_LAUNCHED();
+  k_rank_in_cell<<<nblocks(N, TPB), TPB, 0, st>>>(tmp.as<int32_t>(), key.as<int32_t>(), cellstart.as<int32_t>(), ord, N,
+                                                   perm.as<int32_t>());
+  GC_LAUNCHED();
+  k_apply_perm<<<nblocks(N, TPB), TPB, 0, st>>>(perm.as<int32_t>(), key.as<int32_t>(), ord, N, skey.as<int32_t>(),
+                                                 orig.as<int32_t>());
+  GC_LAUNCHED();
+  timer_end(T_SORT, st);
+  sorted = true;
+  built = false;
+  return GCSPH_OK;
+}
+
+int CellCore::gather_positions(const double* const* xin, double* const* xs) {
+  const double* a2 = D == 3 ? xin[2] : xin[0];
+  double* b2 = D == 3 ? xs[2] : xs[0];
+  if (D == 2)
+    k_gather_pos<2><<<nblocks(N, TPB), TPB, 0, st>>>(perm.as<int32_t>(), N, xin[0], xin[1], a2, xs[0], xs[1], b2);
+  else
+    k_gather_pos<3><<<nblocks(N, TPB), TPB, 0, st>>>(perm.as<int32_t>(), N, xin[0], xin[1], a2, xs[0], xs[1], b2);
+  GC_LAUNCHED();
+  return GCSPH_OK;
+}
+
+int CellCore::gather_positions_by_orig(const double* const* xorig, double* const* xs) {
+  const double* a2 = D == 3 ? xorig[2] : xorig[0];
+  double* b2 = D == 3 ? xs[2] : xs[0];
+  if (D == 2)
+    k_gather_pos<2><<<nblocks(N, TPB), TPB, 0, st>>>(orig.as<int32_t>(), N, xorig[0], xorig[1], a2, xs[0], xs[1], b2);
+  else
+    k_gather_pos<3><<<nblocks(N, TPB), TPB, 0, st>>>(orig.as<int32_t>(), N, xorig[0], xorig[1], a2, xs[0], xs[1], b2);
+  GC_LAUNCHED();
+  return GCSPH_OK;
+}
+
+int CellCore::build_pairs(const double* const* xs) {
+  if (!sorted) return fail(GCSPH_ESTATE, "pair build before binning");
+  const double* x2 = D == 3 ? xs[2] : xs[0];
+  timer_begin(T_PAIRS, st);
+  if (D == 2)
+    k_pairs<2, 0><<<nblocks(N, TPB), TPB, 0, st>>>(xs[0], xs[1], x2, skey.as<int32_t>(), cellstart.as<int32_t>(), N, g,
+                                                    cnt_full.as<int32_t>(), cnt_up.as<int32_t>(), nullptr, nullptr);
+  else
+    k_pairs<3, 0><<<nblocks(N, TPB), TPB, 0, st>>>(xs[0], xs[1], x2, skey.as<int32_t>(), cellstart.as<int32_t>(), N, g,
+                                                    cnt_full.as<int32_t>(), cnt_up.as<int32_t>(), nullptr, nullptr);
+  GC_LAUNCHED();
+  int rc = exclusive_scan_i32_to_i64(cnt_full.as<int32_t>(), rs_full.as<int64_t>(), N, scratch.as<int64_t>(), st);
+  if (rc) return rc;
+  rc = exclusive_scan_i32_to_i64(cnt_up.as<int32_t>(), rs_up.as<int64_t>(), N, scratch.as<int64_t>(), st);
+  if (rc) return rc;
+  timer_end(T_PAIRS, st);
+  GC_CUDA(cudaMemcpyAsync(pin, rs_full.as<int64_t>() + N, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+  GC_CUDA(cudaMemcpyAsync(pin + 1, rs_up.as<int64_t>() + N, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+  GC_CUDA(cudaStreamSynchronize(st));
+  timer_collect();
+  nfull = pin[0];
+  nup = pin[1];
+  if (nfull > nbr_cap) {
+    int64_t want = nfull + nfull / 4 + 1024;
+    if ((rc = nbr.ensure(sizeof(int32_t) * want, st))) return rc;
+    nbr_cap = want;
+  }
+  timer_begin(T_PAIRS, st);
+  if (D == 2)
+    k_pairs<2, 1><<<nblocks(N, TPB), TPB, 0, st>>>(xs[0], xs[1], x2, skey.as<int32_t>(), cellstart.as<int32_t>(), N, g,
+                                                    nullptr, nullptr, rs_full.as<int64_t>(), nbr.as<int32_t>());
+  else
+    k_pairs<3, 1><<<nblocks(N, TPB), TPB, 0, st>>>(xs[0], xs[1], x2, skey.as<int32_t>(), cellstart.as<int32_t>(), N, g,
+                                                    nullptr, nullptr, rs_full.as<int64_t>(), nbr.as<int32_t>());
+  GC_LAUNCHED();
+  timer_end(T_PAIRS, st);
+  built = true;
+  return GCSPH_OK;
+}
+
+int CellCore::emit(int32_t* pairs, int64_t cap, int fillzero, int64_t* pairsn) {
+  if (!built) return fail(GCSPH_ESTATE, "no pair set built yet");
+  if (cap < 0) return fail(GCSPH_EINVAL, "negative capacity");
+  if (pairsn) *pairsn = nup;
+  if (cap > 0 && !pairs) return fail(GCSPH_EINVAL, "null pair buffer");
+  if (cap > 0) {
+    k_emit_pairs<<<nblocks(N, TPB), TPB, 0, st>>>(rs_full.as<int64_t>(), rs_up.as<int64_t>(), nbr.as<int32_t>(),
+                                                   orig.as<int32_t>(), N, cap, pairs);
+    GC_LAUNCHED();
+    if (fillzero && nup < cap)
+      GC_CUDA(cudaMemsetAsync(pairs + 2 * nup, 0, sizeof(int32_t) * 2 * (size_t)(cap - nup), st));
+  }
+  GC_CUDA(cudaStreamSynchronize(st));
+  if (nup > cap) return fail(GCSPH_ECAPACITY, "pair list holds %lld of %lld pairs", (long long)cap, (long long)nup);
+  return GCSPH_OK;
+}
+
+int CellCore::maxpairs(int64_t* out) {
+  int64_t* d = scratch.as<int64_t>();
+  GC_CUDA(cudaMemsetAsync(d, 0, sizeof(int64_t), st));
+  if (D == 2)
+    k_maxpairs<2><<<nblocks(g.ncell, TPB), TPB, 0, st>>>(count.as<int32_t>(), g, (unsigned long long*)d);
+  else
+    k_maxpairs<3><<<nblocks(g.ncell, TPB), TPB, 0, st>>>(count.as<int32_t>(), g, (unsigned long long*)d);
+  GC_LAUNCHED();
+  return read_scalar(d, out);
+}
+
+}  // namespace gcsph
+
+// ---------------------------------------------------------------------------
+// C ABI: gcl_*
+// ---------------------------------------------------------------------------
+using namespace gcsph;
+
+static int gcl_full_update(gcl_handle* h) {
+  int rc = h->core.sort(h->xuser, nullptr);
+  if (rc) return rc;
+  double* xs[3] = {h->xs[0].as<double>(), h->xs[1].as<double>(), h->core.D == 3 ? h->xs[2].as<double>() : nullptr};
+  if ((rc = h->core.gather_positions(h->xuser, xs))) return rc;
+  return h->core.build_pairs((const double* const*)xs);
+}
+
+extern "C" {
+
+int gcl_create(int32_t D, int64_t N, const double* const* x_dev, const double* cellsize, double dist,
+               const double* MIN_or_null, const double* MAX_or_null, void* stream, gcl_handle** out) {
+  if (!out || !x_dev || !cellsize) return fail(GCSPH_EINVAL, "null argument");
+  *out = nullptr;
+  if (D != 2 && D != 3) return fail(GCSPH_EINVAL, "wrong dimention: D=%d (2 or 3)", (int)D);
+  for (int d = 0; d < D; ++d)
+    if (!x_dev[d]) return fail(GCSPH_EINVAL, "null coordinate array %d", d + 1);
+  gcl_handle* h = new gcl_handle();
+  for (int d = 0; d < D; ++d) h->xuser[d] = x_dev[d];
+  int rc = h->core.init(D, N, cellsize, dist, MIN_or_null, MAX_or_null, x_dev, (cudaStream_t)stream);
+  if (!rc)
+    for (int d = 0; d < D && !rc; ++d) rc = h->xs[d].ensure(sizeof(double) * N, h->core.st);
+  if (!rc) rc = gcl_full_update(h);
+  if (rc) {
+    std::string keep = gcsph_last_error();
+    h->core.release();
+    for (auto& b : h->xs) b.release();
+    delete h;
+    set_error("%s", keep.c_str());
+    return rc;
+  }
+  *out = h;
+  return GCSPH_OK;
+}
+
+void gcl_destroy(gcl_handle* h) {
+  if (!h) return;
+  cudaStreamSynchronize(h->core.st);
+  h->core.release();
+  for (auto& b : h->xs) b.release();
+  delete h;
+}
+
+int gcl_grid(const gcl_handle* h, double* cs, double* offset, int64_t* cell) {
+  if (!h) return fail(GCSPH_EINVAL, "null handle");
+  for (int d = 0; d < h->core.D; ++d) {
+    if (cs) cs[d] = h->core.cs[d];
+    if (offset) offset[d] = h->core.g.offset[d];
+    if (cell) cell[d] = h->core.g.nc[d];
+  }
+  return GCSPH_OK;
+}
+
+int gcl_update(gcl_handle* h, int64_t* pairsn_out) {
+  if (!h) return fail(GCSPH_EINVAL, "null handle");
+  int rc = gcl_full_update(h);
+  if (rc) return rc;
+  if (pairsn_out) *pairsn_out = h->core.nup;
+  GC_CUDA(cudaStreamSynchronize(h->core.st));
+  return GCSPH_OK;
+}
+
+int gcl_partialupdate(gcl_handle* h, int64_t* pairsn_out) {
+  if (!h) return fail(GCSPH_EINVAL, "null handle");
+  if (!h->core.sorted) return fail(GCSPH_ESTATE, "partialupdate before any update");
+  double* xs[3] = {h->xs[0].as<double>(), h->xs[1].as<double>(), h->core.D == 3 ? h->xs[2].as<double>() : nullptr};
+  int rc = h->core.gather_positions_by_orig(h->xuser, xs);
+  if (rc) return rc;
+  if ((rc = h->core.build_pairs((const double* const*)xs))) return rc;
+  if (pairsn_out) *pairsn_out = h->core.nup;
+  GC_CUDA(cudaStreamSynchronize(h->core.st));
+  return GCSPH_OK;
+}
+
+int gcl_emit_pairs(gcl_handle* h, int32_t* pairs_dev, int64_t cap, int fillzero, int64_t* pairsn_out) {
+  if (!h) return fail(GCSPH_EINVAL, "null handle");
+  return h->core.emit(pairs_dev, cap, fillzero, pairsn_out);
+}
+
+int gcl_cellpnum(gcl_handle* h, int32_t* cellpnum_dev) {
+  if (!h || !cellpnum_dev) return fail(GCSPH_EINVAL, "null argument");
+  GC_CUDA(cudaMemcpyAsync(cellpnum_dev, h->core.count.p, sizeof(int32_t) * h->core.g.ncell, cudaMemcpyDeviceToDevice,
+                          h->core.st));
+  GC_CUDA(cudaStreamSynchronize(h->core.st));
+  return GCSPH_OK;
+}
+
+int gcl_maxpairs(gcl_handle* h, int64_t* out) {
+  if (!h || !out) return fail(GCSPH_EINVAL, "null argument");
+  return h->core.maxpairs(out);
+}
+
+}  // extern "C"

@@ -1,0 +1,68 @@
+// celllist.cuh -- cell binning + pair-set build shared by gcl_* and sph_*.
+//
+// HBM layout (all device, one handle):
+//   key[N], slot[N]     cell key and arrival slot of each particle in input order
+//   count[ncell]        particles per cell (= the reference's cellpnum)
+//   cellstart[ncell+1]  exclusive scan of count
+//   tmp[N]              arrival-ordered members of each cell
+//   perm[N]             sorted position -> input index; cells ascending, and
+//                       inside a cell ascending ORIGINAL particle index
+//   skey[N], orig[N]    cell key and original index of each sorted particle
+//   rs_full[N+1], nbr[] CSR of every neighbour (both directions) of each sorted
+//                       particle, neighbours ascending -- the fused SPH sums walk it
+//   rs_up[N+1]          per-particle count of neighbours with a larger sorted
+//                       index, scanned -- position of that particle's pairs in
+//                       the emitted (min,max) pair list
+#pragma once
+#include "gcsph_common.cuh"
+
+namespace gcsph {
+
+struct Grid {
+  int D;
+  double offset[3];
+  double hinv[3];
+  int nc[3];
+  int64_t ncell;
+  double dist2;
+};
+
+struct CellCore {
+  int D = 2;
+  int64_t N = 0;
+  double dist = 0, cs[3] = {0, 0, 0};
+  Grid g{};
+  cudaStream_t st = 0;
+
+  DevBuf count, cellstart, key, slot, tmp, perm, skey, orig, cnt_full, cnt_up, rs_full, rs_up, nbr, scratch;
+  int64_t* pin = nullptr;  // pinned host scalars
+  int64_t nfull = 0, nup = 0, nbr_cap = 0;
+  bool sorted = false, built = false;
+
+  int init(int D_, int64_t N_, const double* cellsize, double dist_, const double* MIN, const double* MAX,
+           const double* const* xin, cudaStream_t s);
+  void release();
+  // bin xin (input order) into the frozen grid and sort by (cell, ord[i]);
+  // ord == nullptr means the input order is the original order.
+  int sort(const double* const* xin, const int32_t* ord);
+  // gather xs[d][k] = xin[d][perm[k]] (and orig[k] = ord[perm[k]] is done by sort)
+  int gather_positions(const double* const* xin, double* const* xs);
+  // gather xs[d][k] = xorig[d][orig[k]] for partial updates
+  int gather_positions_by_orig(const double* const* xorig, double* const* xs);
+  // count + scan + fill of the neighbour CSR on sorted positions xs
+  int build_pairs(const double* const* xs);
+  // (min,max) 1-based original indices of every pair, first cap written
+  int emit(int32_t* pairs, int64_t cap, int fillzero, int64_t* pairsn);
+  // мaxpairs over the current counts (src/gpukernels_cls.jl:109-286)
+  int maxpairs(int64_t* out);
+  int read_scalar(const int64_t* dev, int64_t* host);
+};
+
+}  // namespace gcsph
+
+// opaque C-ABI handle of the cell list (include/gcsph.h)
+struct gcl_handle {
+  gcsph::CellCore core;
+  const double* xuser[3] = {nullptr, nullptr, nullptr};
+  gcsph::DevBuf xs[3];
+};

@@ -1,0 +1,175 @@
+// gcsph_common.cuh -- shared device math and host plumbing for libgcsph.so.
+//
+// The FP64 drop-in path is compiled with -fmad=false so that every expression
+// below rounds exactly like the reference's Julia source (left-to-right, no
+// contraction); the CPU oracle uses the same operation order, so the two agree
+// bit-for-bit up to summation order and libm's cos.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string.h>
+#include <string>
+
+#include "../../include/gcsph.h"
+
+// Float64(pi), the value Julia uses for the Irrational pi.
+#define GCSPH_PI64 3.141592653589793
+
+namespace gcsph {
+
+// ----------------------------------------------------------------------------
+// error reporting (thread-local last error, int status codes at the ABI)
+// ----------------------------------------------------------------------------
+void set_error(const char* fmt, ...);
+int fail(int code, const char* fmt, ...);
+int cuda_fail(cudaError_t e, const char* what, const char* file, int line);
+void count_launch(int n = 1);
+
+#define GC_CUDA(call)                                                          \
+  do {                                                                         \
+    cudaError_t _e = (call);                                                   \
+    if (_e != cudaSuccess) return ::gcsph::cuda_fail(_e, #call, __FILE__, __LINE__); \
+  } while (0)
+
+#define GC_LAUNCHED()                                                          \
+  do {                                                                         \
+    ::gcsph::count_launch();                                                   \
+    cudaError_t _e = cudaPeekAtLastError();                                    \
+    if (_e != cudaSuccess) return ::gcsph::cuda_fail(_e, "kernel launch", __FILE__, __LINE__); \
+  } while (0)
+
+inline int nblocks(int64_t n, int threads) {
+  int64_t b = (n + threads - 1) / threads;
+  return (int)(b < 1 ? 1 : b);
+}
+
+// ----------------------------------------------------------------------------
+// WendlandC2 (SPHKernels.jl 2.2, published formula; call sites
+// src/gpukernels_sph.jl:95,150,207,343,1490,1519).  u = r * Hinv.
+//   W  = sigma_D Hinv^D     (1-u)^4 (1+4u)   for u < 1
+//   dW = sigma_D Hinv^(D+1) (-20 u (1-u)^3)  for u < 1
+// sigma_2 = 7/pi, sigma_3 = 21/(2 pi).
+// ----------------------------------------------------------------------------
+template <int D>
+__host__ __device__ inline double wc2_sigma() {
+  return D == 2 ? 7.0 / GCSPH_PI64 : 21.0 / (2.0 * GCSPH_PI64);
+}
+template <int D>
+__host__ __device__ inline double wc2_norm_w(double Hinv) {
+  double p = Hinv;
+  for (int k = 1; k < D; ++k) p = p * Hinv;
+  return wc2_sigma<D>() * p;
+}
+template <int D>
+__host__ __device__ inline double wc2_norm_dw(double Hinv) {
+  double p = Hinv;
+  for (int k = 1; k < D + 1; ++k) p = p * Hinv;
+  return wc2_sigma<D>() * p;
+}
+// nW = wc2_norm_w<D>(Hinv) precomputed once per launch
+__host__ __device__ inline double wc2_w(double u, double nW) {
+  if (!(u < 1.0)) return 0.0;
+  double t = 1.0 - u;
+  double t2 = t * t;
+  double t4 = t2 * t2;
+  return ((1.0 + 4.0 * u) * t4) * nW;
+}
+__host__ __device__ inline double wc2_dw(double u, double nDW) {
+  if (!(u < 1.0)) return 0.0;
+  double t = 1.0 - u;
+  double t3 = (t * t) * t;
+  return ((-20.0 * u) * t3) * nDW;
+}
+
+// powfancy7th, src/gpukernels_sph.jl:499-515 (bit-trick guess + 2 Newton steps)
+__host__ __device__ inline double powfancy7th(double x, double ginv, int gamma) {
+  if (gamma == 7) {
+    double ax = fabs(x);
+#ifdef __CUDA_ARCH__
+    unsigned long long bits = (unsigned long long)__double_as_longlong(ax);
+    bits = 0x36cd000000000000ULL + bits / 7ULL;
+    double t = __longlong_as_double((long long)bits);
+#else
+    uint64_t bits;
+    memcpy(&bits, &ax, 8);
+    bits = 0x36cd000000000000ULL + bits / 7ULL;
+    double t;
+    memcpy(&t, &bits, 8);
+#endif
+    t = copysign(t, x);
+    for (int it = 0; it < 2; ++it) {
+      double t2 = t * t;
+      double t3 = t2 * t;
+      double t4 = t2 * t2;
+      double xot4 = x / t4;
+      t = t - (t * (t3 - xot4)) / (4.0 * t3 + 3.0 * xot4);
+    }
+    return t;
+  }
+  return pow(x, ginv);
+}
+
+// Float64 ^ Int of the Tait EOS: gamma == 7 as ((x2*x2)*x2)*x, otherwise
+// left-to-right products (same sequence as the oracle).
+__host__ __device__ inline double ipow(double x, int n) {
+  if (n == 7) {
+    double x2 = x * x, x4 = x2 * x2, x6 = x4 * x2;
+    return x6 * x;
+  }
+  if (n == 0) return 1.0;
+  double r = x;
+  int m = n < 0 ? -n : n;
+  for (int k = 1; k < m; ++k) r = r * x;
+  return n < 0 ? 1.0 / r : r;
+}
+
+// pressure(), src/gpukernels_sph.jl:691-697
+__host__ __device__ inline double eos(double rho, int gamma, double rho0, double P0, int pt) {
+  if (pt <= 1 && rho < rho0) return 0.0;
+  return P0 * (ipow(rho / rho0, gamma) - 1.0);
+}
+
+// positive doubles order like their bit patterns: atomicMax on the bits
+__device__ inline void atomic_max_pos(unsigned long long* addr, double v) {
+  if (!(v > 0.0)) return;
+  atomicMax(addr, (unsigned long long)__double_as_longlong(v));
+}
+
+// Warp/block max of a non-negative double, one atomic per block
+__device__ inline double warp_max(double v) {
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+
+// ----------------------------------------------------------------------------
+// device exclusive scan (3 phases, no inter-block waiting)
+// ----------------------------------------------------------------------------
+// out[i] = sum_{j<i} in[j] for i in [0, n]; out[n] = total.  scratch must
+// hold scan_scratch_elems(n) int64 values.
+int64_t scan_scratch_elems(int64_t n);
+int exclusive_scan_i32_to_i64(const int32_t* in, int64_t* out, int64_t n, int64_t* scratch,
+                              cudaStream_t s);
+int exclusive_scan_i32_to_i32(const int32_t* in, int32_t* out, int64_t n, int64_t* scratch,
+                              cudaStream_t s);
+
+// ----------------------------------------------------------------------------
+// per-kernel-family CUDA-event timers (off unless gcsph_timing_enable(1))
+// ----------------------------------------------------------------------------
+enum TimerId {
+  T_STAGE1 = 0, T_STAGE2, T_DPC, T_XSPH, T_CSPM, T_SORT, T_PAIRS, T_STATE, T_POST, T_DT, T_COUNT
+};
+bool timing_on();
+void timer_begin(int id, cudaStream_t s);
+void timer_end(int id, cudaStream_t s);
+void timer_collect();  // after a stream sync: fold finished event pairs into the totals
+
+// device buffer helper
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  int ensure(size_t need, cudaStream_t s, bool zero = false);
+  void release();
+  template <class T> T* as() const { return (T*)p; }
+};
+
+}  // namespace gcsph

@@ -1,0 +1,1014 @@
+// sph_step.cu -- SPHProblem + stepsolve! (src/sphproblem.jl:113-345) on sm_103a.
+//
+// Design: the reference runs ~25-35 one-thread-per-pair kernels per step, each
+// scattering FP64 atomics into both particles and each followed by a host
+// sync.  Here the particles live in cell order in HBM and every pair pass is a
+// GATHER: one thread owns one particle, walks its neighbour CSR (both
+// directions, ascending), evaluates each pair term from its own side and
+// accumulates in registers.  No atomics, deterministic sums, and the
+// per-particle updates are fused into the epilogues:
+//   k_stage1 : W, ∇W (stored per CSR entry), ∂ρ∂tDDT!, ∂v∂t!, ∂v∂t_av!,
+//              ∂v∂t_visc!, gravity, fbmolforce!(0.4, 2dx), ∂v∂tpF! at (x,ρ,v)
+//              + the three half-step predictors + pressure at ρΔt½
+//   k_stage2 : the same sums at (xΔt½,ρΔt½,vΔt½) with the stage-1 ∇W,
+//              fbmolforce!(bound_D, bound_l) at x + symplectic_update!
+//              + pressure at the new ρ + block max of |cΔx|
+//   k_dpc, k_xsph, k_cspm : DPC / XSPH / CSPM passes with their updates
+// Each term is evaluated from the owning particle's side; the reference's
+// j-side formulas are exactly the i-side formula seen from j (negated Δx, Δv
+// and ∇W are exact in IEEE arithmetic), so no term changes meaning.
+// Arrays that a pass reads from neighbours and also updates are ping-ponged.
+#include <math.h>
+#include "celllist.cuh"
+
+namespace gcsph {
+
+static constexpr int STPB = 128;
+
+struct StepConst {
+  double h, eta2, m0, rho0, ginv, DDTkh, DDTgz, P0, alpha, c0, nu, g, s, Hinv, nW, nDW;
+  double fb_d, fb_r0, fb_eta2;  // fbmolforce constants of the stage being run
+  double twoh, pfc, hp1;        // 2h, 1.5*pi, 0.1h  (∂v∂tpF!)
+  double dpc_l0inv, dpc_nW, dpc_whinv, dpc_pmin, dpc_pmax, dpc_lambda, dpc_kernlim, dpc_eta2;
+  double xsph_c;                // 2*m0*eps
+  double cfl, dt_eta2;          // Δt_stepping
+  double tmin, tmax;
+  int gamma, use_visc, use_pF, timestepping;
+};
+
+// device scalars of a running solve
+struct Scal {
+  double dt;
+  double etime;
+  unsigned long long maxcdx;  // bits of max |cΔx| of the current step
+  unsigned long long amax;    // bits of max |a|
+  unsigned long long vmax;    // bits of max |h v.x/(x.x+η²)|
+  double pad[3];
+};
+
+template <int D>
+struct SArr {
+  const int64_t* rs;
+  const int32_t* nbr;
+  const int32_t* pt;
+  const int32_t* orig;
+  double* x[3];
+  double* v[3];
+  double* rho;
+  double* P1;
+  double* xh[3];
+  double* vh[3];
+  double* rhoh;
+  double* P2;
+  double* We;
+  double* gWe[3];
+  double* a[3];
+  double* drho;
+  double* cdx[3];
+  double* buf2[3];
+  double* Plast;
+  double* xo[3];
+  double* xho[3];
+  double* vho[3];
+  double* vo[3];
+  double* rhoho;
+  double* rhoo;
+};
+
+template <int D>
+__device__ inline double dotD(const double* a, const double* b) {
+  double s = a[0] * b[0];
+#pragma unroll
+  for (int d = 1; d < D; ++d) s = s + a[d] * b[d];
+  return s;
+}
+
+// Julia min/max propagate NaN (fmin/fmax do not)
+__device__ inline double jl_min(double a, double b) { return (a != a || b != b) ? (a + b) : fmin(a, b); }
+__device__ inline double jl_max(double a, double b) { return (a != a || b != b) ? (a + b) : fmax(a, b); }
+
+// ∂ρ∂tDDT! pair value seen from particle k (src/gpukernels_sph.jl:579-625)
+template <int D>
+__device__ inline double ddt_term(const StepConst& c, int ptk, int ptm, const double* dx, double r2, const double* gw,
+                                  const double* dv, double rk, double rm) {
+  if (!(ptk > 0 && ptm > 0)) return 0.0;
+  double dot3 = -dotD<D>(dx, gw);
+  double m0dot = c.m0 * dotD<D>(dv, gw);
+  double s = m0dot;
+  if (ptk > 1) {
+    double drhopvp = c.rho0 * powfancy7th(1.0 + c.DDTgz * dx[1], c.ginv, c.gamma) - c.rho0;
+    double visc_densi = c.DDTkh * ((rm - rk) - drhopvp) / (r2 + c.eta2);
+    double delta = visc_densi * dot3 * c.m0 / rm;
+    s += delta;
+  }
+  return s;
+}
+
+// all momentum terms of one pair seen from k; accumulators kept apart so the
+// final sum follows the reference's kernel order (∂v∂t!, av, visc, grav, fb, pF)
+template <int D>
+struct Acc {
+  double p[D], av[D], vi[D], fb[D], pf[D];
+  __device__ void zero() {
+#pragma unroll
+    for (int d = 0; d < D; ++d) p[d] = av[d] = vi[d] = fb[d] = pf[d] = 0.0;
+  }
+};
+
+template <int D>
+__device__ inline void mom_terms(const StepConst& c, Acc<D>& A, int ptk, int ptm, const double* dx, double r2,
+                                 const double* gw, const double* dv, double rk, double rm, double Pk, double Pm) {
+  // ∂v∂t!, :755-772
+  if (ptk * ptm > 0) {
+    double Pfac = (Pk + Pm) / (rk * rm);
+    double sc = -c.m0 * Pfac;
+#pragma unroll
+    for (int d = 0; d < D; ++d) A.p[d] += sc * gw[d];
+  }
+  if (ptk > 0 && ptm > 0) {
+    // ∂v∂t_av!, :869-897
+    double rhom = (rk + rm) * 0.5;
+    double cond = dotD<D>(dv, dx);
+    if (cond < 0.0) {
+      double dmu = c.h * cond / (r2 + c.eta2);
+      double dPi = (-c.alpha * c.c0 * dmu) / rhom;
+      double sc = -dPi * c.m0;
+#pragma unroll
+      for (int d = 0; d < D; ++d) A.av[d] += sc * gw[d];
+    }
+    // ∂v∂t_visc!, :967-980
+    if (c.use_visc) {
+      double nuterm = 4.0 * c.nu * c.m0 * dotD<D>(dx, gw) / ((rk + rm) * (r2 + c.eta2));
+#pragma unroll
+      for (int d = 0; d < D; ++d) A.vi[d] += nuterm * dv[d];
+    }
+  }
+}
+
+// fbmolforce!, :1891-1901 (mask: exactly one side real)
+template <int D>
+__device__ inline void fb_term(const StepConst& c, Acc<D>& A, int ptk, int ptm, const double* dx, double r2) {
+  if ((ptk > 0) == (ptm > 0)) return;
+  double r = sqrt(r2);
+  if (r < c.fb_r0) {
+    double q = c.fb_r0 / (r + c.fb_eta2);
+    double q2 = q * q, q4 = q2 * q2, q8 = q4 * q4, q12 = q8 * q4;
+    double Fc = c.fb_d * (q12 - q4) / (r2 + c.fb_eta2);
+#pragma unroll
+    for (int d = 0; d < D; ++d) A.fb[d] += dx[d] * Fc;
+  }
+}
+
+// ∂v∂tpF!, :1387-1397
+template <int D>
+__device__ inline void pf_term(const StepConst& c, Acc<D>& A, int ptk, int ptm, const double* dx, double r) {
+  if (!(ptk > 0 && ptm > 0)) return;
+  if (r < c.twoh) {
+    double scos = c.s * cos(c.pfc * r / c.twoh) / (r + c.hp1);
+#pragma unroll
+    for (int d = 0; d < D; ++d) A.pf[d] += scos * dx[d] / c.m0;
+  }
+}
+
+// a = ((((p + av) + visc) - g) + fb) + pF
+template <int D>
+__device__ inline void finish_acc(const StepConst& c, const Acc<D>& A, double* a) {
+#pragma unroll
+  for (int d = 0; d < D; ++d) {
+    double v = A.p[d] + A.av[d];
+    if (c.use_visc) v = v + A.vi[d];
+    v = v - (d == 1 ? c.g : 0.0);
+    v = v + A.fb[d];
+    if (c.use_pF) v = v + A.pf[d];
+    a[d] = v;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// stage 1 at (x, ρ, v) + predictors
+// ---------------------------------------------------------------------------
+template <int D>
+__global__ void __launch_bounds__(STPB) k_stage1(StepConst c, const Scal* __restrict__ sc, int64_t N, SArr<D> S) {
+  int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= N) return;
+  const double dt = sc->dt;
+  double xk[D], vk[D];
+#pragma unroll
+  for (int d = 0; d < D; ++d) { xk[d] = S.x[d][k]; vk[d] = S.v[d][k]; }
+  const double rk = S.rho[k], Pk = S.P1[k];
+  const int ptk = S.pt[k];
+  double drho = 0.0;
+  Acc<D> A;
+  A.zero();
+  const int64_t e0 = S.rs[k], e1 = S.rs[k + 1];
+  for (int64_t e = e0; e < e1; ++e) {
+    const int32_t m = S.nbr[e];
+    double dx[D], dv[D], gw[D];
+#pragma unroll
+    for (int d = 0; d < D; ++d) { dx[d] = xk[d] - S.x[d][m]; dv[d] = vk[d] - S.v[d][m]; }
+    const double r2 = dotD<D>(dx, dx);
+    const double r = sqrt(r2);
+    const double u = r * c.Hinv;
+    S.We[e] = wc2_w(u, c.nW);                       // sphW!, :84-100
+    const double dwk_r = wc2_dw(u, c.nDW) / r;      // sph∇W!, :196-213
+#pragma unroll
+    for (int d = 0; d < D; ++d) { gw[d] = dx[d] * dwk_r; S.gWe[d][e] = gw[d]; }
+    const int ptm = S.pt[m];
+    const double rm = S.rho[m];
+    drho += ddt_term<D>(c, ptk, ptm, dx, r2, gw, dv, rk, rm);
+    mom_terms<D>(c, A, ptk, ptm, dx, r2, gw, dv, rk, rm, Pk, S.P1[m]);
+    fb_term<D>(c, A, ptk, ptm, dx, r2);
+    if (c.use_pF) pf_term<D>(c, A, ptk, ptm, dx, r);
+  }
+  double a[D];
+  finish_acc<D>(c, A, a);
+  // update_ρp∂ρ∂tΔt!, update_vp∂v∂tΔt!, update_xpvΔt! (:1088-1169), Δt/2
+  const double hdt = dt * 0.5;
+  double rv = S.rhoh[k] + drho * hdt;
+  if (rv < c.rho0 && ptk < 0) rv = c.rho0;
+  S.rhoh[k] = rv;
+#pragma unroll
+  for (int d = 0; d < D; ++d) {
+    double vh = S.vh[d][k];
+    if (ptk > 1) vh = vh + a[d] * hdt;
+    S.vh[d][k] = vh;
+    S.xh[d][k] = S.xh[d][k] + vh * hdt;
+  }
+  S.P2[k] = eos(rv, c.gamma, c.rho0, c.P0, ptk);   // pressure! at ρΔt½
+}
+
+// ---------------------------------------------------------------------------
+// stage 2 at (xΔt½, ρΔt½, vΔt½) with stage-1 ∇W, + symplectic_update!
+// ---------------------------------------------------------------------------
+template <int D>
+__global__ void __launch_bounds__(STPB) k_stage2(StepConst c, Scal* __restrict__ sc, int64_t N, SArr<D> S) {
+  int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  double mc = 0.0;
+  if (k < N) {
+    const double dt = sc->dt;
+    double xk[D], xhk[D], vhk[D];
+#pragma unroll
+    for (int d = 0; d < D; ++d) { xk[d] = S.x[d][k]; xhk[d] = S.xh[d][k]; vhk[d] = S.vh[d][k]; }
+    const double rk = S.rhoh[k], Pk = S.P2[k];
+    const int ptk = S.pt[k];
+    double drho = 0.0;
+    Acc<D> A;
+    A.zero();
+    const int64_t e0 = S.rs[k], e1 = S.rs[k + 1];
+    for (int64_t e = e0; e < e1; ++e) {
+      const int32_t m = S.nbr[e];
+      double dx[D], dv[D], gw[D], dxf[D];
+#pragma unroll
+      for (int d = 0; d < D; ++d) {
+        dx[d] = xhk[d] - S.xh[d][m];
+        dv[d] = vhk[d] - S.vh[d][m];
+        gw[d] = S.gWe[d][e];
+      }
+      const double r2 = dotD<D>(dx, dx);
+      const int ptm = S.pt[m];
+      const double rm = S.rhoh[m];
+      drho += ddt_term<D>(c, ptk, ptm, dx, r2, gw, dv, rk, rm);
+      mom_terms<D>(c, A, ptk, ptm, dx, r2, gw, dv, rk, rm, Pk, S.P2[m]);
+      if ((ptk > 0) != (ptm > 0)) {
+#pragma unroll
+        for (int d = 0; d < D; ++d) dxf[d] = xk[d] - S.x[d][m];
+        fb_term<D>(c, A, ptk, ptm, dxf, dotD<D>(dxf, dxf));
+      }
+      if (c.use_pF) pf_term<D>(c, A, ptk, ptm, dx, sqrt(r2));
+    }
+    double a[D];
+    finish_acc<D>(c, A, a);
+    S.drho[k] = drho;
+    S.Plast[k] = Pk;
+    // symplectic_update!, :1204-1245
+    const double epsi = -(drho / rk) * dt;
+    double rv = S.rho[k] * (2.0 - epsi) / (2.0 + epsi);
+    if (rv < c.rho0 && ptk <= 1) rv = c.rho0;
+    S.rho[k] = rv;
+    S.rhoho[k] = rv;
+    S.P1[k] = eos(rv, c.gamma, c.rho0, c.P0, ptk);
+    const double ml = ptk > 1 ? 1.0 : 0.0;
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      S.a[d][k] = a[d];
+      const double vv = S.v[d][k];
+      const double nv = vv + a[d] * dt * ml;
+      S.vho[d][k] = nv;
+      S.v[d][k] = nv;
+      const double ddx = (vv + nv) * 0.5 * dt;
+      const double cd = S.cdx[d][k] + ddx;
+      S.cdx[d][k] = cd;
+      mc = fmax(mc, fabs(cd));
+      const double xv = xk[d] + ddx;
+      S.xho[d][k] = xv;
+      S.xo[d][k] = xv;
+    }
+  }
+  // maximum(maximum.(abs, cΔx)), src/sphproblem.jl:325
+  mc = warp_max(mc);
+  __shared__ double smax[STPB / 32];
+  if ((threadIdx.x & 31) == 0) smax[threadIdx.x >> 5] = mc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double m = smax[0];
+    for (int w = 1; w < STPB / 32; ++w) m = fmax(m, smax[w]);
+    atomic_max_pos(&sc->maxcdx, m);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// dpcreg! + update_dpcreg!  (:1500-1553, :1617-1632)
+// ---------------------------------------------------------------------------
+template <int D>
+__global__ void __launch_bounds__(STPB) k_dpc(StepConst c, const Scal* __restrict__ sc, int64_t N, SArr<D> S) {
+  int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= N) return;
+  const double dt = sc->dt;
+  double xk[D], vk[D], sum[D];
+#pragma unroll
+  for (int d = 0; d < D; ++d) { xk[d] = S.x[d][k]; vk[d] = S.v[d][k]; sum[d] = 0.0; }
+  const double rk = S.rho[k], Pk = S.P1[k];
+  const int ptk = S.pt[k];
+  const int64_t e0 = S.rs[k], e1 = S.rs[k + 1];
+  if (ptk > 0) {
+    for (int64_t e = e0; e < e1; ++e) {
+      const int32_t m = S.nbr[e];
+      if (!(S.pt[m] > 0)) continue;
+      double dx[D], dv[D];
+#pragma unroll
+      for (int d = 0; d < D; ++d) { dx[d] = xk[d] - S.x[d][m]; dv[d] = vk[d] - S.v[d][m]; }
+      const double rm = S.rho[m];
+      const double r2 = dotD<D>(dx, dx);
+      const double r = sqrt(r2);
+      const double u = r * c.dpc_l0inv;
+      const double w = wc2_w(u, c.dpc_nW);
+      const double chi = sqrt(w * c.dpc_whinv);
+      const double kk = u < c.dpc_kernlim ? 1.0 : chi;
+      const double Pb = chi * jl_max(jl_min(c.dpc_lambda * fabs(Pk + S.P1[m]), c.dpc_lambda * c.dpc_pmax), c.dpc_pmin);
+      const double vr = dotD<D>(dv, dx);
+      if (vr < 0.0) {
+        const double vrdr = vr / (r2 + c.dpc_eta2);
+#pragma unroll
+        for (int d = 0; d < D; ++d) sum[d] += kk * (-vrdr * dx[d]);
+      } else {
+        const double tvar = 2.0 * dt * Pb / ((rk + rm) * (r2 + c.dpc_eta2));
+#pragma unroll
+        for (int d = 0; d < D; ++d) sum[d] += tvar * dx[d];
+      }
+    }
+  }
+  S.Plast[k] = Pk;
+#pragma unroll
+  for (int d = 0; d < D; ++d) {
+    S.buf2[d][k] = sum[d];
+    double nv = vk[d], nx = xk[d];
+    if (ptk > 1) {
+      nv = vk[d] + sum[d];
+      nx = xk[d] + sum[d] * dt;
+    }
+    S.vo[d][k] = nv;
+    S.xo[d][k] = nx;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// xsphcorr! + update_xsphcorr!  (:1757-1779, :1827-1838), stage-1 W
+// ---------------------------------------------------------------------------
+template <int D>
+__global__ void __launch_bounds__(STPB) k_xsph(StepConst c, const Scal* __restrict__ sc, int64_t N, SArr<D> S) {
+  int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= N) return;
+  const double dt = sc->dt;
+  double vk[D], sum[D];
+#pragma unroll
+  for (int d = 0; d < D; ++d) { vk[d] = S.v[d][k]; sum[d] = 0.0; }
+  const double rk = S.rho[k];
+  const int ptk = S.pt[k];
+  if (ptk > 1) {
+    const int64_t e0 = S.rs[k], e1 = S.rs[k + 1];
+    for (int64_t e = e0; e < e1; ++e) {
+      const int32_t m = S.nbr[e];
+      if (!(S.pt[m] > 1)) continue;
+      const double xs = c.xsph_c * S.We[e] / (rk + S.rho[m]);
+#pragma unroll
+      for (int d = 0; d < D; ++d) sum[d] += (S.v[d][m] - vk[d]) * xs;
+    }
+  }
+#pragma unroll
+  for (int d = 0; d < D; ++d) {
+    S.buf2[d][k] = sum[d];
+    if (ptk > 1) S.x[d][k] = S.x[d][k] + sum[d] * dt;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// cspmcorr!  (:1693-1719), stage-1 W; writes ρ to the other buffer
+// ---------------------------------------------------------------------------
+template <int D>
+__global__ void __launch_bounds__(STPB) k_cspm(StepConst c, int64_t N, SArr<D> S) {
+  int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= N) return;
+  const double rk = S.rho[k];
+  const int ptk = S.pt[k];
+  double s1 = 0.0, s2 = 0.0;
+  if (ptk > 0) {
+    const int64_t e0 = S.rs[k], e1 = S.rs[k + 1];
+    for (int64_t e = e0; e < e1; ++e) {
+      const int32_t m = S.nbr[e];
+      if (!(S.pt[m] > 0)) continue;
+      const double w = S.We[e];
+      s1 += c.m0 * w;
+      s2 += w * c.m0 / S.rho[m];
+    }
+  }
+  double nr = s1 / s2;
+  double rv = isnan(nr) ? rk : nr;
+  S.rhoo[k] = rv;
+  S.P1[k] = eos(rv, c.gamma, c.rho0, c.P0, ptk);
+  S.buf2[0][k] = s1;
+  S.buf2[1][k] = s2;
+  if (D == 3) S.buf2[2][k] = 0.0;
+}
+
+// ---------------------------------------------------------------------------
+// Δt_stepping (:1293-1353): device maxima, then the scalar update
+// ---------------------------------------------------------------------------
+template <int D>
+__global__ void __launch_bounds__(STPB) k_dt_reduce(StepConst c, Scal* __restrict__ sc, int64_t N, SArr<D> S) {
+  int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  double am = 0.0, vm = 0.0;
+  if (k < N) {
+    double av[D], vv[D], pp[D];
+#pragma unroll
+    for (int d = 0; d < D; ++d) { av[d] = S.a[d][k]; vv[d] = S.v[d][k]; pp[d] = S.x[d][k]; }
+    am = sqrt(dotD<D>(av, av));
+    vm = fabs(c.h * dotD<D>(vv, pp) / (dotD<D>(pp, pp) + c.dt_eta2));
+  }
+  am = warp_max(am);
+  vm = warp_max(vm);
+  if ((threadIdx.x & 31) == 0) {
+    atomic_max_pos(&sc->amax, am);
+    atomic_max_pos(&sc->vmax, vm);
+  }
+}
+
+__global__ void k_step_end(StepConst c, Scal* __restrict__ sc) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double dt = sc->dt;
+  sc->etime = sc->etime + dt;  // prob.etime += prob.Δt, src/sphproblem.jl:331
+  if (c.timestepping) {
+    double amax = __longlong_as_double((long long)sc->amax);
+    double vmax = __longlong_as_double((long long)sc->vmax);
+    double dt1 = sqrt(c.h / (3.0 * amax));
+    double dt2 = c.h / (c.c0 + vmax);
+    double nd = c.cfl * jl_min(dt1, dt2);
+    nd = jl_min(jl_max(nd, c.tmin), c.tmax);
+    sc->dt = nd;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// post-batch sph∑W! + sph∑∇W! (:139-156, :332-359) on original-order arrays
+// ---------------------------------------------------------------------------
+template <int D>
+__global__ void __launch_bounds__(STPB) k_sums_post(StepConst c, int64_t N, const int64_t* __restrict__ rs,
+                                                     const int32_t* __restrict__ nbr, const int32_t* __restrict__ orig,
+                                                     const int32_t* __restrict__ pt, const double* __restrict__ x0,
+                                                     const double* __restrict__ x1, const double* __restrict__ x2,
+                                                     double* __restrict__ sumW, double* __restrict__ sg0,
+                                                     double* __restrict__ sg1, double* __restrict__ sg2) {
+  int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= N) return;
+  const double* X[3] = {x0, x1, x2};
+  const int32_t o = orig[k];
+  double xk[D];
+#pragma unroll
+  for (int d = 0; d < D; ++d) xk[d] = X[d][o];
+  const bool rk = pt[o] > 0;
+  double sw = 0.0, sg[D];
+#pragma unroll
+  for (int d = 0; d < D; ++d) sg[d] = 0.0;
+  for (int64_t e = rs[k]; e < rs[k + 1]; ++e) {
+    const int32_t om = orig[nbr[e]];
+    if ((pt[om] > 0) != rk) continue;
+    double dx[D];
+#pragma unroll
+    for (int d = 0; d < D; ++d) dx[d] = xk[d] - X[d][om];
+    const double r = sqrt(dotD<D>(dx, dx));
+    const double u = r * c.Hinv;
+    sw += wc2_w(u, c.nW);
+    const double dwk_r = wc2_dw(u, c.nDW) / r;
+#pragma unroll
+    for (int d = 0; d < D; ++d) sg[d] += dx[d] * dwk_r;
+  }
+  sumW[o] = sw;
+  double* SG[3] = {sg0, sg1, sg2};
+#pragma unroll
+  for (int d = 0; d < D; ++d) SG[d][o] = sg[d];
+}
+
+// ---------------------------------------------------------------------------
+// state gather (original -> cell order) and scatter (cell -> original order)
+// ---------------------------------------------------------------------------
+template <int D>
+struct StateIO {
+  // original-order arrays
+  double* x[3];
+  double* v[3];
+  double* rho;
+  const int32_t* pt;
+  double* rhoh;
+  double* vh[3];
+  double* xh[3];
+  double* cdx[3];
+  double* a[3];
+  double* drho;
+  double* buf2[3];
+  double* P;
+};
+
+template <int D>
+__global__ void k_gather_state(StepConst c, int64_t N, const int32_t* __restrict__ orig, StateIO<D> O, SArr<D> S) {
+  int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= N) return;
+  const int32_t o = orig[k];
+  const int pt = O.pt[o];
+  ((int32_t*)S.pt)[k] = pt;
+  const double r = O.rho[o];
+  S.rho[k] = r;
+  S.P1[k] = eos(r, c.gamma, c.rho0, c.P0, pt);
+  S.rhoh[k] = O.rhoh[o];
+#pragma unroll
+  for (int d = 0; d < D; ++d) {
+    S.x[d][k] = O.x[d][o];
+    S.v[d][k] = O.v[d][o];
+    S.vh[d][k] = O.vh[d][o];
+    S.xh[d][k] = O.xh[d][o];
+    S.buf2[d][k] = O.buf2[d][o];
+    S.cdx[d][k] = 0.0;  // cΔx reset after update!, src/sphproblem.jl:229
+  }
+}
+
+template <int D>
+__global__ void k_scatter_state(int64_t N, const int32_t* __restrict__ orig, StateIO<D> O, SArr<D> S) {
+  int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= N) return;
+  const int32_t o = orig[k];
+  O.rho[o] = S.rho[k];
+  O.rhoh[o] = S.rhoh[k];
+  O.drho[o] = S.drho[k];
+  O.P[o] = S.Plast[k];
+#pragma unroll
+  for (int d = 0; d < D; ++d) {
+    O.x[d][o] = S.x[d][k];
+    O.v[d][o] = S.v[d][k];
+    O.vh[d][o] = S.vh[d][k];
+    O.xh[d][o] = S.xh[d][k];
+    O.cdx[d][o] = S.cdx[d][k];
+    O.a[d][o] = S.a[d][k];
+    O.buf2[d][o] = S.buf2[d][k];
+  }
+}
+
+}  // namespace gcsph
+
+// ===========================================================================
+// host side
+// ===========================================================================
+using namespace gcsph;
+
+struct sph_handle {
+  gcl_handle* cl = nullptr;
+  int D = 2;
+  int64_t N = 0;
+  gcsph_params prm{};
+  // caller arrays (original order)
+  double* rho_u = nullptr;
+  double* v_u[3] = {nullptr, nullptr, nullptr};
+  const int32_t* pt_u = nullptr;
+  DevBuf vown[3];
+  // library-owned original-order arrays
+  DevBuf rhoh_o, vh_o[3], xh_o[3], cdx_o[3], P_o, a_o[3], drho_o, buf2_o[3], sumW_o, sumgW_o[3];
+  // cell-order working arrays
+  DevBuf X[2][3], XH[2][3], V[2][3], VH[2][3], RHO[2], RHOH[2], P1, P2, PT, A[3], DRHO, CDX[3], BUF2[3], PLAST, We,
+      GWe[3];
+  int ix = 0, ixh = 0, iv = 0, ivh = 0, irho = 0, irhoh = 0;
+  int64_t we_cap = 0;
+  DevBuf scal;
+  Scal* pin = nullptr;
+  bool in_cell_order = false;
+};
+
+static StepConst make_const(const sph_handle* h) {
+  const gcsph_params& p = h->prm;
+  StepConst c{};
+  c.h = p.h;
+  c.eta2 = (0.1 * p.h) * (0.1 * p.h);
+  c.m0 = p.m0;
+  c.rho0 = p.rho0;
+  c.gamma = p.gamma;
+  c.ginv = 1.0 / (double)p.gamma;
+  c.DDTkh = 2.0 * p.h * p.delta * p.c0;
+  double Cb = (p.c0 * p.c0 * p.rho0) * c.ginv;
+  c.DDTgz = p.rho0 * p.g / Cb;
+  c.P0 = p.c0 * p.c0 * p.rho0 / (double)p.gamma;
+  c.alpha = p.alpha;
+  c.c0 = p.c0;
+  c.nu = p.nu;
+  c.g = p.g;
+  c.s = p.s;
+  c.Hinv = 1.0 / p.H;
+  if (h->D == 2) {
+    c.nW = wc2_norm_w<2>(c.Hinv);
+    c.nDW = wc2_norm_dw<2>(c.Hinv);
+  } else {
+    c.nW = wc2_norm_w<3>(c.Hinv);
+    c.nDW = wc2_norm_dw<3>(c.Hinv);
+  }
+  c.twoh = 2.0 * p.h;
+  c.pfc = 1.5 * GCSPH_PI64;
+  c.hp1 = 0.1 * p.h;
+  c.use_visc = p.nu > 0;
+  c.use_pF = p.s > 0;
+  if (p.dpc_l0 > 0) {
+    c.dpc_l0inv = 1.0 / p.dpc_l0;
+    c.dpc_nW = h->D == 2 ? wc2_norm_w<2>(c.dpc_l0inv) : wc2_norm_w<3>(c.dpc_l0inv);
+    c.dpc_whinv = 1.0 / wc2_w(0.5, c.dpc_nW);
+    c.dpc_pmin = p.dpc_pmin;
+    c.dpc_pmax = p.dpc_pmax;
+    c.dpc_lambda = p.dpc_lambda;
+    c.dpc_kernlim = gcsph_dpckernlim(h->D);
+    c.dpc_eta2 = (0.1 * p.dpc_l0) * (0.1 * p.dpc_l0);
+  }
+  c.xsph_c = 2.0 * p.m0 * p.xsph_eps;
+  c.cfl = p.CFL;
+  c.dt_eta2 = (0.01 * p.h) * (0.01 * p.h);
+  return c;
+}
+
+template <int D>
+static SArr<D> make_arr(sph_handle* h) {
+  SArr<D> S{};
+  CellCore& core = h->cl->core;
+  S.rs = core.rs_full.as<int64_t>();
+  S.nbr = core.nbr.as<int32_t>();
+  S.pt = h->PT.as<int32_t>();
+  S.orig = core.orig.as<int32_t>();
+  for (int d = 0; d < D; ++d) {
+    S.x[d] = h->X[h->ix][d].as<double>();
+    S.xo[d] = h->X[h->ix ^ 1][d].as<double>();
+    S.v[d] = h->V[h->iv][d].as<double>();
+    S.vo[d] = h->V[h->iv ^ 1][d].as<double>();
+    S.xh[d] = h->XH[h->ixh][d].as<double>();
+    S.xho[d] = h->XH[h->ixh ^ 1][d].as<double>();
+    S.vh[d] = h->VH[h->ivh][d].as<double>();
+    S.vho[d] = h->VH[h->ivh ^ 1][d].as<double>();
+    S.gWe[d] = h->GWe[d].as<double>();
+    S.a[d] = h->A[d].as<double>();
+    S.cdx[d] = h->CDX[d].as<double>();
+    S.buf2[d] = h->BUF2[d].as<double>();
+  }
+  S.rho = h->RHO[h->irho].as<double>();
+  S.rhoo = h->RHO[h->irho ^ 1].as<double>();
+  S.rhoh = h->RHOH[h->irhoh].as<double>();
+  S.rhoho = h->RHOH[h->irhoh ^ 1].as<double>();
+  S.P1 = h->P1.as<double>();
+  S.P2 = h->P2.as<double>();
+  S.We = h->We.as<double>();
+  S.drho = h->DRHO.as<double>();
+  S.Plast = h->PLAST.as<double>();
+  return S;
+}
+
+template <int D>
+static StateIO<D> make_io(sph_handle* h) {
+  StateIO<D> O{};
+  for (int d = 0; d < D; ++d) {
+    O.x[d] = (double*)h->cl->xuser[d];
+    O.v[d] = h->v_u[d];
+    O.vh[d] = h->vh_o[d].as<double>();
+    O.xh[d] = h->xh_o[d].as<double>();
+    O.cdx[d] = h->cdx_o[d].as<double>();
+    O.a[d] = h->a_o[d].as<double>();
+    O.buf2[d] = h->buf2_o[d].as<double>();
+  }
+  O.rho = h->rho_u;
+  O.pt = h->pt_u;
+  O.rhoh = h->rhoh_o.as<double>();
+  O.drho = h->drho_o.as<double>();
+  O.P = h->P_o.as<double>();
+  return O;
+}
+
+template <int D>
+static int scatter_state(sph_handle* h) {
+  CellCore& core = h->cl->core;
+  timer_begin(T_STATE, core.st);
+  k_scatter_state<D><<<nblocks(h->N, 256), 256, 0, core.st>>>(h->N, core.orig.as<int32_t>(), make_io<D>(h),
+                                                             make_arr<D>(h));
+  GC_LAUNCHED();
+  timer_end(T_STATE, core.st);
+  h->in_cell_order = false;
+  return GCSPH_OK;
+}
+
+// update! inside stepsolve!: bin the original-order points, sort, gather the
+// whole state into cell order, rebuild the neighbour CSR
+template <int D>
+static int rebuild(sph_handle* h, const StepConst& c) {
+  CellCore& core = h->cl->core;
+  int rc;
+  if (h->in_cell_order && (rc = scatter_state<D>(h))) return rc;
+  if ((rc = core.sort(h->cl->xuser, nullptr))) return rc;
+  h->ix = h->ixh = h->iv = h->ivh = h->irho = h->irhoh = 0;
+  timer_begin(T_STATE, core.st);
+  k_gather_state<D><<<nblocks(h->N, 256), 256, 0, core.st>>>(c, h->N, core.orig.as<int32_t>(), make_io<D>(h),
+                                                            make_arr<D>(h));
+  GC_LAUNCHED();
+  timer_end(T_STATE, core.st);
+  h->in_cell_order = true;
+  double* xs[3] = {h->X[0][0].as<double>(), h->X[0][1].as<double>(), D == 3 ? h->X[0][2].as<double>() : nullptr};
+  if ((rc = core.build_pairs((const double* const*)xs))) return rc;
+  if (core.nfull > h->we_cap) {
+    int64_t want = core.nbr_cap;
+    if ((rc = h->We.ensure(sizeof(double) * want, core.st))) return rc;
+    for (int d = 0; d < D; ++d)
+      if ((rc = h->GWe[d].ensure(sizeof(double) * want, core.st))) return rc;
+    h->we_cap = want;
+  }
+  return GCSPH_OK;
+}
+
+template <int D>
+static int step_impl(sph_handle* h, int32_t n, int timestepping, double tmin, double tmax, int64_t* updaten_out,
+                     double* maxcdx_out) {
+  CellCore& core = h->cl->core;
+  cudaStream_t st = core.st;
+  StepConst c = make_const(h);
+  c.timestepping = timestepping;
+  c.tmin = tmin;
+  c.tmax = tmax;
+  Scal* dsc = h->scal.as<Scal>();
+  h->pin->dt = h->prm.dt;
+  h->pin->etime = h->prm.etime;
+  h->pin->maxcdx = h->pin->amax = h->pin->vmax = 0;
+  GC_CUDA(cudaMemcpyAsync(dsc, h->pin, sizeof(Scal), cudaMemcpyHostToDevice, st));
+  const gcsph_params& p = h->prm;
+  bool skip = false;
+  int64_t updaten = 0;
+  double maxout = 0.0;
+  int32_t cspmcnt = 0;
+  int rc;
+  const int nb = nblocks(h->N, STPB);
+  for (int32_t it = 0; it < n; ++it) {
+    cspmcnt += 1;
+    if (!skip) {
+      if ((rc = rebuild<D>(h, c))) return rc;
+      skip = true;
+      updaten += 1;
+    }
+    GC_CUDA(cudaMemsetAsync(&dsc->maxcdx, 0, 3 * sizeof(unsigned long long), st));
+    c.fb_d = 0.4;
+    c.fb_r0 = 2.0 * p.dx;
+    c.fb_eta2 = 0.01 * (c.fb_r0 * c.fb_r0);
+    timer_begin(T_STAGE1, st);
+    k_stage1<D><<<nb, STPB, 0, st>>>(c, dsc, h->N, make_arr<D>(h));
+    GC_LAUNCHED();
+    timer_end(T_STAGE1, st);
+    c.fb_d = p.bound_D;
+    c.fb_r0 = p.bound_l;
+    c.fb_eta2 = 0.01 * (c.fb_r0 * c.fb_r0);
+    timer_begin(T_STAGE2, st);
+    k_stage2<D><<<nb, STPB, 0, st>>>(c, dsc, h->N, make_arr<D>(h));
+    GC_LAUNCHED();
+    timer_end(T_STAGE2, st);
+    h->ix ^= 1;
+    h->ixh ^= 1;
+    h->ivh ^= 1;
+    h->irhoh ^= 1;
+    if (p.dpc_l0 > 0) {
+      timer_begin(T_DPC, st);
+      k_dpc<D><<<nb, STPB, 0, st>>>(c, dsc, h->N, make_arr<D>(h));
+      GC_LAUNCHED();
+      timer_end(T_DPC, st);
+      h->iv ^= 1;
+      h->ix ^= 1;
+    }
+    if (p.xsph_eps > 0) {
+      timer_begin(T_XSPH, st);
+      k_xsph<D><<<nb, STPB, 0, st>>>(c, dsc, h->N, make_arr<D>(h));
+      GC_LAUNCHED();
+      timer_end(T_XSPH, st);
+    }
+    if (p.cspmn > 0 && cspmcnt == p.cspmn) {
+      timer_begin(T_CSPM, st);
+      k_cspm<D><<<nb, STPB, 0, st>>>(c, h->N, make_arr<D>(h));
+      GC_LAUNCHED();
+      timer_end(T_CSPM, st);
+      h->irho ^= 1;
+      cspmcnt = 0;
+    }
+    if (timestepping) {
+      timer_begin(T_DT, st);
+      k_dt_reduce<D><<<nb, STPB, 0, st>>>(c, dsc, h->N, make_arr<D>(h));
+      GC_LAUNCHED();
+      timer_end(T_DT, st);
+    }
+    k_step_end<<<1, 32, 0, st>>>(c, dsc);
+    GC_LAUNCHED();
+    GC_CUDA(cudaMemcpyAsync(&h->pin->maxcdx, &dsc->maxcdx, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+    GC_CUDA(cudaStreamSynchronize(st));
+    timer_collect();
+    unsigned long long bits = h->pin->maxcdx;
+    double mc;
+    memcpy(&mc, &bits, 8);
+    if (mc > 0.9 * p.nui) skip = false;
+    if (mc > maxout) maxout = mc;
+  }
+  if (h->in_cell_order && (rc = scatter_state<D>(h))) return rc;
+  // post-batch ∑W, ∑∇W on the last pair set and the final points
+  if (core.built) {
+    const double* x2 = D == 3 ? h->cl->xuser[2] : h->cl->xuser[0];
+    double* sg2 = D == 3 ? h->sumgW_o[2].as<double>() : h->sumgW_o[0].as<double>();
+    timer_begin(T_POST, st);
+    k_sums_post<D><<<nb, STPB, 0, st>>>(c, h->N, core.rs_full.as<int64_t>(), core.nbr.as<int32_t>(),
+                                        core.orig.as<int32_t>(), h->pt_u, h->cl->xuser[0], h->cl->xuser[1], x2,
+                                        h->sumW_o.as<double>(), h->sumgW_o[0].as<double>(),
+                                        h->sumgW_o[1].as<double>(), sg2);
+    GC_LAUNCHED();
+    timer_end(T_POST, st);
+  }
+  GC_CUDA(cudaMemcpyAsync(h->pin, dsc, sizeof(Scal), cudaMemcpyDeviceToHost, st));
+  GC_CUDA(cudaStreamSynchronize(st));
+  timer_collect();
+  h->prm.dt = h->pin->dt;
+  h->prm.etime = h->pin->etime;
+  if (updaten_out) *updaten_out = updaten;
+  if (maxcdx_out) *maxcdx_out = maxout;
+  return GCSPH_OK;
+}
+
+extern "C" {
+
+int sph_create(gcl_handle* cl, const gcsph_params* prm, double* rho_dev, double* const* v_dev,
+               const int32_t* ptype_dev, sph_handle** out) {
+  if (!cl || !prm || !rho_dev || !ptype_dev || !out) return fail(GCSPH_EINVAL, "null argument");
+  *out = nullptr;
+  if (prm->gamma <= 0) return fail(GCSPH_EINVAL, "gamma must be a positive integer");
+  sph_handle* h = new sph_handle();
+  h->cl = cl;
+  h->D = cl->core.D;
+  h->N = cl->core.N;
+  h->prm = *prm;
+  h->rho_u = rho_dev;
+  h->pt_u = ptype_dev;
+  cudaStream_t st = cl->core.st;
+  const int64_t N = h->N;
+  const size_t nb = sizeof(double) * (size_t)N;
+  int rc = GCSPH_OK;
+  auto E = [&](DevBuf& b, size_t bytes, bool zero) {
+    if (!rc) rc = b.ensure(bytes, st, zero);
+  };
+  for (int d = 0; d < h->D; ++d) {
+    if (v_dev && v_dev[d]) {
+      h->v_u[d] = v_dev[d];
+    } else {
+      E(h->vown[d], nb, true);
+      h->v_u[d] = h->vown[d].as<double>();
+    }
+    E(h->vh_o[d], nb, false);
+    E(h->xh_o[d], nb, false);
+    E(h->cdx_o[d], nb, true);
+    E(h->a_o[d], nb, true);
+    E(h->buf2_o[d], nb, true);
+    E(h->sumgW_o[d], nb, true);
+    for (int b = 0; b < 2; ++b) {
+      E(h->X[b][d], nb, false);
+      E(h->XH[b][d], nb, false);
+      E(h->V[b][d], nb, false);
+      E(h->VH[b][d], nb, false);
+    }
+    E(h->A[d], nb, true);
+    E(h->CDX[d], nb, true);
+    E(h->BUF2[d], nb, true);
+  }
+  E(h->rhoh_o, nb, false);
+  E(h->P_o, nb, true);
+  E(h->drho_o, nb, true);
+  E(h->sumW_o, nb, true);
+  for (int b = 0; b < 2; ++b) {
+    E(h->RHO[b], nb, false);
+    E(h->RHOH[b], nb, false);
+  }
+  E(h->P1, nb, true);
+  E(h->P2, nb, true);
+  E(h->PT, sizeof(int32_t) * N, false);
+  E(h->DRHO, nb, true);
+  E(h->PLAST, nb, true);
+  E(h->scal, sizeof(Scal), true);
+  if (!rc) {
+    cudaError_t e = cudaMallocHost((void**)&h->pin, sizeof(Scal));
+    if (e != cudaSuccess) rc = cuda_fail(e, "cudaMallocHost", __FILE__, __LINE__);
+  }
+  if (!rc) {
+    // ρΔt½ = deepcopy(ρ), vΔt½ = deepcopy.(v), xΔt½ = deepcopy(points) (src/sphproblem.jl:141-143)
+    cudaError_t e = cudaMemcpyAsync(h->rhoh_o.p, rho_dev, nb, cudaMemcpyDeviceToDevice, st);
+    for (int d = 0; d < h->D && e == cudaSuccess; ++d) {
+      e = cudaMemcpyAsync(h->vh_o[d].p, h->v_u[d], nb, cudaMemcpyDeviceToDevice, st);
+      if (e == cudaSuccess) e = cudaMemcpyAsync(h->xh_o[d].p, cl->xuser[d], nb, cudaMemcpyDeviceToDevice, st);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) rc = cuda_fail(e, "initial copies", __FILE__, __LINE__);
+  }
+  if (rc) {
+    std::string keep = gcsph_last_error();
+    sph_destroy(h);
+    set_error("%s", keep.c_str());
+    return rc;
+  }
+  *out = h;
+  return GCSPH_OK;
+}
+
+void sph_destroy(sph_handle* h) {
+  if (!h) return;
+  if (h->cl) cudaStreamSynchronize(h->cl->core.st);
+  DevBuf* one[] = {&h->rhoh_o, &h->P_o, &h->drho_o, &h->sumW_o, &h->P1, &h->P2, &h->PT, &h->DRHO, &h->PLAST,
+                   &h->We, &h->scal, &h->RHO[0], &h->RHO[1], &h->RHOH[0], &h->RHOH[1]};
+  for (DevBuf* b : one) b->release();
+  for (int d = 0; d < 3; ++d) {
+    h->vown[d].release();
+    h->vh_o[d].release();
+    h->xh_o[d].release();
+    h->cdx_o[d].release();
+    h->a_o[d].release();
+    h->buf2_o[d].release();
+    h->sumgW_o[d].release();
+    h->A[d].release();
+    h->CDX[d].release();
+    h->BUF2[d].release();
+    h->GWe[d].release();
+    for (int b = 0; b < 2; ++b) {
+      h->X[b][d].release();
+      h->XH[b][d].release();
+      h->V[b][d].release();
+      h->VH[b][d].release();
+    }
+  }
+  if (h->pin) cudaFreeHost(h->pin);
+  delete h;
+}
+
+int sph_set_params(sph_handle* h, const gcsph_params* prm) {
+  if (!h || !prm) return fail(GCSPH_EINVAL, "null argument");
+  if (prm->gamma <= 0) return fail(GCSPH_EINVAL, "gamma must be a positive integer");
+  h->prm = *prm;
+  return GCSPH_OK;
+}
+
+int sph_get_params(const sph_handle* h, gcsph_params* prm) {
+  if (!h || !prm) return fail(GCSPH_EINVAL, "null argument");
+  *prm = h->prm;
+  return GCSPH_OK;
+}
+
+int sph_step(sph_handle* h, int32_t n, int timestepping, double tmin, double tmax, int64_t* updaten,
+             double* maxcdx) {
+  if (!h) return fail(GCSPH_EINVAL, "null handle");
+  if (n < 0) return fail(GCSPH_EINVAL, "n must be >= 0");
+  if (timestepping && tmin > tmax) return fail(GCSPH_EINVAL, "timelims[1] should be < timelims[2]");
+  return h->D == 2 ? step_impl<2>(h, n, timestepping, tmin, tmax, updaten, maxcdx)
+                   : step_impl<3>(h, n, timestepping, tmin, tmax, updaten, maxcdx);
+}
+
+int sph_get_field(sph_handle* h, int32_t field, void* dst) {
+  if (!h || !dst) return fail(GCSPH_EINVAL, "null argument");
+  cudaStream_t st = h->cl->core.st;
+  const size_t nb = sizeof(double) * (size_t)h->N;
+  const void* src[3] = {nullptr, nullptr, nullptr};
+  int nvec = 1;
+  size_t bytes = nb;
+  switch (field) {
+    case GCSPH_F_X: nvec = h->D; for (int d = 0; d < h->D; ++d) src[d] = h->cl->xuser[d]; break;
+    case GCSPH_F_RHO: src[0] = h->rho_u; break;
+    case GCSPH_F_V: nvec = h->D; for (int d = 0; d < h->D; ++d) src[d] = h->v_u[d]; break;
+    case GCSPH_F_P: src[0] = h->P_o.p; break;
+    case GCSPH_F_A: nvec = h->D; for (int d = 0; d < h->D; ++d) src[d] = h->a_o[d].p; break;
+    case GCSPH_F_DRHODT: src[0] = h->drho_o.p; break;
+    case GCSPH_F_RHOH: src[0] = h->rhoh_o.p; break;
+    case GCSPH_F_VH: nvec = h->D; for (int d = 0; d < h->D; ++d) src[d] = h->vh_o[d].p; break;
+    case GCSPH_F_XH: nvec = h->D; for (int d = 0; d < h->D; ++d) src[d] = h->xh_o[d].p; break;
+    case GCSPH_F_CDX: nvec = h->D; for (int d = 0; d < h->D; ++d) src[d] = h->cdx_o[d].p; break;
+    case GCSPH_F_SUMW: src[0] = h->sumW_o.p; break;
+    case GCSPH_F_SUMGW: nvec = h->D; for (int d = 0; d < h->D; ++d) src[d] = h->sumgW_o[d].p; break;
+    case GCSPH_F_BUF2: nvec = h->D; for (int d = 0; d < h->D; ++d) src[d] = h->buf2_o[d].p; break;
+    case GCSPH_F_PTYPE: src[0] = h->pt_u; bytes = sizeof(int32_t) * (size_t)h->N; break;
+    default: return fail(GCSPH_EINVAL, "unknown field %d", (int)field);
+  }
+  for (int d = 0; d < nvec; ++d)
+    GC_CUDA(cudaMemcpyAsync((char*)dst + (size_t)d * bytes, src[d], bytes, cudaMemcpyDeviceToDevice, st));
+  GC_CUDA(cudaStreamSynchronize(st));
+  return GCSPH_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,157 @@
+"""Particle set-ups: dam-break lattices, uniform random clouds, fixture loader.
+
+These stand in for the reference's CSV inputs (src/auxillary.jl:3-11 and
+test/input/*.csv) and for the parameter sets of its examples
+(README.md:107-123, examples/timesolve3d.jl:15-29).  Coordinates follow the
+reference's axis convention: component 2 is vertical (gravity acts on it,
+src/sphproblem.jl:10-17); in 3-D component 3 is the tank depth.
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+SEED = 20261203
+
+
+@dataclass
+class Case:
+    """One particle set-up plus the SPHProblem constructor arguments."""
+    x: np.ndarray            # (D, N) float64
+    rho: np.ndarray          # (N,) float64
+    ptype: np.ndarray        # (N,) int32
+    dx: float
+    h: float
+    H: float
+    dist: float
+    cellsize: tuple
+    rho0: float = 1000.0
+    m0: float = 0.0
+    dt: float = 1e-5
+    alpha: float = 0.01
+    c0: float = 0.0
+    gamma: int = 7
+    delta: float = 0.1
+    CFL: float = 0.2
+    g: float = 9.81
+    s: float = 0.0
+    extra: dict = field(default_factory=dict)   # mutable fields set after construction
+
+    @property
+    def D(self):
+        return int(self.x.shape[0])
+
+    @property
+    def N(self):
+        return int(self.x.shape[1])
+
+
+def _lattice(lo, hi, dx):
+    """Cell-centred lattice coordinates in [lo, hi)."""
+    n = int(round((hi - lo) / dx))
+    return lo + (np.arange(n) + 0.5) * dx
+
+
+def dam_break_2d(dx=0.02, fluid=(1.0, 2.0), tank=(4.0, 3.0), layers=3, layer_ptype=None, rho=1000.0,
+                 dist_factor=1.0) -> Case:
+    """2-D dam break: fluid column fluid[0] x fluid[1] at the left wall of a
+    tank[0] x tank[1] tank with `layers` lattice rows of fixed particles on the
+    floor and both walls.  layer_ptype[l] is the ptype of boundary row l
+    (0 = innermost); default all 0, the fixture convention is (1, 0, 0)."""
+    if layer_ptype is None:
+        layer_ptype = (0,) * layers
+    fx = _lattice(0.0, fluid[0], dx)
+    fy = _lattice(0.0, fluid[1], dx)
+    FX, FY = np.meshgrid(fx, fy, indexing="ij")
+    xs, ys, pts = [FX.ravel()], [FY.ravel()], [np.full(FX.size, 2, np.int32)]
+    for l in range(layers):
+        off = (l + 0.5) * dx
+        # floor row spans the walls' layers too
+        bx = np.arange(-(layers - 0.5) * dx, tank[0] + (layers - 0.5) * dx + 0.5 * dx, dx)
+        xs.append(bx); ys.append(np.full(bx.size, -off)); pts.append(np.full(bx.size, layer_ptype[l], np.int32))
+        wy = _lattice(0.0, tank[1], dx)
+        for wx in (-off, tank[0] + off):
+            xs.append(np.full(wy.size, wx)); ys.append(wy); pts.append(np.full(wy.size, layer_ptype[l], np.int32))
+    x = np.stack([np.concatenate(xs), np.concatenate(ys)]).astype(np.float64)
+    ptype = np.concatenate(pts).astype(np.int32)
+    h = 1.2 * math.sqrt(2) * dx
+    H = 2 * h
+    dist = dist_factor * H
+    rho0 = 1000.0
+    g = 9.81
+    return Case(x=np.ascontiguousarray(x), rho=np.full(x.shape[1], float(rho)), ptype=ptype, dx=dx, h=h, H=H,
+                dist=dist, cellsize=(dist, dist), rho0=rho0, m0=rho0 * dx * dx, dt=1e-5, alpha=0.01,
+                c0=math.sqrt(g * 2) * 20, gamma=7, delta=0.1, CFL=0.2, g=g)
+
+
+def dam_break_3d(dx=0.01, fluid=(1.0, 2.0, 0.5), tank=(4.0, 3.0, 1.0), layers=3, layer_ptype=None, rho=1000.0,
+                 dist_factor=1.0, full_physics=True) -> Case:
+    """3-D dam break (component 2 vertical): fluid block fluid = (length,
+    height, depth) in a tank of (length, height, depth) with `layers` lattice
+    layers on the floor and all four walls.  h = sqrt(3 dx^2)
+    (examples/timesolve3d.jl:16); full_physics sets ν=0.2, s=0.05, DPC
+    l₀=0.005 λ=0.005 pmax=36000, XSPH ε=0.5 (README.md:142-150)."""
+    if layer_ptype is None:
+        layer_ptype = (1,) + (0,) * (layers - 1)
+    fx, fy, fz = (_lattice(0.0, fluid[d], dx) for d in range(3))
+    F = np.meshgrid(fx, fy, fz, indexing="ij")
+    parts = [np.stack([f.ravel() for f in F])]
+    pts = [np.full(F[0].size, 2, np.int32)]
+    # boundary: all lattice sites of the enlarged box that are outside the tank
+    # interior (x<0 or x>L or z<0 or z>W) or below the floor, within `layers` rows
+    L, Ht, W = tank
+    bx = (np.arange(-layers, int(round(L / dx)) + layers) + 0.5) * dx
+    by = (np.arange(-layers, int(round(Ht / dx))) + 0.5) * dx
+    bz = (np.arange(-layers, int(round(W / dx)) + layers) + 0.5) * dx
+    BX, BY, BZ = np.meshgrid(bx, by, bz, indexing="ij")
+    # layer index = how many rows outside the interior (0 = innermost)
+    ox = np.maximum(np.maximum(-BX, BX - L), 0.0)
+    oy = np.maximum(-BY, 0.0)
+    oz = np.maximum(np.maximum(-BZ, BZ - W), 0.0)
+    depth = np.maximum(np.maximum(ox, oy), oz)
+    outside = depth > 0
+    lay = np.floor(depth / dx + 1e-9).astype(np.int64)
+    sel = outside & (lay < layers)
+    parts.append(np.stack([BX[sel], BY[sel], BZ[sel]]))
+    lp = np.asarray(layer_ptype, np.int32)
+    pts.append(lp[lay[sel]])
+    x = np.ascontiguousarray(np.concatenate(parts, axis=1).astype(np.float64))
+    ptype = np.concatenate(pts).astype(np.int32)
+    h = math.sqrt(3 * dx ** 2)
+    H = 2 * h
+    dist = dist_factor * H
+    rho0 = 1000.0
+    g = 9.81
+    c = Case(x=x, rho=np.full(x.shape[1], float(rho)), ptype=ptype, dx=dx, h=h, H=H, dist=dist,
+             cellsize=(dist, dist, dist), rho0=rho0, m0=rho0 * dx * dx * dx, dt=1e-5, alpha=0.01,
+             c0=math.sqrt(g * 2) * 20, gamma=7, delta=0.1, CFL=0.2, g=g)
+    if full_physics:
+        c.s = 0.05
+        c.extra = dict(nu=0.2, dpc_l0=0.005, dpc_lambda=0.005, dpc_pmax=36000.0, xsph_eps=0.5)
+    return c
+
+
+def uniform_points(N: int, D: int, seed: int = SEED) -> np.ndarray:
+    """N uniform points in [0,1)^D, (D, N) float64, numpy PCG64(seed)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    return np.ascontiguousarray(rng.random((D, N)))
+
+
+def load_fixture(path: str) -> Case:
+    """Load a compact .npz made from the reference's 2-D CSV fixtures
+    (tests/golden/make_golden.py) with the README demo's parameters
+    (README.md:107-123)."""
+    z = np.load(path)
+    x = np.ascontiguousarray(z["x"].astype(np.float64))
+    dx = float(z["dx"])
+    h = 1.2 * math.sqrt(2) * dx
+    H = 2 * h
+    rho0 = 1000.0
+    g = 9.81
+    return Case(x=x, rho=np.ascontiguousarray(z["rho"].astype(np.float64)),
+                ptype=np.ascontiguousarray(z["ptype"].astype(np.int32)), dx=dx, h=h, H=H, dist=H,
+                cellsize=(H, H), rho0=rho0, m0=rho0 * dx * dx, dt=1e-5, alpha=0.01, c0=math.sqrt(g * 2) * 20,
+                gamma=7, delta=0.1, CFL=0.2, g=g)
+

@@ -1,0 +1,234 @@
+/*
+ * gcsph.h -- C ABI of libgcsph.so, the GB300 (sm_103a) hot path of
+ * GPUCellListSPH.jl: cell-list binning, the half-stencil pair list, the SPH
+ * pair sums and the symplectic step with its CFL reduction.
+ *
+ * Every pointer named *_dev is a device pointer (a CuPtr from Julia, a
+ * torch.Tensor.data_ptr() from Python).  Vector fields are passed as an array
+ * of D device pointers held in HOST memory (Julia: Ref(ntuple of CuPtr)), the
+ * layout of the reference's NTuple{D, CuArray{T}}.  Particle indices in pair
+ * lists are 1-based Int32, (min, max) ordered, exactly as the reference's
+ * CuArray{Tuple{Int32,Int32}}.  All calls are synchronous at return (the
+ * reference wraps every launch in CUDA.@sync) and report errors by status code
+ * plus gcsph_last_error(); nothing traps or throws across the ABI.
+ *
+ * Citations (file:line) are to the reference package GPUCellListSPH.jl.
+ */
+#ifndef GCSPH_H
+#define GCSPH_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#pragma GCC visibility push(default)
+#endif
+
+#define GCSPH_OK 0
+#define GCSPH_EINVAL 1     /* bad argument (Julia: error("...")) */
+#define GCSPH_ECAPACITY 2  /* caller buffer too small; the needed count is returned */
+#define GCSPH_ECUDA 3      /* CUDA runtime error */
+#define GCSPH_ENOMEM 4     /* device allocation failed */
+#define GCSPH_ESTATE 5     /* call out of order (e.g. pairs requested before a build) */
+
+typedef struct gcl_handle gcl_handle;
+typedef struct sph_handle sph_handle;
+
+/* ---------------------------------------------------------------- library */
+const char* gcsph_last_error(void);
+int gcsph_version(void);
+/* number of kernels this library has launched so far (process-wide) */
+uint64_t gcsph_launch_count(void);
+
+/* CUDA-event timers per kernel family, recorded on the launching stream
+ * (BenchmarkTools / Profile stand-ins, examples/cellist.jl:23-27).  Off by
+ * default; names: stage1 stage2 dpc xsph cspm sort pairs state post dt. */
+int gcsph_timing_enable(int on);
+int gcsph_timing_reset(void);
+int gcsph_timing_count(void);
+const char* gcsph_timing_name(int32_t id);
+int gcsph_timing_get(int32_t id, int64_t* launches, double* total_ms);
+
+/* ---------------------------------------------------------------- cell list */
+
+/* GPUCellList(points, cellsize, dist; MIN, MAX) -- src/celllist.jl:22-88.
+ * Freezes the grid (MIN lowered by |(MIN+sqrt(eps))*sqrt(eps)|, CELL =
+ * ceil((MAX-MIN)/cs), cs raised to dist) and runs the first build.  x_dev are
+ * the D coordinate arrays (the struct's `points`), read on every update and
+ * written back by sph_step; they must outlive the handle.  stream may be NULL
+ * (legacy default stream). */
+int gcl_create(int32_t D, int64_t N, const double* const* x_dev, const double* cellsize, double dist,
+               const double* MIN_or_null, const double* MAX_or_null, void* stream, gcl_handle** out);
+void gcl_destroy(gcl_handle* h);
+
+/* c.cs, c.offset, c.grid -- src/celllist.jl:1-15 */
+int gcl_grid(const gcl_handle* h, double* cs, double* offset, int64_t* cell);
+
+/* update!(c) -- src/celllist.jl:95-134: re-bin every point into the frozen
+ * grid, then neib_search! (src/gpukernels_cls.jl:561-587).  *pairsn_out is the
+ * pair count (c.pairsn). */
+int gcl_update(gcl_handle* h, int64_t* pairsn_out);
+
+/* partialupdate!(c) -- src/celllist.jl:141-145: pair search with the cell
+ * membership of the last update and the current coordinates. */
+int gcl_partialupdate(gcl_handle* h, int64_t* pairsn_out);
+
+/* neighborlist(c) / neighborlistview(c) -- src/celllist.jl:152-163.  Writes
+ * the pair set of the last build as (min,max) 1-based pairs into pairs_dev
+ * (2*cap int32).  If the set holds more than cap pairs the first cap are
+ * written and GCSPH_ECAPACITY is returned with *pairsn_out = the full count
+ * (the reference counts past capacity too, src/gpukernels_cls.jl:333-338).
+ * fillzero != 0 zero-fills pairs [pairsn, cap) (src/celllist.jl:112,142). */
+int gcl_emit_pairs(gcl_handle* h, int32_t* pairs_dev, int64_t cap, int fillzero, int64_t* pairsn_out);
+
+/* c.cellpnum (Int32[CELL...], column-major) -- src/gpukernels_cls.jl:29-60 */
+int gcl_cellpnum(gcl_handle* h, int32_t* cellpnum_dev);
+
+/* мaxpairs(c.cellpnum) -- src/gpukernels_cls.jl:109-286 */
+int gcl_maxpairs(gcl_handle* h, int64_t* out);
+
+/* ---------------------------------------------------------------- SPH problem */
+
+/* Mutable SPHProblem scalars, src/sphproblem.jl:62-112 (defaults :172-191). */
+typedef struct {
+  double dx, h, H, rho0, m0, dt, alpha, nu, g, c0, s, delta, CFL, nui, etime;
+  double dpc_l0, dpc_pmin, dpc_pmax, dpc_lambda, xsph_eps, bound_D, bound_l;
+  int32_t gamma, cspmn;
+} gcsph_params;
+
+/* Fields for sph_get_field (src/sphproblem.jl:348-390 getters and the
+ * struct's work arrays), always in original particle order. */
+enum {
+  GCSPH_F_X = 0,      /* get_points        D x N */
+  GCSPH_F_RHO = 1,    /* get_density       N */
+  GCSPH_F_V = 2,      /* get_velocity      D x N */
+  GCSPH_F_P = 3,      /* get_pressure      N */
+  GCSPH_F_A = 4,      /* get_acceleration  D x N (∑∂v∂t) */
+  GCSPH_F_DRHODT = 5, /* ∑∂ρ∂t             N */
+  GCSPH_F_RHOH = 6,   /* ρΔt½              N */
+  GCSPH_F_VH = 7,     /* vΔt½              D x N */
+  GCSPH_F_XH = 8,     /* xΔt½              D x N */
+  GCSPH_F_CDX = 9,    /* cΔx               D x N */
+  GCSPH_F_SUMW = 10,  /* get_sumw          N */
+  GCSPH_F_SUMGW = 11, /* get_sumgradw      D x N */
+  GCSPH_F_BUF2 = 12,  /* buf2 (DPC / XSPH / CSPM sums) D x N */
+  GCSPH_F_PTYPE = 13  /* get_ptype         N (int32) */
+};
+
+/* SPHProblem(system, dx, h, H, kernel, ρ, ptype, ρ₀, m₀, Δt, α, c₀, γ, δᵩ,
+ * CFL; v, g, s) -- src/sphproblem.jl:113-192, WendlandC2 kernel of dimension
+ * D.  rho_dev, v_dev (D arrays, or NULL for zeros) and ptype_dev are the
+ * caller's arrays; sph_step reads them at entry and writes ρ, v and the
+ * cell list's points back before it returns. */
+int sph_create(gcl_handle* cl, const gcsph_params* prm, double* rho_dev, double* const* v_dev,
+               const int32_t* ptype_dev, sph_handle** out);
+void sph_destroy(sph_handle* h);
+int sph_set_params(sph_handle* h, const gcsph_params* prm);
+int sph_get_params(const sph_handle* h, gcsph_params* prm);
+
+/* stepsolve!(prob, n; timestepping, timelims) -- src/sphproblem.jl:204-345.
+ * Returns (updaten, maxcΔxout) through the out pointers. */
+int sph_step(sph_handle* h, int32_t n, int timestepping, double tmin, double tmax, int64_t* updaten,
+             double* maxcdx);
+
+/* copy one field (enum above) into a caller device buffer */
+int sph_get_field(sph_handle* h, int32_t field, void* dst_dev);
+
+/* ---------------------------------------------------------------- pair kernels
+ * The reference's exported kernel functions, driven by a caller pair list
+ * (1-based (i,j), rows with i == 0 skipped) over caller device arrays, one
+ * thread per pair with FP64 atomics like the reference.  x/v/∇W/a/buf are
+ * arrays of D device pointers (host memory).  stream may be NULL. */
+
+/* sphW!(W, pairs, points, H⁻¹, kernel) -- src/gpukernels_sph.jl:75-100 */
+int gcsph_sphW(int32_t D, int64_t N, int64_t P, const int32_t* pairs_dev, const double* const* x_dev,
+               double Hinv, double* W_dev, void* stream);
+/* sph∇W!(∇W, pairs, points, H⁻¹, kernel) -- :186-213 */
+int gcsph_sphgradW(int32_t D, int64_t N, int64_t P, const int32_t* pairs_dev, const double* const* x_dev,
+                   double Hinv, double* const* gW_dev, void* stream);
+/* sph∑W!(∑W, pairs, points, kernel, H⁻¹, ptype) -- :129-156 (adds) */
+int gcsph_sphsumW(int32_t D, int64_t N, int64_t P, const int32_t* pairs_dev, const double* const* x_dev,
+                  double Hinv, const int32_t* ptype_dev, double* sumW_dev, void* stream);
+/* sph∑∇W!(∑∇W, pairs, points, kernel, H⁻¹, ptype) -- :322-359 (adds) */
+int gcsph_sphsumgradW(int32_t D, int64_t N, int64_t P, const int32_t* pairs_dev, const double* const* x_dev,
+                      double Hinv, const int32_t* ptype_dev, double* const* sumgW_dev, void* stream);
+/* ∂ρ∂tDDT!(∑∂ρ∂t, pairs, ∇W, ρ, v, points, h, m₀, ρ₀, c₀, γ, g, δᵩ, ptype) -- :542-631 (zeroes first) */
+int gcsph_drhodt_ddt(int32_t D, int64_t N, int64_t P, const int32_t* pairs_dev, const double* const* gW_dev,
+                     const double* rho_dev, const double* const* v_dev, const double* const* x_dev, double h,
+                     double m0, double rho0, double c0, int32_t gamma, double g, double delta,
+                     const int32_t* ptype_dev, double* drhodt_dev, void* stream);
+/* pressure!(P, ρ, c₀, γ, ρ₀, ptype) -- :710-727 */
+int gcsph_pressure(int64_t N, const double* rho_dev, double c0, int32_t gamma, double rho0,
+                   const int32_t* ptype_dev, double* P_dev, void* stream);
+/* ∂v∂t!(∑∂v∂t, ∇W, P, pairs, m₀, ρ, ptype) -- :740-776 (adds) */
+int gcsph_dvdt(int32_t D, int64_t N, int64_t P, const int32_t* pairs_dev, const double* const* gW_dev,
+               const double* P_dev, double m0, const double* rho_dev, const int32_t* ptype_dev,
+               double* const* a_dev, void* stream);
+/* ∂v∂t_av!(∑∂v∂t, ∇W, pairs, points, h, ρ, α, v, c₀, m₀, ptype) -- :852-901 (adds) */
+int gcsph_dvdt_av(int32_t D, int64_t N, int64_t P, const int32_t* pairs_dev, const double* const* gW_dev,
+                  const double* const* x_dev, double h, const double* rho_dev, double alpha,
+                  const double* const* v_dev, double c0, double m0, const int32_t* ptype_dev,
+                  double* const* a_dev, void* stream);
+/* ∂v∂t_visc!(∑∂v∂t, ∇W, v, ρ, points, pairs, h, m₀, 𝜈, ptype) -- :952-991 (adds) */
+int gcsph_dvdt_visc(int32_t D, int64_t N, int64_t P, const int32_t* pairs_dev, const double* const* gW_dev,
+                    const double* const* v_dev, const double* rho_dev, const double* const* x_dev, double h,
+                    double m0, double nu, const int32_t* ptype_dev, double* const* a_dev, void* stream);
+/* ∂v∂t_addgrav!(∑∂v∂t, gravvec(g, dim)) -- :1031-1051, src/sphproblem.jl:10-17 */
+int gcsph_addgrav(int32_t D, int64_t N, double g, double* const* a_dev, void* stream);
+/* fbmolforce!(∑∂v∂t, pairs, points, d, r₀, ptype) -- :1875-1913 (adds) */
+int gcsph_fbmolforce(int32_t D, int64_t N, int64_t P, const int32_t* pairs_dev, const double* const* x_dev,
+                     double d, double r0, const int32_t* ptype_dev, double* const* a_dev, void* stream);
+/* ∂v∂tpF!(∑∂v∂t, pairs, points, s, h, m₀, ptype) -- :1373-1409 (adds) */
+int gcsph_dvdt_pF(int32_t D, int64_t N, int64_t P, const int32_t* pairs_dev, const double* const* x_dev,
+                  double s, double h, double m0, const int32_t* ptype_dev, double* const* a_dev, void* stream);
+/* update_ρp∂ρ∂tΔt!(ρ, ∑∂ρ∂t, Δt, ρ₀, ptype) -- :1078-1096 */
+int gcsph_update_rho(int64_t N, double* rho_dev, const double* drhodt_dev, double dt, double rho0,
+                     const int32_t* ptype_dev, void* stream);
+/* update_vp∂v∂tΔt!(v, ∑∂v∂t, Δt, ptype) -- :1107-1127 */
+int gcsph_update_v(int32_t D, int64_t N, double* const* v_dev, const double* const* a_dev, double dt,
+                   const int32_t* ptype_dev, void* stream);
+/* update_xpvΔt!(x, v, Δt) -- :1150-1169 */
+int gcsph_update_x(int32_t D, int64_t N, double* const* x_dev, const double* const* v_dev, double dt,
+                   void* stream);
+/* symplectic_update!(ρ, ρΔt½, v, vΔt½, x, xΔt½, ∑∂ρ∂t, ∑∂v∂t, Δt, cΔx, ρ₀, ptype) -- :1193-1245 */
+int gcsph_symplectic(int32_t D, int64_t N, double* rho_dev, double* rhoh_dev, double* const* v_dev,
+                     double* const* vh_dev, double* const* x_dev, double* const* xh_dev,
+                     const double* drhodt_dev, const double* const* a_dev, double dt, double* const* cdx_dev,
+                     double rho0, const int32_t* ptype_dev, void* stream);
+/* dpcreg!(∑Δvdpc, v, ρ, P, pairs, points, kernel, l₀, Pmin, Pmax, Δt, λ, dpckernlim, ptype) -- :1485-1553 (zeroes first) */
+int gcsph_dpcreg(int32_t D, int64_t N, int64_t P, double* const* buf_dev, const double* const* v_dev,
+                 const double* rho_dev, const double* P_dev, const int32_t* pairs_dev, const double* const* x_dev,
+                 double l0, double Pmin, double Pmax, double dt, double lambda, double dpckernlim,
+                 const int32_t* ptype_dev, void* stream);
+/* update_dpcreg!(v, x, ∑Δvdpc, Δt, ptype) -- :1607-1632 */
+int gcsph_update_dpcreg(int32_t D, int64_t N, double* const* v_dev, double* const* x_dev,
+                        const double* const* buf_dev, double dt, const int32_t* ptype_dev, void* stream);
+/* xsphcorr!(∑Δvxsph, pairs, W, ρ, v, m₀, 𝜀, ptype) -- :1745-1779 (zeroes first) */
+int gcsph_xsphcorr(int32_t D, int64_t N, int64_t P, double* const* buf_dev, const int32_t* pairs_dev,
+                   const double* W_dev, const double* rho_dev, const double* const* v_dev, double m0, double eps,
+                   const int32_t* ptype_dev, void* stream);
+/* update_xsphcorr!(x, ∑Δvxsph, Δt, ptype) -- :1817-1838 */
+int gcsph_update_xsph(int32_t D, int64_t N, double* const* x_dev, const double* const* buf_dev, double dt,
+                      const int32_t* ptype_dev, void* stream);
+/* cspmcorr!(∑ρcspm, W, ρ, m₀, pairs, ptype) -- :1673-1719 (zeroes buf first; updates ρ) */
+int gcsph_cspmcorr(int32_t D, int64_t N, int64_t P, double* const* buf_dev, const double* W_dev,
+                   double* rho_dev, double m0, const int32_t* pairs_dev, const int32_t* ptype_dev, void* stream);
+/* Δt_stepping(buf, a, v, points, c₀, h, CFL, timelims) -- :1293-1353; *dt_out is the new Δt */
+int gcsph_dt_stepping(int32_t D, int64_t N, const double* const* a_dev, const double* const* v_dev,
+                      const double* const* x_dev, double c0, double h, double CFL, double tmin, double tmax,
+                      double* dt_out, void* stream);
+/* dpckernlim = find_zero(x -> 1 - 𝒲(k, x, 1), 0.5) -- src/sphproblem.jl:218 (host scalar) */
+double gcsph_dpckernlim(int32_t D);
+
+#if defined(__GNUC__)
+#pragma GCC visibility pop
+#endif
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GCSPH_H */

@@ -1,0 +1,1146 @@
+/*
+ * gcsph_oracle.c -- CPU restatement of GPUCellListSPH.jl's per-step hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This file is the parity oracle: the tests, the
+ * smoke check and bench.py's CPU-baseline leg call it as the checker.  The
+ * product (libgcsph.so) never links it and never falls back to it.
+ *
+ * Parity status: UNPINNED against the reference's own outputs.  The reference
+ * is Julia + CUDA.jl and GPU-only; it cannot run in this environment and its
+ * test suite holds no expected values (test/runtests.jl:6-18 makes no
+ * assertion).  What IS pinned: the pair set, by an independent O(N^2) brute
+ * force over the same clamped cells (orc_pairs_bruteforce) and by the
+ * reference's own count identity (README.md:51,58).  Every other function
+ * restates the reference expression by expression (Julia evaluates left to
+ * right; `2h` binds tighter than `/`; `x^2` is x*x; no FMA contraction: build
+ * with -ffp-contract=off).  Where the reference calls third-party arithmetic
+ * whose source is not vendored (SPHKernels.jl 2.2 WendlandC2; CUDA.jl's
+ * lowering of Float64^Int) the published formula is restated and the
+ * evaluation order chosen here is documented at the function.
+ *
+ * Conventions: coordinates and vector fields are SoA, component d of particle
+ * i at a[d*N + i].  Pair lists are int32 (i, j) interleaved, 1-based, i < j,
+ * exactly the layout of Julia's CuArray{Tuple{Int32,Int32}}.  A pair whose
+ * first index is 0 is skipped, as every reference pair kernel does.
+ *
+ * nthreads > 1 runs the pair loops with OpenMP over thread-private
+ * accumulators that are reduced in thread order (deterministic for a fixed
+ * thread count); nthreads == 1 is the serial, pair-order oracle.
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+#include <float.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#define ORC_API __attribute__((visibility("default")))
+/* Float64(pi), the value Julia uses for the Irrational pi */
+#define PI64 3.141592653589793
+
+static int g_threads = 1;
+ORC_API void orc_set_threads(int n) { g_threads = n < 1 ? 1 : n; }
+ORC_API int orc_get_threads(void) { return g_threads; }
+ORC_API int orc_max_threads(void) {
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}
+
+/* ------------------------------------------------------------------------ */
+/* Small vector helpers (StaticArrays semantics, left-to-right)              */
+/* ------------------------------------------------------------------------ */
+static inline double dotv(int D, const double *a, const double *b) {
+    /* LinearAlgebra.dot on SVector: ((a1*b1) + a2*b2) + a3*b3 */
+    double s = a[0] * b[0];
+    for (int d = 1; d < D; ++d) s = s + a[d] * b[d];
+    return s;
+}
+static inline void getv(int D, const double *arr, int64_t N, int64_t i, double *out) {
+    for (int d = 0; d < D; ++d) out[d] = arr[(int64_t)d * N + i];
+}
+
+/* ------------------------------------------------------------------------ */
+/* WendlandC2 (SPHKernels.jl 2.2, not vendored; call sites                   */
+/* src/gpukernels_sph.jl:95,150,207,343,1490,1519).  Published formula       */
+/* (Wendland 1995, normalisation of Dehnen & Aly 2012):                      */
+/*   W(u)   = sigma_D Hinv^D     (1-u)^4 (1+4u),  u < 1, else 0              */
+/*   dW(u)  = sigma_D Hinv^(D+1) (-20 u (1-u)^3), u < 1, else 0              */
+/* sigma_2 = 7/pi, sigma_3 = 21/(2 pi).  Evaluation order chosen here (and   */
+/* used identically by the CUDA kernels): n = sigma*Hinv^D as repeated        */
+/* products; t=1-u; t4=(t*t)*(t*t); W = ((1+4u)*t4)*n; dW = ((-20u)*t3)*n.    */
+/* ------------------------------------------------------------------------ */
+static inline double wc2_sigma(int D) { return D == 2 ? 7.0 / PI64 : 21.0 / (2.0 * PI64); }
+static inline double ipow_small(double x, int n) {
+    /* x^n by left-to-right repeated products (n >= 1) */
+    double r = x;
+    for (int k = 1; k < n; ++k) r = r * x;
+    return r;
+}
+ORC_API double orc_wendland_w(int D, double u, double Hinv) {
+    if (!(u < 1.0)) return 0.0;
+    double n = wc2_sigma(D) * ipow_small(Hinv, D);
+    double t = 1.0 - u;
+    double t2 = t * t;
+    double t4 = t2 * t2;
+    return ((1.0 + 4.0 * u) * t4) * n;
+}
+ORC_API double orc_wendland_dw(int D, double u, double Hinv) {
+    if (!(u < 1.0)) return 0.0;
+    double n = wc2_sigma(D) * ipow_small(Hinv, D + 1);
+    double t = 1.0 - u;
+    double t3 = (t * t) * t;
+    return ((-20.0 * u) * t3) * n;
+}
+
+/* powfancy7th, src/gpukernels_sph.jl:499-515.  Bit-trick initial guess     */
+/* (public Julia Discourse thread cited there) + 2 Newton steps for          */
+/* t^3 - x/t^4 = 0.  The reference runs the Newton loop under @fastmath;    */
+/* here every operation is IEEE round-to-nearest in source order.           */
+ORC_API double orc_powfancy7th(double x, double ginv, int32_t gamma) {
+    if (gamma == 7) {
+        double ax = fabs(x);
+        uint64_t bits;
+        memcpy(&bits, &ax, 8);
+        bits = 0x36cd000000000000ULL + bits / 7ULL;
+        double t;
+        memcpy(&t, &bits, 8);
+        t = copysign(t, x);
+        for (int it = 0; it < 2; ++it) {
+            double t2 = t * t;
+            double t3 = t2 * t;
+            double t4 = t2 * t2;
+            double xot4 = x / t4;
+            t = t - (t * (t3 - xot4)) / (4.0 * t3 + 3.0 * xot4);
+        }
+        return t;
+    }
+    return pow(x, ginv);
+}
+
+/* Float64 ^ Int as used by the Tait EOS (src/gpukernels_sph.jl:696).  The   */
+/* reference's device lowering lives in CUDA.jl (not vendored); here: gamma  */
+/* == 7 as x2=x*x, x4=x2*x2, x6=x4*x2, x7=x6*x, other gamma by left-to-right */
+/* products.  Identical sequence in the CUDA kernels.                        */
+ORC_API double orc_ipow(double x, int32_t n) {
+    if (n == 7) {
+        double x2 = x * x, x4 = x2 * x2, x6 = x4 * x2;
+        return x6 * x;
+    }
+    if (n == 0) return 1.0;
+    if (n < 0) return 1.0 / ipow_small(x, -n);
+    return ipow_small(x, n);
+}
+
+/* pressure(), src/gpukernels_sph.jl:691-697 */
+static inline double eos(double rho, int32_t gamma, double rho0, double P0, int32_t pt) {
+    if (pt <= 1 && rho < rho0) return 0.0;
+    return P0 * (orc_ipow(rho / rho0, gamma) - 1.0);
+}
+
+/* dpckernlim = find_zero(x -> 1 - W(k, x, 1.0), 0.5), src/sphproblem.jl:218 */
+/* (Roots.jl, unpinned).  Restated as bisection on [0,1] down to adjacent    */
+/* doubles, returning the endpoint with the smaller |f|.                      */
+ORC_API double orc_dpckernlim(int D) {
+    double lo = 0.0, hi = 1.0;
+    double flo = 1.0 - orc_wendland_w(D, lo, 1.0);
+    for (int it = 0; it < 2000; ++it) {
+        double mid = lo + (hi - lo) * 0.5;
+        if (mid <= lo || mid >= hi) break;
+        double fm = 1.0 - orc_wendland_w(D, mid, 1.0);
+        if (fm == 0.0) return mid;
+        if ((fm < 0.0) == (flo < 0.0)) { lo = mid; flo = fm; } else { hi = mid; }
+    }
+    double fl = fabs(1.0 - orc_wendland_w(D, lo, 1.0));
+    double fh = fabs(1.0 - orc_wendland_w(D, hi, 1.0));
+    return fl <= fh ? lo : hi;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Cell list (src/celllist.jl, src/gpukernels_cls.jl)                         */
+/* ------------------------------------------------------------------------ */
+
+/* Grid set-up, src/celllist.jl:27-46.  cs[i] raised to dist (:32-39),      */
+/* MIN = min - |(min + sqrt(eps))*sqrt(eps)| (:41-42), MAX = max (:43),       */
+/* CELL = ceil(Int, (MAX-MIN)/cs) (:46).  Returns 0, or 1 on a bad grid.     */
+ORC_API int orc_grid(int D, int64_t N, const double *x, const double *cellsize, double dist,
+                     const double *MINin, const double *MAXin, double *cs, double *offset,
+                     int64_t *cell) {
+    const double seps = 1.4901161193847656e-08; /* sqrt(eps(Float64)) == 2^-26 */
+    for (int d = 0; d < D; ++d) {
+        cs[d] = cellsize[d] < dist ? dist : cellsize[d];
+        double mn, mx;
+        if (MINin) mn = MINin[d];
+        else {
+            mn = x[(int64_t)d * N];
+            for (int64_t i = 1; i < N; ++i) { double v = x[(int64_t)d * N + i]; if (v < mn) mn = v; }
+        }
+        if (MAXin) mx = MAXin[d];
+        else {
+            mx = x[(int64_t)d * N];
+            for (int64_t i = 1; i < N; ++i) { double v = x[(int64_t)d * N + i]; if (v > mx) mx = v; }
+        }
+        mn = mn - fabs((mn + seps) * seps);
+        offset[d] = mn;
+        double c = ceil((mx - mn) / cs[d]);
+        if (!(c >= 1.0) || c > 2.0e9) return 1;
+        cell[d] = (int64_t)c;
+    }
+    return 0;
+}
+
+/* kernel_cellmap!, src/gpukernels_cls.jl:29-60: p = (x - offset) * (1/cs)   */
+/* (1/cs on the host, :21), cell = ceil(Int32, min(max(p, 1), CELL)).        */
+/* pcell is 1-based, D*N SoA; cellpnum is column-major over CELL.            */
+ORC_API void orc_cellmap(int D, int64_t N, const double *x, const double *cs, const double *offset,
+                         const int64_t *cell, int32_t *pcell, int32_t *cellpnum) {
+    double hinv[3];
+    int64_t ncell = 1;
+    for (int d = 0; d < D; ++d) { hinv[d] = 1.0 / cs[d]; ncell *= cell[d]; }
+    if (cellpnum) memset(cellpnum, 0, sizeof(int32_t) * (size_t)ncell);
+    for (int64_t i = 0; i < N; ++i) {
+        int64_t lin = 0, stride = 1;
+        for (int d = 0; d < D; ++d) {
+            double p = (x[(int64_t)d * N + i] - offset[d]) * hinv[d];
+            double c = fmin(fmax(p, 1.0), (double)cell[d]);
+            int32_t ci = (int32_t)ceil(c);
+            pcell[(int64_t)d * N + i] = ci;
+            lin += (int64_t)(ci - 1) * stride;
+            stride *= cell[d];
+        }
+        if (cellpnum) cellpnum[lin] += 1;
+    }
+}
+
+/* мaxpairs, src/gpukernels_cls.jl:109-286: sum over non-empty cells of      */
+/* Int(n(n-1)*0.5) + n * (sum of the half-stencil neighbour counts).         */
+static const int OFF2M[4][2] = {{-1, 1}, {0, 1}, {1, 1}, {1, 0}};
+static const int OFF3M[13][3] = {{-1, 1, 0}, {0, 1, 0}, {1, 1, 0}, {1, 0, 0},
+                                 {-1, 1, 1}, {0, 1, 1}, {1, 1, 1}, {1, 0, 1}, {0, 0, 1},
+                                 {-1, 1, -1}, {0, 1, -1}, {1, 1, -1}, {1, 0, -1}};
+ORC_API int64_t orc_maxpairs(int D, const int32_t *cellpnum, const int64_t *cell) {
+    int64_t nx = cell[0], ny = cell[1], nz = D == 3 ? cell[2] : 1;
+    int64_t total = 0;
+    for (int64_t z = 0; z < nz; ++z)
+        for (int64_t y = 0; y < ny; ++y)
+            for (int64_t xx = 0; xx < nx; ++xx) {
+                int64_t n = cellpnum[xx + nx * (y + ny * z)];
+                if (n <= 0) continue;
+                int64_t m = 0;
+                int no = D == 2 ? 4 : 13;
+                for (int o = 0; o < no; ++o) {
+                    int64_t a = xx + (D == 2 ? OFF2M[o][0] : OFF3M[o][0]);
+                    int64_t b = y + (D == 2 ? OFF2M[o][1] : OFF3M[o][1]);
+                    int64_t c = z + (D == 2 ? 0 : OFF3M[o][2]);
+                    if (a >= 0 && a < nx && b >= 0 && b < ny && c >= 0 && c < nz)
+                        m += cellpnum[a + nx * (b + ny * c)];
+                }
+                total += (int64_t)((double)(n * (n - 1)) * 0.5) + m * n;
+            }
+    return total;
+}
+
+/* r^2 exactly as the reference writes it, src/gpukernels_cls.jl:326,390,   */
+/* 456,527: (xi-xj)^2 + (yi-yj)^2 [+ (zi-zj)^2], left to right, no FMA.     */
+static inline double r2_ref(int D, const double *x, int64_t N, int64_t i, int64_t j) {
+    double d0 = x[i] - x[j];
+    double d1 = x[N + i] - x[N + j];
+    double s = d0 * d0 + d1 * d1;
+    if (D == 3) { double d2 = x[2 * N + i] - x[2 * N + j]; s = s + d2 * d2; }
+    return s;
+}
+
+static inline void emit_pair(int32_t *pairs, int64_t cap, int64_t *cnt, int64_t a, int64_t b) {
+    int64_t k = *cnt;
+    if (k < cap) {
+        int32_t i = (int32_t)(a + 1), j = (int32_t)(b + 1);
+        pairs[2 * k] = i < j ? i : j;
+        pairs[2 * k + 1] = i < j ? j : i;
+    }
+    *cnt = k + 1;
+}
+
+/* neib_search!, src/gpukernels_cls.jl:561-587: neib_internal! (:293-416)   */
+/* over each cell's members (celllist order: fillcells_naive!, :67-101,      */
+/* filled here in particle order), then neib_external! (:423-554) for the    */
+/* half-stencil offsets (2D :564-567, 3D :572-586).  Pairs are (min,max)     */
+/* 1-based; the count is always returned, writes stop at cap (the reference  */
+/* drops whole flush chunks past capacity, :334; the SET is what matters).   */
+static const int OFF2S[4][2] = {{1, -1}, {0, 1}, {1, 1}, {1, 0}};
+static const int OFF3S[13][3] = {{1, -1, 0}, {0, 1, 0}, {1, 1, 0}, {1, 0, 0},
+                                 {1, -1, 1}, {0, 1, 1}, {1, 1, 1}, {1, 0, 1}, {0, 0, 1},
+                                 {1, -1, -1}, {0, 1, -1}, {1, 1, -1}, {1, 0, -1}};
+ORC_API int64_t orc_neib_search(int D, int64_t N, const double *x, const int32_t *pcell,
+                                const int64_t *cell, double dist, int32_t *pairs, int64_t cap) {
+    int64_t nx = cell[0], ny = cell[1], nz = D == 3 ? cell[2] : 1;
+    int64_t ncell = nx * ny * nz;
+    double dist2 = dist * dist;
+    /* cell membership lists (CSR) in particle order */
+    int64_t *start = (int64_t *)calloc((size_t)ncell + 1, sizeof(int64_t));
+    int64_t *memb = (int64_t *)malloc(sizeof(int64_t) * (size_t)(N > 0 ? N : 1));
+    int64_t *fillp = (int64_t *)malloc(sizeof(int64_t) * (size_t)ncell);
+    int64_t *lin = (int64_t *)malloc(sizeof(int64_t) * (size_t)(N > 0 ? N : 1));
+    for (int64_t i = 0; i < N; ++i) {
+        int64_t l = (pcell[i] - 1) + nx * ((pcell[N + i] - 1) + ny * (D == 3 ? (pcell[2 * N + i] - 1) : 0));
+        lin[i] = l;
+        start[l + 1] += 1;
+    }
+    for (int64_t c = 0; c < ncell; ++c) start[c + 1] += start[c];
+    for (int64_t c = 0; c < ncell; ++c) fillp[c] = start[c];
+    for (int64_t i = 0; i < N; ++i) memb[fillp[lin[i]]++] = i;
+    int64_t cnt = 0;
+    /* internal */
+    for (int64_t c = 0; c < ncell; ++c) {
+        int64_t s = start[c], e = start[c + 1];
+        if (e - s <= 1) continue;
+        for (int64_t a = s; a < e - 1; ++a)
+            for (int64_t b = a + 1; b < e; ++b) {
+                int64_t i = memb[a], j = memb[b];
+                if (r2_ref(D, x, N, i, j) < dist2) emit_pair(pairs, cap, &cnt, i, j);
+            }
+    }
+    /* external, one offset at a time like the reference's launches */
+    int no = D == 2 ? 4 : 13;
+    for (int o = 0; o < no; ++o) {
+        int ox = D == 2 ? OFF2S[o][0] : OFF3S[o][0];
+        int oy = D == 2 ? OFF2S[o][1] : OFF3S[o][1];
+        int oz = D == 2 ? 0 : OFF3S[o][2];
+        for (int64_t z = 0; z < nz; ++z)
+            for (int64_t y = 0; y < ny; ++y)
+                for (int64_t xx = 0; xx < nx; ++xx) {
+                    int64_t a = xx + ox, b = y + oy, cc = z + oz;
+                    if (a < 0 || a >= nx || b < 0 || b >= ny || cc < 0 || cc >= nz) continue;
+                    int64_t c = xx + nx * (y + ny * z), cn = a + nx * (b + ny * cc);
+                    if (start[c + 1] - start[c] <= 0) continue;
+                    for (int64_t p = start[c]; p < start[c + 1]; ++p)
+                        for (int64_t q = start[cn]; q < start[cn + 1]; ++q) {
+                            int64_t i = memb[p], j = memb[q];
+                            if (r2_ref(D, x, N, i, j) < dist2) emit_pair(pairs, cap, &cnt, i, j);
+                        }
+                }
+    }
+    free(start); free(memb); free(fillp); free(lin);
+    return cnt;
+}
+
+/* Independent check of the pair SET: all i<j whose clamped cells are within */
+/* Chebyshev distance 1 and whose reference-order r^2 < dist^2.  O(N^2).     */
+ORC_API int64_t orc_pairs_bruteforce(int D, int64_t N, const double *x, const int32_t *pcell,
+                                     double dist, int32_t *pairs, int64_t cap) {
+    double dist2 = dist * dist;
+    int64_t cnt = 0;
+    for (int64_t i = 0; i < N; ++i)
+        for (int64_t j = i + 1; j < N; ++j) {
+            int near = 1;
+            for (int d = 0; d < D; ++d) {
+                int32_t dc = pcell[(int64_t)d * N + i] - pcell[(int64_t)d * N + j];
+                if (dc > 1 || dc < -1) { near = 0; break; }
+            }
+            if (near && r2_ref(D, x, N, i, j) < dist2) emit_pair(pairs, cap, &cnt, i, j);
+        }
+    return cnt;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Thread-private accumulation for the pair loops                            */
+/* ------------------------------------------------------------------------ */
+/* Each pair kernel is written as a body over one pair index that adds into  */
+/* `nacc` arrays of length N.  Serial: the body adds straight into the       */
+/* outputs in pair order.  Threaded: each thread owns private zeroed copies  */
+/* for a static chunk of pairs; copies are then added in thread order.       */
+typedef void (*pair_body_fn)(int64_t p, double *const *acc, const void *ctx);
+
+static void run_pairs(int64_t P, int64_t N, int nacc, double *const *out, pair_body_fn body,
+                      const void *ctx) {
+    int T = g_threads;
+    if (T <= 1 || P < 4096) {
+        for (int64_t p = 0; p < P; ++p) body(p, out, ctx);
+        return;
+    }
+#ifdef _OPENMP
+    double *priv = (double *)calloc((size_t)T * (size_t)nacc * (size_t)N, sizeof(double));
+#pragma omp parallel num_threads(T)
+    {
+        int t = omp_get_thread_num();
+        int nt = omp_get_num_threads();
+        double *mine[8];
+        for (int a = 0; a < nacc; ++a) mine[a] = priv + ((size_t)t * nacc + a) * (size_t)N;
+        int64_t lo = P * t / nt, hi = P * (t + 1) / nt;
+        for (int64_t p = lo; p < hi; ++p) body(p, mine, ctx);
+#pragma omp barrier
+        /* reduce: each thread owns a slice of particles; threads added in order */
+        int64_t ilo = N * t / nt, ihi = N * (t + 1) / nt;
+        for (int a = 0; a < nacc; ++a)
+            for (int64_t i = ilo; i < ihi; ++i) {
+                double s = out[a][i];
+                for (int u = 0; u < nt; ++u) s += priv[((size_t)u * nacc + a) * (size_t)N + i];
+                out[a][i] = s;
+            }
+    }
+    free(priv);
+#else
+    for (int64_t p = 0; p < P; ++p) body(p, out, ctx);
+#endif
+}
+
+/* Per-particle loops */
+#ifdef _OPENMP
+#define PFOR _Pragma("omp parallel for schedule(static) num_threads(g_threads) if(g_threads > 1)")
+#else
+#define PFOR
+#endif
+
+/* ------------------------------------------------------------------------ */
+/* Pair kernels (src/gpukernels_sph.jl), scatter form over the pair list     */
+/* ------------------------------------------------------------------------ */
+typedef struct {
+    int D; int64_t N; const int32_t *pairs; const double *x; double Hinv;
+    double *W; double *gW; int64_t P; const int32_t *ptype;
+} ctx_w;
+
+/* kernel_sphW!, :84-100: W[p] = W(norm(dx)*Hinv, Hinv) */
+static void body_sphW(int64_t p, double *const *acc, const void *vc) {
+    (void)acc;
+    const ctx_w *c = (const ctx_w *)vc;
+    int32_t pi = c->pairs[2 * p], pj = c->pairs[2 * p + 1];
+    if (pi == 0) return;
+    int64_t i = pi - 1, j = pj - 1;
+    double dx[3];
+    for (int d = 0; d < c->D; ++d) dx[d] = c->x[(int64_t)d * c->N + i] - c->x[(int64_t)d * c->N + j];
+    double r = sqrt(dotv(c->D, dx, dx));
+    double u = r * c->Hinv;
+    c->W[p] = orc_wendland_w(c->D, u, c->Hinv);
+}
+ORC_API void orc_sphW(int D, int64_t N, int64_t P, const int32_t *pairs, const double *x, double Hinv, double *W) {
+    ctx_w c = {D, N, pairs, x, Hinv, W, NULL, P, NULL};
+    for (int64_t p = 0; p < P; ++p) body_sphW(p, NULL, &c);
+}
+
+/* kernel_sph∇W!, :196-213: ∇W[p] = dx * (dW(u)/r); SoA ∇W[d*P + p] */
+static void body_sphgW(int64_t p, double *const *acc, const void *vc) {
+    (void)acc;
+    const ctx_w *c = (const ctx_w *)vc;
+    int32_t pi = c->pairs[2 * p], pj = c->pairs[2 * p + 1];
+    if (pi == 0) return;
+    int64_t i = pi - 1, j = pj - 1;
+    double dx[3];
+    for (int d = 0; d < c->D; ++d) dx[d] = c->x[(int64_t)d * c->N + i] - c->x[(int64_t)d * c->N + j];
+    double r = sqrt(dotv(c->D, dx, dx));
+    double u = r * c->Hinv;
+    double dwk_r = orc_wendland_dw(c->D, u, c->Hinv) / r;
+    for (int d = 0; d < c->D; ++d) c->gW[(int64_t)d * c->P + p] = dx[d] * dwk_r;
+}
+ORC_API void orc_sphgradW(int D, int64_t N, int64_t P, const int32_t *pairs, const double *x, double Hinv, double *gW) {
+    ctx_w c = {D, N, pairs, x, Hinv, NULL, gW, P, NULL};
+    for (int64_t p = 0; p < P; ++p) body_sphgW(p, NULL, &c);
+}
+
+/* kernel_sph∑W!, :139-156 (mask !((pt_i>0) xor (pt_j>0))) */
+static void body_sumW(int64_t p, double *const *acc, const void *vc) {
+    const ctx_w *c = (const ctx_w *)vc;
+    int32_t pi = c->pairs[2 * p], pj = c->pairs[2 * p + 1];
+    if (pi == 0) return;
+    int64_t i = pi - 1, j = pj - 1;
+    if ((c->ptype[i] > 0) != (c->ptype[j] > 0)) return;
+    double dx[3];
+    for (int d = 0; d < c->D; ++d) dx[d] = c->x[(int64_t)d * c->N + i] - c->x[(int64_t)d * c->N + j];
+    double r = sqrt(dotv(c->D, dx, dx));
+    double w = orc_wendland_w(c->D, r * c->Hinv, c->Hinv);
+    acc[0][i] += w;
+    acc[0][j] += w;
+}
+ORC_API void orc_sphsumW(int D, int64_t N, int64_t P, const int32_t *pairs, const double *x, double Hinv,
+                         const int32_t *ptype, double *sumW) {
+    ctx_w c = {D, N, pairs, x, Hinv, NULL, NULL, P, ptype};
+    double *out[1] = {sumW};
+    run_pairs(P, N, 1, out, body_sumW, &c);
+}
+
+/* kernel_sph∑∇W!, :332-359: ∑∇W_i += ∇w, ∑∇W_j -= ∇w (same mask) */
+static void body_sumgW(int64_t p, double *const *acc, const void *vc) {
+    const ctx_w *c = (const ctx_w *)vc;
+    int32_t pi = c->pairs[2 * p], pj = c->pairs[2 * p + 1];
+    if (pi == 0) return;
+    int64_t i = pi - 1, j = pj - 1;
+    if ((c->ptype[i] > 0) != (c->ptype[j] > 0)) return;
+    double dx[3];
+    for (int d = 0; d < c->D; ++d) dx[d] = c->x[(int64_t)d * c->N + i] - c->x[(int64_t)d * c->N + j];
+    double r = sqrt(dotv(c->D, dx, dx));
+    double dwk_r = orc_wendland_dw(c->D, r * c->Hinv, c->Hinv) / r;
+    for (int d = 0; d < c->D; ++d) {
+        double g = dx[d] * dwk_r;
+        acc[d][i] += g;
+        acc[d][j] -= g;
+    }
+}
+ORC_API void orc_sphsumgradW(int D, int64_t N, int64_t P, const int32_t *pairs, const double *x, double Hinv,
+                             const int32_t *ptype, double *sumgW) {
+    ctx_w c = {D, N, pairs, x, Hinv, NULL, NULL, P, ptype};
+    double *out[3] = {sumgW, sumgW + N, sumgW + 2 * N};
+    run_pairs(P, N, D, out, body_sumgW, &c);
+}
+
+/* ∂ρ∂tDDT!, :542-631 */
+typedef struct {
+    int D; int64_t N, P; const int32_t *pairs; const double *gW; const double *rho; const double *v;
+    const double *x; double eta2, m0, rho0, ginv, DDTkh, DDTgz; int32_t gamma; const int32_t *ptype;
+} ctx_ddt;
+static void body_ddt(int64_t p, double *const *acc, const void *vc) {
+    const ctx_ddt *c = (const ctx_ddt *)vc;
+    int32_t pi = c->pairs[2 * p], pj = c->pairs[2 * p + 1];
+    if (!(pi > 0)) return;
+    int64_t i = pi - 1, j = pj - 1;
+    if (!(c->ptype[i] > 0 && c->ptype[j] > 0)) return;
+    int D = c->D; int64_t N = c->N;
+    double dx[3], dv[3], gw[3];
+    for (int d = 0; d < D; ++d) {
+        dx[d] = c->x[(int64_t)d * N + i] - c->x[(int64_t)d * N + j];
+        dv[d] = c->v[(int64_t)d * N + i] - c->v[(int64_t)d * N + j];
+        gw[d] = c->gW[(int64_t)d * c->P + p];
+    }
+    double r2 = dotv(D, dx, dx);
+    double rhoi = c->rho[i], rhoj = c->rho[j];
+    double dot3 = -dotv(D, dx, gw);
+    double m0dot = c->m0 * dotv(D, dv, gw);
+    double si = m0dot, sj = m0dot;
+    if (c->ptype[i] > 1) {
+        double drhopvp = c->rho0 * orc_powfancy7th(1.0 + c->DDTgz * dx[1], c->ginv, c->gamma) - c->rho0;
+        double visc_densi = c->DDTkh * ((rhoj - rhoi) - drhopvp) / (r2 + c->eta2);
+        double delta_i = visc_densi * dot3 * c->m0 / rhoj;
+        si += delta_i;
+    }
+    acc[0][i] += si;
+    if (c->ptype[j] > 1) {
+        double drhopvn = c->rho0 * orc_powfancy7th(1.0 - c->DDTgz * dx[1], c->ginv, c->gamma) - c->rho0;
+        double visc_densi = c->DDTkh * ((rhoi - rhoj) - drhopvn) / (r2 + c->eta2);
+        double delta_j = visc_densi * dot3 * c->m0 / rhoi;
+        sj += delta_j;
+    }
+    acc[0][j] += sj;
+}
+/* Host constants of ∂ρ∂tDDT! (:556-560); zeroes the output first (:555). */
+ORC_API void orc_drhodt_ddt(int D, int64_t N, int64_t P, const int32_t *pairs, const double *gW,
+                            const double *rho, const double *v, const double *x, double h, double m0,
+                            double rho0, double c0, int32_t gamma, double g, double delta,
+                            const int32_t *ptype, double *drhodt) {
+    memset(drhodt, 0, sizeof(double) * (size_t)N);
+    double eta2 = (0.1 * h) * (0.1 * h);
+    double ginv = 1.0 / (double)gamma;
+    double DDTkh = 2.0 * h * delta * c0;
+    double Cb = (c0 * c0 * rho0) * ginv;
+    double DDTgz = rho0 * g / Cb;
+    ctx_ddt c = {D, N, P, pairs, gW, rho, v, x, eta2, m0, rho0, ginv, DDTkh, DDTgz, gamma, ptype};
+    double *out[1] = {drhodt};
+    run_pairs(P, N, 1, out, body_ddt, &c);
+}
+
+/* pressure!, :710-727: P0 = c0^2*rho0/gamma on the host (:712) */
+ORC_API void orc_pressure(int64_t N, const double *rho, double c0, int32_t gamma, double rho0,
+                          const int32_t *ptype, double *P) {
+    double P0 = c0 * c0 * rho0 / (double)gamma;
+    PFOR
+    for (int64_t i = 0; i < N; ++i) P[i] = eos(rho[i], gamma, rho0, P0, ptype[i]);
+}
+
+/* ∂v∂t!, :740-776: mask ptype_i*ptype_j > 0; f = -m0*Pfac*∇W */
+typedef struct {
+    int D; int64_t N, P; const int32_t *pairs; const double *gW; const double *Pr; const double *rho;
+    const double *v; const double *x; double h, eta2, alpha, c0, m0, nu; const int32_t *ptype;
+} ctx_mom;
+static void body_dvdt(int64_t p, double *const *acc, const void *vc) {
+    const ctx_mom *c = (const ctx_mom *)vc;
+    int32_t pi = c->pairs[2 * p], pj = c->pairs[2 * p + 1];
+    if (pi == 0) return;
+    int64_t i = pi - 1, j = pj - 1;
+    if (!(c->ptype[i] * c->ptype[j] > 0)) return;
+    double Pfac = (c->Pr[i] + c->Pr[j]) / (c->rho[i] * c->rho[j]);
+    double s = -c->m0 * Pfac;
+    for (int d = 0; d < c->D; ++d) {
+        double f = s * c->gW[(int64_t)d * c->P + p];
+        acc[d][i] += f;
+        acc[d][j] -= f;
+    }
+}
+ORC_API void orc_dvdt(int D, int64_t N, int64_t P, const int32_t *pairs, const double *gW, const double *Pr,
+                      double m0, const double *rho, const int32_t *ptype, double *a) {
+    ctx_mom c = {D, N, P, pairs, gW, Pr, rho, NULL, NULL, 0, 0, 0, 0, m0, 0, ptype};
+    double *out[3] = {a, a + N, a + 2 * N};
+    run_pairs(P, N, D, out, body_dvdt, &c);
+}
+
+/* ∂v∂t_av!, :852-901 (Monaghan artificial viscosity) */
+static void body_av(int64_t p, double *const *acc, const void *vc) {
+    const ctx_mom *c = (const ctx_mom *)vc;
+    int32_t pi = c->pairs[2 * p], pj = c->pairs[2 * p + 1];
+    if (pi == 0) return;
+    int64_t i = pi - 1, j = pj - 1;
+    if (!(c->ptype[i] > 0 && c->ptype[j] > 0)) return;
+    int D = c->D; int64_t N = c->N;
+    double dx[3], dv[3];
+    for (int d = 0; d < D; ++d) {
+        dx[d] = c->x[(int64_t)d * N + i] - c->x[(int64_t)d * N + j];
+        dv[d] = c->v[(int64_t)d * N + i] - c->v[(int64_t)d * N + j];
+    }
+    double r2 = dotv(D, dx, dx);
+    double rhom = (c->rho[i] + c->rho[j]) * 0.5;
+    double cond = dotv(D, dv, dx);
+    if (cond < 0.0) {
+        double dmu = c->h * cond / (r2 + c->eta2);
+        double dPi = (-c->alpha * c->c0 * dmu) / rhom;
+        double s = -dPi * c->m0;
+        for (int d = 0; d < D; ++d) {
+            double f = s * c->gW[(int64_t)d * c->P + p];
+            acc[d][i] += f;
+            acc[d][j] -= f;
+        }
+    }
+}
+ORC_API void orc_dvdt_av(int D, int64_t N, int64_t P, const int32_t *pairs, const double *gW, const double *x,
+                         double h, const double *rho, double alpha, const double *v, double c0, double m0,
+                         const int32_t *ptype, double *a) {
+    double eta2 = (0.1 * h) * (0.1 * h);
+    ctx_mom c = {D, N, P, pairs, gW, NULL, rho, v, x, h, eta2, alpha, c0, m0, 0, ptype};
+    double *out[3] = {a, a + N, a + 2 * N};
+    run_pairs(P, N, D, out, body_av, &c);
+}
+
+/* ∂v∂t_visc!, :952-991 (laminar viscosity) */
+static void body_visc(int64_t p, double *const *acc, const void *vc) {
+    const ctx_mom *c = (const ctx_mom *)vc;
+    int32_t pi = c->pairs[2 * p], pj = c->pairs[2 * p + 1];
+    if (pi == 0) return;
+    int64_t i = pi - 1, j = pj - 1;
+    if (!(c->ptype[i] > 0 && c->ptype[j] > 0)) return;
+    int D = c->D; int64_t N = c->N;
+    double dx[3], dv[3], gw[3];
+    for (int d = 0; d < D; ++d) {
+        dx[d] = c->x[(int64_t)d * N + i] - c->x[(int64_t)d * N + j];
+        dv[d] = c->v[(int64_t)d * N + i] - c->v[(int64_t)d * N + j];
+        gw[d] = c->gW[(int64_t)d * c->P + p];
+    }
+    double r2 = dotv(D, dx, dx);
+    double nuterm = 4.0 * c->nu * c->m0 * dotv(D, dx, gw) / ((c->rho[i] + c->rho[j]) * (r2 + c->eta2));
+    for (int d = 0; d < D; ++d) {
+        double f = nuterm * dv[d];
+        acc[d][i] += f;
+        acc[d][j] -= f;
+    }
+}
+ORC_API void orc_dvdt_visc(int D, int64_t N, int64_t P, const int32_t *pairs, const double *gW, const double *v,
+                           const double *rho, const double *x, double h, double m0, double nu,
+                           const int32_t *ptype, double *a) {
+    double eta2 = (0.1 * h) * (0.1 * h);
+    ctx_mom c = {D, N, P, pairs, gW, NULL, rho, v, x, h, eta2, 0, 0, m0, nu, ptype};
+    double *out[3] = {a, a + N, a + 2 * N};
+    run_pairs(P, N, D, out, body_visc, &c);
+}
+
+/* ∂v∂t_addgrav!, :1031-1051 with gravvec, src/sphproblem.jl:10-17 */
+ORC_API void orc_addgrav(int D, int64_t N, double g, double *a) {
+    PFOR
+    for (int64_t i = 0; i < N; ++i) {
+        a[i] -= 0.0;
+        a[N + i] -= g;
+        if (D == 3) a[2 * N + i] -= 0.0;
+    }
+}
+
+/* fbmolforce!, :1875-1913 (mask xor of ptype>0) */
+typedef struct {
+    int D; int64_t N; const int32_t *pairs; const double *x; double d, r0, eta2, s, h, m0;
+    const int32_t *ptype;
+} ctx_bf;
+static void body_fbmol(int64_t p, double *const *acc, const void *vc) {
+    const ctx_bf *c = (const ctx_bf *)vc;
+    int32_t pi = c->pairs[2 * p], pj = c->pairs[2 * p + 1];
+    if (pi == 0) return;
+    int64_t i = pi - 1, j = pj - 1;
+    if ((c->ptype[i] > 0) == (c->ptype[j] > 0)) return;
+    int D = c->D; int64_t N = c->N;
+    double dx[3];
+    for (int d = 0; d < D; ++d) dx[d] = c->x[(int64_t)d * N + i] - c->x[(int64_t)d * N + j];
+    double r2 = dotv(D, dx, dx);
+    double r = sqrt(r2);
+    if (r < c->r0) {
+        double q = c->r0 / (r + c->eta2);
+        double q2 = q * q, q4 = q2 * q2, q8 = q4 * q4, q12 = q8 * q4;
+        double Fc = c->d * (q12 - q4) / (r2 + c->eta2);
+        for (int d = 0; d < D; ++d) {
+            double f = dx[d] * Fc;
+            acc[d][i] += f;
+            acc[d][j] -= f;
+        }
+    }
+}
+ORC_API void orc_fbmolforce(int D, int64_t N, int64_t P, const int32_t *pairs, const double *x, double d,
+                            double r0, const int32_t *ptype, double *a) {
+    double eta2 = 0.01 * (r0 * r0);
+    ctx_bf c = {D, N, pairs, x, d, r0, eta2, 0, 0, 0, ptype};
+    double *out[3] = {a, a + N, a + 2 * N};
+    run_pairs(P, N, D, out, body_fbmol, &c);
+}
+
+/* ∂v∂tpF!, :1373-1409 (surface tension) */
+static void body_pF(int64_t p, double *const *acc, const void *vc) {
+    const ctx_bf *c = (const ctx_bf *)vc;
+    int32_t pi = c->pairs[2 * p], pj = c->pairs[2 * p + 1];
+    if (pi == 0) return;
+    int64_t i = pi - 1, j = pj - 1;
+    if (!(c->ptype[i] > 0 && c->ptype[j] > 0)) return;
+    int D = c->D; int64_t N = c->N;
+    double dx[3];
+    for (int d = 0; d < D; ++d) dx[d] = c->x[(int64_t)d * N + i] - c->x[(int64_t)d * N + j];
+    double r = sqrt(dotv(D, dx, dx));
+    if (r < 2.0 * c->h) {
+        double scos = c->s * cos((1.5 * PI64) * r / (2.0 * c->h)) / (r + 0.1 * c->h);
+        for (int d = 0; d < D; ++d) {
+            double f = scos * dx[d] / c->m0;
+            acc[d][i] += f;
+            acc[d][j] -= f;
+        }
+    }
+}
+ORC_API void orc_dvdt_pF(int D, int64_t N, int64_t P, const int32_t *pairs, const double *x, double s,
+                         double h, double m0, const int32_t *ptype, double *a) {
+    ctx_bf c = {D, N, pairs, x, 0, 0, 0, s, h, m0, ptype};
+    double *out[3] = {a, a + N, a + 2 * N};
+    run_pairs(P, N, D, out, body_pF, &c);
+}
+
+/* update_ρp∂ρ∂tΔt!, :1078-1096 (dt already halved by the caller) */
+ORC_API void orc_update_rho(int64_t N, double *rho, const double *drhodt, double dt, double rho0,
+                            const int32_t *ptype) {
+    PFOR
+    for (int64_t i = 0; i < N; ++i) {
+        double r = rho[i] + drhodt[i] * dt;
+        if (r < rho0 && ptype[i] < 0) r = rho0;
+        rho[i] = r;
+    }
+}
+/* update_vp∂v∂tΔt!, :1107-1127 */
+ORC_API void orc_update_v(int D, int64_t N, double *v, const double *a, double dt, const int32_t *ptype) {
+    PFOR
+    for (int64_t i = 0; i < N; ++i)
+        if (ptype[i] > 1)
+            for (int d = 0; d < D; ++d) v[(int64_t)d * N + i] += a[(int64_t)d * N + i] * dt;
+}
+/* update_xpvΔt!, :1150-1169 */
+ORC_API void orc_update_x(int D, int64_t N, double *x, const double *v, double dt) {
+    PFOR
+    for (int64_t i = 0; i < N; ++i)
+        for (int d = 0; d < D; ++d) x[(int64_t)d * N + i] += v[(int64_t)d * N + i] * dt;
+}
+/* symplectic_update!, :1193-1245 */
+ORC_API void orc_symplectic(int D, int64_t N, double *rho, double *rhoh, double *v, double *vh, double *x,
+                            double *xh, const double *drhodt, const double *a, double dt, double *cdx,
+                            double rho0, const int32_t *ptype) {
+    PFOR
+    for (int64_t i = 0; i < N; ++i) {
+        double epsi = -(drhodt[i] / rhoh[i]) * dt;
+        double rv = rho[i] * (2.0 - epsi) / (2.0 + epsi);
+        if (rv < rho0 && ptype[i] <= 1) rv = rho0;
+        rhoh[i] = rv;
+        rho[i] = rv;
+        double ml = ptype[i] > 1 ? 1.0 : 0.0;
+        for (int d = 0; d < D; ++d) {
+            int64_t k = (int64_t)d * N + i;
+            double vv = v[k];
+            double nv = vv + a[k] * dt * ml;
+            vh[k] = nv;
+            v[k] = nv;
+            double ddx = (vv + nv) * 0.5 * dt;
+            cdx[k] += ddx;
+            double xv = x[k] + ddx;
+            xh[k] = xv;
+            x[k] = xv;
+        }
+    }
+}
+
+/* dpcreg!, :1485-1553 */
+typedef struct {
+    int D; int64_t N; const int32_t *pairs; const double *v; const double *rho; const double *Pr;
+    const double *x; double l0, l0inv, whinv, Pmin, Pmax, dt, lambda, kernlim, eta2; const int32_t *ptype;
+} ctx_dpc;
+static void body_dpc(int64_t p, double *const *acc, const void *vc) {
+    const ctx_dpc *c = (const ctx_dpc *)vc;
+    int32_t pi = c->pairs[2 * p], pj = c->pairs[2 * p + 1];
+    if (pi == 0) return;
+    int64_t i = pi - 1, j = pj - 1;
+    if (!(c->ptype[i] > 0 && c->ptype[j] > 0)) return;
+    int D = c->D; int64_t N = c->N;
+    double dx[3], dv[3], dd[3];
+    for (int d = 0; d < D; ++d) {
+        dx[d] = c->x[(int64_t)d * N + i] - c->x[(int64_t)d * N + j];
+        dv[d] = c->v[(int64_t)d * N + i] - c->v[(int64_t)d * N + j];
+    }
+    double rhoi = c->rho[i], rhoj = c->rho[j];
+    double r2 = dotv(D, dx, dx);
+    double r = sqrt(r2);
+    double u = r * c->l0inv;
+    double w = orc_wendland_w(D, u, c->l0inv);
+    double chi = sqrt(w * c->whinv);
+    double k = u < c->kernlim ? 1.0 : chi;
+    double Pb = chi * fmax(fmin(c->lambda * fabs(c->Pr[i] + c->Pr[j]), c->lambda * c->Pmax), c->Pmin);
+    double vr = dotv(D, dv, dx);
+    if (vr < 0.0) {
+        double vrdr = vr / (r2 + c->eta2);
+        for (int d = 0; d < D; ++d) dd[d] = k * (-vrdr * dx[d]);
+    } else {
+        double tvar = 2.0 * c->dt * Pb / ((rhoi + rhoj) * (r2 + c->eta2));
+        for (int d = 0; d < D; ++d) dd[d] = tvar * dx[d];
+    }
+    for (int d = 0; d < D; ++d) {
+        acc[d][i] += dd[d];
+        acc[d][j] -= dd[d];
+    }
+}
+ORC_API void orc_dpcreg(int D, int64_t N, int64_t P, double *buf, const double *v, const double *rho,
+                        const double *Pr, const int32_t *pairs, const double *x, double l0, double Pmin,
+                        double Pmax, double dt, double lambda, double kernlim, const int32_t *ptype) {
+    memset(buf, 0, sizeof(double) * (size_t)D * (size_t)N);
+    double l0inv = 1.0 / l0;
+    double whinv = 1.0 / orc_wendland_w(D, 0.5, l0inv);
+    ctx_dpc c = {D, N, pairs, v, rho, Pr, x, l0, l0inv, whinv, Pmin, Pmax, dt, lambda, kernlim,
+                 (0.1 * l0) * (0.1 * l0), ptype};
+    double *out[3] = {buf, buf + N, buf + 2 * N};
+    run_pairs(P, N, D, out, body_dpc, &c);
+}
+/* update_dpcreg!, :1607-1632 */
+ORC_API void orc_update_dpcreg(int D, int64_t N, double *v, double *x, const double *buf, double dt,
+                               const int32_t *ptype) {
+    PFOR
+    for (int64_t i = 0; i < N; ++i)
+        if (ptype[i] > 1)
+            for (int d = 0; d < D; ++d) {
+                int64_t k = (int64_t)d * N + i;
+                v[k] += buf[k];
+                x[k] += buf[k] * dt;
+            }
+}
+
+/* xsphcorr!, :1745-1779 (mask both ptype > 1; uses the stored W) */
+typedef struct {
+    int D; int64_t N; const int32_t *pairs; const double *W; const double *rho; const double *v;
+    double m0, eps; const int32_t *ptype;
+} ctx_xs;
+static void body_xsph(int64_t p, double *const *acc, const void *vc) {
+    const ctx_xs *c = (const ctx_xs *)vc;
+    int32_t pi = c->pairs[2 * p], pj = c->pairs[2 * p + 1];
+    if (pi == 0) return;
+    int64_t i = pi - 1, j = pj - 1;
+    if (!(c->ptype[i] > 1 && c->ptype[j] > 1)) return;
+    double xs = 2.0 * c->m0 * c->eps * c->W[p] / (c->rho[i] + c->rho[j]);
+    for (int d = 0; d < c->D; ++d) {
+        double dv = c->v[(int64_t)d * c->N + j] - c->v[(int64_t)d * c->N + i];
+        double f = dv * xs;
+        acc[d][i] += f;
+        acc[d][j] -= f;
+    }
+}
+ORC_API void orc_xsphcorr(int D, int64_t N, int64_t P, double *buf, const int32_t *pairs, const double *W,
+                          const double *rho, const double *v, double m0, double eps, const int32_t *ptype) {
+    memset(buf, 0, sizeof(double) * (size_t)D * (size_t)N);
+    ctx_xs c = {D, N, pairs, W, rho, v, m0, eps, ptype};
+    double *out[3] = {buf, buf + N, buf + 2 * N};
+    run_pairs(P, N, D, out, body_xsph, &c);
+}
+/* update_xsphcorr!, :1817-1838 */
+ORC_API void orc_update_xsph(int D, int64_t N, double *x, const double *buf, double dt, const int32_t *ptype) {
+    PFOR
+    for (int64_t i = 0; i < N; ++i)
+        if (ptype[i] > 1)
+            for (int d = 0; d < D; ++d) x[(int64_t)d * N + i] += buf[(int64_t)d * N + i] * dt;
+}
+
+/* cspmcorr!, :1673-1719: buf[0..N) = ∑ m0 W, buf[N..2N) = ∑ W m0 / ρ_other */
+static void body_cspm(int64_t p, double *const *acc, const void *vc) {
+    const ctx_xs *c = (const ctx_xs *)vc;
+    int32_t pi = c->pairs[2 * p], pj = c->pairs[2 * p + 1];
+    if (pi == 0) return;
+    int64_t i = pi - 1, j = pj - 1;
+    if (!(c->ptype[i] > 0 && c->ptype[j] > 0)) return;
+    double w = c->W[p];
+    acc[0][i] += c->m0 * w;
+    acc[1][i] += w * c->m0 / c->rho[j];
+    acc[0][j] += c->m0 * w;
+    acc[1][j] += w * c->m0 / c->rho[i];
+}
+ORC_API void orc_cspmcorr(int D, int64_t N, int64_t P, double *buf, const double *W, double *rho, double m0,
+                          const int32_t *pairs, const int32_t *ptype) {
+    memset(buf, 0, sizeof(double) * (size_t)D * (size_t)N);
+    ctx_xs c = {D, N, pairs, W, rho, NULL, m0, 0, ptype};
+    double *out[2] = {buf, buf + N};
+    run_pairs(P, N, 2, out, body_cspm, &c);
+    PFOR
+    for (int64_t i = 0; i < N; ++i) {
+        double nr = buf[i] / buf[N + i];
+        if (!isnan(nr)) rho[i] = nr;
+    }
+}
+
+/* Δt_stepping, :1293-1353 (returns the new dt) */
+ORC_API double orc_dt_stepping(int D, int64_t N, const double *a, const double *v, const double *x, double c0,
+                               double h, double CFL, double tmin, double tmax) {
+    double eta2 = (0.01 * h) * (0.01 * h);
+    double amax = -INFINITY, vmax = -INFINITY;
+    for (int64_t i = 0; i < N; ++i) {
+        double av[3], vv[3], pp[3];
+        getv(D, a, N, i, av);
+        getv(D, v, N, i, vv);
+        getv(D, x, N, i, pp);
+        double an = sqrt(dotv(D, av, av));
+        if (an > amax) amax = an;
+        double b = fabs(h * dotv(D, vv, pp) / (dotv(D, pp, pp) + eta2));
+        if (b > vmax) vmax = b;
+    }
+    double dt1 = sqrt(h / (3.0 * amax));
+    double dt2 = h / (c0 + vmax);
+    double dt = CFL * fmin(dt1, dt2);
+    dt = fmin(fmax(dt, tmin), tmax);
+    return dt;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Full problem: GPUCellList + SPHProblem + stepsolve!                       */
+/* ------------------------------------------------------------------------ */
+typedef struct {
+    double dx, h, H, rho0, m0, dt, alpha, nu, g, c0, s, delta, CFL, nui, etime;
+    double dpc_l0, dpc_pmin, dpc_pmax, dpc_lambda, xsph_eps, bound_D, bound_l;
+    int32_t gamma, cspmn;
+} OrcParams;
+
+typedef struct {
+    int D; int64_t N;
+    double dist, cs[3], offset[3]; int64_t cell[3];
+    double *x;             /* system.points, D*N */
+    int32_t *pcell;        /* D*N */
+    int32_t *cellpnum;
+    int32_t *pairs; int64_t cap, pairsn;
+    OrcParams prm;
+    double *rho, *rhoh, *v, *vh, *xh, *P, *drhodt, *a, *buf, *buf2, *cdx, *sumW, *sumgW;
+    int32_t *ptype;
+    double *W, *gW; int64_t wlen;
+} OrcSys;
+
+static void *xmalloc(size_t n) { void *p = calloc(n ? n : 1, 1); return p; }
+
+/* update!, src/celllist.jl:95-134 (capacity policy included) */
+static void sys_update_impl(OrcSys *S) {
+    int D = S->D; int64_t N = S->N;
+    int64_t ncell = S->cell[0] * S->cell[1] * (D == 3 ? S->cell[2] : 1);
+    (void)ncell;
+    orc_cellmap(D, N, S->x, S->cs, S->offset, S->cell, S->pcell, S->cellpnum);
+    if (S->pairsn > S->cap || (double)S->pairsn < (double)S->cap * 0.6) {
+        free(S->pairs);
+        S->cap = (int64_t)ceil((double)S->pairsn / 0.8);
+        S->pairs = (int32_t *)xmalloc(sizeof(int32_t) * 2 * (size_t)S->cap);
+    } else {
+        memset(S->pairs, 0, sizeof(int32_t) * 2 * (size_t)S->cap);
+    }
+    S->pairsn = orc_neib_search(D, N, S->x, S->pcell, S->cell, S->dist, S->pairs, S->cap);
+    if (S->pairsn > S->cap) {
+        free(S->pairs);
+        S->cap = (int64_t)ceil((double)S->pairsn / 0.8);
+        S->pairs = (int32_t *)xmalloc(sizeof(int32_t) * 2 * (size_t)S->cap);
+        S->pairsn = orc_neib_search(D, N, S->x, S->pcell, S->cell, S->dist, S->pairs, S->cap);
+    }
+}
+
+/* GPUCellList(points, cellsize, dist) + SPHProblem(...), src/celllist.jl:22-88, */
+/* src/sphproblem.jl:113-192.  Copies every input.  prm carries the mutable   */
+/* SPHProblem fields (defaults are applied by the caller).                     */
+ORC_API void *orc_sys_create(int D, int64_t N, const double *x, const double *cellsize, double dist,
+                             const double *rho, const double *v, const int32_t *ptype, const OrcParams *prm) {
+    OrcSys *S = (OrcSys *)xmalloc(sizeof(OrcSys));
+    S->D = D; S->N = N; S->dist = dist; S->prm = *prm;
+    size_t dn = (size_t)D * (size_t)N;
+    S->x = (double *)xmalloc(sizeof(double) * dn);
+    memcpy(S->x, x, sizeof(double) * dn);
+    if (orc_grid(D, N, S->x, cellsize, dist, NULL, NULL, S->cs, S->offset, S->cell)) { free(S->x); free(S); return NULL; }
+    int64_t ncell = S->cell[0] * S->cell[1] * (D == 3 ? S->cell[2] : 1);
+    S->pcell = (int32_t *)xmalloc(sizeof(int32_t) * dn);
+    S->cellpnum = (int32_t *)xmalloc(sizeof(int32_t) * (size_t)ncell);
+    orc_cellmap(D, N, S->x, S->cs, S->offset, S->cell, S->pcell, S->cellpnum);
+    int64_t mp = orc_maxpairs(D, S->cellpnum, S->cell);
+    S->cap = mp;
+    S->pairs = (int32_t *)xmalloc(sizeof(int32_t) * 2 * (size_t)(mp > 0 ? mp : 1));
+    S->pairsn = orc_neib_search(D, N, S->x, S->pcell, S->cell, dist, S->pairs, S->cap);
+    if ((double)S->pairsn < (double)mp * 0.8) {
+        int64_t nc = (int64_t)ceil((double)S->pairsn / 0.8);
+        int32_t *np = (int32_t *)xmalloc(sizeof(int32_t) * 2 * (size_t)(nc > 0 ? nc : 1));
+        memcpy(np, S->pairs, sizeof(int32_t) * 2 * (size_t)nc);
+        free(S->pairs);
+        S->pairs = np; S->cap = nc;
+    }
+    S->rho = (double *)xmalloc(sizeof(double) * N); memcpy(S->rho, rho, sizeof(double) * N);
+    S->rhoh = (double *)xmalloc(sizeof(double) * N); memcpy(S->rhoh, rho, sizeof(double) * N);
+    S->v = (double *)xmalloc(sizeof(double) * dn);
+    if (v) memcpy(S->v, v, sizeof(double) * dn);
+    S->vh = (double *)xmalloc(sizeof(double) * dn); memcpy(S->vh, S->v, sizeof(double) * dn);
+    S->xh = (double *)xmalloc(sizeof(double) * dn); memcpy(S->xh, S->x, sizeof(double) * dn);
+    S->ptype = (int32_t *)xmalloc(sizeof(int32_t) * N); memcpy(S->ptype, ptype, sizeof(int32_t) * N);
+    S->P = (double *)xmalloc(sizeof(double) * N);
+    S->drhodt = (double *)xmalloc(sizeof(double) * N);
+    S->a = (double *)xmalloc(sizeof(double) * dn);
+    S->buf = (double *)xmalloc(sizeof(double) * N);
+    S->buf2 = (double *)xmalloc(sizeof(double) * dn);
+    S->cdx = (double *)xmalloc(sizeof(double) * dn);
+    S->sumW = (double *)xmalloc(sizeof(double) * N);
+    S->sumgW = (double *)xmalloc(sizeof(double) * dn);
+    S->wlen = S->pairsn;
+    S->W = (double *)xmalloc(sizeof(double) * (size_t)S->wlen);
+    S->gW = (double *)xmalloc(sizeof(double) * (size_t)D * (size_t)S->wlen);
+    return S;
+}
+
+ORC_API void orc_sys_destroy(void *hs) {
+    OrcSys *S = (OrcSys *)hs;
+    if (!S) return;
+    free(S->x); free(S->pcell); free(S->cellpnum); free(S->pairs);
+    free(S->rho); free(S->rhoh); free(S->v); free(S->vh); free(S->xh); free(S->P); free(S->drhodt);
+    free(S->a); free(S->buf); free(S->buf2); free(S->cdx); free(S->sumW); free(S->sumgW);
+    free(S->ptype); free(S->W); free(S->gW); free(S);
+}
+
+ORC_API void orc_sys_set_params(void *hs, const OrcParams *prm) { ((OrcSys *)hs)->prm = *prm; }
+ORC_API void orc_sys_get_params(void *hs, OrcParams *prm) { *prm = ((OrcSys *)hs)->prm; }
+
+/* _stepsolve!, src/sphproblem.jl:207-345, one step after another in the      */
+/* reference's order (stage-1 ∇W reused by stage 2, fbmolforce at x in both  */
+/* stages, XSPH/CSPM on stage-1 W, post-batch ∑W/∑∇W).                          */
+ORC_API void orc_sys_stepsolve(void *hs, int32_t n, int timestepping, double tmin, double tmax,
+                               int64_t *updaten_out, double *maxcdx_out) {
+    OrcSys *S = (OrcSys *)hs;
+    OrcParams *p = &S->prm;
+    int D = S->D; int64_t N = S->N;
+    size_t dn = (size_t)D * (size_t)N;
+    int skipupdate = 0;
+    int64_t updaten = 0;
+    double maxcdxout = 0.0;
+    int32_t cspmcorrn = 0;
+    double kernlim = orc_dpckernlim(D);
+    double Hinv = 1.0 / p->H;
+    for (int32_t it = 0; it < n; ++it) {
+        cspmcorrn += 1;
+        if (!skipupdate) {
+            sys_update_impl(S);
+            memset(S->cdx, 0, sizeof(double) * dn);
+            skipupdate = 1;
+            updaten += 1;
+        }
+        int64_t P = S->pairsn;
+        memset(S->a, 0, sizeof(double) * dn);
+        if (S->wlen != P) {
+            free(S->W); free(S->gW);
+            S->wlen = P;
+            S->W = (double *)xmalloc(sizeof(double) * (size_t)P);
+            S->gW = (double *)xmalloc(sizeof(double) * (size_t)D * (size_t)P);
+        }
+        const int32_t *pr = S->pairs;
+        double *x = S->x;
+        orc_sphW(D, N, P, pr, x, Hinv, S->W);
+        orc_sphgradW(D, N, P, pr, x, Hinv, S->gW);
+        orc_drhodt_ddt(D, N, P, pr, S->gW, S->rho, S->v, x, p->h, p->m0, p->rho0, p->c0, p->gamma, p->g,
+                       p->delta, S->ptype, S->drhodt);
+        orc_pressure(N, S->rho, p->c0, p->gamma, p->rho0, S->ptype, S->P);
+        orc_dvdt(D, N, P, pr, S->gW, S->P, p->m0, S->rho, S->ptype, S->a);
+        orc_dvdt_av(D, N, P, pr, S->gW, x, p->h, S->rho, p->alpha, S->v, p->c0, p->m0, S->ptype, S->a);
+        if (p->nu > 0) orc_dvdt_visc(D, N, P, pr, S->gW, S->v, S->rho, x, p->h, p->m0, p->nu, S->ptype, S->a);
+        orc_addgrav(D, N, p->g, S->a);
+        orc_fbmolforce(D, N, P, pr, x, 0.4, 2.0 * p->dx, S->ptype, S->a);
+        if (p->s > 0) orc_dvdt_pF(D, N, P, pr, x, p->s, p->h, p->m0, S->ptype, S->a);
+        orc_update_rho(N, S->rhoh, S->drhodt, p->dt * 0.5, p->rho0, S->ptype);
+        orc_update_v(D, N, S->vh, S->a, p->dt * 0.5, S->ptype);
+        orc_update_x(D, N, S->xh, S->vh, p->dt * 0.5);
+        memset(S->a, 0, sizeof(double) * dn);
+        orc_drhodt_ddt(D, N, P, pr, S->gW, S->rhoh, S->vh, S->xh, p->h, p->m0, p->rho0, p->c0, p->gamma,
+                       p->g, p->delta, S->ptype, S->drhodt);
+        orc_pressure(N, S->rhoh, p->c0, p->gamma, p->rho0, S->ptype, S->P);
+        orc_dvdt(D, N, P, pr, S->gW, S->P, p->m0, S->rhoh, S->ptype, S->a);
+        orc_dvdt_av(D, N, P, pr, S->gW, S->xh, p->h, S->rhoh, p->alpha, S->vh, p->c0, p->m0, S->ptype, S->a);
+        if (p->nu > 0)
+            orc_dvdt_visc(D, N, P, pr, S->gW, S->vh, S->rhoh, S->xh, p->h, p->m0, p->nu, S->ptype, S->a);
+        orc_addgrav(D, N, p->g, S->a);
+        orc_fbmolforce(D, N, P, pr, x, p->bound_D, p->bound_l, S->ptype, S->a);
+        if (p->s > 0) orc_dvdt_pF(D, N, P, pr, S->xh, p->s, p->h, p->m0, S->ptype, S->a);
+        orc_symplectic(D, N, S->rho, S->rhoh, S->v, S->vh, x, S->xh, S->drhodt, S->a, p->dt, S->cdx, p->rho0,
+                       S->ptype);
+        if (p->dpc_l0 > 0) {
+            orc_pressure(N, S->rho, p->c0, p->gamma, p->rho0, S->ptype, S->P);
+            orc_dpcreg(D, N, P, S->buf2, S->v, S->rho, S->P, pr, x, p->dpc_l0, p->dpc_pmin, p->dpc_pmax, p->dt,
+                       p->dpc_lambda, kernlim, S->ptype);
+            orc_update_dpcreg(D, N, S->v, x, S->buf2, p->dt, S->ptype);
+        }
+        if (p->xsph_eps > 0) {
+            orc_xsphcorr(D, N, P, S->buf2, pr, S->W, S->rho, S->v, p->m0, p->xsph_eps, S->ptype);
+            orc_update_xsph(D, N, x, S->buf2, p->dt, S->ptype);
+        }
+        if (p->cspmn > 0 && cspmcorrn == p->cspmn) {
+            orc_cspmcorr(D, N, P, S->buf2, S->W, S->rho, p->m0, pr, S->ptype);
+            cspmcorrn = 0;
+        }
+        double mc = 0.0;
+        for (size_t k = 0; k < dn; ++k) { double aa = fabs(S->cdx[k]); if (aa > mc) mc = aa; }
+        if (mc > 0.9 * p->nui) skipupdate = 0;
+        if (mc > maxcdxout) maxcdxout = mc;
+        p->etime += p->dt;
+        if (timestepping) p->dt = orc_dt_stepping(D, N, S->a, S->v, x, p->c0, p->h, p->CFL, tmin, tmax);
+    }
+    memset(S->sumW, 0, sizeof(double) * N);
+    memset(S->sumgW, 0, sizeof(double) * dn);
+    orc_sphsumW(D, N, S->pairsn, S->pairs, S->x, Hinv, S->ptype, S->sumW);
+    orc_sphsumgradW(D, N, S->pairsn, S->pairs, S->x, Hinv, S->ptype, S->sumgW);
+    if (updaten_out) *updaten_out = updaten;
+    if (maxcdx_out) *maxcdx_out = maxcdxout;
+}
+
+/* Field access for tests (original particle order). */
+enum { OF_X = 0, OF_RHO, OF_V, OF_P, OF_A, OF_DRHODT, OF_RHOH, OF_VH, OF_XH, OF_CDX, OF_SUMW, OF_SUMGW,
+       OF_BUF2, OF_PTYPE };
+ORC_API int orc_sys_get(void *hs, int field, void *out) {
+    OrcSys *S = (OrcSys *)hs;
+    size_t N = (size_t)S->N, dn = (size_t)S->D * N;
+    switch (field) {
+    case OF_X: memcpy(out, S->x, 8 * dn); return 0;
+    case OF_RHO: memcpy(out, S->rho, 8 * N); return 0;
+    case OF_V: memcpy(out, S->v, 8 * dn); return 0;
+    case OF_P: memcpy(out, S->P, 8 * N); return 0;
+    case OF_A: memcpy(out, S->a, 8 * dn); return 0;
+    case OF_DRHODT: memcpy(out, S->drhodt, 8 * N); return 0;
+    case OF_RHOH: memcpy(out, S->rhoh, 8 * N); return 0;
+    case OF_VH: memcpy(out, S->vh, 8 * dn); return 0;
+    case OF_XH: memcpy(out, S->xh, 8 * dn); return 0;
+    case OF_CDX: memcpy(out, S->cdx, 8 * dn); return 0;
+    case OF_SUMW: memcpy(out, S->sumW, 8 * N); return 0;
+    case OF_SUMGW: memcpy(out, S->sumgW, 8 * dn); return 0;
+    case OF_BUF2: memcpy(out, S->buf2, 8 * dn); return 0;
+    case OF_PTYPE: memcpy(out, S->ptype, 4 * N); return 0;
+    }
+    return 1;
+}
+ORC_API int64_t orc_sys_pairsn(void *hs) { return ((OrcSys *)hs)->pairsn; }
+ORC_API int64_t orc_sys_paircap(void *hs) { return ((OrcSys *)hs)->cap; }
+ORC_API void orc_sys_pairs(void *hs, int32_t *out) {
+    OrcSys *S = (OrcSys *)hs;
+    memcpy(out, S->pairs, sizeof(int32_t) * 2 * (size_t)S->cap);
+}
+ORC_API void orc_sys_grid(void *hs, double *cs, double *offset, int64_t *cell) {
+    OrcSys *S = (OrcSys *)hs;
+    for (int d = 0; d < S->D; ++d) { cs[d] = S->cs[d]; offset[d] = S->offset[d]; cell[d] = S->cell[d]; }
+}
+/* partialupdate!, src/celllist.jl:141-145: stale pcell, current points */
+ORC_API void orc_sys_partialupdate(void *hs, int fillzero) {
+    OrcSys *S = (OrcSys *)hs;
+    if (fillzero) memset(S->pairs, 0, sizeof(int32_t) * 2 * (size_t)S->cap);
+    S->pairsn = orc_neib_search(S->D, S->N, S->x, S->pcell, S->cell, S->dist, S->pairs, S->cap);
+}
+ORC_API void orc_sys_update(void *hs) { sys_update_impl((OrcSys *)hs); }
+ORC_API void orc_sys_set_x(void *hs, const double *x) {
+    OrcSys *S = (OrcSys *)hs;
+    memcpy(S->x, x, sizeof(double) * (size_t)S->D * (size_t)S->N);
+}

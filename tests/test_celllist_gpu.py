@@ -1,0 +1,165 @@
+"""GPU parity of the cell list: the pair set from libgcsph.so must equal the
+oracle's / the golden fixture's bit for bit (compared as sorted sets)."""
+import ctypes as C
+import math
+import os
+
+import numpy as np
+import pytest
+import torch
+
+from conftest import GOLDEN
+
+pytestmark = pytest.mark.gpu
+
+
+def _set(orc, pairs):
+    return orc.pair_set(pairs.cpu().numpy() if torch.is_tensor(pairs) else pairs)
+
+
+def _oracle_pairs(orc, x, cs, dist, MIN=None, MAX=None):
+    c, off, cell = orc.grid(x, cs, dist, MIN, MAX)
+    pcell, cpn = orc.cellmap(x, c, off, cell)
+    pairs, n = orc.neib_search(x, pcell, cell, dist)
+    return pairs, n, (c, off, cell, pcell, cpn)
+
+
+def _golden_hash(pairs):
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("mg", os.path.join(GOLDEN, "make_golden.py"))
+    mg = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mg)
+    return mg.pair_hash(pairs)
+
+
+@pytest.mark.parametrize("tag", ["H", "1p1H"])
+def test_fixture_dp002_pairs_match_golden(gpu_pkg, orc, tag):
+    z = np.load(os.path.join(GOLDEN, "dambreak2d_dp002.npz"))
+    dist = float(z[f"pairs_{tag}_dist"])
+    c = gpu_pkg.GPUCellList(tuple(z["x"]), (dist, dist), dist)
+    assert c.pairsn == int(z[f"pairs_{tag}_n"])
+    ps = _set(orc, c.neighborlistview())
+    assert [int(v) for v in _golden_hash(ps)] == [int(v) for v in z[f"pairs_{tag}_hash"]]
+    # README.md:51 identity, zero tail, (min,max) order
+    full = c.neighborlist().cpu().numpy()
+    assert int((full[:, 0] != 0).sum()) == c.pairsn
+    v = full[: c.pairsn]
+    assert (v[:, 0] < v[:, 1]).all() and v.min() >= 1 and v.max() <= c.n
+    # constructor capacity policy, src/celllist.jl:80-86
+    mp = c.maxpairs()
+    assert mp >= c.pairsn
+    want_cap = math.ceil(c.pairsn / 0.8) if c.pairsn < mp * 0.8 else mp
+    assert full.shape[0] == want_cap
+
+
+def test_fixture_dp004_full_set(gpu_pkg, orc):
+    z = np.load(os.path.join(GOLDEN, "dambreak2d_dp004.npz"))
+    dist = float(z["pairs_H_dist"])
+    c = gpu_pkg.GPUCellList(tuple(z["x"]), (dist, dist), dist)
+    assert np.array_equal(_set(orc, c.neighborlistview()), orc.pair_set(z["pairs_H"]))
+
+
+def test_fixture_3d_boundary_hash(gpu_pkg, orc):
+    z = np.load(os.path.join(GOLDEN, "dambreak3d_boundary.npz"))
+    dist = float(z["pairs_dist"])
+    c = gpu_pkg.GPUCellList(tuple(z["x"]), (dist,) * 3, dist)
+    assert c.pairsn == int(z["pairs_n"])
+    assert [int(v) for v in _golden_hash(_set(orc, c.neighborlistview()))] == [int(v) for v in z["pairs_hash"]]
+
+
+@pytest.mark.parametrize("D,N,dist,seed", [(2, 20000, 0.016, 1), (3, 30000, 0.03, 2), (2, 3000, 0.3, 3),
+                                           (3, 2000, 0.4, 4), (2, 1, 0.1, 5), (3, 2, 0.5, 6)])
+def test_random_sets_match_oracle(gpu_pkg, orc, D, N, dist, seed):
+    x = np.random.default_rng(seed).random((D, N))
+    c = gpu_pkg.GPUCellList(tuple(x), (dist,) * D, dist)
+    pairs, n, (cs, off, cell, pcell, cpn) = _oracle_pairs(orc, x, (dist,) * D, dist)
+    assert c.pairsn == n
+    assert np.array_equal(_set(orc, c.neighborlistview()), orc.pair_set(pairs))
+    assert c.grid == tuple(int(v) for v in cell)
+    assert np.allclose(c.offset, off, rtol=0, atol=0)
+    assert np.array_equal(c.cellpnum.cpu().numpy(), cpn)
+
+
+def test_adversarial_points(gpu_pkg, orc):
+    dist = 0.25
+    pts = [(0.0, 0.0), (0.25, 0.0), (0.5, 0.5), (0.5, 0.5), (0.75, 0.0), (0.75, 0.2499999), (1.0, 1.0),
+           (1.0, 0.75), (3.0, 3.0), (3.1, 3.05), (2.0, 0.0)]
+    x = np.array(pts, dtype=np.float64).T.copy()
+    c = gpu_pkg.GPUCellList(tuple(x), (dist, dist), dist)
+    pairs, n, _ = _oracle_pairs(orc, x, (dist, dist), dist)
+    got = {tuple(p) for p in _set(orc, c.neighborlistview()).tolist()}
+    assert got == {tuple(p) for p in orc.pair_set(pairs).tolist()}
+    assert (1, 2) not in got and (3, 4) in got
+
+
+def test_clamped_cells_with_given_box(gpu_pkg, orc):
+    x = np.random.default_rng(11).uniform(-0.5, 1.5, (3, 3000))
+    dist = 0.1
+    c = gpu_pkg.GPUCellList(tuple(x), (dist,) * 3, dist, MIN=(0, 0, 0), MAX=(1, 1, 1))
+    pairs, n, _ = _oracle_pairs(orc, x, (dist,) * 3, dist, MIN=(0, 0, 0), MAX=(1, 1, 1))
+    assert c.pairsn == n
+    assert np.array_equal(_set(orc, c.neighborlistview()), orc.pair_set(pairs))
+
+
+def test_single_overfull_cell(gpu_pkg, orc):
+    x = np.random.default_rng(12).uniform(0, 0.01, (2, 700))
+    c = gpu_pkg.GPUCellList(tuple(x), (1.0, 1.0), 1.0)
+    assert c.pairsn == 700 * 699 // 2
+    assert int(c.cellpnum.max().item()) == 700
+
+
+def test_update_and_partialupdate_follow_reference_semantics(gpu_pkg, orc):
+    """update! re-bins moved points; partialupdate! keeps the stale cells
+    (src/celllist.jl:95-145).  Both compared with the oracle's own sequence."""
+    rng = np.random.default_rng(21)
+    D, N, dist = 2, 20000, 0.016
+    x = rng.random((D, N))
+    c = gpu_pkg.GPUCellList(tuple(x), (dist, dist), dist)
+    p = orc.default_params(0.01, 0.01, 0.016, 1000, 0.1, 1e-5, 0.01, 10, 7, 0.1, 0.2, dist)
+    o = orc.OracleSystem(x, (dist, dist), dist, np.full(N, 1000.0), np.full(N, 2, np.int32), p)
+    x2 = x + rng.uniform(-0.6, 0.6, x.shape) * dist
+    for d in range(D):
+        c.points[d].copy_(torch.from_numpy(x2[d]))
+    o.set_x(x2)
+    c.partialupdate()
+    o.partialupdate()
+    assert c.pairsn == o.pairsn
+    assert np.array_equal(_set(orc, c.neighborlistview()), orc.pair_set(o.pairs()[: o.pairsn]))
+    c.update()
+    o.update()
+    assert c.pairsn == o.pairsn
+    assert np.array_equal(_set(orc, c.neighborlistview()), orc.pair_set(o.pairs()[: o.pairsn]))
+    full = c.neighborlist().cpu().numpy()
+    assert int((full[:, 0] != 0).sum()) == c.pairsn   # README.md:58
+
+
+def test_emit_reports_capacity_overflow(gpu_pkg):
+    from importlib import import_module
+    L = gpu_pkg.load_library()
+    lib_mod = import_module(gpu_pkg.__name__ + "._lib")
+    x = np.random.default_rng(4).random((2, 5000))
+    c = gpu_pkg.GPUCellList(tuple(x), (0.05, 0.05), 0.05)
+    small = torch.zeros((10, 2), dtype=torch.int32, device="cuda")
+    n = C.c_int64()
+    rc = L.gcl_emit_pairs(c._h, C.c_void_p(small.data_ptr()), 10, 1, C.byref(n))
+    assert rc == lib_mod.GCSPH_ECAPACITY and n.value == c.pairsn
+    # the first 10 pairs are the first 10 of the full list
+    assert torch.equal(small, c.neighborlistview()[:10])
+
+
+@pytest.mark.parametrize("D,N,dist", [(2, 200_000, 0.016), (3, 4_000_000, 0.008)])
+def test_full_size_pair_sets(gpu_pkg, orc, D, N, dist):
+    """The cell-list configuration at full size: 200k 2-D / 4M 3-D uniform
+    points, pair sets compared with the oracle, then a jittered
+    partialupdate! compared by count and set."""
+    x = gpu_pkg.workloads.uniform_points(N, D)
+    c = gpu_pkg.GPUCellList(tuple(x), (dist,) * D, dist)
+    pairs, n, _ = _oracle_pairs(orc, x, (dist,) * D, dist)
+    assert c.pairsn == n
+    got = c.neighborlistview().cpu().numpy().astype(np.int64)
+    assert (got[:, 0] < got[:, 1]).all()
+    want = pairs.astype(np.int64)
+    kg = np.sort(got[:, 0] * (1 << 32) + got[:, 1])
+    kw = np.sort(want[:, 0] * (1 << 32) + want[:, 1])
+    assert np.array_equal(kg, kw)
+    assert np.unique(kg).size == kg.size

@@ -1,0 +1,227 @@
+"""CPU tests of the oracle: pinned against the golden fixtures, the O(N^2)
+brute force and closed-form properties of the restated formulas."""
+import math
+import os
+import struct
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+
+
+# ----------------------------------------------------------------- formulas
+def test_wendland_normalisation_and_derivative(orc):
+    L = orc.lib()
+    for D in (2, 3):
+        H = 0.37
+        Hinv = 1 / H
+        r = np.linspace(0, H, 200001)
+        w = np.array([L.orc_wendland_w(D, ri * Hinv, Hinv) for ri in r[::50]])
+        rr = r[::50]
+        shell = 2 * math.pi * rr if D == 2 else 4 * math.pi * rr ** 2
+        integral = np.trapezoid(w * shell, rr)
+        assert abs(integral - 1.0) < 1e-6, (D, integral)
+        # dW/dr from the restated d𝒲 matches a central difference of W
+        for u in (0.1, 0.35, 0.6, 0.93):
+            e = 1e-6
+            fd = (L.orc_wendland_w(D, u + e, Hinv) - L.orc_wendland_w(D, u - e, Hinv)) / (2 * e * H)
+            an = L.orc_wendland_dw(D, u, Hinv)
+            assert abs(fd - an) <= 1e-6 * abs(an) + 1e-9
+        assert L.orc_wendland_w(D, 1.0, Hinv) == 0.0 and L.orc_wendland_dw(D, 1.5, Hinv) == 0.0
+
+
+def _pf7_py(x):
+    """Independent Python restatement of powfancy7th (src/gpukernels_sph.jl:499-515)."""
+    bits = struct.unpack("<Q", struct.pack("<d", abs(x)))[0]
+    t = struct.unpack("<d", struct.pack("<Q", (0x36CD000000000000 + bits // 7) & 0xFFFFFFFFFFFFFFFF))[0]
+    t = math.copysign(t, x)
+    for _ in range(2):
+        t2 = t * t
+        t3 = t2 * t
+        t4 = t2 * t2
+        xot4 = x / t4
+        t = t - (t * (t3 - xot4)) / (4 * t3 + 3 * xot4)
+    return t
+
+
+def test_powfancy7th_bit_exact_and_accuracy(orc):
+    L = orc.lib()
+    rng = np.random.default_rng(5)
+    xs = np.concatenate([1 + rng.uniform(-5e-3, 5e-3, 2000), rng.uniform(0.5, 2.0, 2000), [1.0, 0.999, 1.001]])
+    for x in xs:
+        got = L.orc_powfancy7th(float(x), 1 / 7, 7)
+        assert got == _pf7_py(float(x))
+        # two Newton steps from the bit-trick guess: close to x^(1/7), not exact
+        assert abs(got - x ** (1 / 7)) < 1e-5
+    # gamma != 7 falls back to x^(1/gamma)
+    assert L.orc_powfancy7th(2.0, 1 / 5, 5) == 2.0 ** (1 / 5)
+
+
+def test_ipow_and_dpckernlim(orc):
+    L = orc.lib()
+    for x in (0.9, 1.0, 1.0001, 1.7):
+        x2 = x * x
+        assert L.orc_ipow(x, 7) == (x2 * x2) * x2 * x
+    for D in (2, 3):
+        k = L.orc_dpckernlim(D)
+        assert 0 < k < 1
+        assert abs(L.orc_wendland_w(D, k, 1.0) - 1.0) < 1e-14
+
+
+# ----------------------------------------------------------------- cell list
+def _cells(orc, x, cs, dist, MIN=None, MAX=None):
+    c, off, cell = orc.grid(x, cs, dist, MIN, MAX)
+    pcell, cpn = orc.cellmap(x, c, off, cell)
+    return c, off, cell, pcell, cpn
+
+
+@pytest.mark.parametrize("D,N,dist", [(2, 3000, 0.03), (3, 4000, 0.07), (2, 500, 0.2), (3, 300, 0.25)])
+def test_cell_search_equals_bruteforce(orc, D, N, dist):
+    rng = np.random.default_rng(N + D)
+    x = rng.random((D, N))
+    c, off, cell, pcell, cpn = _cells(orc, x, (dist,) * D, dist)
+    pairs, n = orc.neib_search(x, pcell, cell, dist)
+    bf = orc.pairs_bruteforce(x, pcell, dist)
+    assert n == len(pairs) == len(bf)
+    assert np.array_equal(orc.pair_set(pairs), orc.pair_set(bf))
+    assert orc.maxpairs(D, cpn, cell) >= n
+    assert int(cpn.sum()) == N
+
+
+def test_cell_search_adversarial(orc):
+    dist = 0.25  # exactly representable; dist^2 = 0.0625 exactly
+    pts = [
+        (0.0, 0.0), (0.25, 0.0),          # r^2 == dist^2 exactly: NOT a pair (strict <)
+        (0.5, 0.5), (0.5, 0.5),           # duplicates: r = 0 is a pair
+        (0.75, 0.0), (0.75, 0.2499999),   # just inside
+        (1.0, 1.0), (1.0, 0.75),          # on a cell face, exactly dist apart
+        (3.0, 3.0), (3.1, 3.05),          # far corner
+        (2.0, 0.0),                       # lonely
+    ]
+    x = np.array(pts, dtype=np.float64).T.copy()
+    c, off, cell, pcell, cpn = _cells(orc, x, (dist, dist), dist)
+    pairs, n = orc.neib_search(x, pcell, cell, dist)
+    ps = {tuple(p) for p in orc.pair_set(pairs).tolist()}
+    assert (1, 2) not in ps
+    assert (3, 4) in ps
+    assert (5, 6) in ps
+    assert (7, 8) not in ps
+    assert (9, 10) in ps
+    bf = orc.pairs_bruteforce(x, pcell, dist)
+    assert np.array_equal(orc.pair_set(pairs), orc.pair_set(bf))
+
+
+def test_clamped_out_of_box_points(orc):
+    """MIN/MAX given smaller than the data: points outside clamp into edge cells
+    (src/gpukernels_cls.jl:36) and only pair with Chebyshev-adjacent cells."""
+    rng = np.random.default_rng(3)
+    x = rng.uniform(-0.5, 1.5, (2, 800))
+    dist = 0.1
+    c, off, cell, pcell, cpn = _cells(orc, x, (dist, dist), dist, MIN=(0.0, 0.0), MAX=(1.0, 1.0))
+    assert pcell.min() >= 1 and all(pcell[d].max() <= cell[d] for d in range(2))
+    pairs, n = orc.neib_search(x, pcell, cell, dist)
+    bf = orc.pairs_bruteforce(x, pcell, dist)
+    assert np.array_equal(orc.pair_set(pairs), orc.pair_set(bf))
+
+
+def test_overfull_single_cell(orc):
+    rng = np.random.default_rng(9)
+    x = rng.uniform(0, 0.01, (3, 400))
+    dist = 1.0
+    c, off, cell, pcell, cpn = _cells(orc, x, (dist,) * 3, dist)
+    assert cpn.max() == 400
+    pairs, n = orc.neib_search(x, pcell, cell, dist)
+    assert n == 400 * 399 // 2
+
+
+# ----------------------------------------------------------------- golden fixtures
+def _golden_hash(pairs):
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("mg", os.path.join(GOLDEN, "make_golden.py"))
+    mg = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mg)
+    return mg.pair_hash(pairs)
+
+
+def test_golden_pairs_dp004_full_set(orc):
+    z = np.load(os.path.join(GOLDEN, "dambreak2d_dp004.npz"))
+    x = z["x"]
+    dist = float(z["pairs_H_dist"])
+    c, off, cell, pcell, cpn = _cells(orc, x, (dist, dist), dist)
+    pairs, n = orc.neib_search(x, pcell, cell, dist)
+    assert np.array_equal(orc.pair_set(pairs), orc.pair_set(z["pairs_H"]))
+
+
+@pytest.mark.parametrize("tag", ["H", "1p1H"])
+def test_golden_pairs_dp002_hash(orc, tag):
+    z = np.load(os.path.join(GOLDEN, "dambreak2d_dp002.npz"))
+    x = z["x"]
+    dist = float(z[f"pairs_{tag}_dist"])
+    c, off, cell, pcell, cpn = _cells(orc, x, (dist, dist), dist)
+    pairs, n = orc.neib_search(x, pcell, cell, dist)
+    assert n == int(z[f"pairs_{tag}_n"])
+    s, xr = _golden_hash(orc.pair_set(pairs))
+    assert [s, xr] == [int(v) for v in z[f"pairs_{tag}_hash"]]
+
+
+def test_golden_pairs_3d_boundary_hash(orc):
+    z = np.load(os.path.join(GOLDEN, "dambreak3d_boundary.npz"))
+    x = z["x"]
+    dist = float(z["pairs_dist"])
+    c, off, cell, pcell, cpn = _cells(orc, x, (dist,) * 3, dist)
+    pairs, n = orc.neib_search(x, pcell, cell, dist)
+    assert n == int(z["pairs_n"])
+    s, xr = _golden_hash(orc.pair_set(pairs))
+    assert [s, xr] == [int(v) for v in z["pairs_hash"]]
+
+
+# ----------------------------------------------------------------- full problem
+def _small_case(pkg, **kw):
+    return pkg.workloads.dam_break_2d(dx=0.05, fluid=(0.5, 0.6), tank=(1.0, 1.0), **kw)
+
+
+def _oracle_system(orc, case):
+    p = orc.default_params(case.dx, case.h, case.H, case.rho0, case.m0, case.dt, case.alpha, case.c0, case.gamma,
+                           case.delta, case.CFL, case.dist, g=case.g, s=case.s)
+    for k, v in case.extra.items():
+        setattr(p, k, v)
+    return orc.OracleSystem(case.x, case.cellsize, case.dist, case.rho, case.ptype, p)
+
+
+def test_oracle_constructor_capacity_and_readme_identity(orc, pkg):
+    case = _small_case(pkg)
+    s = _oracle_system(orc, case)
+    pairs = s.pairs()
+    # count(x -> !iszero(x[1]), system.pairs) == system.pairsn  (README.md:51)
+    assert int((pairs[:, 0] != 0).sum()) == s.pairsn
+    assert len(pairs) == math.ceil(s.pairsn / 0.8) or len(pairs) >= s.pairsn
+
+
+def test_oracle_step_invariants(orc, pkg):
+    case = _small_case(pkg, layer_ptype=(1, 0, 0))
+    s = _oracle_system(orc, case)
+    un, mc = s.stepsolve(40)
+    assert un >= 1 and mc > 0
+    x = s.get("x")
+    rho = s.get("rho")
+    assert np.isfinite(x).all() and np.isfinite(rho).all()
+    fl = case.ptype == 2
+    # fluid stays inside the tank; boundary particles never move
+    assert x[0, fl].min() > -case.dx and x[1, fl].min() > -case.dx
+    assert np.array_equal(x[:, ~fl], case.x[:, ~fl])
+    assert abs(s.params.etime - 40 * case.dt) < 1e-15
+
+
+def test_oracle_threads_match_serial(orc, pkg):
+    case = pkg.workloads.dam_break_2d(dx=0.04, fluid=(0.6, 0.8), tank=(1.2, 1.0), layer_ptype=(1, 0, 0))
+    orc.set_threads(1)
+    a = _oracle_system(orc, case)
+    a.stepsolve(10)
+    orc.set_threads(max(2, min(4, orc.max_threads())))
+    b = _oracle_system(orc, case)
+    b.stepsolve(10)
+    orc.set_threads(1)
+    for f in ("x", "v", "rho", "a"):
+        va, vb = a.get(f), b.get(f)
+        assert np.abs(va - vb).max() <= 1e-12 * max(np.abs(va).max(), 1e-300), f

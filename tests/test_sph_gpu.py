@@ -1,0 +1,279 @@
+"""GPU parity of the SPH path against the oracle.
+
+Tolerance (the FP64 contract): every field within 1e-12 relative, measured
+normwise per field as max|gpu - oracle| / max|oracle|.  Displacements from
+the start are checked as well (normwise 1e-9), which is far stricter than
+the 1e-12-of-position test for particles that moved a few micrometres.
+"""
+import math
+
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+RTOL = 1e-12
+FIELDS = ("x", "rho", "v", "P", "a", "drhodt", "rhoh", "vh", "xh", "cdx", "sumW", "sumgW", "buf2")
+
+
+def relerr(got, want):
+    got = np.asarray(got, dtype=np.float64)
+    want = np.asarray(want, dtype=np.float64)
+    scale = np.abs(want).max() if want.size else 0.0
+    diff = np.abs(got - want).max() if want.size else 0.0
+    if diff == 0.0:
+        return 0.0
+    return diff / scale if scale > 0 else math.inf
+
+
+def make_pair(pkg, orc, case):
+    system = pkg.GPUCellList(tuple(case.x), case.cellsize, case.dist)
+    prob = pkg.SPHProblem(system, case.dx, case.h, case.H, pkg.WendlandC2(dim=case.D), case.rho, case.ptype,
+                          case.rho0, case.m0, case.dt, case.alpha, case.c0, case.gamma, case.delta, case.CFL,
+                          g=case.g, s=case.s)
+    p = orc.default_params(case.dx, case.h, case.H, case.rho0, case.m0, case.dt, case.alpha, case.c0, case.gamma,
+                           case.delta, case.CFL, case.dist, g=case.g, s=case.s)
+    for k, v in case.extra.items():
+        setattr(prob, k, v)
+        setattr(p, k, v)
+    ref = orc.OracleSystem(case.x, case.cellsize, case.dist, case.rho, case.ptype, p)
+    return prob, ref
+
+
+def gpu_field(prob, name):
+    if name == "x":
+        return torch.stack(prob.system.points).cpu().numpy()
+    if name == "rho":
+        return prob.rho.cpu().numpy()
+    if name == "v":
+        return torch.stack(prob.v).cpu().numpy()
+    f = prob.field(name)
+    return (torch.stack(f) if isinstance(f, tuple) else f).cpu().numpy()
+
+
+def compare(prob, ref, case, fields=FIELDS, rtol=RTOL):
+    errs = {}
+    for name in fields:
+        errs[name] = relerr(gpu_field(prob, name), ref.get(name))
+    bad = {k: v for k, v in errs.items() if not v <= rtol}
+    assert not bad, f"fields over {rtol}: {bad}"
+    d_got = gpu_field(prob, "x") - case.x
+    d_want = ref.get("x") - case.x
+    assert relerr(d_got, d_want) <= 1e-9
+    return errs
+
+
+def run_both(prob, ref, n, **kw):
+    a = prob.stepsolve(n, **kw)
+    b = ref.stepsolve(n, **kw)
+    assert a[0] == b[0], (a, b)
+    assert abs(a[1] - b[1]) <= 1e-12 * max(abs(b[1]), 1e-300), (a, b)
+    assert prob.etime == ref.params.etime
+    return a
+
+
+def test_dam_break_2d_c1_100_steps(gpu_pkg, orc):
+    """The plain FP64 configuration: 2-D dam break, dx=0.02, boundary ptype 0,
+    cell list rebuilt every step, 100 steps (CSPM fires at 15, 30, ...)."""
+    case = gpu_pkg.workloads.dam_break_2d()
+    prob, ref = make_pair(gpu_pkg, orc, case)
+    un, _ = run_both(prob, ref, 100)
+    assert un == 100
+    compare(prob, ref, case)
+
+
+def test_fixture_dp002_readme_parameters(gpu_pkg, orc):
+    """The reference's own 2-D fixture (ptype 2 / 1 / 0, hydrostatic ρ) with
+    the README demo parameters, in two stepsolve! calls."""
+    import os
+    from conftest import GOLDEN
+    case = gpu_pkg.workloads.load_fixture(os.path.join(GOLDEN, "dambreak2d_dp002.npz"))
+    prob, ref = make_pair(gpu_pkg, orc, case)
+    run_both(prob, ref, 20)
+    run_both(prob, ref, 20)
+    compare(prob, ref, case)
+
+
+def test_full_physics_2d(gpu_pkg, orc):
+    case = gpu_pkg.workloads.dam_break_2d(dx=0.04, fluid=(0.6, 0.8), tank=(1.2, 1.0), layer_ptype=(1, 0, 0))
+    case.s = 0.05
+    case.extra = dict(nu=0.2, dpc_l0=case.dx * 0.7, dpc_lambda=0.005, dpc_pmax=36000.0, xsph_eps=0.5, cspmn=7)
+    prob, ref = make_pair(gpu_pkg, orc, case)
+    run_both(prob, ref, 30)
+    compare(prob, ref, case)
+
+
+def test_full_physics_3d(gpu_pkg, orc):
+    case = gpu_pkg.workloads.dam_break_3d(dx=0.05, fluid=(0.3, 0.4, 0.2), tank=(0.6, 0.6, 0.3))
+    case.extra = dict(case.extra, dpc_l0=0.03)
+    prob, ref = make_pair(gpu_pkg, orc, case)
+    run_both(prob, ref, 16)
+    compare(prob, ref, case)
+
+
+def test_skin_and_timestepping(gpu_pkg, orc):
+    """dist = 1.1H gives a Verlet skin (rebuild only when max|cΔx| > 0.9(dist-H),
+    src/sphproblem.jl:325-328) and Δt_stepping changes Δt every step."""
+    case = gpu_pkg.workloads.dam_break_2d(dx=0.04, fluid=(0.6, 0.8), tank=(1.2, 1.0), layer_ptype=(1, 0, 0),
+                                          dist_factor=1.1)
+    prob, ref = make_pair(gpu_pkg, orc, case)
+    lims = (1e-7, case.CFL * case.H / (3 * case.c0))
+    for _ in range(3):
+        un, _ = run_both(prob, ref, 25, timestepping=True, timelims=lims)
+    assert un < 25  # the skin skipped rebuilds
+    assert prob.dt == ref.params.dt
+    compare(prob, ref, case)
+
+
+def test_zero_steps_and_getters(gpu_pkg, orc):
+    case = gpu_pkg.workloads.dam_break_2d(dx=0.05, fluid=(0.5, 0.6), tank=(1.0, 1.0))
+    prob, ref = make_pair(gpu_pkg, orc, case)
+    assert prob.stepsolve(0) == (0, 0.0)
+    ref.stepsolve(0)
+    for name in ("sumW", "sumgW"):
+        assert relerr(gpu_field(prob, name), ref.get(name)) <= RTOL
+    assert torch.equal(gpu_pkg.get_ptype(prob).cpu(), torch.from_numpy(case.ptype))
+    assert gpu_pkg.get_points(prob) is prob.system.points
+
+
+# ----------------------------------------------------------------- standalone kernels
+def _kernel_setup(pkg, orc, D=2):
+    rng = np.random.default_rng(7)
+    if D == 2:
+        case = pkg.workloads.dam_break_2d(dx=0.04, fluid=(0.6, 0.8), tank=(1.2, 1.0), layer_ptype=(1, 0, 0))
+    else:
+        case = pkg.workloads.dam_break_3d(dx=0.05, fluid=(0.3, 0.4, 0.2), tank=(0.6, 0.6, 0.3))
+    N = case.N
+    x = case.x + rng.uniform(-0.2, 0.2, case.x.shape) * case.dx
+    c, off, cell = orc.grid(x, case.cellsize, case.dist)
+    pcell, _ = orc.cellmap(x, c, off, cell)
+    pairs, n = orc.neib_search(x, pcell, cell, case.dist)
+    pairs = np.ascontiguousarray(np.concatenate([pairs, np.zeros((5, 2), np.int32)]))  # zero tail is skipped
+    rho = case.rho0 * (1 + rng.uniform(-0.01, 0.01, N))
+    v = rng.uniform(-0.3, 0.3, (D, N))
+    return case, np.ascontiguousarray(x), pairs, np.ascontiguousarray(rho), np.ascontiguousarray(v)
+
+
+@pytest.mark.parametrize("D", [2, 3])
+def test_pair_kernels_match_oracle(gpu_pkg, orc, D):
+    K = gpu_pkg.kernels
+    case, x, pairs, rho, v = _kernel_setup(gpu_pkg, orc, D)
+    N, P = case.N, pairs.shape[0]
+    pt = case.ptype
+    T = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+    vecT = lambda a: tuple(T(a[d]) for d in range(D))
+    tx, tv, trho, tpt, tpairs = vecT(x), vecT(v), T(rho), T(pt), T(pairs)
+    Hinv = 1 / case.H
+    # W, ∇W
+    W = torch.zeros(P, dtype=torch.float64, device="cuda")
+    gW = tuple(torch.zeros(P, dtype=torch.float64, device="cuda") for _ in range(D))
+    K.sphW(W, tpairs, tx, Hinv)
+    K.sphgradW(gW, tpairs, tx, Hinv)
+    oW = np.zeros(P); ogW = np.zeros((D, P))
+    orc.call("orc_sphW", D, N, P, pairs, x, Hinv, oW)
+    orc.call("orc_sphgradW", D, N, P, pairs, x, Hinv, ogW)
+    assert np.array_equal(W.cpu().numpy(), oW)
+    assert np.array_equal(torch.stack(gW).cpu().numpy(), ogW)
+    # ∑W, ∑∇W
+    sW = torch.zeros(N, dtype=torch.float64, device="cuda")
+    sgW = tuple(torch.zeros(N, dtype=torch.float64, device="cuda") for _ in range(D))
+    K.sphsumW(sW, tpairs, tx, None, Hinv, tpt)
+    K.sphsumgradW(sgW, tpairs, tx, None, Hinv, tpt)
+    osW = np.zeros(N); osgW = np.zeros((D, N))
+    orc.call("orc_sphsumW", D, N, P, pairs, x, Hinv, pt, osW)
+    orc.call("orc_sphsumgradW", D, N, P, pairs, x, Hinv, pt, osgW)
+    assert relerr(sW.cpu().numpy(), osW) <= RTOL
+    assert relerr(torch.stack(sgW).cpu().numpy(), osgW) <= RTOL
+    # ∂ρ∂tDDT, pressure
+    dr = torch.zeros(N, dtype=torch.float64, device="cuda")
+    K.drhodtDDT(dr, tpairs, gW, trho, tv, tx, case.h, case.m0, case.rho0, case.c0, case.gamma, case.g, case.delta, tpt)
+    odr = np.zeros(N)
+    orc.call("orc_drhodt_ddt", D, N, P, pairs, ogW, rho, v, x, case.h, case.m0, case.rho0, case.c0, case.gamma, case.g,
+             case.delta, pt, odr)
+    assert relerr(dr.cpu().numpy(), odr) <= RTOL
+    Pr = torch.zeros(N, dtype=torch.float64, device="cuda")
+    K.pressure(Pr, trho, case.c0, case.gamma, case.rho0, tpt)
+    oP = np.zeros(N)
+    orc.call("orc_pressure", N, rho, case.c0, case.gamma, case.rho0, pt, oP)
+    assert np.array_equal(Pr.cpu().numpy(), oP)
+    # momentum terms, each accumulated on top of the previous like stepsolve!
+    a = tuple(torch.zeros(N, dtype=torch.float64, device="cuda") for _ in range(D))
+    oa = np.zeros((D, N))
+    K.dvdt(a, gW, Pr, tpairs, case.m0, trho, tpt)
+    orc.call("orc_dvdt", D, N, P, pairs, ogW, oP, case.m0, rho, pt, oa)
+    assert relerr(torch.stack(a).cpu().numpy(), oa) <= RTOL
+    K.dvdt_av(a, gW, tpairs, tx, case.h, trho, case.alpha, tv, case.c0, case.m0, tpt)
+    orc.call("orc_dvdt_av", D, N, P, pairs, ogW, x, case.h, rho, case.alpha, v, case.c0, case.m0, pt, oa)
+    assert relerr(torch.stack(a).cpu().numpy(), oa) <= RTOL
+    K.dvdt_visc(a, gW, tv, trho, tx, tpairs, case.h, case.m0, 0.2, tpt)
+    orc.call("orc_dvdt_visc", D, N, P, pairs, ogW, v, rho, x, case.h, case.m0, 0.2, pt, oa)
+    assert relerr(torch.stack(a).cpu().numpy(), oa) <= RTOL
+    K.dvdt_addgrav(a, case.g)
+    orc.call("orc_addgrav", D, N, case.g, oa)
+    K.fbmolforce(a, tpairs, tx, 0.4, 2 * case.dx, tpt)
+    orc.call("orc_fbmolforce", D, N, P, pairs, x, 0.4, 2 * case.dx, pt, oa)
+    K.dvdtpF(a, tpairs, tx, 0.05, case.h, case.m0, tpt)
+    orc.call("orc_dvdt_pF", D, N, P, pairs, x, 0.05, case.h, case.m0, pt, oa)
+    assert relerr(torch.stack(a).cpu().numpy(), oa) <= RTOL
+    # predictors, corrector
+    rh = trho.clone(); orh = rho.copy()
+    K.update_rho(rh, dr, 0.5e-5, case.rho0, tpt)
+    orc.call("orc_update_rho", N, orh, odr, 0.5e-5, case.rho0, pt)
+    vh = tuple(t.clone() for t in tv); ovh = v.copy()
+    K.update_v(vh, a, 0.5e-5, tpt)
+    orc.call("orc_update_v", D, N, ovh, oa, 0.5e-5, pt)
+    xh = tuple(t.clone() for t in tx); oxh = x.copy()
+    K.update_x(xh, vh, 0.5e-5)
+    orc.call("orc_update_x", D, N, oxh, ovh, 0.5e-5)
+    assert relerr(rh.cpu().numpy(), orh) <= RTOL
+    assert relerr(torch.stack(xh).cpu().numpy(), oxh) <= RTOL
+    r2 = trho.clone(); v2 = tuple(t.clone() for t in tv); x2 = tuple(t.clone() for t in tx)
+    cdx = tuple(torch.zeros(N, dtype=torch.float64, device="cuda") for _ in range(D))
+    orr, ov2, ox2, ocdx = rho.copy(), v.copy(), x.copy(), np.zeros((D, N))
+    orh2, ovh2, oxh2 = orh.copy(), ovh.copy(), oxh.copy()
+    K.symplectic_update(r2, rh, v2, vh, x2, xh, dr, a, 1e-5, cdx, case.rho0, tpt)
+    orc.call("orc_symplectic", D, N, orr, orh2, ov2, ovh2, ox2, oxh2, odr, oa, 1e-5, ocdx, case.rho0, pt)
+    assert relerr(r2.cpu().numpy(), orr) <= RTOL
+    assert relerr(torch.stack(v2).cpu().numpy(), ov2) <= RTOL
+    assert relerr(torch.stack(cdx).cpu().numpy(), ocdx) <= RTOL
+    # DPC, XSPH, CSPM
+    buf = tuple(torch.zeros(N, dtype=torch.float64, device="cuda") for _ in range(D))
+    obuf = np.zeros((D, N))
+    klim = K.dpckernlim(D)
+    l0 = case.dx * 0.7
+    K.dpcreg(buf, tv, trho, Pr, tpairs, tx, None, l0, 1.0, 36000.0, 1e-5, 0.005, klim, tpt)
+    orc.call("orc_dpcreg", D, N, P, obuf, v, rho, oP, pairs, x, l0, 1.0, 36000.0, 1e-5, 0.005, klim, pt)
+    assert relerr(torch.stack(buf).cpu().numpy(), obuf) <= RTOL
+    v3 = tuple(t.clone() for t in tv); x3 = tuple(t.clone() for t in tx)
+    ov3, ox3 = v.copy(), x.copy()
+    K.update_dpcreg(v3, x3, buf, 1e-5, tpt)
+    orc.call("orc_update_dpcreg", D, N, ov3, ox3, obuf, 1e-5, pt)
+    assert relerr(torch.stack(v3).cpu().numpy(), ov3) <= RTOL
+    K.xsphcorr(buf, tpairs, W, trho, tv, case.m0, 0.5, tpt)
+    orc.call("orc_xsphcorr", D, N, P, obuf, pairs, oW, rho, v, case.m0, 0.5, pt)
+    assert relerr(torch.stack(buf).cpu().numpy(), obuf) <= RTOL
+    K.update_xsphcorr(x3, buf, 1e-5, tpt)
+    orc.call("orc_update_xsph", D, N, ox3, obuf, 1e-5, pt)
+    assert relerr(torch.stack(x3).cpu().numpy(), ox3) <= RTOL
+    r4 = trho.clone(); or4 = rho.copy()
+    K.cspmcorr(buf, W, r4, case.m0, tpairs, tpt)
+    orc.call("orc_cspmcorr", D, N, P, obuf, oW, or4, case.m0, pairs, pt)
+    assert relerr(r4.cpu().numpy(), or4) <= RTOL
+    # Δt_stepping
+    dt = K.dt_stepping(a, tv, tx, case.c0, case.h, case.CFL, (0.0, 1.0))
+    odt = orc.call("orc_dt_stepping", D, N, oa, v, x, case.c0, case.h, case.CFL, 0.0, 1.0)
+    assert abs(dt - odt) <= RTOL * odt
+
+
+def test_kernels_bitwise_where_no_atomics(gpu_pkg, orc):
+    """Per-pair and per-particle kernels have no summation: bit-identical."""
+    pkg = gpu_pkg
+    case, x, pairs, rho, v = _kernel_setup(pkg, orc, 2)
+    N, P, D = case.N, pairs.shape[0], 2
+    T = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+    W = torch.zeros(P, dtype=torch.float64, device="cuda")
+    pkg.kernels.sphW(W, T(pairs), (T(x[0]), T(x[1])), 1 / case.H)
+    oW = np.zeros(P)
+    orc.call("orc_sphW", D, N, P, pairs, x, 1 / case.H, oW)
+    assert np.array_equal(W.cpu().numpy(), oW)
