@@ -109,6 +109,34 @@ __host__ __device__ inline double powfancy7th(double x, double ginv, int gamma) 
   return pow(x, ginv);
 }
 
+#define GC_INLINE __host__ __device__ inline
+/* cos(x) by Cody-Waite reduction modulo pi/2 (pi/2 split into a 33-bit head
+ * and its tail) and the Taylor series of cos / sin on |r| <= pi/4 (terms to
+ * r^16 / r^17) in Horner form in r^2.  Plain IEEE operations without FMA, so
+ * the CPU oracle and the CUDA kernels produce the same bits; |x| < 2^20 pi/2
+ * keeps k*head exact.  Used for the surface-tension cosine (∂v∂tpF!). */
+GC_INLINE double gc_cos(double x) {
+  const double PIO2_HI = 1.5707963267341256;    /* 0x3FF921FB54400000 */
+  const double PIO2_LO = 6.077100506506192e-11; /* pi/2 - PIO2_HI */
+  const double INV_PIO2 = 0.6366197723675814;
+  double kd = floor(x * INV_PIO2 + 0.5);
+  double r = (x - kd * PIO2_HI) - kd * PIO2_LO;
+  double z = r * r;
+  double c = 1.0 + z * (-0.5 + z * (0.041666666666666664 + z * (-0.001388888888888889 +
+             z * (2.48015873015873e-05 + z * (-2.755731922398589e-07 + z * (2.08767569878681e-09 +
+             z * (-1.1470745597729725e-11 + z * 4.779477332387385e-14)))))));
+  double s = r + r * z * (-0.16666666666666666 + z * (0.008333333333333333 + z * (-0.0001984126984126984 +
+             z * (2.7557319223985893e-06 + z * (-2.505210838544172e-08 + z * (1.6059043836821613e-10 +
+             z * (-7.647163731819816e-13 + z * 2.8114572543455206e-15)))))));
+  long long k = (long long)kd;
+  switch ((int)(k & 3)) {
+    case 0: return c;
+    case 1: return -s;
+    case 2: return -c;
+    default: return s;
+  }
+}
+
 // Float64 ^ Int of the Tait EOS: gamma == 7 as ((x2*x2)*x2)*x, otherwise
 // left-to-right products (same sequence as the oracle).
 __host__ __device__ inline double ipow(double x, int n) {

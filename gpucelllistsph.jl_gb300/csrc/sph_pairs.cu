@@ -275,7 +275,7 @@ __global__ void k_fn_pF(int64_t P, const int32_t* __restrict__ pairs, V3 x, doub
   for (int d = 0; d < D; ++d) dx[d] = x.p[d][i] - x.p[d][j];
   double r = sqrt(dotp<D>(dx, dx));
   if (r < 2.0 * h) {
-    double scos = s * cos((1.5 * GCSPH_PI64) * r / (2.0 * h)) / (r + 0.1 * h);
+    double scos = s * gc_cos((1.5 * GCSPH_PI64) * r / (2.0 * h)) / (r + 0.1 * h);
     double f[D];
 #pragma unroll
     for (int d = 0; d < D; ++d) f[d] = scos * dx[d] / m0;

@@ -164,7 +164,7 @@ template <int D>
 __device__ inline void pf_term(const StepConst& c, Acc<D>& A, int ptk, int ptm, const double* dx, double r) {
   if (!(ptk > 0 && ptm > 0)) return;
   if (r < c.twoh) {
-    double scos = c.s * cos(c.pfc * r / c.twoh) / (r + c.hp1);
+    double scos = c.s * gc_cos(c.pfc * r / c.twoh) / (r + c.hp1);
 #pragma unroll
     for (int d = 0; d < D; ++d) A.pf[d] += scos * dx[d] / c.m0;
   }
@@ -215,7 +215,7 @@ __global__ void __launch_bounds__(STPB) k_stage1(StepConst c, const Scal* __rest
     for (int d = 0; d < D; ++d) { gw[d] = dx[d] * dwk_r; S.gWe[d][e] = gw[d]; }
     const int ptm = S.pt[m];
     const double rm = S.rho[m];
-    drho += ddt_term<D>(c, ptk, ptm, dx, r2, gw, dv, rk, rm);
+    if (ptk > 0 && ptm > 0) drho += ddt_term<D>(c, ptk, ptm, dx, r2, gw, dv, rk, rm);
     mom_terms<D>(c, A, ptk, ptm, dx, r2, gw, dv, rk, rm, Pk, S.P1[m]);
     fb_term<D>(c, A, ptk, ptm, dx, r2);
     if (c.use_pF) pf_term<D>(c, A, ptk, ptm, dx, r);
@@ -267,7 +267,7 @@ __global__ void __launch_bounds__(STPB) k_stage2(StepConst c, Scal* __restrict__
       const double r2 = dotD<D>(dx, dx);
       const int ptm = S.pt[m];
       const double rm = S.rhoh[m];
-      drho += ddt_term<D>(c, ptk, ptm, dx, r2, gw, dv, rk, rm);
+      if (ptk > 0 && ptm > 0) drho += ddt_term<D>(c, ptk, ptm, dx, r2, gw, dv, rk, rm);
       mom_terms<D>(c, A, ptk, ptm, dx, r2, gw, dv, rk, rm, Pk, S.P2[m]);
       if ((ptk > 0) != (ptm > 0)) {
 #pragma unroll

@@ -122,6 +122,35 @@ ORC_API double orc_powfancy7th(double x, double ginv, int32_t gamma) {
     return pow(x, ginv);
 }
 
+#define GC_INLINE static inline
+/* cos(x) by Cody-Waite reduction modulo pi/2 (pi/2 split into a 33-bit head
+ * and its tail) and the Taylor series of cos / sin on |r| <= pi/4 (terms to
+ * r^16 / r^17) in Horner form in r^2.  Plain IEEE operations without FMA, so
+ * the CPU oracle and the CUDA kernels produce the same bits; |x| < 2^20 pi/2
+ * keeps k*head exact.  Used for the surface-tension cosine (∂v∂tpF!). */
+GC_INLINE double gc_cos(double x) {
+  const double PIO2_HI = 1.5707963267341256;    /* 0x3FF921FB54400000 */
+  const double PIO2_LO = 6.077100506506192e-11; /* pi/2 - PIO2_HI */
+  const double INV_PIO2 = 0.6366197723675814;
+  double kd = floor(x * INV_PIO2 + 0.5);
+  double r = (x - kd * PIO2_HI) - kd * PIO2_LO;
+  double z = r * r;
+  double c = 1.0 + z * (-0.5 + z * (0.041666666666666664 + z * (-0.001388888888888889 +
+             z * (2.48015873015873e-05 + z * (-2.755731922398589e-07 + z * (2.08767569878681e-09 +
+             z * (-1.1470745597729725e-11 + z * 4.779477332387385e-14)))))));
+  double s = r + r * z * (-0.16666666666666666 + z * (0.008333333333333333 + z * (-0.0001984126984126984 +
+             z * (2.7557319223985893e-06 + z * (-2.505210838544172e-08 + z * (1.6059043836821613e-10 +
+             z * (-7.647163731819816e-13 + z * 2.8114572543455206e-15)))))));
+  long long k = (long long)kd;
+  switch ((int)(k & 3)) {
+    case 0: return c;
+    case 1: return -s;
+    case 2: return -c;
+    default: return s;
+  }
+}
+ORC_API double orc_cos(double x) { return gc_cos(x); }
+
 /* Float64 ^ Int as used by the Tait EOS (src/gpukernels_sph.jl:696).  The   */
 /* reference's device lowering lives in CUDA.jl (not vendored); here: gamma  */
 /* == 7 as x2=x*x, x4=x2*x2, x6=x4*x2, x7=x6*x, other gamma by left-to-right */
@@ -696,7 +725,7 @@ static void body_pF(int64_t p, double *const *acc, const void *vc) {
     for (int d = 0; d < D; ++d) dx[d] = c->x[(int64_t)d * N + i] - c->x[(int64_t)d * N + j];
     double r = sqrt(dotv(D, dx, dx));
     if (r < 2.0 * c->h) {
-        double scos = c->s * cos((1.5 * PI64) * r / (2.0 * c->h)) / (r + 0.1 * c->h);
+        double scos = c->s * gc_cos((1.5 * PI64) * r / (2.0 * c->h)) / (r + 0.1 * c->h);
         for (int d = 0; d < D; ++d) {
             double f = scos * dx[d] / c->m0;
             acc[d][i] += f;
@@ -929,6 +958,47 @@ typedef struct {
 
 static void *xmalloc(size_t n) { void *p = calloc(n ? n : 1, 1); return p; }
 
+/* Canonical pair order used for the oracle's summations.  The reference's
+ * pair list order is whatever its atomics produced (unspecified); the oracle
+ * fixes it: particles ranked by (cell key, index), pairs sorted by
+ * (lower rank, higher rank).  A serial scatter over this list adds each
+ * particle's pair terms in ascending partner rank -- the same order the
+ * CUDA gather walks its neighbour rows -- so both sum in the same order. */
+static const int64_t *g_rank_for_cmp;
+static int cmp_key_index(const void *a, const void *b) {
+    const int64_t *x = (const int64_t *)a, *y = (const int64_t *)b;
+    if (x[0] != y[0]) return x[0] < y[0] ? -1 : 1;
+    return x[1] < y[1] ? -1 : (x[1] > y[1]);
+}
+static int cmp_pair_rank(const void *a, const void *b) {
+    const int32_t *p = (const int32_t *)a, *q = (const int32_t *)b;
+    int64_t ra = g_rank_for_cmp[p[0] - 1], rb = g_rank_for_cmp[p[1] - 1];
+    int64_t sa = g_rank_for_cmp[q[0] - 1], sb = g_rank_for_cmp[q[1] - 1];
+    int64_t lo1 = ra < rb ? ra : rb, hi1 = ra < rb ? rb : ra;
+    int64_t lo2 = sa < sb ? sa : sb, hi2 = sa < sb ? sb : sa;
+    if (lo1 != lo2) return lo1 < lo2 ? -1 : 1;
+    return hi1 < hi2 ? -1 : (hi1 > hi2);
+}
+ORC_API void orc_canonical_pair_order(int D, int64_t N, const int32_t *pcell, const int64_t *cell, int32_t *pairs,
+                                      int64_t P) {
+    int64_t *ki = (int64_t *)malloc(sizeof(int64_t) * 2 * (size_t)(N > 0 ? N : 1));
+    int64_t *rank = (int64_t *)malloc(sizeof(int64_t) * (size_t)(N > 0 ? N : 1));
+    for (int64_t i = 0; i < N; ++i) {
+        int64_t key = (pcell[i] - 1) + cell[0] * ((pcell[N + i] - 1) + cell[1] * (D == 3 ? (pcell[2 * N + i] - 1) : 0));
+        ki[2 * i] = key;
+        ki[2 * i + 1] = i;
+    }
+    qsort(ki, (size_t)N, 2 * sizeof(int64_t), cmp_key_index);
+    for (int64_t r = 0; r < N; ++r) rank[ki[2 * r + 1]] = r;
+    g_rank_for_cmp = rank;
+    int64_t nz = 0;
+    while (nz < P && pairs[2 * nz] != 0) ++nz;
+    qsort(pairs, (size_t)nz, 2 * sizeof(int32_t), cmp_pair_rank);
+    g_rank_for_cmp = NULL;
+    free(ki);
+    free(rank);
+}
+
 /* update!, src/celllist.jl:95-134 (capacity policy included) */
 static void sys_update_impl(OrcSys *S) {
     int D = S->D; int64_t N = S->N;
@@ -949,6 +1019,7 @@ static void sys_update_impl(OrcSys *S) {
         S->pairs = (int32_t *)xmalloc(sizeof(int32_t) * 2 * (size_t)S->cap);
         S->pairsn = orc_neib_search(D, N, S->x, S->pcell, S->cell, S->dist, S->pairs, S->cap);
     }
+    orc_canonical_pair_order(D, N, S->pcell, S->cell, S->pairs, S->pairsn < S->cap ? S->pairsn : S->cap);
 }
 
 /* GPUCellList(points, cellsize, dist) + SPHProblem(...), src/celllist.jl:22-88, */
@@ -977,6 +1048,7 @@ ORC_API void *orc_sys_create(int D, int64_t N, const double *x, const double *ce
         free(S->pairs);
         S->pairs = np; S->cap = nc;
     }
+    orc_canonical_pair_order(D, N, S->pcell, S->cell, S->pairs, S->pairsn < S->cap ? S->pairsn : S->cap);
     S->rho = (double *)xmalloc(sizeof(double) * N); memcpy(S->rho, rho, sizeof(double) * N);
     S->rhoh = (double *)xmalloc(sizeof(double) * N); memcpy(S->rhoh, rho, sizeof(double) * N);
     S->v = (double *)xmalloc(sizeof(double) * dn);
@@ -1025,6 +1097,9 @@ ORC_API void orc_sys_stepsolve(void *hs, int32_t n, int timestepping, double tmi
     int32_t cspmcorrn = 0;
     double kernlim = orc_dpckernlim(D);
     double Hinv = 1.0 / p->H;
+    double *tmp = (double *)xmalloc(sizeof(double) * dn);
+#define ZT(t) (memset((t), 0, sizeof(double) * dn), (t))
+#define FOLD(a, t) do { for (size_t q_ = 0; q_ < dn; ++q_) (a)[q_] = (a)[q_] + (t)[q_]; } while (0)
     for (int32_t it = 0; it < n; ++it) {
         cspmcorrn += 1;
         if (!skipupdate) {
@@ -1048,12 +1123,23 @@ ORC_API void orc_sys_stepsolve(void *hs, int32_t n, int timestepping, double tmi
         orc_drhodt_ddt(D, N, P, pr, S->gW, S->rho, S->v, x, p->h, p->m0, p->rho0, p->c0, p->gamma, p->g,
                        p->delta, S->ptype, S->drhodt);
         orc_pressure(N, S->rho, p->c0, p->gamma, p->rho0, S->ptype, S->P);
-        orc_dvdt(D, N, P, pr, S->gW, S->P, p->m0, S->rho, S->ptype, S->a);
-        orc_dvdt_av(D, N, P, pr, S->gW, x, p->h, S->rho, p->alpha, S->v, p->c0, p->m0, S->ptype, S->a);
-        if (p->nu > 0) orc_dvdt_visc(D, N, P, pr, S->gW, S->v, S->rho, x, p->h, p->m0, p->nu, S->ptype, S->a);
+        /* each kernel's pair terms are summed per particle into a zeroed
+           accumulator and added to ∑∂v∂t in the reference's kernel order */
+        orc_dvdt(D, N, P, pr, S->gW, S->P, p->m0, S->rho, S->ptype, ZT(tmp));
+        FOLD(S->a, tmp);
+        orc_dvdt_av(D, N, P, pr, S->gW, x, p->h, S->rho, p->alpha, S->v, p->c0, p->m0, S->ptype, ZT(tmp));
+        FOLD(S->a, tmp);
+        if (p->nu > 0) {
+            orc_dvdt_visc(D, N, P, pr, S->gW, S->v, S->rho, x, p->h, p->m0, p->nu, S->ptype, ZT(tmp));
+            FOLD(S->a, tmp);
+        }
         orc_addgrav(D, N, p->g, S->a);
-        orc_fbmolforce(D, N, P, pr, x, 0.4, 2.0 * p->dx, S->ptype, S->a);
-        if (p->s > 0) orc_dvdt_pF(D, N, P, pr, x, p->s, p->h, p->m0, S->ptype, S->a);
+        orc_fbmolforce(D, N, P, pr, x, 0.4, 2.0 * p->dx, S->ptype, ZT(tmp));
+        FOLD(S->a, tmp);
+        if (p->s > 0) {
+            orc_dvdt_pF(D, N, P, pr, x, p->s, p->h, p->m0, S->ptype, ZT(tmp));
+            FOLD(S->a, tmp);
+        }
         orc_update_rho(N, S->rhoh, S->drhodt, p->dt * 0.5, p->rho0, S->ptype);
         orc_update_v(D, N, S->vh, S->a, p->dt * 0.5, S->ptype);
         orc_update_x(D, N, S->xh, S->vh, p->dt * 0.5);
@@ -1061,13 +1147,21 @@ ORC_API void orc_sys_stepsolve(void *hs, int32_t n, int timestepping, double tmi
         orc_drhodt_ddt(D, N, P, pr, S->gW, S->rhoh, S->vh, S->xh, p->h, p->m0, p->rho0, p->c0, p->gamma,
                        p->g, p->delta, S->ptype, S->drhodt);
         orc_pressure(N, S->rhoh, p->c0, p->gamma, p->rho0, S->ptype, S->P);
-        orc_dvdt(D, N, P, pr, S->gW, S->P, p->m0, S->rhoh, S->ptype, S->a);
-        orc_dvdt_av(D, N, P, pr, S->gW, S->xh, p->h, S->rhoh, p->alpha, S->vh, p->c0, p->m0, S->ptype, S->a);
-        if (p->nu > 0)
-            orc_dvdt_visc(D, N, P, pr, S->gW, S->vh, S->rhoh, S->xh, p->h, p->m0, p->nu, S->ptype, S->a);
+        orc_dvdt(D, N, P, pr, S->gW, S->P, p->m0, S->rhoh, S->ptype, ZT(tmp));
+        FOLD(S->a, tmp);
+        orc_dvdt_av(D, N, P, pr, S->gW, S->xh, p->h, S->rhoh, p->alpha, S->vh, p->c0, p->m0, S->ptype, ZT(tmp));
+        FOLD(S->a, tmp);
+        if (p->nu > 0) {
+            orc_dvdt_visc(D, N, P, pr, S->gW, S->vh, S->rhoh, S->xh, p->h, p->m0, p->nu, S->ptype, ZT(tmp));
+            FOLD(S->a, tmp);
+        }
         orc_addgrav(D, N, p->g, S->a);
-        orc_fbmolforce(D, N, P, pr, x, p->bound_D, p->bound_l, S->ptype, S->a);
-        if (p->s > 0) orc_dvdt_pF(D, N, P, pr, S->xh, p->s, p->h, p->m0, S->ptype, S->a);
+        orc_fbmolforce(D, N, P, pr, x, p->bound_D, p->bound_l, S->ptype, ZT(tmp));
+        FOLD(S->a, tmp);
+        if (p->s > 0) {
+            orc_dvdt_pF(D, N, P, pr, S->xh, p->s, p->h, p->m0, S->ptype, ZT(tmp));
+            FOLD(S->a, tmp);
+        }
         orc_symplectic(D, N, S->rho, S->rhoh, S->v, S->vh, x, S->xh, S->drhodt, S->a, p->dt, S->cdx, p->rho0,
                        S->ptype);
         if (p->dpc_l0 > 0) {
@@ -1091,6 +1185,9 @@ ORC_API void orc_sys_stepsolve(void *hs, int32_t n, int timestepping, double tmi
         p->etime += p->dt;
         if (timestepping) p->dt = orc_dt_stepping(D, N, S->a, S->v, x, p->c0, p->h, p->CFL, tmin, tmax);
     }
+    free(tmp);
+#undef ZT
+#undef FOLD
     memset(S->sumW, 0, sizeof(double) * N);
     memset(S->sumgW, 0, sizeof(double) * dn);
     orc_sphsumW(D, N, S->pairsn, S->pairs, S->x, Hinv, S->ptype, S->sumW);
@@ -1138,6 +1235,7 @@ ORC_API void orc_sys_partialupdate(void *hs, int fillzero) {
     OrcSys *S = (OrcSys *)hs;
     if (fillzero) memset(S->pairs, 0, sizeof(int32_t) * 2 * (size_t)S->cap);
     S->pairsn = orc_neib_search(S->D, S->N, S->x, S->pcell, S->cell, S->dist, S->pairs, S->cap);
+    orc_canonical_pair_order(S->D, S->N, S->pcell, S->cell, S->pairs, S->pairsn < S->cap ? S->pairsn : S->cap);
 }
 ORC_API void orc_sys_update(void *hs) { sys_update_impl((OrcSys *)hs); }
 ORC_API void orc_sys_set_x(void *hs, const double *x) {

@@ -58,6 +58,20 @@ def test_powfancy7th_bit_exact_and_accuracy(orc):
     assert L.orc_powfancy7th(2.0, 1 / 5, 5) == 2.0 ** (1 / 5)
 
 
+def test_own_cosine_accuracy(orc):
+    """The shared Cody-Waite + Taylor cosine (used by ∂v∂tpF! in both the
+    oracle and the CUDA kernels) is within 2 ulp of libm over the range the
+    surface-tension term uses, [0, 1.5 pi], and beyond."""
+    import ctypes as C
+    f = orc.lib().orc_cos
+    f.restype = C.c_double
+    f.argtypes = [C.c_double]
+    xs = np.concatenate([np.linspace(0, 1.5 * math.pi, 20001), np.linspace(-40, 40, 20001)])
+    for x in xs:
+        got, want = f(float(x)), math.cos(float(x))
+        assert abs(got - want) <= 2 * np.spacing(max(abs(want), 2.0 ** -30)) + 1e-17, (x, got, want)
+
+
 def test_ipow_and_dpckernlim(orc):
     L = orc.lib()
     for x in (0.9, 1.0, 1.0001, 1.7):

@@ -52,12 +52,19 @@ def gpu_field(prob, name):
     return (torch.stack(f) if isinstance(f, tuple) else f).cpu().numpy()
 
 
-def compare(prob, ref, case, fields=FIELDS, rtol=RTOL):
+def compare(prob, ref, case, fields=FIELDS, rtol=RTOL, exact=True):
+    """Contract: every field within rtol.  With exact=True also bit-identical:
+    the CUDA gather walks each neighbour row in the order the serial oracle
+    scatters over its canonically ordered pair list, with identical per-pair
+    arithmetic, so no summation-order difference is left."""
     errs = {}
     for name in fields:
         errs[name] = relerr(gpu_field(prob, name), ref.get(name))
     bad = {k: v for k, v in errs.items() if not v <= rtol}
     assert not bad, f"fields over {rtol}: {bad}"
+    if exact:
+        nonzero = {k: v for k, v in errs.items() if v != 0.0}
+        assert not nonzero, f"not bit-identical: {nonzero}"
     d_got = gpu_field(prob, "x") - case.x
     d_want = ref.get("x") - case.x
     assert relerr(d_got, d_want) <= 1e-9
