@@ -133,15 +133,22 @@ __device__ inline double r2_ref(double ax, double ay, double az, double bx, doub
   return s;
 }
 
-// MODE 0: count (full, up); MODE 1: fill nbr
-template <int D, int MODE>
+// MODE 0: count (full, up); MODE 1: fill nbr.  L lanes share one particle:
+// the candidates of each x-row are tested L at a time, and the fill keeps the
+// row ascending by compacting each round's hits with a sub-warp ballot.
+template <int D, int MODE, int L>
 __global__ void __launch_bounds__(TPB) k_pairs(const double* __restrict__ x0, const double* __restrict__ x1,
                                                const double* __restrict__ x2, const int32_t* __restrict__ skey,
                                                const int32_t* __restrict__ cellstart, int64_t N, Grid g,
                                                int32_t* __restrict__ cnt_full, int32_t* __restrict__ cnt_up,
                                                const int64_t* __restrict__ rs_full, int32_t* __restrict__ nbr) {
-  int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= N) return;
+  const int64_t gt = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t k = gt / L;
+  const int lane = (int)(gt % L);
+  if (k >= N) return;  // the whole sub-group leaves together
+  const unsigned lanew = threadIdx.x & 31u;
+  const unsigned gbase = lanew & ~(unsigned)(L - 1);
+  const unsigned gm = L == 32 ? 0xffffffffu : (((1u << L) - 1u) << gbase);
   const int nx = g.nc[0], ny = g.nc[1], nz = D == 3 ? g.nc[2] : 1;
   int32_t key = skey[k];
   int cx = key % nx;
@@ -161,23 +168,34 @@ __global__ void __launch_bounds__(TPB) k_pairs(const double* __restrict__ x0, co
       if (y < 0 || y >= ny) continue;
       int64_t base = (int64_t)nx * ((int64_t)y + (int64_t)ny * z);
       int32_t m0 = cellstart[base + xlo], m1 = cellstart[base + xhi + 1];
-      for (int32_t m = m0; m < m1; ++m) {
-        if (m == k) continue;
-        double r2 = r2_ref<D>(ax, ay, az, x0[m], x1[m], D == 3 ? x2[m] : 0.0);
-        if (r2 < g.dist2) {
-          if (MODE == 0) {
-            ++nf;
-            nu += (m > k);
-          } else {
-            nbr[wpos++] = m;
-          }
+      for (int32_t mb = m0; mb < m1; mb += L) {
+        const int32_t m = mb + lane;
+        bool hit = false;
+        if (m < m1 && m != k) {
+          double r2 = r2_ref<D>(ax, ay, az, x0[m], x1[m], D == 3 ? x2[m] : 0.0);
+          hit = r2 < g.dist2;
+        }
+        if (MODE == 0) {
+          nf += hit;
+          nu += hit && (m > k);
+        } else {
+          const unsigned bal = (__ballot_sync(gm, hit) >> gbase) & (L == 32 ? 0xffffffffu : ((1u << L) - 1u));
+          if (hit) nbr[wpos + __popc(bal & ((1u << lane) - 1u))] = m;
+          wpos += __popc(bal);
         }
       }
     }
   }
   if (MODE == 0) {
-    cnt_full[k] = nf;
-    cnt_up[k] = nu;
+#pragma unroll
+    for (int o = L / 2; o > 0; o >>= 1) {
+      nf += __shfl_xor_sync(gm, nf, o);
+      nu += __shfl_xor_sync(gm, nu, o);
+    }
+    if (lane == 0) {
+      cnt_full[k] = nf;
+      cnt_up[k] = nu;
+    }
   }
 }
 
@@ -363,16 +381,47 @@ int CellCore::gather_positions_by_orig(const double* const* xorig, double* const
   return GCSPH_OK;
 }
 
+// lanes per particle in the pair search: about 8 candidates per lane
+int CellCore::pair_lanes() const {
+  if (lanes > 0) return lanes;
+  double per_cell = (double)N / (double)g.ncell;
+  double cand = per_cell * (D == 3 ? 27.0 : 9.0);
+  int L = 1;
+  while (L < 32 && (double)L * 8.0 < cand) L <<= 1;
+  return L;
+}
+
+#define PAIRS_LAUNCH(MODE, L, ...)                                                               \
+  do {                                                                                           \
+    const int _g = nblocks(N * (int64_t)(L), TPB);                                               \
+    if (D == 2) {                                                                                \
+      switch (L) {                                                                               \
+        case 1: k_pairs<2, MODE, 1><<<_g, TPB, 0, st>>>(__VA_ARGS__); break;                     \
+        case 2: k_pairs<2, MODE, 2><<<_g, TPB, 0, st>>>(__VA_ARGS__); break;                     \
+        case 4: k_pairs<2, MODE, 4><<<_g, TPB, 0, st>>>(__VA_ARGS__); break;                     \
+        case 8: k_pairs<2, MODE, 8><<<_g, TPB, 0, st>>>(__VA_ARGS__); break;                     \
+        case 16: k_pairs<2, MODE, 16><<<_g, TPB, 0, st>>>(__VA_ARGS__); break;                   \
+        default: k_pairs<2, MODE, 32><<<_g, TPB, 0, st>>>(__VA_ARGS__); break;                   \
+      }                                                                                          \
+    } else {                                                                                     \
+      switch (L) {                                                                               \
+        case 1: k_pairs<3, MODE, 1><<<_g, TPB, 0, st>>>(__VA_ARGS__); break;                     \
+        case 2: k_pairs<3, MODE, 2><<<_g, TPB, 0, st>>>(__VA_ARGS__); break;                     \
+        case 4: k_pairs<3, MODE, 4><<<_g, TPB, 0, st>>>(__VA_ARGS__); break;                     \
+        case 8: k_pairs<3, MODE, 8><<<_g, TPB, 0, st>>>(__VA_ARGS__); break;                     \
+        case 16: k_pairs<3, MODE, 16><<<_g, TPB, 0, st>>>(__VA_ARGS__); break;                   \
+        default: k_pairs<3, MODE, 32><<<_g, TPB, 0, st>>>(__VA_ARGS__); break;                   \
+      }                                                                                          \
+    }                                                                                            \
+  } while (0)
+
 int CellCore::build_pairs(const double* const* xs) {
   if (!sorted) return fail(GCSPH_ESTATE, "pair build before binning");
   const double* x2 = D == 3 ? xs[2] : xs[0];
   timer_begin(T_PAIRS, st);
-  if (D == 2)
-    k_pairs<2, 0><<<nblocks(N, TPB), TPB, 0, st>>>(xs[0], xs[1], x2, skey.as<int32_t>(), cellstart.as<int32_t>(), N, g,
-                                                    cnt_full.as<int32_t>(), cnt_up.as<int32_t>(), nullptr, nullptr);
-  else
-    k_pairs<3, 0><<<nblocks(N, TPB), TPB, 0, st>>>(xs[0], xs[1], x2, skey.as<int32_t>(), cellstart.as<int32_t>(), N, g,
-                                                    cnt_full.as<int32_t>(), cnt_up.as<int32_t>(), nullptr, nullptr);
+  const int L = pair_lanes();
+  PAIRS_LAUNCH(0, L, xs[0], xs[1], x2, skey.as<int32_t>(), cellstart.as<int32_t>(), N, g, cnt_full.as<int32_t>(),
+               cnt_up.as<int32_t>(), nullptr, nullptr);
   GC_LAUNCHED();
   int rc = exclusive_scan_i32_to_i64(cnt_full.as<int32_t>(), rs_full.as<int64_t>(), N, scratch.as<int64_t>(), st);
   if (rc) return rc;
@@ -391,12 +440,8 @@ int CellCore::build_pairs(const double* const* xs) {
     nbr_cap = want;
   }
   timer_begin(T_PAIRS, st);
-  if (D == 2)
-    k_pairs<2, 1><<<nblocks(N, TPB), TPB, 0, st>>>(xs[0], xs[1], x2, skey.as<int32_t>(), cellstart.as<int32_t>(), N, g,
-                                                    nullptr, nullptr, rs_full.as<int64_t>(), nbr.as<int32_t>());
-  else
-    k_pairs<3, 1><<<nblocks(N, TPB), TPB, 0, st>>>(xs[0], xs[1], x2, skey.as<int32_t>(), cellstart.as<int32_t>(), N, g,
-                                                    nullptr, nullptr, rs_full.as<int64_t>(), nbr.as<int32_t>());
+  PAIRS_LAUNCH(1, L, xs[0], xs[1], x2, skey.as<int32_t>(), cellstart.as<int32_t>(), N, g, nullptr, nullptr,
+               rs_full.as<int64_t>(), nbr.as<int32_t>());
   GC_LAUNCHED();
   timer_end(T_PAIRS, st);
   built = true;

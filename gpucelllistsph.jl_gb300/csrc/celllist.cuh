@@ -38,6 +38,8 @@ struct CellCore {
   int64_t* pin = nullptr;  // pinned host scalars
   int64_t nfull = 0, nup = 0, nbr_cap = 0;
   bool sorted = false, built = false;
+  int lanes = 0;  // lanes per particle in the pair search; 0 = by mean candidate count
+  int pair_lanes() const;
 
   int init(int D_, int64_t N_, const double* cellsize, double dist_, const double* MIN, const double* MAX,
            const double* const* xin, cudaStream_t s);

@@ -185,12 +185,49 @@ __device__ inline void finish_acc(const StepConst& c, const Acc<D>& A, double* a
 }
 
 // ---------------------------------------------------------------------------
+// Sub-warp cooperation: L lanes (1, 2, 4, 8, 16 or 32) share one particle.
+// Lane l walks row entries e0+l, e0+l+L, ...; the per-lane partial sums are
+// combined by a butterfly (xor offsets L/2 .. 1), after which every lane
+// holds the same total.  L = 1 is the serial row order -- the order the
+// oracle's scatter over its canonically ordered pair list produces -- so it
+// reproduces the oracle bit for bit; L > 1 re-associates the sums (within
+// the FP64 contract) and fills the GPU when particles are few.
+// ---------------------------------------------------------------------------
+template <int L>
+__device__ inline unsigned group_mask() {
+  if (L == 32) return 0xffffffffu;
+  const unsigned lanew = threadIdx.x & 31u;
+  return ((1u << L) - 1u) << (lanew & ~(unsigned)(L - 1));
+}
+template <int L>
+__device__ inline double group_sum(double v, unsigned gm) {
+#pragma unroll
+  for (int o = L / 2; o > 0; o >>= 1) v = v + __shfl_xor_sync(gm, v, o);
+  return v;
+}
+template <int D, int L>
+__device__ inline void group_sum_acc(Acc<D>& A, const StepConst& c, unsigned gm) {
+  if (L == 1) return;
+#pragma unroll
+  for (int d = 0; d < D; ++d) {
+    A.p[d] = group_sum<L>(A.p[d], gm);
+    A.av[d] = group_sum<L>(A.av[d], gm);
+    if (c.use_visc) A.vi[d] = group_sum<L>(A.vi[d], gm);
+    A.fb[d] = group_sum<L>(A.fb[d], gm);
+    if (c.use_pF) A.pf[d] = group_sum<L>(A.pf[d], gm);
+  }
+}
+
+// ---------------------------------------------------------------------------
 // stage 1 at (x, ρ, v) + predictors
 // ---------------------------------------------------------------------------
-template <int D>
+template <int D, int L>
 __global__ void __launch_bounds__(STPB) k_stage1(StepConst c, const Scal* __restrict__ sc, int64_t N, SArr<D> S) {
-  int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= N) return;
+  const int64_t gt = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t k = gt / L;
+  const int lane = (int)(gt % L);
+  if (k >= N) return;  // whole sub-group leaves together
+  const unsigned gm = group_mask<L>();
   const double dt = sc->dt;
   double xk[D], vk[D];
 #pragma unroll
@@ -201,7 +238,7 @@ __global__ void __launch_bounds__(STPB) k_stage1(StepConst c, const Scal* __rest
   Acc<D> A;
   A.zero();
   const int64_t e0 = S.rs[k], e1 = S.rs[k + 1];
-  for (int64_t e = e0; e < e1; ++e) {
+  for (int64_t e = e0 + lane; e < e1; e += L) {
     const int32_t m = S.nbr[e];
     double dx[D], dv[D], gw[D];
 #pragma unroll
@@ -220,6 +257,9 @@ __global__ void __launch_bounds__(STPB) k_stage1(StepConst c, const Scal* __rest
     fb_term<D>(c, A, ptk, ptm, dx, r2);
     if (c.use_pF) pf_term<D>(c, A, ptk, ptm, dx, r);
   }
+  drho = group_sum<L>(drho, gm);
+  group_sum_acc<D, L>(A, c, gm);
+  if (lane != 0) return;
   double a[D];
   finish_acc<D>(c, A, a);
   // update_ρp∂ρ∂tΔt!, update_vp∂v∂tΔt!, update_xpvΔt! (:1088-1169), Δt/2
@@ -240,11 +280,14 @@ __global__ void __launch_bounds__(STPB) k_stage1(StepConst c, const Scal* __rest
 // ---------------------------------------------------------------------------
 // stage 2 at (xΔt½, ρΔt½, vΔt½) with stage-1 ∇W, + symplectic_update!
 // ---------------------------------------------------------------------------
-template <int D>
+template <int D, int L>
 __global__ void __launch_bounds__(STPB) k_stage2(StepConst c, Scal* __restrict__ sc, int64_t N, SArr<D> S) {
-  int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t gt = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t k = gt / L;
+  const int lane = (int)(gt % L);
   double mc = 0.0;
   if (k < N) {
+    const unsigned gm = group_mask<L>();
     const double dt = sc->dt;
     double xk[D], xhk[D], vhk[D];
 #pragma unroll
@@ -255,7 +298,7 @@ __global__ void __launch_bounds__(STPB) k_stage2(StepConst c, Scal* __restrict__
     Acc<D> A;
     A.zero();
     const int64_t e0 = S.rs[k], e1 = S.rs[k + 1];
-    for (int64_t e = e0; e < e1; ++e) {
+    for (int64_t e = e0 + lane; e < e1; e += L) {
       const int32_t m = S.nbr[e];
       double dx[D], dv[D], gw[D], dxf[D];
 #pragma unroll
@@ -276,32 +319,36 @@ __global__ void __launch_bounds__(STPB) k_stage2(StepConst c, Scal* __restrict__
       }
       if (c.use_pF) pf_term<D>(c, A, ptk, ptm, dx, sqrt(r2));
     }
-    double a[D];
-    finish_acc<D>(c, A, a);
-    S.drho[k] = drho;
-    S.Plast[k] = Pk;
-    // symplectic_update!, :1204-1245
-    const double epsi = -(drho / rk) * dt;
-    double rv = S.rho[k] * (2.0 - epsi) / (2.0 + epsi);
-    if (rv < c.rho0 && ptk <= 1) rv = c.rho0;
-    S.rho[k] = rv;
-    S.rhoho[k] = rv;
-    S.P1[k] = eos(rv, c.gamma, c.rho0, c.P0, ptk);
-    const double ml = ptk > 1 ? 1.0 : 0.0;
+    drho = group_sum<L>(drho, gm);
+    group_sum_acc<D, L>(A, c, gm);
+    if (lane == 0) {
+      double a[D];
+      finish_acc<D>(c, A, a);
+      S.drho[k] = drho;
+      S.Plast[k] = Pk;
+      // symplectic_update!, :1204-1245
+      const double epsi = -(drho / rk) * dt;
+      double rv = S.rho[k] * (2.0 - epsi) / (2.0 + epsi);
+      if (rv < c.rho0 && ptk <= 1) rv = c.rho0;
+      S.rho[k] = rv;
+      S.rhoho[k] = rv;
+      S.P1[k] = eos(rv, c.gamma, c.rho0, c.P0, ptk);
+      const double ml = ptk > 1 ? 1.0 : 0.0;
 #pragma unroll
-    for (int d = 0; d < D; ++d) {
-      S.a[d][k] = a[d];
-      const double vv = S.v[d][k];
-      const double nv = vv + a[d] * dt * ml;
-      S.vho[d][k] = nv;
-      S.v[d][k] = nv;
-      const double ddx = (vv + nv) * 0.5 * dt;
-      const double cd = S.cdx[d][k] + ddx;
-      S.cdx[d][k] = cd;
-      mc = fmax(mc, fabs(cd));
-      const double xv = xk[d] + ddx;
-      S.xho[d][k] = xv;
-      S.xo[d][k] = xv;
+      for (int d = 0; d < D; ++d) {
+        S.a[d][k] = a[d];
+        const double vv = S.v[d][k];
+        const double nv = vv + a[d] * dt * ml;
+        S.vho[d][k] = nv;
+        S.v[d][k] = nv;
+        const double ddx = (vv + nv) * 0.5 * dt;
+        const double cd = S.cdx[d][k] + ddx;
+        S.cdx[d][k] = cd;
+        mc = fmax(mc, fabs(cd));
+        const double xv = xk[d] + ddx;
+        S.xho[d][k] = xv;
+        S.xo[d][k] = xv;
+      }
     }
   }
   // maximum(maximum.(abs, cΔx)), src/sphproblem.jl:325
@@ -319,10 +366,13 @@ __global__ void __launch_bounds__(STPB) k_stage2(StepConst c, Scal* __restrict__
 // ---------------------------------------------------------------------------
 // dpcreg! + update_dpcreg!  (:1500-1553, :1617-1632)
 // ---------------------------------------------------------------------------
-template <int D>
+template <int D, int L>
 __global__ void __launch_bounds__(STPB) k_dpc(StepConst c, const Scal* __restrict__ sc, int64_t N, SArr<D> S) {
-  int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t gt = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t k = gt / L;
+  const int lane = (int)(gt % L);
   if (k >= N) return;
+  const unsigned gm = group_mask<L>();
   const double dt = sc->dt;
   double xk[D], vk[D], sum[D];
 #pragma unroll
@@ -331,7 +381,7 @@ __global__ void __launch_bounds__(STPB) k_dpc(StepConst c, const Scal* __restric
   const int ptk = S.pt[k];
   const int64_t e0 = S.rs[k], e1 = S.rs[k + 1];
   if (ptk > 0) {
-    for (int64_t e = e0; e < e1; ++e) {
+    for (int64_t e = e0 + lane; e < e1; e += L) {
       const int32_t m = S.nbr[e];
       if (!(S.pt[m] > 0)) continue;
       double dx[D], dv[D];
@@ -357,6 +407,9 @@ __global__ void __launch_bounds__(STPB) k_dpc(StepConst c, const Scal* __restric
       }
     }
   }
+#pragma unroll
+  for (int d = 0; d < D; ++d) sum[d] = group_sum<L>(sum[d], gm);
+  if (lane != 0) return;
   S.Plast[k] = Pk;
 #pragma unroll
   for (int d = 0; d < D; ++d) {
@@ -374,10 +427,13 @@ __global__ void __launch_bounds__(STPB) k_dpc(StepConst c, const Scal* __restric
 // ---------------------------------------------------------------------------
 // xsphcorr! + update_xsphcorr!  (:1757-1779, :1827-1838), stage-1 W
 // ---------------------------------------------------------------------------
-template <int D>
+template <int D, int L>
 __global__ void __launch_bounds__(STPB) k_xsph(StepConst c, const Scal* __restrict__ sc, int64_t N, SArr<D> S) {
-  int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t gt = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t k = gt / L;
+  const int lane = (int)(gt % L);
   if (k >= N) return;
+  const unsigned gm = group_mask<L>();
   const double dt = sc->dt;
   double vk[D], sum[D];
 #pragma unroll
@@ -386,7 +442,7 @@ __global__ void __launch_bounds__(STPB) k_xsph(StepConst c, const Scal* __restri
   const int ptk = S.pt[k];
   if (ptk > 1) {
     const int64_t e0 = S.rs[k], e1 = S.rs[k + 1];
-    for (int64_t e = e0; e < e1; ++e) {
+    for (int64_t e = e0 + lane; e < e1; e += L) {
       const int32_t m = S.nbr[e];
       if (!(S.pt[m] > 1)) continue;
       const double xs = c.xsph_c * S.We[e] / (rk + S.rho[m]);
@@ -394,6 +450,9 @@ __global__ void __launch_bounds__(STPB) k_xsph(StepConst c, const Scal* __restri
       for (int d = 0; d < D; ++d) sum[d] += (S.v[d][m] - vk[d]) * xs;
     }
   }
+#pragma unroll
+  for (int d = 0; d < D; ++d) sum[d] = group_sum<L>(sum[d], gm);
+  if (lane != 0) return;
 #pragma unroll
   for (int d = 0; d < D; ++d) {
     S.buf2[d][k] = sum[d];
@@ -404,16 +463,19 @@ __global__ void __launch_bounds__(STPB) k_xsph(StepConst c, const Scal* __restri
 // ---------------------------------------------------------------------------
 // cspmcorr!  (:1693-1719), stage-1 W; writes ρ to the other buffer
 // ---------------------------------------------------------------------------
-template <int D>
+template <int D, int L>
 __global__ void __launch_bounds__(STPB) k_cspm(StepConst c, int64_t N, SArr<D> S) {
-  int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t gt = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t k = gt / L;
+  const int lane = (int)(gt % L);
   if (k >= N) return;
+  const unsigned gm = group_mask<L>();
   const double rk = S.rho[k];
   const int ptk = S.pt[k];
   double s1 = 0.0, s2 = 0.0;
   if (ptk > 0) {
     const int64_t e0 = S.rs[k], e1 = S.rs[k + 1];
-    for (int64_t e = e0; e < e1; ++e) {
+    for (int64_t e = e0 + lane; e < e1; e += L) {
       const int32_t m = S.nbr[e];
       if (!(S.pt[m] > 0)) continue;
       const double w = S.We[e];
@@ -421,6 +483,9 @@ __global__ void __launch_bounds__(STPB) k_cspm(StepConst c, int64_t N, SArr<D> S
       s2 += w * c.m0 / S.rho[m];
     }
   }
+  s1 = group_sum<L>(s1, gm);
+  s2 = group_sum<L>(s2, gm);
+  if (lane != 0) return;
   double nr = s1 / s2;
   double rv = isnan(nr) ? rk : nr;
   S.rhoo[k] = rv;
@@ -470,15 +535,18 @@ __global__ void k_step_end(StepConst c, Scal* __restrict__ sc) {
 // ---------------------------------------------------------------------------
 // post-batch sph∑W! + sph∑∇W! (:139-156, :332-359) on original-order arrays
 // ---------------------------------------------------------------------------
-template <int D>
+template <int D, int L>
 __global__ void __launch_bounds__(STPB) k_sums_post(StepConst c, int64_t N, const int64_t* __restrict__ rs,
                                                      const int32_t* __restrict__ nbr, const int32_t* __restrict__ orig,
                                                      const int32_t* __restrict__ pt, const double* __restrict__ x0,
                                                      const double* __restrict__ x1, const double* __restrict__ x2,
                                                      double* __restrict__ sumW, double* __restrict__ sg0,
                                                      double* __restrict__ sg1, double* __restrict__ sg2) {
-  int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t gt = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t k = gt / L;
+  const int lane = (int)(gt % L);
   if (k >= N) return;
+  const unsigned gm = group_mask<L>();
   const double* X[3] = {x0, x1, x2};
   const int32_t o = orig[k];
   double xk[D];
@@ -488,7 +556,7 @@ __global__ void __launch_bounds__(STPB) k_sums_post(StepConst c, int64_t N, cons
   double sw = 0.0, sg[D];
 #pragma unroll
   for (int d = 0; d < D; ++d) sg[d] = 0.0;
-  for (int64_t e = rs[k]; e < rs[k + 1]; ++e) {
+  for (int64_t e = rs[k] + lane; e < rs[k + 1]; e += L) {
     const int32_t om = orig[nbr[e]];
     if ((pt[om] > 0) != rk) continue;
     double dx[D];
@@ -501,6 +569,10 @@ __global__ void __launch_bounds__(STPB) k_sums_post(StepConst c, int64_t N, cons
 #pragma unroll
     for (int d = 0; d < D; ++d) sg[d] += dx[d] * dwk_r;
   }
+  sw = group_sum<L>(sw, gm);
+#pragma unroll
+  for (int d = 0; d < D; ++d) sg[d] = group_sum<L>(sg[d], gm);
+  if (lane != 0) return;
   sumW[o] = sw;
   double* SG[3] = {sg0, sg1, sg2};
 #pragma unroll
@@ -594,6 +666,7 @@ struct sph_handle {
       GWe[3];
   int ix = 0, ixh = 0, iv = 0, ivh = 0, irho = 0, irhoh = 0;
   int64_t we_cap = 0;
+  int lanes = 0;  // lanes per particle in the pair passes; 0 = by mean row length
   DevBuf scal;
   Scal* pin = nullptr;
   bool in_cell_order = false;
@@ -739,6 +812,30 @@ static int rebuild(sph_handle* h, const StepConst& c) {
   return GCSPH_OK;
 }
 
+// L lanes per particle: one launch per pair pass, N*L threads
+#define PAIR_LAUNCH(KER, L, ...)                                                              \
+  do {                                                                                        \
+    const int _g = nblocks(h->N * (int64_t)(L), STPB);                                        \
+    switch (L) {                                                                              \
+      case 1: KER<D, 1><<<_g, STPB, 0, st>>>(__VA_ARGS__); break;                             \
+      case 2: KER<D, 2><<<_g, STPB, 0, st>>>(__VA_ARGS__); break;                             \
+      case 4: KER<D, 4><<<_g, STPB, 0, st>>>(__VA_ARGS__); break;                             \
+      case 8: KER<D, 8><<<_g, STPB, 0, st>>>(__VA_ARGS__); break;                             \
+      case 16: KER<D, 16><<<_g, STPB, 0, st>>>(__VA_ARGS__); break;                           \
+      default: KER<D, 32><<<_g, STPB, 0, st>>>(__VA_ARGS__); break;                           \
+    }                                                                                         \
+  } while (0)
+
+static int choose_lanes(const sph_handle* h) {
+  if (h->lanes > 0) return h->lanes;
+  const CellCore& core = h->cl->core;
+  double mean = h->N > 0 ? (double)core.nfull / (double)h->N : 0.0;
+  // about four neighbours per lane
+  int L = 1;
+  while (L < 32 && (double)L * 4.0 < mean) L <<= 1;
+  return L;
+}
+
 template <int D>
 static int step_impl(sph_handle* h, int32_t n, int timestepping, double tmin, double tmax, int64_t* updaten_out,
                      double* maxcdx_out) {
@@ -772,14 +869,15 @@ static int step_impl(sph_handle* h, int32_t n, int timestepping, double tmin, do
     c.fb_r0 = 2.0 * p.dx;
     c.fb_eta2 = 0.01 * (c.fb_r0 * c.fb_r0);
     timer_begin(T_STAGE1, st);
-    k_stage1<D><<<nb, STPB, 0, st>>>(c, dsc, h->N, make_arr<D>(h));
+    const int L = choose_lanes(h);
+    PAIR_LAUNCH(k_stage1, L, c, dsc, h->N, make_arr<D>(h));
     GC_LAUNCHED();
     timer_end(T_STAGE1, st);
     c.fb_d = p.bound_D;
     c.fb_r0 = p.bound_l;
     c.fb_eta2 = 0.01 * (c.fb_r0 * c.fb_r0);
     timer_begin(T_STAGE2, st);
-    k_stage2<D><<<nb, STPB, 0, st>>>(c, dsc, h->N, make_arr<D>(h));
+    PAIR_LAUNCH(k_stage2, L, c, dsc, h->N, make_arr<D>(h));
     GC_LAUNCHED();
     timer_end(T_STAGE2, st);
     h->ix ^= 1;
@@ -788,7 +886,7 @@ static int step_impl(sph_handle* h, int32_t n, int timestepping, double tmin, do
     h->irhoh ^= 1;
     if (p.dpc_l0 > 0) {
       timer_begin(T_DPC, st);
-      k_dpc<D><<<nb, STPB, 0, st>>>(c, dsc, h->N, make_arr<D>(h));
+      PAIR_LAUNCH(k_dpc, L, c, dsc, h->N, make_arr<D>(h));
       GC_LAUNCHED();
       timer_end(T_DPC, st);
       h->iv ^= 1;
@@ -796,13 +894,13 @@ static int step_impl(sph_handle* h, int32_t n, int timestepping, double tmin, do
     }
     if (p.xsph_eps > 0) {
       timer_begin(T_XSPH, st);
-      k_xsph<D><<<nb, STPB, 0, st>>>(c, dsc, h->N, make_arr<D>(h));
+      PAIR_LAUNCH(k_xsph, L, c, dsc, h->N, make_arr<D>(h));
       GC_LAUNCHED();
       timer_end(T_XSPH, st);
     }
     if (p.cspmn > 0 && cspmcnt == p.cspmn) {
       timer_begin(T_CSPM, st);
-      k_cspm<D><<<nb, STPB, 0, st>>>(c, h->N, make_arr<D>(h));
+      PAIR_LAUNCH(k_cspm, L, c, h->N, make_arr<D>(h));
       GC_LAUNCHED();
       timer_end(T_CSPM, st);
       h->irho ^= 1;
@@ -831,7 +929,8 @@ static int step_impl(sph_handle* h, int32_t n, int timestepping, double tmin, do
     const double* x2 = D == 3 ? h->cl->xuser[2] : h->cl->xuser[0];
     double* sg2 = D == 3 ? h->sumgW_o[2].as<double>() : h->sumgW_o[0].as<double>();
     timer_begin(T_POST, st);
-    k_sums_post<D><<<nb, STPB, 0, st>>>(c, h->N, core.rs_full.as<int64_t>(), core.nbr.as<int32_t>(),
+    const int L = choose_lanes(h);
+    PAIR_LAUNCH(k_sums_post, L, c, h->N, core.rs_full.as<int64_t>(), core.nbr.as<int32_t>(),
                                         core.orig.as<int32_t>(), h->pt_u, h->cl->xuser[0], h->cl->xuser[1], x2,
                                         h->sumW_o.as<double>(), h->sumgW_o[0].as<double>(),
                                         h->sumgW_o[1].as<double>(), sg2);
@@ -963,6 +1062,14 @@ int sph_set_params(sph_handle* h, const gcsph_params* prm) {
   if (!h || !prm) return fail(GCSPH_EINVAL, "null argument");
   if (prm->gamma <= 0) return fail(GCSPH_EINVAL, "gamma must be a positive integer");
   h->prm = *prm;
+  return GCSPH_OK;
+}
+
+int sph_set_lanes(sph_handle* h, int32_t lanes) {
+  if (!h) return fail(GCSPH_EINVAL, "null handle");
+  if (!(lanes == 0 || lanes == 1 || lanes == 2 || lanes == 4 || lanes == 8 || lanes == 16 || lanes == 32))
+    return fail(GCSPH_EINVAL, "lanes must be 0 (auto), 1, 2, 4, 8, 16 or 32");
+  h->lanes = lanes;
   return GCSPH_OK;
 }
 

@@ -111,6 +111,11 @@ class SPHProblem:
         else:
             object.__setattr__(self, name, value)
 
+    def set_lanes(self, lanes: int):
+        """Lanes per particle in the pair passes (0 = auto, 1 = serial row
+        order, bit-identical to the CPU oracle)."""
+        _lib.check(_lib.load().sph_set_lanes(self._h, int(lanes)))
+
     # --------------------------------------------------------------- fields
     def field(self, name: str):
         """Copy of one library field in original particle order."""

@@ -129,6 +129,14 @@ void sph_destroy(sph_handle* h);
 int sph_set_params(sph_handle* h, const gcsph_params* prm);
 int sph_get_params(const sph_handle* h, gcsph_params* prm);
 
+/* Lanes that share one particle in the pair passes (no reference
+ * counterpart; a tuning knob).  1 walks each neighbour row serially -- the
+ * summation order of a serial scatter over the canonically ordered pair list,
+ * bit-identical to the CPU oracle; 2..32 split the row across lanes and
+ * combine with a fixed butterfly (FP64 results within 1e-12 of lanes = 1).
+ * 0 (default) picks about four neighbours per lane. */
+int sph_set_lanes(sph_handle* h, int32_t lanes);
+
 /* stepsolve!(prob, n; timestepping, timelims) -- src/sphproblem.jl:204-345.
  * Returns (updaten, maxcΔxout) through the out pointers. */
 int sph_step(sph_handle* h, int32_t n, int timestepping, double tmin, double tmax, int64_t* updaten,
