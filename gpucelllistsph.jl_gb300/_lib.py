@@ -56,6 +56,8 @@ _SIGS = {
     "gcl_emit_pairs": (C.c_int, [vp, vp, i64, C.c_int, C.POINTER(i64)]),
     "gcl_cellpnum": (C.c_int, [vp, vp]),
     "gcl_maxpairs": (C.c_int, [vp, C.POINTER(i64)]),
+    "gcl_pairs_noalloc": (C.c_int, [i32, i64, PP, C.POINTER(f64), f64, C.POINTER(f64), C.POINTER(f64), vp, i64,
+                                    C.c_int, C.POINTER(i64), vp]),
     "sph_create": (C.c_int, [vp, C.POINTER(gcsph_params), vp, PP, vp, C.POINTER(vp)]),
     "sph_destroy": (None, [vp]),
     "sph_set_params": (C.c_int, [vp, C.POINTER(gcsph_params)]),

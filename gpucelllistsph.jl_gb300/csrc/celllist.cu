@@ -14,6 +14,8 @@
 // each sorted particle scans the 3^D stencil as 3^(D-1) contiguous x-rows of
 // the sorted arrays and the pairs land at scanned offsets, so the emitted list
 // is deterministic (ascending sorted index).
+#include <mutex>
+
 #include "celllist.cuh"
 
 namespace gcsph {
@@ -576,3 +578,269 @@ int gcl_maxpairs(gcl_handle* h, int64_t* out) {
 }
 
 }  // extern "C"
+
+// ===========================================================================
+// gcl_pairs_noalloc: GPUCellList + neighborlist in one call that allocates no
+// memory.  For callers that may not allocate device memory while they run --
+// a host whose own memory pool already holds the device (a Julia or PyTorch
+// process that reserved it), a plugin whose framework forbids allocation, or
+// a time-critical loop that cannot absorb cudaMalloc's implicit device
+// synchronisation.  Every intermediate array lives in one file-scope
+// __device__ arena sized for GCSPH_NOALLOC_MAX_POINTS points and
+// GCSPH_NOALLOC_MAX_CELLS grid cells; each GPU that loads this library keeps
+// that arena (24 MiB) until the process exits.  The caller passes the
+// coordinates and owns the output pair buffer.
+// ===========================================================================
+namespace gcsph {
+namespace noalloc {
+
+constexpr int64_t MAXN = GCSPH_NOALLOC_MAX_POINTS;
+constexpr int64_t MAXC = GCSPH_NOALLOC_MAX_CELLS;
+constexpr int64_t al(int64_t b) { return (b + 255) / 256 * 256; }
+constexpr int64_t tile = 2048;  // items per block of the device scan
+constexpr int64_t scan_elems(int64_t m) {
+  return ((m + tile - 1) / tile) <= 1 ? 1 : 2 * ((m + tile - 1) / tile) + 1 + scan_elems((m + tile - 1) / tile);
+}
+constexpr int MINMAX_BLOCKS = 4 * 152;
+// arena layout, byte offsets
+constexpr int64_t O_KEY = 0;
+constexpr int64_t O_SLOT = O_KEY + al(4 * MAXN);
+constexpr int64_t O_TMP = O_SLOT + al(4 * MAXN);
+constexpr int64_t O_PERM = O_TMP + al(4 * MAXN);
+constexpr int64_t O_SKEY = O_PERM + al(4 * MAXN);
+constexpr int64_t O_ORIG = O_SKEY + al(4 * MAXN);
+constexpr int64_t O_XS = O_ORIG + al(4 * MAXN);
+constexpr int64_t O_COUNT = O_XS + al(3 * 8 * MAXN);
+constexpr int64_t O_CSTART = O_COUNT + al(4 * MAXC);
+constexpr int64_t O_CFULL = O_CSTART + al(4 * (MAXC + 1));
+constexpr int64_t O_CUP = O_CFULL + al(4 * MAXN);
+constexpr int64_t O_RSUP = O_CUP + al(4 * MAXN);
+constexpr int64_t O_SCAN = O_RSUP + al(8 * (MAXN + 1));
+constexpr int64_t O_MINMAX = O_SCAN + al(8 * scan_elems((MAXC > MAXN ? MAXC : MAXN) + 1));
+constexpr int64_t BYTES = O_MINMAX + al(8 * 2 * MINMAX_BLOCKS);
+
+}  // namespace noalloc
+}  // namespace gcsph
+
+// the scratch of gcl_pairs_noalloc; host code must not use this name as a
+// device address -- it reaches the kernels through cudaGetSymbolAddress
+static __device__ __align__(256) unsigned char g_noalloc_arena[gcsph::noalloc::BYTES];
+
+namespace gcsph {
+namespace noalloc {
+
+// fill pass that writes the (min,max) 1-based pairs of each sorted particle's
+// larger-index neighbours straight into the caller's list, ascending, at the
+// scanned offset: the same list gcl_emit_pairs writes from the neighbour CSR
+template <int D, int L>
+__global__ void __launch_bounds__(TPB) k_pairs_direct(const double* __restrict__ x0, const double* __restrict__ x1,
+                                                      const double* __restrict__ x2, const int32_t* __restrict__ skey,
+                                                      const int32_t* __restrict__ cellstart,
+                                                      const int32_t* __restrict__ orig, int64_t N, Grid g,
+                                                      const int64_t* __restrict__ rs_up, int64_t cap,
+                                                      int32_t* __restrict__ pairs) {
+  const int64_t gt = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t k = gt / L;
+  const int lane = (int)(gt % L);
+  if (k >= N) return;
+  const unsigned lanew = threadIdx.x & 31u;
+  const unsigned gbase = lanew & ~(unsigned)(L - 1);
+  const unsigned gm = L == 32 ? 0xffffffffu : (((1u << L) - 1u) << gbase);
+  const int nx = g.nc[0], ny = g.nc[1], nz = D == 3 ? g.nc[2] : 1;
+  const int32_t key = skey[k];
+  const int cx = key % nx;
+  const int t = key / nx;
+  const int cy = t % ny;
+  const int cz = t / ny;
+  const double ax = x0[k], ay = x1[k], az = D == 3 ? x2[k] : 0.0;
+  const int32_t ok = orig[k] + 1;
+  int64_t wpos = rs_up[k];
+  const int xlo = cx > 0 ? cx - 1 : 0;
+  const int xhi = cx < nx - 1 ? cx + 1 : nx - 1;
+  for (int dz = (D == 3 ? -1 : 0); dz <= (D == 3 ? 1 : 0); ++dz) {
+    const int z = cz + dz;
+    if (z < 0 || z >= nz) continue;
+    for (int dy = -1; dy <= 1; ++dy) {
+      const int y = cy + dy;
+      if (y < 0 || y >= ny) continue;
+      const int64_t base = (int64_t)nx * ((int64_t)y + (int64_t)ny * z);
+      const int32_t m0 = cellstart[base + xlo], m1 = cellstart[base + xhi + 1];
+      for (int32_t mb = m0; mb < m1; mb += L) {
+        const int32_t m = mb + lane;
+        bool hit = false;
+        if (m < m1 && m > k) hit = r2_ref<D>(ax, ay, az, x0[m], x1[m], D == 3 ? x2[m] : 0.0) < g.dist2;
+        const unsigned bal = (__ballot_sync(gm, hit) >> gbase) & (L == 32 ? 0xffffffffu : ((1u << L) - 1u));
+        if (hit) {
+          const int64_t pos = wpos + __popc(bal & ((1u << lane) - 1u));
+          if (pos < cap) {
+            const int32_t om = orig[m] + 1;
+            pairs[2 * pos] = ok < om ? ok : om;
+            pairs[2 * pos + 1] = ok < om ? om : ok;
+          }
+        }
+        wpos += __popc(bal);
+      }
+    }
+  }
+}
+
+static std::mutex g_mu;
+static void* g_arena_of[128] = {nullptr};
+
+// device address of the arena on the current device; set up once per device
+static int arena(unsigned char** out) {
+  int dev = 0;
+  GC_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 128) return fail(GCSPH_EINVAL, "device ordinal %d out of range", dev);
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!g_arena_of[dev]) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_arena);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(g_noalloc_arena)", __FILE__, __LINE__);
+    g_arena_of[dev] = p;
+  }
+  *out = (unsigned char*)g_arena_of[dev];
+  return GCSPH_OK;
+}
+
+template <int D>
+static int run(int64_t N, const double* const* x, const double* cellsize, double dist, const double* MIN,
+               const double* MAX, int32_t* pairs, int64_t cap, int fillzero, int64_t* pairsn, cudaStream_t st) {
+  unsigned char* A = nullptr;
+  int rc = arena(&A);
+  if (rc) return rc;
+  int32_t* key = (int32_t*)(A + O_KEY);
+  int32_t* slot = (int32_t*)(A + O_SLOT);
+  int32_t* tmpv = (int32_t*)(A + O_TMP);
+  int32_t* perm = (int32_t*)(A + O_PERM);
+  int32_t* skey = (int32_t*)(A + O_SKEY);
+  int32_t* orig = (int32_t*)(A + O_ORIG);
+  double* xs[3] = {(double*)(A + O_XS), (double*)(A + O_XS) + MAXN, (double*)(A + O_XS) + 2 * MAXN};
+  int32_t* count = (int32_t*)(A + O_COUNT);
+  int32_t* cstart = (int32_t*)(A + O_CSTART);
+  int32_t* cfull = (int32_t*)(A + O_CFULL);
+  int32_t* cup = (int32_t*)(A + O_CUP);
+  int64_t* rsup = (int64_t*)(A + O_RSUP);
+  int64_t* scan = (int64_t*)(A + O_SCAN);
+  double* mm = (double*)(A + O_MINMAX);
+  // frozen grid, src/celllist.jl:27-46
+  const double seps = 1.4901161193847656e-08;  // sqrt(eps(Float64)) = 2^-26
+  Grid g{};
+  int64_t ncell = 1;
+  for (int d = 0; d < D; ++d) {
+    double lo, hi;
+    if (!MIN || !MAX) {
+      double host[2 * MINMAX_BLOCKS];  // pageable stack copy of the per-block partials
+      k_minmax<<<MINMAX_BLOCKS, TPB, 0, st>>>(x[d], N, mm);
+      GC_LAUNCHED();
+      GC_CUDA(cudaMemcpyAsync(host, mm, sizeof(host), cudaMemcpyDeviceToHost, st));
+      GC_CUDA(cudaStreamSynchronize(st));
+      lo = INFINITY;
+      hi = -INFINITY;
+      for (int b = 0; b < MINMAX_BLOCKS; ++b) {
+        lo = fmin(lo, host[2 * b]);
+        hi = fmax(hi, host[2 * b + 1]);
+      }
+    }
+    if (MIN) lo = MIN[d];
+    if (MAX) hi = MAX[d];
+    const double cs = cellsize[d] < dist ? dist : cellsize[d];
+    lo = lo - fabs((lo + seps) * seps);
+    const double c = ceil((hi - lo) / cs);
+    if (!(c >= 1.0) || c > 2.0e9) return fail(GCSPH_EINVAL, "degenerate grid in dim %d (CELL=%g)", d + 1, c);
+    g.offset[d] = lo;
+    g.hinv[d] = 1.0 / cs;
+    g.nc[d] = (int)c;
+    ncell *= (int64_t)c;
+    if (ncell > MAXC)
+      return fail(GCSPH_EINVAL,
+                  "gcl_pairs_noalloc: the cell grid needs more than %lld cells, the limit of its static scratch "
+                  "(use gcl_create for larger grids)",
+                  (long long)MAXC);
+  }
+  for (int d = D; d < 3; ++d) g.nc[d] = 1;
+  g.D = D;
+  g.ncell = ncell;
+  g.dist2 = dist * dist;
+  // binning and counting sort; the arena keeps the previous call's contents,
+  // so the per-cell counters are cleared first
+  GC_CUDA(cudaMemsetAsync(count, 0, sizeof(int32_t) * ncell, st));
+  const double* x2 = D == 3 ? x[2] : x[0];
+  k_cellkey<D><<<nblocks(N, TPB), TPB, 0, st>>>(x[0], x[1], x2, N, g, key, slot, count);
+  GC_LAUNCHED();
+  if ((rc = exclusive_scan_i32_to_i32(count, cstart, ncell, scan, st))) return rc;
+  k_scatter_arrival<<<nblocks(N, TPB), TPB, 0, st>>>(key, slot, cstart, N, tmpv);
+  GC_LAUNCHED();
+  k_rank_in_cell<<<nblocks(N, TPB), TPB, 0, st>>>(tmpv, key, cstart, nullptr, N, perm);
+  GC_LAUNCHED();
+  k_apply_perm<<<nblocks(N, TPB), TPB, 0, st>>>(perm, key, nullptr, N, skey, orig);
+  GC_LAUNCHED();
+  k_gather_pos<D><<<nblocks(N, TPB), TPB, 0, st>>>(perm, N, x[0], x[1], x2, xs[0], xs[1], D == 3 ? xs[2] : xs[0]);
+  GC_LAUNCHED();
+  // pair counts, offsets, then the pairs themselves
+  const double cand = (double)N / (double)ncell * (D == 3 ? 27.0 : 9.0);
+  int L = 1;
+  while (L < 32 && (double)L * 8.0 < cand) L <<= 1;
+  const double* xc2 = D == 3 ? xs[2] : xs[0];
+  const int gb = nblocks(N * (int64_t)L, TPB);
+#define NA_CASES(KER, ...)                                              \
+  switch (L) {                                                          \
+    case 1: KER<D, 1><<<gb, TPB, 0, st>>>(__VA_ARGS__); break;          \
+    case 2: KER<D, 2><<<gb, TPB, 0, st>>>(__VA_ARGS__); break;          \
+    case 4: KER<D, 4><<<gb, TPB, 0, st>>>(__VA_ARGS__); break;          \
+    case 8: KER<D, 8><<<gb, TPB, 0, st>>>(__VA_ARGS__); break;          \
+    case 16: KER<D, 16><<<gb, TPB, 0, st>>>(__VA_ARGS__); break;        \
+    default: KER<D, 32><<<gb, TPB, 0, st>>>(__VA_ARGS__); break;        \
+  }
+  switch (L) {
+    case 1: k_pairs<D, 0, 1><<<gb, TPB, 0, st>>>(xs[0], xs[1], xc2, skey, cstart, N, g, cfull, cup, nullptr, nullptr); break;
+    case 2: k_pairs<D, 0, 2><<<gb, TPB, 0, st>>>(xs[0], xs[1], xc2, skey, cstart, N, g, cfull, cup, nullptr, nullptr); break;
+    case 4: k_pairs<D, 0, 4><<<gb, TPB, 0, st>>>(xs[0], xs[1], xc2, skey, cstart, N, g, cfull, cup, nullptr, nullptr); break;
+    case 8: k_pairs<D, 0, 8><<<gb, TPB, 0, st>>>(xs[0], xs[1], xc2, skey, cstart, N, g, cfull, cup, nullptr, nullptr); break;
+    case 16: k_pairs<D, 0, 16><<<gb, TPB, 0, st>>>(xs[0], xs[1], xc2, skey, cstart, N, g, cfull, cup, nullptr, nullptr); break;
+    default: k_pairs<D, 0, 32><<<gb, TPB, 0, st>>>(xs[0], xs[1], xc2, skey, cstart, N, g, cfull, cup, nullptr, nullptr); break;
+  }
+  GC_LAUNCHED();
+  if ((rc = exclusive_scan_i32_to_i64(cup, rsup, N, scan, st))) return rc;
+  int64_t total = 0;
+  GC_CUDA(cudaMemcpyAsync(&total, rsup + N, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+  GC_CUDA(cudaStreamSynchronize(st));
+  if (cap > 0) {
+    NA_CASES(k_pairs_direct, xs[0], xs[1], xc2, skey, cstart, orig, N, g, rsup, cap, pairs);
+    GC_LAUNCHED();
+    if (fillzero && total < cap)
+      GC_CUDA(cudaMemsetAsync(pairs + 2 * total, 0, sizeof(int32_t) * 2 * (size_t)(cap - total), st));
+  }
+#undef NA_CASES
+  GC_CUDA(cudaStreamSynchronize(st));
+  if (pairsn) *pairsn = total;
+  if (total > cap)
+    return fail(GCSPH_ECAPACITY, "pair list holds %lld of %lld pairs", (long long)cap, (long long)total);
+  return GCSPH_OK;
+}
+
+}  // namespace noalloc
+}  // namespace gcsph
+
+extern "C" int gcl_pairs_noalloc(int32_t D, int64_t N, const double* const* x_dev, const double* cellsize,
+                                 double dist, const double* MIN_or_null, const double* MAX_or_null,
+                                 int32_t* pairs_dev, int64_t cap, int fillzero, int64_t* pairsn_out, void* stream) {
+  using namespace gcsph;
+  if (!x_dev || !cellsize) return fail(GCSPH_EINVAL, "null argument");
+  if (D != 2 && D != 3) return fail(GCSPH_EINVAL, "wrong dimention: D=%d (2 or 3)", (int)D);
+  for (int d = 0; d < D; ++d)
+    if (!x_dev[d]) return fail(GCSPH_EINVAL, "null coordinate array %d", d + 1);
+  if (N < 1) return fail(GCSPH_EINVAL, "N=%lld out of range", (long long)N);
+  if (N > noalloc::MAXN)
+    return fail(GCSPH_EINVAL,
+                "gcl_pairs_noalloc: %lld points exceed the limit of its static scratch, %lld "
+                "(use gcl_create for larger sets)",
+                (long long)N, (long long)noalloc::MAXN);
+  if (!(dist > 0)) return fail(GCSPH_EINVAL, "dist must be > 0");
+  if (cap < 0 || (cap > 0 && !pairs_dev)) return fail(GCSPH_EINVAL, "bad pair buffer");
+  cudaStream_t st = (cudaStream_t)stream;
+  return D == 2 ? noalloc::run<2>(N, x_dev, cellsize, dist, MIN_or_null, MAX_or_null, pairs_dev, cap, fillzero,
+                                  pairsn_out, st)
+                : noalloc::run<3>(N, x_dev, cellsize, dist, MIN_or_null, MAX_or_null, pairs_dev, cap, fillzero,
+                                  pairsn_out, st);
+}

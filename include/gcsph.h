@@ -90,6 +90,27 @@ int gcl_cellpnum(gcl_handle* h, int32_t* cellpnum_dev);
 /* мaxpairs(c.cellpnum) -- src/gpukernels_cls.jl:109-286 */
 int gcl_maxpairs(gcl_handle* h, int64_t* out);
 
+/* No counterpart in the reference.  The pair list of GPUCellList(points,
+ * cellsize, dist; MIN, MAX) in a single call that allocates no memory, for
+ * callers that must not allocate device memory while they run: a host whose
+ * own pool already holds the device (a Julia or PyTorch process), a plugin
+ * whose framework forbids allocation, a time-critical loop that cannot take
+ * cudaMalloc's implicit device synchronisation.  All intermediate arrays sit
+ * in one static device array (24 MiB, kept by every GPU that loads the
+ * library until the process exits) sized for at most
+ * GCSPH_NOALLOC_MAX_POINTS points and GCSPH_NOALLOC_MAX_CELLS grid cells;
+ * larger inputs are rejected with GCSPH_EINVAL.  Output: the same (min,max)
+ * 1-based list, in the same order, that gcl_create + gcl_emit_pairs give;
+ * GCSPH_ECAPACITY and the full count when it does not fit in cap.  The first
+ * call on a device looks up the array's device address (make that first call
+ * before any stream capture).  Calls share the array: two calls that overlap
+ * on the GPU (different streams, threads) race and corrupt each other. */
+#define GCSPH_NOALLOC_MAX_POINTS 262144
+#define GCSPH_NOALLOC_MAX_CELLS 1048576
+int gcl_pairs_noalloc(int32_t D, int64_t N, const double* const* x_dev, const double* cellsize, double dist,
+                      const double* MIN_or_null, const double* MAX_or_null, int32_t* pairs_dev, int64_t cap,
+                      int fillzero, int64_t* pairsn_out, void* stream);
+
 /* ---------------------------------------------------------------- SPH problem */
 
 /* Mutable SPHProblem scalars, src/sphproblem.jl:62-112 (defaults :172-191). */
