@@ -327,7 +327,7 @@ int CellCore::init(int D_, int64_t N_, const double* cellsize, double dist_, con
 
 void CellCore::release() {
   DevBuf* all[] = {&count, &cellstart, &key, &slot, &tmp, &perm, &skey, &orig, &cnt_full, &cnt_up, &rs_full,
-                   &rs_up, &nbr, &scratch};
+                   &rs_up, &nbr, &scratch, &pf[0], &pf[1], &pf[2], &pfmax};
   for (DevBuf* b : all) b->release();
   if (pin) cudaFreeHost(pin);
   pin = nullptr;
@@ -383,6 +383,128 @@ int CellCore::gather_positions_by_orig(const double* const* xorig, double* const
   return GCSPH_OK;
 }
 
+// ---------------------------------------------------------------------------
+// FP32 prefilter for the pair test.  GB300 issues 64x more FP32 than FP64
+// instructions per cycle, so candidates are first tested on FP32 copies of
+// (x - offset).  With B = max |x - offset| every FP32 coordinate is within
+// 2^-24 B(1+2^-29) of its exact value, so with e0 = 2^-22 B (twice the
+// worst case of a difference of two such coordinates plus its own rounding)
+//   |r2f - r2| <= band = 2 e0 sqrt(D T') + D e0^2 + 2^-20 T'     (T' = 1.5 dist^2)
+// covers the coordinate errors, the FP32 squares and sums and the FP64
+// reference expression's own rounding for every candidate with r2 <= T'.
+// A candidate is IN when r2f < T - band and OUT when r2f > T + band (both
+// bounds rounded outwards); only candidates inside the band take the exact
+// FP64 test of the reference, so the pair set is unchanged bit for bit.
+// ---------------------------------------------------------------------------
+template <int D>
+__global__ void k_make_pf(const double* __restrict__ x0, const double* __restrict__ x1,
+                          const double* __restrict__ x2, int64_t N, Grid g, float* __restrict__ f0,
+                          float* __restrict__ f1, float* __restrict__ f2, unsigned long long* __restrict__ bmax) {
+  int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  double b = 0.0;
+  if (k < N) {
+    const double* X[3] = {x0, x1, x2};
+    float* F[3] = {f0, f1, f2};
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      const double v = X[d][k] - g.offset[d];
+      F[d][k] = (float)v;
+      b = fmax(b, fabs(v));
+    }
+    if (b != b) b = INFINITY;  // NaN coordinate: every candidate of the set goes to FP64
+  }
+  b = warp_max(b);
+  if ((threadIdx.x & 31) == 0) atomic_max_pos(bmax, b);
+}
+
+template <int D>
+__device__ inline void pf_thresholds(const unsigned long long* bmax, double dist2, float* tlo, float* thi) {
+  const double B = __longlong_as_double((long long)*bmax) * (1.0 + 0x1p-28);
+  const double e0 = B * 0x1p-22;
+  const double Tp = 1.5 * dist2;
+  const double band = 2.0 * e0 * sqrt((double)D * Tp) + (double)D * e0 * e0 + Tp * 0x1p-20;
+  *tlo = __double2float_rd(dist2 - band);
+  *thi = __double2float_ru(dist2 + band);
+}
+
+// k_pairs with the FP32 prefilter; same output, same order
+template <int D, int MODE, int L>
+__global__ void __launch_bounds__(TPB) k_pairs32(const double* __restrict__ x0, const double* __restrict__ x1,
+                                                 const double* __restrict__ x2, const float* __restrict__ f0,
+                                                 const float* __restrict__ f1, const float* __restrict__ f2,
+                                                 const unsigned long long* __restrict__ bmax,
+                                                 const int32_t* __restrict__ skey,
+                                                 const int32_t* __restrict__ cellstart, int64_t N, Grid g,
+                                                 int32_t* __restrict__ cnt_full, int32_t* __restrict__ cnt_up,
+                                                 const int64_t* __restrict__ rs_full, int32_t* __restrict__ nbr) {
+  const int64_t gt = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t k = gt / L;
+  const int lane = (int)(gt % L);
+  if (k >= N) return;
+  float tlo, thi;
+  pf_thresholds<D>(bmax, g.dist2, &tlo, &thi);
+  const unsigned lanew = threadIdx.x & 31u;
+  const unsigned gbase = lanew & ~(unsigned)(L - 1);
+  const unsigned gm = L == 32 ? 0xffffffffu : (((1u << L) - 1u) << gbase);
+  const int nx = g.nc[0], ny = g.nc[1], nz = D == 3 ? g.nc[2] : 1;
+  const int32_t key = skey[k];
+  const int cx = key % nx;
+  const int t = key / nx;
+  const int cy = t % ny;
+  const int cz = t / ny;
+  const float ax = f0[k], ay = f1[k], az = D == 3 ? f2[k] : 0.0f;
+  int32_t nf = 0, nu = 0;
+  int64_t wpos = MODE == 1 ? rs_full[k] : 0;
+  const int xlo = cx > 0 ? cx - 1 : 0;
+  const int xhi = cx < nx - 1 ? cx + 1 : nx - 1;
+  for (int dz = (D == 3 ? -1 : 0); dz <= (D == 3 ? 1 : 0); ++dz) {
+    const int z = cz + dz;
+    if (z < 0 || z >= nz) continue;
+    for (int dy = -1; dy <= 1; ++dy) {
+      const int y = cy + dy;
+      if (y < 0 || y >= ny) continue;
+      const int64_t base = (int64_t)nx * ((int64_t)y + (int64_t)ny * z);
+      const int32_t m0 = cellstart[base + xlo], m1 = cellstart[base + xhi + 1];
+      for (int32_t mb = m0; mb < m1; mb += L) {
+        const int32_t m = mb + lane;
+        bool hit = false;
+        if (m < m1 && m != k) {
+          const float d0 = ax - f0[m], d1 = ay - f1[m];
+          float r2f = d0 * d0 + d1 * d1;
+          if (D == 3) {
+            const float d2 = az - f2[m];
+            r2f = r2f + d2 * d2;
+          }
+          if (r2f < tlo) {
+            hit = true;
+          } else if (!(r2f > thi)) {  // inside the band (or NaN): the reference's FP64 test
+            hit = r2_ref<D>(x0[k], x1[k], D == 3 ? x2[k] : 0.0, x0[m], x1[m], D == 3 ? x2[m] : 0.0) < g.dist2;
+          }
+        }
+        if (MODE == 0) {
+          nf += hit;
+          nu += hit && (m > k);
+        } else {
+          const unsigned bal = (__ballot_sync(gm, hit) >> gbase) & (L == 32 ? 0xffffffffu : ((1u << L) - 1u));
+          if (hit) nbr[wpos + __popc(bal & ((1u << lane) - 1u))] = m;
+          wpos += __popc(bal);
+        }
+      }
+    }
+  }
+  if (MODE == 0) {
+#pragma unroll
+    for (int o = L / 2; o > 0; o >>= 1) {
+      nf += __shfl_xor_sync(gm, nf, o);
+      nu += __shfl_xor_sync(gm, nu, o);
+    }
+    if (lane == 0) {
+      cnt_full[k] = nf;
+      cnt_up[k] = nu;
+    }
+  }
+}
+
 // lanes per particle in the pair search: about 8 candidates per lane
 int CellCore::pair_lanes() const {
   if (lanes > 0) return lanes;
@@ -417,13 +539,48 @@ int CellCore::pair_lanes() const {
     }                                                                                            \
   } while (0)
 
+#define PAIRS32_LAUNCH(MODE, L, ...)                                                             \
+  do {                                                                                           \
+    const int _g = nblocks(N * (int64_t)(L), TPB);                                               \
+    if (D == 2) {                                                                                \
+      switch (L) {                                                                               \
+        case 1: k_pairs32<2, MODE, 1><<<_g, TPB, 0, st>>>(__VA_ARGS__); break;                   \
+        case 2: k_pairs32<2, MODE, 2><<<_g, TPB, 0, st>>>(__VA_ARGS__); break;                   \
+        case 4: k_pairs32<2, MODE, 4><<<_g, TPB, 0, st>>>(__VA_ARGS__); break;                   \
+        case 8: k_pairs32<2, MODE, 8><<<_g, TPB, 0, st>>>(__VA_ARGS__); break;                   \
+        case 16: k_pairs32<2, MODE, 16><<<_g, TPB, 0, st>>>(__VA_ARGS__); break;                 \
+        default: k_pairs32<2, MODE, 32><<<_g, TPB, 0, st>>>(__VA_ARGS__); break;                 \
+      }                                                                                          \
+    } else {                                                                                     \
+      switch (L) {                                                                               \
+        case 1: k_pairs32<3, MODE, 1><<<_g, TPB, 0, st>>>(__VA_ARGS__); break;                   \
+        case 2: k_pairs32<3, MODE, 2><<<_g, TPB, 0, st>>>(__VA_ARGS__); break;                   \
+        case 4: k_pairs32<3, MODE, 4><<<_g, TPB, 0, st>>>(__VA_ARGS__); break;                   \
+        case 8: k_pairs32<3, MODE, 8><<<_g, TPB, 0, st>>>(__VA_ARGS__); break;                   \
+        case 16: k_pairs32<3, MODE, 16><<<_g, TPB, 0, st>>>(__VA_ARGS__); break;                 \
+        default: k_pairs32<3, MODE, 32><<<_g, TPB, 0, st>>>(__VA_ARGS__); break;                 \
+      }                                                                                          \
+    }                                                                                            \
+  } while (0)
+
 int CellCore::build_pairs(const double* const* xs) {
   if (!sorted) return fail(GCSPH_ESTATE, "pair build before binning");
   const double* x2 = D == 3 ? xs[2] : xs[0];
   timer_begin(T_PAIRS, st);
   const int L = pair_lanes();
-  PAIRS_LAUNCH(0, L, xs[0], xs[1], x2, skey.as<int32_t>(), cellstart.as<int32_t>(), N, g, cnt_full.as<int32_t>(),
-               cnt_up.as<int32_t>(), nullptr, nullptr);
+  int rc0;
+  for (int d = 0; d < D; ++d)
+    if ((rc0 = pf[d].ensure(sizeof(float) * N, st))) return rc0;
+  if ((rc0 = pfmax.ensure(sizeof(unsigned long long), st, true))) return rc0;
+  float* f2 = D == 3 ? pf[2].as<float>() : pf[0].as<float>();
+  unsigned long long* bm = pfmax.as<unsigned long long>();
+  if (D == 2)
+    k_make_pf<2><<<nblocks(N, TPB), TPB, 0, st>>>(xs[0], xs[1], x2, N, g, pf[0].as<float>(), pf[1].as<float>(), f2, bm);
+  else
+    k_make_pf<3><<<nblocks(N, TPB), TPB, 0, st>>>(xs[0], xs[1], x2, N, g, pf[0].as<float>(), pf[1].as<float>(), f2, bm);
+  GC_LAUNCHED();
+  PAIRS32_LAUNCH(0, L, xs[0], xs[1], x2, pf[0].as<float>(), pf[1].as<float>(), f2, bm, skey.as<int32_t>(),
+                 cellstart.as<int32_t>(), N, g, cnt_full.as<int32_t>(), cnt_up.as<int32_t>(), nullptr, nullptr);
   GC_LAUNCHED();
   int rc = exclusive_scan_i32_to_i64(cnt_full.as<int32_t>(), rs_full.as<int64_t>(), N, scratch.as<int64_t>(), st);
   if (rc) return rc;
@@ -442,8 +599,8 @@ int CellCore::build_pairs(const double* const* xs) {
     nbr_cap = want;
   }
   timer_begin(T_PAIRS, st);
-  PAIRS_LAUNCH(1, L, xs[0], xs[1], x2, skey.as<int32_t>(), cellstart.as<int32_t>(), N, g, nullptr, nullptr,
-               rs_full.as<int64_t>(), nbr.as<int32_t>());
+  PAIRS32_LAUNCH(1, L, xs[0], xs[1], x2, pf[0].as<float>(), pf[1].as<float>(), f2, bm, skey.as<int32_t>(),
+                 cellstart.as<int32_t>(), N, g, nullptr, nullptr, rs_full.as<int64_t>(), nbr.as<int32_t>());
   GC_LAUNCHED();
   timer_end(T_PAIRS, st);
   built = true;

@@ -35,6 +35,7 @@ struct CellCore {
   cudaStream_t st = 0;
 
   DevBuf count, cellstart, key, slot, tmp, perm, skey, orig, cnt_full, cnt_up, rs_full, rs_up, nbr, scratch;
+  DevBuf pf[3], pfmax;  // FP32 (x - offset) copies for the prefilter, and max |x - offset|
   int64_t* pin = nullptr;  // pinned host scalars
   int64_t nfull = 0, nup = 0, nbr_cap = 0;
   bool sorted = false, built = false;

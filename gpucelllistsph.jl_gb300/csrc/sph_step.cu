@@ -60,6 +60,8 @@ struct SArr {
   double* vh[3];
   double* rhoh;
   double* P2;
+  double* ir;   // 1/ρ (FAST stage 1)
+  double* irh;  // 1/ρΔt½ (FAST stage 2)
   double* We;
   double* gWe[3];
   double* a[3];
@@ -170,6 +172,74 @@ __device__ inline void pf_term(const StepConst& c, Acc<D>& A, int ptk, int ptm, 
   }
 }
 
+// ---------------------------------------------------------------------------
+// FAST variants (lanes > 1): the same terms with fewer FP64 divisions -- the
+// FP64 pipe issues 2 thread-instructions per cycle per SM on GB300 and an IEEE
+// division costs ~8 of them.  1/ρ per particle is precomputed, 1/(r²+η²) is
+// shared by ∂ρ∂tDDT!, ∂v∂t_av! and ∂v∂t_visc!, 1/(ρᵢ+ρⱼ) by av and visc, and
+// powfancy7th's Newton step t - t(t³ - x/t⁴)/(4t³ + 3x/t⁴) is evaluated in the
+// equal form t - t(t⁷ - x)/(4t⁷ + 3x) with one division.  Each change moves a
+// result by a few ulp, inside the spread the reference's own atomics give.
+// ---------------------------------------------------------------------------
+__device__ inline double powfancy7th_1div(double x, double ginv, int gamma) {
+  if (gamma != 7) return pow(x, ginv);
+  const double ax = fabs(x);
+  unsigned long long bits = (unsigned long long)__double_as_longlong(ax);
+  bits = 0x36cd000000000000ULL + bits / 7ULL;
+  double t = copysign(__longlong_as_double((long long)bits), x);
+#pragma unroll
+  for (int it = 0; it < 2; ++it) {
+    const double t2 = t * t;
+    const double t3 = t2 * t;
+    const double t7 = t3 * (t2 * t2);
+    t = t - (t * (t7 - x)) / (4.0 * t7 + 3.0 * x);
+  }
+  return t;
+}
+
+template <int D>
+__device__ inline double ddt_term_fast(const StepConst& c, int ptk, const double* dx, double inv_r2eta,
+                                       const double* gw, const double* dv, double rk, double rm, double irm) {
+  double dot3 = -dotD<D>(dx, gw);
+  double s = c.m0 * dotD<D>(dv, gw);
+  if (ptk > 1) {
+    double drhopvp = c.rho0 * powfancy7th_1div(1.0 + c.DDTgz * dx[1], c.ginv, c.gamma) - c.rho0;
+    double visc_densi = c.DDTkh * ((rm - rk) - drhopvp) * inv_r2eta;
+    s += visc_densi * dot3 * c.m0 * irm;
+  }
+  return s;
+}
+
+template <int D>
+__device__ inline void mom_terms_fast(const StepConst& c, Acc<D>& A, int ptk, int ptm, const double* dx,
+                                      double inv_r2eta, const double* gw, const double* dv, double rk, double rm,
+                                      double irk, double irm, double Pk, double Pm) {
+  if (ptk * ptm > 0) {
+    const double sc = -c.m0 * ((Pk + Pm) * (irk * irm));
+#pragma unroll
+    for (int d = 0; d < D; ++d) A.p[d] += sc * gw[d];
+  }
+  if (ptk > 0 && ptm > 0) {
+    const double cond = dotD<D>(dv, dx);
+    const bool av = cond < 0.0;
+    if (av || c.use_visc) {
+      const double inv_sum = 1.0 / (rk + rm);
+      if (av) {
+        const double dmu = c.h * cond * inv_r2eta;
+        const double dPi = (-c.alpha * c.c0 * dmu) * (2.0 * inv_sum);
+        const double sc = -dPi * c.m0;
+#pragma unroll
+        for (int d = 0; d < D; ++d) A.av[d] += sc * gw[d];
+      }
+      if (c.use_visc) {
+        const double nuterm = 4.0 * c.nu * c.m0 * dotD<D>(dx, gw) * inv_sum * inv_r2eta;
+#pragma unroll
+        for (int d = 0; d < D; ++d) A.vi[d] += nuterm * dv[d];
+      }
+    }
+  }
+}
+
 // a = ((((p + av) + visc) - g) + fb) + pF
 template <int D>
 __device__ inline void finish_acc(const StepConst& c, const Acc<D>& A, double* a) {
@@ -221,7 +291,7 @@ __device__ inline void group_sum_acc(Acc<D>& A, const StepConst& c, unsigned gm)
 // ---------------------------------------------------------------------------
 // stage 1 at (x, ρ, v) + predictors
 // ---------------------------------------------------------------------------
-template <int D, int L>
+template <int D, int L, bool FAST = (L > 1)>
 __global__ void __launch_bounds__(STPB) k_stage1(StepConst c, const Scal* __restrict__ sc, int64_t N, SArr<D> S) {
   const int64_t gt = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int64_t k = gt / L;
@@ -233,6 +303,7 @@ __global__ void __launch_bounds__(STPB) k_stage1(StepConst c, const Scal* __rest
 #pragma unroll
   for (int d = 0; d < D; ++d) { xk[d] = S.x[d][k]; vk[d] = S.v[d][k]; }
   const double rk = S.rho[k], Pk = S.P1[k];
+  const double irk = FAST ? S.ir[k] : 0.0;
   const int ptk = S.pt[k];
   double drho = 0.0;
   Acc<D> A;
@@ -244,16 +315,33 @@ __global__ void __launch_bounds__(STPB) k_stage1(StepConst c, const Scal* __rest
 #pragma unroll
     for (int d = 0; d < D; ++d) { dx[d] = xk[d] - S.x[d][m]; dv[d] = vk[d] - S.v[d][m]; }
     const double r2 = dotD<D>(dx, dx);
-    const double r = sqrt(r2);
-    const double u = r * c.Hinv;
-    S.We[e] = wc2_w(u, c.nW);                       // sphW!, :84-100
-    const double dwk_r = wc2_dw(u, c.nDW) / r;      // sph∇W!, :196-213
+    double r, dwk_r;
+    if (FAST) {
+      const double ri = rsqrt(r2);
+      r = r2 > 0.0 ? r2 * ri : 0.0;
+      const double u = r * c.Hinv;
+      S.We[e] = wc2_w(u, c.nW);
+      dwk_r = wc2_dw(u, c.nDW) * ri;
+    } else {
+      r = sqrt(r2);
+      const double u = r * c.Hinv;
+      S.We[e] = wc2_w(u, c.nW);                     // sphW!, :84-100
+      dwk_r = wc2_dw(u, c.nDW) / r;                 // sph∇W!, :196-213
+    }
 #pragma unroll
     for (int d = 0; d < D; ++d) { gw[d] = dx[d] * dwk_r; S.gWe[d][e] = gw[d]; }
     const int ptm = S.pt[m];
     const double rm = S.rho[m];
-    if (ptk > 0 && ptm > 0) drho += ddt_term<D>(c, ptk, ptm, dx, r2, gw, dv, rk, rm);
-    mom_terms<D>(c, A, ptk, ptm, dx, r2, gw, dv, rk, rm, Pk, S.P1[m]);
+    if (FAST) {
+      const bool both = ptk > 0 && ptm > 0;
+      const double inv_r2eta = both ? 1.0 / (r2 + c.eta2) : 0.0;
+      const double irm = S.ir[m];
+      if (both) drho += ddt_term_fast<D>(c, ptk, dx, inv_r2eta, gw, dv, rk, rm, irm);
+      mom_terms_fast<D>(c, A, ptk, ptm, dx, inv_r2eta, gw, dv, rk, rm, irk, irm, Pk, S.P1[m]);
+    } else {
+      if (ptk > 0 && ptm > 0) drho += ddt_term<D>(c, ptk, ptm, dx, r2, gw, dv, rk, rm);
+      mom_terms<D>(c, A, ptk, ptm, dx, r2, gw, dv, rk, rm, Pk, S.P1[m]);
+    }
     fb_term<D>(c, A, ptk, ptm, dx, r2);
     if (c.use_pF) pf_term<D>(c, A, ptk, ptm, dx, r);
   }
@@ -275,12 +363,13 @@ __global__ void __launch_bounds__(STPB) k_stage1(StepConst c, const Scal* __rest
     S.xh[d][k] = S.xh[d][k] + vh * hdt;
   }
   S.P2[k] = eos(rv, c.gamma, c.rho0, c.P0, ptk);   // pressure! at ρΔt½
+  S.irh[k] = 1.0 / rv;
 }
 
 // ---------------------------------------------------------------------------
 // stage 2 at (xΔt½, ρΔt½, vΔt½) with stage-1 ∇W, + symplectic_update!
 // ---------------------------------------------------------------------------
-template <int D, int L>
+template <int D, int L, bool FAST = (L > 1)>
 __global__ void __launch_bounds__(STPB) k_stage2(StepConst c, Scal* __restrict__ sc, int64_t N, SArr<D> S) {
   const int64_t gt = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int64_t k = gt / L;
@@ -293,6 +382,7 @@ __global__ void __launch_bounds__(STPB) k_stage2(StepConst c, Scal* __restrict__
 #pragma unroll
     for (int d = 0; d < D; ++d) { xk[d] = S.x[d][k]; xhk[d] = S.xh[d][k]; vhk[d] = S.vh[d][k]; }
     const double rk = S.rhoh[k], Pk = S.P2[k];
+    const double irk = FAST ? S.irh[k] : 0.0;
     const int ptk = S.pt[k];
     double drho = 0.0;
     Acc<D> A;
@@ -310,8 +400,16 @@ __global__ void __launch_bounds__(STPB) k_stage2(StepConst c, Scal* __restrict__
       const double r2 = dotD<D>(dx, dx);
       const int ptm = S.pt[m];
       const double rm = S.rhoh[m];
-      if (ptk > 0 && ptm > 0) drho += ddt_term<D>(c, ptk, ptm, dx, r2, gw, dv, rk, rm);
-      mom_terms<D>(c, A, ptk, ptm, dx, r2, gw, dv, rk, rm, Pk, S.P2[m]);
+      if (FAST) {
+        const bool both = ptk > 0 && ptm > 0;
+        const double inv_r2eta = both ? 1.0 / (r2 + c.eta2) : 0.0;
+        const double irm = S.irh[m];
+        if (both) drho += ddt_term_fast<D>(c, ptk, dx, inv_r2eta, gw, dv, rk, rm, irm);
+        mom_terms_fast<D>(c, A, ptk, ptm, dx, inv_r2eta, gw, dv, rk, rm, irk, irm, Pk, S.P2[m]);
+      } else {
+        if (ptk > 0 && ptm > 0) drho += ddt_term<D>(c, ptk, ptm, dx, r2, gw, dv, rk, rm);
+        mom_terms<D>(c, A, ptk, ptm, dx, r2, gw, dv, rk, rm, Pk, S.P2[m]);
+      }
       if ((ptk > 0) != (ptm > 0)) {
 #pragma unroll
         for (int d = 0; d < D; ++d) dxf[d] = xk[d] - S.x[d][m];
@@ -333,6 +431,7 @@ __global__ void __launch_bounds__(STPB) k_stage2(StepConst c, Scal* __restrict__
       S.rho[k] = rv;
       S.rhoho[k] = rv;
       S.P1[k] = eos(rv, c.gamma, c.rho0, c.P0, ptk);
+      S.ir[k] = 1.0 / rv;
       const double ml = ptk > 1 ? 1.0 : 0.0;
 #pragma unroll
       for (int d = 0; d < D; ++d) {
@@ -490,6 +589,7 @@ __global__ void __launch_bounds__(STPB) k_cspm(StepConst c, int64_t N, SArr<D> S
   double rv = isnan(nr) ? rk : nr;
   S.rhoo[k] = rv;
   S.P1[k] = eos(rv, c.gamma, c.rho0, c.P0, ptk);
+  S.ir[k] = 1.0 / rv;
   S.buf2[0][k] = s1;
   S.buf2[1][k] = s2;
   if (D == 3) S.buf2[2][k] = 0.0;
@@ -609,6 +709,7 @@ __global__ void k_gather_state(StepConst c, int64_t N, const int32_t* __restrict
   const double r = O.rho[o];
   S.rho[k] = r;
   S.P1[k] = eos(r, c.gamma, c.rho0, c.P0, pt);
+  S.ir[k] = 1.0 / r;
   S.rhoh[k] = O.rhoh[o];
 #pragma unroll
   for (int d = 0; d < D; ++d) {
@@ -663,7 +764,7 @@ struct sph_handle {
   DevBuf rhoh_o, vh_o[3], xh_o[3], cdx_o[3], P_o, a_o[3], drho_o, buf2_o[3], sumW_o, sumgW_o[3];
   // cell-order working arrays
   DevBuf X[2][3], XH[2][3], V[2][3], VH[2][3], RHO[2], RHOH[2], P1, P2, PT, A[3], DRHO, CDX[3], BUF2[3], PLAST, We,
-      GWe[3];
+      GWe[3], IR, IRH;
   int ix = 0, ixh = 0, iv = 0, ivh = 0, irho = 0, irhoh = 0;
   int64_t we_cap = 0;
   int lanes = 0;  // lanes per particle in the pair passes; 0 = by mean row length
@@ -747,6 +848,8 @@ static SArr<D> make_arr(sph_handle* h) {
   S.rhoho = h->RHOH[h->irhoh ^ 1].as<double>();
   S.P1 = h->P1.as<double>();
   S.P2 = h->P2.as<double>();
+  S.ir = h->IR.as<double>();
+  S.irh = h->IRH.as<double>();
   S.We = h->We.as<double>();
   S.drho = h->DRHO.as<double>();
   S.Plast = h->PLAST.as<double>();
@@ -1001,6 +1104,8 @@ int sph_create(gcl_handle* cl, const gcsph_params* prm, double* rho_dev, double*
   }
   E(h->P1, nb, true);
   E(h->P2, nb, true);
+  E(h->IR, nb, true);
+  E(h->IRH, nb, true);
   E(h->PT, sizeof(int32_t) * N, false);
   E(h->DRHO, nb, true);
   E(h->PLAST, nb, true);
@@ -1033,7 +1138,7 @@ void sph_destroy(sph_handle* h) {
   if (!h) return;
   if (h->cl) cudaStreamSynchronize(h->cl->core.st);
   DevBuf* one[] = {&h->rhoh_o, &h->P_o, &h->drho_o, &h->sumW_o, &h->P1, &h->P2, &h->PT, &h->DRHO, &h->PLAST,
-                   &h->We, &h->scal, &h->RHO[0], &h->RHO[1], &h->RHOH[0], &h->RHOH[1]};
+                   &h->We, &h->IR, &h->IRH, &h->scal, &h->RHO[0], &h->RHO[1], &h->RHOH[0], &h->RHOH[1]};
   for (DevBuf* b : one) b->release();
   for (int d = 0; d < 3; ++d) {
     h->vown[d].release();
