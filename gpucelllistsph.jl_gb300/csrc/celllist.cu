@@ -15,6 +15,7 @@
 // the sorted arrays and the pairs land at scanned offsets, so the emitted list
 // is deterministic (ascending sorted index).
 #include <mutex>
+#include <utility>
 
 #include "celllist.cuh"
 
@@ -327,7 +328,7 @@ int CellCore::init(int D_, int64_t N_, const double* cellsize, double dist_, con
 
 void CellCore::release() {
   DevBuf* all[] = {&count, &cellstart, &key, &slot, &tmp, &perm, &skey, &orig, &cnt_full, &cnt_up, &rs_full,
-                   &rs_up, &nbr, &scratch, &pf[0], &pf[1], &pf[2], &pfmax};
+                   &rs_up, &nbr, &scratch, &pf[0], &pf[1], &pf[2], &pfmax, &orig_b};
   for (DevBuf* b : all) b->release();
   if (pin) cudaFreeHost(pin);
   pin = nullptr;
@@ -352,12 +353,19 @@ int CellCore::sort(const double* const* xin, const int32_t* ord) {
   k_rank_in_cell<<<nblocks(N, TPB), TPB, 0, st>>>(tmp.as<int32_t>(), key.as<int32_t>(), cellstart.as<int32_t>(), ord, N,
                                                    perm.as<int32_t>());
   GC_LAUNCHED();
+  // ord may be `orig` itself (re-sorting particles already in cell order), so
+  // the new map is written to the spare buffer and the two are swapped
+  int rc2 = orig_b.ensure(sizeof(int32_t) * N, st);
+  if (rc2) return rc2;
   k_apply_perm<<<nblocks(N, TPB), TPB, 0, st>>>(perm.as<int32_t>(), key.as<int32_t>(), ord, N, skey.as<int32_t>(),
-                                                 orig.as<int32_t>());
+                                                 orig_b.as<int32_t>());
   GC_LAUNCHED();
+  std::swap(orig.p, orig_b.p);
+  std::swap(orig.bytes, orig_b.bytes);
   timer_end(T_SORT, st);
   sorted = true;
   built = false;
+  up_valid = false;
   return GCSPH_OK;
 }
 
@@ -436,11 +444,16 @@ __global__ void __launch_bounds__(TPB) k_pairs32(const double* __restrict__ x0, 
                                                  const int32_t* __restrict__ skey,
                                                  const int32_t* __restrict__ cellstart, int64_t N, Grid g,
                                                  int32_t* __restrict__ cnt_full, int32_t* __restrict__ cnt_up,
-                                                 const int64_t* __restrict__ rs_full, int32_t* __restrict__ nbr) {
+                                                 const int64_t* __restrict__ rs_full, int32_t* __restrict__ nbr,
+                                                 int64_t cap, int* __restrict__ ovf) {
   const int64_t gt = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int64_t k = gt / L;
   const int lane = (int)(gt % L);
   if (k >= N) return;
+  if (MODE == 1 && rs_full[k + 1] > cap) {  // the row does not fit: report, write nothing
+    if (ovf && lane == 0) atomicExch(ovf, 1);
+    return;
+  }
   float tlo, thi;
   pf_thresholds<D>(bmax, g.dist2, &tlo, &thi);
   const unsigned lanew = threadIdx.x & 31u;
@@ -563,7 +576,7 @@ int CellCore::pair_lanes() const {
     }                                                                                            \
   } while (0)
 
-int CellCore::build_pairs(const double* const* xs) {
+int CellCore::build_pairs(const double* const* xs, int* ovf_dev) {
   if (!sorted) return fail(GCSPH_ESTATE, "pair build before binning");
   const double* x2 = D == 3 ? xs[2] : xs[0];
   timer_begin(T_PAIRS, st);
@@ -580,36 +593,70 @@ int CellCore::build_pairs(const double* const* xs) {
     k_make_pf<3><<<nblocks(N, TPB), TPB, 0, st>>>(xs[0], xs[1], x2, N, g, pf[0].as<float>(), pf[1].as<float>(), f2, bm);
   GC_LAUNCHED();
   PAIRS32_LAUNCH(0, L, xs[0], xs[1], x2, pf[0].as<float>(), pf[1].as<float>(), f2, bm, skey.as<int32_t>(),
-                 cellstart.as<int32_t>(), N, g, cnt_full.as<int32_t>(), cnt_up.as<int32_t>(), nullptr, nullptr);
+                 cellstart.as<int32_t>(), N, g, cnt_full.as<int32_t>(), cnt_up.as<int32_t>(), nullptr, nullptr, 0,
+                 nullptr);
   GC_LAUNCHED();
   int rc = exclusive_scan_i32_to_i64(cnt_full.as<int32_t>(), rs_full.as<int64_t>(), N, scratch.as<int64_t>(), st);
   if (rc) return rc;
-  rc = exclusive_scan_i32_to_i64(cnt_up.as<int32_t>(), rs_up.as<int64_t>(), N, scratch.as<int64_t>(), st);
-  if (rc) return rc;
   timer_end(T_PAIRS, st);
-  GC_CUDA(cudaMemcpyAsync(pin, rs_full.as<int64_t>() + N, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
-  GC_CUDA(cudaMemcpyAsync(pin + 1, rs_up.as<int64_t>() + N, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
-  GC_CUDA(cudaStreamSynchronize(st));
-  timer_collect();
-  nfull = pin[0];
-  nup = pin[1];
-  if (nfull > nbr_cap) {
-    int64_t want = nfull + nfull / 4 + 1024;
-    if ((rc = nbr.ensure(sizeof(int32_t) * want, st))) return rc;
-    nbr_cap = want;
+  if (ovf_dev && nbr_cap > 0) {
+    // no host round trip: fill into the current capacity; a row that would
+    // pass it raises *ovf_dev, the caller's kernels then skip the step and
+    // the caller grows the buffers (grow_nbr) and repeats it
+    nfull = -1;
+  } else {
+    GC_CUDA(cudaMemcpyAsync(pin, rs_full.as<int64_t>() + N, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+    GC_CUDA(cudaStreamSynchronize(st));
+    timer_collect();
+    nfull = pin[0];
+    nfull_est = nfull;
+    if (nfull > nbr_cap && (rc = grow_nbr(nfull))) return rc;
   }
   timer_begin(T_PAIRS, st);
   PAIRS32_LAUNCH(1, L, xs[0], xs[1], x2, pf[0].as<float>(), pf[1].as<float>(), f2, bm, skey.as<int32_t>(),
-                 cellstart.as<int32_t>(), N, g, nullptr, nullptr, rs_full.as<int64_t>(), nbr.as<int32_t>());
+                 cellstart.as<int32_t>(), N, g, nullptr, nullptr, rs_full.as<int64_t>(), nbr.as<int32_t>(), nbr_cap,
+                 ovf_dev);
   GC_LAUNCHED();
   timer_end(T_PAIRS, st);
   built = true;
+  up_valid = false;
+  return GCSPH_OK;
+}
+
+int CellCore::grow_nbr(int64_t need) {
+  const int64_t want = need + need / 4 + 1024;
+  int rc = nbr.ensure(sizeof(int32_t) * want, st);
+  if (rc) return rc;
+  nbr_cap = want;
+  return GCSPH_OK;
+}
+
+int CellCore::read_nfull() {
+  GC_CUDA(cudaMemcpyAsync(pin, rs_full.as<int64_t>() + N, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+  GC_CUDA(cudaStreamSynchronize(st));
+  nfull = pin[0];
+  nfull_est = nfull;
+  return GCSPH_OK;
+}
+
+// offsets of each sorted particle's pairs in the (min,max) list: scanned on
+// demand, the stepping loop never needs them
+int CellCore::ensure_up() {
+  if (up_valid) return GCSPH_OK;
+  int rc = exclusive_scan_i32_to_i64(cnt_up.as<int32_t>(), rs_up.as<int64_t>(), N, scratch.as<int64_t>(), st);
+  if (rc) return rc;
+  GC_CUDA(cudaMemcpyAsync(pin + 1, rs_up.as<int64_t>() + N, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+  GC_CUDA(cudaStreamSynchronize(st));
+  nup = pin[1];
+  up_valid = true;
   return GCSPH_OK;
 }
 
 int CellCore::emit(int32_t* pairs, int64_t cap, int fillzero, int64_t* pairsn) {
   if (!built) return fail(GCSPH_ESTATE, "no pair set built yet");
   if (cap < 0) return fail(GCSPH_EINVAL, "negative capacity");
+  int rc0 = ensure_up();
+  if (rc0) return rc0;
   if (pairsn) *pairsn = nup;
   if (cap > 0 && !pairs) return fail(GCSPH_EINVAL, "null pair buffer");
   if (cap > 0) {
@@ -699,6 +746,7 @@ int gcl_update(gcl_handle* h, int64_t* pairsn_out) {
   if (!h) return fail(GCSPH_EINVAL, "null handle");
   int rc = gcl_full_update(h);
   if (rc) return rc;
+  if ((rc = h->core.ensure_up())) return rc;
   if (pairsn_out) *pairsn_out = h->core.nup;
   GC_CUDA(cudaStreamSynchronize(h->core.st));
   return GCSPH_OK;
@@ -711,6 +759,7 @@ int gcl_partialupdate(gcl_handle* h, int64_t* pairsn_out) {
   int rc = h->core.gather_positions_by_orig(h->xuser, xs);
   if (rc) return rc;
   if ((rc = h->core.build_pairs((const double* const*)xs))) return rc;
+  if ((rc = h->core.ensure_up())) return rc;
   if (pairsn_out) *pairsn_out = h->core.nup;
   GC_CUDA(cudaStreamSynchronize(h->core.st));
   return GCSPH_OK;

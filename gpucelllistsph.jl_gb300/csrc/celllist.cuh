@@ -34,11 +34,12 @@ struct CellCore {
   Grid g{};
   cudaStream_t st = 0;
 
-  DevBuf count, cellstart, key, slot, tmp, perm, skey, orig, cnt_full, cnt_up, rs_full, rs_up, nbr, scratch;
+  DevBuf count, cellstart, key, slot, tmp, perm, skey, orig, orig_b, cnt_full, cnt_up, rs_full, rs_up, nbr, scratch;
   DevBuf pf[3], pfmax;  // FP32 (x - offset) copies for the prefilter, and max |x - offset|
   int64_t* pin = nullptr;  // pinned host scalars
   int64_t nfull = 0, nup = 0, nbr_cap = 0;
-  bool sorted = false, built = false;
+  int64_t nfull_est = 0;  // last neighbour-entry count read back (lane choice); nfull is -1 while unknown
+  bool sorted = false, built = false, up_valid = false;
   int lanes = 0;  // lanes per particle in the pair search; 0 = by mean candidate count
   int pair_lanes() const;
 
@@ -52,8 +53,13 @@ struct CellCore {
   int gather_positions(const double* const* xin, double* const* xs);
   // gather xs[d][k] = xorig[d][orig[k]] for partial updates
   int gather_positions_by_orig(const double* const* xorig, double* const* xs);
-  // count + scan + fill of the neighbour CSR on sorted positions xs
-  int build_pairs(const double* const* xs);
+  // count + scan + fill of the neighbour CSR on sorted positions xs.  With
+  // ovf_dev (and buffers already sized once) the fill does not wait for the
+  // count: rows past nbr_cap raise *ovf_dev instead (see grow_nbr).
+  int build_pairs(const double* const* xs, int* ovf_dev = nullptr);
+  int grow_nbr(int64_t need);
+  int read_nfull();
+  int ensure_up();
   // (min,max) 1-based original indices of every pair, first cap written
   int emit(int32_t* pairs, int64_t cap, int fillzero, int64_t* pairsn);
   // мaxpairs over the current counts (src/gpukernels_cls.jl:109-286)

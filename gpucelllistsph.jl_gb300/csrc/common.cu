@@ -193,8 +193,61 @@ int64_t scan_scratch_elems(int64_t m) {
   return 2 * nb + 1 + scan_scratch_elems(nb);
 }
 
+// one block walks the whole array in tiles of 1024 x 8 items, carrying the
+// running total: a single launch for the small arrays of small problems
+template <class TIn, class TOut>
+__global__ void __launch_bounds__(1024) k_scan_single(const TIn* __restrict__ in, TOut* __restrict__ out,
+                                                      int64_t n_in, int64_t m) {
+  __shared__ long long wtot[32];
+  const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+  long long carry = 0;
+  for (int64_t tile0 = 0; tile0 < m; tile0 += 1024LL * SCAN_ITEMS) {
+    const int64_t base = tile0 + (int64_t)tid * SCAN_ITEMS;
+    long long v[SCAN_ITEMS];
+    long long s = 0;
+#pragma unroll
+    for (int j = 0; j < SCAN_ITEMS; ++j) {
+      const int64_t idx = base + j;
+      const long long x = idx < n_in ? (long long)in[idx] : 0;
+      v[j] = s;
+      s += x;
+    }
+    long long inc = s;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const long long y = __shfl_up_sync(0xffffffffu, inc, o);
+      if (lane >= o) inc += y;
+    }
+    if (lane == 31) wtot[w] = inc;
+    __syncthreads();
+    if (w == 0) {
+      long long t = wtot[lane];
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const long long y = __shfl_up_sync(0xffffffffu, t, o);
+        if (lane >= o) t += y;
+      }
+      wtot[lane] = t;
+    }
+    __syncthreads();
+    const long long excl = carry + (w > 0 ? wtot[w - 1] : 0) + inc - s;
+#pragma unroll
+    for (int j = 0; j < SCAN_ITEMS; ++j) {
+      const int64_t idx = base + j;
+      if (idx < m) out[idx] = (TOut)(excl + v[j]);
+    }
+    carry += wtot[31];
+    __syncthreads();
+  }
+}
+
 template <class TIn, class TOut>
 static int scan_impl(const TIn* in, TOut* out, int64_t n_in, int64_t m, int64_t* scratch, cudaStream_t s) {
+  if (m <= 65536) {
+    k_scan_single<TIn, TOut><<<1, 1024, 0, s>>>(in, out, n_in, m);
+    GC_LAUNCHED();
+    return GCSPH_OK;
+  }
   int64_t nb = (m + SCAN_TILE - 1) / SCAN_TILE;
   if (nb < 1) nb = 1;
   if (nb > 0x7fffffffLL) return fail(GCSPH_EINVAL, "scan too large");

@@ -43,7 +43,9 @@ struct Scal {
   unsigned long long maxcdx;  // bits of max |cΔx| of the current step
   unsigned long long amax;    // bits of max |a|
   unsigned long long vmax;    // bits of max |h v.x/(x.x+η²)|
-  double pad[3];
+  int ovf;                    // the neighbour CSR outgrew its buffers: this step's kernels skip
+  int pad0;
+  double pad[2];
 };
 
 template <int D>
@@ -52,6 +54,7 @@ struct SArr {
   const int32_t* nbr;
   const int32_t* pt;
   const int32_t* orig;
+  const int* ovf;  // set: the step's kernels skip (buffers outgrown, see rebuild)
   double* x[3];
   double* v[3];
   double* rho;
@@ -293,6 +296,7 @@ __device__ inline void group_sum_acc(Acc<D>& A, const StepConst& c, unsigned gm)
 // ---------------------------------------------------------------------------
 template <int D, int L, bool FAST = (L > 1)>
 __global__ void __launch_bounds__(STPB) k_stage1(StepConst c, const Scal* __restrict__ sc, int64_t N, SArr<D> S) {
+  if (*S.ovf) return;
   const int64_t gt = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int64_t k = gt / L;
   const int lane = (int)(gt % L);
@@ -371,6 +375,7 @@ __global__ void __launch_bounds__(STPB) k_stage1(StepConst c, const Scal* __rest
 // ---------------------------------------------------------------------------
 template <int D, int L, bool FAST = (L > 1)>
 __global__ void __launch_bounds__(STPB) k_stage2(StepConst c, Scal* __restrict__ sc, int64_t N, SArr<D> S) {
+  if (*S.ovf) return;  // uniform over the grid, before the block reduction below
   const int64_t gt = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int64_t k = gt / L;
   const int lane = (int)(gt % L);
@@ -467,6 +472,7 @@ __global__ void __launch_bounds__(STPB) k_stage2(StepConst c, Scal* __restrict__
 // ---------------------------------------------------------------------------
 template <int D, int L>
 __global__ void __launch_bounds__(STPB) k_dpc(StepConst c, const Scal* __restrict__ sc, int64_t N, SArr<D> S) {
+  if (*S.ovf) return;
   const int64_t gt = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int64_t k = gt / L;
   const int lane = (int)(gt % L);
@@ -528,6 +534,7 @@ __global__ void __launch_bounds__(STPB) k_dpc(StepConst c, const Scal* __restric
 // ---------------------------------------------------------------------------
 template <int D, int L>
 __global__ void __launch_bounds__(STPB) k_xsph(StepConst c, const Scal* __restrict__ sc, int64_t N, SArr<D> S) {
+  if (*S.ovf) return;
   const int64_t gt = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int64_t k = gt / L;
   const int lane = (int)(gt % L);
@@ -564,6 +571,7 @@ __global__ void __launch_bounds__(STPB) k_xsph(StepConst c, const Scal* __restri
 // ---------------------------------------------------------------------------
 template <int D, int L>
 __global__ void __launch_bounds__(STPB) k_cspm(StepConst c, int64_t N, SArr<D> S) {
+  if (*S.ovf) return;
   const int64_t gt = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int64_t k = gt / L;
   const int lane = (int)(gt % L);
@@ -600,6 +608,7 @@ __global__ void __launch_bounds__(STPB) k_cspm(StepConst c, int64_t N, SArr<D> S
 // ---------------------------------------------------------------------------
 template <int D>
 __global__ void __launch_bounds__(STPB) k_dt_reduce(StepConst c, Scal* __restrict__ sc, int64_t N, SArr<D> S) {
+  if (*S.ovf) return;
   int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   double am = 0.0, vm = 0.0;
   if (k < N) {
@@ -618,7 +627,7 @@ __global__ void __launch_bounds__(STPB) k_dt_reduce(StepConst c, Scal* __restric
 }
 
 __global__ void k_step_end(StepConst c, Scal* __restrict__ sc) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  if (threadIdx.x != 0 || blockIdx.x != 0 || sc->ovf) return;
   double dt = sc->dt;
   sc->etime = sc->etime + dt;  // prob.etime += prob.Δt, src/sphproblem.jl:331
   if (c.timestepping) {
@@ -722,6 +731,44 @@ __global__ void k_gather_state(StepConst c, int64_t N, const int32_t* __restrict
   }
 }
 
+// destination buffers of an in-loop re-sort
+template <int D>
+struct PermOut {
+  double* x[3];
+  double* xh[3];
+  double* v[3];
+  double* vh[3];
+  double* rho;
+  double* rhoh;
+  int32_t* pt;
+  double* buf2[3];
+};
+
+// new[k] = old[perm[k]] for the whole cell-order state; cΔx restarts at 0
+// (src/sphproblem.jl:229), P(ρ) and 1/ρ are recomputed for stage 1
+template <int D>
+__global__ void k_permute_state(StepConst c, int64_t N, const int32_t* __restrict__ perm, SArr<D> S, PermOut<D> O) {
+  int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= N) return;
+  const int32_t i = perm[k];
+  const int pt = S.pt[i];
+  O.pt[k] = pt;
+  const double r = S.rho[i];
+  O.rho[k] = r;
+  O.rhoh[k] = S.rhoh[i];
+  S.P1[k] = eos(r, c.gamma, c.rho0, c.P0, pt);
+  S.ir[k] = 1.0 / r;
+#pragma unroll
+  for (int d = 0; d < D; ++d) {
+    O.x[d][k] = S.x[d][i];
+    O.xh[d][k] = S.xh[d][i];
+    O.v[d][k] = S.v[d][i];
+    O.vh[d][k] = S.vh[d][i];
+    O.buf2[d][k] = S.buf2[d][i];
+    S.cdx[d][k] = 0.0;
+  }
+}
+
 template <int D>
 __global__ void k_scatter_state(int64_t N, const int32_t* __restrict__ orig, StateIO<D> O, SArr<D> S) {
   int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -765,6 +812,7 @@ struct sph_handle {
   // cell-order working arrays
   DevBuf X[2][3], XH[2][3], V[2][3], VH[2][3], RHO[2], RHOH[2], P1, P2, PT, A[3], DRHO, CDX[3], BUF2[3], PLAST, We,
       GWe[3], IR, IRH;
+  DevBuf PT_b, BUF2_b[3];  // spares for the in-loop re-sort
   int ix = 0, ixh = 0, iv = 0, ivh = 0, irho = 0, irhoh = 0;
   int64_t we_cap = 0;
   int lanes = 0;  // lanes per particle in the pair passes; 0 = by mean row length
@@ -853,7 +901,38 @@ static SArr<D> make_arr(sph_handle* h) {
   S.We = h->We.as<double>();
   S.drho = h->DRHO.as<double>();
   S.Plast = h->PLAST.as<double>();
+  S.ovf = &h->scal.as<Scal>()->ovf;
   return S;
+}
+
+template <int D>
+static PermOut<D> make_alt(sph_handle* h) {
+  PermOut<D> O{};
+  for (int d = 0; d < D; ++d) {
+    O.x[d] = h->X[h->ix ^ 1][d].as<double>();
+    O.xh[d] = h->XH[h->ixh ^ 1][d].as<double>();
+    O.v[d] = h->V[h->iv ^ 1][d].as<double>();
+    O.vh[d] = h->VH[h->ivh ^ 1][d].as<double>();
+    O.buf2[d] = h->BUF2_b[d].as<double>();
+  }
+  O.rho = h->RHO[h->irho ^ 1].as<double>();
+  O.rhoh = h->RHOH[h->irhoh ^ 1].as<double>();
+  O.pt = h->PT_b.as<int32_t>();
+  return O;
+}
+
+// W and ∇W per neighbour entry follow the neighbour CSR's capacity
+template <int D>
+static int grow_entry_arrays(sph_handle* h) {
+  CellCore& core = h->cl->core;
+  if (core.nbr_cap <= h->we_cap) return GCSPH_OK;
+  const int64_t want = core.nbr_cap;
+  int rc;
+  if ((rc = h->We.ensure(sizeof(double) * want, core.st))) return rc;
+  for (int d = 0; d < D; ++d)
+    if ((rc = h->GWe[d].ensure(sizeof(double) * want, core.st))) return rc;
+  h->we_cap = want;
+  return GCSPH_OK;
 }
 
 template <int D>
@@ -891,28 +970,48 @@ static int scatter_state(sph_handle* h) {
 // update! inside stepsolve!: bin the original-order points, sort, gather the
 // whole state into cell order, rebuild the neighbour CSR
 template <int D>
-static int rebuild(sph_handle* h, const StepConst& c) {
+static int rebuild(sph_handle* h, const StepConst& c, int* ovf_dev) {
   CellCore& core = h->cl->core;
   int rc;
-  if (h->in_cell_order && (rc = scatter_state<D>(h))) return rc;
-  if ((rc = core.sort(h->cl->xuser, nullptr))) return rc;
-  h->ix = h->ixh = h->iv = h->ivh = h->irho = h->irhoh = 0;
-  timer_begin(T_STATE, core.st);
-  k_gather_state<D><<<nblocks(h->N, 256), 256, 0, core.st>>>(c, h->N, core.orig.as<int32_t>(), make_io<D>(h),
-                                                            make_arr<D>(h));
-  GC_LAUNCHED();
-  timer_end(T_STATE, core.st);
-  h->in_cell_order = true;
-  double* xs[3] = {h->X[0][0].as<double>(), h->X[0][1].as<double>(), D == 3 ? h->X[0][2].as<double>() : nullptr};
-  if ((rc = core.build_pairs((const double* const*)xs))) return rc;
-  if (core.nfull > h->we_cap) {
-    int64_t want = core.nbr_cap;
-    if ((rc = h->We.ensure(sizeof(double) * want, core.st))) return rc;
-    for (int d = 0; d < D; ++d)
-      if ((rc = h->GWe[d].ensure(sizeof(double) * want, core.st))) return rc;
-    h->we_cap = want;
+  if (!h->in_cell_order) {
+    // first update! of a call: bin the original-order points and gather the state
+    if ((rc = core.sort(h->cl->xuser, nullptr))) return rc;
+    h->ix = h->ixh = h->iv = h->ivh = h->irho = h->irhoh = 0;
+    timer_begin(T_STATE, core.st);
+    k_gather_state<D><<<nblocks(h->N, 256), 256, 0, core.st>>>(c, h->N, core.orig.as<int32_t>(), make_io<D>(h),
+                                                              make_arr<D>(h));
+    GC_LAUNCHED();
+    timer_end(T_STATE, core.st);
+    h->in_cell_order = true;
+  } else {
+    // update! inside the loop: re-bin the cell-ordered points, ties broken by
+    // original index (the same canonical order), then permute the state from
+    // the old cell order straight into the new one
+    const double* xc[3] = {h->X[h->ix][0].as<double>(), h->X[h->ix][1].as<double>(),
+                           D == 3 ? h->X[h->ix][2].as<double>() : nullptr};
+    if ((rc = core.sort(xc, core.orig.as<int32_t>()))) return rc;
+    timer_begin(T_STATE, core.st);
+    k_permute_state<D><<<nblocks(h->N, 256), 256, 0, core.st>>>(c, h->N, core.perm.as<int32_t>(), make_arr<D>(h),
+                                                               make_alt<D>(h));
+    GC_LAUNCHED();
+    timer_end(T_STATE, core.st);
+    h->ix ^= 1;
+    h->ixh ^= 1;
+    h->iv ^= 1;
+    h->ivh ^= 1;
+    h->irho ^= 1;
+    h->irhoh ^= 1;
+    std::swap(h->PT.p, h->PT_b.p);
+    std::swap(h->PT.bytes, h->PT_b.bytes);
+    for (int d = 0; d < D; ++d) {
+      std::swap(h->BUF2[d].p, h->BUF2_b[d].p);
+      std::swap(h->BUF2[d].bytes, h->BUF2_b[d].bytes);
+    }
   }
-  return GCSPH_OK;
+  const double* xs[3] = {h->X[h->ix][0].as<double>(), h->X[h->ix][1].as<double>(),
+                         D == 3 ? h->X[h->ix][2].as<double>() : nullptr};
+  if ((rc = core.build_pairs(xs, ovf_dev))) return rc;
+  return grow_entry_arrays<D>(h);
 }
 
 // L lanes per particle: one launch per pair pass, N*L threads
@@ -932,7 +1031,7 @@ static int rebuild(sph_handle* h, const StepConst& c) {
 static int choose_lanes(const sph_handle* h) {
   if (h->lanes > 0) return h->lanes;
   const CellCore& core = h->cl->core;
-  double mean = h->N > 0 ? (double)core.nfull / (double)h->N : 0.0;
+  double mean = h->N > 0 ? (double)core.nfull_est / (double)h->N : 0.0;
   // about four neighbours per lane
   int L = 1;
   while (L < 32 && (double)L * 4.0 < mean) L <<= 1;
@@ -961,13 +1060,16 @@ static int step_impl(sph_handle* h, int32_t n, int timestepping, double tmin, do
   int rc;
   const int nb = nblocks(h->N, STPB);
   for (int32_t it = 0; it < n; ++it) {
+    const int32_t cspm_before = cspmcnt;
     cspmcnt += 1;
+    // per-step device scalars: max|cΔx|, the Δt maxima and the overflow flag
+    GC_CUDA(cudaMemsetAsync(&dsc->maxcdx, 0, 4 * sizeof(unsigned long long), st));
     if (!skip) {
-      if ((rc = rebuild<D>(h, c))) return rc;
+      if ((rc = rebuild<D>(h, c, &dsc->ovf))) return rc;
       skip = true;
       updaten += 1;
     }
-    GC_CUDA(cudaMemsetAsync(&dsc->maxcdx, 0, 3 * sizeof(unsigned long long), st));
+    const int saved[6] = {h->ix, h->ixh, h->iv, h->ivh, h->irho, h->irhoh};
     c.fb_d = 0.4;
     c.fb_r0 = 2.0 * p.dx;
     c.fb_eta2 = 0.01 * (c.fb_r0 * c.fb_r0);
@@ -1017,9 +1119,27 @@ static int step_impl(sph_handle* h, int32_t n, int timestepping, double tmin, do
     }
     k_step_end<<<1, 32, 0, st>>>(c, dsc);
     GC_LAUNCHED();
-    GC_CUDA(cudaMemcpyAsync(&h->pin->maxcdx, &dsc->maxcdx, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+    GC_CUDA(cudaMemcpyAsync(h->pin, dsc, sizeof(Scal), cudaMemcpyDeviceToHost, st));
     GC_CUDA(cudaStreamSynchronize(st));
     timer_collect();
+    if (h->pin->ovf) {
+      // the rebuilt neighbour CSR did not fit: every kernel of this step
+      // skipped, so the state is the re-sorted one -- grow and repeat the step
+      h->ix = saved[0];
+      h->ixh = saved[1];
+      h->iv = saved[2];
+      h->ivh = saved[3];
+      h->irho = saved[4];
+      h->irhoh = saved[5];
+      if ((rc = core.read_nfull())) return rc;
+      if ((rc = core.grow_nbr(core.nfull))) return rc;
+      if ((rc = grow_entry_arrays<D>(h))) return rc;
+      cspmcnt = cspm_before;
+      skip = false;
+      updaten -= 1;
+      it -= 1;
+      continue;
+    }
     unsigned long long bits = h->pin->maxcdx;
     double mc;
     memcpy(&mc, &bits, 8);
@@ -1093,6 +1213,7 @@ int sph_create(gcl_handle* cl, const gcsph_params* prm, double* rho_dev, double*
     E(h->A[d], nb, true);
     E(h->CDX[d], nb, true);
     E(h->BUF2[d], nb, true);
+    E(h->BUF2_b[d], nb, true);
   }
   E(h->rhoh_o, nb, false);
   E(h->P_o, nb, true);
@@ -1107,6 +1228,7 @@ int sph_create(gcl_handle* cl, const gcsph_params* prm, double* rho_dev, double*
   E(h->IR, nb, true);
   E(h->IRH, nb, true);
   E(h->PT, sizeof(int32_t) * N, false);
+  E(h->PT_b, sizeof(int32_t) * N, false);
   E(h->DRHO, nb, true);
   E(h->PLAST, nb, true);
   E(h->scal, sizeof(Scal), true);
@@ -1138,9 +1260,10 @@ void sph_destroy(sph_handle* h) {
   if (!h) return;
   if (h->cl) cudaStreamSynchronize(h->cl->core.st);
   DevBuf* one[] = {&h->rhoh_o, &h->P_o, &h->drho_o, &h->sumW_o, &h->P1, &h->P2, &h->PT, &h->DRHO, &h->PLAST,
-                   &h->We, &h->IR, &h->IRH, &h->scal, &h->RHO[0], &h->RHO[1], &h->RHOH[0], &h->RHOH[1]};
+                   &h->We, &h->IR, &h->IRH, &h->scal, &h->RHO[0], &h->RHO[1], &h->RHOH[0], &h->RHOH[1], &h->PT_b};
   for (DevBuf* b : one) b->release();
   for (int d = 0; d < 3; ++d) {
+    h->BUF2_b[d].release();
     h->vown[d].release();
     h->vh_o[d].release();
     h->xh_o[d].release();

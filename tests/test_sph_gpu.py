@@ -212,6 +212,30 @@ def test_skin_and_timestepping(gpu_pkg, orc, lanes):
     check(orc, prob, ref, case, lanes, [(25, dict(timestepping=True, timelims=lims))] * 3)
 
 
+def test_neighbour_buffers_regrow_mid_step(gpu_pkg, orc):
+    """The cell list is built on a spread-out copy of the particles (few pairs,
+    small neighbour buffers); the particles are then put back and stepped.  The
+    first rebuild inside stepsolve! outgrows the buffers without waiting for
+    the host, every kernel of that step skips, the library grows the buffers
+    and repeats the step: the result must match the oracle started from the
+    compact positions."""
+    case = gpu_pkg.workloads.dam_break_2d(dx=0.04, fluid=(0.6, 0.8), tank=(1.2, 1.0), layer_ptype=(1, 0, 0))
+    centre = case.x.mean(axis=1, keepdims=True)
+    spread = centre + 3.0 * (case.x - centre)
+    system = gpu_pkg.GPUCellList(tuple(spread), case.cellsize, case.dist)
+    few = system.pairsn
+    for d in range(case.D):
+        system.points[d].copy_(torch.from_numpy(np.ascontiguousarray(case.x[d])))
+    prob = gpu_pkg.SPHProblem(system, case.dx, case.h, case.H, gpu_pkg.WendlandC2(dim=2), case.rho, case.ptype,
+                              case.rho0, case.m0, case.dt, case.alpha, case.c0, case.gamma, case.delta, case.CFL)
+    p = orc.default_params(case.dx, case.h, case.H, case.rho0, case.m0, case.dt, case.alpha, case.c0, case.gamma,
+                           case.delta, case.CFL, case.dist)
+    ref = orc.OracleSystem(case.x, case.cellsize, case.dist, case.rho, case.ptype, p)
+    run_both(prob, ref, 10)
+    assert system.pairsn > 2 * few
+    check(orc, prob, ref, case, 0, [(10, {})])
+
+
 @pytest.mark.parametrize("lanes", [2, 4, 8, 16, 32])
 def test_every_lane_width_agrees(gpu_pkg, orc, lanes):
     case = gpu_pkg.workloads.dam_break_2d(dx=0.04, fluid=(0.6, 0.8), tank=(1.2, 1.0), layer_ptype=(1, 0, 0))
