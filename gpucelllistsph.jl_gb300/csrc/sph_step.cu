@@ -468,6 +468,242 @@ __global__ void __launch_bounds__(STPB) k_stage2(StepConst c, Scal* __restrict__
 }
 
 // ---------------------------------------------------------------------------
+// Pair-once stage passes (lanes > 1, the default).  The gather above
+// evaluates every pair twice, once from each side; on GB300 the FP64 pipe is
+// the bound, so here each pair is evaluated once.  Pass A: the smaller-index
+// particle k of every pair walks the larger-index part of its row, computes
+// the pair once and writes both sides' contributions into per-entry slots --
+// slot e in k's row and slot mirror[e] in m's row.  Pass B: each particle sums
+// its whole row in ascending order (deterministic, no atomics) and runs the
+// predictor or the corrector.  Cost: one write + one read of (1+D) doubles per
+// neighbour entry.
+// ---------------------------------------------------------------------------
+struct PairBuf {
+  double* cd;          // ∂ρ/∂t contribution per neighbour entry
+  double* ca[3];       // ∂v/∂t contribution per neighbour entry (gravity not included)
+  const int32_t* mir;  // entry of the same pair in the partner's row
+  const int32_t* up;   // number of larger-index neighbours (row tail) per particle
+};
+
+// all momentum terms of one pair (FAST expressions), summed into f
+template <int D>
+__device__ inline void pair_force_fast(const StepConst& c, int ptk, int ptm, const double* dx, double r2,
+                                       double inv_r2eta, const double* gw, const double* dv, double rk, double rm,
+                                       double irk, double irm, double Pk, double Pm, double* f) {
+  Acc<D> A;
+  A.zero();
+  mom_terms_fast<D>(c, A, ptk, ptm, dx, inv_r2eta, gw, dv, rk, rm, irk, irm, Pk, Pm);
+#pragma unroll
+  for (int d = 0; d < D; ++d) f[d] = (A.p[d] + A.av[d]) + (c.use_visc ? A.vi[d] : 0.0);
+}
+
+template <int D, int STAGE>
+__device__ inline void pair_tail_terms(const StepConst& c, int ptk, int ptm, const double* dxf, const double* dx,
+                                       double r, double* f) {
+  Acc<D> A;
+  A.zero();
+  fb_term<D>(c, A, ptk, ptm, dxf, dotD<D>(dxf, dxf));
+  if (c.use_pF) pf_term<D>(c, A, ptk, ptm, dx, r);
+#pragma unroll
+  for (int d = 0; d < D; ++d) f[d] = (f[d] + A.fb[d]) + (c.use_pF ? A.pf[d] : 0.0);
+}
+
+template <int D, int L, int STAGE>
+__global__ void __launch_bounds__(STPB) k_pairA(StepConst c, int64_t N, SArr<D> S, PairBuf B) {
+  if (*S.ovf) return;
+  const int64_t gt = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t k = gt / L;
+  const int lane = (int)(gt % L);
+  if (k >= N) return;
+  // stage 1 at (x, ρ, v, P(ρ)); stage 2 at (xΔt½, ρΔt½, vΔt½, P(ρΔt½)) with stage-1 ∇W, fb at x
+  const double* const* XP = STAGE == 1 ? S.x : S.xh;
+  const double* const* VP = STAGE == 1 ? S.v : S.vh;
+  const double* RP = STAGE == 1 ? S.rho : S.rhoh;
+  const double* PP = STAGE == 1 ? S.P1 : S.P2;
+  const double* IP = STAGE == 1 ? S.ir : S.irh;
+  double xk[D], vk[D], xf[D];
+#pragma unroll
+  for (int d = 0; d < D; ++d) {
+    xk[d] = XP[d][k];
+    vk[d] = VP[d][k];
+    xf[d] = S.x[d][k];
+  }
+  const double rk = RP[k], Pk = PP[k], irk = IP[k];
+  const int ptk = S.pt[k];
+  const int64_t e1 = S.rs[k + 1];
+  const int64_t e0 = e1 - B.up[k];
+  for (int64_t e = e0 + lane; e < e1; e += L) {
+    const int32_t m = S.nbr[e];
+    const int32_t me = B.mir[e];
+    double dx[D], dv[D], gw[D];
+#pragma unroll
+    for (int d = 0; d < D; ++d) { dx[d] = xk[d] - XP[d][m]; dv[d] = vk[d] - VP[d][m]; }
+    const double r2 = dotD<D>(dx, dx);
+    double r;
+    if (STAGE == 1) {
+      const double ri = rsqrt(r2);
+      r = r2 > 0.0 ? r2 * ri : 0.0;
+      const double u = r * c.Hinv;
+      const double w = wc2_w(u, c.nW);
+      const double dwk_r = wc2_dw(u, c.nDW) * ri;
+      S.We[e] = w;
+      S.We[me] = w;
+#pragma unroll
+      for (int d = 0; d < D; ++d) {
+        gw[d] = dx[d] * dwk_r;
+        S.gWe[d][e] = gw[d];
+        S.gWe[d][me] = -gw[d];
+      }
+    } else {
+      r = c.use_pF ? (r2 > 0.0 ? r2 * rsqrt(r2) : 0.0) : 0.0;
+#pragma unroll
+      for (int d = 0; d < D; ++d) gw[d] = S.gWe[d][e];
+    }
+    const int ptm = S.pt[m];
+    const double rm = RP[m], irm = IP[m];
+    const bool both = ptk > 0 && ptm > 0;
+    double dk = 0.0, dm = 0.0;
+    const double inv_r2eta = both ? 1.0 / (r2 + c.eta2) : 0.0;
+    if (both) {
+      const double dot3 = -dotD<D>(dx, gw);
+      const double m0dot = c.m0 * dotD<D>(dv, gw);
+      dk = m0dot;
+      dm = m0dot;
+      if (ptk > 1) {
+        const double dp = c.rho0 * powfancy7th_1div(1.0 + c.DDTgz * dx[1], c.ginv, c.gamma) - c.rho0;
+        dk += c.DDTkh * ((rm - rk) - dp) * inv_r2eta * dot3 * c.m0 * irm;
+      }
+      if (ptm > 1) {
+        const double dn = c.rho0 * powfancy7th_1div(1.0 - c.DDTgz * dx[1], c.ginv, c.gamma) - c.rho0;
+        dm += c.DDTkh * ((rk - rm) - dn) * inv_r2eta * dot3 * c.m0 * irk;
+      }
+    }
+    double f[D];
+    pair_force_fast<D>(c, ptk, ptm, dx, r2, inv_r2eta, gw, dv, rk, rm, irk, irm, Pk, PP[m], f);
+    double dxf[D];
+#pragma unroll
+    for (int d = 0; d < D; ++d) dxf[d] = STAGE == 1 ? dx[d] : xf[d] - S.x[d][m];
+    pair_tail_terms<D, STAGE>(c, ptk, ptm, dxf, dx, r, f);
+    B.cd[e] = dk;
+    B.cd[me] = dm;
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      B.ca[d][e] = f[d];
+      B.ca[d][me] = -f[d];
+    }
+  }
+}
+
+// pass B, stage 1: row sums + the three half-step predictors
+template <int D>
+__global__ void __launch_bounds__(STPB) k_pairB1(StepConst c, const Scal* __restrict__ sc, int64_t N, SArr<D> S,
+                                                 PairBuf B) {
+  if (*S.ovf) return;
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= N) return;
+  double drho = 0.0, a[D];
+#pragma unroll
+  for (int d = 0; d < D; ++d) a[d] = 0.0;
+  for (int64_t e = S.rs[k]; e < S.rs[k + 1]; ++e) {
+    drho += B.cd[e];
+#pragma unroll
+    for (int d = 0; d < D; ++d) a[d] += B.ca[d][e];
+  }
+  a[1] = a[1] - c.g;
+  const int ptk = S.pt[k];
+  const double hdt = sc->dt * 0.5;
+  double rv = S.rhoh[k] + drho * hdt;
+  if (rv < c.rho0 && ptk < 0) rv = c.rho0;
+  S.rhoh[k] = rv;
+#pragma unroll
+  for (int d = 0; d < D; ++d) {
+    double vh = S.vh[d][k];
+    if (ptk > 1) vh = vh + a[d] * hdt;
+    S.vh[d][k] = vh;
+    S.xh[d][k] = S.xh[d][k] + vh * hdt;
+  }
+  S.P2[k] = eos(rv, c.gamma, c.rho0, c.P0, ptk);
+  S.irh[k] = 1.0 / rv;
+}
+
+// pass B, stage 2: row sums + symplectic_update! + max |cΔx|
+template <int D>
+__global__ void __launch_bounds__(STPB) k_pairB2(StepConst c, Scal* __restrict__ sc, int64_t N, SArr<D> S,
+                                                 PairBuf B) {
+  if (*S.ovf) return;
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  double mc = 0.0;
+  if (k < N) {
+    const double dt = sc->dt;
+    double drho = 0.0, a[D];
+#pragma unroll
+    for (int d = 0; d < D; ++d) a[d] = 0.0;
+    for (int64_t e = S.rs[k]; e < S.rs[k + 1]; ++e) {
+      drho += B.cd[e];
+#pragma unroll
+      for (int d = 0; d < D; ++d) a[d] += B.ca[d][e];
+    }
+    a[1] = a[1] - c.g;
+    const int ptk = S.pt[k];
+    S.drho[k] = drho;
+    S.Plast[k] = S.P2[k];
+    const double epsi = -(drho / S.rhoh[k]) * dt;
+    double rv = S.rho[k] * (2.0 - epsi) / (2.0 + epsi);
+    if (rv < c.rho0 && ptk <= 1) rv = c.rho0;
+    S.rho[k] = rv;
+    S.rhoho[k] = rv;
+    S.P1[k] = eos(rv, c.gamma, c.rho0, c.P0, ptk);
+    S.ir[k] = 1.0 / rv;
+    const double ml = ptk > 1 ? 1.0 : 0.0;
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      S.a[d][k] = a[d];
+      const double vv = S.v[d][k];
+      const double nv = vv + a[d] * dt * ml;
+      S.vho[d][k] = nv;
+      S.v[d][k] = nv;
+      const double ddx = (vv + nv) * 0.5 * dt;
+      const double cd = S.cdx[d][k] + ddx;
+      S.cdx[d][k] = cd;
+      mc = fmax(mc, fabs(cd));
+      const double xv = S.x[d][k] + ddx;
+      S.xho[d][k] = xv;
+      S.xo[d][k] = xv;
+    }
+  }
+  mc = warp_max(mc);
+  __shared__ double smax[STPB / 32];
+  if ((threadIdx.x & 31) == 0) smax[threadIdx.x >> 5] = mc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double m = smax[0];
+    for (int w = 1; w < STPB / 32; ++w) m = fmax(m, smax[w]);
+    atomic_max_pos(&sc->maxcdx, m);
+  }
+}
+
+// mirror index of every pair entry: position of k in the row of its partner m
+__global__ void k_mirror(int64_t N, const int64_t* __restrict__ rs, const int32_t* __restrict__ nbr,
+                         const int32_t* __restrict__ cnt_full, const int32_t* __restrict__ cnt_up,
+                         const int* __restrict__ ovf, int32_t* __restrict__ mir) {
+  if (*ovf) return;
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= N) return;
+  const int64_t e1 = rs[k + 1];
+  for (int64_t e = e1 - cnt_up[k]; e < e1; ++e) {
+    const int32_t m = nbr[e];
+    int64_t lo = rs[m], hi = rs[m] + (cnt_full[m] - cnt_up[m]);  // k sits in m's smaller-index part
+    while (lo < hi) {
+      const int64_t mid = (lo + hi) >> 1;
+      if (nbr[mid] < k) lo = mid + 1;
+      else hi = mid;
+    }
+    mir[e] = (int32_t)lo;
+    mir[lo] = (int32_t)e;
+  }
+}
+
+// ---------------------------------------------------------------------------
 // dpcreg! + update_dpcreg!  (:1500-1553, :1617-1632)
 // ---------------------------------------------------------------------------
 template <int D, int L>
@@ -813,6 +1049,7 @@ struct sph_handle {
   DevBuf X[2][3], XH[2][3], V[2][3], VH[2][3], RHO[2], RHOH[2], P1, P2, PT, A[3], DRHO, CDX[3], BUF2[3], PLAST, We,
       GWe[3], IR, IRH;
   DevBuf PT_b, BUF2_b[3];  // spares for the in-loop re-sort
+  DevBuf CD, CA[3], MIR;    // pair-once passes: per-entry contributions and mirror index
   int ix = 0, ixh = 0, iv = 0, ivh = 0, irho = 0, irhoh = 0;
   int64_t we_cap = 0;
   int lanes = 0;  // lanes per particle in the pair passes; 0 = by mean row length
@@ -929,10 +1166,24 @@ static int grow_entry_arrays(sph_handle* h) {
   const int64_t want = core.nbr_cap;
   int rc;
   if ((rc = h->We.ensure(sizeof(double) * want, core.st))) return rc;
-  for (int d = 0; d < D; ++d)
+  if ((rc = h->CD.ensure(sizeof(double) * want, core.st))) return rc;
+  if ((rc = h->MIR.ensure(sizeof(int32_t) * want, core.st))) return rc;
+  for (int d = 0; d < D; ++d) {
     if ((rc = h->GWe[d].ensure(sizeof(double) * want, core.st))) return rc;
+    if ((rc = h->CA[d].ensure(sizeof(double) * want, core.st))) return rc;
+  }
   h->we_cap = want;
   return GCSPH_OK;
+}
+
+template <int D>
+static PairBuf make_pairbuf(sph_handle* h) {
+  PairBuf B{};
+  B.cd = h->CD.as<double>();
+  for (int d = 0; d < D; ++d) B.ca[d] = h->CA[d].as<double>();
+  B.mir = h->MIR.as<int32_t>();
+  B.up = h->cl->core.cnt_up.as<int32_t>();
+  return B;
 }
 
 template <int D>
@@ -1011,7 +1262,12 @@ static int rebuild(sph_handle* h, const StepConst& c, int* ovf_dev) {
   const double* xs[3] = {h->X[h->ix][0].as<double>(), h->X[h->ix][1].as<double>(),
                          D == 3 ? h->X[h->ix][2].as<double>() : nullptr};
   if ((rc = core.build_pairs(xs, ovf_dev))) return rc;
-  return grow_entry_arrays<D>(h);
+  if ((rc = grow_entry_arrays<D>(h))) return rc;
+  k_mirror<<<nblocks(h->N, 256), 256, 0, core.st>>>(h->N, core.rs_full.as<int64_t>(), core.nbr.as<int32_t>(),
+                                                      core.cnt_full.as<int32_t>(), core.cnt_up.as<int32_t>(), ovf_dev,
+                                                      h->MIR.as<int32_t>());
+  GC_LAUNCHED();
+  return GCSPH_OK;
 }
 
 // L lanes per particle: one launch per pair pass, N*L threads
@@ -1027,6 +1283,29 @@ static int rebuild(sph_handle* h, const StepConst& c, int* ovf_dev) {
       default: KER<D, 32><<<_g, STPB, 0, st>>>(__VA_ARGS__); break;                           \
     }                                                                                         \
   } while (0)
+
+// pass A walks only the larger-index half of each row
+#define PAIRA_LAUNCH(L, STAGE, ...)                                                           \
+  do {                                                                                        \
+    const int _g = nblocks(h->N * (int64_t)(L), STPB);                                        \
+    switch (L) {                                                                              \
+      case 1: k_pairA<D, 1, STAGE><<<_g, STPB, 0, st>>>(__VA_ARGS__); break;                  \
+      case 2: k_pairA<D, 2, STAGE><<<_g, STPB, 0, st>>>(__VA_ARGS__); break;                  \
+      case 4: k_pairA<D, 4, STAGE><<<_g, STPB, 0, st>>>(__VA_ARGS__); break;                  \
+      case 8: k_pairA<D, 8, STAGE><<<_g, STPB, 0, st>>>(__VA_ARGS__); break;                  \
+      case 16: k_pairA<D, 16, STAGE><<<_g, STPB, 0, st>>>(__VA_ARGS__); break;                \
+      default: k_pairA<D, 32, STAGE><<<_g, STPB, 0, st>>>(__VA_ARGS__); break;                \
+    }                                                                                         \
+  } while (0)
+
+static int choose_lanes_upper(const sph_handle* h) {
+  if (h->lanes > 1) return h->lanes;
+  const CellCore& core = h->cl->core;
+  double mean = h->N > 0 ? 0.5 * (double)core.nfull_est / (double)h->N : 0.0;
+  int L = 1;
+  while (L < 32 && (double)L * 4.0 < mean) L <<= 1;
+  return L;
+}
 
 static int choose_lanes(const sph_handle* h) {
   if (h->lanes > 0) return h->lanes;
@@ -1073,16 +1352,30 @@ static int step_impl(sph_handle* h, int32_t n, int timestepping, double tmin, do
     c.fb_d = 0.4;
     c.fb_r0 = 2.0 * p.dx;
     c.fb_eta2 = 0.01 * (c.fb_r0 * c.fb_r0);
-    timer_begin(T_STAGE1, st);
     const int L = choose_lanes(h);
-    PAIR_LAUNCH(k_stage1, L, c, dsc, h->N, make_arr<D>(h));
+    const bool once = L > 1;  // pair-once passes; L = 1 keeps the serial gather (bit-identical to the oracle)
+    const int LA = choose_lanes_upper(h);
+    timer_begin(T_STAGE1, st);
+    if (once) {
+      PAIRA_LAUNCH(LA, 1, c, h->N, make_arr<D>(h), make_pairbuf<D>(h));
+      GC_LAUNCHED();
+      k_pairB1<D><<<nb, STPB, 0, st>>>(c, dsc, h->N, make_arr<D>(h), make_pairbuf<D>(h));
+    } else {
+      PAIR_LAUNCH(k_stage1, L, c, dsc, h->N, make_arr<D>(h));
+    }
     GC_LAUNCHED();
     timer_end(T_STAGE1, st);
     c.fb_d = p.bound_D;
     c.fb_r0 = p.bound_l;
     c.fb_eta2 = 0.01 * (c.fb_r0 * c.fb_r0);
     timer_begin(T_STAGE2, st);
-    PAIR_LAUNCH(k_stage2, L, c, dsc, h->N, make_arr<D>(h));
+    if (once) {
+      PAIRA_LAUNCH(LA, 2, c, h->N, make_arr<D>(h), make_pairbuf<D>(h));
+      GC_LAUNCHED();
+      k_pairB2<D><<<nb, STPB, 0, st>>>(c, dsc, h->N, make_arr<D>(h), make_pairbuf<D>(h));
+    } else {
+      PAIR_LAUNCH(k_stage2, L, c, dsc, h->N, make_arr<D>(h));
+    }
     GC_LAUNCHED();
     timer_end(T_STAGE2, st);
     h->ix ^= 1;
@@ -1262,7 +1555,10 @@ void sph_destroy(sph_handle* h) {
   DevBuf* one[] = {&h->rhoh_o, &h->P_o, &h->drho_o, &h->sumW_o, &h->P1, &h->P2, &h->PT, &h->DRHO, &h->PLAST,
                    &h->We, &h->IR, &h->IRH, &h->scal, &h->RHO[0], &h->RHO[1], &h->RHOH[0], &h->RHOH[1], &h->PT_b};
   for (DevBuf* b : one) b->release();
+  h->CD.release();
+  h->MIR.release();
   for (int d = 0; d < 3; ++d) {
+    h->CA[d].release();
     h->BUF2_b[d].release();
     h->vown[d].release();
     h->vh_o[d].release();

@@ -66,7 +66,7 @@ def gpu_field(prob, name):
     return (torch.stack(f) if isinstance(f, tuple) else f).cpu().numpy()
 
 
-def noise_floor(orc, case, calls, v=None, seeds=(1, 2)):
+def noise_floor(orc, case, calls, v=None, seeds=(1, 2, 3, 4)):
     """How far the reference's own algorithm moves under another summation
     order: the oracle re-run with its pair list shuffled (an order the
     reference's atomics may produce on any run), per field, normwise."""
@@ -102,13 +102,13 @@ def compare(prob, ref, case, fields=FIELDS, rtol=RTOL, exact=True, floor=None):
     the CUDA gather walks each neighbour row in the order the serial oracle
     scatters over its canonically ordered pair list, with identical per-pair
     arithmetic, so no summation-order difference is left.  With a noise floor
-    (lanes > 1 re-associate the sums) a field may also sit within 8x of how
-    far the reference moves under another summation order -- the P of a
+    (lanes > 1 re-associate the sums) a field may also sit within 16x of the
+    largest of four re-orderings of the reference's own sums -- the P of a
     barely compressed column, (ρ/ρ₀)^7 - 1, is that ill-conditioned."""
     errs = {}
     for name in fields:
         errs[name] = relerr(gpu_field(prob, name), ref.get(name))
-    tol = {k: max(rtol, 8.0 * (floor or {}).get(k, 0.0)) for k in fields}
+    tol = {k: max(rtol, 16.0 * (floor or {}).get(k, 0.0)) for k in fields}
     bad = {k: (v, tol[k]) for k, v in errs.items() if not v <= tol[k]}
     assert not bad, f"fields over tolerance (err, tol): {bad}"
     if exact:
