@@ -63,6 +63,8 @@ _SIGS = {
     "sph_set_params": (C.c_int, [vp, C.POINTER(gcsph_params)]),
     "sph_get_params": (C.c_int, [vp, C.POINTER(gcsph_params)]),
     "sph_set_lanes": (C.c_int, [vp, i32]),
+    "sph_set_graphs": (C.c_int, [vp, i32]),
+    "sph_graph_stats": (C.c_int, [vp, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
     "sph_step": (C.c_int, [vp, i32, C.c_int, f64, f64, C.POINTER(i64), C.POINTER(f64)]),
     "sph_get_field": (C.c_int, [vp, i32, vp]),
     "gcsph_dpckernlim": (f64, [i32]),

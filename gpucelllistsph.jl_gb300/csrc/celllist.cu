@@ -628,6 +628,7 @@ int CellCore::grow_nbr(int64_t need) {
   int rc = nbr.ensure(sizeof(int32_t) * want, st);
   if (rc) return rc;
   nbr_cap = want;
+  gen += 1;
   return GCSPH_OK;
 }
 

@@ -39,6 +39,7 @@ struct CellCore {
   int64_t* pin = nullptr;  // pinned host scalars
   int64_t nfull = 0, nup = 0, nbr_cap = 0;
   int64_t nfull_est = 0;  // last neighbour-entry count read back (lane choice); nfull is -1 while unknown
+  int64_t gen = 0;        // bumped whenever a buffer a captured step graph points into is reallocated
   bool sorted = false, built = false, up_valid = false;
   int lanes = 0;  // lanes per particle in the pair search; 0 = by mean candidate count
   int pair_lanes() const;

@@ -41,8 +41,8 @@ void count_launch(int n) { g_launches.fetch_add((unsigned long long)n, std::memo
 // ---------------------------------------------------------------------------
 // timers
 // ---------------------------------------------------------------------------
-static const char* kTimerNames[T_COUNT] = {"stage1", "stage2", "dpc", "xsph", "cspm", "sort",
-                                            "pairs",  "state",  "post", "dt"};
+static const char* kTimerNames[T_COUNT] = {"stage1", "stage2", "dpc", "xsph", "cspm",  "sort",
+                                            "pairs",  "state",  "post", "dt",   "rowsum"};
 struct TimerState {
   std::mutex mu;
   bool on = false;
@@ -63,8 +63,43 @@ static TimerState g_timer;
 
 bool timing_on() { return g_timer.on; }
 
+static thread_local std::vector<TimerRec>* t_sink = nullptr;
+static thread_local cudaEvent_t t_open[T_COUNT];
+
+void timer_capture_to(std::vector<TimerRec>* sink) {
+  t_sink = sink;
+  for (int i = 0; i < T_COUNT; ++i) t_open[i] = nullptr;
+}
+
+void timer_account(const std::vector<TimerRec>& recs) {
+  if (!g_timer.on || recs.empty()) return;
+  std::lock_guard<std::mutex> lk(g_timer.mu);
+  for (const TimerRec& r : recs) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, r.a, r.b) != cudaSuccess) continue;
+    g_timer.ms[r.id] += ms;
+    g_timer.launches[r.id] += 1;
+  }
+  cudaGetLastError();
+}
+
+void timer_release(std::vector<TimerRec>& recs) {
+  for (TimerRec& r : recs) {
+    if (r.a) cudaEventDestroy(r.a);
+    if (r.b) cudaEventDestroy(r.b);
+  }
+  recs.clear();
+}
+
 void timer_begin(int id, cudaStream_t s) {
   if (!g_timer.on) return;
+  if (t_sink) {
+    cudaEvent_t e = nullptr;
+    if (cudaEventCreate(&e) != cudaSuccess) return;
+    cudaEventRecordWithFlags(e, s, cudaEventRecordExternal);
+    t_open[id] = e;
+    return;
+  }
   std::lock_guard<std::mutex> lk(g_timer.mu);
   cudaEvent_t e = g_timer.get();
   cudaEventRecord(e, s);
@@ -73,6 +108,16 @@ void timer_begin(int id, cudaStream_t s) {
 
 void timer_end(int id, cudaStream_t s) {
   if (!g_timer.on) return;
+  if (t_sink) {
+    cudaEvent_t a = t_open[id];
+    if (!a) return;
+    cudaEvent_t b = nullptr;
+    if (cudaEventCreate(&b) != cudaSuccess) return;
+    cudaEventRecordWithFlags(b, s, cudaEventRecordExternal);
+    t_sink->push_back({id, a, b});
+    t_open[id] = nullptr;
+    return;
+  }
   std::lock_guard<std::mutex> lk(g_timer.mu);
   cudaEvent_t a = g_timer.open[id];
   if (!a) return;

@@ -5,6 +5,7 @@
 // contraction); the CPU oracle uses the same operation order, so the two agree
 // bit-for-bit up to summation order and libm's cos.
 #pragma once
+#include <vector>
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <string.h>
@@ -184,12 +185,22 @@ int exclusive_scan_i32_to_i32(const int32_t* in, int32_t* out, int64_t n, int64_
 // per-kernel-family CUDA-event timers (off unless gcsph_timing_enable(1))
 // ----------------------------------------------------------------------------
 enum TimerId {
-  T_STAGE1 = 0, T_STAGE2, T_DPC, T_XSPH, T_CSPM, T_SORT, T_PAIRS, T_STATE, T_POST, T_DT, T_COUNT
+  T_STAGE1 = 0, T_STAGE2, T_DPC, T_XSPH, T_CSPM, T_SORT, T_PAIRS, T_STATE, T_POST, T_DT, T_ROWSUM, T_COUNT
 };
 bool timing_on();
 void timer_begin(int id, cudaStream_t s);
 void timer_end(int id, cudaStream_t s);
 void timer_collect();  // after a stream sync: fold finished event pairs into the totals
+// timers inside a captured graph: while a sink is set, timer_begin/timer_end
+// record external event nodes into the capture and list them in the sink;
+// after each replay has finished, timer_account folds their intervals in
+struct TimerRec {
+  int id;
+  cudaEvent_t a, b;
+};
+void timer_capture_to(std::vector<TimerRec>* sink);
+void timer_account(const std::vector<TimerRec>& recs);
+void timer_release(std::vector<TimerRec>& recs);
 
 // device buffer helper
 struct DevBuf {

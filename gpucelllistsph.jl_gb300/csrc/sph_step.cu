@@ -20,6 +20,7 @@
 // Arrays that a pass reads from neighbours and also updates are ping-ponged.
 #include <math.h>
 #include "celllist.cuh"
+#include "pf7_series.cuh"
 
 namespace gcsph {
 
@@ -34,6 +35,8 @@ struct StepConst {
   double cfl, dt_eta2;          // Δt_stepping
   double tmin, tmax;
   int gamma, use_visc, use_pF, timestepping;
+  double reb_thr;  // update! is due after a step whose max |cΔx| passes this (0.9 (dist - H))
+  int count_reb;   // this step's decision counts toward the call's update! total
 };
 
 // device scalars of a running solve
@@ -45,7 +48,8 @@ struct Scal {
   unsigned long long vmax;    // bits of max |h v.x/(x.x+η²)|
   int ovf;                    // the neighbour CSR outgrew its buffers: this step's kernels skip
   int pad0;
-  double pad[2];
+  unsigned long long maxout;  // bits of the largest max |cΔx| of the call (stepsolve!'s second result)
+  long long nreb;             // update! calls of the call (stepsolve!'s first result)
 };
 
 template <int D>
@@ -470,20 +474,42 @@ __global__ void __launch_bounds__(STPB) k_stage2(StepConst c, Scal* __restrict__
 // ---------------------------------------------------------------------------
 // Pair-once stage passes (lanes > 1, the default).  The gather above
 // evaluates every pair twice, once from each side; on GB300 the FP64 pipe is
-// the bound, so here each pair is evaluated once.  Pass A: the smaller-index
-// particle k of every pair walks the larger-index part of its row, computes
-// the pair once and writes both sides' contributions into per-entry slots --
-// slot e in k's row and slot mirror[e] in m's row.  Pass B: each particle sums
-// its whole row in ascending order (deterministic, no atomics) and runs the
-// predictor or the corrector.  Cost: one write + one read of (1+D) doubles per
-// neighbour entry.
+// the bound, so here each pair is evaluated once.  Pass A: one thread per pair
+// (k, m), k < m in cell order -- every thread has the same work, whatever the
+// row lengths -- computes the pair and writes both sides' contributions into
+// per-entry slots: slot e in k's row and slot mirror(e) in m's row.  Pass B:
+// each particle sums its whole row (L lanes, fixed order -- deterministic, no
+// atomics) and runs the predictor or the corrector.  Cost: one write + one
+// read of (1+D) doubles per neighbour entry.
 // ---------------------------------------------------------------------------
 struct PairBuf {
-  double* cd;          // ∂ρ/∂t contribution per neighbour entry
-  double* ca[3];       // ∂v/∂t contribution per neighbour entry (gravity not included)
-  const int32_t* mir;  // entry of the same pair in the partner's row
-  const int32_t* up;   // number of larger-index neighbours (row tail) per particle
+  double* cd;             // ∂ρ/∂t contribution per neighbour entry
+  double* ca[3];          // ∂v/∂t contribution per neighbour entry (gravity not included)
+  const int4* pq;         // (k, m, e, mirror(e)) of every pair, k < m
+  const int64_t* npair;   // number of pairs (device scalar)
 };
+
+// powfancy7th(x) - 1 for x = 1 + eps, src/gpukernels_sph.jl:499-515.  Where
+// |eps| <= PF7_EPS_MAX the exact Taylor series of that iteration's output
+// (gen_pf7_series.py, bias included) replaces its two divisions; elsewhere
+// the iteration itself runs.  eps is taken as (1 + eps) - 1, the argument the
+// reference's rounded x carries.  Callers form ρ0 (1 + r) - ρ0 as the
+// reference forms ρ0 t - ρ0: 1 + r rounds to the t the iteration returns.
+__device__ inline double pf7m1_fast(double eps_in, double ginv, int gamma) {
+  const double x = 1.0 + eps_in;
+  const double e = x - 1.0;  // exact for x in [0.5, 2]
+  if (gamma == 7 && fabs(e) <= PF7_EPS_MAX) {
+    const double cu[PF7_UP_N] = PF7_UP_C;
+    const double cl[PF7_LO_N] = PF7_LO_C;
+    static_assert(PF7_UP_N == PF7_LO_N, "series lengths");
+    const bool up = e >= 0.0;
+    double r = up ? cu[PF7_UP_N - 1] : cl[PF7_UP_N - 1];
+#pragma unroll
+    for (int i = PF7_UP_N - 2; i >= 0; --i) r = fma(r, e, up ? cu[i] : cl[i]);
+    return r;
+  }
+  return powfancy7th_1div(x, ginv, gamma) - 1.0;
+}
 
 // all momentum terms of one pair (FAST expressions), summed into f
 template <int D>
@@ -508,107 +534,112 @@ __device__ inline void pair_tail_terms(const StepConst& c, int ptk, int ptm, con
   for (int d = 0; d < D; ++d) f[d] = (f[d] + A.fb[d]) + (c.use_pF ? A.pf[d] : 0.0);
 }
 
-template <int D, int L, int STAGE>
-__global__ void __launch_bounds__(STPB) k_pairA(StepConst c, int64_t N, SArr<D> S, PairBuf B) {
+template <int D, int STAGE>
+__global__ void __launch_bounds__(STPB) k_pairA(StepConst c, SArr<D> S, PairBuf B) {
   if (*S.ovf) return;
-  const int64_t gt = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const int64_t k = gt / L;
-  const int lane = (int)(gt % L);
-  if (k >= N) return;
+  const int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (u >= *B.npair) return;
+  const int4 q = B.pq[u];
+  const int k = q.x, m = q.y, e = q.z, me = q.w;
   // stage 1 at (x, ρ, v, P(ρ)); stage 2 at (xΔt½, ρΔt½, vΔt½, P(ρΔt½)) with stage-1 ∇W, fb at x
   const double* const* XP = STAGE == 1 ? S.x : S.xh;
   const double* const* VP = STAGE == 1 ? S.v : S.vh;
   const double* RP = STAGE == 1 ? S.rho : S.rhoh;
   const double* PP = STAGE == 1 ? S.P1 : S.P2;
   const double* IP = STAGE == 1 ? S.ir : S.irh;
-  double xk[D], vk[D], xf[D];
+  double dx[D], dv[D], gw[D];
 #pragma unroll
   for (int d = 0; d < D; ++d) {
-    xk[d] = XP[d][k];
-    vk[d] = VP[d][k];
-    xf[d] = S.x[d][k];
+    dx[d] = XP[d][k] - XP[d][m];
+    dv[d] = VP[d][k] - VP[d][m];
   }
-  const double rk = RP[k], Pk = PP[k], irk = IP[k];
-  const int ptk = S.pt[k];
-  const int64_t e1 = S.rs[k + 1];
-  const int64_t e0 = e1 - B.up[k];
-  for (int64_t e = e0 + lane; e < e1; e += L) {
-    const int32_t m = S.nbr[e];
-    const int32_t me = B.mir[e];
-    double dx[D], dv[D], gw[D];
-#pragma unroll
-    for (int d = 0; d < D; ++d) { dx[d] = xk[d] - XP[d][m]; dv[d] = vk[d] - VP[d][m]; }
-    const double r2 = dotD<D>(dx, dx);
-    double r;
-    if (STAGE == 1) {
-      const double ri = rsqrt(r2);
-      r = r2 > 0.0 ? r2 * ri : 0.0;
-      const double u = r * c.Hinv;
-      const double w = wc2_w(u, c.nW);
-      const double dwk_r = wc2_dw(u, c.nDW) * ri;
-      S.We[e] = w;
-      S.We[me] = w;
-#pragma unroll
-      for (int d = 0; d < D; ++d) {
-        gw[d] = dx[d] * dwk_r;
-        S.gWe[d][e] = gw[d];
-        S.gWe[d][me] = -gw[d];
-      }
-    } else {
-      r = c.use_pF ? (r2 > 0.0 ? r2 * rsqrt(r2) : 0.0) : 0.0;
-#pragma unroll
-      for (int d = 0; d < D; ++d) gw[d] = S.gWe[d][e];
-    }
-    const int ptm = S.pt[m];
-    const double rm = RP[m], irm = IP[m];
-    const bool both = ptk > 0 && ptm > 0;
-    double dk = 0.0, dm = 0.0;
-    const double inv_r2eta = both ? 1.0 / (r2 + c.eta2) : 0.0;
-    if (both) {
-      const double dot3 = -dotD<D>(dx, gw);
-      const double m0dot = c.m0 * dotD<D>(dv, gw);
-      dk = m0dot;
-      dm = m0dot;
-      if (ptk > 1) {
-        const double dp = c.rho0 * powfancy7th_1div(1.0 + c.DDTgz * dx[1], c.ginv, c.gamma) - c.rho0;
-        dk += c.DDTkh * ((rm - rk) - dp) * inv_r2eta * dot3 * c.m0 * irm;
-      }
-      if (ptm > 1) {
-        const double dn = c.rho0 * powfancy7th_1div(1.0 - c.DDTgz * dx[1], c.ginv, c.gamma) - c.rho0;
-        dm += c.DDTkh * ((rk - rm) - dn) * inv_r2eta * dot3 * c.m0 * irk;
-      }
-    }
-    double f[D];
-    pair_force_fast<D>(c, ptk, ptm, dx, r2, inv_r2eta, gw, dv, rk, rm, irk, irm, Pk, PP[m], f);
-    double dxf[D];
-#pragma unroll
-    for (int d = 0; d < D; ++d) dxf[d] = STAGE == 1 ? dx[d] : xf[d] - S.x[d][m];
-    pair_tail_terms<D, STAGE>(c, ptk, ptm, dxf, dx, r, f);
-    B.cd[e] = dk;
-    B.cd[me] = dm;
+  const double r2 = dotD<D>(dx, dx);
+  double r;
+  if (STAGE == 1) {
+    const double ri = rsqrt(r2);
+    r = r2 > 0.0 ? r2 * ri : 0.0;
+    const double u1 = r * c.Hinv;
+    const double w = wc2_w(u1, c.nW);
+    const double dwk_r = wc2_dw(u1, c.nDW) * ri;
+    S.We[e] = w;
+    S.We[me] = w;
 #pragma unroll
     for (int d = 0; d < D; ++d) {
-      B.ca[d][e] = f[d];
-      B.ca[d][me] = -f[d];
+      gw[d] = dx[d] * dwk_r;
+      S.gWe[d][e] = gw[d];
+      S.gWe[d][me] = -gw[d];
     }
+  } else {
+    r = c.use_pF ? (r2 > 0.0 ? r2 * rsqrt(r2) : 0.0) : 0.0;
+#pragma unroll
+    for (int d = 0; d < D; ++d) gw[d] = S.gWe[d][e];
+  }
+  const int ptk = S.pt[k], ptm = S.pt[m];
+  const double rk = RP[k], rm = RP[m], irk = IP[k], irm = IP[m];
+  const bool both = ptk > 0 && ptm > 0;
+  double dk = 0.0, dm = 0.0;
+  const double inv_r2eta = both ? 1.0 / (r2 + c.eta2) : 0.0;
+  if (both) {
+    // ∂ρ∂tDDT!, src/gpukernels_sph.jl:520-575, both sides of the pair
+    const double dot3 = -dotD<D>(dx, gw);
+    const double m0dot = c.m0 * dotD<D>(dv, gw);
+    dk = m0dot;
+    dm = m0dot;
+    const double ez = c.DDTgz * dx[1];
+    if (ptk > 1) {
+      const double dp = c.rho0 * (1.0 + pf7m1_fast(ez, c.ginv, c.gamma)) - c.rho0;
+      dk += c.DDTkh * ((rm - rk) - dp) * inv_r2eta * dot3 * c.m0 * irm;
+    }
+    if (ptm > 1) {
+      const double dn = c.rho0 * (1.0 + pf7m1_fast(-ez, c.ginv, c.gamma)) - c.rho0;
+      dm += c.DDTkh * ((rk - rm) - dn) * inv_r2eta * dot3 * c.m0 * irk;
+    }
+  }
+  double f[D];
+  pair_force_fast<D>(c, ptk, ptm, dx, r2, inv_r2eta, gw, dv, rk, rm, irk, irm, PP[k], PP[m], f);
+  double dxf[D];
+#pragma unroll
+  for (int d = 0; d < D; ++d) dxf[d] = STAGE == 1 ? dx[d] : S.x[d][k] - S.x[d][m];
+  pair_tail_terms<D, STAGE>(c, ptk, ptm, dxf, dx, r, f);
+  B.cd[e] = dk;
+  B.cd[me] = dm;
+#pragma unroll
+  for (int d = 0; d < D; ++d) {
+    B.ca[d][e] = f[d];
+    B.ca[d][me] = -f[d];
   }
 }
 
-// pass B, stage 1: row sums + the three half-step predictors
-template <int D>
-__global__ void __launch_bounds__(STPB) k_pairB1(StepConst c, const Scal* __restrict__ sc, int64_t N, SArr<D> S,
-                                                 PairBuf B) {
-  if (*S.ovf) return;
-  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= N) return;
-  double drho = 0.0, a[D];
+// row sums of the per-entry contributions of particle k, L lanes
+template <int D, int L>
+__device__ inline void row_sums(const SArr<D>& S, const PairBuf& B, int64_t k, int lane, unsigned gm, double& drho,
+                                double* a) {
+  drho = 0.0;
 #pragma unroll
   for (int d = 0; d < D; ++d) a[d] = 0.0;
-  for (int64_t e = S.rs[k]; e < S.rs[k + 1]; ++e) {
+  const int64_t e0 = S.rs[k], e1 = S.rs[k + 1];
+  for (int64_t e = e0 + lane; e < e1; e += L) {
     drho += B.cd[e];
 #pragma unroll
     for (int d = 0; d < D; ++d) a[d] += B.ca[d][e];
   }
+  drho = group_sum<L>(drho, gm);
+#pragma unroll
+  for (int d = 0; d < D; ++d) a[d] = group_sum<L>(a[d], gm);
+}
+
+// pass B, stage 1: row sums + the three half-step predictors
+template <int D, int L>
+__global__ void __launch_bounds__(STPB) k_pairB1(StepConst c, const Scal* __restrict__ sc, int64_t N, SArr<D> S,
+                                                 PairBuf B) {
+  if (*S.ovf) return;
+  const int64_t gt = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t k = gt / L;
+  const int lane = (int)(gt % L);
+  if (k >= N) return;  // whole sub-group leaves together
+  double drho, a[D];
+  row_sums<D, L>(S, B, k, lane, group_mask<L>(), drho, a);
+  if (lane != 0) return;
   a[1] = a[1] - c.g;
   const int ptk = S.pt[k];
   const double hdt = sc->dt * 0.5;
@@ -627,48 +658,46 @@ __global__ void __launch_bounds__(STPB) k_pairB1(StepConst c, const Scal* __rest
 }
 
 // pass B, stage 2: row sums + symplectic_update! + max |cΔx|
-template <int D>
+template <int D, int L>
 __global__ void __launch_bounds__(STPB) k_pairB2(StepConst c, Scal* __restrict__ sc, int64_t N, SArr<D> S,
                                                  PairBuf B) {
-  if (*S.ovf) return;
-  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (*S.ovf) return;  // uniform over the grid, before the block reduction below
+  const int64_t gt = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t k = gt / L;
+  const int lane = (int)(gt % L);
   double mc = 0.0;
   if (k < N) {
-    const double dt = sc->dt;
-    double drho = 0.0, a[D];
+    double drho, a[D];
+    row_sums<D, L>(S, B, k, lane, group_mask<L>(), drho, a);
+    if (lane == 0) {
+      const double dt = sc->dt;
+      a[1] = a[1] - c.g;
+      const int ptk = S.pt[k];
+      S.drho[k] = drho;
+      S.Plast[k] = S.P2[k];
+      const double epsi = -(drho / S.rhoh[k]) * dt;
+      double rv = S.rho[k] * (2.0 - epsi) / (2.0 + epsi);
+      if (rv < c.rho0 && ptk <= 1) rv = c.rho0;
+      S.rho[k] = rv;
+      S.rhoho[k] = rv;
+      S.P1[k] = eos(rv, c.gamma, c.rho0, c.P0, ptk);
+      S.ir[k] = 1.0 / rv;
+      const double ml = ptk > 1 ? 1.0 : 0.0;
 #pragma unroll
-    for (int d = 0; d < D; ++d) a[d] = 0.0;
-    for (int64_t e = S.rs[k]; e < S.rs[k + 1]; ++e) {
-      drho += B.cd[e];
-#pragma unroll
-      for (int d = 0; d < D; ++d) a[d] += B.ca[d][e];
-    }
-    a[1] = a[1] - c.g;
-    const int ptk = S.pt[k];
-    S.drho[k] = drho;
-    S.Plast[k] = S.P2[k];
-    const double epsi = -(drho / S.rhoh[k]) * dt;
-    double rv = S.rho[k] * (2.0 - epsi) / (2.0 + epsi);
-    if (rv < c.rho0 && ptk <= 1) rv = c.rho0;
-    S.rho[k] = rv;
-    S.rhoho[k] = rv;
-    S.P1[k] = eos(rv, c.gamma, c.rho0, c.P0, ptk);
-    S.ir[k] = 1.0 / rv;
-    const double ml = ptk > 1 ? 1.0 : 0.0;
-#pragma unroll
-    for (int d = 0; d < D; ++d) {
-      S.a[d][k] = a[d];
-      const double vv = S.v[d][k];
-      const double nv = vv + a[d] * dt * ml;
-      S.vho[d][k] = nv;
-      S.v[d][k] = nv;
-      const double ddx = (vv + nv) * 0.5 * dt;
-      const double cd = S.cdx[d][k] + ddx;
-      S.cdx[d][k] = cd;
-      mc = fmax(mc, fabs(cd));
-      const double xv = S.x[d][k] + ddx;
-      S.xho[d][k] = xv;
-      S.xo[d][k] = xv;
+      for (int d = 0; d < D; ++d) {
+        S.a[d][k] = a[d];
+        const double vv = S.v[d][k];
+        const double nv = vv + a[d] * dt * ml;
+        S.vho[d][k] = nv;
+        S.v[d][k] = nv;
+        const double ddx = (vv + nv) * 0.5 * dt;
+        const double cd = S.cdx[d][k] + ddx;
+        S.cdx[d][k] = cd;
+        mc = fmax(mc, fabs(cd));
+        const double xv = S.x[d][k] + ddx;
+        S.xho[d][k] = xv;
+        S.xo[d][k] = xv;
+      }
     }
   }
   mc = warp_max(mc);
@@ -682,24 +711,34 @@ __global__ void __launch_bounds__(STPB) k_pairB2(StepConst c, Scal* __restrict__
   }
 }
 
-// mirror index of every pair entry: position of k in the row of its partner m
-__global__ void k_mirror(int64_t N, const int64_t* __restrict__ rs, const int32_t* __restrict__ nbr,
-                         const int32_t* __restrict__ cnt_full, const int32_t* __restrict__ cnt_up,
-                         const int* __restrict__ ovf, int32_t* __restrict__ mir) {
+// the flat pair list of the pair-once passes: pair u = rs_up[k] + j is k's
+// j-th larger-index neighbour m, at entry e of k's row; its mirror is the
+// position of k in the smaller-index part of m's row (binary search, the row
+// is ascending).  QL lanes per particle share its row tail.
+constexpr int QL = 8;
+__global__ void __launch_bounds__(256) k_pair_quads(int64_t N, const int64_t* __restrict__ rs,
+                                                    const int32_t* __restrict__ nbr,
+                                                    const int32_t* __restrict__ cnt_full,
+                                                    const int32_t* __restrict__ cnt_up,
+                                                    const int64_t* __restrict__ rs_up, const int* __restrict__ ovf,
+                                                    int4* __restrict__ pq) {
   if (*ovf) return;
-  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t gt = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t k = gt / QL;
+  const int lane = (int)(gt % QL);
   if (k >= N) return;
   const int64_t e1 = rs[k + 1];
-  for (int64_t e = e1 - cnt_up[k]; e < e1; ++e) {
+  const int64_t e0 = e1 - cnt_up[k];
+  const int64_t u0 = rs_up[k] - e0;
+  for (int64_t e = e0 + lane; e < e1; e += QL) {
     const int32_t m = nbr[e];
-    int64_t lo = rs[m], hi = rs[m] + (cnt_full[m] - cnt_up[m]);  // k sits in m's smaller-index part
+    int64_t lo = rs[m], hi = rs[m] + (cnt_full[m] - cnt_up[m]);
     while (lo < hi) {
       const int64_t mid = (lo + hi) >> 1;
       if (nbr[mid] < k) lo = mid + 1;
       else hi = mid;
     }
-    mir[e] = (int32_t)lo;
-    mir[lo] = (int32_t)e;
+    pq[u0 + e] = make_int4((int)k, (int)m, (int)e, (int)lo);
   }
 }
 
@@ -866,6 +905,10 @@ __global__ void k_step_end(StepConst c, Scal* __restrict__ sc) {
   if (threadIdx.x != 0 || blockIdx.x != 0 || sc->ovf) return;
   double dt = sc->dt;
   sc->etime = sc->etime + dt;  // prob.etime += prob.Δt, src/sphproblem.jl:331
+  // maximum(maximum.(abs, cΔx)) > 0.9 nui  =>  update! before the next step (:325-327)
+  const double mc = __longlong_as_double((long long)sc->maxcdx);
+  if (sc->maxcdx > sc->maxout) sc->maxout = sc->maxcdx;
+  if (c.count_reb && mc > c.reb_thr) sc->nreb += 1;
   if (c.timestepping) {
     double amax = __longlong_as_double((long long)sc->amax);
     double vmax = __longlong_as_double((long long)sc->vmax);
@@ -886,7 +929,9 @@ __global__ void __launch_bounds__(STPB) k_sums_post(StepConst c, int64_t N, cons
                                                      const int32_t* __restrict__ pt, const double* __restrict__ x0,
                                                      const double* __restrict__ x1, const double* __restrict__ x2,
                                                      double* __restrict__ sumW, double* __restrict__ sg0,
-                                                     double* __restrict__ sg1, double* __restrict__ sg2) {
+                                                     double* __restrict__ sg1, double* __restrict__ sg2,
+                                                     const int* __restrict__ ovf) {
+  if (*ovf) return;
   const int64_t gt = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int64_t k = gt / L;
   const int lane = (int)(gt % L);
@@ -1007,6 +1052,7 @@ __global__ void k_permute_state(StepConst c, int64_t N, const int32_t* __restric
 
 template <int D>
 __global__ void k_scatter_state(int64_t N, const int32_t* __restrict__ orig, StateIO<D> O, SArr<D> S) {
+  if (*S.ovf) return;  // a captured call that overflowed leaves the caller's arrays untouched
   int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= N) return;
   const int32_t o = orig[k];
@@ -1033,6 +1079,40 @@ __global__ void k_scatter_state(int64_t N, const int32_t* __restrict__ orig, Sta
 // ===========================================================================
 using namespace gcsph;
 
+// captured stepsolve! calls (see step_graph)
+struct HostSide {
+  int idx[6];
+  void* pt[2];
+  void* buf2[3][2];
+  void* orig[2];
+  bool sorted, built, up_valid, in_cell_order;
+  int64_t nfull;
+};
+
+struct GraphKey {
+  int32_t n, timestepping, lanes, timing;
+  double tmin, tmax;
+  gcsph_params prm;  // dt and etime zeroed: they live on the device
+  int64_t nbr_cap, we_cap, gen;
+  HostSide at;       // buffer indices and pointer pairs at the start
+  const void* user[8];  // the caller's arrays the call reads and writes
+};
+
+struct StepGraph {
+  GraphKey key;
+  cudaGraphExec_t exec = nullptr;
+  HostSide after{};
+  long long launches = 0;
+  std::vector<TimerRec> timers;
+  unsigned long long used = 0;
+};
+
+static void graph_free(StepGraph& g) {
+  if (g.exec) cudaGraphExecDestroy(g.exec);
+  g.exec = nullptr;
+  timer_release(g.timers);
+}
+
 struct sph_handle {
   gcl_handle* cl = nullptr;
   int D = 2;
@@ -1049,13 +1129,18 @@ struct sph_handle {
   DevBuf X[2][3], XH[2][3], V[2][3], VH[2][3], RHO[2], RHOH[2], P1, P2, PT, A[3], DRHO, CDX[3], BUF2[3], PLAST, We,
       GWe[3], IR, IRH;
   DevBuf PT_b, BUF2_b[3];  // spares for the in-loop re-sort
-  DevBuf CD, CA[3], MIR;    // pair-once passes: per-entry contributions and mirror index
+  DevBuf CD, CA[3], PQ;     // pair-once passes: per-entry contributions, flat pair list
   int ix = 0, ixh = 0, iv = 0, ivh = 0, irho = 0, irhoh = 0;
   int64_t we_cap = 0;
   int lanes = 0;  // lanes per particle in the pair passes; 0 = by mean row length
   DevBuf scal;
   Scal* pin = nullptr;
   bool in_cell_order = false;
+  bool use_graphs = true;
+  StepGraph graphs[4];
+  unsigned long long graph_clock = 0;
+  int64_t n_captures = 0, n_replays = 0;
+  cudaStream_t cap_stream = nullptr;  // records captures only; replays run on the cell list's stream
 };
 
 static StepConst make_const(const sph_handle* h) {
@@ -1167,7 +1252,8 @@ static int grow_entry_arrays(sph_handle* h) {
   int rc;
   if ((rc = h->We.ensure(sizeof(double) * want, core.st))) return rc;
   if ((rc = h->CD.ensure(sizeof(double) * want, core.st))) return rc;
-  if ((rc = h->MIR.ensure(sizeof(int32_t) * want, core.st))) return rc;
+  if (want / 2 + 1 > (int64_t)INT32_MAX) return fail(GCSPH_ECAPACITY, "neighbour entries past 2^31");
+  if ((rc = h->PQ.ensure(sizeof(int4) * (want / 2 + 1), core.st))) return rc;
   for (int d = 0; d < D; ++d) {
     if ((rc = h->GWe[d].ensure(sizeof(double) * want, core.st))) return rc;
     if ((rc = h->CA[d].ensure(sizeof(double) * want, core.st))) return rc;
@@ -1181,8 +1267,8 @@ static PairBuf make_pairbuf(sph_handle* h) {
   PairBuf B{};
   B.cd = h->CD.as<double>();
   for (int d = 0; d < D; ++d) B.ca[d] = h->CA[d].as<double>();
-  B.mir = h->MIR.as<int32_t>();
-  B.up = h->cl->core.cnt_up.as<int32_t>();
+  B.pq = h->PQ.as<int4>();
+  B.npair = h->cl->core.rs_up.as<int64_t>() + h->N;
   return B;
 }
 
@@ -1263,10 +1349,16 @@ static int rebuild(sph_handle* h, const StepConst& c, int* ovf_dev) {
                          D == 3 ? h->X[h->ix][2].as<double>() : nullptr};
   if ((rc = core.build_pairs(xs, ovf_dev))) return rc;
   if ((rc = grow_entry_arrays<D>(h))) return rc;
-  k_mirror<<<nblocks(h->N, 256), 256, 0, core.st>>>(h->N, core.rs_full.as<int64_t>(), core.nbr.as<int32_t>(),
-                                                      core.cnt_full.as<int32_t>(), core.cnt_up.as<int32_t>(), ovf_dev,
-                                                      h->MIR.as<int32_t>());
+  // flat pair list: offsets by a device scan (no read-back), then the quads
+  timer_begin(T_PAIRS, core.st);
+  if ((rc = exclusive_scan_i32_to_i64(core.cnt_up.as<int32_t>(), core.rs_up.as<int64_t>(), h->N,
+                                      core.scratch.as<int64_t>(), core.st)))
+    return rc;
+  k_pair_quads<<<nblocks(h->N * QL, 256), 256, 0, core.st>>>(h->N, core.rs_full.as<int64_t>(), core.nbr.as<int32_t>(),
+                                                         core.cnt_full.as<int32_t>(), core.cnt_up.as<int32_t>(),
+                                                         core.rs_up.as<int64_t>(), ovf_dev, h->PQ.as<int4>());
   GC_LAUNCHED();
+  timer_end(T_PAIRS, core.st);
   return GCSPH_OK;
 }
 
@@ -1284,28 +1376,23 @@ static int rebuild(sph_handle* h, const StepConst& c, int* ovf_dev) {
     }                                                                                         \
   } while (0)
 
-// pass A walks only the larger-index half of each row
-#define PAIRA_LAUNCH(L, STAGE, ...)                                                           \
+// pass A: one thread per pair, the grid sized by the entry capacity (the
+// pair count itself stays on the device)
+#define PAIRA_LAUNCH(STAGE, ...)                                                              \
+  k_pairA<D, STAGE><<<nblocks(h->cl->core.nbr_cap / 2 + 1, STPB), STPB, 0, st>>>(__VA_ARGS__)
+
+// pass B: L lanes per row
+#define PAIRB_LAUNCH(KER, L, ...)                                                             \
   do {                                                                                        \
     const int _g = nblocks(h->N * (int64_t)(L), STPB);                                        \
     switch (L) {                                                                              \
-      case 1: k_pairA<D, 1, STAGE><<<_g, STPB, 0, st>>>(__VA_ARGS__); break;                  \
-      case 2: k_pairA<D, 2, STAGE><<<_g, STPB, 0, st>>>(__VA_ARGS__); break;                  \
-      case 4: k_pairA<D, 4, STAGE><<<_g, STPB, 0, st>>>(__VA_ARGS__); break;                  \
-      case 8: k_pairA<D, 8, STAGE><<<_g, STPB, 0, st>>>(__VA_ARGS__); break;                  \
-      case 16: k_pairA<D, 16, STAGE><<<_g, STPB, 0, st>>>(__VA_ARGS__); break;                \
-      default: k_pairA<D, 32, STAGE><<<_g, STPB, 0, st>>>(__VA_ARGS__); break;                \
+      case 2: KER<D, 2><<<_g, STPB, 0, st>>>(__VA_ARGS__); break;                             \
+      case 4: KER<D, 4><<<_g, STPB, 0, st>>>(__VA_ARGS__); break;                             \
+      case 8: KER<D, 8><<<_g, STPB, 0, st>>>(__VA_ARGS__); break;                             \
+      case 16: KER<D, 16><<<_g, STPB, 0, st>>>(__VA_ARGS__); break;                           \
+      default: KER<D, 32><<<_g, STPB, 0, st>>>(__VA_ARGS__); break;                           \
     }                                                                                         \
   } while (0)
-
-static int choose_lanes_upper(const sph_handle* h) {
-  if (h->lanes > 1) return h->lanes;
-  const CellCore& core = h->cl->core;
-  double mean = h->N > 0 ? 0.5 * (double)core.nfull_est / (double)h->N : 0.0;
-  int L = 1;
-  while (L < 32 && (double)L * 4.0 < mean) L <<= 1;
-  return L;
-}
 
 static int choose_lanes(const sph_handle* h) {
   if (h->lanes > 0) return h->lanes;
@@ -1318,18 +1405,133 @@ static int choose_lanes(const sph_handle* h) {
 }
 
 template <int D>
-static int step_impl(sph_handle* h, int32_t n, int timestepping, double tmin, double tmax, int64_t* updaten_out,
-                     double* maxcdx_out) {
+static int finish_call(sph_handle* h, const StepConst& c, Scal* dsc) {
   CellCore& core = h->cl->core;
   cudaStream_t st = core.st;
-  StepConst c = make_const(h);
-  c.timestepping = timestepping;
-  c.tmin = tmin;
-  c.tmax = tmax;
-  Scal* dsc = h->scal.as<Scal>();
+  int rc;
+  if (h->in_cell_order && (rc = scatter_state<D>(h))) return rc;
+  // post-batch ∑W, ∑∇W on the last pair set and the final points
+  if (core.built) {
+    const double* x2 = D == 3 ? h->cl->xuser[2] : h->cl->xuser[0];
+    double* sg2 = D == 3 ? h->sumgW_o[2].as<double>() : h->sumgW_o[0].as<double>();
+    timer_begin(T_POST, st);
+    const int L = choose_lanes(h);
+    PAIR_LAUNCH(k_sums_post, L, c, h->N, core.rs_full.as<int64_t>(), core.nbr.as<int32_t>(),
+                                        core.orig.as<int32_t>(), h->pt_u, h->cl->xuser[0], h->cl->xuser[1], x2,
+                                        h->sumW_o.as<double>(), h->sumgW_o[0].as<double>(),
+                                        h->sumgW_o[1].as<double>(), sg2, &dsc->ovf);
+    GC_LAUNCHED();
+    timer_end(T_POST, st);
+  }
+  return GCSPH_OK;
+}
+
+// everything of one step after update!: both stages, DPC, XSPH, CSPM, Δt.
+// Shared by the eager loop and the graph capture; only the host-side buffer
+// indices change here, in an order fixed by the parameters.
+template <int D>
+static int enqueue_stages(sph_handle* h, StepConst& c, Scal* dsc, int32_t& cspmcnt) {
+  CellCore& core = h->cl->core;
+  cudaStream_t st = core.st;
+  const gcsph_params& p = h->prm;
+  const int nb = nblocks(h->N, STPB);
+  cspmcnt += 1;
+  c.fb_d = 0.4;
+  c.fb_r0 = 2.0 * p.dx;
+  c.fb_eta2 = 0.01 * (c.fb_r0 * c.fb_r0);
+  const int L = choose_lanes(h);
+  const bool once = L > 1;  // pair-once passes; L = 1 keeps the serial gather (bit-identical to the oracle)
+  // stage 1 (predictor) and stage 2 (corrector); the pair-once form times
+  // pass A as the stage and the two row-sum passes together
+  if (once) {
+    timer_begin(T_STAGE1, st);
+    PAIRA_LAUNCH(1, c, make_arr<D>(h), make_pairbuf<D>(h));
+    GC_LAUNCHED();
+    timer_end(T_STAGE1, st);
+    timer_begin(T_ROWSUM, st);
+    PAIRB_LAUNCH(k_pairB1, L, c, dsc, h->N, make_arr<D>(h), make_pairbuf<D>(h));
+    GC_LAUNCHED();
+    timer_end(T_ROWSUM, st);
+  } else {
+    timer_begin(T_STAGE1, st);
+    PAIR_LAUNCH(k_stage1, L, c, dsc, h->N, make_arr<D>(h));
+    GC_LAUNCHED();
+    timer_end(T_STAGE1, st);
+  }
+  c.fb_d = p.bound_D;
+  c.fb_r0 = p.bound_l;
+  c.fb_eta2 = 0.01 * (c.fb_r0 * c.fb_r0);
+  if (once) {
+    timer_begin(T_STAGE2, st);
+    PAIRA_LAUNCH(2, c, make_arr<D>(h), make_pairbuf<D>(h));
+    GC_LAUNCHED();
+    timer_end(T_STAGE2, st);
+    timer_begin(T_ROWSUM, st);
+    PAIRB_LAUNCH(k_pairB2, L, c, dsc, h->N, make_arr<D>(h), make_pairbuf<D>(h));
+    GC_LAUNCHED();
+    timer_end(T_ROWSUM, st);
+  } else {
+    timer_begin(T_STAGE2, st);
+    PAIR_LAUNCH(k_stage2, L, c, dsc, h->N, make_arr<D>(h));
+    GC_LAUNCHED();
+    timer_end(T_STAGE2, st);
+  }
+  h->ix ^= 1;
+  h->ixh ^= 1;
+  h->ivh ^= 1;
+  h->irhoh ^= 1;
+  if (p.dpc_l0 > 0) {
+    timer_begin(T_DPC, st);
+    PAIR_LAUNCH(k_dpc, L, c, dsc, h->N, make_arr<D>(h));
+    GC_LAUNCHED();
+    timer_end(T_DPC, st);
+    h->iv ^= 1;
+    h->ix ^= 1;
+  }
+  if (p.xsph_eps > 0) {
+    timer_begin(T_XSPH, st);
+    PAIR_LAUNCH(k_xsph, L, c, dsc, h->N, make_arr<D>(h));
+    GC_LAUNCHED();
+    timer_end(T_XSPH, st);
+  }
+  if (p.cspmn > 0 && cspmcnt == p.cspmn) {
+    timer_begin(T_CSPM, st);
+    PAIR_LAUNCH(k_cspm, L, c, h->N, make_arr<D>(h));
+    GC_LAUNCHED();
+    timer_end(T_CSPM, st);
+    h->irho ^= 1;
+    cspmcnt = 0;
+  }
+  if (c.timestepping) {
+    timer_begin(T_DT, st);
+    k_dt_reduce<D><<<nb, STPB, 0, st>>>(c, dsc, h->N, make_arr<D>(h));
+    GC_LAUNCHED();
+    timer_end(T_DT, st);
+  }
+  k_step_end<<<1, 32, 0, st>>>(c, dsc);
+  GC_LAUNCHED();
+  return GCSPH_OK;
+}
+
+// device scalars at the start of a call
+static void init_scal(sph_handle* h, int32_t n) {
   h->pin->dt = h->prm.dt;
   h->pin->etime = h->prm.etime;
   h->pin->maxcdx = h->pin->amax = h->pin->vmax = 0;
+  h->pin->ovf = 0;
+  h->pin->pad0 = 0;
+  h->pin->maxout = 0;
+  h->pin->nreb = n > 0 ? 1 : 0;  // the first step always runs update!
+}
+
+// _stepsolve!, one host round trip per step: the host reads the step's
+// scalars, decides update!, and on a neighbour overflow grows and repeats
+template <int D>
+static int step_eager(sph_handle* h, StepConst c, int32_t n, int64_t* updaten_out, double* maxcdx_out) {
+  CellCore& core = h->cl->core;
+  cudaStream_t st = core.st;
+  Scal* dsc = h->scal.as<Scal>();
+  init_scal(h, n);
   GC_CUDA(cudaMemcpyAsync(dsc, h->pin, sizeof(Scal), cudaMemcpyHostToDevice, st));
   const gcsph_params& p = h->prm;
   bool skip = false;
@@ -1337,10 +1539,9 @@ static int step_impl(sph_handle* h, int32_t n, int timestepping, double tmin, do
   double maxout = 0.0;
   int32_t cspmcnt = 0;
   int rc;
-  const int nb = nblocks(h->N, STPB);
+  c.count_reb = 0;
   for (int32_t it = 0; it < n; ++it) {
     const int32_t cspm_before = cspmcnt;
-    cspmcnt += 1;
     // per-step device scalars: max|cΔx|, the Δt maxima and the overflow flag
     GC_CUDA(cudaMemsetAsync(&dsc->maxcdx, 0, 4 * sizeof(unsigned long long), st));
     if (!skip) {
@@ -1349,69 +1550,7 @@ static int step_impl(sph_handle* h, int32_t n, int timestepping, double tmin, do
       updaten += 1;
     }
     const int saved[6] = {h->ix, h->ixh, h->iv, h->ivh, h->irho, h->irhoh};
-    c.fb_d = 0.4;
-    c.fb_r0 = 2.0 * p.dx;
-    c.fb_eta2 = 0.01 * (c.fb_r0 * c.fb_r0);
-    const int L = choose_lanes(h);
-    const bool once = L > 1;  // pair-once passes; L = 1 keeps the serial gather (bit-identical to the oracle)
-    const int LA = choose_lanes_upper(h);
-    timer_begin(T_STAGE1, st);
-    if (once) {
-      PAIRA_LAUNCH(LA, 1, c, h->N, make_arr<D>(h), make_pairbuf<D>(h));
-      GC_LAUNCHED();
-      k_pairB1<D><<<nb, STPB, 0, st>>>(c, dsc, h->N, make_arr<D>(h), make_pairbuf<D>(h));
-    } else {
-      PAIR_LAUNCH(k_stage1, L, c, dsc, h->N, make_arr<D>(h));
-    }
-    GC_LAUNCHED();
-    timer_end(T_STAGE1, st);
-    c.fb_d = p.bound_D;
-    c.fb_r0 = p.bound_l;
-    c.fb_eta2 = 0.01 * (c.fb_r0 * c.fb_r0);
-    timer_begin(T_STAGE2, st);
-    if (once) {
-      PAIRA_LAUNCH(LA, 2, c, h->N, make_arr<D>(h), make_pairbuf<D>(h));
-      GC_LAUNCHED();
-      k_pairB2<D><<<nb, STPB, 0, st>>>(c, dsc, h->N, make_arr<D>(h), make_pairbuf<D>(h));
-    } else {
-      PAIR_LAUNCH(k_stage2, L, c, dsc, h->N, make_arr<D>(h));
-    }
-    GC_LAUNCHED();
-    timer_end(T_STAGE2, st);
-    h->ix ^= 1;
-    h->ixh ^= 1;
-    h->ivh ^= 1;
-    h->irhoh ^= 1;
-    if (p.dpc_l0 > 0) {
-      timer_begin(T_DPC, st);
-      PAIR_LAUNCH(k_dpc, L, c, dsc, h->N, make_arr<D>(h));
-      GC_LAUNCHED();
-      timer_end(T_DPC, st);
-      h->iv ^= 1;
-      h->ix ^= 1;
-    }
-    if (p.xsph_eps > 0) {
-      timer_begin(T_XSPH, st);
-      PAIR_LAUNCH(k_xsph, L, c, dsc, h->N, make_arr<D>(h));
-      GC_LAUNCHED();
-      timer_end(T_XSPH, st);
-    }
-    if (p.cspmn > 0 && cspmcnt == p.cspmn) {
-      timer_begin(T_CSPM, st);
-      PAIR_LAUNCH(k_cspm, L, c, h->N, make_arr<D>(h));
-      GC_LAUNCHED();
-      timer_end(T_CSPM, st);
-      h->irho ^= 1;
-      cspmcnt = 0;
-    }
-    if (timestepping) {
-      timer_begin(T_DT, st);
-      k_dt_reduce<D><<<nb, STPB, 0, st>>>(c, dsc, h->N, make_arr<D>(h));
-      GC_LAUNCHED();
-      timer_end(T_DT, st);
-    }
-    k_step_end<<<1, 32, 0, st>>>(c, dsc);
-    GC_LAUNCHED();
+    if ((rc = enqueue_stages<D>(h, c, dsc, cspmcnt))) return rc;
     GC_CUDA(cudaMemcpyAsync(h->pin, dsc, sizeof(Scal), cudaMemcpyDeviceToHost, st));
     GC_CUDA(cudaStreamSynchronize(st));
     timer_collect();
@@ -1436,23 +1575,10 @@ static int step_impl(sph_handle* h, int32_t n, int timestepping, double tmin, do
     unsigned long long bits = h->pin->maxcdx;
     double mc;
     memcpy(&mc, &bits, 8);
-    if (mc > 0.9 * p.nui) skip = false;
+    if (mc > c.reb_thr) skip = false;
     if (mc > maxout) maxout = mc;
   }
-  if (h->in_cell_order && (rc = scatter_state<D>(h))) return rc;
-  // post-batch ∑W, ∑∇W on the last pair set and the final points
-  if (core.built) {
-    const double* x2 = D == 3 ? h->cl->xuser[2] : h->cl->xuser[0];
-    double* sg2 = D == 3 ? h->sumgW_o[2].as<double>() : h->sumgW_o[0].as<double>();
-    timer_begin(T_POST, st);
-    const int L = choose_lanes(h);
-    PAIR_LAUNCH(k_sums_post, L, c, h->N, core.rs_full.as<int64_t>(), core.nbr.as<int32_t>(),
-                                        core.orig.as<int32_t>(), h->pt_u, h->cl->xuser[0], h->cl->xuser[1], x2,
-                                        h->sumW_o.as<double>(), h->sumgW_o[0].as<double>(),
-                                        h->sumgW_o[1].as<double>(), sg2);
-    GC_LAUNCHED();
-    timer_end(T_POST, st);
-  }
+  if ((rc = finish_call<D>(h, c, dsc))) return rc;
   GC_CUDA(cudaMemcpyAsync(h->pin, dsc, sizeof(Scal), cudaMemcpyDeviceToHost, st));
   GC_CUDA(cudaStreamSynchronize(st));
   timer_collect();
@@ -1461,6 +1587,223 @@ static int step_impl(sph_handle* h, int32_t n, int timestepping, double tmin, do
   if (updaten_out) *updaten_out = updaten;
   if (maxcdx_out) *maxcdx_out = maxout;
   return GCSPH_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Captured calls.  When update! is due after every step (nui <= 0, as with
+// dist = H), a whole stepsolve! call -- gather, n x (update!, stages, Δt),
+// scatter, post sums -- is one CUDA graph, replayed with one host round trip.
+// The decisions the eager loop takes on the host move to the device:
+// k_step_end counts update! calls and keeps the largest max|cΔx| the way the
+// host loop does.  update! also runs after a step whose max|cΔx| is exactly
+// 0 (nothing moved), where the host loop skips it: the re-sort of unmoved
+// points by (cell, original index) is the identity and the pair set is the
+// same, so the state is too.  A neighbour overflow inside the replay skips
+// every later kernel, the final scatter included, so the caller's
+// original-order arrays still hold the call's inputs: the host grows the
+// buffers and runs the call again eagerly.
+// ---------------------------------------------------------------------------
+static HostSide host_side(const sph_handle* h) {
+  HostSide s{};
+  const CellCore& core = h->cl->core;
+  s.idx[0] = h->ix;
+  s.idx[1] = h->ixh;
+  s.idx[2] = h->iv;
+  s.idx[3] = h->ivh;
+  s.idx[4] = h->irho;
+  s.idx[5] = h->irhoh;
+  s.pt[0] = h->PT.p;
+  s.pt[1] = h->PT_b.p;
+  for (int d = 0; d < 3; ++d) {
+    s.buf2[d][0] = h->BUF2[d].p;
+    s.buf2[d][1] = h->BUF2_b[d].p;
+  }
+  s.orig[0] = core.orig.p;
+  s.orig[1] = core.orig_b.p;
+  s.sorted = core.sorted;
+  s.built = core.built;
+  s.up_valid = core.up_valid;
+  s.in_cell_order = h->in_cell_order;
+  s.nfull = core.nfull;
+  return s;
+}
+
+// the pairs swapped by the re-sorts are equal-sized, so pointers alone move
+static void set_host_side(sph_handle* h, const HostSide& s) {
+  CellCore& core = h->cl->core;
+  h->ix = s.idx[0];
+  h->ixh = s.idx[1];
+  h->iv = s.idx[2];
+  h->ivh = s.idx[3];
+  h->irho = s.idx[4];
+  h->irhoh = s.idx[5];
+  h->PT.p = s.pt[0];
+  h->PT_b.p = s.pt[1];
+  for (int d = 0; d < 3; ++d) {
+    h->BUF2[d].p = s.buf2[d][0];
+    h->BUF2_b[d].p = s.buf2[d][1];
+  }
+  core.orig.p = s.orig[0];
+  core.orig_b.p = s.orig[1];
+  core.sorted = s.sorted;
+  core.built = s.built;
+  core.up_valid = s.up_valid;
+  h->in_cell_order = s.in_cell_order;
+  core.nfull = s.nfull;
+}
+
+static GraphKey graph_key(const sph_handle* h, int32_t n, int timestepping, double tmin, double tmax) {
+  GraphKey k;
+  memset(&k, 0, sizeof(k));  // padding compares too
+  k.n = n;
+  k.timestepping = timestepping;
+  k.lanes = choose_lanes(h);
+  k.timing = timing_on() ? 1 : 0;
+  k.tmin = timestepping ? tmin : 0.0;
+  k.tmax = timestepping ? tmax : 0.0;
+  k.prm = h->prm;
+  k.prm.dt = 0.0;
+  k.prm.etime = 0.0;
+  k.nbr_cap = h->cl->core.nbr_cap;
+  k.we_cap = h->we_cap;
+  k.gen = h->cl->core.gen;
+  k.at = host_side(h);
+  // flags and counts the capture does not depend on (it always starts by
+  // binning the caller's points) stay out of the key
+  k.at.sorted = k.at.built = k.at.up_valid = k.at.in_cell_order = false;
+  k.at.nfull = 0;
+  for (int d = 0; d < 3; ++d) {
+    k.user[d] = h->cl->xuser[d];
+    k.user[3 + d] = h->v_u[d];
+  }
+  k.user[6] = h->rho_u;
+  k.user[7] = h->pt_u;
+  return k;
+}
+
+template <int D>
+static int graph_capture(sph_handle* h, StepConst c, int32_t n, StepGraph& g) {
+  CellCore& core = h->cl->core;
+  // the caller's stream may be the legacy default stream, which cannot be
+  // captured: record into a private stream (nothing runs there)
+  if (!h->cap_stream) GC_CUDA(cudaStreamCreateWithFlags(&h->cap_stream, cudaStreamNonBlocking));
+  const cudaStream_t run_st = core.st;
+  cudaStream_t st = h->cap_stream;
+  Scal* dsc = h->scal.as<Scal>();
+  const HostSide before = host_side(h);
+  const unsigned long long l0 = gcsph_launch_count();
+  GC_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+  core.st = st;
+  timer_capture_to(&g.timers);
+  int rc = GCSPH_OK;
+  int32_t cspmcnt = 0;
+  for (int32_t it = 0; it < n && rc == GCSPH_OK; ++it) {
+    // per-step maxima; the overflow flag stays set once raised
+    cudaError_t e = cudaMemsetAsync(&dsc->maxcdx, 0, 3 * sizeof(unsigned long long), st);
+    if (e != cudaSuccess) {
+      rc = cuda_fail(e, "cudaMemsetAsync", __FILE__, __LINE__);
+      break;
+    }
+    c.count_reb = it + 1 < n;
+    if ((rc = rebuild<D>(h, c, &dsc->ovf))) break;
+    rc = enqueue_stages<D>(h, c, dsc, cspmcnt);
+  }
+  if (rc == GCSPH_OK) rc = finish_call<D>(h, c, dsc);
+  timer_capture_to(nullptr);
+  core.st = run_st;
+  cudaGraph_t graph = nullptr;
+  cudaError_t e = cudaStreamEndCapture(st, &graph);
+  const unsigned long long l1 = gcsph_launch_count();
+  count_launch(-(int)(l1 - l0));  // captured, not run: each replay counts them
+  if (rc == GCSPH_OK && e != cudaSuccess) rc = cuda_fail(e, "cudaStreamEndCapture", __FILE__, __LINE__);
+  if (rc == GCSPH_OK) {
+    e = cudaGraphInstantiate(&g.exec, graph, 0);
+    if (e != cudaSuccess) rc = cuda_fail(e, "cudaGraphInstantiate", __FILE__, __LINE__);
+  }
+  if (graph) cudaGraphDestroy(graph);
+  g.after = host_side(h);
+  set_host_side(h, before);
+  if (rc != GCSPH_OK) {
+    cudaGetLastError();
+    graph_free(g);
+    return rc;
+  }
+  g.launches = (long long)(l1 - l0);
+  return GCSPH_OK;
+}
+
+// GCSPH_OK with *done = false: not eligible, run the eager loop
+template <int D>
+static int step_graph(sph_handle* h, const StepConst& c, int32_t n, int timestepping, double tmin, double tmax,
+                      int64_t* updaten_out, double* maxcdx_out, bool* done) {
+  *done = false;
+  CellCore& core = h->cl->core;
+  if (!h->use_graphs || n < 1 || !(c.reb_thr <= 0.0) || h->in_cell_order || core.nbr_cap <= 0 ||
+      h->we_cap < core.nbr_cap || core.nfull_est <= 0)
+    return GCSPH_OK;
+  cudaStream_t st = core.st;
+  Scal* dsc = h->scal.as<Scal>();
+  const GraphKey key = graph_key(h, n, timestepping, tmin, tmax);
+  StepGraph* g = nullptr;
+  for (StepGraph& e : h->graphs)
+    if (e.exec && memcmp(&e.key, &key, sizeof(key)) == 0) g = &e;
+  if (!g) {
+    // least recently used slot
+    g = &h->graphs[0];
+    for (StepGraph& e : h->graphs)
+      if (!e.exec || e.used < g->used) g = &e;
+    graph_free(*g);
+    g->key = key;
+    if (graph_capture<D>(h, c, n, *g) != GCSPH_OK) {
+      // capture is an optimisation: the eager loop runs the call
+      cudaGetLastError();
+      set_error("");
+      return GCSPH_OK;
+    }
+    h->n_captures += 1;
+  }
+  g->used = ++h->graph_clock;
+  init_scal(h, n);
+  GC_CUDA(cudaMemcpyAsync(dsc, h->pin, sizeof(Scal), cudaMemcpyHostToDevice, st));
+  GC_CUDA(cudaGraphLaunch(g->exec, st));
+  GC_CUDA(cudaMemcpyAsync(h->pin, dsc, sizeof(Scal), cudaMemcpyDeviceToHost, st));
+  GC_CUDA(cudaStreamSynchronize(st));
+  count_launch((int)g->launches);
+  timer_account(g->timers);
+  if (h->pin->ovf) {
+    // the caller's arrays are untouched; grow past the count that overflowed
+    int rc;
+    if ((rc = core.read_nfull())) return rc;
+    if ((rc = core.grow_nbr(core.nfull))) return rc;
+    if ((rc = grow_entry_arrays<D>(h))) return rc;
+    core.sorted = core.built = core.up_valid = false;
+    return GCSPH_OK;  // not done: the eager loop runs the call
+  }
+  set_host_side(h, g->after);
+  h->n_replays += 1;
+  h->prm.dt = h->pin->dt;
+  h->prm.etime = h->pin->etime;
+  double mo;
+  unsigned long long bits = h->pin->maxout;
+  memcpy(&mo, &bits, 8);
+  if (updaten_out) *updaten_out = h->pin->nreb;
+  if (maxcdx_out) *maxcdx_out = mo;
+  *done = true;
+  return GCSPH_OK;
+}
+
+template <int D>
+static int step_impl(sph_handle* h, int32_t n, int timestepping, double tmin, double tmax, int64_t* updaten_out,
+                     double* maxcdx_out) {
+  StepConst c = make_const(h);
+  c.timestepping = timestepping;
+  c.tmin = tmin;
+  c.tmax = tmax;
+  c.reb_thr = 0.9 * h->prm.nui;
+  bool done = false;
+  int rc = step_graph<D>(h, c, n, timestepping, tmin, tmax, updaten_out, maxcdx_out, &done);
+  if (rc || done) return rc;
+  return step_eager<D>(h, c, n, updaten_out, maxcdx_out);
 }
 
 extern "C" {
@@ -1552,11 +1895,13 @@ int sph_create(gcl_handle* cl, const gcsph_params* prm, double* rho_dev, double*
 void sph_destroy(sph_handle* h) {
   if (!h) return;
   if (h->cl) cudaStreamSynchronize(h->cl->core.st);
+  for (StepGraph& g : h->graphs) graph_free(g);
+  if (h->cap_stream) cudaStreamDestroy(h->cap_stream);
   DevBuf* one[] = {&h->rhoh_o, &h->P_o, &h->drho_o, &h->sumW_o, &h->P1, &h->P2, &h->PT, &h->DRHO, &h->PLAST,
                    &h->We, &h->IR, &h->IRH, &h->scal, &h->RHO[0], &h->RHO[1], &h->RHOH[0], &h->RHOH[1], &h->PT_b};
   for (DevBuf* b : one) b->release();
   h->CD.release();
-  h->MIR.release();
+  h->PQ.release();
   for (int d = 0; d < 3; ++d) {
     h->CA[d].release();
     h->BUF2_b[d].release();
@@ -1586,6 +1931,19 @@ int sph_set_params(sph_handle* h, const gcsph_params* prm) {
   if (!h || !prm) return fail(GCSPH_EINVAL, "null argument");
   if (prm->gamma <= 0) return fail(GCSPH_EINVAL, "gamma must be a positive integer");
   h->prm = *prm;
+  return GCSPH_OK;
+}
+
+int sph_set_graphs(sph_handle* h, int32_t on) {
+  if (!h) return fail(GCSPH_EINVAL, "null handle");
+  h->use_graphs = on != 0;
+  return GCSPH_OK;
+}
+
+int sph_graph_stats(const sph_handle* h, int64_t* captures, int64_t* replays) {
+  if (!h) return fail(GCSPH_EINVAL, "null handle");
+  if (captures) *captures = h->n_captures;
+  if (replays) *replays = h->n_replays;
   return GCSPH_OK;
 }
 

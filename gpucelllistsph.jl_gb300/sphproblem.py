@@ -116,6 +116,17 @@ class SPHProblem:
         order, bit-identical to the CPU oracle)."""
         _lib.check(_lib.load().sph_set_lanes(self._h, int(lanes)))
 
+    def set_graphs(self, on: bool):
+        """Run stepsolve! calls as captured CUDA graphs where update! follows
+        every step (default on); off runs one host round trip per step."""
+        _lib.check(_lib.load().sph_set_graphs(self._h, int(bool(on))))
+
+    def graph_stats(self):
+        """(graphs captured, calls replayed as a graph) so far."""
+        a, b = C.c_int64(), C.c_int64()
+        _lib.check(_lib.load().sph_graph_stats(self._h, C.byref(a), C.byref(b)))
+        return int(a.value), int(b.value)
+
     # --------------------------------------------------------------- fields
     def field(self, name: str):
         """Copy of one library field in original particle order."""

@@ -158,6 +158,16 @@ int sph_get_params(const sph_handle* h, gcsph_params* prm);
  * 0 (default) picks about four neighbours per lane. */
 int sph_set_lanes(sph_handle* h, int32_t lanes);
 
+/* Captured calls (no reference counterpart; on by default).  When update! is
+ * due after every step (nui <= 0, e.g. dist = H), sph_step runs the whole
+ * call -- gather, n steps, scatter, post sums -- as one CUDA graph with one
+ * host round trip, instead of one round trip per step.  Results are
+ * identical to the per-step loop; a neighbour overflow inside the graph
+ * falls back to that loop for the call.  0 turns capture off. */
+int sph_set_graphs(sph_handle* h, int32_t on);
+/* How many graphs were captured and how many calls ran as a graph replay. */
+int sph_graph_stats(const sph_handle* h, int64_t* captures, int64_t* replays);
+
 /* stepsolve!(prob, n; timestepping, timelims) -- src/sphproblem.jl:204-345.
  * Returns (updaten, maxcΔxout) through the out pointers. */
 int sph_step(sph_handle* h, int32_t n, int timestepping, double tmin, double tmax, int64_t* updaten,

@@ -513,6 +513,23 @@ ORC_API void orc_sphsumgradW(int D, int64_t N, int64_t P, const int32_t *pairs, 
     run_pairs(P, N, D, out, body_sumgW, &c);
 }
 
+/* seed != 0: move every powfancy7th result used by ∂ρ∂tDDT! by -1, 0 or +1
+   ulp (a pure hash of seed, pair and side picks which) -- measures how much
+   the results move when that function's last-bit rounding differs, as it
+   does between any two correct evaluations of the same iteration */
+static uint64_t g_pf7_jitter = 0;
+ORC_API void orc_set_pf7_jitter(uint64_t seed) { g_pf7_jitter = seed; }
+static double pf7_jittered(double t, int64_t i, int64_t j, int side) {
+    if (!g_pf7_jitter) return t;
+    uint64_t z = g_pf7_jitter ^ ((uint64_t)i * 0x9E3779B97F4A7C15ULL) ^ ((uint64_t)j * 0xC2B2AE3D27D4EB4FULL) ^
+                 (uint64_t)side;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL; /* splitmix64 finaliser */
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+    z ^= z >> 31;
+    int k = (int)(z % 3ULL);
+    return k == 0 ? t : nextafter(t, k == 1 ? INFINITY : -INFINITY);
+}
+
 /* ∂ρ∂tDDT!, :542-631 */
 typedef struct {
     int D; int64_t N, P; const int32_t *pairs; const double *gW; const double *rho; const double *v;
@@ -537,14 +554,14 @@ static void body_ddt(int64_t p, double *const *acc, const void *vc) {
     double m0dot = c->m0 * dotv(D, dv, gw);
     double si = m0dot, sj = m0dot;
     if (c->ptype[i] > 1) {
-        double drhopvp = c->rho0 * orc_powfancy7th(1.0 + c->DDTgz * dx[1], c->ginv, c->gamma) - c->rho0;
+        double drhopvp = c->rho0 * pf7_jittered(orc_powfancy7th(1.0 + c->DDTgz * dx[1], c->ginv, c->gamma), i, j, 0) - c->rho0;
         double visc_densi = c->DDTkh * ((rhoj - rhoi) - drhopvp) / (r2 + c->eta2);
         double delta_i = visc_densi * dot3 * c->m0 / rhoj;
         si += delta_i;
     }
     acc[0][i] += si;
     if (c->ptype[j] > 1) {
-        double drhopvn = c->rho0 * orc_powfancy7th(1.0 - c->DDTgz * dx[1], c->ginv, c->gamma) - c->rho0;
+        double drhopvn = c->rho0 * pf7_jittered(orc_powfancy7th(1.0 - c->DDTgz * dx[1], c->ginv, c->gamma), i, j, 1) - c->rho0;
         double visc_densi = c->DDTkh * ((rhoi - rhoj) - drhopvn) / (r2 + c->eta2);
         double delta_j = visc_densi * dot3 * c->m0 / rhoi;
         sj += delta_j;
@@ -1260,4 +1277,10 @@ ORC_API void orc_sys_update(void *hs) { sys_update_impl((OrcSys *)hs); }
 ORC_API void orc_sys_set_x(void *hs, const double *x) {
     OrcSys *S = (OrcSys *)hs;
     memcpy(S->x, x, sizeof(double) * (size_t)S->D * (size_t)S->N);
+}
+
+/* the half-step positions an SPHProblem copies from x when it is built */
+ORC_API void orc_sys_set_xh(void *hs, const double *x) {
+    OrcSys *S = (OrcSys *)hs;
+    memcpy(S->xh, x, sizeof(double) * (size_t)S->D * (size_t)S->N);
 }

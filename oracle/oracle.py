@@ -88,6 +88,7 @@ def lib():
         L.orc_sys_partialupdate.argtypes = [C.c_void_p, C.c_int]
         L.orc_sys_update.argtypes = [C.c_void_p]
         L.orc_sys_set_x.argtypes = [C.c_void_p, f64p]
+        L.orc_sys_set_xh.argtypes = [C.c_void_p, f64p]
         I, N64, P64, D64 = C.c_int, C.c_int64, C.c_int64, C.c_double
         vpp = C.c_void_p
         sigs = {
@@ -279,3 +280,6 @@ class OracleSystem:
 
     def set_x(self, x):
         lib().orc_sys_set_x(self._h, np.ascontiguousarray(x, dtype=np.float64))
+
+    def set_xh(self, x):
+        lib().orc_sys_set_xh(self._h, np.ascontiguousarray(x, dtype=np.float64))

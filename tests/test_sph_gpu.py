@@ -68,11 +68,16 @@ def gpu_field(prob, name):
 
 def noise_floor(orc, case, calls, v=None, seeds=(1, 2, 3, 4)):
     """How far the reference's own algorithm moves under another summation
-    order: the oracle re-run with its pair list shuffled (an order the
-    reference's atomics may produce on any run), per field, normwise."""
+    order and another last-bit rounding of powfancy7th: the oracle re-run with
+    its pair list shuffled (an order the reference's atomics may produce on
+    any run) and each powfancy7th result moved by -1/0/+1 ulp (the split-row
+    path evaluates that iteration by its exact series, correctly rounded,
+    which can sit one ulp from the iteration's own rounding), per field,
+    normwise."""
     import ctypes as C
     L = orc.lib()
     L.orc_set_pair_shuffle.argtypes = [C.c_uint64]
+    L.orc_set_pf7_jitter.argtypes = [C.c_uint64]
     p = orc.default_params(case.dx, case.h, case.H, case.rho0, case.m0, case.dt, case.alpha, case.c0, case.gamma,
                            case.delta, case.CFL, case.dist, g=case.g, s=case.s)
     for k, val in case.extra.items():
@@ -80,12 +85,14 @@ def noise_floor(orc, case, calls, v=None, seeds=(1, 2, 3, 4)):
 
     def run(seed):
         L.orc_set_pair_shuffle(seed)
+        L.orc_set_pf7_jitter(seed)
         try:
             s = orc.OracleSystem(case.x, case.cellsize, case.dist, case.rho, case.ptype, p, v=v)
             for n, kw in calls:
                 s.stepsolve(n, **kw)
         finally:
             L.orc_set_pair_shuffle(0)
+            L.orc_set_pf7_jitter(0)
         return s
 
     base = run(0)
@@ -104,11 +111,21 @@ def compare(prob, ref, case, fields=FIELDS, rtol=RTOL, exact=True, floor=None):
     arithmetic, so no summation-order difference is left.  With a noise floor
     (lanes > 1 re-associate the sums) a field may also sit within 16x of the
     largest of four re-orderings of the reference's own sums -- the P of a
-    barely compressed column, (ρ/ρ₀)^7 - 1, is that ill-conditioned."""
+    barely compressed column, (ρ/ρ₀)^7 - 1, is that ill-conditioned, so P may
+    also differ by what the EOS makes of the ρ difference actually reached."""
     errs = {}
     for name in fields:
         errs[name] = relerr(gpu_field(prob, name), ref.get(name))
     tol = {k: max(rtol, 16.0 * (floor or {}).get(k, 0.0)) for k in fields}
+    if not exact and "P" in fields:
+        # P = P0((ρ/ρ0)^γ - 1) is a function of ρ: the ρ actually reached moves
+        # it by up to γ P0 (ρ/ρ0)^(γ-1) Δρ/ρ0, plus the rounding of the EOS itself
+        rho_ref, P_ref = ref.get("rho"), ref.get("P")
+        P0 = case.c0 ** 2 * case.rho0 / case.gamma
+        drho = np.linalg.norm(gpu_field(prob, "rho") - rho_ref)
+        lip = case.gamma * P0 * float(np.max(rho_ref / case.rho0)) ** (case.gamma - 1) / case.rho0
+        bound = lip * drho + 8 * np.finfo(np.float64).eps * P0 * np.sqrt(rho_ref.size)
+        tol["P"] = max(tol["P"], bound / max(np.linalg.norm(P_ref), 1e-300))
     bad = {k: (v, tol[k]) for k, v in errs.items() if not v <= tol[k]}
     assert not bad, f"fields over tolerance (err, tol): {bad}"
     if exact:
@@ -212,13 +229,15 @@ def test_skin_and_timestepping(gpu_pkg, orc, lanes):
     check(orc, prob, ref, case, lanes, [(25, dict(timestepping=True, timelims=lims))] * 3)
 
 
-def test_neighbour_buffers_regrow_mid_step(gpu_pkg, orc):
+@pytest.mark.parametrize("lanes", [1, 4])
+def test_neighbour_buffers_regrow_mid_step(gpu_pkg, orc, lanes):
     """The cell list is built on a spread-out copy of the particles (few pairs,
     small neighbour buffers); the particles are then put back and stepped.  The
     first rebuild inside stepsolve! outgrows the buffers without waiting for
     the host, every kernel of that step skips, the library grows the buffers
-    and repeats the step: the result must match the oracle started from the
-    compact positions."""
+    and repeats the step.  The oracle is built the same way (its grid frozen on
+    the spread copy, positions then replaced), so the serial path must be
+    bit-identical and the split rows within the noise floor."""
     case = gpu_pkg.workloads.dam_break_2d(dx=0.04, fluid=(0.6, 0.8), tank=(1.2, 1.0), layer_ptype=(1, 0, 0))
     centre = case.x.mean(axis=1, keepdims=True)
     spread = centre + 3.0 * (case.x - centre)
@@ -230,10 +249,13 @@ def test_neighbour_buffers_regrow_mid_step(gpu_pkg, orc):
                               case.rho0, case.m0, case.dt, case.alpha, case.c0, case.gamma, case.delta, case.CFL)
     p = orc.default_params(case.dx, case.h, case.H, case.rho0, case.m0, case.dt, case.alpha, case.c0, case.gamma,
                            case.delta, case.CFL, case.dist)
-    ref = orc.OracleSystem(case.x, case.cellsize, case.dist, case.rho, case.ptype, p)
+    prob.set_lanes(lanes)
+    ref = orc.OracleSystem(spread, case.cellsize, case.dist, case.rho, case.ptype, p)
+    ref.set_x(case.x)
+    ref.set_xh(case.x)  # the GPU problem was built after the points were put back
     run_both(prob, ref, 10)
     assert system.pairsn > 2 * few
-    check(orc, prob, ref, case, 0, [(10, {})])
+    check(orc, prob, ref, case, lanes, [(10, {})])
 
 
 @pytest.mark.parametrize("lanes", [2, 4, 8, 16, 32])
