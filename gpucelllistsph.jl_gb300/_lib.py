@@ -35,6 +35,15 @@ class gcsph_params(C.Structure):
         ("gamma", C.c_int32), ("cspmn", C.c_int32)]
 
 
+class gcsph_ens_params(C.Structure):
+    """Mirror of gcsph_ens_params (one ensemble instance)."""
+    _fields_ = [(n, C.c_double) for n in (
+        "dx", "h", "H", "rho0", "m0", "dt", "alpha", "nu", "g", "c0", "s", "delta", "bound_D", "bound_l")] + [
+        ("grid_min", C.c_double * 3), ("grid_max", C.c_double * 3), ("gamma", C.c_int32), ("cspmn", C.c_int32)]
+
+
+ENS_FIELDS = {"x": 0, "v": 1, "rho": 2, "P": 3, "ptype": 4, "drho": 5}
+
 vp = C.c_void_p
 i32, i64, f64 = C.c_int32, C.c_int64, C.c_double
 PP = C.POINTER(C.c_void_p)  # host array of device pointers
@@ -66,6 +75,17 @@ _SIGS = {
     "sph_set_graphs": (C.c_int, [vp, i32]),
     "sph_graph_stats": (C.c_int, [vp, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
     "sph_step": (C.c_int, [vp, i32, C.c_int, f64, f64, C.POINTER(i64), C.POINTER(f64)]),
+    "ens_create": (C.c_int, [i32, vp, C.POINTER(vp)]),
+    "ens_destroy": (None, [vp]),
+    "ens_bytes_per_particle": (C.c_int, [i32, C.POINTER(i64)]),
+    "ens_add": (C.c_int, [vp, i64, vp, vp, vp, vp, C.POINTER(gcsph_ens_params), C.POINTER(i32)]),
+    "ens_remove": (C.c_int, [vp, i32]),
+    "ens_step": (C.c_int, [vp, i32]),
+    "ens_get": (C.c_int, [vp, i32, i32, vp]),
+    "ens_info": (C.c_int, [vp, i32, C.POINTER(i64), C.POINTER(i64), C.POINTER(f64)]),
+    "ens_totals": (C.c_int, [vp, C.POINTER(i32), C.POINTER(i64), C.POINTER(i64)]),
+    "ens_set_tuning": (C.c_int, [vp, i32, i32]),
+    "ens_get_tuning": (C.c_int, [vp, C.POINTER(i32), C.POINTER(i64), C.POINTER(i64)]),
     "sph_get_field": (C.c_int, [vp, i32, vp]),
     "gcsph_dpckernlim": (f64, [i32]),
     "gcsph_sphW": (C.c_int, [i32, i64, i64, vp, PP, f64, vp, vp]),

@@ -24,6 +24,7 @@ UNITS = {
     "celllist.cu": ["-fmad=false"],
     "sph_step.cu": ["-fmad=false"],
     "sph_pairs.cu": ["-fmad=false"],
+    "ensemble.cu": [],
 }
 
 

@@ -1,0 +1,1154 @@
+// ensemble.cu -- batched FP32 SPH: many independent dam-break instances
+// advanced together, one launch per pass over all of them.
+//
+// The reference steps one SPHProblem at a time (src/sphproblem.jl:204-345).
+// Here every admitted instance lives in one segmented particle space:
+// instance s owns particles [p_off_s, p_off_s + n_s) and cell keys
+// [key_off_s, key_off_s + ncell_s), so one counting sort over the global keys
+// keeps each instance's particles in its own range, in cell order, ties by
+// the instance-local particle id (deterministic, and independent of which
+// other instances are present).  The pair passes walk the 3^D neighbour cells
+// of each particle directly (no neighbour list): the cell edge equals the
+// kernel support H, so every pair within H is found, and every SPH term of the
+// path vanishes beyond H.
+//
+// Precision: pair arithmetic and per-particle sums in FP32 (Kahan-compensated);
+// density held as δρ = ρ - ρ₀ so the EOS (1+δρ/ρ₀)^γ - 1 and the
+// density-diffusion difference (δρ_j - δρ_i) - ρ₀((1+ε)^(1/γ) - 1) carry no
+// cancellation against ρ₀; positions in FP64 (the symplectic position update
+// runs in FP64) and, for the pair passes, as FP32 offsets from the corner of
+// the particle's cell, so a pair's separation is exact to ~1e-7 of H.
+//
+// Physics per pair and per particle follows the FP64 path kernel by kernel
+// (∂ρ∂tDDT!, ∂v∂t!, ∂v∂t_av!, ∂v∂t_visc!, gravity!, fbmolforce!, ∂v∂tpF!,
+// the half-step predictors and symplectic_update!), fixed Δt per instance.
+#include <math.h>
+#include <algorithm>
+#include <map>
+#include <vector>
+#include "gcsph_common.cuh"
+
+namespace gcsph {
+namespace {
+
+constexpr int ENS_MAX_TPB = 512;
+
+// per-instance constants (device table, indexed by packing position)
+struct EnsInst {
+  double origin[3];
+  double csinv;  // 1 / cell edge
+  double cs;
+  double dt;
+  int nc[3];
+  int key_off;
+  int gamma;
+  int use_visc, use_pF;
+  int cspmn;
+  float csf, H2, h, Hinv, nW, nDW, m0, rho0, c0, P0, alpha, DDTkh, DDTgz, eta2, g, nu, s, twoh, pfc, hp1;
+  float fb_d[2], fb_r0[2], fb_eta2[2];  // fbmolforce constants of stage 1 and stage 2
+  float pc[4];                           // (1+ε)^(1/γ) - 1 series coefficients
+};
+
+struct EnsArr {
+  int64_t N;
+  const int32_t* inst;
+  const int32_t* skey;       // global cell key of each (sorted) particle
+  const int32_t* cellstart;  // first particle of each global cell, K+1 entries
+  double* x[3];              // positions (FP64)
+  float* v[3];
+  float* dr;                 // ρ - ρ₀
+  float* drb;                // ρΔt½ - ρ₀ at the step's start: the predictor's base (cspmcorr! leaves it)
+  const int32_t* pt;
+  float* off[3];             // x - cell corner (FP32)
+  float* offh[3];            // half-step positions - cell corner
+  float* vh[3];
+  float* drh;
+};
+
+struct KSum {
+  float s = 0.f, c = 0.f;
+  __device__ __forceinline__ void add(float x) {
+    const float y = x - c;
+    const float t = s + y;
+    c = (t - s) - y;
+    s = t;
+  }
+};
+
+template <int D>
+__device__ __forceinline__ float dot32(const float* a, const float* b) {
+  float r = a[0] * b[0];
+#pragma unroll
+  for (int d = 1; d < D; ++d) r = fmaf(a[d], b[d], r);
+  return r;
+}
+
+// P0 ((1+e)^γ - 1), e = δρ/ρ₀, without cancellation (pressure(), src/gpukernels_sph.jl:691-697)
+__device__ __forceinline__ float eos32(float dr, int pt, const EnsInst& I) {
+  if (pt <= 1 && dr < 0.f) return 0.f;
+  const float e = dr / I.rho0;
+  float p;
+  if (I.gamma == 7)
+    p = e * (7.f + e * (21.f + e * (35.f + e * (35.f + e * (21.f + e * (7.f + e))))));
+  else
+    p = expm1f((float)I.gamma * log1pf(e));
+  return I.P0 * p;
+}
+
+// (1+ε)^(1/γ) - 1 (powfancy7th(1+ε) - 1, src/gpukernels_sph.jl:499-515)
+__device__ __forceinline__ float root_m1(float eps, const EnsInst& I) {
+  if (fabsf(eps) < 0.01f) return eps * (I.pc[0] + eps * (I.pc[1] + eps * (I.pc[2] + eps * I.pc[3])));
+  return powf(1.f + eps, 1.f / (float)I.gamma) - 1.f;
+}
+
+__device__ __forceinline__ void cell_of(int key, const EnsInst& I, int& c0, int& c1, int& c2) {
+  int local = key - I.key_off;
+  c0 = local % I.nc[0];
+  local /= I.nc[0];
+  c1 = local % I.nc[1];
+  c2 = local / I.nc[1];
+}
+
+// ---------------------------------------------------------------------------
+// binning (segmented counting sort)
+// ---------------------------------------------------------------------------
+template <int D>
+__global__ void k_ens_key(int64_t N, const int32_t* __restrict__ inst, const double* __restrict__ x0,
+                          const double* __restrict__ x1, const double* __restrict__ x2,
+                          const EnsInst* __restrict__ T, int32_t* __restrict__ key, int32_t* __restrict__ slot,
+                          int32_t* __restrict__ count) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  const EnsInst& I = T[inst[i]];
+  const double xs[3] = {x0[i], x1[i], D == 3 ? x2[i] : 0.0};
+  int c[3] = {0, 0, 0};
+#pragma unroll
+  for (int d = 0; d < D; ++d) {
+    double f = floor((xs[d] - I.origin[d]) * I.csinv);
+    f = f >= 0.0 ? f : 0.0;  // also NaN -> 0: points outside the frozen grid clamp to its edge cells
+    c[d] = f < (double)(I.nc[d] - 1) ? (int)f : I.nc[d] - 1;
+  }
+  const int k = I.key_off + c[0] + I.nc[0] * (c[1] + I.nc[1] * c[2]);
+  key[i] = k;
+  slot[i] = atomicAdd(&count[k], 1);
+}
+
+__global__ void k_ens_scatter(int64_t N, const int32_t* __restrict__ key, const int32_t* __restrict__ slot,
+                              const int32_t* __restrict__ cellstart, int32_t* __restrict__ tmp) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  tmp[cellstart[key[i]] + slot[i]] = (int32_t)i;
+}
+
+// rank inside the cell by instance-local id (ids are unique inside an instance)
+__global__ void k_ens_rank(int64_t N, const int32_t* __restrict__ tmp, const int32_t* __restrict__ key,
+                           const int32_t* __restrict__ cellstart, const int32_t* __restrict__ id,
+                           int32_t* __restrict__ perm) {
+  const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= N) return;
+  const int32_t i = tmp[q];
+  const int32_t c = key[i];
+  const int32_t s = cellstart[c], e = cellstart[c + 1];
+  const int32_t oi = id[i];
+  int32_t r = 0;
+  for (int32_t t = s; t < e; ++t) r += id[tmp[t]] < oi;
+  perm[s + r] = i;
+}
+
+struct EnsState {
+  double* x[3];
+  float* v[3];
+  float* dr;
+  float* drb;
+  int32_t* pt;
+  int32_t* id;
+};
+
+// new[k] = old[perm[k]]; FP32 offsets from the new cell's corner
+template <int D>
+__global__ void k_ens_permute(int64_t N, const int32_t* __restrict__ perm, const int32_t* __restrict__ key,
+                              const int32_t* __restrict__ inst, const EnsInst* __restrict__ T, EnsState in,
+                              EnsState out, int32_t* __restrict__ skey, float* __restrict__ o0,
+                              float* __restrict__ o1, float* __restrict__ o2) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= N) return;
+  const int32_t i = perm[k];
+  const int32_t kk = key[i];
+  skey[k] = kk;
+  const EnsInst& I = T[inst[k]];
+  int c0, c1, c2;
+  cell_of(kk, I, c0, c1, c2);
+#pragma unroll
+  for (int d = 0; d < D; ++d) {
+    const double xv = in.x[d][i];
+    out.x[d][k] = xv;
+    out.v[d][k] = in.v[d][i];
+    const int cd = d == 0 ? c0 : (d == 1 ? c1 : c2);
+    float* o = d == 0 ? o0 : (d == 1 ? o1 : o2);
+    o[k] = (float)(xv - (I.origin[d] + (double)cd * I.cs));
+  }
+  out.dr[k] = in.dr[i];
+  out.drb[k] = in.drb[i];
+  out.pt[k] = in.pt[i];
+  out.id[k] = in.id[i];
+}
+
+// ---------------------------------------------------------------------------
+// the two pair passes (cell walk), persistent grid-stride loops
+// ---------------------------------------------------------------------------
+template <int D, int STAGE>
+__global__ void __launch_bounds__(ENS_MAX_TPB) k_ens_stage(EnsArr A, const EnsInst* __restrict__ T) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < A.N; i += stride) {
+    const EnsInst& I = T[A.inst[i]];
+    int cx0, cy0, cz0;
+    cell_of(A.skey[i], I, cx0, cy0, cz0);
+    float oi[D], ohi[D], vi[D];
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      oi[d] = A.off[d][i];
+      ohi[d] = STAGE == 1 ? oi[d] : A.offh[d][i];
+      vi[d] = STAGE == 1 ? A.v[d][i] : A.vh[d][i];
+    }
+    const int pti = A.pt[i];
+    const float dri = STAGE == 1 ? A.dr[i] : A.drh[i];
+    const float rhoi = I.rho0 + dri;
+    const float Pi = eos32(dri, pti, I);
+    const int fbs = STAGE - 1;
+    KSum drho, acc[D];
+    const int zlo = D == 3 ? -1 : 0, zhi = D == 3 ? 1 : 0;
+    for (int dz = zlo; dz <= zhi; ++dz) {
+      const int cz = cz0 + dz;
+      if (cz < 0 || cz >= I.nc[2]) continue;
+      for (int dy = -1; dy <= 1; ++dy) {
+        const int cy = cy0 + dy;
+        if (cy < 0 || cy >= I.nc[1]) continue;
+        const int row = I.key_off + I.nc[0] * (cy + I.nc[1] * cz);
+        for (int dxc = -1; dxc <= 1; ++dxc) {
+          const int cx = cx0 + dxc;
+          if (cx < 0 || cx >= I.nc[0]) continue;
+          const int j0 = A.cellstart[row + cx], j1 = A.cellstart[row + cx + 1];
+          const float shx = (float)dxc * I.csf, shy = (float)dy * I.csf, shz = (float)dz * I.csf;
+          for (int j = j0; j < j1; ++j) {
+            if (j == i) continue;
+            float d[D];
+#pragma unroll
+            for (int q = 0; q < D; ++q) d[q] = (oi[q] - A.off[q][j]) - (q == 0 ? shx : (q == 1 ? shy : shz));
+            const float r2 = dot32<D>(d, d);
+            if (!(r2 < I.H2)) continue;
+            // sph∇W!: W'(r)/r of WendlandC2 = -20 nDW Hinv (1-q)^3
+            const float r = sqrtf(r2);
+            const float u = r * I.Hinv;
+            const float t = u < 1.f ? 1.f - u : 0.f;
+            const float dwr = -20.f * I.nDW * I.Hinv * (t * t * t);
+            float gw[D], dd[D], dv[D];
+#pragma unroll
+            for (int q = 0; q < D; ++q) {
+              gw[q] = d[q] * dwr;
+              dd[q] = STAGE == 1 ? d[q] : (ohi[q] - A.offh[q][j]) - (q == 0 ? shx : (q == 1 ? shy : shz));
+              dv[q] = vi[q] - (STAGE == 1 ? A.v[q][j] : A.vh[q][j]);
+            }
+            const float r2d = STAGE == 1 ? r2 : dot32<D>(dd, dd);
+            const int ptj = A.pt[j];
+            const float drj = STAGE == 1 ? A.dr[j] : A.drh[j];
+            const float rhoj = I.rho0 + drj;
+            const bool both = pti > 0 && ptj > 0;
+            const float inv = 1.f / (r2d + I.eta2);
+            float f[D];
+#pragma unroll
+            for (int q = 0; q < D; ++q) f[q] = 0.f;
+            if (both) {
+              // ∂ρ∂tDDT!
+              float term = I.m0 * dot32<D>(dv, gw);
+              if (pti > 1) {
+                const float dp = I.rho0 * root_m1(I.DDTgz * dd[1], I);
+                term += I.DDTkh * ((drj - dri) - dp) * inv * (-dot32<D>(dd, gw)) * I.m0 / rhoj;
+              }
+              drho.add(term);
+            }
+            if (pti * ptj > 0) {
+              // ∂v∂t!
+              const float sc = -I.m0 * (Pi + eos32(drj, ptj, I)) / (rhoi * rhoj);
+#pragma unroll
+              for (int q = 0; q < D; ++q) f[q] = sc * gw[q];
+            }
+            if (both) {
+              const float cond = dot32<D>(dv, dd);
+              if (cond < 0.f) {
+                // ∂v∂t_av!
+                const float dmu = I.h * cond * inv;
+                const float dPi = (-I.alpha * I.c0 * dmu) / ((rhoi + rhoj) * 0.5f);
+#pragma unroll
+                for (int q = 0; q < D; ++q) f[q] += -dPi * I.m0 * gw[q];
+              }
+              if (I.use_visc) {
+                // ∂v∂t_visc!
+                const float nt = 4.f * I.nu * I.m0 * dot32<D>(dd, gw) / (rhoi + rhoj) * inv;
+#pragma unroll
+                for (int q = 0; q < D; ++q) f[q] += nt * dv[q];
+              }
+              if (I.use_pF) {
+                // ∂v∂tpF!
+                const float rd = sqrtf(r2d);
+                if (rd < I.twoh) {
+                  const float scos = I.s * __cosf(I.pfc * rd / I.twoh) / (rd + I.hp1);  // argument in [0, 1.5π)
+#pragma unroll
+                  for (int q = 0; q < D; ++q) f[q] += scos * dd[q] / I.m0;
+                }
+              }
+            }
+            if ((pti > 0) != (ptj > 0) && r < I.fb_r0[fbs]) {
+              // fbmolforce! at x
+              const float qq = I.fb_r0[fbs] / (r + I.fb_eta2[fbs]);
+              const float q2 = qq * qq, q4 = q2 * q2, q8 = q4 * q4;
+              const float Fc = I.fb_d[fbs] * (q8 * q4 - q4) / (r2 + I.fb_eta2[fbs]);
+#pragma unroll
+              for (int q = 0; q < D; ++q) f[q] += d[q] * Fc;
+            }
+#pragma unroll
+            for (int q = 0; q < D; ++q) acc[q].add(f[q]);
+          }
+        }
+      }
+    }
+    float a[D];
+#pragma unroll
+    for (int q = 0; q < D; ++q) a[q] = acc[q].s - (q == 1 ? I.g : 0.f);
+    const float dt = (float)I.dt;
+    if (STAGE == 1) {
+      // update_ρp∂ρ∂tΔt!, update_vp∂v∂tΔt!, update_xpvΔt! at Δt/2
+      const float hdt = 0.5f * dt;
+      float drh = A.drb[i] + drho.s * hdt;
+      if (drh < 0.f && pti < 0) drh = 0.f;
+      A.drh[i] = drh;
+#pragma unroll
+      for (int q = 0; q < D; ++q) {
+        float vh = vi[q];
+        if (pti > 1) vh = vh + a[q] * hdt;
+        A.vh[q][i] = vh;
+        A.offh[q][i] = oi[q] + vh * hdt;
+      }
+    } else {
+      // symplectic_update!: δρ_new = δρ - ρ 2ε/(2+ε), positions in FP64
+      const float dr0 = A.dr[i];
+      const float epsi = -(drho.s / rhoi) * dt;
+      float dn = dr0 - (I.rho0 + dr0) * (2.f * epsi / (2.f + epsi));
+      if (dn < 0.f && pti <= 1) dn = 0.f;
+      A.dr[i] = dn;
+      A.drb[i] = dn;
+#pragma unroll
+      for (int q = 0; q < D; ++q) {
+        const float v0 = A.v[q][i];
+        const float nv = pti > 1 ? v0 + a[q] * dt : v0;
+        A.v[q][i] = nv;
+        A.x[q][i] = A.x[q][i] + ((double)v0 + (double)nv) * 0.5 * I.dt;
+      }
+    }
+  }
+}
+
+// cspmcorr! (src/gpukernels_sph.jl:1693-1719) of the instances whose step
+// count reaches a multiple of cspmn with this step: ρ = Σ m0 W / Σ (m0/ρ_j) W
+// over real neighbours at the step's starting positions, with the updated ρ_j;
+// formed as δρ = Σ m0 W δρ_j/ρ_j / Σ m0 W/ρ_j (no cancellation against ρ₀).
+// The result goes to δρ½ (free after the corrector) and is applied by
+// k_ens_cspm_apply, so every particle reads the pre-correction densities.
+__device__ __forceinline__ bool cspm_due(const EnsInst& I, const int32_t* istep, int s) {
+  return I.cspmn > 0 && (istep[s] + 1) % I.cspmn == 0;
+}
+
+template <int D>
+__global__ void __launch_bounds__(ENS_MAX_TPB) k_ens_cspm(EnsArr A, const EnsInst* __restrict__ T,
+                                                          const int32_t* __restrict__ istep) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < A.N; i += stride) {
+    const int s = A.inst[i];
+    const EnsInst& I = T[s];
+    if (!cspm_due(I, istep, s)) continue;
+    const float dri = A.dr[i];
+    if (!(A.pt[i] > 0)) {
+      A.drh[i] = dri;  // Σ over nothing: 0/0, the reference keeps ρ
+      continue;
+    }
+    int cx0, cy0, cz0;
+    cell_of(A.skey[i], I, cx0, cy0, cz0);
+    float oi[D];
+#pragma unroll
+    for (int d = 0; d < D; ++d) oi[d] = A.off[d][i];
+    KSum s2, s3;
+    const int zlo = D == 3 ? -1 : 0, zhi = D == 3 ? 1 : 0;
+    for (int dz = zlo; dz <= zhi; ++dz) {
+      const int cz = cz0 + dz;
+      if (cz < 0 || cz >= I.nc[2]) continue;
+      for (int dy = -1; dy <= 1; ++dy) {
+        const int cy = cy0 + dy;
+        if (cy < 0 || cy >= I.nc[1]) continue;
+        const int row = I.key_off + I.nc[0] * (cy + I.nc[1] * cz);
+        for (int dxc = -1; dxc <= 1; ++dxc) {
+          const int cx = cx0 + dxc;
+          if (cx < 0 || cx >= I.nc[0]) continue;
+          const int j0 = A.cellstart[row + cx], j1 = A.cellstart[row + cx + 1];
+          const float shx = (float)dxc * I.csf, shy = (float)dy * I.csf, shz = (float)dz * I.csf;
+          for (int j = j0; j < j1; ++j) {
+            if (j == i || !(A.pt[j] > 0)) continue;
+            float d[D];
+#pragma unroll
+            for (int q = 0; q < D; ++q) d[q] = (oi[q] - A.off[q][j]) - (q == 0 ? shx : (q == 1 ? shy : shz));
+            const float r2 = dot32<D>(d, d);
+            if (!(r2 < I.H2)) continue;
+            const float u = sqrtf(r2) * I.Hinv;
+            const float t = u < 1.f ? 1.f - u : 0.f;
+            const float t2 = t * t;
+            const float w = (1.f + 4.f * u) * (t2 * t2) * I.nW;
+            const float drj = A.dr[j];
+            const float mw = I.m0 * w / (I.rho0 + drj);
+            s2.add(mw);
+            s3.add(mw * drj);
+          }
+        }
+      }
+    }
+    const float nd = s3.s / s2.s;
+    A.drh[i] = nd == nd ? nd : dri;
+  }
+}
+
+__global__ void k_ens_cspm_apply(int64_t N, const int32_t* __restrict__ inst, const EnsInst* __restrict__ T,
+                                 const int32_t* __restrict__ istep, const float* __restrict__ drh,
+                                 float* __restrict__ dr) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  const int s = inst[i];
+  if (cspm_due(T[s], istep, s)) dr[i] = drh[i];
+}
+
+// one more step done, per instance
+__global__ void k_ens_tick(int ninst, int32_t* __restrict__ istep) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s < ninst) istep[s] += 1;
+}
+
+// gather one instance's field into its original particle order
+__global__ void k_ens_out(int64_t n, int64_t p0, const int32_t* __restrict__ id, const double* __restrict__ xd,
+                          const float* __restrict__ xf, const int32_t* __restrict__ xi, int mode, double base,
+                          double* __restrict__ out) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const int64_t q = p0 + k;
+  double v;
+  if (mode == 0) v = xd[q];
+  else if (mode == 1) v = base + (double)xf[q];
+  else v = (double)xi[q];
+  out[id[q]] = v;
+}
+
+__global__ void k_ens_pressure_out(int64_t n, int64_t p0, const int32_t* __restrict__ id,
+                                   const float* __restrict__ dr, const int32_t* __restrict__ pt,
+                                   const EnsInst* __restrict__ T, int si, double* __restrict__ out) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const int64_t q = p0 + k;
+  out[id[q]] = (double)eos32(dr[q], pt[q], T[si]);
+}
+
+__global__ void k_fill_i32(int32_t* __restrict__ p, int64_t n, int32_t v) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n) p[k] = v;
+}
+
+// repack after a removal: new range r takes old particles [old_off, old_off + n)
+struct Move {
+  int64_t new_off, old_off, n;
+};
+__global__ void k_ens_repack(int nmoves, const Move* __restrict__ mv, int64_t N, int D, EnsState in, EnsState out) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= N) return;
+  int lo = 0, hi = nmoves - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (mv[mid].new_off <= k) lo = mid;
+    else hi = mid - 1;
+  }
+  const int64_t src = mv[lo].old_off + (k - mv[lo].new_off);
+  for (int d = 0; d < D; ++d) {
+    out.x[d][k] = in.x[d][src];
+    out.v[d][k] = in.v[d][src];
+  }
+  out.dr[k] = in.dr[src];
+  out.drb[k] = in.drb[src];
+  out.pt[k] = in.pt[src];
+  out.id[k] = in.id[src];
+}
+
+}  // namespace
+}  // namespace gcsph
+
+using namespace gcsph;
+
+struct EnsHostInst {
+  int32_t slot;
+  int64_t n, p_off;
+  int64_t key_off, ncell;
+  gcsph_ens_params prm;
+  int64_t steps;
+  EnsInst dev;
+};
+
+struct EnsGraph {
+  int64_t n_steps = -1, N = -1, K = -1, gen = -1;
+  int cur = -1, tpb = 0, timing = 0;
+  cudaGraphExec_t exec = nullptr;
+  unsigned long long used = 0;
+  long long launches = 0;
+  std::vector<TimerRec> timers;
+};
+
+struct gcsph_ens {
+  int D = 2;
+  cudaStream_t st = 0;
+  cudaStream_t cap = nullptr;
+  std::vector<EnsHostInst> inst;  // packing order
+  int32_t next_slot = 0;
+  int64_t N = 0, K = 0, cap_n = 0, cap_k = 0;
+  int cur = 0;
+  int64_t gen = 0;  // layout generation (graphs and tuning follow it)
+  // state, double-buffered for the re-sort
+  DevBuf X[2][3], V[2][3], DR[2], DRB[2], PT[2], ID[2];
+  DevBuf INST, KEY, SLOT, TMP, PERM, SKEY, OFF[3], OFFH[3], VH[3], DRH, COUNT, CELLSTART, SCRATCH, TAB, MOVES, OUT;
+  DevBuf ISTEP;          // steps done per instance (cspmcorr! schedule), packing order
+  int tpb = 0;           // 0: not tuned yet
+  bool tpb_fixed = false;
+  int64_t tuned_n = 0;   // particle count the choice was made on
+  int sms = 0, occ[4] = {0, 0, 0, 0};
+  EnsGraph graphs[4];
+  unsigned long long clock = 0;
+  bool use_graphs = true;
+  bool any_cspm = false;  // some instance runs cspmcorr!
+  int64_t n_captures = 0, n_replays = 0;
+};
+
+namespace {
+
+const int kTpbs[3] = {128, 256, 512};
+
+EnsState ens_state(gcsph_ens* e, int b) {
+  EnsState s{};
+  for (int d = 0; d < 3; ++d) {
+    s.x[d] = e->X[b][d].as<double>();
+    s.v[d] = e->V[b][d].as<float>();
+  }
+  s.dr = e->DR[b].as<float>();
+  s.drb = e->DRB[b].as<float>();
+  s.pt = e->PT[b].as<int32_t>();
+  s.id = e->ID[b].as<int32_t>();
+  return s;
+}
+
+EnsArr ens_arr(gcsph_ens* e) {
+  EnsArr A{};
+  A.N = e->N;
+  A.inst = e->INST.as<int32_t>();
+  A.skey = e->SKEY.as<int32_t>();
+  A.cellstart = e->CELLSTART.as<int32_t>();
+  for (int d = 0; d < 3; ++d) {
+    A.x[d] = e->X[e->cur][d].as<double>();
+    A.v[d] = e->V[e->cur][d].as<float>();
+    A.off[d] = e->OFF[d].as<float>();
+    A.offh[d] = e->OFFH[d].as<float>();
+    A.vh[d] = e->VH[d].as<float>();
+  }
+  A.dr = e->DR[e->cur].as<float>();
+  A.drb = e->DRB[e->cur].as<float>();
+  A.drh = e->DRH.as<float>();
+  A.pt = e->PT[e->cur].as<int32_t>();
+  return A;
+}
+
+void graph_free(EnsGraph& g) {
+  if (g.exec) cudaGraphExecDestroy(g.exec);
+  timer_release(g.timers);
+  g = EnsGraph{};
+}
+
+void graphs_free(gcsph_ens* e) {
+  for (EnsGraph& g : e->graphs) graph_free(g);
+}
+
+// grow every per-particle buffer to hold n particles (keeps the first N)
+int ens_reserve(gcsph_ens* e, int64_t n) {
+  if (n <= e->cap_n) return GCSPH_OK;
+  const int64_t want = std::max<int64_t>(n, e->cap_n + e->cap_n / 2 + 1024);
+  // move live state through fresh buffers: DevBuf::ensure does not keep contents
+  int rc;
+  for (int b = 0; b < 2; ++b) {
+    auto keep = [&](DevBuf& buf, size_t esz) -> int {
+      DevBuf fresh;
+      int r = fresh.ensure(esz * want, e->st);
+      if (r) return r;
+      if (b == e->cur && e->N > 0 && buf.p)
+        GC_CUDA(cudaMemcpyAsync(fresh.p, buf.p, esz * e->N, cudaMemcpyDeviceToDevice, e->st));
+      GC_CUDA(cudaStreamSynchronize(e->st));
+      buf.release();
+      buf = fresh;
+      fresh.p = nullptr;
+      return GCSPH_OK;
+    };
+    for (int d = 0; d < e->D; ++d) {
+      if ((rc = keep(e->X[b][d], sizeof(double)))) return rc;
+      if ((rc = keep(e->V[b][d], sizeof(float)))) return rc;
+    }
+    if ((rc = keep(e->DR[b], sizeof(float)))) return rc;
+    if ((rc = keep(e->DRB[b], sizeof(float)))) return rc;
+    if ((rc = keep(e->PT[b], sizeof(int32_t)))) return rc;
+    if ((rc = keep(e->ID[b], sizeof(int32_t)))) return rc;
+  }
+  DevBuf* i32[] = {&e->INST, &e->KEY, &e->SLOT, &e->TMP, &e->PERM, &e->SKEY};
+  for (DevBuf* b : i32)
+    if ((rc = b->ensure(sizeof(int32_t) * want, e->st))) return rc;
+  for (int d = 0; d < e->D; ++d) {
+    if ((rc = e->OFF[d].ensure(sizeof(float) * want, e->st))) return rc;
+    if ((rc = e->OFFH[d].ensure(sizeof(float) * want, e->st))) return rc;
+    if ((rc = e->VH[d].ensure(sizeof(float) * want, e->st))) return rc;
+  }
+  if ((rc = e->DRH.ensure(sizeof(float) * want, e->st))) return rc;
+  if ((rc = e->SCRATCH.ensure(sizeof(int64_t) * scan_scratch_elems(std::max<int64_t>(want, e->cap_k) + 1), e->st)))
+    return rc;
+  e->cap_n = want;
+  return GCSPH_OK;
+}
+
+int ens_reserve_cells(gcsph_ens* e, int64_t k) {
+  if (k + 1 > (int64_t)INT32_MAX) return fail(GCSPH_ECAPACITY, "ensemble cell count past 2^31");
+  if (k <= e->cap_k) return GCSPH_OK;
+  const int64_t want = std::max<int64_t>(k, e->cap_k + e->cap_k / 2 + 4096);
+  int rc;
+  if ((rc = e->COUNT.ensure(sizeof(int32_t) * want, e->st))) return rc;
+  if ((rc = e->CELLSTART.ensure(sizeof(int32_t) * (want + 1), e->st))) return rc;
+  if ((rc = e->SCRATCH.ensure(sizeof(int64_t) * scan_scratch_elems(std::max<int64_t>(want, e->cap_n) + 1), e->st)))
+    return rc;
+  e->cap_k = want;
+  return GCSPH_OK;
+}
+
+// device instance table + per-particle instance index after a layout change
+int ens_relayout(gcsph_ens* e) {
+  int64_t p = 0, k = 0;
+  for (EnsHostInst& h : e->inst) {
+    h.p_off = p;
+    h.key_off = k;
+    h.dev.key_off = (int)k;
+    p += h.n;
+    k += h.ncell;
+  }
+  e->N = p;
+  e->K = k;
+  e->any_cspm = false;
+  for (const EnsHostInst& h : e->inst) e->any_cspm = e->any_cspm || h.prm.cspmn > 0;
+  int rc;
+  if ((rc = ens_reserve_cells(e, k))) return rc;
+  std::vector<EnsInst> tab(e->inst.size());
+  for (size_t s = 0; s < e->inst.size(); ++s) tab[s] = e->inst[s].dev;
+  if ((rc = e->TAB.ensure(sizeof(EnsInst) * std::max<size_t>(tab.size(), 1), e->st))) return rc;
+  if (!tab.empty())
+    GC_CUDA(cudaMemcpyAsync(e->TAB.p, tab.data(), sizeof(EnsInst) * tab.size(), cudaMemcpyHostToDevice, e->st));
+  std::vector<int32_t> isteps(e->inst.size());
+  for (size_t s = 0; s < e->inst.size(); ++s) isteps[s] = (int32_t)(e->inst[s].steps % 2000000000LL);
+  if ((rc = e->ISTEP.ensure(sizeof(int32_t) * std::max<size_t>(isteps.size(), 1), e->st))) return rc;
+  if (!isteps.empty())
+    GC_CUDA(cudaMemcpyAsync(e->ISTEP.p, isteps.data(), sizeof(int32_t) * isteps.size(), cudaMemcpyHostToDevice,
+                            e->st));
+  for (size_t s = 0; s < e->inst.size(); ++s) {
+    const EnsHostInst& h = e->inst[s];
+    if (h.n == 0) continue;
+    k_fill_i32<<<nblocks(h.n, 256), 256, 0, e->st>>>(e->INST.as<int32_t>() + h.p_off, h.n, (int32_t)s);
+    GC_LAUNCHED();
+  }
+  GC_CUDA(cudaStreamSynchronize(e->st));
+  e->gen += 1;
+  graphs_free(e);
+  return GCSPH_OK;
+}
+
+int ens_occupancy(gcsph_ens* e) {
+  if (e->sms) return GCSPH_OK;
+  int dev = 0;
+  GC_CUDA(cudaGetDevice(&dev));
+  GC_CUDA(cudaDeviceGetAttribute(&e->sms, cudaDevAttrMultiProcessorCount, dev));
+  for (int t = 0; t < 3; ++t) {
+    int b = 0;
+    if (e->D == 2)
+      GC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_ens_stage<2, 2>, kTpbs[t], 0));
+    else
+      GC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_ens_stage<3, 2>, kTpbs[t], 0));
+    e->occ[t] = std::max(b, 1);
+  }
+  return GCSPH_OK;
+}
+
+int tpb_index(int tpb) {
+  for (int t = 0; t < 3; ++t)
+    if (kTpbs[t] == tpb) return t;
+  return 1;
+}
+
+// one step of every instance: bin, re-sort, predictor pass, corrector pass
+template <int D>
+int ens_enqueue_step(gcsph_ens* e, cudaStream_t st, int tpb) {
+  const int64_t N = e->N;
+  const EnsInst* T = e->TAB.as<EnsInst>();
+  GC_CUDA(cudaMemsetAsync(e->COUNT.p, 0, sizeof(int32_t) * e->K, st));
+  const double* x2 = D == 3 ? e->X[e->cur][2].as<double>() : e->X[e->cur][0].as<double>();
+  k_ens_key<D><<<nblocks(N, 256), 256, 0, st>>>(N, e->INST.as<int32_t>(), e->X[e->cur][0].as<double>(),
+                                                 e->X[e->cur][1].as<double>(), x2, T, e->KEY.as<int32_t>(),
+                                                 e->SLOT.as<int32_t>(), e->COUNT.as<int32_t>());
+  GC_LAUNCHED();
+  int rc = exclusive_scan_i32_to_i32(e->COUNT.as<int32_t>(), e->CELLSTART.as<int32_t>(), e->K,
+                                     e->SCRATCH.as<int64_t>(), st);
+  if (rc) return rc;
+  k_ens_scatter<<<nblocks(N, 256), 256, 0, st>>>(N, e->KEY.as<int32_t>(), e->SLOT.as<int32_t>(),
+                                                 e->CELLSTART.as<int32_t>(), e->TMP.as<int32_t>());
+  GC_LAUNCHED();
+  k_ens_rank<<<nblocks(N, 256), 256, 0, st>>>(N, e->TMP.as<int32_t>(), e->KEY.as<int32_t>(),
+                                              e->CELLSTART.as<int32_t>(), e->ID[e->cur].as<int32_t>(),
+                                              e->PERM.as<int32_t>());
+  GC_LAUNCHED();
+  float* o2 = D == 3 ? e->OFF[2].as<float>() : e->OFF[0].as<float>();
+  k_ens_permute<D><<<nblocks(N, 256), 256, 0, st>>>(N, e->PERM.as<int32_t>(), e->KEY.as<int32_t>(),
+                                                     e->INST.as<int32_t>(), T, ens_state(e, e->cur),
+                                                     ens_state(e, e->cur ^ 1), e->SKEY.as<int32_t>(),
+                                                     e->OFF[0].as<float>(), e->OFF[1].as<float>(), o2);
+  GC_LAUNCHED();
+  e->cur ^= 1;
+  const int t = tpb_index(tpb);
+  const int64_t want = (N + tpb - 1) / tpb;
+  const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)e->sms * e->occ[t]));
+  EnsArr A = ens_arr(e);
+  timer_begin(T_STAGE1, st);
+  k_ens_stage<D, 1><<<grid, tpb, 0, st>>>(A, T);
+  GC_LAUNCHED();
+  timer_end(T_STAGE1, st);
+  timer_begin(T_STAGE2, st);
+  k_ens_stage<D, 2><<<grid, tpb, 0, st>>>(A, T);
+  GC_LAUNCHED();
+  timer_end(T_STAGE2, st);
+  const int32_t ninst = (int32_t)e->inst.size();
+  if (e->any_cspm) {
+    timer_begin(T_CSPM, st);
+    k_ens_cspm<D><<<grid, tpb, 0, st>>>(A, T, e->ISTEP.as<int32_t>());
+    GC_LAUNCHED();
+    k_ens_cspm_apply<<<nblocks(N, 256), 256, 0, st>>>(N, e->INST.as<int32_t>(), T, e->ISTEP.as<int32_t>(),
+                                                      e->DRH.as<float>(), e->DR[e->cur].as<float>());
+    GC_LAUNCHED();
+    timer_end(T_CSPM, st);
+  }
+  k_ens_tick<<<nblocks(ninst, 128), 128, 0, st>>>(ninst, e->ISTEP.as<int32_t>());
+  GC_LAUNCHED();
+  return GCSPH_OK;
+}
+
+int enqueue_step(gcsph_ens* e, cudaStream_t st, int tpb) {
+  return e->D == 2 ? ens_enqueue_step<2>(e, st, tpb) : ens_enqueue_step<3>(e, st, tpb);
+}
+
+// block size of the pair passes: each candidate runs two real steps (the
+// arithmetic per particle does not depend on the launch shape, so tuning
+// steps are ordinary steps), the fastest pair of passes wins
+int ens_autotune(gcsph_ens* e, int32_t budget, int32_t* steps_used) {
+  *steps_used = 0;
+  if (e->tpb_fixed) return GCSPH_OK;
+  if (e->tpb && e->tuned_n > 0 && e->N <= 2 * e->tuned_n && 2 * e->N >= e->tuned_n) return GCSPH_OK;
+  if (budget < 6) {
+    // too few steps to time three shapes: a default now, a tuning later
+    if (!e->tpb) e->tpb = 256;
+    return GCSPH_OK;
+  }
+  cudaEvent_t a, b;
+  GC_CUDA(cudaEventCreate(&a));
+  GC_CUDA(cudaEventCreate(&b));
+  float best = 1e30f;
+  int pick = 256;
+  int rc = GCSPH_OK;
+  for (int t = 0; t < 3 && rc == GCSPH_OK; ++t) {
+    float tot = 0.f;
+    for (int r = 0; r < 2 && rc == GCSPH_OK; ++r) {
+      cudaEventRecord(a, e->st);
+      rc = enqueue_step(e, e->st, kTpbs[t]);
+      cudaEventRecord(b, e->st);
+      cudaEventSynchronize(b);
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, a, b);
+      if (r > 0) tot += ms;  // the first run of each shape warms caches
+      *steps_used += 1;
+    }
+    if (tot < best) {
+      best = tot;
+      pick = kTpbs[t];
+    }
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  if (rc) return rc;
+  e->tpb = pick;
+  e->tuned_n = e->N;
+  return GCSPH_OK;
+}
+
+int ens_run(gcsph_ens* e, int32_t n) {
+  if (n <= 0 || e->N == 0) return GCSPH_OK;
+  if (!e->use_graphs) {
+    for (int32_t it = 0; it < n; ++it) {
+      int rc = enqueue_step(e, e->st, e->tpb);
+      if (rc) return rc;
+    }
+    GC_CUDA(cudaStreamSynchronize(e->st));
+    timer_collect();
+    return GCSPH_OK;
+  }
+  EnsGraph* g = nullptr;
+  const int timing = timing_on() ? 1 : 0;
+  for (EnsGraph& c : e->graphs)
+    if (c.exec && c.n_steps == n && c.N == e->N && c.K == e->K && c.gen == e->gen && c.cur == e->cur &&
+        c.tpb == e->tpb && c.timing == timing)
+      g = &c;
+  if (!g) {
+    g = &e->graphs[0];
+    for (EnsGraph& c : e->graphs)
+      if (!c.exec || c.used < g->used) g = &c;
+    graph_free(*g);
+    if (!e->cap) GC_CUDA(cudaStreamCreateWithFlags(&e->cap, cudaStreamNonBlocking));
+    const int cur0 = e->cur;
+    const unsigned long long l0 = gcsph_launch_count();
+    GC_CUDA(cudaStreamBeginCapture(e->cap, cudaStreamCaptureModeThreadLocal));
+    timer_capture_to(&g->timers);
+    int rc = GCSPH_OK;
+    for (int32_t it = 0; it < n && rc == GCSPH_OK; ++it) rc = enqueue_step(e, e->cap, e->tpb);
+    timer_capture_to(nullptr);
+    cudaGraph_t graph = nullptr;
+    cudaError_t ce = cudaStreamEndCapture(e->cap, &graph);
+    const unsigned long long l1 = gcsph_launch_count();
+    count_launch(-(int)(l1 - l0));
+    const int cur1 = e->cur;
+    e->cur = cur0;
+    if (rc == GCSPH_OK && ce != cudaSuccess) rc = cuda_fail(ce, "cudaStreamEndCapture", __FILE__, __LINE__);
+    if (rc == GCSPH_OK) {
+      ce = cudaGraphInstantiate(&g->exec, graph, 0);
+      if (ce != cudaSuccess) rc = cuda_fail(ce, "cudaGraphInstantiate", __FILE__, __LINE__);
+    }
+    if (graph) cudaGraphDestroy(graph);
+    if (rc != GCSPH_OK) {
+      cudaGetLastError();
+      graph_free(*g);
+      return rc;
+    }
+    g->timing = timing;
+    g->n_steps = n;
+    g->N = e->N;
+    g->K = e->K;
+    g->gen = e->gen;
+    g->cur = cur0;
+    g->tpb = e->tpb;
+    g->launches = (long long)(l1 - l0);
+    (void)cur1;
+    e->n_captures += 1;
+  }
+  g->used = ++e->clock;
+  GC_CUDA(cudaGraphLaunch(g->exec, e->st));
+  GC_CUDA(cudaStreamSynchronize(e->st));
+  count_launch((int)g->launches);
+  timer_account(g->timers);
+  if (n & 1) e->cur ^= 1;
+  e->n_replays += 1;
+  return GCSPH_OK;
+}
+
+EnsHostInst* find_slot(gcsph_ens* e, int32_t slot, size_t* pos = nullptr) {
+  for (size_t s = 0; s < e->inst.size(); ++s)
+    if (e->inst[s].slot == slot) {
+      if (pos) *pos = s;
+      return &e->inst[s];
+    }
+  return nullptr;
+}
+
+}  // namespace
+
+extern "C" {
+
+int ens_create(int32_t D, void* stream, gcsph_ens** out) {
+  if (!out) return fail(GCSPH_EINVAL, "null argument");
+  *out = nullptr;
+  if (D != 2 && D != 3) return fail(GCSPH_EINVAL, "wrong dimention: D=%d (2 or 3)", (int)D);
+  gcsph_ens* e = new gcsph_ens();
+  e->D = D;
+  e->st = (cudaStream_t)stream;
+  int rc = ens_occupancy(e);
+  if (rc) {
+    delete e;
+    return rc;
+  }
+  *out = e;
+  return GCSPH_OK;
+}
+
+void ens_destroy(gcsph_ens* e) {
+  if (!e) return;
+  cudaStreamSynchronize(e->st);
+  graphs_free(e);
+  if (e->cap) cudaStreamDestroy(e->cap);
+  for (int b = 0; b < 2; ++b) {
+    for (int d = 0; d < 3; ++d) {
+      e->X[b][d].release();
+      e->V[b][d].release();
+    }
+    e->DR[b].release();
+    e->DRB[b].release();
+    e->PT[b].release();
+    e->ID[b].release();
+  }
+  DevBuf* one[] = {&e->INST, &e->KEY, &e->SLOT, &e->TMP, &e->PERM, &e->SKEY, &e->DRH, &e->COUNT, &e->CELLSTART,
+                   &e->SCRATCH, &e->TAB, &e->MOVES, &e->OUT, &e->ISTEP};
+  for (DevBuf* b : one) b->release();
+  for (int d = 0; d < 3; ++d) {
+    e->OFF[d].release();
+    e->OFFH[d].release();
+    e->VH[d].release();
+  }
+  delete e;
+}
+
+int ens_bytes_per_particle(int32_t D, int64_t* bytes) {
+  if (!bytes || (D != 2 && D != 3)) return fail(GCSPH_EINVAL, "bad argument");
+  // 2 x (x f64, v f32) per dim + 2 x (δρ, δρ base, ptype, id) + inst, key,
+  // slot, tmp, perm, skey + (off, offh, vh) per dim + δρ½, plus about one
+  // cell per particle
+  *bytes = 2 * D * (8 + 4) + 2 * 16 + 6 * 4 + D * 12 + 4 + 8;
+  return GCSPH_OK;
+}
+
+int ens_add(gcsph_ens* e, int64_t n, const double* x, const double* v, const double* rho, const int32_t* ptype,
+            const gcsph_ens_params* p, int32_t* slot_out) {
+  if (!e || !x || !rho || !ptype || !p || !slot_out) return fail(GCSPH_EINVAL, "null argument");
+  if (n <= 0 || n > (int64_t)INT32_MAX / 2) return fail(GCSPH_EINVAL, "particle count %lld", (long long)n);
+  if (!(p->H > 0) || !(p->dt > 0) || p->gamma <= 0) return fail(GCSPH_EINVAL, "H, dt and gamma must be positive");
+  const int D = e->D;
+  EnsHostInst h{};
+  h.slot = e->next_slot++;
+  h.n = n;
+  h.prm = *p;
+  h.steps = 0;
+  EnsInst& I = h.dev;
+  memset(&I, 0, sizeof(I));
+  const double cs = p->H;
+  int64_t ncell = 1;
+  for (int d = 0; d < 3; ++d) {
+    if (d < D) {
+      if (!(p->grid_max[d] > p->grid_min[d])) return fail(GCSPH_EINVAL, "empty grid in dimension %d", d + 1);
+      I.origin[d] = p->grid_min[d];
+      const double span = p->grid_max[d] - p->grid_min[d];
+      const double nc = floor(span / cs) + 1.0;
+      if (nc > 1e8) return fail(GCSPH_EINVAL, "grid too fine");
+      I.nc[d] = (int)nc;
+    } else {
+      I.origin[d] = 0.0;
+      I.nc[d] = 1;
+    }
+    ncell *= I.nc[d];
+  }
+  if (ncell > (int64_t)INT32_MAX / 2) return fail(GCSPH_EINVAL, "grid of %lld cells", (long long)ncell);
+  h.ncell = ncell;
+  I.cs = cs;
+  I.csinv = 1.0 / cs;
+  I.csf = (float)cs;
+  I.dt = p->dt;
+  I.gamma = p->gamma;
+  I.cspmn = p->cspmn > 0 ? p->cspmn : 0;
+  I.use_visc = p->nu > 0;
+  I.use_pF = p->s > 0;
+  I.H2 = (float)(p->H * p->H);
+  I.h = (float)p->h;
+  I.Hinv = (float)(1.0 / p->H);
+  I.nW = (float)(D == 2 ? wc2_norm_w<2>(1.0 / p->H) : wc2_norm_w<3>(1.0 / p->H));
+  I.nDW = (float)(D == 2 ? wc2_norm_dw<2>(1.0 / p->H) : wc2_norm_dw<3>(1.0 / p->H));
+  I.m0 = (float)p->m0;
+  I.rho0 = (float)p->rho0;
+  I.c0 = (float)p->c0;
+  I.P0 = (float)(p->c0 * p->c0 * p->rho0 / (double)p->gamma);
+  I.alpha = (float)p->alpha;
+  I.DDTkh = (float)(2.0 * p->h * p->delta * p->c0);
+  I.DDTgz = (float)(p->rho0 * p->g / ((p->c0 * p->c0 * p->rho0) / (double)p->gamma));
+  I.eta2 = (float)((0.1 * p->h) * (0.1 * p->h));
+  I.g = (float)p->g;
+  I.nu = (float)p->nu;
+  I.s = (float)p->s;
+  I.twoh = (float)(2.0 * p->h);
+  I.pfc = (float)(1.5 * GCSPH_PI64);
+  I.hp1 = (float)(0.1 * p->h);
+  const double r01 = 2.0 * p->dx;
+  I.fb_d[0] = 0.4f;
+  I.fb_r0[0] = (float)r01;
+  I.fb_eta2[0] = (float)(0.01 * r01 * r01);
+  I.fb_d[1] = (float)p->bound_D;
+  I.fb_r0[1] = (float)p->bound_l;
+  I.fb_eta2[1] = (float)(0.01 * p->bound_l * p->bound_l);
+  const double a = 1.0 / (double)p->gamma;
+  const double c1 = a, c2 = c1 * (a - 1.0) / 2.0, c3 = c2 * (a - 2.0) / 3.0, c4 = c3 * (a - 3.0) / 4.0;
+  I.pc[0] = (float)c1;
+  I.pc[1] = (float)c2;
+  I.pc[2] = (float)c3;
+  I.pc[3] = (float)c4;
+  // host staging in the engine's types
+  std::vector<float> vf((size_t)D * n, 0.f), drf((size_t)n);
+  std::vector<int32_t> ids((size_t)n);
+  for (int64_t i = 0; i < n; ++i) {
+    drf[i] = (float)(rho[i] - p->rho0);
+    ids[i] = (int32_t)i;
+  }
+  if (v)
+    for (int64_t i = 0; i < (int64_t)D * n; ++i) vf[i] = (float)v[i];
+  const int64_t at = e->N;
+  int rc;
+  if ((rc = ens_reserve(e, at + n))) return rc;
+  const int b = e->cur;
+  for (int d = 0; d < D; ++d) {
+    GC_CUDA(cudaMemcpyAsync(e->X[b][d].as<double>() + at, x + (size_t)d * n, sizeof(double) * n,
+                            cudaMemcpyHostToDevice, e->st));
+    GC_CUDA(cudaMemcpyAsync(e->V[b][d].as<float>() + at, vf.data() + (size_t)d * n, sizeof(float) * n,
+                            cudaMemcpyHostToDevice, e->st));
+  }
+  GC_CUDA(cudaMemcpyAsync(e->DR[b].as<float>() + at, drf.data(), sizeof(float) * n, cudaMemcpyHostToDevice, e->st));
+  GC_CUDA(cudaMemcpyAsync(e->DRB[b].as<float>() + at, drf.data(), sizeof(float) * n, cudaMemcpyHostToDevice, e->st));
+  GC_CUDA(cudaMemcpyAsync(e->PT[b].as<int32_t>() + at, ptype, sizeof(int32_t) * n, cudaMemcpyHostToDevice, e->st));
+  GC_CUDA(cudaMemcpyAsync(e->ID[b].as<int32_t>() + at, ids.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice,
+                          e->st));
+  GC_CUDA(cudaStreamSynchronize(e->st));
+  e->inst.push_back(h);
+  if ((rc = ens_relayout(e))) {
+    e->inst.pop_back();
+    ens_relayout(e);
+    return rc;
+  }
+  *slot_out = h.slot;
+  return GCSPH_OK;
+}
+
+int ens_remove(gcsph_ens* e, int32_t slot) {
+  if (!e) return fail(GCSPH_EINVAL, "null handle");
+  size_t pos = 0;
+  if (!find_slot(e, slot, &pos)) return fail(GCSPH_EINVAL, "no instance in slot %d", (int)slot);
+  std::vector<Move> mv;
+  int64_t p = 0;
+  for (size_t s = 0; s < e->inst.size(); ++s) {
+    if (s == pos) continue;
+    mv.push_back({p, e->inst[s].p_off, e->inst[s].n});
+    p += e->inst[s].n;
+  }
+  e->inst.erase(e->inst.begin() + (long)pos);
+  int rc;
+  if (p > 0) {
+    if ((rc = e->MOVES.ensure(sizeof(Move) * mv.size(), e->st))) return rc;
+    GC_CUDA(cudaMemcpyAsync(e->MOVES.p, mv.data(), sizeof(Move) * mv.size(), cudaMemcpyHostToDevice, e->st));
+    k_ens_repack<<<nblocks(p, 256), 256, 0, e->st>>>((int)mv.size(), e->MOVES.as<Move>(), p, e->D,
+                                                      ens_state(e, e->cur), ens_state(e, e->cur ^ 1));
+    GC_LAUNCHED();
+    e->cur ^= 1;
+  }
+  return ens_relayout(e);
+}
+
+int ens_step(gcsph_ens* e, int32_t n) {
+  if (!e) return fail(GCSPH_EINVAL, "null handle");
+  if (n < 0) return fail(GCSPH_EINVAL, "n must be >= 0");
+  if (e->N == 0 || n == 0) return GCSPH_OK;
+  int32_t used = 0;
+  int rc = ens_autotune(e, n, &used);
+  if (rc) return rc;
+  // tuning steps are real steps; they count toward n
+  if (n - used > 0 && (rc = ens_run(e, n - used))) return rc;
+  for (EnsHostInst& h : e->inst) h.steps += n;
+  return GCSPH_OK;
+}
+
+int ens_get(gcsph_ens* e, int32_t slot, int32_t field, double* out_host) {
+  if (!e || !out_host) return fail(GCSPH_EINVAL, "null argument");
+  size_t pos = 0;
+  EnsHostInst* h = find_slot(e, slot, &pos);
+  if (!h) return fail(GCSPH_EINVAL, "no instance in slot %d", (int)slot);
+  const int D = e->D;
+  const int64_t n = h->n;
+  int rc;
+  const int comps = (field == GCSPH_ENS_X || field == GCSPH_ENS_V) ? D : 1;
+  if ((rc = e->OUT.ensure(sizeof(double) * n * comps, e->st))) return rc;
+  double* o = e->OUT.as<double>();
+  const int b = e->cur;
+  const int32_t* id = e->ID[b].as<int32_t>();
+  const int nb = nblocks(n, 256);
+  switch (field) {
+    case GCSPH_ENS_X:
+      for (int d = 0; d < D; ++d)
+        k_ens_out<<<nb, 256, 0, e->st>>>(n, h->p_off, id, e->X[b][d].as<double>(), nullptr, nullptr, 0, 0.0,
+                                          o + (size_t)d * n);
+      break;
+    case GCSPH_ENS_V:
+      for (int d = 0; d < D; ++d)
+        k_ens_out<<<nb, 256, 0, e->st>>>(n, h->p_off, id, nullptr, e->V[b][d].as<float>(), nullptr, 1, 0.0,
+                                          o + (size_t)d * n);
+      break;
+    case GCSPH_ENS_RHO:
+      k_ens_out<<<nb, 256, 0, e->st>>>(n, h->p_off, id, nullptr, e->DR[b].as<float>(), nullptr, 1, h->prm.rho0, o);
+      break;
+    case GCSPH_ENS_DRHO:
+      k_ens_out<<<nb, 256, 0, e->st>>>(n, h->p_off, id, nullptr, e->DR[b].as<float>(), nullptr, 1, 0.0, o);
+      break;
+    case GCSPH_ENS_P:
+      k_ens_pressure_out<<<nb, 256, 0, e->st>>>(n, h->p_off, id, e->DR[b].as<float>(), e->PT[b].as<int32_t>(),
+                                                 e->TAB.as<EnsInst>(), (int)pos, o);
+      break;
+    case GCSPH_ENS_PTYPE:
+      k_ens_out<<<nb, 256, 0, e->st>>>(n, h->p_off, id, nullptr, nullptr, e->PT[b].as<int32_t>(), 2, 0.0, o);
+      break;
+    default:
+      return fail(GCSPH_EINVAL, "unknown ensemble field %d", (int)field);
+  }
+  GC_LAUNCHED();
+  GC_CUDA(cudaMemcpyAsync(out_host, o, sizeof(double) * n * comps, cudaMemcpyDeviceToHost, e->st));
+  GC_CUDA(cudaStreamSynchronize(e->st));
+  return GCSPH_OK;
+}
+
+int ens_info(gcsph_ens* e, int32_t slot, int64_t* n, int64_t* steps, double* etime) {
+  if (!e) return fail(GCSPH_EINVAL, "null handle");
+  EnsHostInst* h = find_slot(e, slot);
+  if (!h) return fail(GCSPH_EINVAL, "no instance in slot %d", (int)slot);
+  if (n) *n = h->n;
+  if (steps) *steps = h->steps;
+  if (etime) *etime = (double)h->steps * h->prm.dt;
+  return GCSPH_OK;
+}
+
+int ens_totals(gcsph_ens* e, int32_t* ninst, int64_t* nparticles, int64_t* ncells) {
+  if (!e) return fail(GCSPH_EINVAL, "null handle");
+  if (ninst) *ninst = (int32_t)e->inst.size();
+  if (nparticles) *nparticles = e->N;
+  if (ncells) *ncells = e->K;
+  return GCSPH_OK;
+}
+
+int ens_set_tuning(gcsph_ens* e, int32_t tpb, int32_t graphs) {
+  if (!e) return fail(GCSPH_EINVAL, "null handle");
+  if (!(tpb == 0 || tpb == 128 || tpb == 256 || tpb == 512)) return fail(GCSPH_EINVAL, "tpb must be 0, 128, 256 or 512");
+  e->tpb = tpb;
+  e->tpb_fixed = tpb != 0;
+  e->tuned_n = 0;
+  e->use_graphs = graphs != 0;
+  return GCSPH_OK;
+}
+
+int ens_get_tuning(gcsph_ens* e, int32_t* tpb, int64_t* captures, int64_t* replays) {
+  if (!e) return fail(GCSPH_EINVAL, "null handle");
+  if (tpb) *tpb = e->tpb;
+  if (captures) *captures = e->n_captures;
+  if (replays) *replays = e->n_replays;
+  return GCSPH_OK;
+}
+
+}  // extern "C"

@@ -272,9 +272,12 @@ __device__ inline void finish_acc(const StepConst& c, const Acc<D>& A, double* a
 // ---------------------------------------------------------------------------
 template <int L>
 __device__ inline unsigned group_mask() {
-  if (L == 32) return 0xffffffffu;
-  const unsigned lanew = threadIdx.x & 31u;
-  return ((1u << L) - 1u) << (lanew & ~(unsigned)(L - 1));
+  if constexpr (L == 32) {
+    return 0xffffffffu;
+  } else {
+    const unsigned lanew = threadIdx.x & 31u;
+    return ((1u << L) - 1u) << (lanew & ~(unsigned)(L - 1));
+  }
 }
 template <int L>
 __device__ inline double group_sum(double v, unsigned gm) {

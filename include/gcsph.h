@@ -262,6 +262,49 @@ int gcsph_dt_stepping(int32_t D, int64_t N, const double* const* a_dev, const do
 /* dpckernlim = find_zero(x -> 1 - 𝒲(k, x, 1), 0.5) -- src/sphproblem.jl:218 (host scalar) */
 double gcsph_dpckernlim(int32_t D);
 
+/* ------------------------------------------------------------------------
+ * Batched FP32 ensemble (no reference counterpart: the reference steps one
+ * SPHProblem at a time).  Many independent instances -- each its own particle
+ * set, parameters, frozen cell grid (cell edge = H) and fixed Δt -- advance
+ * together, one launch per pass over all of them.  Pair arithmetic and
+ * per-particle sums in FP32 (Kahan), density held as ρ - ρ₀, positions in
+ * FP64.  The physics per step is that of sph_step with dist = H: ∂ρ∂tDDT!,
+ * ∂v∂t!, ∂v∂t_av!, ∂v∂t_visc! (ν > 0), gravity!, fbmolforce!, ∂v∂tpF! (s > 0),
+ * the half-step predictors, symplectic_update! and cspmcorr! every cspmn
+ * steps (counted from the instance's admission, as within one stepsolve!).  An instance's results do
+ * not depend on which other instances share the ensemble (bit-identical).
+ * Host arrays in ens_add / ens_get are HOST pointers, D-major (x[d*n + i]).
+ * ------------------------------------------------------------------------ */
+typedef struct gcsph_ens gcsph_ens;
+typedef struct {
+  double dx, h, H, rho0, m0, dt, alpha, nu, g, c0, s, delta;
+  double bound_D, bound_l;           /* stage-2 fbmolforce constants (stage 1: 0.4, 2dx) */
+  double grid_min[3], grid_max[3];   /* frozen cell grid; points outside clamp to edge cells */
+  int32_t gamma;
+  int32_t cspmn;                     /* cspmcorr! every cspmn steps since admission (0: never) */
+} gcsph_ens_params;
+
+enum { GCSPH_ENS_X = 0, GCSPH_ENS_V = 1, GCSPH_ENS_RHO = 2, GCSPH_ENS_P = 3, GCSPH_ENS_PTYPE = 4, GCSPH_ENS_DRHO = 5 };
+
+int ens_create(int32_t D, void* stream, gcsph_ens** out);
+void ens_destroy(gcsph_ens* e);
+/* device bytes one particle needs (admission by free HBM) */
+int ens_bytes_per_particle(int32_t D, int64_t* bytes);
+/* admit an instance of n particles; v may be NULL (at rest); returns its slot */
+int ens_add(gcsph_ens* e, int64_t n, const double* x, const double* v, const double* rho, const int32_t* ptype,
+            const gcsph_ens_params* p, int32_t* slot);
+int ens_remove(gcsph_ens* e, int32_t slot);
+/* n steps of every instance (a captured graph per n; the first steps after a
+ * layout change may time three block sizes -- ordinary steps all the same) */
+int ens_step(gcsph_ens* e, int32_t n);
+/* one field of one instance, in its original particle order, as double */
+int ens_get(gcsph_ens* e, int32_t slot, int32_t field, double* out_host);
+int ens_info(gcsph_ens* e, int32_t slot, int64_t* n, int64_t* steps, double* etime);
+int ens_totals(gcsph_ens* e, int32_t* ninst, int64_t* nparticles, int64_t* ncells);
+/* tpb 0 = autotune (128/256/512), graphs 0 = one launch sequence per step */
+int ens_set_tuning(gcsph_ens* e, int32_t tpb, int32_t graphs);
+int ens_get_tuning(gcsph_ens* e, int32_t* tpb, int64_t* captures, int64_t* replays);
+
 #if defined(__GNUC__)
 #pragma GCC visibility pop
 #endif

@@ -1,0 +1,140 @@
+"""Batched FP32 ensemble against the FP64 oracle, and its isolation contract.
+
+Tolerance (the FP32 contract): after 100 steps, relative L2 error in ρ and v
+against the FP64 oracle at most 1e-4; the displacement from the start within
+1e-4 relative L2 as well.  An instance's results are bit-identical alone and
+in a mix, whatever joined or left the ensemble, and whatever launch shape or
+capture mode ran it.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-4
+
+
+def rel_l2(got, want):
+    got = np.asarray(got, dtype=np.float64).ravel()
+    want = np.asarray(want, dtype=np.float64).ravel()
+    n = np.linalg.norm(want)
+    return np.linalg.norm(got - want) / n if n > 0 else np.linalg.norm(got - want)
+
+
+def oracle_run(orc, case, n, nu=0.0, s=0.0):
+    p = orc.default_params(case.dx, case.h, case.H, case.rho0, case.m0, case.dt, case.alpha, case.c0, case.gamma,
+                           case.delta, case.CFL, case.dist, g=case.g, s=s)
+    p.nu = nu
+    ref = orc.OracleSystem(case.x, case.cellsize, case.dist, case.rho, case.ptype, p)
+    ref.stepsolve(n)
+    return ref
+
+
+def errors(ens, slot, ref, case):
+    x = ens.get(slot, "x")
+    return {
+        "rho": rel_l2(ens.get(slot, "rho"), ref.get("rho")),
+        "drho": rel_l2(ens.get(slot, "rho") - case.rho0, ref.get("rho") - case.rho0),
+        "v": rel_l2(ens.get(slot, "v"), ref.get("v")),
+        "disp": rel_l2(x - case.x, ref.get("x") - case.x),
+    }
+
+
+def test_fp32_dam_break_2d_c1_against_fp64(gpu_pkg, orc):
+    """The plain FP64 configuration's dam break (dx = 0.02), 100 steps."""
+    case = gpu_pkg.workloads.dam_break_2d()
+    ens = gpu_pkg.Ensemble(2)
+    slot = ens.add(gpu_pkg.spec_from_case(case))
+    ens.step(100)
+    assert ens.info(slot)["steps"] == 100
+    ref = oracle_run(orc, case, 100)
+    err = errors(ens, slot, ref, case)
+    print("fp32 vs fp64, 2-D dam break dx=0.02, 100 steps:", err)
+    assert err["rho"] <= TOL and err["v"] <= TOL and err["disp"] <= TOL, err
+    assert np.array_equal(ens.get(slot, "ptype"), case.ptype)
+
+
+def test_fp32_3d_viscous_surface_tension_against_fp64(gpu_pkg, orc):
+    """A small 3-D block with ν and surface tension on, 100 steps."""
+    case = gpu_pkg.workloads.dam_break_3d(dx=0.04, fluid=(0.4, 0.6, 0.2), tank=(0.8, 0.8, 0.3),
+                                          full_physics=False)
+    spec = gpu_pkg.spec_from_case(case)
+    spec.nu, spec.s = 0.2, 0.05
+    ens = gpu_pkg.Ensemble(3)
+    slot = ens.add(spec)
+    ens.step(100)
+    ref = oracle_run(orc, case, 100, nu=0.2, s=0.05)
+    err = errors(ens, slot, ref, case)
+    print("fp32 vs fp64, 3-D block, 100 steps:", err)
+    assert err["rho"] <= TOL and err["v"] <= TOL and err["disp"] <= TOL, err
+
+
+def _specs(pkg):
+    w = pkg.workloads
+    a = pkg.spec_from_case(w.dam_break_2d(dx=0.04, fluid=(0.6, 0.8), tank=(1.2, 1.0)))
+    b = pkg.spec_from_case(w.dam_break_2d(dx=0.03, fluid=(0.3, 0.9), tank=(1.0, 1.2)), alpha=0.03, delta=0.15)
+    c = pkg.spec_from_case(w.dam_break_2d(dx=0.05, fluid=(1.0, 0.5), tank=(2.0, 1.0)), dt=2e-5)
+    d = pkg.spec_from_case(w.dam_break_2d(dx=0.025, fluid=(0.5, 0.5), tank=(0.8, 0.8)))
+    return a, b, c, d
+
+
+FIELDS = ("x", "v", "rho", "P", "ptype")
+
+
+def test_same_alone_and_in_the_mix(gpu_pkg):
+    a, b, c, d = _specs(gpu_pkg)
+    alone = gpu_pkg.Ensemble(2)
+    sa = alone.add(a)
+    alone.step(30)
+    alone.step(20)
+    mix = gpu_pkg.Ensemble(2)
+    mix.add(b)
+    sm = mix.add(a)
+    sc = mix.add(c)
+    mix.step(30)
+    mix.remove(sc)          # one leaves ...
+    mix.add(d)              # ... another joins
+    mix.step(20)
+    assert mix.info(sm)["steps"] == 50
+    for f in FIELDS:
+        assert np.array_equal(alone.get(sa, f), mix.get(sm, f)), f
+
+
+def test_late_admission_matches_a_fresh_run(gpu_pkg):
+    a, b, c, _ = _specs(gpu_pkg)
+    fresh = gpu_pkg.Ensemble(2)
+    sf = fresh.add(c)
+    fresh.step(25)
+    busy = gpu_pkg.Ensemble(2)
+    busy.add(a)
+    busy.add(b)
+    busy.step(40)
+    sl = busy.add(c)
+    busy.step(25)
+    assert busy.info(sl)["steps"] == 25
+    for f in FIELDS:
+        assert np.array_equal(fresh.get(sf, f), busy.get(sl, f)), f
+
+
+@pytest.mark.parametrize("tpb,graphs", [(128, True), (512, False), (0, True)])
+def test_launch_shape_and_capture_do_not_change_results(gpu_pkg, tpb, graphs):
+    a, b, _, _ = _specs(gpu_pkg)
+    ref = gpu_pkg.Ensemble(2)
+    ref.set_tuning(256, False)
+    r1, r2 = ref.add(a), ref.add(b)
+    ref.step(12)
+    ens = gpu_pkg.Ensemble(2)
+    ens.set_tuning(tpb, graphs)
+    e1, e2 = ens.add(a), ens.add(b)
+    ens.step(5)
+    ens.step(7)
+    for f in FIELDS:
+        assert np.array_equal(ref.get(r1, f), ens.get(e1, f)), f
+        assert np.array_equal(ref.get(r2, f), ens.get(e2, f)), f
+    t = ens.tuning()
+    if graphs:
+        assert t["replays"] >= 1
+    if tpb:
+        assert t["tpb"] == tpb
+    else:
+        assert t["tpb"] in (128, 256, 512)
