@@ -38,6 +38,12 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--no-batched", action="store_true", help="skip the batched FP32 ensemble measurement")
+    ap.add_argument("--batched-instances", type=int, default=256)
+    ap.add_argument("--batched-steps", type=int, default=300, help="timed steps of the ensemble")
+    ap.add_argument("--no-serving", action="store_true", help="skip the serving-loop measurement")
+    ap.add_argument("--serving-requests", type=int, default=40)
+    ap.add_argument("--serving-horizon-scale", type=float, default=0.01)
     return ap.parse_args()
 
 
@@ -162,6 +168,157 @@ def run_reference(args):
            "e2e": {"value": value, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out))
     return 0
+
+
+def rel_l2(a, b):
+    import numpy as np
+    a = np.asarray(a, dtype=np.float64).ravel()
+    b = np.asarray(b, dtype=np.float64).ravel()
+    n = np.linalg.norm(b)
+    return float(np.linalg.norm(a - b) / n) if n > 0 else float(np.linalg.norm(a - b))
+
+
+def plain_fp64_rate(g, cases, steps=30):
+    """particle-steps/s of the FP64 drop-in path (stepsolve!, captured calls)
+    on each case alone, summed over the sample."""
+    import torch
+    tot_ps, tot_s = 0, 0.0
+    for case in cases:
+        system = g.GPUCellList(tuple(case.x), case.cellsize, case.dist)
+        prob = g.SPHProblem(system, case.dx, case.h, case.H, g.WendlandC2(dim=case.D), case.rho, case.ptype,
+                            case.rho0, case.m0, case.dt, case.alpha, case.c0, case.gamma, case.delta, case.CFL)
+        prob.stepsolve(steps)  # sizes the buffers (first call runs per step)
+        prob.stepsolve(steps)  # captures
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        prob.stepsolve(steps)
+        torch.cuda.synchronize()
+        tot_s += time.perf_counter() - t0
+        tot_ps += case.N * steps
+        prob.close()
+        del system
+    return tot_ps / tot_s
+
+
+def fp32_error_vs_fp64(g, case, alpha, delta, steps=100):
+    """Relative L2 error of the FP32 ensemble against the FP64 drop-in path
+    (itself bit-identical / within 1e-12 of the reference algorithm) after
+    `steps` steps of one instance."""
+    spec = g.spec_from_case(case, alpha=alpha, delta=delta)
+    ens = g.Ensemble(case.D)
+    slot = ens.add(spec)
+    ens.step(steps)
+    system = g.GPUCellList(tuple(case.x), case.cellsize, case.dist)
+    prob = g.SPHProblem(system, case.dx, case.h, case.H, g.WendlandC2(dim=case.D), case.rho, case.ptype,
+                        case.rho0, case.m0, case.dt, alpha, case.c0, case.gamma, delta, case.CFL)
+    prob.stepsolve(steps)
+    import torch
+    x64 = torch.stack(system.points).cpu().numpy()
+    out = {"rho": rel_l2(ens.get(slot, "rho"), prob.rho.cpu().numpy()),
+           "rho_minus_rho0": rel_l2(ens.get(slot, "rho") - case.rho0, prob.rho.cpu().numpy() - case.rho0),
+           "v": rel_l2(ens.get(slot, "v"), torch.stack(prob.v).cpu().numpy()),
+           "displacement": rel_l2(ens.get(slot, "x") - case.x, x64 - case.x),
+           "steps": steps, "particles": case.N}
+    ens.close()
+    prob.close()
+    return out
+
+
+def run_batched(g, args, plain_c1):
+    """The batched-ensemble workload: 256 independent 2-D dam breaks
+    (fluid-column counts log-uniform 2k-200k, aspect 0.5-4, dx 0.005-0.02,
+    α 0.005-0.05, δ 0.05-0.2), FP32, all advanced together."""
+    import torch
+    wl = g.workloads.ensemble_2d(args.batched_instances)
+    ens = g.Ensemble(2)
+    t0 = time.perf_counter()
+    for case, al, de in wl:
+        ens.add(g.spec_from_case(case, alpha=al, delta=de))
+    t_admit = time.perf_counter() - t0
+    tot = ens.totals()
+    ens.step(10)  # tuning (three block sizes) + warm-up
+    ens.step(args.batched_steps)  # captures the graph of this many steps
+    torch.cuda.synchronize()
+    L = g.load_library()
+    L.gcsph_timing_enable(0)
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    ens.step(args.batched_steps)
+    b.record()
+    torch.cuda.synchronize()
+    ms = a.elapsed_time(b)
+    value = tot["particles"] * args.batched_steps / (ms / 1e3)
+    # instrumented pass for the per-kernel split
+    L.gcsph_timing_enable(1)
+    L.gcsph_timing_reset()
+    ens.step(20)
+    import ctypes as C
+    fam = {}
+    for tid in range(L.gcsph_timing_count()):
+        n_ = C.c_int64(); t_ = C.c_double()
+        L.gcsph_timing_get(tid, C.byref(n_), C.byref(t_))
+        if n_.value:
+            fam[L.gcsph_timing_name(tid).decode()] = {"launches": int(n_.value), "total_ms": float(t_.value)}
+    L.gcsph_timing_enable(0)
+    tuning = ens.tuning()
+    ens.close()
+    sizes = sorted(wl, key=lambda t: t[0].N)
+    sample = [sizes[0][0], sizes[len(sizes) // 2][0], sizes[-1][0]]
+    plain = plain_fp64_rate(g, sample)
+    small = sizes[0]
+    err = fp32_error_vs_fp64(g, small[0], small[1], small[2])
+    return {"workload": "256 independent 2-D dam breaks, fluid counts log-uniform 2k-200k, aspect 0.5-4, "
+                        "dx 0.005-0.02, alpha 0.005-0.05, delta 0.05-0.2 (seeded), FP32 pair arithmetic, "
+                        "FP64 positions",
+            "instances": tot["instances"], "particles": tot["particles"], "cells": tot["cells"],
+            "value": value, "unit": "particle-steps/s", "timed_steps": args.batched_steps,
+            "ms_per_step": ms / args.batched_steps, "admission_s": t_admit, "tuning": tuning,
+            "kernel_ms_20_steps": fam,
+            "plain_fp64_same_instances": {"value": plain, "unit": "particle-steps/s",
+                                          "sample": "smallest, median and largest instance, each alone, 30 steps"},
+            "ratio_vs_plain_fp64_same_instances": value / plain,
+            "ratio_vs_plain_fp64_c1": value / plain_c1,
+            "error_vs_fp64": err}
+
+
+def run_serving(g, args):
+    """The serving workload: Poisson arrivals (mean 20 req/s) of dam-break
+    solves, 70% 2-D / 30% 3-D, particle counts log-uniform 5k-2M, horizons
+    uniform 0.05-0.5 s scaled by --serving-horizon-scale, FP32 ensembles."""
+    import numpy as np
+    S = g.serving
+    raw = g.workloads.serving_requests(args.serving_requests, horizon_scale=args.serving_horizon_scale)
+    reqs = [S.Request(i, t, g.spec_from_case(c), n) for i, (t, c, n) in enumerate(raw)]
+    loop = S.ServingLoop(chunk=64)
+    stats = loop.run(reqs)
+    loop.close()
+    # the same solves run alone, one after another, on the plain FP64 path:
+    # each one's time from its size class's measured FP64 rate
+    by_d = {2: [c for _, c, _ in raw if c.D == 2], 3: [c for _, c, _ in raw if c.D == 3]}
+    rates = {}
+    for D, cs in by_d.items():
+        if cs:
+            cs = sorted(cs, key=lambda c: c.N)
+            rates[D] = plain_fp64_rate(g, [cs[len(cs) // 2]], steps=20)
+    alone = np.array([c.N * n / rates[c.D] for _, c, n in raw])
+    # sequential service in arrival order
+    t, lat = 0.0, []
+    for (arr, c, n), a in zip(raw, alone):
+        t = max(t, arr) + a
+        lat.append(t - arr)
+    lat = np.array(lat)
+    tot_ps = sum(c.N * n for _, c, n in raw)
+    stats.update({
+        "workload": f"{len(raw)} requests, Poisson 20 req/s, 70% 2-D / 30% 3-D, particle counts log-uniform "
+                    f"5k-2M, horizons uniform 0.05-0.5 s x {args.serving_horizon_scale} (dt 1e-5)",
+        "plain_fp64_alone": {"p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
+                             "particle_steps_per_s": tot_ps / alone.sum(),
+                             "how": "each solve alone, in arrival order, at the FP64 path's measured rate for "
+                                    "its dimension (median-size request of that dimension, 20 steps)"},
+    })
+    stats["throughput_ratio_vs_plain_fp64"] = stats["particle_steps_per_s"] / stats["plain_fp64_alone"][
+        "particle_steps_per_s"]
+    return stats
 
 
 def run_gb300(args):
@@ -314,6 +471,16 @@ def run_gb300(args):
            "kernel_ms": {k: {"launches": v[0], "total_ms": v[1]} for k, v in fam.items() if v[0]},
            "kernel_timing": "library event timers over a second, instrumented pass of the same K bench steps",
            "graphs": dict(zip(("captured", "replayed"), prob.graph_stats()))}
+    if not args.no_batched:
+        try:
+            out["batched_fp32"] = run_batched(g, args, value / ws)
+        except Exception as e:  # noqa: BLE001
+            out["batched_fp32"] = {"error": repr(e)}
+    if not args.no_serving:
+        try:
+            out["serving"] = run_serving(g, args)
+        except Exception as e:  # noqa: BLE001
+            out["serving"] = {"error": repr(e)}
     print(json.dumps(out))
     if ws > 1:
         import torch.distributed as dist

@@ -488,6 +488,8 @@ using namespace gcsph;
 struct EnsHostInst {
   int32_t slot;
   int64_t n, p_off;
+  int64_t filled_off = -1;  // p_off the per-particle instance index was last written for
+  int64_t filled_idx = -1;
   int64_t key_off, ncell;
   gcsph_ens_params prm;
   int64_t steps;
@@ -605,6 +607,7 @@ int ens_reserve(gcsph_ens* e, int64_t n) {
   DevBuf* i32[] = {&e->INST, &e->KEY, &e->SLOT, &e->TMP, &e->PERM, &e->SKEY};
   for (DevBuf* b : i32)
     if ((rc = b->ensure(sizeof(int32_t) * want, e->st))) return rc;
+  for (EnsHostInst& h : e->inst) h.filled_off = -1;  // the instance index buffer was reallocated
   for (int d = 0; d < e->D; ++d) {
     if ((rc = e->OFF[d].ensure(sizeof(float) * want, e->st))) return rc;
     if ((rc = e->OFFH[d].ensure(sizeof(float) * want, e->st))) return rc;
@@ -658,10 +661,12 @@ int ens_relayout(gcsph_ens* e) {
     GC_CUDA(cudaMemcpyAsync(e->ISTEP.p, isteps.data(), sizeof(int32_t) * isteps.size(), cudaMemcpyHostToDevice,
                             e->st));
   for (size_t s = 0; s < e->inst.size(); ++s) {
-    const EnsHostInst& h = e->inst[s];
-    if (h.n == 0) continue;
+    EnsHostInst& h = e->inst[s];
+    if (h.n == 0 || (h.filled_off == h.p_off && h.filled_idx == (int64_t)s)) continue;
     k_fill_i32<<<nblocks(h.n, 256), 256, 0, e->st>>>(e->INST.as<int32_t>() + h.p_off, h.n, (int32_t)s);
     GC_LAUNCHED();
+    h.filled_off = h.p_off;
+    h.filled_idx = (int64_t)s;
   }
   GC_CUDA(cudaStreamSynchronize(e->st));
   e->gen += 1;

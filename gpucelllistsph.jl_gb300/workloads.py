@@ -155,3 +155,73 @@ def load_fixture(path: str) -> Case:
                 cellsize=(H, H), rho0=rho0, m0=rho0 * dx * dx, dt=1e-5, alpha=0.01, c0=math.sqrt(g * 2) * 20,
                 gamma=7, delta=0.1, CFL=0.2, g=g)
 
+
+
+def _log_uniform(rng, lo, hi):
+    return float(math.exp(rng.uniform(math.log(lo), math.log(hi))))
+
+
+def sized_dam_break_2d(n_fluid: int, aspect: float, dx: float) -> Case:
+    """A 2-D dam break whose fluid column holds about n_fluid particles with
+    height/width = aspect, in a tank 4x the column's width and 1.5x its
+    height (the proportions of the 1.0x2.0 column in the 4.0x3.0 tank).
+    c₀ = 10 sqrt(2 g max(height, 4 m)), the reference example's 20 sqrt(2g)
+    for columns up to 4 m."""
+    nx = max(2, int(round(math.sqrt(n_fluid / aspect))))
+    ny = max(2, int(round(n_fluid / nx)))
+    W, Hc = nx * dx, ny * dx
+    c = dam_break_2d(dx=dx, fluid=(W, Hc), tank=(4.0 * W, 1.5 * Hc))
+    c.c0 = 10.0 * math.sqrt(2.0 * c.g * max(Hc, 4.0))
+    return c
+
+
+def sized_dam_break_3d(n_fluid: int, aspect: float, dx: float) -> Case:
+    """A 3-D dam break (component 2 vertical) whose fluid block holds about
+    n_fluid particles, block (L, aspect L, L/2), tank (4L, 1.5 aspect L, L)."""
+    L = dx * (n_fluid / (0.5 * aspect)) ** (1.0 / 3.0)
+    L = max(L, 3 * dx)
+    block = (L, aspect * L, 0.5 * L)
+    c = dam_break_3d(dx=dx, fluid=block, tank=(4.0 * L, 1.5 * aspect * L, L), full_physics=False)
+    c.c0 = 10.0 * math.sqrt(2.0 * c.g * max(block[1], 4.0))
+    return c
+
+
+def ensemble_2d(count: int = 256, seed: int = SEED, n_range=(2_000, 200_000), aspect=(0.5, 4.0),
+                dx_range=(0.005, 0.02), alpha=(0.005, 0.05), delta=(0.05, 0.2)):
+    """The batched-ensemble workload: `count` independent 2-D dam breaks,
+    fluid-column particle counts log-uniform in n_range, column aspect
+    uniform, dx log-uniform, α and δ uniform -- numpy PCG64(seed).  Returns
+    a list of (Case, α, δ)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    out = []
+    for _ in range(count):
+        n = _log_uniform(rng, *n_range)
+        a = float(rng.uniform(*aspect))
+        dx = _log_uniform(rng, *dx_range)
+        al = float(rng.uniform(*alpha))
+        de = float(rng.uniform(*delta))
+        out.append((sized_dam_break_2d(int(n), a, dx), al, de))
+    return out
+
+
+def serving_requests(count: int, seed: int = SEED, rate: float = 20.0, frac_2d: float = 0.7,
+                     n_range=(5_000, 2_000_000), horizon=(0.05, 0.5), horizon_scale: float = 1.0,
+                     aspect=(0.5, 4.0), dx_range=(0.005, 0.02)):
+    """The serving workload: a Poisson stream (mean `rate` requests/s) of
+    dam-break solves, frac_2d of them 2-D, particle counts log-uniform in
+    n_range, physical horizons uniform in `horizon` seconds (times
+    horizon_scale) at Δt = 1e-5.  Returns [(arrival_s, Case, steps)]."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    t = 0.0
+    out = []
+    for _ in range(count):
+        t += float(rng.exponential(1.0 / rate))
+        n = int(_log_uniform(rng, *n_range))
+        a = float(rng.uniform(*aspect))
+        dx = _log_uniform(rng, *dx_range)
+        two = bool(rng.uniform() < frac_2d)
+        hz = float(rng.uniform(*horizon)) * horizon_scale
+        case = sized_dam_break_2d(n, a, dx) if two else sized_dam_break_3d(n, a, dx)
+        steps = max(1, int(round(hz / case.dt)))
+        out.append((t, case, steps))
+    return out

@@ -1,0 +1,93 @@
+"""Host logic of the serving loop (admission, memory gating, exact horizons,
+latency bookkeeping) against a fake ensemble -- no GPU."""
+import numpy as np
+
+
+class FakeEnsemble:
+    log = []
+
+    def __init__(self, D):
+        self.D = D
+        self.slots = {}
+        self.next = 0
+
+    def add(self, spec):
+        s = self.next
+        self.next += 1
+        self.slots[s] = [spec, 0]
+        FakeEnsemble.log.append(("add", self.D, spec.n))
+        return s
+
+    def remove(self, slot):
+        FakeEnsemble.log.append(("remove", self.D, self.slots[slot][0].n, self.slots[slot][1]))
+        del self.slots[slot]
+
+    def step(self, k):
+        for v in self.slots.values():
+            v[1] += k
+
+    def get(self, slot, f):
+        return np.full(3, float(self.slots[slot][1]))
+
+    def close(self):
+        pass
+
+
+class Spec:
+    def __init__(self, D, n):
+        self.D, self.n = D, n
+
+
+def _loop(pkg, **kw):
+    FakeEnsemble.log = []
+    return pkg.serving.ServingLoop(ensemble_factory=FakeEnsemble, bytes_per_particle=lambda D: 100, **kw)
+
+
+def test_every_request_reaches_exactly_its_horizon(pkg):
+    S = pkg.serving
+    reqs = [S.Request(i, 0.0, Spec(2 if i % 3 else 3, 1000 + i), steps) for i, steps in
+            enumerate([5, 130, 64, 1, 77, 200])]
+    loop = _loop(pkg, chunk=64, free_bytes=lambda: 10 ** 12)
+    stats = loop.run(reqs)
+    assert stats["completed"] == len(reqs)
+    removed = {(n, steps) for (tag, D, n, *rest) in FakeEnsemble.log if tag == "remove" for steps in rest}
+    assert removed == {(r.spec.n, r.steps) for r in reqs}
+    for r in reqs:
+        assert r.result["x"][0] == r.steps
+        assert r.latency is not None and r.latency >= 0
+    assert stats["particle_steps"] == sum(r.spec.n * r.steps for r in reqs)
+    assert stats["p50_s"] is not None and stats["p99_s"] >= stats["p50_s"]
+
+
+def test_admission_waits_for_memory(pkg):
+    """Only one request fits at a time: the second is admitted only after the
+    first has left, never alongside it."""
+    S = pkg.serving
+    reqs = [S.Request(0, 0.0, Spec(2, 1000), 10), S.Request(1, 0.0, Spec(2, 1000), 10)]
+    def live():
+        return (sum(1 for t in FakeEnsemble.log if t[0] == "add")
+                - sum(1 for t in FakeEnsemble.log if t[0] == "remove"))
+
+    # 1000 particles x 100 B x 2 = 2e5 B per request; 3e5 B free when idle
+    loop = _loop(pkg, chunk=4, free_bytes=lambda: 3 * 10 ** 5 - live() * 2 * 10 ** 5, reserve=0.0)
+    loop.run(reqs)
+    tags = [t[0] for t in FakeEnsemble.log]
+    assert tags == ["add", "remove", "add", "remove"], tags
+
+
+def test_arrivals_in_the_future_are_waited_for(pkg):
+    S = pkg.serving
+    reqs = [S.Request(0, 0.05, Spec(2, 10), 3)]
+    loop = _loop(pkg, free_bytes=lambda: 10 ** 12)
+    stats = loop.run(reqs)
+    assert reqs[0].admitted >= 0.05
+    assert stats["completed"] == 1
+
+
+def test_a_request_that_can_never_fit_is_refused(pkg):
+    import pytest
+    S = pkg.serving
+    reqs = [S.Request(0, 0.0, Spec(2, 10 ** 6), 3)]
+    loop = _loop(pkg, free_bytes=lambda: 10 ** 6)
+    with pytest.raises(RuntimeError):
+        loop.run(reqs)
