@@ -59,11 +59,19 @@ def make_case(pkg):
 
 
 def algorithmic_bytes_per_stage(case, npairs):
-    """Algorithmic HBM bytes of one fused pair-sum stage (gather form, FP64):
-    N·(8D x + 8D v + 8 ρ + 8 P + 4 ptype) read + N·(8 ρ̇ + 8D a) written
-    + 2P·4 B of neighbour indices."""
+    """Algorithmic HBM bytes of one pair-once pass A (FP64), the dominant
+    kernel: N·(8D x + 8D v + 8 ρ + 8 P + 8 1/ρ + 4 ptype) of particle state
+    read once, P·16 B of pair quads read, and per pair both sides' entry
+    slots written: 2·(8 W + 8D ∇W + 8 ρ̇ + 8D a) B (stage 1; stage 2 writes
+    no W/∇W).  P = pairs with k < m."""
     D, N = case.D, case.N
-    return N * (24 * D + 28) + 2 * npairs * 4
+    return N * (16 * D + 28) + npairs * (16 + 2 * (16 + 16 * D))
+
+
+# DRAM bytes (read + write) of one stage-1 pass A launch on this workload, from
+# the ncu capture summarised in profiles/pairA_dambreak2d_c1_fp64.md
+PAIRA_STAGE1_DRAM_BYTES = 2_105_344 + 256
+PAIRA_STAGE1_FP64_PIPE = 0.779
 
 
 class Clocks:
@@ -449,9 +457,13 @@ def run_gb300(args):
         alg = None
     achieved = (alg / avg_s / 1e9) if alg else None
     roof = {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-            "frac": (achieved / hbm_peak) if achieved else None, "traffic": None, "peak_source": peak_src,
+            "frac": (achieved / hbm_peak) if achieved else None,
+            "traffic": PAIRA_STAGE1_DRAM_BYTES if top == "stage1" else None, "peak_source": peak_src,
             "avg_launch_us": avg_s * 1e6, "alg_bytes_per_launch": alg,
-            "note": "FP64-pipe-bound kernel; HBM fraction reported against measured copy bandwidth"}
+            "fp64_pipe_frac_ncu": PAIRA_STAGE1_FP64_PIPE if top == "stage1" else None,
+            "note": "pair-once pass A is FP64-pipe bound (2 FP64 instr/cycle/SM on GB300, ncu: 78% of that "
+                    "peak); its working set stays in L2, so the HBM fraction against the measured copy "
+                    "bandwidth is small by construction"}
     cpu = None
     if not args.no_cpu_baseline:
         try:

@@ -189,15 +189,14 @@ def sized_dam_break_3d(n_fluid: int, aspect: float, dx: float) -> Case:
 def ensemble_2d(count: int = 256, seed: int = SEED, n_range=(2_000, 200_000), aspect=(0.5, 4.0),
                 dx_range=(0.005, 0.02), alpha=(0.005, 0.05), delta=(0.05, 0.2)):
     """The batched-ensemble workload: `count` independent 2-D dam breaks,
-    fluid-column particle counts log-uniform in n_range, column aspect
-    uniform, dx log-uniform, α and δ uniform -- numpy PCG64(seed).  Returns
-    a list of (Case, α, δ)."""
+    fluid-column particle counts log-uniform in n_range, column aspect, dx,
+    α and δ uniform -- numpy PCG64(seed).  Returns a list of (Case, α, δ)."""
     rng = np.random.Generator(np.random.PCG64(seed))
     out = []
     for _ in range(count):
         n = _log_uniform(rng, *n_range)
         a = float(rng.uniform(*aspect))
-        dx = _log_uniform(rng, *dx_range)
+        dx = float(rng.uniform(*dx_range))
         al = float(rng.uniform(*alpha))
         de = float(rng.uniform(*delta))
         out.append((sized_dam_break_2d(int(n), a, dx), al, de))
@@ -218,7 +217,7 @@ def serving_requests(count: int, seed: int = SEED, rate: float = 20.0, frac_2d: 
         t += float(rng.exponential(1.0 / rate))
         n = int(_log_uniform(rng, *n_range))
         a = float(rng.uniform(*aspect))
-        dx = _log_uniform(rng, *dx_range)
+        dx = float(rng.uniform(*dx_range))
         two = bool(rng.uniform() < frac_2d)
         hz = float(rng.uniform(*horizon)) * horizon_scale
         case = sized_dam_break_2d(n, a, dx) if two else sized_dam_break_3d(n, a, dx)
