@@ -238,10 +238,14 @@ def timesolve(prob: SPHProblem, batch: int = 10, timeframe: float = 1.0, writeti
               timelims=None, anim: bool = False, verbose: bool = True, callback=None):
     """timesolve!(prob; batch, timeframe, ...) -- src/sphproblem.jl:420-511.
 
-    Runs stepsolve(prob, batch) while etime <= timeframe.  Output writing is
-    delegated to `callback(prob, frame_index)` every `writetime` of simulated
-    time (VTK/animation writers are not part of this library); `anim` is not
-    supported (no graphics stack)."""
+    Runs stepsolve(prob, batch) while etime <= timeframe.  With `path` and
+    writetime > 0 it writes OUTPUT_<i>.vtp frames of `vtkvars` every
+    `writetime` of simulated time (and OUTPUT_PVC.pvd with pvc=True), as the
+    reference does; the frames are copied into pinned host memory after the
+    batch that produced them and written by a background thread while the
+    next batches run.  `callback(prob, i)` is called at the same moments.
+    `anim` is not supported (no graphics stack)."""
+    from . import vtkio
     lim = prob.CFL * prob.H / (3 * prob.c0)
     if timelims is None:
         timelims = (math.sqrt(_EPS), lim)
@@ -250,7 +254,7 @@ def timesolve(prob: SPHProblem, batch: int = 10, timeframe: float = 1.0, writeti
     if timestepping:
         timelims = (max(timelims[0], _EPS), min(timelims[1], lim))
     if anim:
-        raise NotImplementedError("animation needs a graphics stack; write frames through `callback`")
+        raise NotImplementedError("animation needs a graphics stack; write frames with `path` or `callback`")
     if verbose:
         print("    Start simulation...")
         print(f"Timestepping: {timestepping}")
@@ -260,17 +264,28 @@ def timesolve(prob: SPHProblem, batch: int = 10, timeframe: float = 1.0, writeti
         print(f"NUI: {prob.nui}")
     nt = prob.etime + writetime
     i = 0
-    if writetime > 0 and callback is not None:
-        callback(prob, i)
+    writer = vtkio.AsyncWriter(path, pvc=pvc) if (writetime > 0 and path is not None) else None
+
+    def frame(k):
+        if writer is not None:
+            writer.submit(f"OUTPUT_{k:05d}", vtkio.Snapshot(prob, vtkvars))
+        if callback is not None:
+            callback(prob, k)
+
+    if writetime > 0:
+        frame(i)
     diag = (0, 0.0)
     t0 = time.perf_counter()
-    while prob.etime <= timeframe:
-        diag = prob.stepsolve(batch, timestepping=timestepping, timelims=timelims)
-        if writetime > 0 and nt < prob.etime:
-            nt += writetime
-            if callback is not None:
-                callback(prob, i)
-        i += 1
+    try:
+        while prob.etime <= timeframe:
+            diag = prob.stepsolve(batch, timestepping=timestepping, timelims=timelims)
+            if writetime > 0 and nt < prob.etime:
+                nt += writetime
+                frame(i)
+            i += 1
+    finally:
+        if writer is not None:
+            writer.close()
     if verbose:
         print(f"iter: {i}, time: {prob.etime}, Δt: {prob.dt}, updn: {diag[0]}, dxpncu: {diag[1]}, "
               f"wall: {time.perf_counter() - t0:.3f}s")
