@@ -44,6 +44,10 @@ def parse():
     ap.add_argument("--no-serving", action="store_true", help="skip the serving-loop measurement")
     ap.add_argument("--serving-requests", type=int, default=40)
     ap.add_argument("--serving-horizon-scale", type=float, default=0.01)
+    ap.add_argument("--c3", action="store_true",
+                    help="instead: 3-D dam break at scale, FP32 ensemble against the FP64 drop-in (one JSON line)")
+    ap.add_argument("--c3-steps", type=int, default=500)
+    ap.add_argument("--c3-dx", type=float, default=0.01)
     return ap.parse_args()
 
 
@@ -329,6 +333,62 @@ def run_serving(g, args):
     return stats
 
 
+def run_c3(args):
+    """3-D dam break at scale: fluid block 1.0 x 2.0 (vertical) x 0.5 m at
+    dx = 0.01 (1.0 M fluid) in a 4.0 x 3.0 x 1.0 m tank with 3 boundary
+    layers, h = √3 dx, full physics (ν = 0.2, s = 0.05, DPC l₀ = 0.005,
+    λ = 0.005, pmax = 36000, XSPH ε = 0.5, CSPM every 15 steps).  The FP32
+    ensemble and the FP64 drop-in each advance it `--c3-steps` steps; the
+    per-field relative L2 error of FP32 against FP64 and both rates."""
+    import torch
+    torch.cuda.set_device(0)
+    import __graft_entry__ as ge
+    g = ge.load_package()
+    case = g.workloads.dam_break_3d(dx=args.c3_dx)
+    n = args.c3_steps
+    N = case.N
+    # FP32 ensemble
+    ens = g.Ensemble(3)
+    slot = ens.add(g.spec_from_case(case))
+    ens.step(10)
+    torch.cuda.synchronize()
+    # a fresh instance for the measured run, so both start from the same state
+    ens.remove(slot)
+    slot = ens.add(g.spec_from_case(case))
+    t0 = time.perf_counter()
+    ens.step(n)
+    torch.cuda.synchronize()
+    t32 = time.perf_counter() - t0
+    f32 = {f: ens.get(slot, f) for f in ("x", "v", "rho")}
+    tuning = ens.tuning()
+    ens.close()
+    # FP64 drop-in
+    system = g.GPUCellList(tuple(case.x), case.cellsize, case.dist)
+    prob = g.SPHProblem(system, case.dx, case.h, case.H, g.WendlandC2(dim=3), case.rho, case.ptype, case.rho0,
+                        case.m0, case.dt, case.alpha, case.c0, case.gamma, case.delta, case.CFL, g=case.g, s=case.s)
+    for k, val in case.extra.items():
+        setattr(prob, k, val)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    prob.stepsolve(n)
+    torch.cuda.synchronize()
+    t64 = time.perf_counter() - t0
+    x64 = torch.stack(system.points).cpu().numpy()
+    v64 = torch.stack(prob.v).cpu().numpy()
+    r64 = prob.rho.cpu().numpy()
+    err = {"rho": rel_l2(f32["rho"], r64), "rho_minus_rho0": rel_l2(f32["rho"] - case.rho0, r64 - case.rho0),
+           "v": rel_l2(f32["v"], v64), "displacement": rel_l2(f32["x"] - case.x, x64 - case.x),
+           "x": rel_l2(f32["x"], x64)}
+    out = {"metric": "particle-steps/s", "workload": "3-D dam break at scale, full physics, FP32 ensemble vs "
+                                                     "FP64 drop-in", "particles": N,
+           "fluid": int((case.ptype == 2).sum()), "steps": n, "dx": args.c3_dx,
+           "fp32": {"value": N * n / t32, "seconds": t32, "tuning": tuning},
+           "fp64": {"value": N * n / t64, "seconds": t64},
+           "ratio_fp32_vs_fp64": t64 / t32, "fp32_error_vs_fp64": err}
+    print(json.dumps(out))
+    return 0
+
+
 def run_gb300(args):
     import torch
     ws, rank, local = dist_env()
@@ -502,6 +562,8 @@ def run_gb300(args):
 
 def main():
     args = parse()
+    if args.c3:
+        return run_c3(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_gb300(args)

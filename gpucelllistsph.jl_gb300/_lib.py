@@ -39,7 +39,9 @@ class gcsph_ens_params(C.Structure):
     """Mirror of gcsph_ens_params (one ensemble instance)."""
     _fields_ = [(n, C.c_double) for n in (
         "dx", "h", "H", "rho0", "m0", "dt", "alpha", "nu", "g", "c0", "s", "delta", "bound_D", "bound_l")] + [
-        ("grid_min", C.c_double * 3), ("grid_max", C.c_double * 3), ("gamma", C.c_int32), ("cspmn", C.c_int32)]
+        ("grid_min", C.c_double * 3), ("grid_max", C.c_double * 3)] + [
+        (n, C.c_double) for n in ("dpc_l0", "dpc_pmin", "dpc_pmax", "dpc_lambda", "xsph_eps")] + [
+        ("gamma", C.c_int32), ("cspmn", C.c_int32)]
 
 
 ENS_FIELDS = {"x": 0, "v": 1, "rho": 2, "P": 3, "ptype": 4, "drho": 5}

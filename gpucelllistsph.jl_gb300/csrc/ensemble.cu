@@ -44,9 +44,12 @@ struct EnsInst {
   int gamma;
   int use_visc, use_pF;
   int cspmn;
+  int use_dpc, use_xsph;
   float csf, H2, h, Hinv, nW, nDW, m0, rho0, c0, P0, alpha, DDTkh, DDTgz, eta2, g, nu, s, twoh, pfc, hp1;
   float fb_d[2], fb_r0[2], fb_eta2[2];  // fbmolforce constants of stage 1 and stage 2
   float pc[4];                           // (1+ε)^(1/γ) - 1 series coefficients
+  float dpc_l0inv, dpc_nW, dpc_whinv, dpc_kernlim, dpc_eta2, dpc_pmin, dpc_pmax, dpc_lambda;
+  float xsph_c;                          // 2 m0 ε
 };
 
 struct EnsArr {
@@ -61,8 +64,11 @@ struct EnsArr {
   const int32_t* pt;
   float* off[3];             // x - cell corner (FP32)
   float* offh[3];            // half-step positions - cell corner
-  float* vh[3];
+  float* vh[3];               // also the dpcreg! sums, after the corrector
   float* drh;
+  float* offn[3];            // x - cell corner after the corrector (dpcreg!)
+  float* dxb[3];             // xΔt½ base - x: dpcreg!/xsphcorr! move x, not xΔt½
+  float* dvb[3];             // vΔt½ base - v: dpcreg! moves v, not vΔt½
 };
 
 struct KSum {
@@ -158,6 +164,8 @@ __global__ void k_ens_rank(int64_t N, const int32_t* __restrict__ tmp, const int
 struct EnsState {
   double* x[3];
   float* v[3];
+  float* dxb[3];
+  float* dvb[3];
   float* dr;
   float* drb;
   int32_t* pt;
@@ -183,6 +191,8 @@ __global__ void k_ens_permute(int64_t N, const int32_t* __restrict__ perm, const
     const double xv = in.x[d][i];
     out.x[d][k] = xv;
     out.v[d][k] = in.v[d][i];
+    out.dxb[d][k] = in.dxb[d][i];
+    out.dvb[d][k] = in.dvb[d][i];
     const int cd = d == 0 ? c0 : (d == 1 ? c1 : c2);
     float* o = d == 0 ? o0 : (d == 1 ? o1 : o2);
     o[k] = (float)(xv - (I.origin[d] + (double)cd * I.cs));
@@ -323,10 +333,10 @@ __global__ void __launch_bounds__(ENS_MAX_TPB) k_ens_stage(EnsArr A, const EnsIn
       A.drh[i] = drh;
 #pragma unroll
       for (int q = 0; q < D; ++q) {
-        float vh = vi[q];
+        float vh = vi[q] + A.dvb[q][i];
         if (pti > 1) vh = vh + a[q] * hdt;
         A.vh[q][i] = vh;
-        A.offh[q][i] = oi[q] + vh * hdt;
+        A.offh[q][i] = (oi[q] + A.dxb[q][i]) + vh * hdt;
       }
     } else {
       // symplectic_update!: δρ_new = δρ - ρ 2ε/(2+ε), positions in FP64
@@ -341,8 +351,168 @@ __global__ void __launch_bounds__(ENS_MAX_TPB) k_ens_stage(EnsArr A, const EnsIn
         const float v0 = A.v[q][i];
         const float nv = pti > 1 ? v0 + a[q] * dt : v0;
         A.v[q][i] = nv;
-        A.x[q][i] = A.x[q][i] + ((double)v0 + (double)nv) * 0.5 * I.dt;
+        const double ddx = ((double)v0 + (double)nv) * 0.5 * I.dt;
+        A.x[q][i] = A.x[q][i] + ddx;
+        A.offn[q][i] = oi[q] + (float)ddx;
+        A.dxb[q][i] = 0.f;
+        A.dvb[q][i] = 0.f;
       }
+    }
+  }
+}
+
+// dpcreg! (src/gpukernels_sph.jl:1500-1553) at the corrected state: pairs of
+// the step (at x), terms at x_{n+1}, v_{n+1}, ρ_{n+1} and P(ρ_{n+1}); the sums
+// go to the vΔt½ buffer (free after the corrector) and k_ens_dpc_apply runs
+// update_dpcreg! (:1617-1632)
+template <int D>
+__global__ void __launch_bounds__(ENS_MAX_TPB) k_ens_dpc(EnsArr A, const EnsInst* __restrict__ T) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < A.N; i += stride) {
+    const EnsInst& I = T[A.inst[i]];
+    if (!I.use_dpc) continue;
+    const int pti = A.pt[i];
+    KSum sum[D];
+    if (pti > 0) {
+      int cx0, cy0, cz0;
+      cell_of(A.skey[i], I, cx0, cy0, cz0);
+      float oi[D], ni[D], vi[D];
+#pragma unroll
+      for (int d = 0; d < D; ++d) {
+        oi[d] = A.off[d][i];
+        ni[d] = A.offn[d][i];
+        vi[d] = A.v[d][i];
+      }
+      const float dri = A.dr[i];
+      const float rhoi = I.rho0 + dri, Pi = eos32(dri, pti, I);
+      const float dt = (float)I.dt;
+      const int zlo = D == 3 ? -1 : 0, zhi = D == 3 ? 1 : 0;
+      for (int dz = zlo; dz <= zhi; ++dz) {
+        const int cz = cz0 + dz;
+        if (cz < 0 || cz >= I.nc[2]) continue;
+        for (int dy = -1; dy <= 1; ++dy) {
+          const int cy = cy0 + dy;
+          if (cy < 0 || cy >= I.nc[1]) continue;
+          const int row = I.key_off + I.nc[0] * (cy + I.nc[1] * cz);
+          for (int dxc = -1; dxc <= 1; ++dxc) {
+            const int cx = cx0 + dxc;
+            if (cx < 0 || cx >= I.nc[0]) continue;
+            const int j0 = A.cellstart[row + cx], j1 = A.cellstart[row + cx + 1];
+            const float shx = (float)dxc * I.csf, shy = (float)dy * I.csf, shz = (float)dz * I.csf;
+            for (int j = j0; j < j1; ++j) {
+              const int ptj = A.pt[j];
+              if (j == i || !(ptj > 0)) continue;
+              float d[D];
+#pragma unroll
+              for (int q = 0; q < D; ++q) d[q] = (oi[q] - A.off[q][j]) - (q == 0 ? shx : (q == 1 ? shy : shz));
+              if (!(dot32<D>(d, d) < I.H2)) continue;  // the step's pair set
+              float dx[D], dv[D];
+#pragma unroll
+              for (int q = 0; q < D; ++q) {
+                dx[q] = (ni[q] - A.offn[q][j]) - (q == 0 ? shx : (q == 1 ? shy : shz));
+                dv[q] = vi[q] - A.v[q][j];
+              }
+              const float drj = A.dr[j];
+              const float rhoj = I.rho0 + drj;
+              const float r2 = dot32<D>(dx, dx);
+              const float u = sqrtf(r2) * I.dpc_l0inv;
+              const float t = u < 1.f ? 1.f - u : 0.f;
+              const float t2 = t * t;
+              const float w = (1.f + 4.f * u) * (t2 * t2) * I.dpc_nW;
+              const float chi = sqrtf(w * I.dpc_whinv);
+              const float kk = u < I.dpc_kernlim ? 1.f : chi;
+              const float Pb = chi * fmaxf(fminf(I.dpc_lambda * fabsf(Pi + eos32(drj, ptj, I)),
+                                                 I.dpc_lambda * I.dpc_pmax), I.dpc_pmin);
+              const float vr = dot32<D>(dv, dx);
+              float c;
+              if (vr < 0.f) c = kk * (-vr / (r2 + I.dpc_eta2));
+              else c = 2.f * dt * Pb / ((rhoi + rhoj) * (r2 + I.dpc_eta2));
+#pragma unroll
+              for (int q = 0; q < D; ++q) sum[q].add(c * dx[q]);
+            }
+          }
+        }
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < D; ++q) A.vh[q][i] = sum[q].s;
+  }
+}
+
+template <int D>
+__global__ void k_ens_dpc_apply(EnsArr A, const EnsInst* __restrict__ T) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= A.N) return;
+  const EnsInst& I = T[A.inst[i]];
+  if (!I.use_dpc || !(A.pt[i] > 1)) return;
+#pragma unroll
+  for (int q = 0; q < D; ++q) {
+    const float s = A.vh[q][i];
+    A.v[q][i] = A.v[q][i] + s;
+    A.dvb[q][i] -= s;
+    const double dx = (double)s * I.dt;
+    A.x[q][i] = A.x[q][i] + dx;
+    A.offn[q][i] += (float)dx;
+    A.dxb[q][i] -= (float)dx;
+  }
+}
+
+// xsphcorr! + update_xsphcorr! (src/gpukernels_sph.jl:1745-1838): stage-1 W
+// (pairs and distances at x), v and ρ after the corrector and dpcreg!;
+// moves x only.  Reads neighbours' v, writes its own x: one pass.
+template <int D>
+__global__ void __launch_bounds__(ENS_MAX_TPB) k_ens_xsph(EnsArr A, const EnsInst* __restrict__ T) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < A.N; i += stride) {
+    const EnsInst& I = T[A.inst[i]];
+    if (!I.use_xsph || !(A.pt[i] > 1)) continue;
+    int cx0, cy0, cz0;
+    cell_of(A.skey[i], I, cx0, cy0, cz0);
+    float oi[D], vi[D];
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      oi[d] = A.off[d][i];
+      vi[d] = A.v[d][i];
+    }
+    const float rhoi = I.rho0 + A.dr[i];
+    KSum sum[D];
+    const int zlo = D == 3 ? -1 : 0, zhi = D == 3 ? 1 : 0;
+    for (int dz = zlo; dz <= zhi; ++dz) {
+      const int cz = cz0 + dz;
+      if (cz < 0 || cz >= I.nc[2]) continue;
+      for (int dy = -1; dy <= 1; ++dy) {
+        const int cy = cy0 + dy;
+        if (cy < 0 || cy >= I.nc[1]) continue;
+        const int row = I.key_off + I.nc[0] * (cy + I.nc[1] * cz);
+        for (int dxc = -1; dxc <= 1; ++dxc) {
+          const int cx = cx0 + dxc;
+          if (cx < 0 || cx >= I.nc[0]) continue;
+          const int j0 = A.cellstart[row + cx], j1 = A.cellstart[row + cx + 1];
+          const float shx = (float)dxc * I.csf, shy = (float)dy * I.csf, shz = (float)dz * I.csf;
+          for (int j = j0; j < j1; ++j) {
+            if (j == i || !(A.pt[j] > 1)) continue;
+            float d[D];
+#pragma unroll
+            for (int q = 0; q < D; ++q) d[q] = (oi[q] - A.off[q][j]) - (q == 0 ? shx : (q == 1 ? shy : shz));
+            const float r2 = dot32<D>(d, d);
+            if (!(r2 < I.H2)) continue;
+            const float u = sqrtf(r2) * I.Hinv;
+            const float t = u < 1.f ? 1.f - u : 0.f;
+            const float t2 = t * t;
+            const float w = (1.f + 4.f * u) * (t2 * t2) * I.nW;
+            const float xs = I.xsph_c * w / (rhoi + (I.rho0 + A.dr[j]));
+#pragma unroll
+            for (int q = 0; q < D; ++q) sum[q].add((A.v[q][j] - vi[q]) * xs);
+          }
+        }
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < D; ++q) {
+      const double dx = (double)sum[q].s * I.dt;
+      A.x[q][i] = A.x[q][i] + dx;
+      A.offn[q][i] += (float)dx;
+      A.dxb[q][i] -= (float)dx;
     }
   }
 }
@@ -473,6 +643,8 @@ __global__ void k_ens_repack(int nmoves, const Move* __restrict__ mv, int64_t N,
   for (int d = 0; d < D; ++d) {
     out.x[d][k] = in.x[d][src];
     out.v[d][k] = in.v[d][src];
+    out.dxb[d][k] = in.dxb[d][src];
+    out.dvb[d][k] = in.dvb[d][src];
   }
   out.dr[k] = in.dr[src];
   out.drb[k] = in.drb[src];
@@ -515,7 +687,8 @@ struct gcsph_ens {
   int cur = 0;
   int64_t gen = 0;  // layout generation (graphs and tuning follow it)
   // state, double-buffered for the re-sort
-  DevBuf X[2][3], V[2][3], DR[2], DRB[2], PT[2], ID[2];
+  DevBuf X[2][3], V[2][3], DXB[2][3], DVB[2][3], DR[2], DRB[2], PT[2], ID[2];
+  DevBuf OFFN[3];
   DevBuf INST, KEY, SLOT, TMP, PERM, SKEY, OFF[3], OFFH[3], VH[3], DRH, COUNT, CELLSTART, SCRATCH, TAB, MOVES, OUT;
   DevBuf ISTEP;          // steps done per instance (cspmcorr! schedule), packing order
   int tpb = 0;           // 0: not tuned yet
@@ -526,6 +699,7 @@ struct gcsph_ens {
   unsigned long long clock = 0;
   bool use_graphs = true;
   bool any_cspm = false;  // some instance runs cspmcorr!
+  bool any_dpc = false, any_xsph = false;
   int64_t n_captures = 0, n_replays = 0;
 };
 
@@ -538,6 +712,8 @@ EnsState ens_state(gcsph_ens* e, int b) {
   for (int d = 0; d < 3; ++d) {
     s.x[d] = e->X[b][d].as<double>();
     s.v[d] = e->V[b][d].as<float>();
+    s.dxb[d] = e->DXB[b][d].as<float>();
+    s.dvb[d] = e->DVB[b][d].as<float>();
   }
   s.dr = e->DR[b].as<float>();
   s.drb = e->DRB[b].as<float>();
@@ -558,6 +734,9 @@ EnsArr ens_arr(gcsph_ens* e) {
     A.off[d] = e->OFF[d].as<float>();
     A.offh[d] = e->OFFH[d].as<float>();
     A.vh[d] = e->VH[d].as<float>();
+    A.offn[d] = e->OFFN[d].as<float>();
+    A.dxb[d] = e->DXB[e->cur][d].as<float>();
+    A.dvb[d] = e->DVB[e->cur][d].as<float>();
   }
   A.dr = e->DR[e->cur].as<float>();
   A.drb = e->DRB[e->cur].as<float>();
@@ -598,6 +777,8 @@ int ens_reserve(gcsph_ens* e, int64_t n) {
     for (int d = 0; d < e->D; ++d) {
       if ((rc = keep(e->X[b][d], sizeof(double)))) return rc;
       if ((rc = keep(e->V[b][d], sizeof(float)))) return rc;
+      if ((rc = keep(e->DXB[b][d], sizeof(float)))) return rc;
+      if ((rc = keep(e->DVB[b][d], sizeof(float)))) return rc;
     }
     if ((rc = keep(e->DR[b], sizeof(float)))) return rc;
     if ((rc = keep(e->DRB[b], sizeof(float)))) return rc;
@@ -612,6 +793,7 @@ int ens_reserve(gcsph_ens* e, int64_t n) {
     if ((rc = e->OFF[d].ensure(sizeof(float) * want, e->st))) return rc;
     if ((rc = e->OFFH[d].ensure(sizeof(float) * want, e->st))) return rc;
     if ((rc = e->VH[d].ensure(sizeof(float) * want, e->st))) return rc;
+    if ((rc = e->OFFN[d].ensure(sizeof(float) * want, e->st))) return rc;
   }
   if ((rc = e->DRH.ensure(sizeof(float) * want, e->st))) return rc;
   if ((rc = e->SCRATCH.ensure(sizeof(int64_t) * scan_scratch_elems(std::max<int64_t>(want, e->cap_k) + 1), e->st)))
@@ -645,8 +827,12 @@ int ens_relayout(gcsph_ens* e) {
   }
   e->N = p;
   e->K = k;
-  e->any_cspm = false;
-  for (const EnsHostInst& h : e->inst) e->any_cspm = e->any_cspm || h.prm.cspmn > 0;
+  e->any_cspm = e->any_dpc = e->any_xsph = false;
+  for (const EnsHostInst& h : e->inst) {
+    e->any_cspm = e->any_cspm || h.prm.cspmn > 0;
+    e->any_dpc = e->any_dpc || h.prm.dpc_l0 > 0;
+    e->any_xsph = e->any_xsph || h.prm.xsph_eps > 0;
+  }
   int rc;
   if ((rc = ens_reserve_cells(e, k))) return rc;
   std::vector<EnsInst> tab(e->inst.size());
@@ -737,6 +923,20 @@ int ens_enqueue_step(gcsph_ens* e, cudaStream_t st, int tpb) {
   GC_LAUNCHED();
   timer_end(T_STAGE2, st);
   const int32_t ninst = (int32_t)e->inst.size();
+  if (e->any_dpc) {
+    timer_begin(T_DPC, st);
+    k_ens_dpc<D><<<grid, tpb, 0, st>>>(A, T);
+    GC_LAUNCHED();
+    k_ens_dpc_apply<D><<<nblocks(N, 256), 256, 0, st>>>(A, T);
+    GC_LAUNCHED();
+    timer_end(T_DPC, st);
+  }
+  if (e->any_xsph) {
+    timer_begin(T_XSPH, st);
+    k_ens_xsph<D><<<grid, tpb, 0, st>>>(A, T);
+    GC_LAUNCHED();
+    timer_end(T_XSPH, st);
+  }
   if (e->any_cspm) {
     timer_begin(T_CSPM, st);
     k_ens_cspm<D><<<grid, tpb, 0, st>>>(A, T, e->ISTEP.as<int32_t>());
@@ -904,6 +1104,8 @@ void ens_destroy(gcsph_ens* e) {
     for (int d = 0; d < 3; ++d) {
       e->X[b][d].release();
       e->V[b][d].release();
+      e->DXB[b][d].release();
+      e->DVB[b][d].release();
     }
     e->DR[b].release();
     e->DRB[b].release();
@@ -917,16 +1119,17 @@ void ens_destroy(gcsph_ens* e) {
     e->OFF[d].release();
     e->OFFH[d].release();
     e->VH[d].release();
+    e->OFFN[d].release();
   }
   delete e;
 }
 
 int ens_bytes_per_particle(int32_t D, int64_t* bytes) {
   if (!bytes || (D != 2 && D != 3)) return fail(GCSPH_EINVAL, "bad argument");
-  // 2 x (x f64, v f32) per dim + 2 x (δρ, δρ base, ptype, id) + inst, key,
-  // slot, tmp, perm, skey + (off, offh, vh) per dim + δρ½, plus about one
-  // cell per particle
-  *bytes = 2 * D * (8 + 4) + 2 * 16 + 6 * 4 + D * 12 + 4 + 8;
+  // 2 x (x f64, v f32, x and v base differences f32) per dim + 2 x (δρ,
+  // δρ base, ptype, id) + inst, key, slot, tmp, perm, skey + (off, offh, vh,
+  // offn) per dim + δρ½, plus about one cell per particle
+  *bytes = 2 * D * (8 + 4 + 8) + 2 * 16 + 6 * 4 + D * 16 + 4 + 8;
   return GCSPH_OK;
 }
 
@@ -995,6 +1198,21 @@ int ens_add(gcsph_ens* e, int64_t n, const double* x, const double* v, const dou
   I.fb_d[1] = (float)p->bound_D;
   I.fb_r0[1] = (float)p->bound_l;
   I.fb_eta2[1] = (float)(0.01 * p->bound_l * p->bound_l);
+  I.use_dpc = p->dpc_l0 > 0;
+  if (I.use_dpc) {
+    const double l0inv = 1.0 / p->dpc_l0;
+    const double nW = D == 2 ? wc2_norm_w<2>(l0inv) : wc2_norm_w<3>(l0inv);
+    I.dpc_l0inv = (float)l0inv;
+    I.dpc_nW = (float)nW;
+    I.dpc_whinv = (float)(1.0 / wc2_w(0.5, nW));
+    I.dpc_kernlim = (float)gcsph_dpckernlim(D);
+    I.dpc_eta2 = (float)((0.1 * p->dpc_l0) * (0.1 * p->dpc_l0));
+    I.dpc_pmin = (float)p->dpc_pmin;
+    I.dpc_pmax = (float)p->dpc_pmax;
+    I.dpc_lambda = (float)p->dpc_lambda;
+  }
+  I.use_xsph = p->xsph_eps > 0;
+  I.xsph_c = (float)(2.0 * p->m0 * p->xsph_eps);
   const double a = 1.0 / (double)p->gamma;
   const double c1 = a, c2 = c1 * (a - 1.0) / 2.0, c3 = c2 * (a - 2.0) / 3.0, c4 = c3 * (a - 3.0) / 4.0;
   I.pc[0] = (float)c1;
@@ -1022,6 +1240,10 @@ int ens_add(gcsph_ens* e, int64_t n, const double* x, const double* v, const dou
   }
   GC_CUDA(cudaMemcpyAsync(e->DR[b].as<float>() + at, drf.data(), sizeof(float) * n, cudaMemcpyHostToDevice, e->st));
   GC_CUDA(cudaMemcpyAsync(e->DRB[b].as<float>() + at, drf.data(), sizeof(float) * n, cudaMemcpyHostToDevice, e->st));
+  for (int d = 0; d < D; ++d) {
+    GC_CUDA(cudaMemsetAsync(e->DXB[b][d].as<float>() + at, 0, sizeof(float) * n, e->st));
+    GC_CUDA(cudaMemsetAsync(e->DVB[b][d].as<float>() + at, 0, sizeof(float) * n, e->st));
+  }
   GC_CUDA(cudaMemcpyAsync(e->PT[b].as<int32_t>() + at, ptype, sizeof(int32_t) * n, cudaMemcpyHostToDevice, e->st));
   GC_CUDA(cudaMemcpyAsync(e->ID[b].as<int32_t>() + at, ids.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice,
                           e->st));

@@ -40,6 +40,11 @@ class InstanceSpec:
     bound_D: float = 0.4
     bound_l: float = 0.0     # 0: 2 dx
     cspmn: int = 15          # cspmcorr! period in steps (SPHProblem's default), 0 = never
+    dpc_l0: float = 0.0      # dpcreg! when > 0 (SPHProblem's defaults below)
+    dpc_pmin: float = 1.0
+    dpc_pmax: float = 10000.0
+    dpc_lambda: float = 0.01
+    xsph_eps: float = 0.0    # xsphcorr! when > 0
     v: np.ndarray | None = None
     grid_min: tuple | None = None
     grid_max: tuple | None = None
@@ -62,11 +67,14 @@ def spec_from_case(case, dt=None, alpha=None, delta=None, margin_cells=2, headro
     hi = case.x.max(axis=1) + margin_cells * case.H
     hi[1] += headroom * (hi[1] - lo[1])
     ex = dict(case.extra) if getattr(case, "extra", None) else {}
+    extra = {k: float(ex[k]) for k in ("dpc_l0", "dpc_pmin", "dpc_pmax", "dpc_lambda", "xsph_eps") if k in ex}
+    if "cspmn" in ex:
+        extra["cspmn"] = int(ex["cspmn"])
     return InstanceSpec(x=case.x, rho=case.rho, ptype=case.ptype, dx=case.dx, h=case.h, H=case.H, rho0=case.rho0,
                         m0=case.m0, dt=case.dt if dt is None else dt, alpha=case.alpha if alpha is None else alpha,
                         c0=case.c0, gamma=case.gamma, delta=case.delta if delta is None else delta, g=case.g,
                         nu=ex.get("nu", 0.0), s=getattr(case, "s", 0.0) or 0.0,
-                        grid_min=tuple(lo[:D]), grid_max=tuple(hi[:D]))
+                        grid_min=tuple(lo[:D]), grid_max=tuple(hi[:D]), **extra)
 
 
 def _params(spec: InstanceSpec) -> _lib.gcsph_ens_params:
@@ -76,6 +84,8 @@ def _params(spec: InstanceSpec) -> _lib.gcsph_ens_params:
     p.bound_l = float(spec.bound_l) if spec.bound_l > 0 else 2.0 * float(spec.dx)
     p.gamma = int(spec.gamma)
     p.cspmn = int(spec.cspmn)
+    for k in ("dpc_l0", "dpc_pmin", "dpc_pmax", "dpc_lambda", "xsph_eps"):
+        setattr(p, k, float(getattr(spec, k)))
     lo = spec.grid_min if spec.grid_min is not None else spec.x.min(axis=1) - 2 * spec.H
     hi = spec.grid_max if spec.grid_max is not None else spec.x.max(axis=1) + 2 * spec.H
     for d in range(spec.D):

@@ -270,8 +270,9 @@ double gcsph_dpckernlim(int32_t D);
  * per-particle sums in FP32 (Kahan), density held as ρ - ρ₀, positions in
  * FP64.  The physics per step is that of sph_step with dist = H: ∂ρ∂tDDT!,
  * ∂v∂t!, ∂v∂t_av!, ∂v∂t_visc! (ν > 0), gravity!, fbmolforce!, ∂v∂tpF! (s > 0),
- * the half-step predictors, symplectic_update! and cspmcorr! every cspmn
- * steps (counted from the instance's admission, as within one stepsolve!).  An instance's results do
+ * the half-step predictors, symplectic_update!, dpcreg! (dpc_l0 > 0),
+ * xsphcorr! (xsph_eps > 0) and cspmcorr! every cspmn steps (counted from the
+ * instance's admission, as within one stepsolve!).  An instance's results do
  * not depend on which other instances share the ensemble (bit-identical).
  * Host arrays in ens_add / ens_get are HOST pointers, D-major (x[d*n + i]).
  * ------------------------------------------------------------------------ */
@@ -280,6 +281,8 @@ typedef struct {
   double dx, h, H, rho0, m0, dt, alpha, nu, g, c0, s, delta;
   double bound_D, bound_l;           /* stage-2 fbmolforce constants (stage 1: 0.4, 2dx) */
   double grid_min[3], grid_max[3];   /* frozen cell grid; points outside clamp to edge cells */
+  double dpc_l0, dpc_pmin, dpc_pmax, dpc_lambda;  /* dpcreg! when dpc_l0 > 0 */
+  double xsph_eps;                   /* xsphcorr! when > 0 */
   int32_t gamma;
   int32_t cspmn;                     /* cspmcorr! every cspmn steps since admission (0: never) */
 } gcsph_ens_params;

@@ -69,6 +69,52 @@ def test_fp32_3d_viscous_surface_tension_against_fp64(gpu_pkg, orc):
     assert err["rho"] <= TOL and err["v"] <= TOL and err["disp"] <= TOL, err
 
 
+def _oracle_full(orc, case, n, v):
+    p = orc.default_params(case.dx, case.h, case.H, case.rho0, case.m0, case.dt, case.alpha, case.c0, case.gamma,
+                           case.delta, case.CFL, case.dist, g=case.g, s=case.s)
+    for k, val in case.extra.items():
+        setattr(p, k, val)
+    ref = orc.OracleSystem(case.x, case.cellsize, case.dist, case.rho, case.ptype, p, v=v)
+    ref.stepsolve(n)
+    return ref
+
+
+def _moving(case, seed=17, amp=0.05):
+    """Random fluid velocities, so that DPC's branch on the sign of Δv·Δx is
+    not decided by rounding noise (lattice pairs at rest)."""
+    rng = np.random.default_rng(seed)
+    v = rng.uniform(-amp, amp, case.x.shape)
+    v[:, case.ptype <= 1] = 0.0
+    return np.ascontiguousarray(v)
+
+
+@pytest.mark.parametrize("D", [2, 3])
+def test_fp32_full_physics_against_fp64(gpu_pkg, orc, D):
+    """ν, surface tension, DPC, XSPH and CSPM on (dpcreg!/xsphcorr! move x and
+    v but not the half-step bases, as in the reference)."""
+    w = gpu_pkg.workloads
+    if D == 2:
+        case = w.dam_break_2d(dx=0.04, fluid=(0.6, 0.8), tank=(1.2, 1.0), layer_ptype=(1, 0, 0))
+        case.s = 0.05
+        case.extra = dict(nu=0.2, dpc_l0=case.dx * 0.7, dpc_lambda=0.005, dpc_pmax=36000.0, xsph_eps=0.5, cspmn=7)
+        n = 60
+    else:
+        case = w.dam_break_3d(dx=0.05, fluid=(0.3, 0.4, 0.2), tank=(0.6, 0.6, 0.3))
+        case.extra = dict(case.extra, dpc_l0=0.03)
+        n = 40
+    v = _moving(case)
+    spec = gpu_pkg.spec_from_case(case)
+    spec.v = v
+    assert spec.dpc_l0 > 0 and spec.xsph_eps > 0 and spec.nu > 0 and spec.s > 0
+    ens = gpu_pkg.Ensemble(D)
+    slot = ens.add(spec)
+    ens.step(n)
+    ref = _oracle_full(orc, case, n, v)
+    err = errors(ens, slot, ref, case)
+    print(f"fp32 vs fp64, full physics {D}-D, {n} steps:", err)
+    assert err["rho"] <= TOL and err["v"] <= TOL and err["disp"] <= TOL, err
+
+
 def _specs(pkg):
     w = pkg.workloads
     a = pkg.spec_from_case(w.dam_break_2d(dx=0.04, fluid=(0.6, 0.8), tank=(1.2, 1.0)))
