@@ -58,6 +58,19 @@ def dist_env():
     return ws, rank, local
 
 
+def max_over_ranks(x: float) -> float:
+    """The largest x over all ranks of the current process group (the slowest
+    replica's time); x itself without one."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(x)
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(x)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def make_case(pkg):
     return pkg.workloads.dam_break_2d()
 
@@ -437,11 +450,7 @@ def run_gb300(args):
         barrier()
     launches = g.launch_count() - launches0
     ms = sum(starts[i].elapsed_time(ends[i]) for i in range(args.steps))
-    if ws > 1:
-        import torch.distributed as dist
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(ms)
     value = ws * N * SUB * args.steps / (ms / 1e3)
     # per-kernel-family timers: the same K bench steps again, instrumented
     # (event nodes between the kernels), so the timed run above stays clean
@@ -494,11 +503,7 @@ def run_gb300(args):
         e_en[i].record()
     barrier()
     ms_e2e = sum(e_st[i].elapsed_time(e_en[i]) for i in range(args.steps))
-    if ws > 1:
-        import torch.distributed as dist
-        t = torch.tensor([ms_e2e], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_e2e = float(t.item())
+    ms_e2e = max_over_ranks(ms_e2e)
     e2e = ws * N * SUB * args.steps / (ms_e2e / 1e3)
     if rank != 0:
         return 0

@@ -224,3 +224,48 @@ def serving_requests(count: int, seed: int = SEED, rate: float = 20.0, frac_2d: 
         steps = max(1, int(round(hz / case.dt)))
         out.append((t, case, steps))
     return out
+
+
+def read_csv_columns(path: str) -> dict:
+    """A DualSPHysics/ParaView-style CSV (quoted header, numeric columns) as
+    {column name: float64 array} -- the DataFrame the reference reads."""
+    import csv
+    with open(path, newline="") as f:
+        names = next(csv.reader(f))
+    data = np.loadtxt(path, delimiter=",", skiprows=1, ndmin=2)
+    if data.shape[1] != len(names):
+        raise ValueError(f"{path}: {len(names)} header names, {data.shape[1]} columns")
+    return {n: np.ascontiguousarray(data[:, i]) for i, n in enumerate(names)}
+
+
+def loadparticles(fluid_csv: str, boundary_csv: str, fluidcols=("Points:0", "Points:2"),
+                  boundarycols=("Points:0", "Points:2")):
+    """loadparticles (src/auxillary.jl:3-11): fluid points, then boundary
+    points, from the named columns (2-D default: ParaView x and z).  Returns
+    (points (D, N) float64, fluid columns, boundary columns)."""
+    if len(fluidcols) != len(boundarycols):
+        raise ValueError("fluid and boundary column lists differ in length")
+    fl = read_csv_columns(fluid_csv)
+    bd = read_csv_columns(boundary_csv)
+    pts = np.stack([np.concatenate([fl[a], bd[b]]) for a, b in zip(fluidcols, boundarycols)])
+    return np.ascontiguousarray(pts), fl, bd
+
+
+def case_from_csv(fluid_csv: str, boundary_csv: str, dx: float, fluidcols=("Points:0", "Points:2"),
+                  boundarycols=("Points:0", "Points:2"), rho_col="Rhop", ptype_col="ptype") -> Case:
+    """A Case from the reference's particle CSVs with the README demo's
+    parameters (h = 1.2√2 dx in 2-D, √3 dx in 3-D, H = 2h, dist = H): density
+    from `rho_col`, ptype from `ptype_col` (fluid rows default to 2 and
+    boundary rows to 0 where the column is absent)."""
+    x, fl, bd = loadparticles(fluid_csv, boundary_csv, fluidcols, boundarycols)
+    D = x.shape[0]
+    rho = np.concatenate([fl.get(rho_col, np.full(len(next(iter(fl.values()))), 1000.0)),
+                          bd.get(rho_col, np.full(len(next(iter(bd.values()))), 1000.0))])
+    nf, nb = len(next(iter(fl.values()))), len(next(iter(bd.values())))
+    pt = np.concatenate([fl.get(ptype_col, np.full(nf, 2.0)), bd.get(ptype_col, np.zeros(nb))]).astype(np.int32)
+    h = 1.2 * math.sqrt(2) * dx if D == 2 else math.sqrt(3 * dx ** 2)
+    H = 2 * h
+    rho0, g = 1000.0, 9.81
+    return Case(x=x, rho=np.ascontiguousarray(rho, dtype=np.float64), ptype=pt, dx=dx, h=h, H=H, dist=H,
+                cellsize=(H,) * D, rho0=rho0, m0=rho0 * dx ** D, dt=1e-5, alpha=0.01, c0=math.sqrt(g * 2) * 20,
+                gamma=7, delta=0.1, CFL=0.2, g=g)
