@@ -75,6 +75,7 @@ _SIGS = {
     "sph_get_params": (C.c_int, [vp, C.POINTER(gcsph_params)]),
     "sph_set_lanes": (C.c_int, [vp, i32]),
     "sph_set_graphs": (C.c_int, [vp, i32]),
+    "sph_set_dt_variant": (C.c_int, [vp, i32]),
     "sph_graph_stats": (C.c_int, [vp, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
     "sph_step": (C.c_int, [vp, i32, C.c_int, f64, f64, C.POINTER(i64), C.POINTER(f64)]),
     "ens_create": (C.c_int, [i32, vp, C.POINTER(vp)]),

@@ -23,6 +23,7 @@ UNITS = {
     "common.cu": [],
     "celllist.cu": ["-fmad=false"],
     "sph_step.cu": ["-fmad=false"],
+    "sph_once.cu": [],
     "sph_pairs.cu": ["-fmad=false"],
     "ensemble.cu": [],
 }

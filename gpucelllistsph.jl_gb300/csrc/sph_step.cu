@@ -18,286 +18,9 @@
 // j-side formulas are exactly the i-side formula seen from j (negated Δx, Δv
 // and ∇W are exact in IEEE arithmetic), so no term changes meaning.
 // Arrays that a pass reads from neighbours and also updates are ping-ponged.
-#include <math.h>
-#include "celllist.cuh"
-#include "pf7_series.cuh"
+#include "sph_step.cuh"
 
 namespace gcsph {
-
-static constexpr int STPB = 128;
-
-struct StepConst {
-  double h, eta2, m0, rho0, ginv, DDTkh, DDTgz, P0, alpha, c0, nu, g, s, Hinv, nW, nDW;
-  double fb_d, fb_r0, fb_eta2;  // fbmolforce constants of the stage being run
-  double twoh, pfc, hp1;        // 2h, 1.5*pi, 0.1h  (∂v∂tpF!)
-  double dpc_l0inv, dpc_nW, dpc_whinv, dpc_pmin, dpc_pmax, dpc_lambda, dpc_kernlim, dpc_eta2;
-  double xsph_c;                // 2*m0*eps
-  double cfl, dt_eta2;          // Δt_stepping
-  double tmin, tmax;
-  int gamma, use_visc, use_pF, timestepping;
-  double reb_thr;  // update! is due after a step whose max |cΔx| passes this (0.9 (dist - H))
-  int count_reb;   // this step's decision counts toward the call's update! total
-};
-
-// device scalars of a running solve
-struct Scal {
-  double dt;
-  double etime;
-  unsigned long long maxcdx;  // bits of max |cΔx| of the current step
-  unsigned long long amax;    // bits of max |a|
-  unsigned long long vmax;    // bits of max |h v.x/(x.x+η²)|
-  int ovf;                    // the neighbour CSR outgrew its buffers: this step's kernels skip
-  int pad0;
-  unsigned long long maxout;  // bits of the largest max |cΔx| of the call (stepsolve!'s second result)
-  long long nreb;             // update! calls of the call (stepsolve!'s first result)
-};
-
-template <int D>
-struct SArr {
-  const int64_t* rs;
-  const int32_t* nbr;
-  const int32_t* pt;
-  const int32_t* orig;
-  const int* ovf;  // set: the step's kernels skip (buffers outgrown, see rebuild)
-  double* x[3];
-  double* v[3];
-  double* rho;
-  double* P1;
-  double* xh[3];
-  double* vh[3];
-  double* rhoh;
-  double* P2;
-  double* ir;   // 1/ρ (FAST stage 1)
-  double* irh;  // 1/ρΔt½ (FAST stage 2)
-  double* We;
-  double* gWe[3];
-  double* a[3];
-  double* drho;
-  double* cdx[3];
-  double* buf2[3];
-  double* Plast;
-  double* xo[3];
-  double* xho[3];
-  double* vho[3];
-  double* vo[3];
-  double* rhoho;
-  double* rhoo;
-};
-
-template <int D>
-__device__ inline double dotD(const double* a, const double* b) {
-  double s = a[0] * b[0];
-#pragma unroll
-  for (int d = 1; d < D; ++d) s = s + a[d] * b[d];
-  return s;
-}
-
-// Julia min/max propagate NaN (fmin/fmax do not)
-__device__ inline double jl_min(double a, double b) { return (a != a || b != b) ? (a + b) : fmin(a, b); }
-__device__ inline double jl_max(double a, double b) { return (a != a || b != b) ? (a + b) : fmax(a, b); }
-
-// ∂ρ∂tDDT! pair value seen from particle k (src/gpukernels_sph.jl:579-625)
-template <int D>
-__device__ inline double ddt_term(const StepConst& c, int ptk, int ptm, const double* dx, double r2, const double* gw,
-                                  const double* dv, double rk, double rm) {
-  if (!(ptk > 0 && ptm > 0)) return 0.0;
-  double dot3 = -dotD<D>(dx, gw);
-  double m0dot = c.m0 * dotD<D>(dv, gw);
-  double s = m0dot;
-  if (ptk > 1) {
-    double drhopvp = c.rho0 * powfancy7th(1.0 + c.DDTgz * dx[1], c.ginv, c.gamma) - c.rho0;
-    double visc_densi = c.DDTkh * ((rm - rk) - drhopvp) / (r2 + c.eta2);
-    double delta = visc_densi * dot3 * c.m0 / rm;
-    s += delta;
-  }
-  return s;
-}
-
-// all momentum terms of one pair seen from k; accumulators kept apart so the
-// final sum follows the reference's kernel order (∂v∂t!, av, visc, grav, fb, pF)
-template <int D>
-struct Acc {
-  double p[D], av[D], vi[D], fb[D], pf[D];
-  __device__ void zero() {
-#pragma unroll
-    for (int d = 0; d < D; ++d) p[d] = av[d] = vi[d] = fb[d] = pf[d] = 0.0;
-  }
-};
-
-template <int D>
-__device__ inline void mom_terms(const StepConst& c, Acc<D>& A, int ptk, int ptm, const double* dx, double r2,
-                                 const double* gw, const double* dv, double rk, double rm, double Pk, double Pm) {
-  // ∂v∂t!, :755-772
-  if (ptk * ptm > 0) {
-    double Pfac = (Pk + Pm) / (rk * rm);
-    double sc = -c.m0 * Pfac;
-#pragma unroll
-    for (int d = 0; d < D; ++d) A.p[d] += sc * gw[d];
-  }
-  if (ptk > 0 && ptm > 0) {
-    // ∂v∂t_av!, :869-897
-    double rhom = (rk + rm) * 0.5;
-    double cond = dotD<D>(dv, dx);
-    if (cond < 0.0) {
-      double dmu = c.h * cond / (r2 + c.eta2);
-      double dPi = (-c.alpha * c.c0 * dmu) / rhom;
-      double sc = -dPi * c.m0;
-#pragma unroll
-      for (int d = 0; d < D; ++d) A.av[d] += sc * gw[d];
-    }
-    // ∂v∂t_visc!, :967-980
-    if (c.use_visc) {
-      double nuterm = 4.0 * c.nu * c.m0 * dotD<D>(dx, gw) / ((rk + rm) * (r2 + c.eta2));
-#pragma unroll
-      for (int d = 0; d < D; ++d) A.vi[d] += nuterm * dv[d];
-    }
-  }
-}
-
-// fbmolforce!, :1891-1901 (mask: exactly one side real)
-template <int D>
-__device__ inline void fb_term(const StepConst& c, Acc<D>& A, int ptk, int ptm, const double* dx, double r2) {
-  if ((ptk > 0) == (ptm > 0)) return;
-  double r = sqrt(r2);
-  if (r < c.fb_r0) {
-    double q = c.fb_r0 / (r + c.fb_eta2);
-    double q2 = q * q, q4 = q2 * q2, q8 = q4 * q4, q12 = q8 * q4;
-    double Fc = c.fb_d * (q12 - q4) / (r2 + c.fb_eta2);
-#pragma unroll
-    for (int d = 0; d < D; ++d) A.fb[d] += dx[d] * Fc;
-  }
-}
-
-// ∂v∂tpF!, :1387-1397
-template <int D>
-__device__ inline void pf_term(const StepConst& c, Acc<D>& A, int ptk, int ptm, const double* dx, double r) {
-  if (!(ptk > 0 && ptm > 0)) return;
-  if (r < c.twoh) {
-    double scos = c.s * gc_cos(c.pfc * r / c.twoh) / (r + c.hp1);
-#pragma unroll
-    for (int d = 0; d < D; ++d) A.pf[d] += scos * dx[d] / c.m0;
-  }
-}
-
-// ---------------------------------------------------------------------------
-// FAST variants (lanes > 1): the same terms with fewer FP64 divisions -- the
-// FP64 pipe issues 2 thread-instructions per cycle per SM on GB300 and an IEEE
-// division costs ~8 of them.  1/ρ per particle is precomputed, 1/(r²+η²) is
-// shared by ∂ρ∂tDDT!, ∂v∂t_av! and ∂v∂t_visc!, 1/(ρᵢ+ρⱼ) by av and visc, and
-// powfancy7th's Newton step t - t(t³ - x/t⁴)/(4t³ + 3x/t⁴) is evaluated in the
-// equal form t - t(t⁷ - x)/(4t⁷ + 3x) with one division.  Each change moves a
-// result by a few ulp, inside the spread the reference's own atomics give.
-// ---------------------------------------------------------------------------
-__device__ inline double powfancy7th_1div(double x, double ginv, int gamma) {
-  if (gamma != 7) return pow(x, ginv);
-  const double ax = fabs(x);
-  unsigned long long bits = (unsigned long long)__double_as_longlong(ax);
-  bits = 0x36cd000000000000ULL + bits / 7ULL;
-  double t = copysign(__longlong_as_double((long long)bits), x);
-#pragma unroll
-  for (int it = 0; it < 2; ++it) {
-    const double t2 = t * t;
-    const double t3 = t2 * t;
-    const double t7 = t3 * (t2 * t2);
-    t = t - (t * (t7 - x)) / (4.0 * t7 + 3.0 * x);
-  }
-  return t;
-}
-
-template <int D>
-__device__ inline double ddt_term_fast(const StepConst& c, int ptk, const double* dx, double inv_r2eta,
-                                       const double* gw, const double* dv, double rk, double rm, double irm) {
-  double dot3 = -dotD<D>(dx, gw);
-  double s = c.m0 * dotD<D>(dv, gw);
-  if (ptk > 1) {
-    double drhopvp = c.rho0 * powfancy7th_1div(1.0 + c.DDTgz * dx[1], c.ginv, c.gamma) - c.rho0;
-    double visc_densi = c.DDTkh * ((rm - rk) - drhopvp) * inv_r2eta;
-    s += visc_densi * dot3 * c.m0 * irm;
-  }
-  return s;
-}
-
-template <int D>
-__device__ inline void mom_terms_fast(const StepConst& c, Acc<D>& A, int ptk, int ptm, const double* dx,
-                                      double inv_r2eta, const double* gw, const double* dv, double rk, double rm,
-                                      double irk, double irm, double Pk, double Pm) {
-  if (ptk * ptm > 0) {
-    const double sc = -c.m0 * ((Pk + Pm) * (irk * irm));
-#pragma unroll
-    for (int d = 0; d < D; ++d) A.p[d] += sc * gw[d];
-  }
-  if (ptk > 0 && ptm > 0) {
-    const double cond = dotD<D>(dv, dx);
-    const bool av = cond < 0.0;
-    if (av || c.use_visc) {
-      const double inv_sum = 1.0 / (rk + rm);
-      if (av) {
-        const double dmu = c.h * cond * inv_r2eta;
-        const double dPi = (-c.alpha * c.c0 * dmu) * (2.0 * inv_sum);
-        const double sc = -dPi * c.m0;
-#pragma unroll
-        for (int d = 0; d < D; ++d) A.av[d] += sc * gw[d];
-      }
-      if (c.use_visc) {
-        const double nuterm = 4.0 * c.nu * c.m0 * dotD<D>(dx, gw) * inv_sum * inv_r2eta;
-#pragma unroll
-        for (int d = 0; d < D; ++d) A.vi[d] += nuterm * dv[d];
-      }
-    }
-  }
-}
-
-// a = ((((p + av) + visc) - g) + fb) + pF
-template <int D>
-__device__ inline void finish_acc(const StepConst& c, const Acc<D>& A, double* a) {
-#pragma unroll
-  for (int d = 0; d < D; ++d) {
-    double v = A.p[d] + A.av[d];
-    if (c.use_visc) v = v + A.vi[d];
-    v = v - (d == 1 ? c.g : 0.0);
-    v = v + A.fb[d];
-    if (c.use_pF) v = v + A.pf[d];
-    a[d] = v;
-  }
-}
-
-// ---------------------------------------------------------------------------
-// Sub-warp cooperation: L lanes (1, 2, 4, 8, 16 or 32) share one particle.
-// Lane l walks row entries e0+l, e0+l+L, ...; the per-lane partial sums are
-// combined by a butterfly (xor offsets L/2 .. 1), after which every lane
-// holds the same total.  L = 1 is the serial row order -- the order the
-// oracle's scatter over its canonically ordered pair list produces -- so it
-// reproduces the oracle bit for bit; L > 1 re-associates the sums (within
-// the FP64 contract) and fills the GPU when particles are few.
-// ---------------------------------------------------------------------------
-template <int L>
-__device__ inline unsigned group_mask() {
-  if constexpr (L == 32) {
-    return 0xffffffffu;
-  } else {
-    const unsigned lanew = threadIdx.x & 31u;
-    return ((1u << L) - 1u) << (lanew & ~(unsigned)(L - 1));
-  }
-}
-template <int L>
-__device__ inline double group_sum(double v, unsigned gm) {
-#pragma unroll
-  for (int o = L / 2; o > 0; o >>= 1) v = v + __shfl_xor_sync(gm, v, o);
-  return v;
-}
-template <int D, int L>
-__device__ inline void group_sum_acc(Acc<D>& A, const StepConst& c, unsigned gm) {
-  if (L == 1) return;
-#pragma unroll
-  for (int d = 0; d < D; ++d) {
-    A.p[d] = group_sum<L>(A.p[d], gm);
-    A.av[d] = group_sum<L>(A.av[d], gm);
-    if (c.use_visc) A.vi[d] = group_sum<L>(A.vi[d], gm);
-    A.fb[d] = group_sum<L>(A.fb[d], gm);
-    if (c.use_pF) A.pf[d] = group_sum<L>(A.pf[d], gm);
-  }
-}
-
 // ---------------------------------------------------------------------------
 // stage 1 at (x, ρ, v) + predictors
 // ---------------------------------------------------------------------------
@@ -463,246 +186,6 @@ __global__ void __launch_bounds__(STPB) k_stage2(StepConst c, Scal* __restrict__
     }
   }
   // maximum(maximum.(abs, cΔx)), src/sphproblem.jl:325
-  mc = warp_max(mc);
-  __shared__ double smax[STPB / 32];
-  if ((threadIdx.x & 31) == 0) smax[threadIdx.x >> 5] = mc;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double m = smax[0];
-    for (int w = 1; w < STPB / 32; ++w) m = fmax(m, smax[w]);
-    atomic_max_pos(&sc->maxcdx, m);
-  }
-}
-
-// ---------------------------------------------------------------------------
-// Pair-once stage passes (lanes > 1, the default).  The gather above
-// evaluates every pair twice, once from each side; on GB300 the FP64 pipe is
-// the bound, so here each pair is evaluated once.  Pass A: one thread per pair
-// (k, m), k < m in cell order -- every thread has the same work, whatever the
-// row lengths -- computes the pair and writes both sides' contributions into
-// per-entry slots: slot e in k's row and slot mirror(e) in m's row.  Pass B:
-// each particle sums its whole row (L lanes, fixed order -- deterministic, no
-// atomics) and runs the predictor or the corrector.  Cost: one write + one
-// read of (1+D) doubles per neighbour entry.
-// ---------------------------------------------------------------------------
-struct PairBuf {
-  double* cd;             // ∂ρ/∂t contribution per neighbour entry
-  double* ca[3];          // ∂v/∂t contribution per neighbour entry (gravity not included)
-  const int4* pq;         // (k, m, e, mirror(e)) of every pair, k < m
-  const int64_t* npair;   // number of pairs (device scalar)
-};
-
-// powfancy7th(x) - 1 for x = 1 + eps, src/gpukernels_sph.jl:499-515.  Where
-// |eps| <= PF7_EPS_MAX the exact Taylor series of that iteration's output
-// (gen_pf7_series.py, bias included) replaces its two divisions; elsewhere
-// the iteration itself runs.  eps is taken as (1 + eps) - 1, the argument the
-// reference's rounded x carries.  Callers form ρ0 (1 + r) - ρ0 as the
-// reference forms ρ0 t - ρ0: 1 + r rounds to the t the iteration returns.
-__device__ inline double pf7m1_fast(double eps_in, double ginv, int gamma) {
-  const double x = 1.0 + eps_in;
-  const double e = x - 1.0;  // exact for x in [0.5, 2]
-  if (gamma == 7 && fabs(e) <= PF7_EPS_MAX) {
-    const double cu[PF7_UP_N] = PF7_UP_C;
-    const double cl[PF7_LO_N] = PF7_LO_C;
-    static_assert(PF7_UP_N == PF7_LO_N, "series lengths");
-    const bool up = e >= 0.0;
-    double r = up ? cu[PF7_UP_N - 1] : cl[PF7_UP_N - 1];
-#pragma unroll
-    for (int i = PF7_UP_N - 2; i >= 0; --i) r = fma(r, e, up ? cu[i] : cl[i]);
-    return r;
-  }
-  return powfancy7th_1div(x, ginv, gamma) - 1.0;
-}
-
-// all momentum terms of one pair (FAST expressions), summed into f
-template <int D>
-__device__ inline void pair_force_fast(const StepConst& c, int ptk, int ptm, const double* dx, double r2,
-                                       double inv_r2eta, const double* gw, const double* dv, double rk, double rm,
-                                       double irk, double irm, double Pk, double Pm, double* f) {
-  Acc<D> A;
-  A.zero();
-  mom_terms_fast<D>(c, A, ptk, ptm, dx, inv_r2eta, gw, dv, rk, rm, irk, irm, Pk, Pm);
-#pragma unroll
-  for (int d = 0; d < D; ++d) f[d] = (A.p[d] + A.av[d]) + (c.use_visc ? A.vi[d] : 0.0);
-}
-
-template <int D, int STAGE>
-__device__ inline void pair_tail_terms(const StepConst& c, int ptk, int ptm, const double* dxf, const double* dx,
-                                       double r, double* f) {
-  Acc<D> A;
-  A.zero();
-  fb_term<D>(c, A, ptk, ptm, dxf, dotD<D>(dxf, dxf));
-  if (c.use_pF) pf_term<D>(c, A, ptk, ptm, dx, r);
-#pragma unroll
-  for (int d = 0; d < D; ++d) f[d] = (f[d] + A.fb[d]) + (c.use_pF ? A.pf[d] : 0.0);
-}
-
-template <int D, int STAGE>
-__global__ void __launch_bounds__(STPB) k_pairA(StepConst c, SArr<D> S, PairBuf B) {
-  if (*S.ovf) return;
-  const int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (u >= *B.npair) return;
-  const int4 q = B.pq[u];
-  const int k = q.x, m = q.y, e = q.z, me = q.w;
-  // stage 1 at (x, ρ, v, P(ρ)); stage 2 at (xΔt½, ρΔt½, vΔt½, P(ρΔt½)) with stage-1 ∇W, fb at x
-  const double* const* XP = STAGE == 1 ? S.x : S.xh;
-  const double* const* VP = STAGE == 1 ? S.v : S.vh;
-  const double* RP = STAGE == 1 ? S.rho : S.rhoh;
-  const double* PP = STAGE == 1 ? S.P1 : S.P2;
-  const double* IP = STAGE == 1 ? S.ir : S.irh;
-  double dx[D], dv[D], gw[D];
-#pragma unroll
-  for (int d = 0; d < D; ++d) {
-    dx[d] = XP[d][k] - XP[d][m];
-    dv[d] = VP[d][k] - VP[d][m];
-  }
-  const double r2 = dotD<D>(dx, dx);
-  double r;
-  if (STAGE == 1) {
-    const double ri = rsqrt(r2);
-    r = r2 > 0.0 ? r2 * ri : 0.0;
-    const double u1 = r * c.Hinv;
-    const double w = wc2_w(u1, c.nW);
-    const double dwk_r = wc2_dw(u1, c.nDW) * ri;
-    S.We[e] = w;
-    S.We[me] = w;
-#pragma unroll
-    for (int d = 0; d < D; ++d) {
-      gw[d] = dx[d] * dwk_r;
-      S.gWe[d][e] = gw[d];
-      S.gWe[d][me] = -gw[d];
-    }
-  } else {
-    r = c.use_pF ? (r2 > 0.0 ? r2 * rsqrt(r2) : 0.0) : 0.0;
-#pragma unroll
-    for (int d = 0; d < D; ++d) gw[d] = S.gWe[d][e];
-  }
-  const int ptk = S.pt[k], ptm = S.pt[m];
-  const double rk = RP[k], rm = RP[m], irk = IP[k], irm = IP[m];
-  const bool both = ptk > 0 && ptm > 0;
-  double dk = 0.0, dm = 0.0;
-  const double inv_r2eta = both ? 1.0 / (r2 + c.eta2) : 0.0;
-  if (both) {
-    // ∂ρ∂tDDT!, src/gpukernels_sph.jl:520-575, both sides of the pair
-    const double dot3 = -dotD<D>(dx, gw);
-    const double m0dot = c.m0 * dotD<D>(dv, gw);
-    dk = m0dot;
-    dm = m0dot;
-    const double ez = c.DDTgz * dx[1];
-    if (ptk > 1) {
-      const double dp = c.rho0 * (1.0 + pf7m1_fast(ez, c.ginv, c.gamma)) - c.rho0;
-      dk += c.DDTkh * ((rm - rk) - dp) * inv_r2eta * dot3 * c.m0 * irm;
-    }
-    if (ptm > 1) {
-      const double dn = c.rho0 * (1.0 + pf7m1_fast(-ez, c.ginv, c.gamma)) - c.rho0;
-      dm += c.DDTkh * ((rk - rm) - dn) * inv_r2eta * dot3 * c.m0 * irk;
-    }
-  }
-  double f[D];
-  pair_force_fast<D>(c, ptk, ptm, dx, r2, inv_r2eta, gw, dv, rk, rm, irk, irm, PP[k], PP[m], f);
-  double dxf[D];
-#pragma unroll
-  for (int d = 0; d < D; ++d) dxf[d] = STAGE == 1 ? dx[d] : S.x[d][k] - S.x[d][m];
-  pair_tail_terms<D, STAGE>(c, ptk, ptm, dxf, dx, r, f);
-  B.cd[e] = dk;
-  B.cd[me] = dm;
-#pragma unroll
-  for (int d = 0; d < D; ++d) {
-    B.ca[d][e] = f[d];
-    B.ca[d][me] = -f[d];
-  }
-}
-
-// row sums of the per-entry contributions of particle k, L lanes
-template <int D, int L>
-__device__ inline void row_sums(const SArr<D>& S, const PairBuf& B, int64_t k, int lane, unsigned gm, double& drho,
-                                double* a) {
-  drho = 0.0;
-#pragma unroll
-  for (int d = 0; d < D; ++d) a[d] = 0.0;
-  const int64_t e0 = S.rs[k], e1 = S.rs[k + 1];
-  for (int64_t e = e0 + lane; e < e1; e += L) {
-    drho += B.cd[e];
-#pragma unroll
-    for (int d = 0; d < D; ++d) a[d] += B.ca[d][e];
-  }
-  drho = group_sum<L>(drho, gm);
-#pragma unroll
-  for (int d = 0; d < D; ++d) a[d] = group_sum<L>(a[d], gm);
-}
-
-// pass B, stage 1: row sums + the three half-step predictors
-template <int D, int L>
-__global__ void __launch_bounds__(STPB) k_pairB1(StepConst c, const Scal* __restrict__ sc, int64_t N, SArr<D> S,
-                                                 PairBuf B) {
-  if (*S.ovf) return;
-  const int64_t gt = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const int64_t k = gt / L;
-  const int lane = (int)(gt % L);
-  if (k >= N) return;  // whole sub-group leaves together
-  double drho, a[D];
-  row_sums<D, L>(S, B, k, lane, group_mask<L>(), drho, a);
-  if (lane != 0) return;
-  a[1] = a[1] - c.g;
-  const int ptk = S.pt[k];
-  const double hdt = sc->dt * 0.5;
-  double rv = S.rhoh[k] + drho * hdt;
-  if (rv < c.rho0 && ptk < 0) rv = c.rho0;
-  S.rhoh[k] = rv;
-#pragma unroll
-  for (int d = 0; d < D; ++d) {
-    double vh = S.vh[d][k];
-    if (ptk > 1) vh = vh + a[d] * hdt;
-    S.vh[d][k] = vh;
-    S.xh[d][k] = S.xh[d][k] + vh * hdt;
-  }
-  S.P2[k] = eos(rv, c.gamma, c.rho0, c.P0, ptk);
-  S.irh[k] = 1.0 / rv;
-}
-
-// pass B, stage 2: row sums + symplectic_update! + max |cΔx|
-template <int D, int L>
-__global__ void __launch_bounds__(STPB) k_pairB2(StepConst c, Scal* __restrict__ sc, int64_t N, SArr<D> S,
-                                                 PairBuf B) {
-  if (*S.ovf) return;  // uniform over the grid, before the block reduction below
-  const int64_t gt = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const int64_t k = gt / L;
-  const int lane = (int)(gt % L);
-  double mc = 0.0;
-  if (k < N) {
-    double drho, a[D];
-    row_sums<D, L>(S, B, k, lane, group_mask<L>(), drho, a);
-    if (lane == 0) {
-      const double dt = sc->dt;
-      a[1] = a[1] - c.g;
-      const int ptk = S.pt[k];
-      S.drho[k] = drho;
-      S.Plast[k] = S.P2[k];
-      const double epsi = -(drho / S.rhoh[k]) * dt;
-      double rv = S.rho[k] * (2.0 - epsi) / (2.0 + epsi);
-      if (rv < c.rho0 && ptk <= 1) rv = c.rho0;
-      S.rho[k] = rv;
-      S.rhoho[k] = rv;
-      S.P1[k] = eos(rv, c.gamma, c.rho0, c.P0, ptk);
-      S.ir[k] = 1.0 / rv;
-      const double ml = ptk > 1 ? 1.0 : 0.0;
-#pragma unroll
-      for (int d = 0; d < D; ++d) {
-        S.a[d][k] = a[d];
-        const double vv = S.v[d][k];
-        const double nv = vv + a[d] * dt * ml;
-        S.vho[d][k] = nv;
-        S.v[d][k] = nv;
-        const double ddx = (vv + nv) * 0.5 * dt;
-        const double cd = S.cdx[d][k] + ddx;
-        S.cdx[d][k] = cd;
-        mc = fmax(mc, fabs(cd));
-        const double xv = S.x[d][k] + ddx;
-        S.xho[d][k] = xv;
-        S.xo[d][k] = xv;
-      }
-    }
-  }
   mc = warp_max(mc);
   __shared__ double smax[STPB / 32];
   if ((threadIdx.x & 31) == 0) smax[threadIdx.x >> 5] = mc;
@@ -894,7 +377,22 @@ __global__ void __launch_bounds__(STPB) k_dt_reduce(StepConst c, Scal* __restric
 #pragma unroll
     for (int d = 0; d < D; ++d) { av[d] = S.a[d][k]; vv[d] = S.v[d][k]; pp[d] = S.x[d][k]; }
     am = sqrt(dotD<D>(av, av));
-    vm = fabs(c.h * dotD<D>(vv, pp) / (dotD<D>(pp, pp) + c.dt_eta2));
+    if (!c.dt_relative) {
+      // as written at src/gpukernels_sph.jl:1316-1326: absolute positions and velocities
+      vm = fabs(c.h * dotD<D>(vv, pp) / (dotD<D>(pp, pp) + c.dt_eta2));
+    } else {
+      // the viscous time-step bound over pairs: max |h Δv·Δx / (|Δx|² + η²)|
+      for (int64_t e = S.rs[k]; e < S.rs[k + 1]; ++e) {
+        const int32_t m = S.nbr[e];
+        double dx[D], dv[D];
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+          dx[d] = pp[d] - S.x[d][m];
+          dv[d] = vv[d] - S.v[d][m];
+        }
+        vm = fmax(vm, fabs(c.h * dotD<D>(dv, dx) / (dotD<D>(dx, dx) + c.dt_eta2)));
+      }
+    }
   }
   am = warp_max(am);
   vm = warp_max(vm);
@@ -1093,7 +591,7 @@ struct HostSide {
 };
 
 struct GraphKey {
-  int32_t n, timestepping, lanes, timing;
+  int32_t n, timestepping, lanes, timing, dt_relative, pad;
   double tmin, tmax;
   gcsph_params prm;  // dt and etime zeroed: they live on the device
   int64_t nbr_cap, we_cap, gen;
@@ -1140,6 +638,7 @@ struct sph_handle {
   Scal* pin = nullptr;
   bool in_cell_order = false;
   bool use_graphs = true;
+  int dt_relative = 0;
   StepGraph graphs[4];
   unsigned long long graph_clock = 0;
   int64_t n_captures = 0, n_replays = 0;
@@ -1381,20 +880,18 @@ static int rebuild(sph_handle* h, const StepConst& c, int* ovf_dev) {
 
 // pass A: one thread per pair, the grid sized by the entry capacity (the
 // pair count itself stays on the device)
+// pass A: one thread per pair, the grid sized by the entry capacity (the
+// pair count itself stays on the device); pass B: L lanes per row
 #define PAIRA_LAUNCH(STAGE, ...)                                                              \
-  k_pairA<D, STAGE><<<nblocks(h->cl->core.nbr_cap / 2 + 1, STPB), STPB, 0, st>>>(__VA_ARGS__)
-
-// pass B: L lanes per row
-#define PAIRB_LAUNCH(KER, L, ...)                                                             \
   do {                                                                                        \
-    const int _g = nblocks(h->N * (int64_t)(L), STPB);                                        \
-    switch (L) {                                                                              \
-      case 2: KER<D, 2><<<_g, STPB, 0, st>>>(__VA_ARGS__); break;                             \
-      case 4: KER<D, 4><<<_g, STPB, 0, st>>>(__VA_ARGS__); break;                             \
-      case 8: KER<D, 8><<<_g, STPB, 0, st>>>(__VA_ARGS__); break;                             \
-      case 16: KER<D, 16><<<_g, STPB, 0, st>>>(__VA_ARGS__); break;                           \
-      default: KER<D, 32><<<_g, STPB, 0, st>>>(__VA_ARGS__); break;                           \
-    }                                                                                         \
+    const int _rc = launch_pairA<D>(STAGE, h->cl->core.nbr_cap / 2 + 1, st, __VA_ARGS__);     \
+    if (_rc) return _rc;                                                                      \
+  } while (0)
+
+#define PAIRB_LAUNCH(STAGE, L, ...)                                                           \
+  do {                                                                                        \
+    const int _rc = launch_pairB<D>(STAGE, L, h->N, st, __VA_ARGS__);                        \
+    if (_rc) return _rc;                                                                      \
   } while (0)
 
 static int choose_lanes(const sph_handle* h) {
@@ -1449,11 +946,9 @@ static int enqueue_stages(sph_handle* h, StepConst& c, Scal* dsc, int32_t& cspmc
   if (once) {
     timer_begin(T_STAGE1, st);
     PAIRA_LAUNCH(1, c, make_arr<D>(h), make_pairbuf<D>(h));
-    GC_LAUNCHED();
     timer_end(T_STAGE1, st);
     timer_begin(T_ROWSUM, st);
-    PAIRB_LAUNCH(k_pairB1, L, c, dsc, h->N, make_arr<D>(h), make_pairbuf<D>(h));
-    GC_LAUNCHED();
+    PAIRB_LAUNCH(1, L, c, dsc, make_arr<D>(h), make_pairbuf<D>(h));
     timer_end(T_ROWSUM, st);
   } else {
     timer_begin(T_STAGE1, st);
@@ -1467,11 +962,9 @@ static int enqueue_stages(sph_handle* h, StepConst& c, Scal* dsc, int32_t& cspmc
   if (once) {
     timer_begin(T_STAGE2, st);
     PAIRA_LAUNCH(2, c, make_arr<D>(h), make_pairbuf<D>(h));
-    GC_LAUNCHED();
     timer_end(T_STAGE2, st);
     timer_begin(T_ROWSUM, st);
-    PAIRB_LAUNCH(k_pairB2, L, c, dsc, h->N, make_arr<D>(h), make_pairbuf<D>(h));
-    GC_LAUNCHED();
+    PAIRB_LAUNCH(2, L, c, dsc, make_arr<D>(h), make_pairbuf<D>(h));
     timer_end(T_ROWSUM, st);
   } else {
     timer_begin(T_STAGE2, st);
@@ -1536,7 +1029,6 @@ static int step_eager(sph_handle* h, StepConst c, int32_t n, int64_t* updaten_ou
   Scal* dsc = h->scal.as<Scal>();
   init_scal(h, n);
   GC_CUDA(cudaMemcpyAsync(dsc, h->pin, sizeof(Scal), cudaMemcpyHostToDevice, st));
-  const gcsph_params& p = h->prm;
   bool skip = false;
   int64_t updaten = 0;
   double maxout = 0.0;
@@ -1662,6 +1154,7 @@ static GraphKey graph_key(const sph_handle* h, int32_t n, int timestepping, doub
   k.timestepping = timestepping;
   k.lanes = choose_lanes(h);
   k.timing = timing_on() ? 1 : 0;
+  k.dt_relative = h->dt_relative;
   k.tmin = timestepping ? tmin : 0.0;
   k.tmax = timestepping ? tmax : 0.0;
   k.prm = h->prm;
@@ -1803,6 +1296,7 @@ static int step_impl(sph_handle* h, int32_t n, int timestepping, double tmin, do
   c.tmin = tmin;
   c.tmax = tmax;
   c.reb_thr = 0.9 * h->prm.nui;
+  c.dt_relative = h->dt_relative;
   bool done = false;
   int rc = step_graph<D>(h, c, n, timestepping, tmin, tmax, updaten_out, maxcdx_out, &done);
   if (rc || done) return rc;
@@ -1940,6 +1434,12 @@ int sph_set_params(sph_handle* h, const gcsph_params* prm) {
 int sph_set_graphs(sph_handle* h, int32_t on) {
   if (!h) return fail(GCSPH_EINVAL, "null handle");
   h->use_graphs = on != 0;
+  return GCSPH_OK;
+}
+
+int sph_set_dt_variant(sph_handle* h, int32_t relative) {
+  if (!h) return fail(GCSPH_EINVAL, "null handle");
+  h->dt_relative = relative != 0;
   return GCSPH_OK;
 }
 

@@ -121,6 +121,12 @@ class SPHProblem:
         every step (default on); off runs one host round trip per step."""
         _lib.check(_lib.load().sph_set_graphs(self._h, int(bool(on))))
 
+    def set_dt_variant(self, relative: bool):
+        """Δt_stepping's velocity term: False (default) as the reference writes
+        it (absolute v·x per particle), True the pair-relative bound
+        max |h Δv·Δx / (|Δx|² + η²)|."""
+        _lib.check(_lib.load().sph_set_dt_variant(self._h, int(bool(relative))))
+
     def graph_stats(self):
         """(graphs captured, calls replayed as a graph) so far."""
         a, b = C.c_int64(), C.c_int64()

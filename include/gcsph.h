@@ -165,6 +165,11 @@ int sph_set_lanes(sph_handle* h, int32_t lanes);
  * identical to the per-step loop; a neighbour overflow inside the graph
  * falls back to that loop for the call.  0 turns capture off. */
 int sph_set_graphs(sph_handle* h, int32_t on);
+/* Δt_stepping's velocity term (src/gpukernels_sph.jl:1316-1326) uses the
+ * absolute v·x / (x·x + η²) of each particle, as written.  relative = 1 uses
+ * the viscous time-step bound over pairs instead, max |h Δv·Δx / (|Δx|² + η²)|
+ * (no reference counterpart; default 0, the reference's formula). */
+int sph_set_dt_variant(sph_handle* h, int32_t relative);
 /* How many graphs were captured and how many calls ran as a graph replay. */
 int sph_graph_stats(const sph_handle* h, int64_t* captures, int64_t* replays);
 
