@@ -470,7 +470,9 @@ def run_gb300(args):
         L.gcsph_timing_get(tid, C.byref(n_), C.byref(t_))
         fam[L.gcsph_timing_name(tid).decode()] = (int(n_.value), float(t_.value))
     L.gcsph_timing_enable(0)
-    top = max(fam, key=lambda k: fam[k][1])
+    # the roofline covers the pair-sum kernel (pass A, stage 1), the hottest single kernel; the
+    # neighbour build is a family of six short kernels (its split is in kernel_ms)
+    top = "stage1" if fam.get("stage1", (0, 0))[0] else max(fam, key=lambda k: fam[k][1])
     npairs = system.pairsn
     # ---------------- end-to-end through the public API with host buffers
     hx = torch.empty((D, N), dtype=torch.float64).pin_memory()

@@ -69,6 +69,12 @@ struct EnsArr {
   float* offn[3];            // x - cell corner after the corrector (dpcreg!)
   float* dxb[3];             // xΔt½ base - x: dpcreg!/xsphcorr! move x, not xΔt½
   float* dvb[3];             // vΔt½ base - v: dpcreg! moves v, not vΔt½
+  int* nl;                   // neighbour list of the step, entry-major (q * ncap + i)
+  int* nlc;                  // entries per particle
+  int64_t ncap;              // particle capacity (the list's row pitch)
+  int nls;                   // entries per particle the list holds
+  int* ovf;                  // a row outgrew nls: every later kernel of the call skips
+  int* nlmax;                // the longest row seen (to size the next try)
 };
 
 struct KSum {
@@ -204,28 +210,33 @@ __global__ void k_ens_permute(int64_t N, const int32_t* __restrict__ perm, const
 }
 
 // ---------------------------------------------------------------------------
-// the two pair passes (cell walk), persistent grid-stride loops
+// neighbour list of the step, built once after the re-sort: the 3^D cell walk
+// with the pair test r < H at x (FP32 offsets), each entry the neighbour's
+// index packed with its cell shift ((dx+1) + 3(dy+1) + 9(dz+1) in the low 5
+// bits).  Stored entry-major (entry q of particle i at q*ncap + i) so that the
+// passes' loads coalesce.  A row that outgrows the stride raises *ovf: every
+// later kernel of the call skips, the host grows the stride and repeats.
 // ---------------------------------------------------------------------------
-template <int D, int STAGE>
-__global__ void __launch_bounds__(ENS_MAX_TPB) k_ens_stage(EnsArr A, const EnsInst* __restrict__ T) {
+__device__ __forceinline__ void shift_of(int ent, const EnsInst& I, float& sx, float& sy, float& sz) {
+  const int code = ent & 31;
+  const int ex = code % 3, r = code / 3;
+  sx = (float)(ex - 1) * I.csf;
+  sy = (float)(r % 3 - 1) * I.csf;
+  sz = (float)(r / 3 - 1) * I.csf;
+}
+
+template <int D>
+__global__ void __launch_bounds__(ENS_MAX_TPB) k_ens_nlist(EnsArr A, const EnsInst* __restrict__ T) {
+  if (*A.ovf) return;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < A.N; i += stride) {
     const EnsInst& I = T[A.inst[i]];
     int cx0, cy0, cz0;
     cell_of(A.skey[i], I, cx0, cy0, cz0);
-    float oi[D], ohi[D], vi[D];
+    float oi[D];
 #pragma unroll
-    for (int d = 0; d < D; ++d) {
-      oi[d] = A.off[d][i];
-      ohi[d] = STAGE == 1 ? oi[d] : A.offh[d][i];
-      vi[d] = STAGE == 1 ? A.v[d][i] : A.vh[d][i];
-    }
-    const int pti = A.pt[i];
-    const float dri = STAGE == 1 ? A.dr[i] : A.drh[i];
-    const float rhoi = I.rho0 + dri;
-    const float Pi = eos32(dri, pti, I);
-    const int fbs = STAGE - 1;
-    KSum drho, acc[D];
+    for (int d = 0; d < D; ++d) oi[d] = A.off[d][i];
+    int cnt = 0;
     const int zlo = D == 3 ? -1 : 0, zhi = D == 3 ? 1 : 0;
     for (int dz = zlo; dz <= zhi; ++dz) {
       const int cz = cz0 + dz;
@@ -239,87 +250,130 @@ __global__ void __launch_bounds__(ENS_MAX_TPB) k_ens_stage(EnsArr A, const EnsIn
           if (cx < 0 || cx >= I.nc[0]) continue;
           const int j0 = A.cellstart[row + cx], j1 = A.cellstart[row + cx + 1];
           const float shx = (float)dxc * I.csf, shy = (float)dy * I.csf, shz = (float)dz * I.csf;
+          const int code = (dxc + 1) + 3 * (dy + 1) + 9 * (dz + 1);
           for (int j = j0; j < j1; ++j) {
             if (j == i) continue;
             float d[D];
 #pragma unroll
             for (int q = 0; q < D; ++q) d[q] = (oi[q] - A.off[q][j]) - (q == 0 ? shx : (q == 1 ? shy : shz));
-            const float r2 = dot32<D>(d, d);
-            if (!(r2 < I.H2)) continue;
-            // sph∇W!: W'(r)/r of WendlandC2 = -20 nDW Hinv (1-q)^3
-            const float r = sqrtf(r2);
-            const float u = r * I.Hinv;
-            const float t = u < 1.f ? 1.f - u : 0.f;
-            const float dwr = -20.f * I.nDW * I.Hinv * (t * t * t);
-            float gw[D], dd[D], dv[D];
-#pragma unroll
-            for (int q = 0; q < D; ++q) {
-              gw[q] = d[q] * dwr;
-              dd[q] = STAGE == 1 ? d[q] : (ohi[q] - A.offh[q][j]) - (q == 0 ? shx : (q == 1 ? shy : shz));
-              dv[q] = vi[q] - (STAGE == 1 ? A.v[q][j] : A.vh[q][j]);
-            }
-            const float r2d = STAGE == 1 ? r2 : dot32<D>(dd, dd);
-            const int ptj = A.pt[j];
-            const float drj = STAGE == 1 ? A.dr[j] : A.drh[j];
-            const float rhoj = I.rho0 + drj;
-            const bool both = pti > 0 && ptj > 0;
-            const float inv = 1.f / (r2d + I.eta2);
-            float f[D];
-#pragma unroll
-            for (int q = 0; q < D; ++q) f[q] = 0.f;
-            if (both) {
-              // ∂ρ∂tDDT!
-              float term = I.m0 * dot32<D>(dv, gw);
-              if (pti > 1) {
-                const float dp = I.rho0 * root_m1(I.DDTgz * dd[1], I);
-                term += I.DDTkh * ((drj - dri) - dp) * inv * (-dot32<D>(dd, gw)) * I.m0 / rhoj;
-              }
-              drho.add(term);
-            }
-            if (pti * ptj > 0) {
-              // ∂v∂t!
-              const float sc = -I.m0 * (Pi + eos32(drj, ptj, I)) / (rhoi * rhoj);
-#pragma unroll
-              for (int q = 0; q < D; ++q) f[q] = sc * gw[q];
-            }
-            if (both) {
-              const float cond = dot32<D>(dv, dd);
-              if (cond < 0.f) {
-                // ∂v∂t_av!
-                const float dmu = I.h * cond * inv;
-                const float dPi = (-I.alpha * I.c0 * dmu) / ((rhoi + rhoj) * 0.5f);
-#pragma unroll
-                for (int q = 0; q < D; ++q) f[q] += -dPi * I.m0 * gw[q];
-              }
-              if (I.use_visc) {
-                // ∂v∂t_visc!
-                const float nt = 4.f * I.nu * I.m0 * dot32<D>(dd, gw) / (rhoi + rhoj) * inv;
-#pragma unroll
-                for (int q = 0; q < D; ++q) f[q] += nt * dv[q];
-              }
-              if (I.use_pF) {
-                // ∂v∂tpF!
-                const float rd = sqrtf(r2d);
-                if (rd < I.twoh) {
-                  const float scos = I.s * __cosf(I.pfc * rd / I.twoh) / (rd + I.hp1);  // argument in [0, 1.5π)
-#pragma unroll
-                  for (int q = 0; q < D; ++q) f[q] += scos * dd[q] / I.m0;
-                }
-              }
-            }
-            if ((pti > 0) != (ptj > 0) && r < I.fb_r0[fbs]) {
-              // fbmolforce! at x
-              const float qq = I.fb_r0[fbs] / (r + I.fb_eta2[fbs]);
-              const float q2 = qq * qq, q4 = q2 * q2, q8 = q4 * q4;
-              const float Fc = I.fb_d[fbs] * (q8 * q4 - q4) / (r2 + I.fb_eta2[fbs]);
-#pragma unroll
-              for (int q = 0; q < D; ++q) f[q] += d[q] * Fc;
-            }
-#pragma unroll
-            for (int q = 0; q < D; ++q) acc[q].add(f[q]);
+            if (!(dot32<D>(d, d) < I.H2)) continue;
+            if (cnt < A.nls) A.nl[(int64_t)cnt * A.ncap + i] = (j << 5) | code;
+            ++cnt;
           }
         }
       }
+    }
+    A.nlc[i] = cnt < A.nls ? cnt : A.nls;
+    if (cnt > A.nls) {
+      atomicMax(A.nlmax, cnt);
+      *A.ovf = 1;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// the two pair passes over the step's neighbour list, persistent grid-stride
+// ---------------------------------------------------------------------------
+template <int D, int STAGE>
+__global__ void __launch_bounds__(ENS_MAX_TPB) k_ens_stage(EnsArr A, const EnsInst* __restrict__ T) {
+  if (*A.ovf) return;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < A.N; i += stride) {
+    const EnsInst& I = T[A.inst[i]];
+    float oi[D], ohi[D], vi[D];
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      oi[d] = A.off[d][i];
+      ohi[d] = STAGE == 1 ? oi[d] : A.offh[d][i];
+      vi[d] = STAGE == 1 ? A.v[d][i] : A.vh[d][i];
+    }
+    const int pti = A.pt[i];
+    const float dri = STAGE == 1 ? A.dr[i] : A.drh[i];
+    const float rhoi = I.rho0 + dri;
+    const float Pi = eos32(dri, pti, I);
+    const int fbs = STAGE - 1;
+    KSum drho, acc[D];
+    const int nn = A.nlc[i];
+    for (int e = 0; e < nn; ++e) {
+      const int ent = A.nl[(int64_t)e * A.ncap + i];
+      const int j = ent >> 5;
+      float shx, shy, shz;
+      shift_of(ent, I, shx, shy, shz);
+      float d[D];
+#pragma unroll
+      for (int q = 0; q < D; ++q) d[q] = (oi[q] - A.off[q][j]) - (q == 0 ? shx : (q == 1 ? shy : shz));
+      const float r2 = dot32<D>(d, d);
+      // sph∇W!: W'(r)/r of WendlandC2 = -20 nDW Hinv (1-q)^3
+      const float r = sqrtf(r2);
+      const float u = r * I.Hinv;
+      const float t = u < 1.f ? 1.f - u : 0.f;
+      const float dwr = -20.f * I.nDW * I.Hinv * (t * t * t);
+      float gw[D], dd[D], dv[D];
+#pragma unroll
+      for (int q = 0; q < D; ++q) {
+        gw[q] = d[q] * dwr;
+        dd[q] = STAGE == 1 ? d[q] : (ohi[q] - A.offh[q][j]) - (q == 0 ? shx : (q == 1 ? shy : shz));
+        dv[q] = vi[q] - (STAGE == 1 ? A.v[q][j] : A.vh[q][j]);
+      }
+      const float r2d = STAGE == 1 ? r2 : dot32<D>(dd, dd);
+      const int ptj = A.pt[j];
+      const float drj = STAGE == 1 ? A.dr[j] : A.drh[j];
+      const float rhoj = I.rho0 + drj;
+      const bool both = pti > 0 && ptj > 0;
+      const float inv = 1.f / (r2d + I.eta2);
+      float f[D];
+#pragma unroll
+      for (int q = 0; q < D; ++q) f[q] = 0.f;
+      if (both) {
+        // ∂ρ∂tDDT!
+        float term = I.m0 * dot32<D>(dv, gw);
+        if (pti > 1) {
+          const float dp = I.rho0 * root_m1(I.DDTgz * dd[1], I);
+          term += I.DDTkh * ((drj - dri) - dp) * inv * (-dot32<D>(dd, gw)) * I.m0 / rhoj;
+        }
+        drho.add(term);
+      }
+      if (pti * ptj > 0) {
+        // ∂v∂t!
+        const float sc = -I.m0 * (Pi + eos32(drj, ptj, I)) / (rhoi * rhoj);
+#pragma unroll
+        for (int q = 0; q < D; ++q) f[q] = sc * gw[q];
+      }
+      if (both) {
+        const float cond = dot32<D>(dv, dd);
+        if (cond < 0.f) {
+          // ∂v∂t_av!
+          const float dmu = I.h * cond * inv;
+          const float dPi = (-I.alpha * I.c0 * dmu) / ((rhoi + rhoj) * 0.5f);
+#pragma unroll
+          for (int q = 0; q < D; ++q) f[q] += -dPi * I.m0 * gw[q];
+        }
+        if (I.use_visc) {
+          // ∂v∂t_visc!
+          const float nt = 4.f * I.nu * I.m0 * dot32<D>(dd, gw) / (rhoi + rhoj) * inv;
+#pragma unroll
+          for (int q = 0; q < D; ++q) f[q] += nt * dv[q];
+        }
+        if (I.use_pF) {
+          // ∂v∂tpF!
+          const float rd = sqrtf(r2d);
+          if (rd < I.twoh) {
+            const float scos = I.s * __cosf(I.pfc * rd / I.twoh) / (rd + I.hp1);  // argument in [0, 1.5π)
+#pragma unroll
+            for (int q = 0; q < D; ++q) f[q] += scos * dd[q] / I.m0;
+          }
+        }
+      }
+      if ((pti > 0) != (ptj > 0) && r < I.fb_r0[fbs]) {
+        // fbmolforce! at x
+        const float qq = I.fb_r0[fbs] / (r + I.fb_eta2[fbs]);
+        const float q2 = qq * qq, q4 = q2 * q2, q8 = q4 * q4;
+        const float Fc = I.fb_d[fbs] * (q8 * q4 - q4) / (r2 + I.fb_eta2[fbs]);
+#pragma unroll
+        for (int q = 0; q < D; ++q) f[q] += d[q] * Fc;
+      }
+#pragma unroll
+      for (int q = 0; q < D; ++q) acc[q].add(f[q]);
     }
     float a[D];
 #pragma unroll
@@ -367,6 +421,7 @@ __global__ void __launch_bounds__(ENS_MAX_TPB) k_ens_stage(EnsArr A, const EnsIn
 // update_dpcreg! (:1617-1632)
 template <int D>
 __global__ void __launch_bounds__(ENS_MAX_TPB) k_ens_dpc(EnsArr A, const EnsInst* __restrict__ T) {
+  if (*A.ovf) return;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < A.N; i += stride) {
     const EnsInst& I = T[A.inst[i]];
@@ -374,64 +429,46 @@ __global__ void __launch_bounds__(ENS_MAX_TPB) k_ens_dpc(EnsArr A, const EnsInst
     const int pti = A.pt[i];
     KSum sum[D];
     if (pti > 0) {
-      int cx0, cy0, cz0;
-      cell_of(A.skey[i], I, cx0, cy0, cz0);
-      float oi[D], ni[D], vi[D];
+      float ni[D], vi[D];
 #pragma unroll
       for (int d = 0; d < D; ++d) {
-        oi[d] = A.off[d][i];
         ni[d] = A.offn[d][i];
         vi[d] = A.v[d][i];
       }
       const float dri = A.dr[i];
       const float rhoi = I.rho0 + dri, Pi = eos32(dri, pti, I);
       const float dt = (float)I.dt;
-      const int zlo = D == 3 ? -1 : 0, zhi = D == 3 ? 1 : 0;
-      for (int dz = zlo; dz <= zhi; ++dz) {
-        const int cz = cz0 + dz;
-        if (cz < 0 || cz >= I.nc[2]) continue;
-        for (int dy = -1; dy <= 1; ++dy) {
-          const int cy = cy0 + dy;
-          if (cy < 0 || cy >= I.nc[1]) continue;
-          const int row = I.key_off + I.nc[0] * (cy + I.nc[1] * cz);
-          for (int dxc = -1; dxc <= 1; ++dxc) {
-            const int cx = cx0 + dxc;
-            if (cx < 0 || cx >= I.nc[0]) continue;
-            const int j0 = A.cellstart[row + cx], j1 = A.cellstart[row + cx + 1];
-            const float shx = (float)dxc * I.csf, shy = (float)dy * I.csf, shz = (float)dz * I.csf;
-            for (int j = j0; j < j1; ++j) {
-              const int ptj = A.pt[j];
-              if (j == i || !(ptj > 0)) continue;
-              float d[D];
+      const int nn = A.nlc[i];
+      for (int e = 0; e < nn; ++e) {
+        const int ent = A.nl[(int64_t)e * A.ncap + i];
+        const int j = ent >> 5;
+        const int ptj = A.pt[j];
+        if (!(ptj > 0)) continue;
+        float shx, shy, shz;
+        shift_of(ent, I, shx, shy, shz);
+        float dx[D], dv[D];
 #pragma unroll
-              for (int q = 0; q < D; ++q) d[q] = (oi[q] - A.off[q][j]) - (q == 0 ? shx : (q == 1 ? shy : shz));
-              if (!(dot32<D>(d, d) < I.H2)) continue;  // the step's pair set
-              float dx[D], dv[D];
-#pragma unroll
-              for (int q = 0; q < D; ++q) {
-                dx[q] = (ni[q] - A.offn[q][j]) - (q == 0 ? shx : (q == 1 ? shy : shz));
-                dv[q] = vi[q] - A.v[q][j];
-              }
-              const float drj = A.dr[j];
-              const float rhoj = I.rho0 + drj;
-              const float r2 = dot32<D>(dx, dx);
-              const float u = sqrtf(r2) * I.dpc_l0inv;
-              const float t = u < 1.f ? 1.f - u : 0.f;
-              const float t2 = t * t;
-              const float w = (1.f + 4.f * u) * (t2 * t2) * I.dpc_nW;
-              const float chi = sqrtf(w * I.dpc_whinv);
-              const float kk = u < I.dpc_kernlim ? 1.f : chi;
-              const float Pb = chi * fmaxf(fminf(I.dpc_lambda * fabsf(Pi + eos32(drj, ptj, I)),
-                                                 I.dpc_lambda * I.dpc_pmax), I.dpc_pmin);
-              const float vr = dot32<D>(dv, dx);
-              float c;
-              if (vr < 0.f) c = kk * (-vr / (r2 + I.dpc_eta2));
-              else c = 2.f * dt * Pb / ((rhoi + rhoj) * (r2 + I.dpc_eta2));
-#pragma unroll
-              for (int q = 0; q < D; ++q) sum[q].add(c * dx[q]);
-            }
-          }
+        for (int q = 0; q < D; ++q) {
+          dx[q] = (ni[q] - A.offn[q][j]) - (q == 0 ? shx : (q == 1 ? shy : shz));
+          dv[q] = vi[q] - A.v[q][j];
         }
+        const float drj = A.dr[j];
+        const float rhoj = I.rho0 + drj;
+        const float r2 = dot32<D>(dx, dx);
+        const float u = sqrtf(r2) * I.dpc_l0inv;
+        const float t = u < 1.f ? 1.f - u : 0.f;
+        const float t2 = t * t;
+        const float w = (1.f + 4.f * u) * (t2 * t2) * I.dpc_nW;
+        const float chi = sqrtf(w * I.dpc_whinv);
+        const float kk = u < I.dpc_kernlim ? 1.f : chi;
+        const float Pb = chi * fmaxf(fminf(I.dpc_lambda * fabsf(Pi + eos32(drj, ptj, I)),
+                                           I.dpc_lambda * I.dpc_pmax), I.dpc_pmin);
+        const float vr = dot32<D>(dv, dx);
+        float c;
+        if (vr < 0.f) c = kk * (-vr / (r2 + I.dpc_eta2));
+        else c = 2.f * dt * Pb / ((rhoi + rhoj) * (r2 + I.dpc_eta2));
+#pragma unroll
+        for (int q = 0; q < D; ++q) sum[q].add(c * dx[q]);
       }
     }
 #pragma unroll
@@ -441,6 +478,7 @@ __global__ void __launch_bounds__(ENS_MAX_TPB) k_ens_dpc(EnsArr A, const EnsInst
 
 template <int D>
 __global__ void k_ens_dpc_apply(EnsArr A, const EnsInst* __restrict__ T) {
+  if (*A.ovf) return;
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= A.N) return;
   const EnsInst& I = T[A.inst[i]];
@@ -462,12 +500,11 @@ __global__ void k_ens_dpc_apply(EnsArr A, const EnsInst* __restrict__ T) {
 // moves x only.  Reads neighbours' v, writes its own x: one pass.
 template <int D>
 __global__ void __launch_bounds__(ENS_MAX_TPB) k_ens_xsph(EnsArr A, const EnsInst* __restrict__ T) {
+  if (*A.ovf) return;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < A.N; i += stride) {
     const EnsInst& I = T[A.inst[i]];
     if (!I.use_xsph || !(A.pt[i] > 1)) continue;
-    int cx0, cy0, cz0;
-    cell_of(A.skey[i], I, cx0, cy0, cz0);
     float oi[D], vi[D];
 #pragma unroll
     for (int d = 0; d < D; ++d) {
@@ -476,36 +513,23 @@ __global__ void __launch_bounds__(ENS_MAX_TPB) k_ens_xsph(EnsArr A, const EnsIns
     }
     const float rhoi = I.rho0 + A.dr[i];
     KSum sum[D];
-    const int zlo = D == 3 ? -1 : 0, zhi = D == 3 ? 1 : 0;
-    for (int dz = zlo; dz <= zhi; ++dz) {
-      const int cz = cz0 + dz;
-      if (cz < 0 || cz >= I.nc[2]) continue;
-      for (int dy = -1; dy <= 1; ++dy) {
-        const int cy = cy0 + dy;
-        if (cy < 0 || cy >= I.nc[1]) continue;
-        const int row = I.key_off + I.nc[0] * (cy + I.nc[1] * cz);
-        for (int dxc = -1; dxc <= 1; ++dxc) {
-          const int cx = cx0 + dxc;
-          if (cx < 0 || cx >= I.nc[0]) continue;
-          const int j0 = A.cellstart[row + cx], j1 = A.cellstart[row + cx + 1];
-          const float shx = (float)dxc * I.csf, shy = (float)dy * I.csf, shz = (float)dz * I.csf;
-          for (int j = j0; j < j1; ++j) {
-            if (j == i || !(A.pt[j] > 1)) continue;
-            float d[D];
+    const int nn = A.nlc[i];
+    for (int e = 0; e < nn; ++e) {
+      const int ent = A.nl[(int64_t)e * A.ncap + i];
+      const int j = ent >> 5;
+      if (!(A.pt[j] > 1)) continue;
+      float shx, shy, shz;
+      shift_of(ent, I, shx, shy, shz);
+      float d[D];
 #pragma unroll
-            for (int q = 0; q < D; ++q) d[q] = (oi[q] - A.off[q][j]) - (q == 0 ? shx : (q == 1 ? shy : shz));
-            const float r2 = dot32<D>(d, d);
-            if (!(r2 < I.H2)) continue;
-            const float u = sqrtf(r2) * I.Hinv;
-            const float t = u < 1.f ? 1.f - u : 0.f;
-            const float t2 = t * t;
-            const float w = (1.f + 4.f * u) * (t2 * t2) * I.nW;
-            const float xs = I.xsph_c * w / (rhoi + (I.rho0 + A.dr[j]));
+      for (int q = 0; q < D; ++q) d[q] = (oi[q] - A.off[q][j]) - (q == 0 ? shx : (q == 1 ? shy : shz));
+      const float u = sqrtf(dot32<D>(d, d)) * I.Hinv;
+      const float t = u < 1.f ? 1.f - u : 0.f;
+      const float t2 = t * t;
+      const float w = (1.f + 4.f * u) * (t2 * t2) * I.nW;
+      const float xs = I.xsph_c * w / (rhoi + (I.rho0 + A.dr[j]));
 #pragma unroll
-            for (int q = 0; q < D; ++q) sum[q].add((A.v[q][j] - vi[q]) * xs);
-          }
-        }
-      }
+      for (int q = 0; q < D; ++q) sum[q].add((A.v[q][j] - vi[q]) * xs);
     }
 #pragma unroll
     for (int q = 0; q < D; ++q) {
@@ -530,6 +554,7 @@ __device__ __forceinline__ bool cspm_due(const EnsInst& I, const int32_t* istep,
 template <int D>
 __global__ void __launch_bounds__(ENS_MAX_TPB) k_ens_cspm(EnsArr A, const EnsInst* __restrict__ T,
                                                           const int32_t* __restrict__ istep) {
+  if (*A.ovf) return;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < A.N; i += stride) {
     const int s = A.inst[i];
@@ -540,43 +565,28 @@ __global__ void __launch_bounds__(ENS_MAX_TPB) k_ens_cspm(EnsArr A, const EnsIns
       A.drh[i] = dri;  // Σ over nothing: 0/0, the reference keeps ρ
       continue;
     }
-    int cx0, cy0, cz0;
-    cell_of(A.skey[i], I, cx0, cy0, cz0);
     float oi[D];
 #pragma unroll
     for (int d = 0; d < D; ++d) oi[d] = A.off[d][i];
     KSum s2, s3;
-    const int zlo = D == 3 ? -1 : 0, zhi = D == 3 ? 1 : 0;
-    for (int dz = zlo; dz <= zhi; ++dz) {
-      const int cz = cz0 + dz;
-      if (cz < 0 || cz >= I.nc[2]) continue;
-      for (int dy = -1; dy <= 1; ++dy) {
-        const int cy = cy0 + dy;
-        if (cy < 0 || cy >= I.nc[1]) continue;
-        const int row = I.key_off + I.nc[0] * (cy + I.nc[1] * cz);
-        for (int dxc = -1; dxc <= 1; ++dxc) {
-          const int cx = cx0 + dxc;
-          if (cx < 0 || cx >= I.nc[0]) continue;
-          const int j0 = A.cellstart[row + cx], j1 = A.cellstart[row + cx + 1];
-          const float shx = (float)dxc * I.csf, shy = (float)dy * I.csf, shz = (float)dz * I.csf;
-          for (int j = j0; j < j1; ++j) {
-            if (j == i || !(A.pt[j] > 0)) continue;
-            float d[D];
+    const int nn = A.nlc[i];
+    for (int e = 0; e < nn; ++e) {
+      const int ent = A.nl[(int64_t)e * A.ncap + i];
+      const int j = ent >> 5;
+      if (!(A.pt[j] > 0)) continue;
+      float shx, shy, shz;
+      shift_of(ent, I, shx, shy, shz);
+      float d[D];
 #pragma unroll
-            for (int q = 0; q < D; ++q) d[q] = (oi[q] - A.off[q][j]) - (q == 0 ? shx : (q == 1 ? shy : shz));
-            const float r2 = dot32<D>(d, d);
-            if (!(r2 < I.H2)) continue;
-            const float u = sqrtf(r2) * I.Hinv;
-            const float t = u < 1.f ? 1.f - u : 0.f;
-            const float t2 = t * t;
-            const float w = (1.f + 4.f * u) * (t2 * t2) * I.nW;
-            const float drj = A.dr[j];
-            const float mw = I.m0 * w / (I.rho0 + drj);
-            s2.add(mw);
-            s3.add(mw * drj);
-          }
-        }
-      }
+      for (int q = 0; q < D; ++q) d[q] = (oi[q] - A.off[q][j]) - (q == 0 ? shx : (q == 1 ? shy : shz));
+      const float u = sqrtf(dot32<D>(d, d)) * I.Hinv;
+      const float t = u < 1.f ? 1.f - u : 0.f;
+      const float t2 = t * t;
+      const float w = (1.f + 4.f * u) * (t2 * t2) * I.nW;
+      const float drj = A.dr[j];
+      const float mw = I.m0 * w / (I.rho0 + drj);
+      s2.add(mw);
+      s3.add(mw * drj);
     }
     const float nd = s3.s / s2.s;
     A.drh[i] = nd == nd ? nd : dri;
@@ -585,17 +595,21 @@ __global__ void __launch_bounds__(ENS_MAX_TPB) k_ens_cspm(EnsArr A, const EnsIns
 
 __global__ void k_ens_cspm_apply(int64_t N, const int32_t* __restrict__ inst, const EnsInst* __restrict__ T,
                                  const int32_t* __restrict__ istep, const float* __restrict__ drh,
-                                 float* __restrict__ dr) {
+                                 float* __restrict__ dr, const int* __restrict__ ovf) {
+  if (*ovf) return;
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= N) return;
   const int s = inst[i];
   if (cspm_due(T[s], istep, s)) dr[i] = drh[i];
 }
 
-// one more step done, per instance
-__global__ void k_ens_tick(int ninst, int32_t* __restrict__ istep) {
+// one more step done, per instance, and for the call
+__global__ void k_ens_tick(int ninst, int32_t* __restrict__ istep, const int* __restrict__ ovf,
+                           int* __restrict__ done) {
+  if (*ovf) return;
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s < ninst) istep[s] += 1;
+  if (s == 0) *done += 1;
 }
 
 // gather one instance's field into its original particle order
@@ -691,6 +705,10 @@ struct gcsph_ens {
   DevBuf OFFN[3];
   DevBuf INST, KEY, SLOT, TMP, PERM, SKEY, OFF[3], OFFH[3], VH[3], DRH, COUNT, CELLSTART, SCRATCH, TAB, MOVES, OUT;
   DevBuf ISTEP;          // steps done per instance (cspmcorr! schedule), packing order
+  DevBuf NL, NLC;        // neighbour list of the step and its row lengths
+  DevBuf FLAGS;          // [0] list overflow, [1] longest row, [2] steps done in the call
+  int nls = 0;           // list entries per particle (grows on overflow)
+  int64_t nl_cap = 0;    // particles the list is sized for
   int tpb = 0;           // 0: not tuned yet
   bool tpb_fixed = false;
   int64_t tuned_n = 0;   // particle count the choice was made on
@@ -741,6 +759,12 @@ EnsArr ens_arr(gcsph_ens* e) {
   A.dr = e->DR[e->cur].as<float>();
   A.drb = e->DRB[e->cur].as<float>();
   A.drh = e->DRH.as<float>();
+  A.nl = e->NL.as<int>();
+  A.nlc = e->NLC.as<int>();
+  A.ncap = e->nl_cap;
+  A.nls = e->nls;
+  A.ovf = e->FLAGS.as<int>();
+  A.nlmax = e->FLAGS.as<int>() + 1;
   A.pt = e->PT[e->cur].as<int32_t>();
   return A;
 }
@@ -815,6 +839,22 @@ int ens_reserve_cells(gcsph_ens* e, int64_t k) {
   return GCSPH_OK;
 }
 
+// the step's neighbour list: nls entries for each of cap_n particles
+int ens_reserve_list(gcsph_ens* e, int nls) {
+  if (nls <= e->nls && e->nl_cap >= e->cap_n) return GCSPH_OK;
+  const int want = std::max(nls, e->nls);
+  if ((double)want * (double)e->cap_n * 4.0 > 64e9) return fail(GCSPH_ENOMEM, "neighbour list too large");
+  int rc;
+  if ((rc = e->NL.ensure(sizeof(int) * (size_t)want * (size_t)e->cap_n, e->st))) return rc;
+  if ((rc = e->NLC.ensure(sizeof(int) * (size_t)e->cap_n, e->st))) return rc;
+  if ((rc = e->FLAGS.ensure(sizeof(int) * 4, e->st, true))) return rc;
+  e->nls = want;
+  e->nl_cap = e->cap_n;
+  e->gen += 1;  // captured graphs point at the old list
+  graphs_free(e);
+  return GCSPH_OK;
+}
+
 // device instance table + per-particle instance index after a layout change
 int ens_relayout(gcsph_ens* e) {
   int64_t p = 0, k = 0;
@@ -825,6 +865,7 @@ int ens_relayout(gcsph_ens* e) {
     p += h.n;
     k += h.ncell;
   }
+  if (p >= (int64_t)1 << 26) return fail(GCSPH_ECAPACITY, "ensemble of %lld particles: at most 2^26", (long long)p);
   e->N = p;
   e->K = k;
   e->any_cspm = e->any_dpc = e->any_xsph = false;
@@ -914,6 +955,10 @@ int ens_enqueue_step(gcsph_ens* e, cudaStream_t st, int tpb) {
   const int64_t want = (N + tpb - 1) / tpb;
   const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)e->sms * e->occ[t]));
   EnsArr A = ens_arr(e);
+  timer_begin(T_PAIRS, st);
+  k_ens_nlist<D><<<grid, tpb, 0, st>>>(A, T);
+  GC_LAUNCHED();
+  timer_end(T_PAIRS, st);
   timer_begin(T_STAGE1, st);
   k_ens_stage<D, 1><<<grid, tpb, 0, st>>>(A, T);
   GC_LAUNCHED();
@@ -942,11 +987,12 @@ int ens_enqueue_step(gcsph_ens* e, cudaStream_t st, int tpb) {
     k_ens_cspm<D><<<grid, tpb, 0, st>>>(A, T, e->ISTEP.as<int32_t>());
     GC_LAUNCHED();
     k_ens_cspm_apply<<<nblocks(N, 256), 256, 0, st>>>(N, e->INST.as<int32_t>(), T, e->ISTEP.as<int32_t>(),
-                                                      e->DRH.as<float>(), e->DR[e->cur].as<float>());
+                                                      e->DRH.as<float>(), e->DR[e->cur].as<float>(), A.ovf);
     GC_LAUNCHED();
     timer_end(T_CSPM, st);
   }
-  k_ens_tick<<<nblocks(ninst, 128), 128, 0, st>>>(ninst, e->ISTEP.as<int32_t>());
+  k_ens_tick<<<nblocks(std::max(ninst, 1), 128), 128, 0, st>>>(ninst, e->ISTEP.as<int32_t>(), A.ovf,
+                                                                  A.ovf + 2);
   GC_LAUNCHED();
   return GCSPH_OK;
 }
@@ -998,17 +1044,7 @@ int ens_autotune(gcsph_ens* e, int32_t budget, int32_t* steps_used) {
   return GCSPH_OK;
 }
 
-int ens_run(gcsph_ens* e, int32_t n) {
-  if (n <= 0 || e->N == 0) return GCSPH_OK;
-  if (!e->use_graphs) {
-    for (int32_t it = 0; it < n; ++it) {
-      int rc = enqueue_step(e, e->st, e->tpb);
-      if (rc) return rc;
-    }
-    GC_CUDA(cudaStreamSynchronize(e->st));
-    timer_collect();
-    return GCSPH_OK;
-  }
+int ens_run_graph(gcsph_ens* e, int32_t n) {
   EnsGraph* g = nullptr;
   const int timing = timing_on() ? 1 : 0;
   for (EnsGraph& c : e->graphs)
@@ -1066,6 +1102,21 @@ int ens_run(gcsph_ens* e, int32_t n) {
   return GCSPH_OK;
 }
 
+
+int ens_run(gcsph_ens* e, int32_t n) {
+  if (n <= 0 || e->N == 0) return GCSPH_OK;
+  if (!e->use_graphs) {
+    for (int32_t it = 0; it < n; ++it) {
+      int rc = enqueue_step(e, e->st, e->tpb);
+      if (rc) return rc;
+    }
+    GC_CUDA(cudaStreamSynchronize(e->st));
+    timer_collect();
+    return GCSPH_OK;
+  }
+  return ens_run_graph(e, n);
+}
+
 EnsHostInst* find_slot(gcsph_ens* e, int32_t slot, size_t* pos = nullptr) {
   for (size_t s = 0; s < e->inst.size(); ++s)
     if (e->inst[s].slot == slot) {
@@ -1113,7 +1164,7 @@ void ens_destroy(gcsph_ens* e) {
     e->ID[b].release();
   }
   DevBuf* one[] = {&e->INST, &e->KEY, &e->SLOT, &e->TMP, &e->PERM, &e->SKEY, &e->DRH, &e->COUNT, &e->CELLSTART,
-                   &e->SCRATCH, &e->TAB, &e->MOVES, &e->OUT, &e->ISTEP};
+                   &e->SCRATCH, &e->TAB, &e->MOVES, &e->OUT, &e->ISTEP, &e->NL, &e->NLC, &e->FLAGS};
   for (DevBuf* b : one) b->release();
   for (int d = 0; d < 3; ++d) {
     e->OFF[d].release();
@@ -1129,7 +1180,8 @@ int ens_bytes_per_particle(int32_t D, int64_t* bytes) {
   // 2 x (x f64, v f32, x and v base differences f32) per dim + 2 x (δρ,
   // δρ base, ptype, id) + inst, key, slot, tmp, perm, skey + (off, offh, vh,
   // offn) per dim + δρ½, plus about one cell per particle
-  *bytes = 2 * D * (8 + 4 + 8) + 2 * 16 + 6 * 4 + D * 16 + 4 + 8;
+  // + the step's neighbour list (64 entries in 2-D, 256 in 3-D, 4 B each) and its length
+  *bytes = 2 * D * (8 + 4 + 8) + 2 * 16 + 6 * 4 + D * 16 + 4 + 8 + (D == 2 ? 64 : 256) * 4 + 4;
   return GCSPH_OK;
 }
 
@@ -1286,12 +1338,33 @@ int ens_step(gcsph_ens* e, int32_t n) {
   if (!e) return fail(GCSPH_EINVAL, "null handle");
   if (n < 0) return fail(GCSPH_EINVAL, "n must be >= 0");
   if (e->N == 0 || n == 0) return GCSPH_OK;
-  int32_t used = 0;
-  int rc = ens_autotune(e, n, &used);
-  if (rc) return rc;
-  // tuning steps are real steps; they count toward n
-  if (n - used > 0 && (rc = ens_run(e, n - used))) return rc;
-  for (EnsHostInst& h : e->inst) h.steps += n;
+  int rc;
+  if ((rc = ens_reserve_list(e, e->nls ? e->nls : (e->D == 2 ? 64 : 256)))) return rc;
+  int32_t left = n;
+  int guard = 0;
+  while (left > 0) {
+    // a call: tuning steps (eager) and the rest (a graph), with the list
+    // overflow flag cleared; the flags say how many steps completed
+    GC_CUDA(cudaMemsetAsync(e->FLAGS.p, 0, sizeof(int) * 4, e->st));
+    int32_t used = 0;
+    if ((rc = ens_autotune(e, left, &used))) return rc;
+    if (left - used > 0 && (rc = ens_run(e, left - used))) return rc;
+    int fl[4];
+    GC_CUDA(cudaMemcpyAsync(fl, e->FLAGS.p, sizeof(fl), cudaMemcpyDeviceToHost, e->st));
+    GC_CUDA(cudaStreamSynchronize(e->st));
+    const int32_t done = fl[2];
+    for (EnsHostInst& h : e->inst) h.steps += done;
+    left -= done;
+    if (fl[0]) {
+      // a neighbour row outgrew the list: the call stopped at the start of
+      // that step (state re-sorted, nothing else changed); grow and go on
+      const int want = std::max(fl[1] + fl[1] / 4 + 8, e->nls + e->nls / 2);
+      if ((rc = ens_reserve_list(e, want))) return rc;
+      if (++guard > 8) return fail(GCSPH_ECAPACITY, "neighbour list keeps overflowing (%d entries)", fl[1]);
+    } else if (left != 0) {
+      return fail(GCSPH_ESTATE, "ensemble call stopped %d steps short without an overflow", left);
+    }
+  }
   return GCSPH_OK;
 }
 
@@ -1367,6 +1440,22 @@ int ens_set_tuning(gcsph_ens* e, int32_t tpb, int32_t graphs) {
   e->tpb_fixed = tpb != 0;
   e->tuned_n = 0;
   e->use_graphs = graphs != 0;
+  return GCSPH_OK;
+}
+
+int ens_set_list_stride(gcsph_ens* e, int32_t nls) {
+  if (!e) return fail(GCSPH_EINVAL, "null handle");
+  if (nls < 1 || nls > 4096) return fail(GCSPH_EINVAL, "list stride %d (1..4096)", (int)nls);
+  cudaStreamSynchronize(e->st);
+  e->NL.release();
+  e->nls = 0;
+  e->nl_cap = 0;
+  return ens_reserve_list(e, nls);
+}
+
+int ens_get_list_stride(gcsph_ens* e, int32_t* nls) {
+  if (!e || !nls) return fail(GCSPH_EINVAL, "null argument");
+  *nls = e->nls;
   return GCSPH_OK;
 }
 

@@ -154,6 +154,14 @@ class Ensemble:
         _lib.check(_lib.load().ens_get_tuning(self._h, C.byref(t), C.byref(a), C.byref(b)))
         return {"tpb": int(t.value), "captures": int(a.value), "replays": int(b.value)}
 
+    def set_list_stride(self, nls: int):
+        _lib.check(_lib.load().ens_set_list_stride(self._h, int(nls)))
+
+    def list_stride(self) -> int:
+        n = C.c_int32()
+        _lib.check(_lib.load().ens_get_list_stride(self._h, C.byref(n)))
+        return int(n.value)
+
     def close(self):
         h = self.__dict__.get("_h")
         if h:

@@ -269,7 +269,9 @@ double gcsph_dpckernlim(int32_t D);
 
 /* ------------------------------------------------------------------------
  * Batched FP32 ensemble (no reference counterpart: the reference steps one
- * SPHProblem at a time).  Many independent instances -- each its own particle
+ * SPHProblem at a time).  Each step re-sorts all instances into cell order
+ * and builds one neighbour list (cell walk, r < H), which every pair pass of
+ * the step then walks.  Many independent instances -- each its own particle
  * set, parameters, frozen cell grid (cell edge = H) and fixed Δt -- advance
  * together, one launch per pass over all of them.  Pair arithmetic and
  * per-particle sums in FP32 (Kahan), density held as ρ - ρ₀, positions in
@@ -312,6 +314,11 @@ int ens_totals(gcsph_ens* e, int32_t* ninst, int64_t* nparticles, int64_t* ncell
 /* tpb 0 = autotune (128/256/512), graphs 0 = one launch sequence per step */
 int ens_set_tuning(gcsph_ens* e, int32_t tpb, int32_t graphs);
 int ens_get_tuning(gcsph_ens* e, int32_t* tpb, int64_t* captures, int64_t* replays);
+/* Entries per particle in the step's neighbour list (default 64 in 2-D, 256
+ * in 3-D; it grows by itself when a row outgrows it, repeating the steps
+ * that had not completed). */
+int ens_set_list_stride(gcsph_ens* e, int32_t nls);
+int ens_get_list_stride(gcsph_ens* e, int32_t* nls);
 
 #if defined(__GNUC__)
 #pragma GCC visibility pop

@@ -184,3 +184,24 @@ def test_launch_shape_and_capture_do_not_change_results(gpu_pkg, tpb, graphs):
         assert t["tpb"] == tpb
     else:
         assert t["tpb"] in (128, 256, 512)
+
+
+@pytest.mark.parametrize("graphs", [True, False])
+def test_neighbour_list_overflow_grows_and_repeats(gpu_pkg, graphs):
+    """A list stride far too small: the call stops at the first step whose
+    rows do not fit, the stride grows and the remaining steps run -- the
+    result is bit-identical to a run that never overflowed."""
+    a, b, _, _ = _specs(gpu_pkg)
+    ref = gpu_pkg.Ensemble(2)
+    r1, r2 = ref.add(a), ref.add(b)
+    ref.step(9)
+    ens = gpu_pkg.Ensemble(2)
+    ens.set_tuning(256, graphs)
+    e1, e2 = ens.add(a), ens.add(b)
+    ens.set_list_stride(4)
+    ens.step(9)
+    assert ens.list_stride() > 4
+    assert ens.info(e1)["steps"] == 9
+    for f in FIELDS:
+        assert np.array_equal(ref.get(r1, f), ens.get(e1, f)), f
+        assert np.array_equal(ref.get(r2, f), ens.get(e2, f)), f
