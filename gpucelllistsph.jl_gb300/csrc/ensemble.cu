@@ -75,7 +75,89 @@ struct EnsArr {
   int nls;                   // entries per particle the list holds
   int* ovf;                  // a row outgrew nls: every later kernel of the call skips
   int* nlmax;                // the longest row seen (to size the next try)
+  // packed per-particle records that neighbours read (float4 loads):
+  //   r1 (2 float4): x offset, v, δρ, ptype       -- stage 1, the list build
+  //   r2 (2 or 3):   xΔt½ offset, vΔt½, δρΔt½, ptype, x offset -- stage 2
+  float4* r1;
+  float4* r2;
 };
+
+// record layouts (D = 2 | D = 3)
+//   r1: [o0 o1 v0 v1][dr pt - -]        | [o0 o1 o2 v0][v1 v2 dr pt]
+//   r2: [h0 h1 w0 w1][drh pt o0 o1]     | [h0 h1 h2 w0][w1 w2 drh pt][o0 o1 o2 -]
+template <int D>
+__device__ __forceinline__ void put_r1(float4* r, int64_t k, const float* o, const float* v, float dr, int pt) {
+  if (D == 2) {
+    r[2 * k] = make_float4(o[0], o[1], v[0], v[1]);
+    r[2 * k + 1] = make_float4(dr, __int_as_float(pt), 0.f, 0.f);
+  } else {
+    r[2 * k] = make_float4(o[0], o[1], o[D - 1], v[0]);
+    r[2 * k + 1] = make_float4(v[1], v[D - 1], dr, __int_as_float(pt));
+  }
+}
+template <int D>
+__device__ __forceinline__ void get_r1_off(const float4* __restrict__ r, int64_t k, float* o) {
+  const float4 a = __ldg(r + 2 * k);
+  o[0] = a.x;
+  o[1] = a.y;
+  if (D == 3) o[D - 1] = a.z;
+}
+// raw record of neighbour j for stage S (2 float4, or 3 for stage 2 in 3-D)
+template <int D, int S>
+struct Rec {
+  float4 a, b, c;
+};
+template <int D, int S>
+__device__ __forceinline__ Rec<D, S> load_rec(const float4* __restrict__ r1, const float4* __restrict__ r2, int j) {
+  Rec<D, S> x;
+  if (S == 1) {
+    x.a = __ldg(r1 + 2 * (int64_t)j);
+    x.b = __ldg(r1 + 2 * (int64_t)j + 1);
+  } else if (D == 2) {
+    x.a = __ldg(r2 + 2 * (int64_t)j);
+    x.b = __ldg(r2 + 2 * (int64_t)j + 1);
+  } else {
+    x.a = __ldg(r2 + 3 * (int64_t)j);
+    x.b = __ldg(r2 + 3 * (int64_t)j + 1);
+    x.c = __ldg(r2 + 3 * (int64_t)j + 2);
+  }
+  return x;
+}
+// decode: o = offset at x, h = offset at xΔt½ (stage 2), v, δρ, ptype
+template <int D, int S>
+__device__ __forceinline__ void decode_rec(const Rec<D, S>& x, float* o, float* h, float* v, float& dr, int& pt) {
+  if (S == 1) {
+    if (D == 2) {
+      o[0] = x.a.x; o[1] = x.a.y; v[0] = x.a.z; v[1] = x.a.w;
+      dr = x.b.x; pt = __float_as_int(x.b.y);
+    } else {
+      o[0] = x.a.x; o[1] = x.a.y; o[D - 1] = x.a.z; v[0] = x.a.w;
+      v[1] = x.b.x; v[D - 1] = x.b.y; dr = x.b.z; pt = __float_as_int(x.b.w);
+    }
+  } else {
+    if (D == 2) {
+      h[0] = x.a.x; h[1] = x.a.y; v[0] = x.a.z; v[1] = x.a.w;
+      dr = x.b.x; pt = __float_as_int(x.b.y); o[0] = x.b.z; o[1] = x.b.w;
+    } else {
+      h[0] = x.a.x; h[1] = x.a.y; h[D - 1] = x.a.z; v[0] = x.a.w;
+      v[1] = x.b.x; v[D - 1] = x.b.y; dr = x.b.z; pt = __float_as_int(x.b.w);
+      o[0] = x.c.x; o[1] = x.c.y; o[D - 1] = x.c.z;
+    }
+  }
+}
+
+template <int D>
+__device__ __forceinline__ void put_r2(float4* r, int64_t k, const float* h, const float* w, float drh, int pt,
+                                       const float* o) {
+  if (D == 2) {
+    r[2 * k] = make_float4(h[0], h[1], w[0], w[1]);
+    r[2 * k + 1] = make_float4(drh, __int_as_float(pt), o[0], o[1]);
+  } else {
+    r[3 * k] = make_float4(h[0], h[1], h[D - 1], w[0]);
+    r[3 * k + 1] = make_float4(w[1], w[D - 1], drh, __int_as_float(pt));
+    r[3 * k + 2] = make_float4(o[0], o[1], o[D - 1], 0.f);
+  }
+}
 
 struct KSum {
   float s = 0.f, c = 0.f;
@@ -183,7 +265,7 @@ template <int D>
 __global__ void k_ens_permute(int64_t N, const int32_t* __restrict__ perm, const int32_t* __restrict__ key,
                               const int32_t* __restrict__ inst, const EnsInst* __restrict__ T, EnsState in,
                               EnsState out, int32_t* __restrict__ skey, float* __restrict__ o0,
-                              float* __restrict__ o1, float* __restrict__ o2) {
+                              float* __restrict__ o1, float* __restrict__ o2, float4* __restrict__ r1) {
   const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= N) return;
   const int32_t i = perm[k];
@@ -192,21 +274,27 @@ __global__ void k_ens_permute(int64_t N, const int32_t* __restrict__ perm, const
   const EnsInst& I = T[inst[k]];
   int c0, c1, c2;
   cell_of(kk, I, c0, c1, c2);
+  float ov[D], vv[D];
 #pragma unroll
   for (int d = 0; d < D; ++d) {
     const double xv = in.x[d][i];
     out.x[d][k] = xv;
-    out.v[d][k] = in.v[d][i];
+    vv[d] = in.v[d][i];
+    out.v[d][k] = vv[d];
     out.dxb[d][k] = in.dxb[d][i];
     out.dvb[d][k] = in.dvb[d][i];
     const int cd = d == 0 ? c0 : (d == 1 ? c1 : c2);
     float* o = d == 0 ? o0 : (d == 1 ? o1 : o2);
-    o[k] = (float)(xv - (I.origin[d] + (double)cd * I.cs));
+    ov[d] = (float)(xv - (I.origin[d] + (double)cd * I.cs));
+    o[k] = ov[d];
   }
-  out.dr[k] = in.dr[i];
+  const float dr = in.dr[i];
+  const int pt = in.pt[i];
+  out.dr[k] = dr;
   out.drb[k] = in.drb[i];
-  out.pt[k] = in.pt[i];
+  out.pt[k] = pt;
   out.id[k] = in.id[i];
+  put_r1<D>(r1, k, ov, vv, dr, pt);
 }
 
 // ---------------------------------------------------------------------------
@@ -253,9 +341,10 @@ __global__ void __launch_bounds__(ENS_MAX_TPB) k_ens_nlist(EnsArr A, const EnsIn
           const int code = (dxc + 1) + 3 * (dy + 1) + 9 * (dz + 1);
           for (int j = j0; j < j1; ++j) {
             if (j == i) continue;
-            float d[D];
+            float d[D], oj[D];
+            get_r1_off<D>(A.r1, j, oj);
 #pragma unroll
-            for (int q = 0; q < D; ++q) d[q] = (oi[q] - A.off[q][j]) - (q == 0 ? shx : (q == 1 ? shy : shz));
+            for (int q = 0; q < D; ++q) d[q] = (oi[q] - oj[q]) - (q == 0 ? shx : (q == 1 ? shy : shz));
             if (!(dot32<D>(d, d) < I.H2)) continue;
             if (cnt < A.nls) A.nl[(int64_t)cnt * A.ncap + i] = (j << 5) | code;
             ++cnt;
@@ -296,12 +385,16 @@ __global__ void __launch_bounds__(ENS_MAX_TPB) k_ens_stage(EnsArr A, const EnsIn
     const int nn = A.nlc[i];
     for (int e = 0; e < nn; ++e) {
       const int ent = A.nl[(int64_t)e * A.ncap + i];
-      const int j = ent >> 5;
+      const Rec<D, STAGE> rec = load_rec<D, STAGE>(A.r1, A.r2, ent >> 5);
       float shx, shy, shz;
       shift_of(ent, I, shx, shy, shz);
+      // the neighbour's record: offsets (at x, and at xΔt½ in stage 2), velocity, δρ, ptype
+      float oj[D], hj[D], vj[D], drj;
+      int ptj;
+      decode_rec<D, STAGE>(rec, oj, hj, vj, drj, ptj);
       float d[D];
 #pragma unroll
-      for (int q = 0; q < D; ++q) d[q] = (oi[q] - A.off[q][j]) - (q == 0 ? shx : (q == 1 ? shy : shz));
+      for (int q = 0; q < D; ++q) d[q] = (oi[q] - oj[q]) - (q == 0 ? shx : (q == 1 ? shy : shz));
       const float r2 = dot32<D>(d, d);
       // sph∇W!: W'(r)/r of WendlandC2 = -20 nDW Hinv (1-q)^3
       const float r = sqrtf(r2);
@@ -312,12 +405,10 @@ __global__ void __launch_bounds__(ENS_MAX_TPB) k_ens_stage(EnsArr A, const EnsIn
 #pragma unroll
       for (int q = 0; q < D; ++q) {
         gw[q] = d[q] * dwr;
-        dd[q] = STAGE == 1 ? d[q] : (ohi[q] - A.offh[q][j]) - (q == 0 ? shx : (q == 1 ? shy : shz));
-        dv[q] = vi[q] - (STAGE == 1 ? A.v[q][j] : A.vh[q][j]);
+        dd[q] = STAGE == 1 ? d[q] : (ohi[q] - hj[q]) - (q == 0 ? shx : (q == 1 ? shy : shz));
+        dv[q] = vi[q] - vj[q];
       }
       const float r2d = STAGE == 1 ? r2 : dot32<D>(dd, dd);
-      const int ptj = A.pt[j];
-      const float drj = STAGE == 1 ? A.dr[j] : A.drh[j];
       const float rhoj = I.rho0 + drj;
       const bool both = pti > 0 && ptj > 0;
       const float inv = 1.f / (r2d + I.eta2);
@@ -385,13 +476,17 @@ __global__ void __launch_bounds__(ENS_MAX_TPB) k_ens_stage(EnsArr A, const EnsIn
       float drh = A.drb[i] + drho.s * hdt;
       if (drh < 0.f && pti < 0) drh = 0.f;
       A.drh[i] = drh;
+      float hh[D], ww[D];
 #pragma unroll
       for (int q = 0; q < D; ++q) {
         float vh = vi[q] + A.dvb[q][i];
         if (pti > 1) vh = vh + a[q] * hdt;
         A.vh[q][i] = vh;
-        A.offh[q][i] = (oi[q] + A.dxb[q][i]) + vh * hdt;
+        ww[q] = vh;
+        hh[q] = (oi[q] + A.dxb[q][i]) + vh * hdt;
+        A.offh[q][i] = hh[q];
       }
+      put_r2<D>(A.r2, i, hh, ww, drh, pti, oi);
     } else {
       // symplectic_update!: δρ_new = δρ - ρ 2ε/(2+ε), positions in FP64
       const float dr0 = A.dr[i];
@@ -707,6 +802,7 @@ struct gcsph_ens {
   DevBuf ISTEP;          // steps done per instance (cspmcorr! schedule), packing order
   DevBuf NL, NLC;        // neighbour list of the step and its row lengths
   DevBuf FLAGS;          // [0] list overflow, [1] longest row, [2] steps done in the call
+  DevBuf R1, R2;         // packed neighbour records of the two stages
   int nls = 0;           // list entries per particle (grows on overflow)
   int64_t nl_cap = 0;    // particles the list is sized for
   int tpb = 0;           // 0: not tuned yet
@@ -765,6 +861,8 @@ EnsArr ens_arr(gcsph_ens* e) {
   A.nls = e->nls;
   A.ovf = e->FLAGS.as<int>();
   A.nlmax = e->FLAGS.as<int>() + 1;
+  A.r1 = e->R1.as<float4>();
+  A.r2 = e->R2.as<float4>();
   A.pt = e->PT[e->cur].as<int32_t>();
   return A;
 }
@@ -820,6 +918,8 @@ int ens_reserve(gcsph_ens* e, int64_t n) {
     if ((rc = e->OFFN[d].ensure(sizeof(float) * want, e->st))) return rc;
   }
   if ((rc = e->DRH.ensure(sizeof(float) * want, e->st))) return rc;
+  if ((rc = e->R1.ensure(sizeof(float4) * 2 * want, e->st))) return rc;
+  if ((rc = e->R2.ensure(sizeof(float4) * (e->D == 2 ? 2 : 3) * want, e->st))) return rc;
   if ((rc = e->SCRATCH.ensure(sizeof(int64_t) * scan_scratch_elems(std::max<int64_t>(want, e->cap_k) + 1), e->st)))
     return rc;
   e->cap_n = want;
@@ -948,7 +1048,8 @@ int ens_enqueue_step(gcsph_ens* e, cudaStream_t st, int tpb) {
   k_ens_permute<D><<<nblocks(N, 256), 256, 0, st>>>(N, e->PERM.as<int32_t>(), e->KEY.as<int32_t>(),
                                                      e->INST.as<int32_t>(), T, ens_state(e, e->cur),
                                                      ens_state(e, e->cur ^ 1), e->SKEY.as<int32_t>(),
-                                                     e->OFF[0].as<float>(), e->OFF[1].as<float>(), o2);
+                                                     e->OFF[0].as<float>(), e->OFF[1].as<float>(), o2,
+                                                     e->R1.as<float4>());
   GC_LAUNCHED();
   e->cur ^= 1;
   const int t = tpb_index(tpb);
@@ -1164,7 +1265,8 @@ void ens_destroy(gcsph_ens* e) {
     e->ID[b].release();
   }
   DevBuf* one[] = {&e->INST, &e->KEY, &e->SLOT, &e->TMP, &e->PERM, &e->SKEY, &e->DRH, &e->COUNT, &e->CELLSTART,
-                   &e->SCRATCH, &e->TAB, &e->MOVES, &e->OUT, &e->ISTEP, &e->NL, &e->NLC, &e->FLAGS};
+                   &e->SCRATCH, &e->TAB, &e->MOVES, &e->OUT, &e->ISTEP, &e->NL, &e->NLC, &e->FLAGS,
+                   &e->R1, &e->R2};
   for (DevBuf* b : one) b->release();
   for (int d = 0; d < 3; ++d) {
     e->OFF[d].release();
@@ -1181,7 +1283,8 @@ int ens_bytes_per_particle(int32_t D, int64_t* bytes) {
   // δρ base, ptype, id) + inst, key, slot, tmp, perm, skey + (off, offh, vh,
   // offn) per dim + δρ½, plus about one cell per particle
   // + the step's neighbour list (64 entries in 2-D, 256 in 3-D, 4 B each) and its length
-  *bytes = 2 * D * (8 + 4 + 8) + 2 * 16 + 6 * 4 + D * 16 + 4 + 8 + (D == 2 ? 64 : 256) * 4 + 4;
+  *bytes = 2 * D * (8 + 4 + 8) + 2 * 16 + 6 * 4 + D * 16 + 4 + 8 + (D == 2 ? 64 : 256) * 4 + 4 +
+           16 * (D == 2 ? 4 : 5);  // packed records
   return GCSPH_OK;
 }
 
