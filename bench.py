@@ -44,6 +44,7 @@ def parse():
     ap.add_argument("--no-serving", action="store_true", help="skip the serving-loop measurement")
     ap.add_argument("--serving-requests", type=int, default=40)
     ap.add_argument("--serving-horizon-scale", type=float, default=0.01)
+    ap.add_argument("--no-celllist", action="store_true", help="skip the cell-list update!/partialupdate! timing")
     ap.add_argument("--c3", action="store_true",
                     help="instead: 3-D dam break at scale, FP32 ensemble against the FP64 drop-in (one JSON line)")
     ap.add_argument("--c3-steps", type=int, default=500)
@@ -346,6 +347,54 @@ def run_serving(g, args):
     return stats
 
 
+# the reference's published update! / partialupdate! medians on 200,000
+# uniform 2-D points, cellsize = dist = 0.016 (README.md:64-91), hardware not stated
+PUBLISHED_UPDATE_MS = 43.195
+PUBLISHED_PARTIAL_MS = 42.673
+
+
+def run_celllist(g, reps=10):
+    """The cell-list workload alone: update! (binning + pair list + emit into
+    the pairs array) and partialupdate! (pair search on the stale cells after
+    jittering the points by U(-0.1, 0.1)·dist), FP64, on 200,000 uniform 2-D
+    points (cellsize = dist = 0.016) and 4,000,000 uniform 3-D points
+    (cellsize = dist = 0.008); median wall time of `reps` synchronous calls."""
+    import numpy as np
+    import torch
+    out = {}
+    for key, N, D, cs in (("2d_200k", 200_000, 2, 0.016), ("3d_4m", 4_000_000, 3, 0.008)):
+        x = g.workloads.uniform_points(N, D)
+        c = g.GPUCellList(tuple(x), (cs,) * D, cs)
+        c.update()
+        c.update()
+
+        def timed(fn):
+            ts = []
+            for _ in range(reps):
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                fn()
+                torch.cuda.synchronize()
+                ts.append(time.perf_counter() - t0)
+            return 1e3 * statistics.median(ts)
+
+        up = timed(c.update)
+        pairs = c.pairsn
+        rng = np.random.default_rng(7)
+        for d in range(D):
+            c.points[d].add_(torch.from_numpy(rng.uniform(-0.1, 0.1, N) * cs).to(c.points[d].device))
+        part = timed(c.partialupdate)
+        out[key] = {"points": N, "pairs": pairs, "update_ms": up, "partialupdate_ms": part,
+                    "pairs_per_s_update": pairs / (up / 1e3)}
+        c.close()
+    out["2d_200k"]["published_update_ms"] = PUBLISHED_UPDATE_MS
+    out["2d_200k"]["published_partialupdate_ms"] = PUBLISHED_PARTIAL_MS
+    out["2d_200k"]["update_speedup_vs_published"] = PUBLISHED_UPDATE_MS / out["2d_200k"]["update_ms"]
+    out["2d_200k"]["partialupdate_speedup_vs_published"] = PUBLISHED_PARTIAL_MS / out["2d_200k"]["partialupdate_ms"]
+    out["note"] = "published medians from the reference's README, hardware not stated"
+    return out
+
+
 def run_c3(args):
     """3-D dam break at scale: fluid block 1.0 x 2.0 (vertical) x 0.5 m at
     dx = 0.01 (1.0 M fluid) in a 4.0 x 3.0 x 1.0 m tank with 3 boundary
@@ -550,6 +599,11 @@ def run_gb300(args):
            "kernel_ms": {k: {"launches": v[0], "total_ms": v[1]} for k, v in fam.items() if v[0]},
            "kernel_timing": "library event timers over a second, instrumented pass of the same K bench steps",
            "graphs": dict(zip(("captured", "replayed"), prob.graph_stats()))}
+    if not args.no_celllist:
+        try:
+            out["celllist"] = run_celllist(g)
+        except Exception as e:  # noqa: BLE001
+            out["celllist"] = {"error": repr(e)}
     if not args.no_batched:
         try:
             out["batched_fp32"] = run_batched(g, args, value / ws)

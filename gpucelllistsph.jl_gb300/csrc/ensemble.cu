@@ -95,13 +95,6 @@ __device__ __forceinline__ void put_r1(float4* r, int64_t k, const float* o, con
     r[2 * k + 1] = make_float4(v[1], v[D - 1], dr, __int_as_float(pt));
   }
 }
-template <int D>
-__device__ __forceinline__ void get_r1_off(const float4* __restrict__ r, int64_t k, float* o) {
-  const float4 a = __ldg(r + 2 * k);
-  o[0] = a.x;
-  o[1] = a.y;
-  if (D == 3) o[D - 1] = a.z;
-}
 // raw record of neighbour j for stage S (2 float4, or 3 for stage 2 in 3-D)
 template <int D, int S>
 struct Rec {
@@ -341,10 +334,9 @@ __global__ void __launch_bounds__(ENS_MAX_TPB) k_ens_nlist(EnsArr A, const EnsIn
           const int code = (dxc + 1) + 3 * (dy + 1) + 9 * (dz + 1);
           for (int j = j0; j < j1; ++j) {
             if (j == i) continue;
-            float d[D], oj[D];
-            get_r1_off<D>(A.r1, j, oj);
+            float d[D];
 #pragma unroll
-            for (int q = 0; q < D; ++q) d[q] = (oi[q] - oj[q]) - (q == 0 ? shx : (q == 1 ? shy : shz));
+            for (int q = 0; q < D; ++q) d[q] = (oi[q] - A.off[q][j]) - (q == 0 ? shx : (q == 1 ? shy : shz));
             if (!(dot32<D>(d, d) < I.H2)) continue;
             if (cnt < A.nls) A.nl[(int64_t)cnt * A.ncap + i] = (j << 5) | code;
             ++cnt;
