@@ -328,7 +328,7 @@ int CellCore::init(int D_, int64_t N_, const double* cellsize, double dist_, con
 
 void CellCore::release() {
   DevBuf* all[] = {&count, &cellstart, &key, &slot, &tmp, &perm, &skey, &orig, &cnt_full, &cnt_up, &rs_full,
-                   &rs_up, &nbr, &scratch, &pf[0], &pf[1], &pf[2], &pfmax, &orig_b};
+                   &rs_up, &nbr, &scratch, &pf[0], &pf[1], &pf[2], &pfmax, &orig_b, &stage};
   for (DevBuf* b : all) b->release();
   if (pin) cudaFreeHost(pin);
   pin = nullptr;
@@ -445,7 +445,11 @@ __global__ void __launch_bounds__(TPB) k_pairs32(const double* __restrict__ x0, 
                                                  const int32_t* __restrict__ cellstart, int64_t N, Grid g,
                                                  int32_t* __restrict__ cnt_full, int32_t* __restrict__ cnt_up,
                                                  const int64_t* __restrict__ rs_full, int32_t* __restrict__ nbr,
-                                                 int64_t cap, int* __restrict__ ovf) {
+                                                 int64_t cap, int* __restrict__ ovf, int32_t* __restrict__ stg,
+                                                 int S) {
+  // MODE 0: count; MODE 2: count and stage the row (ascending) in stg[k*S ..]
+  // when it fits; MODE 1: fill the CSR row -- a copy of the staged row when
+  // the count pass staged it, else the search again
   const int64_t gt = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int64_t k = gt / L;
   const int lane = (int)(gt % L);
@@ -453,6 +457,14 @@ __global__ void __launch_bounds__(TPB) k_pairs32(const double* __restrict__ x0, 
   if (MODE == 1 && rs_full[k + 1] > cap) {  // the row does not fit: report, write nothing
     if (ovf && lane == 0) atomicExch(ovf, 1);
     return;
+  }
+  if (MODE == 1 && stg) {
+    const int64_t r0 = rs_full[k];
+    const int32_t n = (int32_t)(rs_full[k + 1] - r0);
+    if (n <= S) {
+      for (int32_t q = lane; q < n; q += L) nbr[r0 + q] = stg[k * S + q];
+      return;
+    }
   }
   float tlo, thi;
   pf_thresholds<D>(bmax, g.dist2, &tlo, &thi);
@@ -468,6 +480,7 @@ __global__ void __launch_bounds__(TPB) k_pairs32(const double* __restrict__ x0, 
   const float ax = f0[k], ay = f1[k], az = D == 3 ? f2[k] : 0.0f;
   int32_t nf = 0, nu = 0;
   int64_t wpos = MODE == 1 ? rs_full[k] : 0;
+  int32_t spos = 0;  // MODE 2: staged entries so far
   const int xlo = cx > 0 ? cx - 1 : 0;
   const int xhi = cx < nx - 1 ? cx + 1 : nx - 1;
   for (int dz = (D == 3 ? -1 : 0); dz <= (D == 3 ? 1 : 0); ++dz) {
@@ -497,6 +510,13 @@ __global__ void __launch_bounds__(TPB) k_pairs32(const double* __restrict__ x0, 
         if (MODE == 0) {
           nf += hit;
           nu += hit && (m > k);
+        } else if (MODE == 2) {
+          nf += hit;
+          nu += hit && (m > k);
+          const unsigned bal = (__ballot_sync(gm, hit) >> gbase) & (L == 32 ? 0xffffffffu : ((1u << L) - 1u));
+          const int32_t at = spos + __popc(bal & ((1u << lane) - 1u));
+          if (hit && at < S) stg[k * S + at] = m;
+          spos += __popc(bal);
         } else {
           const unsigned bal = (__ballot_sync(gm, hit) >> gbase) & (L == 32 ? 0xffffffffu : ((1u << L) - 1u));
           if (hit) nbr[wpos + __popc(bal & ((1u << lane) - 1u))] = m;
@@ -505,7 +525,7 @@ __global__ void __launch_bounds__(TPB) k_pairs32(const double* __restrict__ x0, 
       }
     }
   }
-  if (MODE == 0) {
+  if (MODE != 1) {
 #pragma unroll
     for (int o = L / 2; o > 0; o >>= 1) {
       nf += __shfl_xor_sync(gm, nf, o);
@@ -592,9 +612,21 @@ int CellCore::build_pairs(const double* const* xs, int* ovf_dev) {
   else
     k_make_pf<3><<<nblocks(N, TPB), TPB, 0, st>>>(xs[0], xs[1], x2, N, g, pf[0].as<float>(), pf[1].as<float>(), f2, bm);
   GC_LAUNCHED();
-  PAIRS32_LAUNCH(0, L, xs[0], xs[1], x2, pf[0].as<float>(), pf[1].as<float>(), f2, bm, skey.as<int32_t>(),
-                 cellstart.as<int32_t>(), N, g, cnt_full.as<int32_t>(), cnt_up.as<int32_t>(), nullptr, nullptr, 0,
-                 nullptr);
+  // rows of up to S neighbours are staged by the count pass and copied by the fill
+  const double mean = N > 0 && nfull_est > 0 ? (double)nfull_est / (double)N : 0.0;
+  int S = 16;
+  while (S < 256 && (double)S < 1.5 * mean + 8.0) S <<= 1;
+  int32_t* sp = nullptr;
+  if (mean > 0 && (rc0 = stage.ensure(sizeof(int32_t) * (size_t)N * (size_t)S, st)) == GCSPH_OK) sp = stage.as<int32_t>();
+  if (rc0) return rc0;
+  if (sp)
+    PAIRS32_LAUNCH(2, L, xs[0], xs[1], x2, pf[0].as<float>(), pf[1].as<float>(), f2, bm, skey.as<int32_t>(),
+                   cellstart.as<int32_t>(), N, g, cnt_full.as<int32_t>(), cnt_up.as<int32_t>(), nullptr, nullptr, 0,
+                   nullptr, sp, S);
+  else
+    PAIRS32_LAUNCH(0, L, xs[0], xs[1], x2, pf[0].as<float>(), pf[1].as<float>(), f2, bm, skey.as<int32_t>(),
+                   cellstart.as<int32_t>(), N, g, cnt_full.as<int32_t>(), cnt_up.as<int32_t>(), nullptr, nullptr, 0,
+                   nullptr, nullptr, 0);
   GC_LAUNCHED();
   int rc = exclusive_scan_i32_to_i64(cnt_full.as<int32_t>(), rs_full.as<int64_t>(), N, scratch.as<int64_t>(), st);
   if (rc) return rc;
@@ -615,7 +647,7 @@ int CellCore::build_pairs(const double* const* xs, int* ovf_dev) {
   timer_begin(T_PAIRS, st);
   PAIRS32_LAUNCH(1, L, xs[0], xs[1], x2, pf[0].as<float>(), pf[1].as<float>(), f2, bm, skey.as<int32_t>(),
                  cellstart.as<int32_t>(), N, g, nullptr, nullptr, rs_full.as<int64_t>(), nbr.as<int32_t>(), nbr_cap,
-                 ovf_dev);
+                 ovf_dev, sp, S);
   GC_LAUNCHED();
   timer_end(T_PAIRS, st);
   built = true;
