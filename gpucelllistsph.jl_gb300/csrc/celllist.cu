@@ -596,7 +596,7 @@ int CellCore::pair_lanes() const {
     }                                                                                            \
   } while (0)
 
-int CellCore::build_pairs(const double* const* xs, int* ovf_dev) {
+int CellCore::build_pairs(const double* const* xs, int* ovf_dev, bool scan_up) {
   if (!sorted) return fail(GCSPH_ESTATE, "pair build before binning");
   const double* x2 = D == 3 ? xs[2] : xs[0];
   timer_begin(T_PAIRS, st);
@@ -628,7 +628,11 @@ int CellCore::build_pairs(const double* const* xs, int* ovf_dev) {
                    cellstart.as<int32_t>(), N, g, cnt_full.as<int32_t>(), cnt_up.as<int32_t>(), nullptr, nullptr, 0,
                    nullptr, nullptr, 0);
   GC_LAUNCHED();
-  int rc = exclusive_scan_i32_to_i64(cnt_full.as<int32_t>(), rs_full.as<int64_t>(), N, scratch.as<int64_t>(), st);
+  int rc = scan_up ? exclusive_scan2_i32_to_i64(cnt_full.as<int32_t>(), rs_full.as<int64_t>(),
+                                                cnt_up.as<int32_t>(), rs_up.as<int64_t>(), N,
+                                                scratch.as<int64_t>(), st)
+                  : exclusive_scan_i32_to_i64(cnt_full.as<int32_t>(), rs_full.as<int64_t>(), N,
+                                              scratch.as<int64_t>(), st);
   if (rc) return rc;
   timer_end(T_PAIRS, st);
   if (ovf_dev && nbr_cap > 0) {

@@ -57,8 +57,10 @@ struct CellCore {
   int gather_positions_by_orig(const double* const* xorig, double* const* xs);
   // count + scan + fill of the neighbour CSR on sorted positions xs.  With
   // ovf_dev (and buffers already sized once) the fill does not wait for the
-  // count: rows past nbr_cap raise *ovf_dev instead (see grow_nbr).
-  int build_pairs(const double* const* xs, int* ovf_dev = nullptr);
+  // count: rows past nbr_cap raise *ovf_dev instead (see grow_nbr).  scan_up
+  // also scans the larger-index counts into rs_up (device only) in the same
+  // launch as the row offsets.
+  int build_pairs(const double* const* xs, int* ovf_dev = nullptr, bool scan_up = false);
   int grow_nbr(int64_t need);
   int read_nfull();
   int ensure_up();

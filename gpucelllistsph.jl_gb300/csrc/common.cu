@@ -239,21 +239,43 @@ int64_t scan_scratch_elems(int64_t m) {
 }
 
 // one block walks the whole array in tiles of 1024 x 8 items, carrying the
-// running total: a single launch for the small arrays of small problems
+// running total: a single launch for the small arrays of small problems.
+// Each tile is loaded coalesced into shared memory, then every thread scans
+// its 8 consecutive items.  Block b scans array b of up to two (in0/out0,
+// in1/out1), so two scans of one size share a launch.
 template <class TIn, class TOut>
-__global__ void __launch_bounds__(1024) k_scan_single(const TIn* __restrict__ in, TOut* __restrict__ out,
+__global__ void __launch_bounds__(1024) k_scan_single(const TIn* __restrict__ in0, TOut* __restrict__ out0,
+                                                      const TIn* __restrict__ in1, TOut* __restrict__ out1,
                                                       int64_t n_in, int64_t m) {
+  constexpr int TILE = 1024 * SCAN_ITEMS;
+  // 32-bit inputs go through shared memory (32 KB); 64-bit ones (block totals) are read directly
+  constexpr bool SMEM = sizeof(TIn) == 4;
+  __shared__ int tile[SMEM ? TILE : 1];
   __shared__ long long wtot[32];
+  const TIn* __restrict__ in = blockIdx.x == 0 ? in0 : in1;
+  TOut* __restrict__ out = blockIdx.x == 0 ? out0 : out1;
   const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
   long long carry = 0;
-  for (int64_t tile0 = 0; tile0 < m; tile0 += 1024LL * SCAN_ITEMS) {
-    const int64_t base = tile0 + (int64_t)tid * SCAN_ITEMS;
+  for (int64_t tile0 = 0; tile0 < m; tile0 += TILE) {
+    if constexpr (SMEM) {
+#pragma unroll
+      for (int j = 0; j < SCAN_ITEMS; ++j) {
+        const int64_t idx = tile0 + (int64_t)j * 1024 + tid;
+        tile[j * 1024 + tid] = idx < n_in ? (int)in[idx] : 0;
+      }
+      __syncthreads();
+    }
     long long v[SCAN_ITEMS];
     long long s = 0;
 #pragma unroll
     for (int j = 0; j < SCAN_ITEMS; ++j) {
-      const int64_t idx = base + j;
-      const long long x = idx < n_in ? (long long)in[idx] : 0;
+      long long x;
+      if constexpr (SMEM) {
+        x = (long long)tile[tid * SCAN_ITEMS + j];
+      } else {
+        const int64_t idx = tile0 + (int64_t)tid * SCAN_ITEMS + j;
+        x = idx < n_in ? (long long)in[idx] : 0;
+      }
       v[j] = s;
       s += x;
     }
@@ -276,6 +298,7 @@ __global__ void __launch_bounds__(1024) k_scan_single(const TIn* __restrict__ in
     }
     __syncthreads();
     const long long excl = carry + (w > 0 ? wtot[w - 1] : 0) + inc - s;
+    const int64_t base = tile0 + (int64_t)tid * SCAN_ITEMS;
 #pragma unroll
     for (int j = 0; j < SCAN_ITEMS; ++j) {
       const int64_t idx = base + j;
@@ -289,7 +312,7 @@ __global__ void __launch_bounds__(1024) k_scan_single(const TIn* __restrict__ in
 template <class TIn, class TOut>
 static int scan_impl(const TIn* in, TOut* out, int64_t n_in, int64_t m, int64_t* scratch, cudaStream_t s) {
   if (m <= 65536) {
-    k_scan_single<TIn, TOut><<<1, 1024, 0, s>>>(in, out, n_in, m);
+    k_scan_single<TIn, TOut><<<1, 1024, 0, s>>>(in, out, in, out, n_in, m);
     GC_LAUNCHED();
     return GCSPH_OK;
   }
@@ -312,6 +335,17 @@ int exclusive_scan_i32_to_i64(const int32_t* in, int64_t* out, int64_t n, int64_
 }
 int exclusive_scan_i32_to_i32(const int32_t* in, int32_t* out, int64_t n, int64_t* scratch, cudaStream_t s) {
   return scan_impl<int32_t, int32_t>(in, out, n, n + 1, scratch, s);
+}
+int exclusive_scan2_i32_to_i64(const int32_t* in0, int64_t* out0, const int32_t* in1, int64_t* out1, int64_t n,
+                               int64_t* scratch, cudaStream_t s) {
+  if (n + 1 <= 65536) {
+    k_scan_single<int32_t, int64_t><<<2, 1024, 0, s>>>(in0, out0, in1, out1, n, n + 1);
+    GC_LAUNCHED();
+    return GCSPH_OK;
+  }
+  int rc = scan_impl<int32_t, int64_t>(in0, out0, n, n + 1, scratch, s);
+  if (rc) return rc;
+  return scan_impl<int32_t, int64_t>(in1, out1, n, n + 1, scratch, s);
 }
 
 }  // namespace gcsph

@@ -306,11 +306,17 @@ __device__ __forceinline__ void shift_of(int ent, const EnsInst& I, float& sx, f
   sz = (float)(r / 3 - 1) * I.csf;
 }
 
-template <int D>
+// L lanes share a particle: candidates go in chunks of L, and a ballot keeps
+// the hits in candidate order, so the list is the same for every L
+template <int D, int L>
 __global__ void __launch_bounds__(ENS_MAX_TPB) k_ens_nlist(EnsArr A, const EnsInst* __restrict__ T) {
   if (*A.ovf) return;
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < A.N; i += stride) {
+  const unsigned lanew = threadIdx.x & 31u;
+  const unsigned gbase = lanew & ~(unsigned)(L - 1);
+  const unsigned gm = L == 32 ? 0xffffffffu : (((1u << L) - 1u) << gbase);
+  const int lane = (int)(lanew - gbase);
+  const int64_t groups = ((int64_t)gridDim.x * blockDim.x) / L;
+  for (int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / L; i < A.N; i += groups) {
     const EnsInst& I = T[A.inst[i]];
     int cx0, cy0, cz0;
     cell_of(A.skey[i], I, cx0, cy0, cz0);
@@ -332,22 +338,36 @@ __global__ void __launch_bounds__(ENS_MAX_TPB) k_ens_nlist(EnsArr A, const EnsIn
           const int j0 = A.cellstart[row + cx], j1 = A.cellstart[row + cx + 1];
           const float shx = (float)dxc * I.csf, shy = (float)dy * I.csf, shz = (float)dz * I.csf;
           const int code = (dxc + 1) + 3 * (dy + 1) + 9 * (dz + 1);
-          for (int j = j0; j < j1; ++j) {
-            if (j == i) continue;
-            float d[D];
+          for (int jb = j0; jb < j1; jb += L) {
+            const int j = jb + lane;
+            bool hit = false;
+            if (j < j1 && j != i) {
+              float d[D];
 #pragma unroll
-            for (int q = 0; q < D; ++q) d[q] = (oi[q] - A.off[q][j]) - (q == 0 ? shx : (q == 1 ? shy : shz));
-            if (!(dot32<D>(d, d) < I.H2)) continue;
-            if (cnt < A.nls) A.nl[(int64_t)cnt * A.ncap + i] = (j << 5) | code;
-            ++cnt;
+              for (int q = 0; q < D; ++q) d[q] = (oi[q] - A.off[q][j]) - (q == 0 ? shx : (q == 1 ? shy : shz));
+              hit = dot32<D>(d, d) < I.H2;
+            }
+            if (L == 1) {
+              if (hit) {
+                if (cnt < A.nls) A.nl[(int64_t)cnt * A.ncap + i] = (j << 5) | code;
+                ++cnt;
+              }
+            } else {
+              const unsigned bal = (__ballot_sync(gm, hit) >> gbase) & (L == 32 ? 0xffffffffu : ((1u << L) - 1u));
+              const int at = cnt + __popc(bal & ((1u << lane) - 1u));
+              if (hit && at < A.nls) A.nl[(int64_t)at * A.ncap + i] = (j << 5) | code;
+              cnt += __popc(bal);
+            }
           }
         }
       }
     }
-    A.nlc[i] = cnt < A.nls ? cnt : A.nls;
-    if (cnt > A.nls) {
-      atomicMax(A.nlmax, cnt);
-      *A.ovf = 1;
+    if (lane == 0) {
+      A.nlc[i] = cnt < A.nls ? cnt : A.nls;
+      if (cnt > A.nls) {
+        atomicMax(A.nlmax, cnt);
+        *A.ovf = 1;
+      }
     }
   }
 }
@@ -771,7 +791,7 @@ struct EnsHostInst {
 
 struct EnsGraph {
   int64_t n_steps = -1, N = -1, K = -1, gen = -1;
-  int cur = -1, tpb = 0, timing = 0;
+  int cur = -1, tpb = 0, timing = 0, nl_lanes = 0;
   cudaGraphExec_t exec = nullptr;
   unsigned long long used = 0;
   long long launches = 0;
@@ -800,7 +820,8 @@ struct gcsph_ens {
   int tpb = 0;           // 0: not tuned yet
   bool tpb_fixed = false;
   int64_t tuned_n = 0;   // particle count the choice was made on
-  int sms = 0, occ[4] = {0, 0, 0, 0};
+  int sms = 0, occ[4] = {0, 0, 0, 0}, occ_nl[4] = {0, 0, 0, 0};
+  int nl_lanes = 4;      // lanes per particle in the list build (tuned after the block size)
   EnsGraph graphs[4];
   unsigned long long clock = 0;
   bool use_graphs = true;
@@ -1005,6 +1026,12 @@ int ens_occupancy(gcsph_ens* e) {
     else
       GC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_ens_stage<3, 2>, kTpbs[t], 0));
     e->occ[t] = std::max(b, 1);
+    int b2 = 0;
+    if (e->D == 2)
+      GC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b2, k_ens_nlist<2, 4>, kTpbs[t], 0));
+    else
+      GC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b2, k_ens_nlist<3, 4>, kTpbs[t], 0));
+    e->occ_nl[t] = std::max(b2, 1);
   }
   return GCSPH_OK;
 }
@@ -1049,7 +1076,18 @@ int ens_enqueue_step(gcsph_ens* e, cudaStream_t st, int tpb) {
   const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)e->sms * e->occ[t]));
   EnsArr A = ens_arr(e);
   timer_begin(T_PAIRS, st);
-  k_ens_nlist<D><<<grid, tpb, 0, st>>>(A, T);
+  {
+    // L lanes per particle in the list build (the list is the same for every L)
+    const int L = e->nl_lanes;
+    const int64_t gwant = (N * L + tpb - 1) / tpb;
+    const int g2 = (int)std::max<int64_t>(1, std::min<int64_t>(gwant, (int64_t)e->sms * e->occ_nl[t]));
+    switch (L) {
+      case 2: k_ens_nlist<D, 2><<<g2, tpb, 0, st>>>(A, T); break;
+      case 4: k_ens_nlist<D, 4><<<g2, tpb, 0, st>>>(A, T); break;
+      case 8: k_ens_nlist<D, 8><<<g2, tpb, 0, st>>>(A, T); break;
+      default: k_ens_nlist<D, 1><<<g2, tpb, 0, st>>>(A, T); break;
+    }
+  }
   GC_LAUNCHED();
   timer_end(T_PAIRS, st);
   timer_begin(T_STAGE1, st);
@@ -1101,8 +1139,8 @@ int ens_autotune(gcsph_ens* e, int32_t budget, int32_t* steps_used) {
   *steps_used = 0;
   if (e->tpb_fixed) return GCSPH_OK;
   if (e->tpb && e->tuned_n > 0 && e->N <= 2 * e->tuned_n && 2 * e->N >= e->tuned_n) return GCSPH_OK;
-  if (budget < 6) {
-    // too few steps to time three shapes: a default now, a tuning later
+  if (budget < 14) {
+    // too few steps to time the shapes: defaults now, a tuning later
     if (!e->tpb) e->tpb = 256;
     return GCSPH_OK;
   }
@@ -1129,6 +1167,29 @@ int ens_autotune(gcsph_ens* e, int32_t budget, int32_t* steps_used) {
       pick = kTpbs[t];
     }
   }
+  // then the lanes per particle of the list build, at that block size
+  const int lanes[4] = {1, 2, 4, 8};
+  float bestl = 1e30f;
+  int pickl = e->nl_lanes;
+  for (int t = 0; t < 4 && rc == GCSPH_OK; ++t) {
+    e->nl_lanes = lanes[t];
+    float tot = 0.f;
+    for (int r = 0; r < 2 && rc == GCSPH_OK; ++r) {
+      cudaEventRecord(a, e->st);
+      rc = enqueue_step(e, e->st, pick);
+      cudaEventRecord(b, e->st);
+      cudaEventSynchronize(b);
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, a, b);
+      if (r > 0) tot += ms;
+      *steps_used += 1;
+    }
+    if (tot < bestl) {
+      bestl = tot;
+      pickl = lanes[t];
+    }
+  }
+  e->nl_lanes = pickl;
   cudaEventDestroy(a);
   cudaEventDestroy(b);
   if (rc) return rc;
@@ -1142,7 +1203,7 @@ int ens_run_graph(gcsph_ens* e, int32_t n) {
   const int timing = timing_on() ? 1 : 0;
   for (EnsGraph& c : e->graphs)
     if (c.exec && c.n_steps == n && c.N == e->N && c.K == e->K && c.gen == e->gen && c.cur == e->cur &&
-        c.tpb == e->tpb && c.timing == timing)
+        c.tpb == e->tpb && c.timing == timing && c.nl_lanes == e->nl_lanes)
       g = &c;
   if (!g) {
     g = &e->graphs[0];
@@ -1175,6 +1236,7 @@ int ens_run_graph(gcsph_ens* e, int32_t n) {
       return rc;
     }
     g->timing = timing;
+    g->nl_lanes = e->nl_lanes;
     g->n_steps = n;
     g->N = e->N;
     g->K = e->K;
@@ -1554,9 +1616,10 @@ int ens_get_list_stride(gcsph_ens* e, int32_t* nls) {
   return GCSPH_OK;
 }
 
-int ens_get_tuning(gcsph_ens* e, int32_t* tpb, int64_t* captures, int64_t* replays) {
+int ens_get_tuning(gcsph_ens* e, int32_t* tpb, int32_t* nl_lanes, int64_t* captures, int64_t* replays) {
   if (!e) return fail(GCSPH_EINVAL, "null handle");
   if (tpb) *tpb = e->tpb;
+  if (nl_lanes) *nl_lanes = e->nl_lanes;
   if (captures) *captures = e->n_captures;
   if (replays) *replays = e->n_replays;
   return GCSPH_OK;

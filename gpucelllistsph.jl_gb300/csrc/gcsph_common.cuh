@@ -180,6 +180,9 @@ int exclusive_scan_i32_to_i64(const int32_t* in, int64_t* out, int64_t n, int64_
                               cudaStream_t s);
 int exclusive_scan_i32_to_i32(const int32_t* in, int32_t* out, int64_t n, int64_t* scratch,
                               cudaStream_t s);
+// two scans of n items each (one launch when they are small)
+int exclusive_scan2_i32_to_i64(const int32_t* in0, int64_t* out0, const int32_t* in1, int64_t* out1, int64_t n,
+                               int64_t* scratch, cudaStream_t s);
 
 // ----------------------------------------------------------------------------
 // per-kernel-family CUDA-event timers (off unless gcsph_timing_enable(1))

@@ -849,13 +849,10 @@ static int rebuild(sph_handle* h, const StepConst& c, int* ovf_dev) {
   }
   const double* xs[3] = {h->X[h->ix][0].as<double>(), h->X[h->ix][1].as<double>(),
                          D == 3 ? h->X[h->ix][2].as<double>() : nullptr};
-  if ((rc = core.build_pairs(xs, ovf_dev))) return rc;
+  if ((rc = core.build_pairs(xs, ovf_dev, true))) return rc;
   if ((rc = grow_entry_arrays<D>(h))) return rc;
-  // flat pair list: offsets by a device scan (no read-back), then the quads
+  // flat pair list: offsets scanned with the row offsets (no read-back), then the quads
   timer_begin(T_PAIRS, core.st);
-  if ((rc = exclusive_scan_i32_to_i64(core.cnt_up.as<int32_t>(), core.rs_up.as<int64_t>(), h->N,
-                                      core.scratch.as<int64_t>(), core.st)))
-    return rc;
   k_pair_quads<<<nblocks(h->N * QL, 256), 256, 0, core.st>>>(h->N, core.rs_full.as<int64_t>(), core.nbr.as<int32_t>(),
                                                          core.cnt_full.as<int32_t>(), core.cnt_up.as<int32_t>(),
                                                          core.rs_up.as<int64_t>(), ovf_dev, h->PQ.as<int4>());

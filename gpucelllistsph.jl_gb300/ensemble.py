@@ -150,9 +150,10 @@ class Ensemble:
         _lib.check(_lib.load().ens_set_tuning(self._h, int(tpb), int(bool(graphs))))
 
     def tuning(self):
-        t, a, b = C.c_int32(), C.c_int64(), C.c_int64()
-        _lib.check(_lib.load().ens_get_tuning(self._h, C.byref(t), C.byref(a), C.byref(b)))
-        return {"tpb": int(t.value), "captures": int(a.value), "replays": int(b.value)}
+        t, L, a, b = C.c_int32(), C.c_int32(), C.c_int64(), C.c_int64()
+        _lib.check(_lib.load().ens_get_tuning(self._h, C.byref(t), C.byref(L), C.byref(a), C.byref(b)))
+        return {"tpb": int(t.value), "list_lanes": int(L.value), "captures": int(a.value),
+                "replays": int(b.value)}
 
     def set_list_stride(self, nls: int):
         _lib.check(_lib.load().ens_set_list_stride(self._h, int(nls)))

@@ -311,9 +311,11 @@ int ens_step(gcsph_ens* e, int32_t n);
 int ens_get(gcsph_ens* e, int32_t slot, int32_t field, double* out_host);
 int ens_info(gcsph_ens* e, int32_t slot, int64_t* n, int64_t* steps, double* etime);
 int ens_totals(gcsph_ens* e, int32_t* ninst, int64_t* nparticles, int64_t* ncells);
-/* tpb 0 = autotune (128/256/512), graphs 0 = one launch sequence per step */
+/* tpb 0 = autotune: the pair passes' block size (128/256/512), then the
+ * lanes per particle of the neighbour-list build (1/2/4/8) -- the results do
+ * not depend on either.  graphs 0 = one launch sequence per step. */
 int ens_set_tuning(gcsph_ens* e, int32_t tpb, int32_t graphs);
-int ens_get_tuning(gcsph_ens* e, int32_t* tpb, int64_t* captures, int64_t* replays);
+int ens_get_tuning(gcsph_ens* e, int32_t* tpb, int32_t* nl_lanes, int64_t* captures, int64_t* replays);
 /* Entries per particle in the step's neighbour list (default 64 in 2-D, 256
  * in 3-D; it grows by itself when a row outgrows it, repeating the steps
  * that had not completed). */

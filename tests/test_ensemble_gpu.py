@@ -173,7 +173,8 @@ def test_launch_shape_and_capture_do_not_change_results(gpu_pkg, tpb, graphs):
     ens.set_tuning(tpb, graphs)
     e1, e2 = ens.add(a), ens.add(b)
     ens.step(5)
-    ens.step(7)
+    ens.step(16)
+    ref.step(9)
     for f in FIELDS:
         assert np.array_equal(ref.get(r1, f), ens.get(e1, f)), f
         assert np.array_equal(ref.get(r2, f), ens.get(e2, f)), f
@@ -183,7 +184,7 @@ def test_launch_shape_and_capture_do_not_change_results(gpu_pkg, tpb, graphs):
     if tpb:
         assert t["tpb"] == tpb
     else:
-        assert t["tpb"] in (128, 256, 512)
+        assert t["tpb"] in (128, 256, 512) and t["list_lanes"] in (1, 2, 4, 8)
 
 
 @pytest.mark.parametrize("graphs", [True, False])
