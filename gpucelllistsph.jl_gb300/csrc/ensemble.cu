@@ -375,11 +375,36 @@ __global__ void __launch_bounds__(ENS_MAX_TPB) k_ens_nlist(EnsArr A, const EnsIn
 // ---------------------------------------------------------------------------
 // the two pair passes over the step's neighbour list, persistent grid-stride
 // ---------------------------------------------------------------------------
+// lanes per particle in the pair passes: fixed per dimension (never tuned),
+// so that the summation order -- and every result -- is the same whatever
+// the launch shape and whatever else is in the ensemble
+template <int D>
+__host__ __device__ constexpr int stage_lanes() {
+  return D == 2 ? 4 : 8;
+}
+
+// Kahan partial sums of the L lanes of a particle, combined by a fixed butterfly
+template <int L>
+__device__ __forceinline__ float lane_total(const KSum& k, unsigned gm) {
+  float s = k.s, c = k.c;
+#pragma unroll
+  for (int o = L / 2; o > 0; o >>= 1) {
+    s += __shfl_xor_sync(gm, s, o);
+    c += __shfl_xor_sync(gm, c, o);
+  }
+  return s - c;
+}
+
 template <int D, int STAGE>
 __global__ void __launch_bounds__(ENS_MAX_TPB) k_ens_stage(EnsArr A, const EnsInst* __restrict__ T) {
   if (*A.ovf) return;
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < A.N; i += stride) {
+  constexpr int L = stage_lanes<D>();
+  const unsigned lanew = threadIdx.x & 31u;
+  const unsigned gbase = lanew & ~(unsigned)(L - 1);
+  const unsigned gm = ((1u << L) - 1u) << gbase;
+  const int lane = (int)(lanew - gbase);
+  const int64_t groups = ((int64_t)gridDim.x * blockDim.x) / L;
+  for (int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / L; i < A.N; i += groups) {
     const EnsInst& I = T[A.inst[i]];
     float oi[D], ohi[D], vi[D];
 #pragma unroll
@@ -395,7 +420,7 @@ __global__ void __launch_bounds__(ENS_MAX_TPB) k_ens_stage(EnsArr A, const EnsIn
     const int fbs = STAGE - 1;
     KSum drho, acc[D];
     const int nn = A.nlc[i];
-    for (int e = 0; e < nn; ++e) {
+    for (int e = lane; e < nn; e += L) {
       const int ent = A.nl[(int64_t)e * A.ncap + i];
       const Rec<D, STAGE> rec = load_rec<D, STAGE>(A.r1, A.r2, ent >> 5);
       float shx, shy, shz;
@@ -480,12 +505,14 @@ __global__ void __launch_bounds__(ENS_MAX_TPB) k_ens_stage(EnsArr A, const EnsIn
     }
     float a[D];
 #pragma unroll
-    for (int q = 0; q < D; ++q) a[q] = acc[q].s - (q == 1 ? I.g : 0.f);
+    for (int q = 0; q < D; ++q) a[q] = lane_total<L>(acc[q], gm) - (q == 1 ? I.g : 0.f);
+    const float drho_s = lane_total<L>(drho, gm);
+    if (lane != 0) continue;
     const float dt = (float)I.dt;
     if (STAGE == 1) {
       // update_ρp∂ρ∂tΔt!, update_vp∂v∂tΔt!, update_xpvΔt! at Δt/2
       const float hdt = 0.5f * dt;
-      float drh = A.drb[i] + drho.s * hdt;
+      float drh = A.drb[i] + drho_s * hdt;
       if (drh < 0.f && pti < 0) drh = 0.f;
       A.drh[i] = drh;
       float hh[D], ww[D];
@@ -502,7 +529,7 @@ __global__ void __launch_bounds__(ENS_MAX_TPB) k_ens_stage(EnsArr A, const EnsIn
     } else {
       // symplectic_update!: δρ_new = δρ - ρ 2ε/(2+ε), positions in FP64
       const float dr0 = A.dr[i];
-      const float epsi = -(drho.s / rhoi) * dt;
+      const float epsi = -(drho_s / rhoi) * dt;
       float dn = dr0 - (I.rho0 + dr0) * (2.f * epsi / (2.f + epsi));
       if (dn < 0.f && pti <= 1) dn = 0.f;
       A.dr[i] = dn;
@@ -1090,12 +1117,14 @@ int ens_enqueue_step(gcsph_ens* e, cudaStream_t st, int tpb) {
   }
   GC_LAUNCHED();
   timer_end(T_PAIRS, st);
+  const int64_t swant = (N * stage_lanes<D>() + tpb - 1) / tpb;
+  const int sgrid = (int)std::max<int64_t>(1, std::min<int64_t>(swant, (int64_t)e->sms * e->occ[t]));
   timer_begin(T_STAGE1, st);
-  k_ens_stage<D, 1><<<grid, tpb, 0, st>>>(A, T);
+  k_ens_stage<D, 1><<<sgrid, tpb, 0, st>>>(A, T);
   GC_LAUNCHED();
   timer_end(T_STAGE1, st);
   timer_begin(T_STAGE2, st);
-  k_ens_stage<D, 2><<<grid, tpb, 0, st>>>(A, T);
+  k_ens_stage<D, 2><<<sgrid, tpb, 0, st>>>(A, T);
   GC_LAUNCHED();
   timer_end(T_STAGE2, st);
   const int32_t ninst = (int32_t)e->inst.size();

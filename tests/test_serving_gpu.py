@@ -10,10 +10,11 @@ pytestmark = pytest.mark.gpu
 
 def _requests(pkg):
     S, w = pkg.serving, pkg.workloads
+    # the first three arrive together (admitted side by side), the rest while they run or after
     cases = [
         (0.00, w.sized_dam_break_2d(3000, 2.0, 0.02), 60),
-        (0.02, w.sized_dam_break_3d(2000, 1.0, 0.03), 45),
-        (0.03, w.sized_dam_break_2d(8000, 0.7, 0.01), 80),
+        (0.00, w.sized_dam_break_3d(2000, 1.0, 0.03), 45),
+        (0.00, w.sized_dam_break_2d(8000, 0.7, 0.01), 80),
         (0.05, w.sized_dam_break_2d(2500, 3.0, 0.015), 33),
         (0.06, w.sized_dam_break_3d(3000, 2.0, 0.02), 70),
     ]
@@ -29,9 +30,8 @@ def test_requests_in_the_mix_match_each_run_alone(gpu_pkg):
     assert stats["completed"] == len(reqs)
     assert stats["p99_s"] >= stats["p50_s"] > 0
     assert stats["particle_steps"] == sum(r.spec.n * r.steps for r in reqs)
-    # overlap: some request was admitted before another had finished
-    spans = sorted((r.admitted, r.done) for r in reqs)
-    assert any(spans[i + 1][0] < spans[i][1] for i in range(len(spans) - 1))
+    # overlap: requests that arrived together ran side by side
+    assert max(r.admitted for r in reqs[:3]) < min(r.done for r in reqs[:3])
     for r in reqs:
         ens = gpu_pkg.Ensemble(r.spec.D)
         s = ens.add(r.spec)
