@@ -395,6 +395,49 @@ def run_celllist(g, reps=10):
     return out
 
 
+# the reference's published stepsolve!(prob, 1) median on its 2-D Dp0.02
+# fixture with dist = H (test/devtest.jl:460-472), hardware not stated
+PUBLISHED_STEPSOLVE1_MS = 5.193
+
+
+def run_fixture(g, reps=50):
+    """stepsolve!(prob, 1) on the reference's own 2-D Dp0.02 fixture (4,704
+    fluid + 1,491 boundary particles, hydrostatic ρ, README parameters):
+    median wall time of one synchronous call through the public API, next to
+    the published figure; and the per-step time of stepsolve!(prob, 15)."""
+    import torch
+    fx = os.path.join(ROOT, "tests", "golden", "dambreak2d_dp002.npz")
+    case = g.workloads.load_fixture(fx)
+    system = g.GPUCellList(tuple(case.x), case.cellsize, case.dist)
+    prob = g.SPHProblem(system, case.dx, case.h, case.H, g.WendlandC2(dim=2), case.rho, case.ptype, case.rho0,
+                        case.m0, case.dt, case.alpha, case.c0, case.gamma, case.delta, case.CFL)
+    for _ in range(5):
+        prob.stepsolve(1)
+    ts = []
+    for _ in range(reps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        prob.stepsolve(1)
+        torch.cuda.synchronize()
+        ts.append(time.perf_counter() - t0)
+    one = 1e3 * statistics.median(ts)
+    prob.stepsolve(15)
+    prob.stepsolve(15)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(10):
+        prob.stepsolve(15)
+    torch.cuda.synchronize()
+    per_step = 1e3 * (time.perf_counter() - t0) / 150
+    prob.close()
+    system.close()
+    return {"workload": "reference fixture test/input Dp0.02 (2-D), dist = H", "particles": case.N,
+            "stepsolve_1_ms": one, "published_stepsolve_1_ms": PUBLISHED_STEPSOLVE1_MS,
+            "speedup_vs_published": PUBLISHED_STEPSOLVE1_MS / one, "stepsolve_15_ms_per_step": per_step,
+            "note": "published median from test/devtest.jl, hardware not stated; one call = one synchronous "
+                    "host round trip through the public API"}
+
+
 def run_c3(args):
     """3-D dam break at scale: fluid block 1.0 x 2.0 (vertical) x 0.5 m at
     dx = 0.01 (1.0 M fluid) in a 4.0 x 3.0 x 1.0 m tank with 3 boundary
@@ -600,6 +643,10 @@ def run_gb300(args):
            "kernel_timing": "library event timers over a second, instrumented pass of the same K bench steps",
            "graphs": dict(zip(("captured", "replayed"), prob.graph_stats()))}
     if not args.no_celllist:
+        try:
+            out["published_fixture"] = run_fixture(g)
+        except Exception as e:  # noqa: BLE001
+            out["published_fixture"] = {"error": repr(e)}
         try:
             out["celllist"] = run_celllist(g)
         except Exception as e:  # noqa: BLE001

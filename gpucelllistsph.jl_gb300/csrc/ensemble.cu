@@ -380,7 +380,7 @@ __global__ void __launch_bounds__(ENS_MAX_TPB) k_ens_nlist(EnsArr A, const EnsIn
 // the launch shape and whatever else is in the ensemble
 template <int D>
 __host__ __device__ constexpr int stage_lanes() {
-  return D == 2 ? 4 : 8;
+  return D == 2 ? 2 : 8;
 }
 
 // Kahan partial sums of the L lanes of a particle, combined by a fixed butterfly
