@@ -262,7 +262,7 @@ def run_batched(g, args, plain_c1):
         ens.add(g.spec_from_case(case, alpha=al, delta=de))
     t_admit = time.perf_counter() - t0
     tot = ens.totals()
-    ens.step(10)  # tuning (three block sizes) + warm-up
+    ens.step(30)  # tuning (block size, list lanes, list tiling: 24 steps) + warm-up
     ens.step(args.batched_steps)  # captures the graph of this many steps
     torch.cuda.synchronize()
     L = g.load_library()
@@ -455,7 +455,7 @@ def run_c3(args):
     # FP32 ensemble
     ens = g.Ensemble(3)
     slot = ens.add(g.spec_from_case(case))
-    ens.step(10)
+    ens.step(30)  # tuning (24 steps) + warm-up
     torch.cuda.synchronize()
     # a fresh instance for the measured run, so both start from the same state
     ens.remove(slot)

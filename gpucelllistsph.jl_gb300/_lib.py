@@ -89,6 +89,8 @@ _SIGS = {
     "ens_totals": (C.c_int, [vp, C.POINTER(i32), C.POINTER(i64), C.POINTER(i64)]),
     "ens_set_tuning": (C.c_int, [vp, i32, i32]),
     "ens_get_tuning": (C.c_int, [vp, C.POINTER(i32), C.POINTER(i32), C.POINTER(i64), C.POINTER(i64)]),
+    "ens_set_list_build": (C.c_int, [vp, i32, i32, i32, i32]),
+    "ens_get_list_build": (C.c_int, [vp, C.POINTER(i32), C.POINTER(i32), C.POINTER(i32), C.POINTER(i32)]),
     "ens_set_list_stride": (C.c_int, [vp, i32]),
     "ens_get_list_stride": (C.c_int, [vp, C.POINTER(i32)]),
     "sph_get_field": (C.c_int, [vp, i32, vp]),

@@ -306,8 +306,35 @@ __device__ __forceinline__ void shift_of(int ent, const EnsInst& I, float& sx, f
   sz = (float)(r / 3 - 1) * I.csf;
 }
 
-// L lanes share a particle: candidates go in chunks of L, and a ballot keeps
-// the hits in candidate order, so the list is the same for every L
+// a candidate's verdict: with L lanes on a particle, a ballot keeps the hits
+// in candidate order, so the list is the same for every L
+template <int L>
+__device__ __forceinline__ void nl_emit(const EnsArr& A, int64_t i, int lane, unsigned gm, unsigned gbase, bool hit,
+                                        int j, int code, int& cnt) {
+  if (L == 1) {
+    if (hit) {
+      if (cnt < A.nls) A.nl[(int64_t)cnt * A.ncap + i] = (j << 5) | code;
+      ++cnt;
+    }
+  } else {
+    const unsigned bal = (__ballot_sync(gm, hit) >> gbase) & (L == 32 ? 0xffffffffu : ((1u << L) - 1u));
+    const int at = cnt + __popc(bal & ((1u << lane) - 1u));
+    if (hit && at < A.nls) A.nl[(int64_t)at * A.ncap + i] = (j << 5) | code;
+    cnt += __popc(bal);
+  }
+}
+
+__device__ __forceinline__ void nl_close(const EnsArr& A, int64_t i, int lane, int cnt) {
+  if (lane == 0) {
+    A.nlc[i] = cnt < A.nls ? cnt : A.nls;
+    if (cnt > A.nls) {
+      atomicMax(A.nlmax, cnt);
+      *A.ovf = 1;
+    }
+  }
+}
+
+// L lanes share a particle: candidates go in chunks of L
 template <int D, int L>
 __global__ void __launch_bounds__(ENS_MAX_TPB) k_ens_nlist(EnsArr A, const EnsInst* __restrict__ T) {
   if (*A.ovf) return;
@@ -347,28 +374,214 @@ __global__ void __launch_bounds__(ENS_MAX_TPB) k_ens_nlist(EnsArr A, const EnsIn
               for (int q = 0; q < D; ++q) d[q] = (oi[q] - A.off[q][j]) - (q == 0 ? shx : (q == 1 ? shy : shz));
               hit = dot32<D>(d, d) < I.H2;
             }
-            if (L == 1) {
-              if (hit) {
-                if (cnt < A.nls) A.nl[(int64_t)cnt * A.ncap + i] = (j << 5) | code;
-                ++cnt;
-              }
-            } else {
-              const unsigned bal = (__ballot_sync(gm, hit) >> gbase) & (L == 32 ? 0xffffffffu : ((1u << L) - 1u));
-              const int at = cnt + __popc(bal & ((1u << lane) - 1u));
-              if (hit && at < A.nls) A.nl[(int64_t)at * A.ncap + i] = (j << 5) | code;
-              cnt += __popc(bal);
-            }
+            nl_emit<L>(A, i, lane, gm, gbase, hit, j, code, cnt);
           }
         }
       }
     }
-    if (lane == 0) {
-      A.nlc[i] = cnt < A.nls ? cnt : A.nls;
-      if (cnt > A.nls) {
-        atomicMax(A.nlmax, cnt);
-        *A.ovf = 1;
+    nl_close(A, i, lane, cnt);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Tiled list build: a block takes a tile of up to `cpb` consecutive cells of
+// one x-row of one instance.  In the sorted particle order the tile's 3^D
+// neighbourhood is 3^(D-1) contiguous particle ranges, one per (dy, dz) row
+// (cells cx0-1 .. cx1), so the block stages their FP32 offsets in shared
+// memory with coalesced copies (cp.async) and runs the candidate loop of
+// k_ens_nlist out of shared memory: the same candidates in the same order
+// through the same ballot, so the list is the same for every variant.  With
+// staging depth 2 the next tile's ranges are copied while the current tile is
+// tested.  A tile whose neighbourhood does not fit the buffer reads global
+// memory instead.  Tiles are numbered instance by instance (tile_off: the
+// first tile of each instance, in packing order), row by row, along x.
+// ---------------------------------------------------------------------------
+constexpr int TILE_CPB_MAX = 16;
+constexpr int TILE_TPB = 128;
+
+__device__ __forceinline__ void cp_async4(void* dst_smem, const void* src) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(dst_smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
+struct TileSm {
+  int s, cxa, rowkey;           // instance, first staged cell, key of cell 0 of the home row
+  int hs, he, total, staged;    // home particles [hs, he), staged particle count, fits the buffer
+  int rok[9];                   // the (dy, dz) row lies inside the grid
+  int delta[9];                 // buffer index - particle index, per row
+  int cs[9][TILE_CPB_MAX + 3];  // cell starts (particle indices) of cells cxa .. cxb + 1, per row
+};
+
+// the geometry of tile t, by warp 0
+template <int D>
+__device__ void tile_geometry(const EnsArr& A, const EnsInst* __restrict__ T, const int* __restrict__ tile_off,
+                              int ninst, int cpb, int cap, int t, TileSm& G) {
+  constexpr int NR = D == 3 ? 9 : 3;
+  const int lane = threadIdx.x & 31;
+  int s = 0;
+  if (lane == 0) {
+    int lo = 0, hi = ninst;  // tile_off[lo] <= t < tile_off[hi]
+    while (hi - lo > 1) {
+      const int mid = (lo + hi) >> 1;
+      if (tile_off[mid] <= t)
+        lo = mid;
+      else
+        hi = mid;
+    }
+    s = lo;
+  }
+  s = __shfl_sync(0xffffffffu, s, 0);
+  const EnsInst& I = T[s];
+  const int tpr = (I.nc[0] + cpb - 1) / cpb;
+  const int lt = t - tile_off[s];
+  const int row = lt / tpr;
+  const int cx0 = (lt - row * tpr) * cpb;
+  const int cx1 = min(cx0 + cpb, I.nc[0]);
+  const int cy = row % I.nc[1], cz = row / I.nc[1];
+  const int cxa = max(cx0 - 1, 0), cxb = min(cx1, I.nc[0] - 1);
+  const int ncs = cxb - cxa + 2;
+  for (int q = lane; q < NR * ncs; q += 32) {
+    const int r = q / ncs, c = q - r * ncs;
+    const int y = cy + (r % 3) - 1, z = cz + (D == 3 ? r / 3 - 1 : 0);
+    const bool in = y >= 0 && y < I.nc[1] && z >= 0 && z < I.nc[2];
+    G.cs[r][c] = in ? A.cellstart[I.key_off + cxa + c + I.nc[0] * (y + I.nc[1] * z)] : 0;
+  }
+  __syncwarp();
+  if (lane == 0) {
+    int tot = 0;
+    for (int r = 0; r < NR; ++r) {
+      const int y = cy + (r % 3) - 1, z = cz + (D == 3 ? r / 3 - 1 : 0);
+      const bool in = y >= 0 && y < I.nc[1] && z >= 0 && z < I.nc[2];
+      G.rok[r] = in;
+      G.delta[r] = tot - G.cs[r][0];
+      tot += in ? G.cs[r][ncs - 1] - G.cs[r][0] : 0;
+    }
+    constexpr int CR = D == 3 ? 4 : 1;  // the home row (dy = dz = 0)
+    G.s = s;
+    G.cxa = cxa;
+    G.rowkey = I.key_off + I.nc[0] * (cy + I.nc[1] * cz);
+    G.hs = G.cs[CR][cx0 - cxa];
+    G.he = G.cs[CR][cx1 - cxa];
+    G.total = tot;
+    G.staged = tot <= cap;
+  }
+}
+
+// copies of the tile's staged offsets (every thread; cp.async, not waited on)
+template <int D>
+__device__ __forceinline__ void tile_stage(const EnsArr& A, const TileSm& G, float* buf, int cap) {
+  constexpr int NR = D == 3 ? 9 : 3;
+  if (!G.staged || G.hs == G.he) return;  // no home particles: nothing to test
+  for (int q = threadIdx.x; q < G.total; q += blockDim.x) {
+    // row r fills buffer indices [delta[r] + cs[r][0], delta[r + 1] + cs[r + 1][0])
+    int r = 0;
+    while (r < NR - 1 && q >= G.delta[r + 1] + G.cs[r + 1][0]) ++r;
+    const int j = q - G.delta[r];
+#pragma unroll
+    for (int d = 0; d < D; ++d) cp_async4(buf + d * cap + q, A.off[d] + j);
+  }
+}
+
+// the home particles of one tile: k_ens_nlist's loop, offsets from the buffer
+template <int D, int L, bool STAGED>
+__device__ __forceinline__ void tile_particles(const EnsArr& A, const EnsInst& I, const TileSm& G,
+                                               const float* __restrict__ buf, int cap) {
+  constexpr int NR = D == 3 ? 9 : 3;
+  constexpr int CR = D == 3 ? 4 : 1;
+  const unsigned lanew = threadIdx.x & 31u;
+  const unsigned gbase = lanew & ~(unsigned)(L - 1);
+  const unsigned gm = L == 32 ? 0xffffffffu : (((1u << L) - 1u) << gbase);
+  const int lane = (int)(lanew - gbase);
+  const int groups = blockDim.x / L;
+  for (int i = G.hs + (int)threadIdx.x / L; i < G.he; i += groups) {
+    const int cxi = A.skey[i] - G.rowkey;
+    float oi[D];
+#pragma unroll
+    for (int d = 0; d < D; ++d) oi[d] = STAGED ? buf[d * cap + i + G.delta[CR]] : A.off[d][i];
+    int cnt = 0;
+    for (int r = 0; r < NR; ++r) {
+      if (!G.rok[r]) continue;
+      const int dy = r % 3 - 1, dz = D == 3 ? r / 3 - 1 : 0;
+      const int dl = G.delta[r];
+      for (int dxc = -1; dxc <= 1; ++dxc) {
+        const int cx = cxi + dxc;
+        if (cx < 0 || cx >= I.nc[0]) continue;
+        const int lc = cx - G.cxa;
+        const int j0 = G.cs[r][lc], j1 = G.cs[r][lc + 1];
+        const float shx = (float)dxc * I.csf, shy = (float)dy * I.csf, shz = (float)dz * I.csf;
+        const int code = (dxc + 1) + 3 * (dy + 1) + 9 * (dz + 1);
+        for (int jb = j0; jb < j1; jb += L) {
+          const int j = jb + lane;
+          bool hit = false;
+          if (j < j1 && j != i) {
+            float d[D];
+#pragma unroll
+            for (int q = 0; q < D; ++q)
+              d[q] = (oi[q] - (STAGED ? buf[q * cap + j + dl] : A.off[q][j])) - (q == 0 ? shx : (q == 1 ? shy : shz));
+            hit = dot32<D>(d, d) < I.H2;
+          }
+          nl_emit<L>(A, i, lane, gm, gbase, hit, j, code, cnt);
+        }
       }
     }
+    nl_close(A, i, lane, cnt);
+  }
+}
+
+template <int D, int L, int DEPTH>
+__global__ void __launch_bounds__(TILE_TPB) k_ens_nlist_tile(EnsArr A, const EnsInst* __restrict__ T,
+                                                             const int* __restrict__ tile_off, int ninst, int cpb,
+                                                             int cap) {
+  if (*A.ovf) return;
+  extern __shared__ float4 tile_smem[];
+  float* const sbuf = reinterpret_cast<float*>(tile_smem);
+  __shared__ TileSm G[DEPTH];
+  const int ntiles = tile_off[ninst];
+  const bool w0 = threadIdx.x < 32;
+  int t = blockIdx.x;
+  if (t >= ntiles) return;
+  int cur = 0;
+  if (w0) tile_geometry<D>(A, T, tile_off, ninst, cpb, cap, t, G[0]);
+  __syncthreads();
+  tile_stage<D>(A, G[0], sbuf, cap);
+  cp_async_commit();
+  for (;;) {
+    const int nt = t + gridDim.x;
+    if (DEPTH == 2) {
+      // the next tile's copies go out before this tile is tested
+      const int nx = cur ^ 1;
+      if (nt < ntiles) {
+        if (w0) tile_geometry<D>(A, T, tile_off, ninst, cpb, cap, nt, G[nx]);
+        __syncthreads();
+        tile_stage<D>(A, G[nx], sbuf + nx * D * cap, cap);
+      }
+      cp_async_commit();
+      cp_async_wait<1>();
+    } else {
+      cp_async_wait<0>();
+    }
+    __syncthreads();
+    const TileSm& g = G[cur];
+    if (g.staged)
+      tile_particles<D, L, true>(A, T[g.s], g, sbuf + cur * D * cap, cap);
+    else
+      tile_particles<D, L, false>(A, T[g.s], g, nullptr, cap);
+    if (nt >= ntiles) break;
+    __syncthreads();  // the buffer and geometry just used are refilled next
+    if (DEPTH == 2) {
+      cur ^= 1;
+    } else {
+      if (w0) tile_geometry<D>(A, T, tile_off, ninst, cpb, cap, nt, G[0]);
+      __syncthreads();
+      tile_stage<D>(A, G[0], sbuf, cap);
+      cp_async_commit();
+    }
+    t = nt;
   }
 }
 
@@ -818,7 +1031,7 @@ struct EnsHostInst {
 
 struct EnsGraph {
   int64_t n_steps = -1, N = -1, K = -1, gen = -1;
-  int cur = -1, tpb = 0, timing = 0, nl_lanes = 0;
+  int cur = -1, tpb = 0, timing = 0, nl_lanes = 0, nl_cpb = -1, nl_depth = 0, nl_cap = 0;
   cudaGraphExec_t exec = nullptr;
   unsigned long long used = 0;
   long long launches = 0;
@@ -849,6 +1062,14 @@ struct gcsph_ens {
   int64_t tuned_n = 0;   // particle count the choice was made on
   int sms = 0, occ[4] = {0, 0, 0, 0}, occ_nl[4] = {0, 0, 0, 0};
   int nl_lanes = 4;      // lanes per particle in the list build (tuned after the block size)
+  int nl_cpb = 0;        // list build: 0 = a thread group per particle, else tiles of nl_cpb cells per block
+  int nl_depth = 1;      // tiles staged ahead (1 or 2)
+  int nl_cap_fix = 0;    // staged particles per tile buffer (0: from the lattice estimate)
+  bool nl_fixed = false; // list build set by the caller: not tuned
+  int tune_phase = 0;    // tuning done so far: 1 block size, 2 list lanes, 3 list tiles
+  double ppc = 1.0;      // particles per cell estimate, (H / dx)^D over the instances
+  DevBuf TILES;          // first tile of each instance, one table per cells-per-block choice
+  int ntiles[4] = {0, 0, 0, 0};
   EnsGraph graphs[4];
   unsigned long long clock = 0;
   bool use_graphs = true;
@@ -860,6 +1081,26 @@ struct gcsph_ens {
 namespace {
 
 const int kTpbs[3] = {128, 256, 512};
+const int kCpbs[4] = {2, 4, 8, 16};  // cells-per-block choices of the tiled list build
+
+int cpb_index(int cpb) {
+  for (int t = 0; t < 4; ++t)
+    if (kCpbs[t] == cpb) return t;
+  return -1;
+}
+
+// staged particles a tile buffer holds: the lattice estimate of the
+// neighbourhood with a margin, within 96 KB of shared memory per block
+int tile_cap(const gcsph_ens* e, int cpb, int depth) {
+  const int per = depth * e->D * (int)sizeof(float);
+  const int hi = (96 * 1024) / per / 32 * 32;
+  if (e->nl_cap_fix > 0) return std::min(e->nl_cap_fix, hi);
+  const double rows = e->D == 3 ? 9.0 : 3.0;
+  const double want = 1.25 * (cpb + 2) * rows * e->ppc + 32.0;
+  int cap = (int)std::min<double>(want, (double)hi);
+  cap = (cap + 31) / 32 * 32;
+  return std::max(32, std::min(cap, hi));
+}
 
 EnsState ens_state(gcsph_ens* e, int b) {
   EnsState s{};
@@ -1021,6 +1262,30 @@ int ens_relayout(gcsph_ens* e) {
   if ((rc = e->TAB.ensure(sizeof(EnsInst) * std::max<size_t>(tab.size(), 1), e->st))) return rc;
   if (!tab.empty())
     GC_CUDA(cudaMemcpyAsync(e->TAB.p, tab.data(), sizeof(EnsInst) * tab.size(), cudaMemcpyHostToDevice, e->st));
+  // tile tables of the tiled list build (one per cells-per-block choice) and
+  // the particles-per-cell estimate that sizes its buffers
+  {
+    const size_t ni = e->inst.size();
+    std::vector<int32_t> tiles(4 * (ni + 1));
+    for (int c = 0; c < 4; ++c) {
+      int64_t acc = 0;
+      for (size_t si = 0; si < ni; ++si) {
+        const EnsInst& I = e->inst[si].dev;
+        tiles[c * (ni + 1) + si] = (int32_t)acc;
+        acc += (int64_t)((I.nc[0] + kCpbs[c] - 1) / kCpbs[c]) * I.nc[1] * I.nc[2];
+      }
+      tiles[c * (ni + 1) + ni] = (int32_t)acc;
+      e->ntiles[c] = (int)acc;
+    }
+    double ppc = 1.0;
+    for (const EnsHostInst& h : e->inst)
+      if (h.prm.dx > 0) ppc = std::max(ppc, std::pow(h.prm.H / h.prm.dx, (double)e->D));
+    e->ppc = ppc;
+    if ((rc = e->TILES.ensure(sizeof(int32_t) * tiles.size(), e->st))) return rc;
+    GC_CUDA(cudaMemcpyAsync(e->TILES.p, tiles.data(), sizeof(int32_t) * tiles.size(), cudaMemcpyHostToDevice,
+                            e->st));
+    GC_CUDA(cudaStreamSynchronize(e->st));
+  }
   std::vector<int32_t> isteps(e->inst.size());
   for (size_t s = 0; s < e->inst.size(); ++s) isteps[s] = (int32_t)(e->inst[s].steps % 2000000000LL);
   if ((rc = e->ISTEP.ensure(sizeof(int32_t) * std::max<size_t>(isteps.size(), 1), e->st))) return rc;
@@ -1039,6 +1304,18 @@ int ens_relayout(gcsph_ens* e) {
   e->gen += 1;
   graphs_free(e);
   return GCSPH_OK;
+}
+
+// the tiled list build's kernel for (lanes, staging depth)
+using TileKern = void (*)(EnsArr, const EnsInst*, const int*, int, int, int);
+template <int D>
+TileKern tile_kernel(int L, int depth) {
+  switch (L) {
+    case 2: return depth == 2 ? k_ens_nlist_tile<D, 2, 2> : k_ens_nlist_tile<D, 2, 1>;
+    case 4: return depth == 2 ? k_ens_nlist_tile<D, 4, 2> : k_ens_nlist_tile<D, 4, 1>;
+    case 8: return depth == 2 ? k_ens_nlist_tile<D, 8, 2> : k_ens_nlist_tile<D, 8, 1>;
+    default: return depth == 2 ? k_ens_nlist_tile<D, 1, 2> : k_ens_nlist_tile<D, 1, 1>;
+  }
 }
 
 int ens_occupancy(gcsph_ens* e) {
@@ -1060,6 +1337,16 @@ int ens_occupancy(gcsph_ens* e) {
       GC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b2, k_ens_nlist<3, 4>, kTpbs[t], 0));
     e->occ_nl[t] = std::max(b2, 1);
   }
+  const int lanes[4] = {1, 2, 4, 8};
+  for (int l = 0; l < 4; ++l)
+    for (int dp = 1; dp <= 2; ++dp) {
+      if (e->D == 2)
+        GC_CUDA(cudaFuncSetAttribute(tile_kernel<2>(lanes[l], dp), cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     96 * 1024));
+      else
+        GC_CUDA(cudaFuncSetAttribute(tile_kernel<3>(lanes[l], dp), cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     96 * 1024));
+    }
   return GCSPH_OK;
 }
 
@@ -1103,7 +1390,18 @@ int ens_enqueue_step(gcsph_ens* e, cudaStream_t st, int tpb) {
   const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)e->sms * e->occ[t]));
   EnsArr A = ens_arr(e);
   timer_begin(T_PAIRS, st);
-  {
+  if (e->nl_cpb > 0) {
+    // tiles of nl_cpb cells per block, neighbourhood staged in shared memory
+    const int ci = cpb_index(e->nl_cpb);
+    const int cap = tile_cap(e, e->nl_cpb, e->nl_depth);
+    const size_t smem = sizeof(float) * (size_t)D * cap * e->nl_depth;
+    const TileKern k = tile_kernel<D>(e->nl_lanes, e->nl_depth);
+    int b = 0;
+    GC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k, TILE_TPB, smem));
+    const int ni = (int)e->inst.size();
+    const int g3 = std::max(1, std::min(e->ntiles[ci], e->sms * std::max(b, 1)));
+    k<<<g3, TILE_TPB, smem, st>>>(A, T, e->TILES.as<int32_t>() + (size_t)ci * (ni + 1), ni, e->nl_cpb, cap);
+  } else {
     // L lanes per particle in the list build (the list is the same for every L)
     const int L = e->nl_lanes;
     const int64_t gwant = (N * L + tpb - 1) / tpb;
@@ -1161,70 +1459,100 @@ int enqueue_step(gcsph_ens* e, cudaStream_t st, int tpb) {
   return e->D == 2 ? ens_enqueue_step<2>(e, st, tpb) : ens_enqueue_step<3>(e, st, tpb);
 }
 
-// block size of the pair passes: each candidate runs two real steps (the
-// arithmetic per particle does not depend on the launch shape, so tuning
-// steps are ordinary steps), the fastest pair of passes wins
+// Launch shapes, tuned in three phases on real steps (the arithmetic per
+// particle does not depend on the launch shape, so tuning steps are ordinary
+// steps); each candidate runs two steps and the second is timed:
+//   1. block size of the pair passes (6 steps);
+//   2. lanes per particle of the list build (8 steps);
+//   3. the list build's tiling: a thread group per particle against tiles of
+//      cells-per-block cells staged in shared memory, three tile sizes at
+//      staging depth 1, then the best at depth 2 (10 steps).
+// A phase runs when the call has the steps for it; the rest wait for a later
+// call.  A particle count that moves past 2x of the tuned one starts over.
 int ens_autotune(gcsph_ens* e, int32_t budget, int32_t* steps_used) {
   *steps_used = 0;
   if (e->tpb_fixed) return GCSPH_OK;
-  if (e->tpb && e->tuned_n > 0 && e->N <= 2 * e->tuned_n && 2 * e->N >= e->tuned_n) return GCSPH_OK;
-  if (budget < 14) {
-    // too few steps to time the shapes: defaults now, a tuning later
-    if (!e->tpb) e->tpb = 256;
-    return GCSPH_OK;
-  }
+  if (e->tune_phase > 0 && !(e->N <= 2 * e->tuned_n && 2 * e->N >= e->tuned_n)) e->tune_phase = 0;
+  if (e->tune_phase >= 3) return GCSPH_OK;
+  if (!e->tpb) e->tpb = 256;
   cudaEvent_t a, b;
   GC_CUDA(cudaEventCreate(&a));
   GC_CUDA(cudaEventCreate(&b));
-  float best = 1e30f;
-  int pick = 256;
   int rc = GCSPH_OK;
-  for (int t = 0; t < 3 && rc == GCSPH_OK; ++t) {
-    float tot = 0.f;
+  auto timed = [&](int tpb) -> float {
+    float last = 0.f;
     for (int r = 0; r < 2 && rc == GCSPH_OK; ++r) {
       cudaEventRecord(a, e->st);
-      rc = enqueue_step(e, e->st, kTpbs[t]);
+      rc = enqueue_step(e, e->st, tpb);
       cudaEventRecord(b, e->st);
       cudaEventSynchronize(b);
       float ms = 0.f;
       cudaEventElapsedTime(&ms, a, b);
-      if (r > 0) tot += ms;  // the first run of each shape warms caches
+      last = ms;  // the first run of each shape warms caches
       *steps_used += 1;
     }
-    if (tot < best) {
-      best = tot;
-      pick = kTpbs[t];
+    return last;
+  };
+  if (e->tune_phase == 0 && budget - *steps_used >= 6) {
+    float best = 1e30f;
+    int pick = 256;
+    for (int t = 0; t < 3 && rc == GCSPH_OK; ++t) {
+      const float ms = timed(kTpbs[t]);
+      if (ms < best) {
+        best = ms;
+        pick = kTpbs[t];
+      }
     }
+    e->tpb = pick;
+    e->tuned_n = e->N;
+    e->tune_phase = 1;
   }
-  // then the lanes per particle of the list build, at that block size
-  const int lanes[4] = {1, 2, 4, 8};
-  float bestl = 1e30f;
-  int pickl = e->nl_lanes;
-  for (int t = 0; t < 4 && rc == GCSPH_OK; ++t) {
-    e->nl_lanes = lanes[t];
-    float tot = 0.f;
-    for (int r = 0; r < 2 && rc == GCSPH_OK; ++r) {
-      cudaEventRecord(a, e->st);
-      rc = enqueue_step(e, e->st, pick);
-      cudaEventRecord(b, e->st);
-      cudaEventSynchronize(b);
-      float ms = 0.f;
-      cudaEventElapsedTime(&ms, a, b);
-      if (r > 0) tot += ms;
-      *steps_used += 1;
+  if (e->tune_phase == 1 && e->nl_fixed) e->tune_phase = 3;
+  if (rc == GCSPH_OK && e->tune_phase == 1 && budget - *steps_used >= 8) {
+    const int lanes[4] = {1, 2, 4, 8};
+    const int cpb0 = e->nl_cpb;
+    e->nl_cpb = 0;
+    float best = 1e30f;
+    int pick = e->nl_lanes;
+    for (int t = 0; t < 4 && rc == GCSPH_OK; ++t) {
+      e->nl_lanes = lanes[t];
+      const float ms = timed(e->tpb);
+      if (ms < best) {
+        best = ms;
+        pick = lanes[t];
+      }
     }
-    if (tot < bestl) {
-      bestl = tot;
-      pickl = lanes[t];
-    }
+    e->nl_lanes = pick;
+    e->nl_cpb = cpb0;
+    e->tune_phase = 2;
   }
-  e->nl_lanes = pickl;
+  if (rc == GCSPH_OK && e->tune_phase == 2 && budget - *steps_used >= 10) {
+    const int c2[3] = {4, 8, 16}, c3[3] = {2, 4, 8};
+    const int* cpbs = e->D == 2 ? c2 : c3;
+    e->nl_cpb = 0;
+    e->nl_depth = 1;
+    float best = timed(e->tpb);
+    int pick = 0, pickd = 1;
+    for (int t = 0; t < 3 && rc == GCSPH_OK; ++t) {
+      e->nl_cpb = cpbs[t];
+      const float ms = timed(e->tpb);
+      if (ms < best) {
+        best = ms;
+        pick = cpbs[t];
+      }
+    }
+    if (pick > 0 && rc == GCSPH_OK) {
+      e->nl_cpb = pick;
+      e->nl_depth = 2;
+      if (timed(e->tpb) < best) pickd = 2;
+    }
+    e->nl_cpb = pick;
+    e->nl_depth = pickd;
+    e->tune_phase = 3;
+  }
   cudaEventDestroy(a);
   cudaEventDestroy(b);
-  if (rc) return rc;
-  e->tpb = pick;
-  e->tuned_n = e->N;
-  return GCSPH_OK;
+  return rc;
 }
 
 int ens_run_graph(gcsph_ens* e, int32_t n) {
@@ -1232,7 +1560,8 @@ int ens_run_graph(gcsph_ens* e, int32_t n) {
   const int timing = timing_on() ? 1 : 0;
   for (EnsGraph& c : e->graphs)
     if (c.exec && c.n_steps == n && c.N == e->N && c.K == e->K && c.gen == e->gen && c.cur == e->cur &&
-        c.tpb == e->tpb && c.timing == timing && c.nl_lanes == e->nl_lanes)
+        c.tpb == e->tpb && c.timing == timing && c.nl_lanes == e->nl_lanes && c.nl_cpb == e->nl_cpb &&
+        c.nl_depth == e->nl_depth && c.nl_cap == e->nl_cap_fix)
       g = &c;
   if (!g) {
     g = &e->graphs[0];
@@ -1266,6 +1595,9 @@ int ens_run_graph(gcsph_ens* e, int32_t n) {
     }
     g->timing = timing;
     g->nl_lanes = e->nl_lanes;
+    g->nl_cpb = e->nl_cpb;
+    g->nl_depth = e->nl_depth;
+    g->nl_cap = e->nl_cap_fix;
     g->n_steps = n;
     g->N = e->N;
     g->K = e->K;
@@ -1625,6 +1957,7 @@ int ens_set_tuning(gcsph_ens* e, int32_t tpb, int32_t graphs) {
   e->tpb = tpb;
   e->tpb_fixed = tpb != 0;
   e->tuned_n = 0;
+  e->tune_phase = 0;
   e->use_graphs = graphs != 0;
   return GCSPH_OK;
 }
@@ -1642,6 +1975,35 @@ int ens_set_list_stride(gcsph_ens* e, int32_t nls) {
 int ens_get_list_stride(gcsph_ens* e, int32_t* nls) {
   if (!e || !nls) return fail(GCSPH_EINVAL, "null argument");
   *nls = e->nls;
+  return GCSPH_OK;
+}
+
+int ens_set_list_build(gcsph_ens* e, int32_t lanes, int32_t cells_per_block, int32_t depth, int32_t cap) {
+  if (!e) return fail(GCSPH_EINVAL, "null handle");
+  if (lanes == 0) {
+    e->nl_fixed = false;
+    if (e->tune_phase > 1) e->tune_phase = 1;
+    return GCSPH_OK;
+  }
+  if (!(lanes == 1 || lanes == 2 || lanes == 4 || lanes == 8)) return fail(GCSPH_EINVAL, "lanes must be 0, 1, 2, 4 or 8");
+  if (!(cells_per_block == 0 || cpb_index(cells_per_block) >= 0))
+    return fail(GCSPH_EINVAL, "cells per block must be 0, 2, 4, 8 or 16");
+  if (depth != 1 && depth != 2) return fail(GCSPH_EINVAL, "staging depth must be 1 or 2");
+  if (cap < 0 || (cap > 0 && cap < 32)) return fail(GCSPH_EINVAL, "tile buffer of %d particles (0, or at least 32)", (int)cap);
+  e->nl_lanes = lanes;
+  e->nl_cpb = cells_per_block;
+  e->nl_depth = depth;
+  e->nl_cap_fix = cap;
+  e->nl_fixed = true;
+  return GCSPH_OK;
+}
+
+int ens_get_list_build(gcsph_ens* e, int32_t* lanes, int32_t* cells_per_block, int32_t* depth, int32_t* cap) {
+  if (!e) return fail(GCSPH_EINVAL, "null handle");
+  if (lanes) *lanes = e->nl_lanes;
+  if (cells_per_block) *cells_per_block = e->nl_cpb;
+  if (depth) *depth = e->nl_depth;
+  if (cap) *cap = e->nl_cpb > 0 ? tile_cap(e, e->nl_cpb, e->nl_depth) : 0;
   return GCSPH_OK;
 }
 

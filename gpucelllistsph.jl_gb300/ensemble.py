@@ -151,9 +151,22 @@ class Ensemble:
 
     def tuning(self):
         t, L, a, b = C.c_int32(), C.c_int32(), C.c_int64(), C.c_int64()
-        _lib.check(_lib.load().ens_get_tuning(self._h, C.byref(t), C.byref(L), C.byref(a), C.byref(b)))
-        return {"tpb": int(t.value), "list_lanes": int(L.value), "captures": int(a.value),
+        lib = _lib.load()
+        _lib.check(lib.ens_get_tuning(self._h, C.byref(t), C.byref(L), C.byref(a), C.byref(b)))
+        c, d, k = C.c_int32(), C.c_int32(), C.c_int32()
+        _lib.check(lib.ens_get_list_build(self._h, None, C.byref(c), C.byref(d), C.byref(k)))
+        return {"tpb": int(t.value), "list_lanes": int(L.value), "cells_per_block": int(c.value),
+                "staging_depth": int(d.value), "tile_capacity": int(k.value), "captures": int(a.value),
                 "replays": int(b.value)}
+
+    def set_list_build(self, lanes: int = 0, cells_per_block: int = 0, depth: int = 1, capacity: int = 0):
+        """Fix the neighbour-list build (lanes = 0: autotuned).  cells_per_block
+        0 = a thread group per particle; 2/4/8/16 = a block per tile of that
+        many cells, the neighbourhood staged in shared memory, `depth` tiles at
+        a time; `capacity` = particles a tile buffer holds (0: from (H/dx)^D).
+        Results do not depend on the choice."""
+        _lib.check(_lib.load().ens_set_list_build(self._h, int(lanes), int(cells_per_block), int(depth),
+                                                  int(capacity)))
 
     def set_list_stride(self, nls: int):
         _lib.check(_lib.load().ens_set_list_stride(self._h, int(nls)))

@@ -312,10 +312,22 @@ int ens_get(gcsph_ens* e, int32_t slot, int32_t field, double* out_host);
 int ens_info(gcsph_ens* e, int32_t slot, int64_t* n, int64_t* steps, double* etime);
 int ens_totals(gcsph_ens* e, int32_t* ninst, int64_t* nparticles, int64_t* ncells);
 /* tpb 0 = autotune: the pair passes' block size (128/256/512), then the
- * lanes per particle of the neighbour-list build (1/2/4/8) -- the results do
- * not depend on either.  graphs 0 = one launch sequence per step. */
+ * lanes per particle of the neighbour-list build (1/2/4/8), then its tiling
+ * (ens_set_list_build) -- the results do not depend on any of them.  graphs
+ * 0 = one launch sequence per step. */
 int ens_set_tuning(gcsph_ens* e, int32_t tpb, int32_t graphs);
 int ens_get_tuning(gcsph_ens* e, int32_t* tpb, int32_t* nl_lanes, int64_t* captures, int64_t* replays);
+/* The neighbour-list build (no counterpart in the reference, which has no
+ * ensembles; its pair search is src/gpukernels_cls.jl:293-587).  lanes 0 =
+ * autotuned.  Otherwise lanes (1/2/4/8) per particle; cells_per_block 0 = one
+ * thread group per particle, 2/4/8/16 = a block per tile of that many cells
+ * of one x-row, with the tile's neighbourhood staged in shared memory, depth
+ * 1 or 2 tiles at a time (2: the next tile is copied while this one is
+ * tested); cap = particles a tile buffer holds (0: sized from (H/dx)^D; a tile
+ * that does not fit reads global memory).  The list, and every result, is the
+ * same for every choice. */
+int ens_set_list_build(gcsph_ens* e, int32_t lanes, int32_t cells_per_block, int32_t depth, int32_t cap);
+int ens_get_list_build(gcsph_ens* e, int32_t* lanes, int32_t* cells_per_block, int32_t* depth, int32_t* cap);
 /* Entries per particle in the step's neighbour list (default 64 in 2-D, 256
  * in 3-D; it grows by itself when a row outgrows it, repeating the steps
  * that had not completed). */

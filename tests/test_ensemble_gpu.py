@@ -187,17 +187,20 @@ def test_launch_shape_and_capture_do_not_change_results(gpu_pkg, tpb, graphs):
         assert t["tpb"] in (128, 256, 512) and t["list_lanes"] in (1, 2, 4, 8)
 
 
-@pytest.mark.parametrize("graphs", [True, False])
-def test_neighbour_list_overflow_grows_and_repeats(gpu_pkg, graphs):
+@pytest.mark.parametrize("graphs,build", [(True, None), (False, None), (True, (2, 8, 2, 0)), (False, (1, 4, 1, 0))])
+def test_neighbour_list_overflow_grows_and_repeats(gpu_pkg, graphs, build):
     """A list stride far too small: the call stops at the first step whose
     rows do not fit, the stride grows and the remaining steps run -- the
-    result is bit-identical to a run that never overflowed."""
+    result is bit-identical to a run that never overflowed, with either list
+    build."""
     a, b, _, _ = _specs(gpu_pkg)
     ref = gpu_pkg.Ensemble(2)
     r1, r2 = ref.add(a), ref.add(b)
     ref.step(9)
     ens = gpu_pkg.Ensemble(2)
     ens.set_tuning(256, graphs)
+    if build:
+        ens.set_list_build(*build)
     e1, e2 = ens.add(a), ens.add(b)
     ens.set_list_stride(4)
     ens.step(9)
@@ -206,3 +209,63 @@ def test_neighbour_list_overflow_grows_and_repeats(gpu_pkg, graphs):
     for f in FIELDS:
         assert np.array_equal(ref.get(r1, f), ens.get(e1, f)), f
         assert np.array_equal(ref.get(r2, f), ens.get(e2, f)), f
+
+
+def _specs3(pkg):
+    w = pkg.workloads
+    a = pkg.spec_from_case(w.dam_break_3d(dx=0.05, fluid=(0.3, 0.4, 0.2), tank=(0.6, 0.6, 0.3), full_physics=False))
+    b = pkg.spec_from_case(w.dam_break_3d(dx=0.06, fluid=(0.4, 0.3, 0.3), tank=(0.9, 0.5, 0.4), full_physics=False),
+                           alpha=0.03)
+    return a, b
+
+
+@pytest.mark.parametrize("D", [2, 3])
+@pytest.mark.parametrize("lanes,cpb,depth,cap", [(1, 4, 1, 0), (2, 8, 2, 0), (4, 16, 1, 0), (8, 2, 2, 0),
+                                                  (2, 4, 1, 32), (1, 8, 2, 64)])
+def test_list_build_variants_give_the_same_results(gpu_pkg, D, lanes, cpb, depth, cap):
+    """Every neighbour-list build -- a thread group per particle, or tiles of
+    cells with their neighbourhood staged in shared memory, one or two tiles
+    at a time, and tiles too big for a small buffer (read from global memory)
+    -- gives the same list in the same order, so the same results bit for bit,
+    over several instances with different grids."""
+    specs = _specs(gpu_pkg)[:3] if D == 2 else _specs3(gpu_pkg)
+    ref = gpu_pkg.Ensemble(D)
+    ref.set_tuning(256, False)
+    ref.set_list_build(4, 0, 1, 0)
+    rs = [ref.add(s) for s in specs]
+    ref.step(12)
+    ens = gpu_pkg.Ensemble(D)
+    ens.set_tuning(256, True)
+    ens.set_list_build(lanes, cpb, depth, cap)
+    es = [ens.add(s) for s in specs]
+    ens.step(5)
+    ens.step(7)
+    for r, e in zip(rs, es):
+        for f in FIELDS:
+            assert np.array_equal(ref.get(r, f), ens.get(e, f)), (f, r)
+    t = ens.tuning()
+    assert (t["list_lanes"], t["cells_per_block"], t["staging_depth"]) == (lanes, cpb, depth)
+    if cap:
+        assert t["tile_capacity"] == cap
+    else:
+        assert t["tile_capacity"] >= 32
+
+
+def test_autotuner_tries_the_tiled_list_build(gpu_pkg):
+    """With enough steps in a call, the tuner runs all three phases (block
+    size, list lanes, list tiling) and the results match a run that was
+    never tuned."""
+    a, b, c, _ = _specs(gpu_pkg)
+    ens = gpu_pkg.Ensemble(2)
+    es = [ens.add(s) for s in (a, b, c)]
+    ens.step(30)
+    t = ens.tuning()
+    assert t["tpb"] in (128, 256, 512) and t["list_lanes"] in (1, 2, 4, 8)
+    assert t["cells_per_block"] in (0, 4, 8, 16) and t["staging_depth"] in (1, 2)
+    ref = gpu_pkg.Ensemble(2)
+    ref.set_tuning(256, False)
+    rs = [ref.add(s) for s in (a, b, c)]
+    ref.step(30)
+    for r, e in zip(rs, es):
+        for f in FIELDS:
+            assert np.array_equal(ref.get(r, f), ens.get(e, f)), f
