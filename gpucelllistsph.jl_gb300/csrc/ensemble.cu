@@ -50,6 +50,9 @@ struct EnsInst {
   float pc[4];                           // (1+ε)^(1/γ) - 1 series coefficients
   float dpc_l0inv, dpc_nW, dpc_whinv, dpc_kernlim, dpc_eta2, dpc_pmin, dpc_pmax, dpc_lambda;
   float xsph_c;                          // 2 m0 ε
+  float rho0inv, m0inv;                  // 1/ρ₀, 1/m₀
+  float dwc;                             // -20 nDW / H: W'(r)/r = dwc (1 - r/H)^3
+  float pfcr;                            // 1.5π / 2h: the cosine's argument per unit r in ∂v∂tpF!
 };
 
 struct EnsArr {
@@ -173,7 +176,7 @@ __device__ __forceinline__ float dot32(const float* a, const float* b) {
 // P0 ((1+e)^γ - 1), e = δρ/ρ₀, without cancellation (pressure(), src/gpukernels_sph.jl:691-697)
 __device__ __forceinline__ float eos32(float dr, int pt, const EnsInst& I) {
   if (pt <= 1 && dr < 0.f) return 0.f;
-  const float e = dr / I.rho0;
+  const float e = dr * I.rho0inv;
   float p;
   if (I.gamma == 7)
     p = e * (7.f + e * (21.f + e * (35.f + e * (35.f + e * (21.f + e * (7.f + e))))));
@@ -629,6 +632,7 @@ __global__ void __launch_bounds__(ENS_MAX_TPB) k_ens_stage(EnsArr A, const EnsIn
     const int pti = A.pt[i];
     const float dri = STAGE == 1 ? A.dr[i] : A.drh[i];
     const float rhoi = I.rho0 + dri;
+    const float irhoi = __fdividef(1.f, rhoi);
     const float Pi = eos32(dri, pti, I);
     const int fbs = STAGE - 1;
     KSum drho, acc[D];
@@ -646,11 +650,13 @@ __global__ void __launch_bounds__(ENS_MAX_TPB) k_ens_stage(EnsArr A, const EnsIn
 #pragma unroll
       for (int q = 0; q < D; ++q) d[q] = (oi[q] - oj[q]) - (q == 0 ? shx : (q == 1 ? shy : shz));
       const float r2 = dot32<D>(d, d);
-      // sph∇W!: W'(r)/r of WendlandC2 = -20 nDW Hinv (1-q)^3
-      const float r = sqrtf(r2);
+      // sph∇W!: W'(r)/r of WendlandC2 = -20 nDW Hinv (1-q)^3.  Reciprocals and
+      // roots here are the approximate intrinsics (within 2 ulp each), far
+      // inside the FP32 path's error against FP64.
+      const float r = r2 > 0.f ? r2 * rsqrtf(r2) : 0.f;
       const float u = r * I.Hinv;
       const float t = u < 1.f ? 1.f - u : 0.f;
-      const float dwr = -20.f * I.nDW * I.Hinv * (t * t * t);
+      const float dwr = I.dwc * (t * t * t);
       float gw[D], dd[D], dv[D];
 #pragma unroll
       for (int q = 0; q < D; ++q) {
@@ -660,8 +666,9 @@ __global__ void __launch_bounds__(ENS_MAX_TPB) k_ens_stage(EnsArr A, const EnsIn
       }
       const float r2d = STAGE == 1 ? r2 : dot32<D>(dd, dd);
       const float rhoj = I.rho0 + drj;
+      const float irhoj = __fdividef(1.f, rhoj);
       const bool both = pti > 0 && ptj > 0;
-      const float inv = 1.f / (r2d + I.eta2);
+      const float inv = __fdividef(1.f, r2d + I.eta2);
       float f[D];
 #pragma unroll
       for (int q = 0; q < D; ++q) f[q] = 0.f;
@@ -670,46 +677,49 @@ __global__ void __launch_bounds__(ENS_MAX_TPB) k_ens_stage(EnsArr A, const EnsIn
         float term = I.m0 * dot32<D>(dv, gw);
         if (pti > 1) {
           const float dp = I.rho0 * root_m1(I.DDTgz * dd[1], I);
-          term += I.DDTkh * ((drj - dri) - dp) * inv * (-dot32<D>(dd, gw)) * I.m0 / rhoj;
+          term += I.DDTkh * ((drj - dri) - dp) * inv * (-dot32<D>(dd, gw)) * I.m0 * irhoj;
         }
         drho.add(term);
       }
       if (pti * ptj > 0) {
         // ∂v∂t!
-        const float sc = -I.m0 * (Pi + eos32(drj, ptj, I)) / (rhoi * rhoj);
+        const float sc = -I.m0 * (Pi + eos32(drj, ptj, I)) * (irhoi * irhoj);
 #pragma unroll
         for (int q = 0; q < D; ++q) f[q] = sc * gw[q];
       }
       if (both) {
         const float cond = dot32<D>(dv, dd);
-        if (cond < 0.f) {
-          // ∂v∂t_av!
-          const float dmu = I.h * cond * inv;
-          const float dPi = (-I.alpha * I.c0 * dmu) / ((rhoi + rhoj) * 0.5f);
+        if (cond < 0.f || I.use_visc) {
+          const float isum = __fdividef(1.f, rhoi + rhoj);
+          if (cond < 0.f) {
+            // ∂v∂t_av!
+            const float dmu = I.h * cond * inv;
+            const float dPi = (-I.alpha * I.c0 * dmu) * (2.f * isum);
 #pragma unroll
-          for (int q = 0; q < D; ++q) f[q] += -dPi * I.m0 * gw[q];
-        }
-        if (I.use_visc) {
-          // ∂v∂t_visc!
-          const float nt = 4.f * I.nu * I.m0 * dot32<D>(dd, gw) / (rhoi + rhoj) * inv;
+            for (int q = 0; q < D; ++q) f[q] += -dPi * I.m0 * gw[q];
+          }
+          if (I.use_visc) {
+            // ∂v∂t_visc!
+            const float nt = 4.f * I.nu * I.m0 * dot32<D>(dd, gw) * isum * inv;
 #pragma unroll
-          for (int q = 0; q < D; ++q) f[q] += nt * dv[q];
+            for (int q = 0; q < D; ++q) f[q] += nt * dv[q];
+          }
         }
         if (I.use_pF) {
           // ∂v∂tpF!
-          const float rd = sqrtf(r2d);
+          const float rd = r2d > 0.f ? r2d * rsqrtf(r2d) : 0.f;
           if (rd < I.twoh) {
-            const float scos = I.s * __cosf(I.pfc * rd / I.twoh) / (rd + I.hp1);  // argument in [0, 1.5π)
+            const float scos = I.s * __cosf(I.pfcr * rd) * __fdividef(1.f, rd + I.hp1);  // argument in [0, 1.5π)
 #pragma unroll
-            for (int q = 0; q < D; ++q) f[q] += scos * dd[q] / I.m0;
+            for (int q = 0; q < D; ++q) f[q] += scos * dd[q] * I.m0inv;
           }
         }
       }
       if ((pti > 0) != (ptj > 0) && r < I.fb_r0[fbs]) {
         // fbmolforce! at x
-        const float qq = I.fb_r0[fbs] / (r + I.fb_eta2[fbs]);
+        const float qq = I.fb_r0[fbs] * __fdividef(1.f, r + I.fb_eta2[fbs]);
         const float q2 = qq * qq, q4 = q2 * q2, q8 = q4 * q4;
-        const float Fc = I.fb_d[fbs] * (q8 * q4 - q4) / (r2 + I.fb_eta2[fbs]);
+        const float Fc = I.fb_d[fbs] * (q8 * q4 - q4) * __fdividef(1.f, r2 + I.fb_eta2[fbs]);
 #pragma unroll
         for (int q = 0; q < D; ++q) f[q] += d[q] * Fc;
       }
@@ -1789,6 +1799,10 @@ int ens_add(gcsph_ens* e, int64_t n, const double* x, const double* v, const dou
   I.pc[1] = (float)c2;
   I.pc[2] = (float)c3;
   I.pc[3] = (float)c4;
+  I.rho0inv = (float)(1.0 / p->rho0);
+  I.m0inv = (float)(1.0 / p->m0);
+  I.dwc = (float)(-20.0 * (D == 2 ? wc2_norm_dw<2>(1.0 / p->H) : wc2_norm_dw<3>(1.0 / p->H)) / p->H);
+  I.pfcr = (float)(1.5 * GCSPH_PI64 / (2.0 * p->h));
   // host staging in the engine's types
   std::vector<float> vf((size_t)D * n, 0.f), drf((size_t)n);
   std::vector<int32_t> ids((size_t)n);
