@@ -165,6 +165,9 @@ struct KSum {
   }
 };
 
+// √x for x >= 0 by the approximate reciprocal root (within a few ulp); 0 at 0
+__device__ __forceinline__ float sqrt_fast(float x) { return x > 0.f ? x * rsqrtf(x) : 0.f; }
+
 template <int D>
 __device__ __forceinline__ float dot32(const float* a, const float* b) {
   float r = a[0] * b[0];
@@ -812,18 +815,18 @@ __global__ void __launch_bounds__(ENS_MAX_TPB) k_ens_dpc(EnsArr A, const EnsInst
         const float drj = A.dr[j];
         const float rhoj = I.rho0 + drj;
         const float r2 = dot32<D>(dx, dx);
-        const float u = sqrtf(r2) * I.dpc_l0inv;
+        const float u = sqrt_fast(r2) * I.dpc_l0inv;
         const float t = u < 1.f ? 1.f - u : 0.f;
         const float t2 = t * t;
         const float w = (1.f + 4.f * u) * (t2 * t2) * I.dpc_nW;
-        const float chi = sqrtf(w * I.dpc_whinv);
+        const float chi = sqrt_fast(w * I.dpc_whinv);
         const float kk = u < I.dpc_kernlim ? 1.f : chi;
         const float Pb = chi * fmaxf(fminf(I.dpc_lambda * fabsf(Pi + eos32(drj, ptj, I)),
                                            I.dpc_lambda * I.dpc_pmax), I.dpc_pmin);
         const float vr = dot32<D>(dv, dx);
         float c;
-        if (vr < 0.f) c = kk * (-vr / (r2 + I.dpc_eta2));
-        else c = 2.f * dt * Pb / ((rhoi + rhoj) * (r2 + I.dpc_eta2));
+        if (vr < 0.f) c = kk * (-vr * __fdividef(1.f, r2 + I.dpc_eta2));
+        else c = 2.f * dt * Pb * __fdividef(1.f, (rhoi + rhoj) * (r2 + I.dpc_eta2));
 #pragma unroll
         for (int q = 0; q < D; ++q) sum[q].add(c * dx[q]);
       }
@@ -880,11 +883,11 @@ __global__ void __launch_bounds__(ENS_MAX_TPB) k_ens_xsph(EnsArr A, const EnsIns
       float d[D];
 #pragma unroll
       for (int q = 0; q < D; ++q) d[q] = (oi[q] - A.off[q][j]) - (q == 0 ? shx : (q == 1 ? shy : shz));
-      const float u = sqrtf(dot32<D>(d, d)) * I.Hinv;
+      const float u = sqrt_fast(dot32<D>(d, d)) * I.Hinv;
       const float t = u < 1.f ? 1.f - u : 0.f;
       const float t2 = t * t;
       const float w = (1.f + 4.f * u) * (t2 * t2) * I.nW;
-      const float xs = I.xsph_c * w / (rhoi + (I.rho0 + A.dr[j]));
+      const float xs = I.xsph_c * w * __fdividef(1.f, rhoi + (I.rho0 + A.dr[j]));
 #pragma unroll
       for (int q = 0; q < D; ++q) sum[q].add((A.v[q][j] - vi[q]) * xs);
     }
@@ -936,12 +939,12 @@ __global__ void __launch_bounds__(ENS_MAX_TPB) k_ens_cspm(EnsArr A, const EnsIns
       float d[D];
 #pragma unroll
       for (int q = 0; q < D; ++q) d[q] = (oi[q] - A.off[q][j]) - (q == 0 ? shx : (q == 1 ? shy : shz));
-      const float u = sqrtf(dot32<D>(d, d)) * I.Hinv;
+      const float u = sqrt_fast(dot32<D>(d, d)) * I.Hinv;
       const float t = u < 1.f ? 1.f - u : 0.f;
       const float t2 = t * t;
       const float w = (1.f + 4.f * u) * (t2 * t2) * I.nW;
       const float drj = A.dr[j];
-      const float mw = I.m0 * w / (I.rho0 + drj);
+      const float mw = I.m0 * w * __fdividef(1.f, I.rho0 + drj);
       s2.add(mw);
       s3.add(mw * drj);
     }
