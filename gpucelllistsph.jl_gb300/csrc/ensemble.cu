@@ -72,7 +72,8 @@ struct EnsArr {
   float* offn[3];            // x - cell corner after the corrector (dpcreg!)
   float* dxb[3];             // xΔt½ base - x: dpcreg!/xsphcorr! move x, not xΔt½
   float* dvb[3];             // vΔt½ base - v: dpcreg! moves v, not vΔt½
-  int* nl;                   // neighbour list of the step, entry-major (q * ncap + i)
+  int* nl;                   // neighbour list of the step, entry-major (q * ncap + i); written with
+                             // streaming stores (evict-first in L2)
   int* nlc;                  // entries per particle
   int64_t ncap;              // particle capacity (the list's row pitch)
   int nls;                   // entries per particle the list holds
@@ -319,13 +320,13 @@ __device__ __forceinline__ void nl_emit(const EnsArr& A, int64_t i, int lane, un
                                         int j, int code, int& cnt) {
   if (L == 1) {
     if (hit) {
-      if (cnt < A.nls) A.nl[(int64_t)cnt * A.ncap + i] = (j << 5) | code;
+      if (cnt < A.nls) __stcs(A.nl + (int64_t)cnt * A.ncap + i, (j << 5) | code);
       ++cnt;
     }
   } else {
     const unsigned bal = (__ballot_sync(gm, hit) >> gbase) & (L == 32 ? 0xffffffffu : ((1u << L) - 1u));
     const int at = cnt + __popc(bal & ((1u << lane) - 1u));
-    if (hit && at < A.nls) A.nl[(int64_t)at * A.ncap + i] = (j << 5) | code;
+    if (hit && at < A.nls) __stcs(A.nl + (int64_t)at * A.ncap + i, (j << 5) | code);
     cnt += __popc(bal);
   }
 }
