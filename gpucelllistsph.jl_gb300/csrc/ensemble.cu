@@ -641,8 +641,12 @@ __global__ void __launch_bounds__(ENS_MAX_TPB) k_ens_stage(EnsArr A, const EnsIn
     const int fbs = STAGE - 1;
     KSum drho, acc[D];
     const int nn = A.nlc[i];
+    // the next entry is loaded one iteration ahead: the list streams from
+    // DRAM, and its latency then overlaps the current neighbour's arithmetic
+    int nxt = lane < nn ? A.nl[(int64_t)lane * A.ncap + i] : 0;
     for (int e = lane; e < nn; e += L) {
-      const int ent = A.nl[(int64_t)e * A.ncap + i];
+      const int ent = nxt;
+      if (e + L < nn) nxt = A.nl[(int64_t)(e + L) * A.ncap + i];
       const Rec<D, STAGE> rec = load_rec<D, STAGE>(A.r1, A.r2, ent >> 5);
       float shx, shy, shz;
       shift_of(ent, I, shx, shy, shz);
@@ -800,8 +804,10 @@ __global__ void __launch_bounds__(ENS_MAX_TPB) k_ens_dpc(EnsArr A, const EnsInst
       const float rhoi = I.rho0 + dri, Pi = eos32(dri, pti, I);
       const float dt = (float)I.dt;
       const int nn = A.nlc[i];
+      int nxt = nn > 0 ? A.nl[i] : 0;  // entries one iteration ahead (as in the stage passes)
       for (int e = 0; e < nn; ++e) {
-        const int ent = A.nl[(int64_t)e * A.ncap + i];
+        const int ent = nxt;
+        if (e + 1 < nn) nxt = A.nl[(int64_t)(e + 1) * A.ncap + i];
         const int j = ent >> 5;
         const int ptj = A.pt[j];
         if (!(ptj > 0)) continue;
@@ -875,8 +881,10 @@ __global__ void __launch_bounds__(ENS_MAX_TPB) k_ens_xsph(EnsArr A, const EnsIns
     const float rhoi = I.rho0 + A.dr[i];
     KSum sum[D];
     const int nn = A.nlc[i];
+    int nxt = nn > 0 ? A.nl[i] : 0;  // entries one iteration ahead (as in the stage passes)
     for (int e = 0; e < nn; ++e) {
-      const int ent = A.nl[(int64_t)e * A.ncap + i];
+      const int ent = nxt;
+      if (e + 1 < nn) nxt = A.nl[(int64_t)(e + 1) * A.ncap + i];
       const int j = ent >> 5;
       if (!(A.pt[j] > 1)) continue;
       float shx, shy, shz;
@@ -931,8 +939,10 @@ __global__ void __launch_bounds__(ENS_MAX_TPB) k_ens_cspm(EnsArr A, const EnsIns
     for (int d = 0; d < D; ++d) oi[d] = A.off[d][i];
     KSum s2, s3;
     const int nn = A.nlc[i];
+    int nxt = nn > 0 ? A.nl[i] : 0;  // entries one iteration ahead (as in the stage passes)
     for (int e = 0; e < nn; ++e) {
-      const int ent = A.nl[(int64_t)e * A.ncap + i];
+      const int ent = nxt;
+      if (e + 1 < nn) nxt = A.nl[(int64_t)(e + 1) * A.ncap + i];
       const int j = ent >> 5;
       if (!(A.pt[j] > 0)) continue;
       float shx, shy, shz;
