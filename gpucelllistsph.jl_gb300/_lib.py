@@ -90,6 +90,9 @@ _SIGS = {
     "ens_set_tuning": (C.c_int, [vp, i32, i32]),
     "ens_get_tuning": (C.c_int, [vp, C.POINTER(i32), C.POINTER(i32), C.POINTER(i64), C.POINTER(i64)]),
     "ens_set_list_build": (C.c_int, [vp, i32, i32, i32, i32]),
+    "ens_set_skin": (C.c_int, [vp, C.c_double]),
+    "ens_get_skin": (C.c_int, [vp, C.POINTER(C.c_double)]),
+    "ens_list_builds": (C.c_int, [vp, i32, C.POINTER(i64)]),
     "ens_get_list_build": (C.c_int, [vp, C.POINTER(i32), C.POINTER(i32), C.POINTER(i32), C.POINTER(i32)]),
     "ens_set_list_stride": (C.c_int, [vp, i32]),
     "ens_get_list_stride": (C.c_int, [vp, C.POINTER(i32)]),

@@ -95,12 +95,14 @@ def _params(spec: InstanceSpec) -> _lib.gcsph_ens_params:
 
 
 class Ensemble:
-    def __init__(self, D: int, stream: int = 0):
+    def __init__(self, D: int, stream: int = 0, skin: float | None = None):
         self.D = int(D)
         h = C.c_void_p()
         _lib.check(_lib.load().ens_create(self.D, C.c_void_p(stream), C.byref(h)))
         self._h = h
         self.specs = {}
+        if skin is not None:
+            self.set_skin(skin)
 
     @staticmethod
     def bytes_per_particle(D: int) -> int:
@@ -167,6 +169,23 @@ class Ensemble:
         Results do not depend on the choice."""
         _lib.check(_lib.load().ens_set_list_build(self._h, int(lanes), int(cells_per_block), int(depth),
                                                   int(capacity)))
+
+    def set_skin(self, skin: float):
+        """List skin: cells and neighbour lists of radius H (1 + skin), rebuilt
+        per instance once a particle has moved about skin H / 2 (0: every
+        step).  Set before the first add."""
+        _lib.check(_lib.load().ens_set_skin(self._h, float(skin)))
+
+    def skin(self) -> float:
+        v = C.c_double()
+        _lib.check(_lib.load().ens_get_skin(self._h, C.byref(v)))
+        return float(v.value)
+
+    def list_builds(self, slot: int) -> int:
+        """How many times the instance's cells and list were built."""
+        v = C.c_int64()
+        _lib.check(_lib.load().ens_list_builds(self._h, int(slot), C.byref(v)))
+        return int(v.value)
 
     def set_list_stride(self, nls: int):
         _lib.check(_lib.load().ens_set_list_stride(self._h, int(nls)))

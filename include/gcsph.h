@@ -327,6 +327,17 @@ int ens_get_tuning(gcsph_ens* e, int32_t* tpb, int32_t* nl_lanes, int64_t* captu
  * that does not fit reads global memory).  The list, and every result, is the
  * same for every choice. */
 int ens_set_list_build(gcsph_ens* e, int32_t lanes, int32_t cells_per_block, int32_t depth, int32_t cap);
+/* The list's skin (no counterpart in the reference, whose update! rebuilds
+ * when max |cΔx| > 0.9 (dist - H), src/sphproblem.jl:222-232): cells and list
+ * radius of H (1 + skin); an instance rebuilds its cells and list when one of
+ * its particles has moved about skin H / 2 since the last build, and every
+ * pass keeps only the pairs with r < H at the step's positions.  Default 0.05
+ * in 2-D, 0.025 in 3-D; 0 rebuilds at every step.  Set before the first
+ * ens_add. */
+int ens_set_skin(gcsph_ens* e, double skin);
+int ens_get_skin(gcsph_ens* e, double* skin);
+/* list builds of one instance so far */
+int ens_list_builds(gcsph_ens* e, int32_t slot, int64_t* builds);
 int ens_get_list_build(gcsph_ens* e, int32_t* lanes, int32_t* cells_per_block, int32_t* depth, int32_t* cap);
 /* Entries per particle in the step's neighbour list (default 64 in 2-D, 256
  * in 3-D; it grows by itself when a row outgrows it, repeating the steps

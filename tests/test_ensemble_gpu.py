@@ -269,3 +269,69 @@ def test_autotuner_tries_the_tiled_list_build(gpu_pkg):
     for r, e in zip(rs, es):
         for f in FIELDS:
             assert np.array_equal(ref.get(r, f), ens.get(e, f)), f
+
+
+def _fast_spec(pkg, case, amp, seed=11):
+    spec = pkg.spec_from_case(case)
+    spec.v = _moving(case, seed=seed, amp=amp)
+    return spec
+
+
+@pytest.mark.parametrize("skin", [0.0, 0.02, 0.1])
+def test_list_skin_against_fp64(gpu_pkg, orc, skin):
+    """Fluid moving at up to 5 m/s, so that with a thin skin the lists are
+    rebuilt several times in 100 steps: with any skin, the pairs of a step are
+    those within H at the step's positions, and the result holds the FP32
+    contract against the FP64 oracle.  Without a skin every step builds."""
+    case = gpu_pkg.workloads.dam_break_2d(dx=0.04, fluid=(0.6, 0.8), tank=(1.2, 1.0), layer_ptype=(1, 0, 0))
+    spec = _fast_spec(gpu_pkg, case, 5.0)
+    ens = gpu_pkg.Ensemble(2, skin=skin)
+    assert ens.skin() == skin
+    slot = ens.add(spec)
+    ens.step(40)
+    ens.step(60)
+    builds = ens.list_builds(slot)
+    if skin == 0.0:
+        assert builds == 100
+    elif skin == 0.02:
+        assert 2 < builds < 60, builds
+    else:
+        assert 1 <= builds < 20, builds
+    ref = _oracle_full(orc, case, 100, spec.v)
+    err = errors(ens, slot, ref, case)
+    print(f"skin {skin}: {builds} list builds in 100 steps, fp32 vs fp64:", err)
+    assert err["rho"] <= TOL and err["v"] <= TOL and err["disp"] <= TOL, err
+
+
+def test_lists_survive_the_removal_of_an_earlier_instance(gpu_pkg):
+    """An instance that keeps its list across a removal in front of it (its
+    particles, cell keys and list rows move down) and an admission behind it:
+    bit-identical to the same instance alone, same number of list builds."""
+    w = gpu_pkg.workloads
+    case = w.dam_break_2d(dx=0.04, fluid=(0.6, 0.8), tank=(1.2, 1.0), layer_ptype=(1, 0, 0))
+    a = _fast_spec(gpu_pkg, case, 5.0)
+    _, b, c, _ = _specs(gpu_pkg)
+    alone = gpu_pkg.Ensemble(2, skin=0.02)
+    sa = alone.add(a)
+    alone.step(27)
+    alone.step(23)
+    mix = gpu_pkg.Ensemble(2, skin=0.02)
+    sb = mix.add(b)
+    sm = mix.add(a)
+    mix.step(27)
+    mix.remove(sb)
+    mix.add(c)
+    mix.step(23)
+    assert mix.list_builds(sm) == alone.list_builds(sa) >= 2
+    for f in FIELDS:
+        assert np.array_equal(alone.get(sa, f), mix.get(sm, f)), f
+
+
+def test_skin_is_set_before_instances(gpu_pkg):
+    a, _, _, _ = _specs(gpu_pkg)
+    ens = gpu_pkg.Ensemble(2)
+    assert ens.skin() == pytest.approx(0.05)
+    assert gpu_pkg.Ensemble(3).skin() == pytest.approx(0.025)
+    ens.add(a)
+    with pytest.raises(RuntimeError):
+        ens.set_skin(0.2)
