@@ -258,8 +258,7 @@ def run_batched(g, args, plain_c1):
     wl = g.workloads.ensemble_2d(args.batched_instances)
     ens = g.Ensemble(2)
     t0 = time.perf_counter()
-    for case, al, de in wl:
-        ens.add(g.spec_from_case(case, alpha=al, delta=de))
+    slots = [ens.add(g.spec_from_case(case, alpha=al, delta=de)) for case, al, de in wl]
     t_admit = time.perf_counter() - t0
     tot = ens.totals()
     ens.step(30)  # tuning (block size, list lanes, list tiling: 24 steps) + warm-up
@@ -267,12 +266,14 @@ def run_batched(g, args, plain_c1):
     torch.cuda.synchronize()
     L = g.load_library()
     L.gcsph_timing_enable(0)
+    builds0 = sum(ens.list_builds(s) for s in slots)
     a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     a.record()
     ens.step(args.batched_steps)
     b.record()
     torch.cuda.synchronize()
     ms = a.elapsed_time(b)
+    builds = sum(ens.list_builds(s) for s in slots) - builds0
     value = tot["particles"] * args.batched_steps / (ms / 1e3)
     # instrumented pass for the per-kernel split
     L.gcsph_timing_enable(1)
@@ -287,6 +288,7 @@ def run_batched(g, args, plain_c1):
             fam[L.gcsph_timing_name(tid).decode()] = {"launches": int(n_.value), "total_ms": float(t_.value)}
     L.gcsph_timing_enable(0)
     tuning = ens.tuning()
+    skin = ens.skin()
     ens.close()
     sizes = sorted(wl, key=lambda t: t[0].N)
     sample = [sizes[0][0], sizes[len(sizes) // 2][0], sizes[-1][0]]
@@ -299,6 +301,7 @@ def run_batched(g, args, plain_c1):
             "instances": tot["instances"], "particles": tot["particles"], "cells": tot["cells"],
             "value": value, "unit": "particle-steps/s", "timed_steps": args.batched_steps,
             "ms_per_step": ms / args.batched_steps, "admission_s": t_admit, "tuning": tuning,
+            "list_skin": skin, "list_builds_in_timed_steps": builds,
             "kernel_ms_20_steps": fam,
             "plain_fp64_same_instances": {"value": plain, "unit": "particle-steps/s",
                                           "sample": "smallest, median and largest instance, each alone, 30 steps"},
