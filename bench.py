@@ -110,6 +110,13 @@ class Clocks:
                  "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
                  "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
                  "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+            # nvidia-smi's start-up (NVML initialisation) stalls CUDA calls of
+            # this process for up to ~100 ms: the timed region starts only
+            # once the sampler has written its first sample
+            for _ in range(300):
+                if os.path.getsize(self.path) > 0:
+                    break
+                time.sleep(0.01)
         except Exception:
             self.proc = None
         return self
