@@ -539,10 +539,23 @@ __global__ void __launch_bounds__(TPB) k_pairs32(const double* __restrict__ x0, 
 }
 
 // lanes per particle in the pair search: about 8 candidates per lane
+// Lanes per point of the pair passes, from the candidates a point tests.
+// After a first build the mean neighbour count m = nfull / N gives them as
+// m times the stencil's volume over the dist-ball's (9/π in 2-D, 81/(4π) in
+// 3-D, times (cellsize/dist)^D); this weights cells by the points in them,
+// where the grid-wide mean N / ncell (the first build's estimate) counts the
+// empty cells of a tank as well -- 4 lanes rather than 16 for a 2-D dam break.
 int CellCore::pair_lanes() const {
   if (lanes > 0) return lanes;
-  double per_cell = (double)N / (double)g.ncell;
-  double cand = per_cell * (D == 3 ? 27.0 : 9.0);
+  double cand;
+  if (nfull_est > 0 && N > 0) {
+    double vol = D == 3 ? 81.0 / (4.0 * GCSPH_PI64) : 9.0 / GCSPH_PI64;
+    for (int d = 0; d < D; ++d) vol *= cs[d] / dist;
+    cand = (double)nfull_est / (double)N * vol;
+  } else {
+    const double per_cell = (double)N / (double)g.ncell;
+    cand = per_cell * (D == 3 ? 27.0 : 9.0);
+  }
   int L = 1;
   while (L < 32 && (double)L * 8.0 < cand) L <<= 1;
   return L;
