@@ -99,6 +99,29 @@ __global__ void k_rank_in_cell(const int32_t* __restrict__ tmp, const int32_t* _
   perm[s + r] = i;
 }
 
+// the rank and its consequences in one pass: the point's slot in cell
+// order, its key there and its original index (k_rank_in_cell then
+// k_apply_perm, without the second launch)
+__global__ void k_rank_apply(const int32_t* __restrict__ tmp, const int32_t* __restrict__ key,
+                             const int32_t* __restrict__ cellstart, const int32_t* __restrict__ ord, int64_t N,
+                             int32_t* __restrict__ perm, int32_t* __restrict__ skey, int32_t* __restrict__ orig) {
+  int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= N) return;
+  int32_t i = tmp[q];
+  int32_t c = key[i];
+  int32_t s = cellstart[c], e = cellstart[c + 1];
+  int32_t oi = ord ? ord[i] : i;
+  int32_t r = 0;
+  for (int32_t t = s; t < e; ++t) {
+    int32_t j = tmp[t];
+    int32_t oj = ord ? ord[j] : j;
+    r += (oj < oi);
+  }
+  perm[s + r] = i;
+  skey[s + r] = c;
+  orig[s + r] = oi;
+}
+
 __global__ void k_apply_perm(const int32_t* __restrict__ perm, const int32_t* __restrict__ key,
                              const int32_t* __restrict__ ord, int64_t N, int32_t* __restrict__ skey,
                              int32_t* __restrict__ orig) {
@@ -350,15 +373,12 @@ int CellCore::sort(const double* const* xin, const int32_t* ord) {
   k_scatter_arrival<<<nblocks(N, TPB), TPB, 0, st>>>(key.as<int32_t>(), slot.as<int32_t>(), cellstart.as<int32_t>(), N,
                                                       tmp.as<int32_t>());
   GC_LAUNCHED();
-  k_rank_in_cell<<<nblocks(N, TPB), TPB, 0, st>>>(tmp.as<int32_t>(), key.as<int32_t>(), cellstart.as<int32_t>(), ord, N,
-                                                   perm.as<int32_t>());
-  GC_LAUNCHED();
   // ord may be `orig` itself (re-sorting particles already in cell order), so
   // the new map is written to the spare buffer and the two are swapped
   int rc2 = orig_b.ensure(sizeof(int32_t) * N, st);
   if (rc2) return rc2;
-  k_apply_perm<<<nblocks(N, TPB), TPB, 0, st>>>(perm.as<int32_t>(), key.as<int32_t>(), ord, N, skey.as<int32_t>(),
-                                                 orig_b.as<int32_t>());
+  k_rank_apply<<<nblocks(N, TPB), TPB, 0, st>>>(tmp.as<int32_t>(), key.as<int32_t>(), cellstart.as<int32_t>(), ord, N,
+                                                 perm.as<int32_t>(), skey.as<int32_t>(), orig_b.as<int32_t>());
   GC_LAUNCHED();
   std::swap(orig.p, orig_b.p);
   std::swap(orig.bytes, orig_b.bytes);
