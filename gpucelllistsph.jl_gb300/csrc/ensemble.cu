@@ -621,9 +621,10 @@ __global__ void __launch_bounds__(TILE_TPB) k_ens_nlist_tile(EnsArr A, const Ens
 // lanes per particle in the pair passes: fixed per dimension (never tuned),
 // so that the summation order -- and every result -- is the same whatever
 // the launch shape and whatever else is in the ensemble
+// (measured on GB300: 2 in 2-D beats 1 and 4; 4 in 3-D beats 2 and 8)
 template <int D>
 __host__ __device__ constexpr int stage_lanes() {
-  return D == 2 ? 2 : 8;
+  return D == 2 ? 2 : 4;
 }
 
 // Kahan partial sums of the L lanes of a particle, combined by a fixed butterfly
