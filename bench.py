@@ -88,8 +88,8 @@ def algorithmic_bytes_per_stage(case, npairs):
 
 # DRAM bytes (read + write) of one stage-1 pass A launch on this workload, from
 # the ncu capture summarised in profiles/pairA_dambreak2d_c1_fp64.md
-PAIRA_STAGE1_DRAM_BYTES = 2_105_344 + 256
-PAIRA_STAGE1_FP64_PIPE = 0.779
+PAIRA_STAGE1_DRAM_BYTES = 2_100_992 + 512
+PAIRA_STAGE1_FP64_PIPE = 0.777
 
 
 class Clocks:
