@@ -50,6 +50,26 @@ vp = C.c_void_p
 i32, i64, f64 = C.c_int32, C.c_int64, C.c_double
 PP = C.POINTER(C.c_void_p)  # host array of device pointers
 
+# serving scheduler: backend callbacks and statistics (mirrors of gcsph.h)
+SRV_ADD = C.CFUNCTYPE(C.c_int, vp, i32, i32, C.POINTER(i32))
+SRV_REMOVE = C.CFUNCTYPE(C.c_int, vp, i32, i32)
+SRV_STEP = C.CFUNCTYPE(C.c_int, vp, i32, i32)
+SRV_HARVEST = C.CFUNCTYPE(C.c_int, vp, i32, i32, i32)
+SRV_FREE = C.CFUNCTYPE(i64, vp)
+SRV_BPP = C.CFUNCTYPE(i64, vp, i32)
+SRV_NOW = C.CFUNCTYPE(f64, vp)
+
+
+class gcsph_srv_backend(C.Structure):
+    _fields_ = [("ctx", vp), ("add", SRV_ADD), ("remove", SRV_REMOVE), ("step", SRV_STEP), ("harvest", SRV_HARVEST),
+                ("free_bytes", SRV_FREE), ("bytes_per_particle", SRV_BPP), ("now", SRV_NOW)]
+
+
+class gcsph_srv_stats(C.Structure):
+    _fields_ = [("requests", i32), ("completed", i32), ("particle_steps", i64), ("wall_s", f64), ("p50_s", f64),
+                ("p99_s", f64), ("mean_s", f64)]
+
+
 _SIGS = {
     "gcsph_last_error": (C.c_char_p, []),
     "gcsph_version": (C.c_int, []),
@@ -94,6 +114,14 @@ _SIGS = {
     "ens_get_skin": (C.c_int, [vp, C.POINTER(C.c_double)]),
     "ens_list_builds": (C.c_int, [vp, i32, C.POINTER(i64)]),
     "ens_get_list_build": (C.c_int, [vp, C.POINTER(i32), C.POINTER(i32), C.POINTER(i32), C.POINTER(i32)]),
+    "srv_create": (C.c_int, [vp, i32, f64, C.c_uint32, C.POINTER(gcsph_srv_backend), C.POINTER(vp)]),
+    "srv_destroy": (None, [vp]),
+    "srv_submit": (C.c_int, [vp, i32, i64, vp, vp, vp, vp, C.POINTER(gcsph_ens_params), i64, f64, C.POINTER(i32)]),
+    "srv_progress": (C.c_int, [vp, C.POINTER(i32), C.POINTER(i32)]),
+    "srv_run": (C.c_int, [vp]),
+    "srv_request": (C.c_int, [vp, i32, C.POINTER(i32), C.POINTER(f64), C.POINTER(f64), C.POINTER(f64)]),
+    "srv_result": (C.c_int, [vp, i32, i32, vp]),
+    "srv_stats": (C.c_int, [vp, C.POINTER(gcsph_srv_stats)]),
     "ens_set_list_stride": (C.c_int, [vp, i32]),
     "ens_get_list_stride": (C.c_int, [vp, C.POINTER(i32)]),
     "sph_get_field": (C.c_int, [vp, i32, vp]),

@@ -26,6 +26,7 @@ UNITS = {
     "sph_once.cu": [],
     "sph_pairs.cu": ["-fmad=false"],
     "ensemble.cu": [],
+    "serving.cu": [],
 }
 
 

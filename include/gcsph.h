@@ -345,6 +345,57 @@ int ens_get_list_build(gcsph_ens* e, int32_t* lanes, int32_t* cells_per_block, i
 int ens_set_list_stride(gcsph_ens* e, int32_t nls);
 int ens_get_list_stride(gcsph_ens* e, int32_t* nls);
 
+/* ---------------------------------------------------------------------------
+ * Serving: continuous batching of dam-break solves over the ensembles (no
+ * counterpart in the reference, which solves one SPHProblem per call,
+ * src/sphproblem.jl:204-345, :420-511).  Submitted requests are admitted
+ * once they have arrived and the device has room (n x bytes per particle x 2
+ * within 1 - reserve of the free memory), advance together in chunks of at
+ * most `chunk` steps cut at the nearest horizon, and release their slot at
+ * their horizon after the fields in `fields` (bit f = GCSPH_ENS field f) are
+ * read back.  Times are seconds since srv_create.
+ * ------------------------------------------------------------------------ */
+typedef struct gcsph_srv gcsph_srv;
+/* The scheduler's view of the ensembles, the free memory and the clock.  NULL
+ * in srv_create selects the library's own (ens_*, cudaMemGetInfo, a steady
+ * clock); a caller's table drives the same scheduling (e.g. host-side tests
+ * against a fake ensemble).  Callbacks return 0 or an error code. */
+typedef struct gcsph_srv_backend {
+  void* ctx;
+  int (*add)(void* ctx, int32_t D, int32_t rid, int32_t* slot);
+  int (*remove)(void* ctx, int32_t D, int32_t slot);
+  int (*step)(void* ctx, int32_t D, int32_t n);
+  int (*harvest)(void* ctx, int32_t D, int32_t slot, int32_t rid); /* read results before the remove */
+  int64_t (*free_bytes)(void* ctx);
+  int64_t (*bytes_per_particle)(void* ctx, int32_t D);
+  double (*now)(void* ctx); /* NULL: the library's steady clock */
+} gcsph_srv_backend;
+typedef struct gcsph_srv_stats {
+  int32_t requests, completed;
+  int64_t particle_steps;
+  double wall_s; /* time of the last completion */
+  double p50_s, p99_s, mean_s; /* time to horizon (arrival to results on the host); NaN before any */
+} gcsph_srv_stats;
+enum { GCSPH_SRV_QUEUED = 0, GCSPH_SRV_RUNNING = 1, GCSPH_SRV_DONE = 2 };
+
+int srv_create(void* stream, int32_t chunk, double reserve, uint32_t fields, const gcsph_srv_backend* backend,
+               gcsph_srv** out);
+void srv_destroy(gcsph_srv* s);
+/* a request: its particles (host arrays as for ens_add; with a caller's
+ * backend they may be NULL), its horizon in steps and its arrival time
+ * (negative: now); *rid numbers the requests from 0 */
+int srv_submit(gcsph_srv* s, int32_t D, int64_t n, const double* x, const double* v, const double* rho,
+               const int32_t* ptype, const gcsph_ens_params* p, int64_t steps, double arrival, int32_t* rid);
+/* one round (admissions, one chunk per ensemble, releases) */
+int srv_progress(gcsph_srv* s, int32_t* running, int32_t* queued);
+/* rounds until every submitted request has reached its horizon, waiting for
+ * arrivals; GCSPH_ECAPACITY if an arrived request cannot fit on an idle device */
+int srv_run(gcsph_srv* s);
+int srv_request(gcsph_srv* s, int32_t rid, int32_t* state, double* arrival, double* admitted, double* done);
+/* a finished request's field, in its original particle order (library backend) */
+int srv_result(gcsph_srv* s, int32_t rid, int32_t field, double* out_host);
+int srv_stats(gcsph_srv* s, gcsph_srv_stats* st);
+
 #if defined(__GNUC__)
 #pragma GCC visibility pop
 #endif

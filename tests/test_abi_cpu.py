@@ -11,6 +11,7 @@ from conftest import ROOT
 def _declared_functions():
     src = open(os.path.join(ROOT, "include", "gcsph.h")).read()
     src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    src = re.sub(r"\{[^{}]*\}", "", src)  # struct and enum bodies (callback members are not exports)
     names = re.findall(r"^\s*(?:const\s+)?[\w\s\*]+?\b(\w+)\s*\(", src, flags=re.M)
     return sorted({n for n in names if n not in ("if", "defined")})
 
