@@ -92,14 +92,20 @@ struct EnsArr {
   float* ob[3];              // offsets at the instance's last list build (same cell corner as off)
 };
 
-// record layouts (D = 2 | D = 3)
-//   r1: [o0 o1 v0 v1][dr pt - -]        | [o0 o1 o2 v0][v1 v2 dr pt]
-//   r2: [h0 h1 w0 w1][drh pt o0 o1]     | [h0 h1 h2 w0][w1 w2 drh pt][o0 o1 o2 -]
+// record layouts (D = 2 | D = 3); P = the EOS of the record's density, where
+// a slot is free, so that neighbours read it instead of evaluating it
+//   r1: [o0 o1 v0 v1][dr pt P -]        | [o0 o1 o2 v0][v1 v2 dr pt]
+//   r2: [h0 h1 w0 w1][drh pt o0 o1]     | [h0 h1 h2 w0][w1 w2 drh pt][o0 o1 o2 P]
+template <int D, int S>
+__host__ __device__ constexpr bool rec_has_p() {
+  return (D == 2 && S == 1) || (D == 3 && S == 2);
+}
 template <int D>
-__device__ __forceinline__ void put_r1(float4* r, int64_t k, const float* o, const float* v, float dr, int pt) {
+__device__ __forceinline__ void put_r1(float4* r, int64_t k, const float* o, const float* v, float dr, int pt,
+                                       float P) {
   if (D == 2) {
     r[2 * k] = make_float4(o[0], o[1], v[0], v[1]);
-    r[2 * k + 1] = make_float4(dr, __int_as_float(pt), 0.f, 0.f);
+    r[2 * k + 1] = make_float4(dr, __int_as_float(pt), P, 0.f);
   } else {
     r[2 * k] = make_float4(o[0], o[1], o[D - 1], v[0]);
     r[2 * k + 1] = make_float4(v[1], v[D - 1], dr, __int_as_float(pt));
@@ -126,13 +132,15 @@ __device__ __forceinline__ Rec<D, S> load_rec(const float4* __restrict__ r1, con
   }
   return x;
 }
-// decode: o = offset at x, h = offset at xΔt½ (stage 2), v, δρ, ptype
+// decode: o = offset at x, h = offset at xΔt½ (stage 2), v, δρ, ptype, and
+// P where the record holds it (rec_has_p)
 template <int D, int S>
-__device__ __forceinline__ void decode_rec(const Rec<D, S>& x, float* o, float* h, float* v, float& dr, int& pt) {
+__device__ __forceinline__ void decode_rec(const Rec<D, S>& x, float* o, float* h, float* v, float& dr, int& pt,
+                                           float& P) {
   if (S == 1) {
     if (D == 2) {
       o[0] = x.a.x; o[1] = x.a.y; v[0] = x.a.z; v[1] = x.a.w;
-      dr = x.b.x; pt = __float_as_int(x.b.y);
+      dr = x.b.x; pt = __float_as_int(x.b.y); P = x.b.z;
     } else {
       o[0] = x.a.x; o[1] = x.a.y; o[D - 1] = x.a.z; v[0] = x.a.w;
       v[1] = x.b.x; v[D - 1] = x.b.y; dr = x.b.z; pt = __float_as_int(x.b.w);
@@ -144,21 +152,21 @@ __device__ __forceinline__ void decode_rec(const Rec<D, S>& x, float* o, float* 
     } else {
       h[0] = x.a.x; h[1] = x.a.y; h[D - 1] = x.a.z; v[0] = x.a.w;
       v[1] = x.b.x; v[D - 1] = x.b.y; dr = x.b.z; pt = __float_as_int(x.b.w);
-      o[0] = x.c.x; o[1] = x.c.y; o[D - 1] = x.c.z;
+      o[0] = x.c.x; o[1] = x.c.y; o[D - 1] = x.c.z; P = x.c.w;
     }
   }
 }
 
 template <int D>
 __device__ __forceinline__ void put_r2(float4* r, int64_t k, const float* h, const float* w, float drh, int pt,
-                                       const float* o) {
+                                       const float* o, float P) {
   if (D == 2) {
     r[2 * k] = make_float4(h[0], h[1], w[0], w[1]);
     r[2 * k + 1] = make_float4(drh, __int_as_float(pt), o[0], o[1]);
   } else {
     r[3 * k] = make_float4(h[0], h[1], h[D - 1], w[0]);
     r[3 * k + 1] = make_float4(w[1], w[D - 1], drh, __int_as_float(pt));
-    r[3 * k + 2] = make_float4(o[0], o[1], o[D - 1], 0.f);
+    r[3 * k + 2] = make_float4(o[0], o[1], o[D - 1], P);
   }
 }
 
@@ -314,25 +322,31 @@ __global__ void k_ens_permute(int64_t N, const int32_t* __restrict__ perm, const
   out.drb[k] = in.drb[i];
   out.pt[k] = pt;
   out.id[k] = in.id[i];
-  put_r1<D>(r1, k, ov, vv, dr, pt);
+  put_r1<D>(r1, k, ov, vv, dr, pt, D == 2 ? eos32(dr, pt, I) : 0.f);
 }
 
 // ---------------------------------------------------------------------------
 // neighbour list, built after the re-sort of the instances that rebuild: the
-// 3^D cell walk with the pair test r < H (1 + skin) at x (FP32 offsets), each
-// entry the neighbour's instance-local index packed with its cell shift
-// ((dx+1) + 3(dy+1) + 9(dz+1) in the low 5 bits).  Every pass keeps only the
-// entries with r < H at the step's x, so the pairs of a step are those the
-// reference's update! finds, whichever step built the list.  Stored entry-major (entry q of particle i at q*ncap + i) so that the
-// passes' loads coalesce.  A row that outgrows the stride raises *ovf: every
-// later kernel of the call skips, the host grows the stride and repeats.
+// 3^D cell walk with the pair test r < H (1 + skin) at x (FP32 offsets).  An
+// entry is the neighbour's instance-local index above 6 bits of cell shift,
+// (dx+1) | (dy+1) << 2 | (dz+1) << 4 (the index is below 2^26, so the entry
+// is read as unsigned).  Every pass keeps only the entries with r < H at the
+// step's x, so the pairs of a step are those the reference's update! finds,
+// whichever step built the list.  Stored entry-major (entry q of particle i
+// at q*ncap + i) so that the passes' loads coalesce.  A row that outgrows the
+// stride raises *ovf: every later kernel of the call skips, the host grows
+// the stride and repeats.
 // ---------------------------------------------------------------------------
+__device__ __forceinline__ int ent_code(int dxc, int dy, int dz) {
+  return (dxc + 1) | ((dy + 1) << 2) | ((dz + 1) << 4);
+}
+__device__ __forceinline__ int ent_make(int j_local, int code) { return (int)(((unsigned)j_local << 6) | code); }
+__device__ __forceinline__ int ent_index(int ent) { return (int)((unsigned)ent >> 6); }
+
 __device__ __forceinline__ void shift_of(int ent, const EnsInst& I, float& sx, float& sy, float& sz) {
-  const int code = ent & 31;
-  const int ex = code % 3, r = code / 3;
-  sx = (float)(ex - 1) * I.csf;
-  sy = (float)(r % 3 - 1) * I.csf;
-  sz = (float)(r / 3 - 1) * I.csf;
+  sx = (float)((ent & 3) - 1) * I.csf;
+  sy = (float)(((ent >> 2) & 3) - 1) * I.csf;
+  sz = (float)(((ent >> 4) & 3) - 1) * I.csf;
 }
 
 // a candidate's verdict: with L lanes on a particle, a ballot keeps the hits
@@ -342,13 +356,13 @@ __device__ __forceinline__ void nl_emit(const EnsArr& A, int64_t i, int lane, un
                                         int j, int code, int& cnt) {
   if (L == 1) {
     if (hit) {
-      if (cnt < A.nls) __stcs(A.nl + (int64_t)cnt * A.ncap + i, (j << 5) | code);
+      if (cnt < A.nls) __stcs(A.nl + (int64_t)cnt * A.ncap + i, ent_make(j, code));
       ++cnt;
     }
   } else {
     const unsigned bal = (__ballot_sync(gm, hit) >> gbase) & (L == 32 ? 0xffffffffu : ((1u << L) - 1u));
     const int at = cnt + __popc(bal & ((1u << lane) - 1u));
-    if (hit && at < A.nls) __stcs(A.nl + (int64_t)at * A.ncap + i, (j << 5) | code);
+    if (hit && at < A.nls) __stcs(A.nl + (int64_t)at * A.ncap + i, ent_make(j, code));
     cnt += __popc(bal);
   }
 }
@@ -394,7 +408,7 @@ __global__ void __launch_bounds__(ENS_MAX_TPB) k_ens_nlist(EnsArr A, const EnsIn
           if (cx < 0 || cx >= I.nc[0]) continue;
           const int j0 = A.cellstart[row + cx], j1 = A.cellstart[row + cx + 1];
           const float shx = (float)dxc * I.csf, shy = (float)dy * I.csf, shz = (float)dz * I.csf;
-          const int code = (dxc + 1) + 3 * (dy + 1) + 9 * (dz + 1);
+          const int code = ent_code(dxc, dy, dz);
           for (int jb = j0; jb < j1; jb += L) {
             const int j = jb + lane;
             bool hit = false;
@@ -544,7 +558,7 @@ __device__ __forceinline__ void tile_particles(const EnsArr& A, const EnsInst& I
         const int lc = cx - G.cxa;
         const int j0 = G.cs[r][lc], j1 = G.cs[r][lc + 1];
         const float shx = (float)dxc * I.csf, shy = (float)dy * I.csf, shz = (float)dz * I.csf;
-        const int code = (dxc + 1) + 3 * (dy + 1) + 9 * (dz + 1);
+        const int code = ent_code(dxc, dy, dz);
         for (int jb = j0; jb < j1; jb += L) {
           const int j = jb + lane;
           bool hit = false;
@@ -672,13 +686,13 @@ __global__ void __launch_bounds__(ENS_MAX_TPB, 2) k_ens_stage(EnsArr A, const En
     for (int e = lane; e < nn; e += L) {
       const int ent = nxt;
       if (e + L < nn) nxt = A.nl[(int64_t)(e + L) * A.ncap + i];
-      const Rec<D, STAGE> rec = load_rec<D, STAGE>(A.r1, A.r2, I.p_off + (ent >> 5));
+      const Rec<D, STAGE> rec = load_rec<D, STAGE>(A.r1, A.r2, I.p_off + ent_index(ent));
       float shx, shy, shz;
       shift_of(ent, I, shx, shy, shz);
       // the neighbour's record: offsets (at x, and at xΔt½ in stage 2), velocity, δρ, ptype
-      float oj[D], hj[D], vj[D], drj;
+      float oj[D], hj[D], vj[D], drj, Prec = 0.f;
       int ptj;
-      decode_rec<D, STAGE>(rec, oj, hj, vj, drj, ptj);
+      decode_rec<D, STAGE>(rec, oj, hj, vj, drj, ptj, Prec);
       float d[D];
 #pragma unroll
       for (int q = 0; q < D; ++q) d[q] = (oi[q] - oj[q]) - (q == 0 ? shx : (q == 1 ? shy : shz));
@@ -717,7 +731,8 @@ __global__ void __launch_bounds__(ENS_MAX_TPB, 2) k_ens_stage(EnsArr A, const En
       }
       if (pti * ptj > 0) {
         // ∂v∂t!
-        const float sc = -I.m0 * (Pi + eos32(drj, ptj, I)) * (irhoi * irhoj);
+        const float Pj = rec_has_p<D, STAGE>() ? Prec : eos32(drj, ptj, I);
+        const float sc = -I.m0 * (Pi + Pj) * (irhoi * irhoj);
 #pragma unroll
         for (int q = 0; q < D; ++q) f[q] = sc * gw[q];
       }
@@ -782,7 +797,7 @@ __global__ void __launch_bounds__(ENS_MAX_TPB, 2) k_ens_stage(EnsArr A, const En
         hh[q] = (oi[q] + A.dxb[q][i]) + vh * hdt;
         A.offh[q][i] = hh[q];
       }
-      put_r2<D>(A.r2, i, hh, ww, drh, pti, oi);
+      put_r2<D>(A.r2, i, hh, ww, drh, pti, oi, D == 3 ? eos32(drh, pti, I) : 0.f);
     } else {
       // symplectic_update!: δρ_new = δρ - ρ 2ε/(2+ε), positions in FP64
       const float dr0 = A.dr[i];
@@ -834,7 +849,7 @@ __global__ void __launch_bounds__(ENS_MAX_TPB) k_ens_dpc(EnsArr A, const EnsInst
       for (int e = 0; e < nn; ++e) {
         const int ent = nxt;
         if (e + 1 < nn) nxt = A.nl[(int64_t)(e + 1) * A.ncap + i];
-        const int j = I.p_off + (ent >> 5);
+        const int j = I.p_off + ent_index(ent);
         const int ptj = A.pt[j];
         if (!(ptj > 0)) continue;
         float shx, shy, shz;
@@ -918,7 +933,7 @@ __global__ void __launch_bounds__(ENS_MAX_TPB) k_ens_xsph(EnsArr A, const EnsIns
     for (int e = 0; e < nn; ++e) {
       const int ent = nxt;
       if (e + 1 < nn) nxt = A.nl[(int64_t)(e + 1) * A.ncap + i];
-      const int j = I.p_off + (ent >> 5);
+      const int j = I.p_off + ent_index(ent);
       if (!(A.pt[j] > 1)) continue;
       float shx, shy, shz;
       shift_of(ent, I, shx, shy, shz);
@@ -978,7 +993,7 @@ __global__ void __launch_bounds__(ENS_MAX_TPB) k_ens_cspm(EnsArr A, const EnsIns
     for (int e = 0; e < nn; ++e) {
       const int ent = nxt;
       if (e + 1 < nn) nxt = A.nl[(int64_t)(e + 1) * A.ncap + i];
-      const int j = I.p_off + (ent >> 5);
+      const int j = I.p_off + ent_index(ent);
       if (!(A.pt[j] > 0)) continue;
       float shx, shy, shz;
       shift_of(ent, I, shx, shy, shz);
