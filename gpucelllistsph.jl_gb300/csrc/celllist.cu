@@ -629,22 +629,31 @@ int CellCore::pair_lanes() const {
     }                                                                                            \
   } while (0)
 
-int CellCore::build_pairs(const double* const* xs, int* ovf_dev, bool scan_up) {
+int CellCore::ensure_pf() {
+  int rc;
+  for (int d = 0; d < D; ++d)
+    if ((rc = pf[d].ensure(sizeof(float) * N, st))) return rc;
+  return pfmax.ensure(sizeof(unsigned long long), st, true);
+}
+
+int CellCore::build_pairs(const double* const* xs, int* ovf_dev, bool scan_up, bool pf_ready) {
   if (!sorted) return fail(GCSPH_ESTATE, "pair build before binning");
   const double* x2 = D == 3 ? xs[2] : xs[0];
   timer_begin(T_PAIRS, st);
   const int L = pair_lanes();
   int rc0;
-  for (int d = 0; d < D; ++d)
-    if ((rc0 = pf[d].ensure(sizeof(float) * N, st))) return rc0;
-  if ((rc0 = pfmax.ensure(sizeof(unsigned long long), st, true))) return rc0;
+  if ((rc0 = ensure_pf())) return rc0;
   float* f2 = D == 3 ? pf[2].as<float>() : pf[0].as<float>();
   unsigned long long* bm = pfmax.as<unsigned long long>();
-  if (D == 2)
-    k_make_pf<2><<<nblocks(N, TPB), TPB, 0, st>>>(xs[0], xs[1], x2, N, g, pf[0].as<float>(), pf[1].as<float>(), f2, bm);
-  else
-    k_make_pf<3><<<nblocks(N, TPB), TPB, 0, st>>>(xs[0], xs[1], x2, N, g, pf[0].as<float>(), pf[1].as<float>(), f2, bm);
-  GC_LAUNCHED();
+  if (!pf_ready) {
+    if (D == 2)
+      k_make_pf<2><<<nblocks(N, TPB), TPB, 0, st>>>(xs[0], xs[1], x2, N, g, pf[0].as<float>(), pf[1].as<float>(), f2,
+                                                     bm);
+    else
+      k_make_pf<3><<<nblocks(N, TPB), TPB, 0, st>>>(xs[0], xs[1], x2, N, g, pf[0].as<float>(), pf[1].as<float>(), f2,
+                                                     bm);
+    GC_LAUNCHED();
+  }
   // rows of up to S neighbours are staged by the count pass and copied by the fill
   const double mean = N > 0 && nfull_est > 0 ? (double)nfull_est / (double)N : 0.0;
   int S = 16;

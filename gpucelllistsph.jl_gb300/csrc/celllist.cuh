@@ -60,7 +60,9 @@ struct CellCore {
   // count: rows past nbr_cap raise *ovf_dev instead (see grow_nbr).  scan_up
   // also scans the larger-index counts into rs_up (device only) in the same
   // launch as the row offsets.
-  int build_pairs(const double* const* xs, int* ovf_dev = nullptr, bool scan_up = false);
+  // pf_ready: the FP32 prefilter copy of xs (pf, pfmax) was written by the caller's permute
+  int build_pairs(const double* const* xs, int* ovf_dev = nullptr, bool scan_up = false, bool pf_ready = false);
+  int ensure_pf();
   int grow_nbr(int64_t need);
   int read_nfull();
   int ensure_up();

@@ -524,6 +524,11 @@ struct PermOut {
   double* rhoh;
   int32_t* pt;
   double* buf2[3];
+  // the pair build's FP32 prefilter copy of the new positions and its bound
+  // (what the cell list's k_make_pf writes), so that it needs no pass of its own
+  float* pf[3];
+  unsigned long long* pfmax;
+  double off[3];
 };
 
 // new[k] = old[perm[k]] for the whole cell-order state; cΔx restarts at 0
@@ -531,6 +536,21 @@ struct PermOut {
 template <int D>
 __global__ void k_permute_state(StepConst c, int64_t N, const int32_t* __restrict__ perm, SArr<D> S, PermOut<D> O) {
   int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  double b = 0.0;
+  if (k < N) {
+    const int32_t i = perm[k];
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      const double xv = S.x[d][i];
+      O.x[d][k] = xv;
+      const double rel = xv - O.off[d];
+      O.pf[d][k] = (float)rel;
+      b = fmax(b, fabs(rel));
+    }
+    if (b != b) b = INFINITY;  // NaN coordinate: every candidate of the set goes to FP64
+  }
+  b = warp_max(b);
+  if ((threadIdx.x & 31) == 0) atomic_max_pos(O.pfmax, b);
   if (k >= N) return;
   const int32_t i = perm[k];
   const int pt = S.pt[i];
@@ -542,7 +562,6 @@ __global__ void k_permute_state(StepConst c, int64_t N, const int32_t* __restric
   S.ir[k] = 1.0 / r;
 #pragma unroll
   for (int d = 0; d < D; ++d) {
-    O.x[d][k] = S.x[d][i];
     O.xh[d][k] = S.xh[d][i];
     O.v[d][k] = S.v[d][i];
     O.vh[d][k] = S.vh[d][i];
@@ -812,6 +831,7 @@ template <int D>
 static int rebuild(sph_handle* h, const StepConst& c, int* ovf_dev) {
   CellCore& core = h->cl->core;
   int rc;
+  bool pf_ready = false;
   if (!h->in_cell_order) {
     // first update! of a call: bin the original-order points and gather the state
     if ((rc = core.sort(h->cl->xuser, nullptr))) return rc;
@@ -829,9 +849,17 @@ static int rebuild(sph_handle* h, const StepConst& c, int* ovf_dev) {
     const double* xc[3] = {h->X[h->ix][0].as<double>(), h->X[h->ix][1].as<double>(),
                            D == 3 ? h->X[h->ix][2].as<double>() : nullptr};
     if ((rc = core.sort(xc, core.orig.as<int32_t>()))) return rc;
+    if ((rc = core.ensure_pf())) return rc;
+    PermOut<D> alt = make_alt<D>(h);
+    for (int d = 0; d < D; ++d) {
+      alt.pf[d] = core.pf[d].as<float>();
+      alt.off[d] = core.g.offset[d];
+    }
+    alt.pfmax = core.pfmax.as<unsigned long long>();
     timer_begin(T_STATE, core.st);
     k_permute_state<D><<<nblocks(h->N, 256), 256, 0, core.st>>>(c, h->N, core.perm.as<int32_t>(), make_arr<D>(h),
-                                                               make_alt<D>(h));
+                                                               alt);
+    pf_ready = true;
     GC_LAUNCHED();
     timer_end(T_STATE, core.st);
     h->ix ^= 1;
@@ -849,7 +877,7 @@ static int rebuild(sph_handle* h, const StepConst& c, int* ovf_dev) {
   }
   const double* xs[3] = {h->X[h->ix][0].as<double>(), h->X[h->ix][1].as<double>(),
                          D == 3 ? h->X[h->ix][2].as<double>() : nullptr};
-  if ((rc = core.build_pairs(xs, ovf_dev, true))) return rc;
+  if ((rc = core.build_pairs(xs, ovf_dev, true, pf_ready))) return rc;
   if ((rc = grow_entry_arrays<D>(h))) return rc;
   // flat pair list: offsets scanned with the row offsets (no read-back), then the quads
   timer_begin(T_PAIRS, core.st);
