@@ -163,3 +163,31 @@ def test_full_size_pair_sets(gpu_pkg, orc, D, N, dist):
     kw = np.sort(want[:, 0] * (1 << 32) + want[:, 1])
     assert np.array_equal(kg, kw)
     assert np.unique(kg).size == kg.size
+
+
+@pytest.mark.parametrize("D", [2, 3])
+def test_tiny_and_degenerate_sets(gpu_pkg, orc, D):
+    """One point (no pairs); two coincident points (r² = 0 < dist²: one pair);
+    two points exactly dist apart (the reference's test is strict: no pair);
+    every case against the oracle.  An empty set is refused, as the
+    reference's bounding box of no points is an error."""
+    dist = 0.1
+    cases = {
+        "one": np.full((D, 1), 0.5),
+        "coincident": np.full((D, 2), 0.5),
+        "exactly_dist": np.zeros((D, 2)),
+        "far": np.array([[0.0, 1.0]] + [[0.0, 0.0]] * (D - 1)),
+    }
+    cases["exactly_dist"][0, 1] = dist
+    want = {"one": 0, "coincident": 1, "exactly_dist": 0, "far": 0}
+    for name, x in cases.items():
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        c = gpu_pkg.GPUCellList(tuple(x), (dist,) * D, dist)
+        pairs, n, _ = _oracle_pairs(orc, x, (dist,) * D, dist)
+        assert c.pairsn == n == want[name], (name, c.pairsn, n)
+        got = _set(orc, c.neighborlistview())
+        assert np.array_equal(got, orc.pair_set(pairs)), name
+        c.update()
+        assert c.pairsn == want[name], name
+    with pytest.raises(RuntimeError):
+        gpu_pkg.GPUCellList(tuple(np.zeros((D, 0))), (dist,) * D, dist)

@@ -277,6 +277,24 @@ def test_zero_steps_and_getters(gpu_pkg, orc):
     assert gpu_pkg.get_points(prob) is prob.system.points
 
 
+@pytest.mark.parametrize("lanes", [1, 0])
+def test_isolated_particles_fall_freely(gpu_pkg, orc, lanes):
+    """Three fluid particles far apart, no boundary within H: every pair sum
+    is empty (no pairs at all), ρ stays, each falls under gravity alone --
+    as the oracle does, bit for bit on serial rows."""
+    import dataclasses
+    base = gpu_pkg.workloads.dam_break_2d(dx=0.05, fluid=(0.5, 0.6), tank=(1.0, 1.0))
+    x = np.array([[0.1, 0.9, 0.5], [0.5, 0.5, 0.9]], dtype=np.float64)
+    case = dataclasses.replace(base, x=x, rho=np.full(3, 1000.0), ptype=np.full(3, 2, np.int32))
+    prob, ref = make_pair(gpu_pkg, orc, case, lanes)
+    assert prob.system.pairsn == 0
+    run_both(prob, ref, 20)
+    check(orc, prob, ref, case, lanes, [(20, {})])
+    v = gpu_field(prob, "v")
+    assert np.allclose(v[1], -case.g * 20 * case.dt, rtol=1e-12, atol=0) and np.all(v[0] == 0)
+    assert np.all(gpu_field(prob, "rho") == 1000.0)
+
+
 # ----------------------------------------------------------------- standalone kernels
 def _kernel_setup(pkg, orc, D=2):
     rng = np.random.default_rng(7)
