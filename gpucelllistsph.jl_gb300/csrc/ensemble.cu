@@ -88,6 +88,13 @@ struct EnsArr {
   //   r2 (2 or 3):   xΔt½ offset, vΔt½, δρΔt½, ptype, x offset -- stage 2
   float4* r1;
   float4* r2;
+  // records of the correction passes, in r1's layout (offsets, v, δρ, ptype):
+  //   r3: offsets after the corrector -- dpcreg!'s neighbours (null: no DPC)
+  //   r4: offsets at the step's start, v after dpcreg! -- xsphcorr!, cspmcorr!
+  //       and dpcreg!'s pair test (null: none of the three)
+  float4* r3;
+  float4* r4;
+  const int32_t* istep;      // steps done per instance (cspmcorr! schedule)
   const int* rb;             // per instance: this step rebuilds the instance's cells and list
   float* ob[3];              // offsets at the instance's last list build (same cell corner as off)
 };
@@ -632,6 +639,10 @@ __global__ void __launch_bounds__(TILE_TPB) k_ens_nlist_tile(EnsArr A, const Ens
 // ---------------------------------------------------------------------------
 // the two pair passes over the step's neighbour list, persistent grid-stride
 // ---------------------------------------------------------------------------
+__device__ __forceinline__ bool cspm_due(const EnsInst& I, const int32_t* istep, int s) {
+  return I.cspmn > 0 && (istep[s] + 1) % I.cspmn == 0;
+}
+
 // lanes per particle in the pair passes: fixed per dimension (never tuned),
 // so that the summation order -- and every result -- is the same whatever
 // the launch shape and whatever else is in the ensemble
@@ -806,17 +817,23 @@ __global__ void __launch_bounds__(ENS_MAX_TPB, 2) k_ens_stage(EnsArr A, const En
       if (dn < 0.f && pti <= 1) dn = 0.f;
       A.dr[i] = dn;
       A.drb[i] = dn;
+      float nvs[D], ons[D];
 #pragma unroll
       for (int q = 0; q < D; ++q) {
         const float v0 = A.v[q][i];
         const float nv = pti > 1 ? v0 + a[q] * dt : v0;
         A.v[q][i] = nv;
+        nvs[q] = nv;
         const double ddx = ((double)v0 + (double)nv) * 0.5 * I.dt;
         A.x[q][i] = A.x[q][i] + ddx;
-        A.offn[q][i] = oi[q] + (float)ddx;
+        ons[q] = oi[q] + (float)ddx;
+        A.offn[q][i] = ons[q];
         A.dxb[q][i] = 0.f;
         A.dvb[q][i] = 0.f;
       }
+      if (A.r3 && I.use_dpc) put_r1<D>(A.r3, i, ons, nvs, dn, pti, 0.f);
+      if (A.r4 && (I.use_dpc || I.use_xsph || cspm_due(I, A.istep, A.inst[i])))
+        put_r1<D>(A.r4, i, oi, nvs, dn, pti, 0.f);
     }
   }
 }
@@ -850,28 +867,38 @@ __global__ void __launch_bounds__(ENS_MAX_TPB) k_ens_dpc(EnsArr A, const EnsInst
         const int ent = nxt;
         if (e + 1 < nn) nxt = A.nl[(int64_t)(e + 1) * A.ncap + i];
         const int j = I.p_off + ent_index(ent);
-        const int ptj = A.pt[j];
-        if (!(ptj > 0)) continue;
+        // the neighbour after the corrector: its record's first half holds
+        // the offsets; beyond l0 (u >= 1) W, χ and Pᵇ vanish and so does the
+        // pair's dpcreg! term, so the rest is read only within l0
+        const float4 ra = __ldg(A.r3 + 2 * (int64_t)j);
         float shx, shy, shz;
         shift_of(ent, I, shx, shy, shz);
-        if (I.reuse) {
-          // a pair of this step: r < H at the step's starting positions
-          float dm[D];
+        const float onj[3] = {ra.x, ra.y, D == 3 ? ra.z : 0.f};
+        float dx[D];
 #pragma unroll
-          for (int q = 0; q < D; ++q) dm[q] = (A.off[q][i] - A.off[q][j]) - (q == 0 ? shx : (q == 1 ? shy : shz));
-          if (!(dot32<D>(dm, dm) < I.H2)) continue;
-        }
-        float dx[D], dv[D];
-#pragma unroll
-        for (int q = 0; q < D; ++q) {
-          dx[q] = (ni[q] - A.offn[q][j]) - (q == 0 ? shx : (q == 1 ? shy : shz));
-          dv[q] = vi[q] - A.v[q][j];
-        }
-        const float drj = A.dr[j];
-        const float rhoj = I.rho0 + drj;
+        for (int q = 0; q < D; ++q) dx[q] = (ni[q] - onj[q]) - (q == 0 ? shx : (q == 1 ? shy : shz));
         const float r2 = dot32<D>(dx, dx);
         const float u = sqrt_fast(r2) * I.dpc_l0inv;
-        const float t = u < 1.f ? 1.f - u : 0.f;
+        if (!(u < 1.f)) continue;
+        const float4 rb = __ldg(A.r3 + 2 * (int64_t)j + 1);
+        const float vj[3] = {D == 2 ? ra.z : ra.w, D == 2 ? ra.w : rb.x, D == 2 ? 0.f : rb.y};
+        const float drj = D == 2 ? rb.x : rb.z;
+        const int ptj = __float_as_int(D == 2 ? rb.y : rb.w);
+        if (!(ptj > 0)) continue;
+        if (I.reuse) {
+          // a pair of this step: r < H at the step's starting positions
+          const float4 sj = __ldg(A.r4 + 2 * (int64_t)j);
+          const float oj[3] = {sj.x, sj.y, sj.z};
+          float dm[D];
+#pragma unroll
+          for (int q = 0; q < D; ++q) dm[q] = (A.off[q][i] - oj[q]) - (q == 0 ? shx : (q == 1 ? shy : shz));
+          if (!(dot32<D>(dm, dm) < I.H2)) continue;
+        }
+        float dv[D];
+#pragma unroll
+        for (int q = 0; q < D; ++q) dv[q] = vi[q] - vj[q];
+        const float rhoj = I.rho0 + drj;
+        const float t = 1.f - u;
         const float t2 = t * t;
         const float w = (1.f + 4.f * u) * (t2 * t2) * I.dpc_nW;
         const float chi = sqrt_fast(w * I.dpc_whinv);
@@ -898,16 +925,20 @@ __global__ void k_ens_dpc_apply(EnsArr A, const EnsInst* __restrict__ T) {
   if (i >= A.N) return;
   const EnsInst& I = T[A.inst[i]];
   if (!I.use_dpc || !(A.pt[i] > 1)) return;
+  float nv[D], o[D];
 #pragma unroll
   for (int q = 0; q < D; ++q) {
     const float s = A.vh[q][i];
-    A.v[q][i] = A.v[q][i] + s;
+    nv[q] = A.v[q][i] + s;
+    A.v[q][i] = nv[q];
     A.dvb[q][i] -= s;
     const double dx = (double)s * I.dt;
     A.x[q][i] = A.x[q][i] + dx;
     A.offn[q][i] += (float)dx;
     A.dxb[q][i] -= (float)dx;
+    o[q] = A.off[q][i];
   }
+  put_r1<D>(A.r4, i, o, nv, A.dr[i], A.pt[i], 0.f);  // the later passes see v after dpcreg!
 }
 
 // xsphcorr! + update_xsphcorr! (src/gpukernels_sph.jl:1745-1838): stage-1 W
@@ -934,21 +965,24 @@ __global__ void __launch_bounds__(ENS_MAX_TPB) k_ens_xsph(EnsArr A, const EnsIns
       const int ent = nxt;
       if (e + 1 < nn) nxt = A.nl[(int64_t)(e + 1) * A.ncap + i];
       const int j = I.p_off + ent_index(ent);
-      if (!(A.pt[j] > 1)) continue;
+      float oj[D], hj[D], vj[D], drj, pu;
+      int ptj;
+      decode_rec<D, 1>(load_rec<D, 1>(A.r4, nullptr, j), oj, hj, vj, drj, ptj, pu);
+      if (!(ptj > 1)) continue;
       float shx, shy, shz;
       shift_of(ent, I, shx, shy, shz);
       float d[D];
 #pragma unroll
-      for (int q = 0; q < D; ++q) d[q] = (oi[q] - A.off[q][j]) - (q == 0 ? shx : (q == 1 ? shy : shz));
+      for (int q = 0; q < D; ++q) d[q] = (oi[q] - oj[q]) - (q == 0 ? shx : (q == 1 ? shy : shz));
       const float r2 = dot32<D>(d, d);
       if (!(r2 < I.H2)) continue;  // in the list's skin
       const float u = sqrt_fast(r2) * I.Hinv;
       const float t = u < 1.f ? 1.f - u : 0.f;
       const float t2 = t * t;
       const float w = (1.f + 4.f * u) * (t2 * t2) * I.nW;
-      const float xs = I.xsph_c * w * __fdividef(1.f, rhoi + (I.rho0 + A.dr[j]));
+      const float xs = I.xsph_c * w * __fdividef(1.f, rhoi + (I.rho0 + drj));
 #pragma unroll
-      for (int q = 0; q < D; ++q) sum[q].add((A.v[q][j] - vi[q]) * xs);
+      for (int q = 0; q < D; ++q) sum[q].add((vj[q] - vi[q]) * xs);
     }
 #pragma unroll
     for (int q = 0; q < D; ++q) {
@@ -966,9 +1000,6 @@ __global__ void __launch_bounds__(ENS_MAX_TPB) k_ens_xsph(EnsArr A, const EnsIns
 // formed as δρ = Σ m0 W δρ_j/ρ_j / Σ m0 W/ρ_j (no cancellation against ρ₀).
 // The result goes to δρ½ (free after the corrector) and is applied by
 // k_ens_cspm_apply, so every particle reads the pre-correction densities.
-__device__ __forceinline__ bool cspm_due(const EnsInst& I, const int32_t* istep, int s) {
-  return I.cspmn > 0 && (istep[s] + 1) % I.cspmn == 0;
-}
 
 template <int D>
 __global__ void __launch_bounds__(ENS_MAX_TPB) k_ens_cspm(EnsArr A, const EnsInst* __restrict__ T,
@@ -994,19 +1025,21 @@ __global__ void __launch_bounds__(ENS_MAX_TPB) k_ens_cspm(EnsArr A, const EnsIns
       const int ent = nxt;
       if (e + 1 < nn) nxt = A.nl[(int64_t)(e + 1) * A.ncap + i];
       const int j = I.p_off + ent_index(ent);
-      if (!(A.pt[j] > 0)) continue;
+      float oj[D], hj[D], vj[D], drj, pu;
+      int ptj;
+      decode_rec<D, 1>(load_rec<D, 1>(A.r4, nullptr, j), oj, hj, vj, drj, ptj, pu);
+      if (!(ptj > 0)) continue;
       float shx, shy, shz;
       shift_of(ent, I, shx, shy, shz);
       float d[D];
 #pragma unroll
-      for (int q = 0; q < D; ++q) d[q] = (oi[q] - A.off[q][j]) - (q == 0 ? shx : (q == 1 ? shy : shz));
+      for (int q = 0; q < D; ++q) d[q] = (oi[q] - oj[q]) - (q == 0 ? shx : (q == 1 ? shy : shz));
       const float r2 = dot32<D>(d, d);
       if (!(r2 < I.H2)) continue;  // in the list's skin
       const float u = sqrt_fast(r2) * I.Hinv;
       const float t = u < 1.f ? 1.f - u : 0.f;
       const float t2 = t * t;
       const float w = (1.f + 4.f * u) * (t2 * t2) * I.nW;
-      const float drj = A.dr[j];
       const float mw = I.m0 * w * __fdividef(1.f, I.rho0 + drj);
       s2.add(mw);
       s3.add(mw * drj);
@@ -1186,6 +1219,7 @@ struct gcsph_ens {
   DevBuf NL, NLC;        // neighbour list of the step and its row lengths
   DevBuf FLAGS;          // [0] list overflow, [1] longest row, [2] steps done in the call
   DevBuf R1, R2;         // packed neighbour records of the two stages
+  DevBuf R3, R4;         // packed neighbour records of the correction passes
   DevBuf OB[3];          // offsets at each instance's last list build
   DevBuf RB, NREB, DMAX; // per instance: rebuild at the next step, list builds, largest displacement²
   double skin = 0.05;    // list radius H (1 + skin); 0: every step rebuilds
@@ -1281,6 +1315,9 @@ EnsArr ens_arr(gcsph_ens* e) {
   A.r2 = e->R2.as<float4>();
   A.pt = e->PT[e->cur].as<int32_t>();
   A.rb = e->RB.as<int>();
+  A.r3 = e->any_dpc ? e->R3.as<float4>() : nullptr;
+  A.r4 = (e->any_dpc || e->any_xsph || e->any_cspm) ? e->R4.as<float4>() : nullptr;
+  A.istep = e->ISTEP.as<int32_t>();
   for (int d = 0; d < 3; ++d) A.ob[d] = e->OB[d < e->D ? d : 0].as<float>();
   return A;
 }
@@ -1353,6 +1390,8 @@ int ens_reserve(gcsph_ens* e, int64_t n) {
   if ((rc = e->DRH.ensure(sizeof(float) * want, e->st))) return rc;
   if ((rc = e->R1.ensure(sizeof(float4) * 2 * want, e->st))) return rc;
   if ((rc = e->R2.ensure(sizeof(float4) * (e->D == 2 ? 2 : 3) * want, e->st))) return rc;
+  if ((rc = e->R3.ensure(sizeof(float4) * 2 * want, e->st))) return rc;
+  if ((rc = e->R4.ensure(sizeof(float4) * 2 * want, e->st))) return rc;
   if ((rc = e->SCRATCH.ensure(sizeof(int64_t) * scan_scratch_elems(std::max<int64_t>(want, e->cap_k) + 1), e->st)))
     return rc;
   e->cap_n = want;
@@ -1910,7 +1949,8 @@ int ens_bytes_per_particle(int32_t D, int64_t* bytes) {
   // offn) per dim + δρ½, plus about one cell per particle
   // + the step's neighbour list (64 entries in 2-D, 256 in 3-D, 4 B each) and its length
   *bytes = 2 * D * (8 + 4 + 8) + 2 * 16 + 6 * 4 + D * 16 + 4 + 8 + (D == 2 ? 64 : 256) * 4 + 4 +
-           16 * (D == 2 ? 4 : 5) +  // packed records
+           16 * (D == 2 ? 4 : 5) +  // packed records of the stages
+           64 +                     // and of the correction passes
            D * 4;                   // offsets at the last list build
   return GCSPH_OK;
 }
