@@ -252,11 +252,17 @@ __global__ void __launch_bounds__(STPB) k_dpc(StepConst c, const Scal* __restric
       if (!(S.pt[m] > 0)) continue;
       double dx[D], dv[D];
 #pragma unroll
-      for (int d = 0; d < D; ++d) { dx[d] = xk[d] - S.x[d][m]; dv[d] = vk[d] - S.v[d][m]; }
-      const double rm = S.rho[m];
+      for (int d = 0; d < D; ++d) dx[d] = xk[d] - S.x[d][m];
       const double r2 = dotD<D>(dx, dx);
       const double r = sqrt(r2);
       const double u = r * c.dpc_l0inv;
+      // u >= 1: W = 0, so χ = 0, the factor (u >= dpckernlim) is χ and Pᵇ = 0 --
+      // the pair adds an exact zero to either branch's sum, which it leaves as
+      // it is (up to the sign of a zero sum): skip it
+      if (!(u < 1.0)) continue;
+#pragma unroll
+      for (int d = 0; d < D; ++d) dv[d] = vk[d] - S.v[d][m];
+      const double rm = S.rho[m];
       const double w = wc2_w(u, c.dpc_nW);
       const double chi = sqrt(w * c.dpc_whinv);
       const double kk = u < c.dpc_kernlim ? 1.0 : chi;
