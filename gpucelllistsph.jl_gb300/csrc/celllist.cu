@@ -17,6 +17,7 @@
 #include <mutex>
 #include <utility>
 
+#include <stdint.h>
 #include "celllist.cuh"
 
 namespace gcsph {
@@ -240,6 +241,28 @@ __global__ void k_emit_pairs(const int64_t* __restrict__ rs_full, const int64_t*
     int32_t om = orig[nbr[r1 - nu + t]] + 1;
     pairs[2 * pos] = ok < om ? ok : om;
     pairs[2 * pos + 1] = ok < om ? om : ok;
+  }
+}
+
+// The same emit with L lanes per point: the row's entries are read
+// contiguously and each pair is one 8-byte store (pairs 8-byte aligned), so a
+// warp's loads and stores coalesce; same positions, same contents.
+template <int L>
+__global__ void k_emit_pairs_l(const int64_t* __restrict__ rs_full, const int64_t* __restrict__ rs_up,
+                               const int32_t* __restrict__ nbr, const int32_t* __restrict__ orig, int64_t N,
+                               int64_t cap, int2* __restrict__ pairs) {
+  const int64_t gt = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t k = gt / L;
+  const int lane = (int)(gt % L);
+  if (k >= N) return;
+  const int64_t r1 = rs_full[k + 1];
+  const int64_t u0 = rs_up[k], nu = rs_up[k + 1] - u0;
+  const int32_t ok = orig[k] + 1;
+  for (int64_t t = lane; t < nu; t += L) {
+    const int64_t pos = u0 + t;
+    if (pos >= cap) break;
+    const int32_t om = orig[nbr[r1 - nu + t]] + 1;
+    pairs[pos] = make_int2(ok < om ? ok : om, ok < om ? om : ok);
   }
 }
 
@@ -739,8 +762,29 @@ int CellCore::emit(int32_t* pairs, int64_t cap, int fillzero, int64_t* pairsn) {
   if (pairsn) *pairsn = nup;
   if (cap > 0 && !pairs) return fail(GCSPH_EINVAL, "null pair buffer");
   if (cap > 0) {
-    k_emit_pairs<<<nblocks(N, TPB), TPB, 0, st>>>(rs_full.as<int64_t>(), rs_up.as<int64_t>(), nbr.as<int32_t>(),
-                                                   orig.as<int32_t>(), N, cap, pairs);
+    if (((uintptr_t)pairs & 7u) == 0) {
+      // lanes per point: about four pairs each, from the mean upper row
+      const double mean = N > 0 ? (double)nup / (double)N : 0.0;
+      int L = 1;
+      while (L < 32 && (double)L * 4.0 < mean) L <<= 1;
+      const int g = nblocks(N * (int64_t)L, TPB);
+      int2* p2 = reinterpret_cast<int2*>(pairs);
+      const int64_t* rf = rs_full.as<int64_t>();
+      const int64_t* ru = rs_up.as<int64_t>();
+      const int32_t* nb = nbr.as<int32_t>();
+      const int32_t* og = orig.as<int32_t>();
+      switch (L) {
+        case 1: k_emit_pairs_l<1><<<g, TPB, 0, st>>>(rf, ru, nb, og, N, cap, p2); break;
+        case 2: k_emit_pairs_l<2><<<g, TPB, 0, st>>>(rf, ru, nb, og, N, cap, p2); break;
+        case 4: k_emit_pairs_l<4><<<g, TPB, 0, st>>>(rf, ru, nb, og, N, cap, p2); break;
+        case 8: k_emit_pairs_l<8><<<g, TPB, 0, st>>>(rf, ru, nb, og, N, cap, p2); break;
+        case 16: k_emit_pairs_l<16><<<g, TPB, 0, st>>>(rf, ru, nb, og, N, cap, p2); break;
+        default: k_emit_pairs_l<32><<<g, TPB, 0, st>>>(rf, ru, nb, og, N, cap, p2); break;
+      }
+    } else {
+      k_emit_pairs<<<nblocks(N, TPB), TPB, 0, st>>>(rs_full.as<int64_t>(), rs_up.as<int64_t>(), nbr.as<int32_t>(),
+                                                     orig.as<int32_t>(), N, cap, pairs);
+    }
     GC_LAUNCHED();
     if (fillzero && nup < cap)
       GC_CUDA(cudaMemsetAsync(pairs + 2 * nup, 0, sizeof(int32_t) * 2 * (size_t)(cap - nup), st));

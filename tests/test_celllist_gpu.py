@@ -147,6 +147,26 @@ def test_emit_reports_capacity_overflow(gpu_pkg):
     assert torch.equal(small, c.neighborlistview()[:10])
 
 
+def test_emit_into_a_buffer_not_8_byte_aligned(gpu_pkg):
+    """A caller's pair buffer that starts 4 bytes into an allocation: the
+    emit stores 4-byte words there instead of pair-wide ones; the contents
+    equal those of the aligned emit, capacity cut included."""
+    L = gpu_pkg.load_library()
+    x = np.random.default_rng(5).random((2, 20000))
+    c = gpu_pkg.GPUCellList(tuple(x), (0.02, 0.02), 0.02)
+    want = c.neighborlistview().clone()
+    n = C.c_int64()
+    for cap in (c.pairsn, c.pairsn // 3):
+        raw = torch.full((2 * c.pairsn + 2,), -7, dtype=torch.int32, device="cuda")
+        ptr = raw.data_ptr() + 4
+        assert ptr % 8 == 4
+        rc = L.gcl_emit_pairs(c._h, C.c_void_p(ptr), cap, 0, C.byref(n))
+        assert n.value == c.pairsn and (rc == 0) == (cap == c.pairsn)
+        got = raw[1:1 + 2 * cap].view(cap, 2)
+        assert torch.equal(got, want[:cap])
+        assert int(raw[0]) == -7 and int(raw[1 + 2 * cap]) == -7  # nothing written outside
+
+
 @pytest.mark.parametrize("D,N,dist", [(2, 200_000, 0.016), (3, 4_000_000, 0.008)])
 def test_full_size_pair_sets(gpu_pkg, orc, D, N, dist):
     """The cell-list configuration at full size: 200k 2-D / 4M 3-D uniform
