@@ -374,7 +374,7 @@ int CellCore::init(int D_, int64_t N_, const double* cellsize, double dist_, con
 
 void CellCore::release() {
   DevBuf* all[] = {&count, &cellstart, &key, &slot, &tmp, &perm, &skey, &orig, &cnt_full, &cnt_up, &rs_full,
-                   &rs_up, &nbr, &scratch, &pf[0], &pf[1], &pf[2], &pfmax, &orig_b, &stage};
+                   &rs_up, &nbr, &scratch, &pf[0], &pf[1], &pf[2], &pfmax, &pfthr, &orig_b, &stage};
   for (DevBuf* b : all) b->release();
   if (pin) cudaFreeHost(pin);
   pin = nullptr;
@@ -478,12 +478,22 @@ __device__ inline void pf_thresholds(const unsigned long long* bmax, double dist
   *thi = __double2float_ru(dist2 + band);
 }
 
+// the thresholds, once per build (they depend only on the bound and dist²;
+// the FP64 arithmetic here would otherwise run in every thread of the pass)
+template <int D>
+__global__ void k_pf_thresh(const unsigned long long* __restrict__ bmax, double dist2, float2* __restrict__ thr) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  float lo, hi;
+  pf_thresholds<D>(bmax, dist2, &lo, &hi);
+  *thr = make_float2(lo, hi);
+}
+
 // k_pairs with the FP32 prefilter; same output, same order
 template <int D, int MODE, int L>
 __global__ void __launch_bounds__(TPB) k_pairs32(const double* __restrict__ x0, const double* __restrict__ x1,
                                                  const double* __restrict__ x2, const float* __restrict__ f0,
                                                  const float* __restrict__ f1, const float* __restrict__ f2,
-                                                 const unsigned long long* __restrict__ bmax,
+                                                 const float2* __restrict__ thr,
                                                  const int32_t* __restrict__ skey,
                                                  const int32_t* __restrict__ cellstart, int64_t N, Grid g,
                                                  int32_t* __restrict__ cnt_full, int32_t* __restrict__ cnt_up,
@@ -509,8 +519,8 @@ __global__ void __launch_bounds__(TPB) k_pairs32(const double* __restrict__ x0, 
       return;
     }
   }
-  float tlo, thi;
-  pf_thresholds<D>(bmax, g.dist2, &tlo, &thi);
+  const float2 tt = *thr;
+  const float tlo = tt.x, thi = tt.y;
   const unsigned lanew = threadIdx.x & 31u;
   const unsigned gbase = lanew & ~(unsigned)(L - 1);
   const unsigned gm = L == 32 ? 0xffffffffu : (((1u << L) - 1u) << gbase);
@@ -656,6 +666,7 @@ int CellCore::ensure_pf() {
   int rc;
   for (int d = 0; d < D; ++d)
     if ((rc = pf[d].ensure(sizeof(float) * N, st))) return rc;
+  if ((rc = pfthr.ensure(sizeof(float2), st))) return rc;
   return pfmax.ensure(sizeof(unsigned long long), st, true);
 }
 
@@ -677,6 +688,12 @@ int CellCore::build_pairs(const double* const* xs, int* ovf_dev, bool scan_up, b
                                                      bm);
     GC_LAUNCHED();
   }
+  float2* thr = pfthr.as<float2>();
+  if (D == 2)
+    k_pf_thresh<2><<<1, 32, 0, st>>>(bm, g.dist2, thr);
+  else
+    k_pf_thresh<3><<<1, 32, 0, st>>>(bm, g.dist2, thr);
+  GC_LAUNCHED();
   // rows of up to S neighbours are staged by the count pass and copied by the fill
   const double mean = N > 0 && nfull_est > 0 ? (double)nfull_est / (double)N : 0.0;
   int S = 16;
@@ -685,11 +702,11 @@ int CellCore::build_pairs(const double* const* xs, int* ovf_dev, bool scan_up, b
   if (mean > 0 && (rc0 = stage.ensure(sizeof(int32_t) * (size_t)N * (size_t)S, st)) == GCSPH_OK) sp = stage.as<int32_t>();
   if (rc0) return rc0;
   if (sp)
-    PAIRS32_LAUNCH(2, L, xs[0], xs[1], x2, pf[0].as<float>(), pf[1].as<float>(), f2, bm, skey.as<int32_t>(),
+    PAIRS32_LAUNCH(2, L, xs[0], xs[1], x2, pf[0].as<float>(), pf[1].as<float>(), f2, thr, skey.as<int32_t>(),
                    cellstart.as<int32_t>(), N, g, cnt_full.as<int32_t>(), cnt_up.as<int32_t>(), nullptr, nullptr, 0,
                    nullptr, sp, S);
   else
-    PAIRS32_LAUNCH(0, L, xs[0], xs[1], x2, pf[0].as<float>(), pf[1].as<float>(), f2, bm, skey.as<int32_t>(),
+    PAIRS32_LAUNCH(0, L, xs[0], xs[1], x2, pf[0].as<float>(), pf[1].as<float>(), f2, thr, skey.as<int32_t>(),
                    cellstart.as<int32_t>(), N, g, cnt_full.as<int32_t>(), cnt_up.as<int32_t>(), nullptr, nullptr, 0,
                    nullptr, nullptr, 0);
   GC_LAUNCHED();
@@ -714,7 +731,7 @@ int CellCore::build_pairs(const double* const* xs, int* ovf_dev, bool scan_up, b
     if (nfull > nbr_cap && (rc = grow_nbr(nfull))) return rc;
   }
   timer_begin(T_PAIRS, st);
-  PAIRS32_LAUNCH(1, L, xs[0], xs[1], x2, pf[0].as<float>(), pf[1].as<float>(), f2, bm, skey.as<int32_t>(),
+  PAIRS32_LAUNCH(1, L, xs[0], xs[1], x2, pf[0].as<float>(), pf[1].as<float>(), f2, thr, skey.as<int32_t>(),
                  cellstart.as<int32_t>(), N, g, nullptr, nullptr, rs_full.as<int64_t>(), nbr.as<int32_t>(), nbr_cap,
                  ovf_dev, sp, S);
   GC_LAUNCHED();

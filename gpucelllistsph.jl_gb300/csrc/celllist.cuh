@@ -36,6 +36,7 @@ struct CellCore {
 
   DevBuf count, cellstart, key, slot, tmp, perm, skey, orig, orig_b, cnt_full, cnt_up, rs_full, rs_up, nbr, scratch;
   DevBuf pf[3], pfmax;  // FP32 (x - offset) copies for the prefilter, and max |x - offset|
+  DevBuf pfthr;         // the prefilter's two FP32 thresholds (float2), from pfmax once per build
   DevBuf stage;         // neighbour rows staged by the count pass (fixed stride), copied by the fill
   int64_t* pin = nullptr;  // pinned host scalars
   int64_t nfull = 0, nup = 0, nbr_cap = 0;
