@@ -1078,6 +1078,23 @@ __global__ void k_ens_disp(EnsArr A, const EnsInst* __restrict__ T, unsigned* __
     }
     bits = d2 == d2 ? __float_as_uint(d2) : 0x7f800000u;  // NaN: rebuild
   }
+  // the common case: the block's particles belong to one instance -- one
+  // atomic per block (per-warp atomics on a few hundred addresses contend)
+  __shared__ int s_first;
+  __shared__ unsigned s_wmax[32];
+  if (threadIdx.x == 0) s_first = s;
+  __syncthreads();
+  if (__syncthreads_and(s == s_first)) {
+    const unsigned m = __reduce_max_sync(0xffffffffu, bits);
+    if ((threadIdx.x & 31) == 0) s_wmax[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      unsigned b = 0u;
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) b = max(b, s_wmax[w]);
+      if (in && b != 0u) atomicMax(dmax + s, b);
+    }
+    return;
+  }
   const unsigned grp = __match_any_sync(0xffffffffu, s);
   const unsigned m = __reduce_max_sync(grp, bits);
   if (in && m != 0u && (threadIdx.x & 31) == __ffs(grp) - 1) atomicMax(dmax + s, m);
