@@ -98,7 +98,9 @@ class Clocks:
     def __init__(self, index):
         self.index = index
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_bench_{os.getpid()}.csv")
+        import tempfile
+        out = os.environ.get("GCSPH_CLOCKS_DIR") or tempfile.gettempdir()
+        self.path = os.path.join(out, f"clocks_bench_{os.getpid()}.csv")
 
     def __enter__(self):
         try:
