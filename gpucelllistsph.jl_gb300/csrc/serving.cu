@@ -19,6 +19,7 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <string>
 #include <thread>
 #include <vector>
 #include "gcsph_common.cuh"
@@ -51,6 +52,9 @@ struct gcsph_srv {
   gcsph_srv_backend be{};
   bool own = false;        // the library's backend
   void* stream = nullptr;
+  // the library's backend, no stream given: one stream per dimension, so the
+  // 2-D and 3-D ensembles' chunks run side by side
+  cudaStream_t dim_st[2] = {nullptr, nullptr};
   int32_t chunk = 64;
   double reserve = 0.1;
   uint32_t fields = 7;     // bit f: read back GCSPH_ENS field f at the horizon
@@ -70,7 +74,8 @@ int own_add(void* ctx, int32_t D, int32_t rid, int32_t* slot) {
   gcsph_srv* s = (gcsph_srv*)ctx;
   gcsph_ens*& e = ens_of(s, D);
   int rc;
-  if (!e && (rc = ens_create(D, s->stream, &e))) return rc;
+  void* st = s->dim_st[D == 3 ? 1 : 0] ? (void*)s->dim_st[D == 3 ? 1 : 0] : s->stream;
+  if (!e && (rc = ens_create(D, st, &e))) return rc;
   SrvReq& r = s->req[rid];
   rc = ens_add(e, r.n, r.x.data(), r.has_v ? r.v.data() : nullptr, r.rho.data(), r.ptype.data(), &r.prm, slot);
   if (rc) return rc;
@@ -159,16 +164,36 @@ int round(gcsph_srv* s, int* advanced) {
     r.admitted = now_of(s);
     r.remaining = r.steps;
   }
+  int64_t kd[2] = {s->chunk, s->chunk}, lived[2] = {0, 0};
+  for (const SrvReq& r : s->req)
+    if (r.state == RQ_RUNNING) {
+      const int di = r.D == 3 ? 1 : 0;
+      kd[di] = std::min(kd[di], r.remaining);
+      lived[di] += r.n;
+    }
+  int rcd[2] = {GCSPH_OK, GCSPH_OK};
+  if (s->dim_st[0] && s->dim_st[1] && lived[0] > 0 && lived[1] > 0) {
+    // both ensembles run: the 3-D chunk from a second host thread, on its own
+    // stream, while this thread runs the 2-D one (an error's message is
+    // carried back: the library keeps it per thread)
+    std::string msg3;
+    std::thread t([&] {
+      rcd[1] = s->be.step(s->be.ctx, 3, (int32_t)kd[1]);
+      if (rcd[1]) msg3 = gcsph_last_error();
+    });
+    rcd[0] = s->be.step(s->be.ctx, 2, (int32_t)kd[0]);
+    t.join();
+    if (rcd[0]) return rcd[0];
+    if (rcd[1]) return fail(rcd[1], "%s", msg3.c_str());
+  } else {
+    for (int di = 0; di < 2; ++di)
+      if (lived[di] > 0 && (rcd[di] = s->be.step(s->be.ctx, 2 + di, (int32_t)kd[di]))) return rcd[di];
+  }
   for (int32_t D = 2; D <= 3; ++D) {
-    int64_t k = s->chunk, live = 0;
-    for (const SrvReq& r : s->req)
-      if (r.state == RQ_RUNNING && r.D == D) {
-        k = std::min(k, r.remaining);
-        live += r.n;
-      }
+    const int di = D == 3 ? 1 : 0;
+    const int64_t k = kd[di], live = lived[di];
     if (live == 0) continue;
-    int rc = s->be.step(s->be.ctx, D, (int32_t)k);
-    if (rc) return rc;
+    int rc;
     *advanced = 1;
     s->particle_steps += k * live;
     for (size_t i = 0; i < s->req.size(); ++i) {
@@ -210,6 +235,12 @@ int srv_create(void* stream, int32_t chunk, double reserve, uint32_t fields, con
     s->be = *backend;
   } else {
     s->own = true;
+    if (!stream)
+      for (cudaStream_t& st : s->dim_st)
+        if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) {
+          cudaGetLastError();
+          st = nullptr;
+        }
     s->be.ctx = s;
     s->be.add = own_add;
     s->be.remove = own_remove;
@@ -227,6 +258,8 @@ void srv_destroy(gcsph_srv* s) {
   if (!s) return;
   for (gcsph_ens* e : s->ens)
     if (e) ens_destroy(e);
+  for (cudaStream_t st : s->dim_st)
+    if (st) cudaStreamDestroy(st);
   delete s;
 }
 
