@@ -374,7 +374,7 @@ int CellCore::init(int D_, int64_t N_, const double* cellsize, double dist_, con
 
 void CellCore::release() {
   DevBuf* all[] = {&count, &cellstart, &key, &slot, &tmp, &perm, &skey, &orig, &cnt_full, &cnt_up, &rs_full,
-                   &rs_up, &nbr, &scratch, &pf[0], &pf[1], &pf[2], &pfmax, &pfthr, &orig_b, &stage};
+                   &rs_up, &nbr, &scratch, &pf[0], &pf[1], &pf[2], &pfmax, &pfthr, &pfcnt, &orig_b, &stage};
   for (DevBuf* b : all) b->release();
   if (pin) cudaFreeHost(pin);
   pin = nullptr;
@@ -450,7 +450,8 @@ int CellCore::gather_positions_by_orig(const double* const* xorig, double* const
 template <int D>
 __global__ void k_make_pf(const double* __restrict__ x0, const double* __restrict__ x1,
                           const double* __restrict__ x2, int64_t N, Grid g, float* __restrict__ f0,
-                          float* __restrict__ f1, float* __restrict__ f2, unsigned long long* __restrict__ bmax) {
+                          float* __restrict__ f1, float* __restrict__ f2, unsigned long long* __restrict__ bmax,
+                          float2* __restrict__ thr, unsigned* __restrict__ cnt) {
   int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   double b = 0.0;
   if (k < N) {
@@ -466,27 +467,9 @@ __global__ void k_make_pf(const double* __restrict__ x0, const double* __restric
   }
   b = warp_max(b);
   if ((threadIdx.x & 31) == 0) atomic_max_pos(bmax, b);
+  pf_thresholds_last_block<D>(bmax, g.dist2, thr, cnt);
 }
 
-template <int D>
-__device__ inline void pf_thresholds(const unsigned long long* bmax, double dist2, float* tlo, float* thi) {
-  const double B = __longlong_as_double((long long)*bmax) * (1.0 + 0x1p-28);
-  const double e0 = B * 0x1p-22;
-  const double Tp = 1.5 * dist2;
-  const double band = 2.0 * e0 * sqrt((double)D * Tp) + (double)D * e0 * e0 + Tp * 0x1p-20;
-  *tlo = __double2float_rd(dist2 - band);
-  *thi = __double2float_ru(dist2 + band);
-}
-
-// the thresholds, once per build (they depend only on the bound and dist²;
-// the FP64 arithmetic here would otherwise run in every thread of the pass)
-template <int D>
-__global__ void k_pf_thresh(const unsigned long long* __restrict__ bmax, double dist2, float2* __restrict__ thr) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  float lo, hi;
-  pf_thresholds<D>(bmax, dist2, &lo, &hi);
-  *thr = make_float2(lo, hi);
-}
 
 // k_pairs with the FP32 prefilter; same output, same order
 template <int D, int MODE, int L>
@@ -667,6 +650,7 @@ int CellCore::ensure_pf() {
   for (int d = 0; d < D; ++d)
     if ((rc = pf[d].ensure(sizeof(float) * N, st))) return rc;
   if ((rc = pfthr.ensure(sizeof(float2), st))) return rc;
+  if ((rc = pfcnt.ensure(sizeof(unsigned), st, true))) return rc;
   return pfmax.ensure(sizeof(unsigned long long), st, true);
 }
 
@@ -679,21 +663,17 @@ int CellCore::build_pairs(const double* const* xs, int* ovf_dev, bool scan_up, b
   if ((rc0 = ensure_pf())) return rc0;
   float* f2 = D == 3 ? pf[2].as<float>() : pf[0].as<float>();
   unsigned long long* bm = pfmax.as<unsigned long long>();
+  float2* thr = pfthr.as<float2>();
   if (!pf_ready) {
+    // (the pass's last block turns the bound into the two thresholds)
     if (D == 2)
       k_make_pf<2><<<nblocks(N, TPB), TPB, 0, st>>>(xs[0], xs[1], x2, N, g, pf[0].as<float>(), pf[1].as<float>(), f2,
-                                                     bm);
+                                                     bm, thr, pfcnt.as<unsigned>());
     else
       k_make_pf<3><<<nblocks(N, TPB), TPB, 0, st>>>(xs[0], xs[1], x2, N, g, pf[0].as<float>(), pf[1].as<float>(), f2,
-                                                     bm);
+                                                     bm, thr, pfcnt.as<unsigned>());
     GC_LAUNCHED();
   }
-  float2* thr = pfthr.as<float2>();
-  if (D == 2)
-    k_pf_thresh<2><<<1, 32, 0, st>>>(bm, g.dist2, thr);
-  else
-    k_pf_thresh<3><<<1, 32, 0, st>>>(bm, g.dist2, thr);
-  GC_LAUNCHED();
   // rows of up to S neighbours are staged by the count pass and copied by the fill
   const double mean = N > 0 && nfull_est > 0 ? (double)nfull_est / (double)N : 0.0;
   int S = 16;

@@ -27,6 +27,37 @@ struct Grid {
   double dist2;
 };
 
+template <int D>
+__device__ inline void pf_thresholds_from(unsigned long long bits, double dist2, float* tlo, float* thi) {
+  const double B = __longlong_as_double((long long)bits) * (1.0 + 0x1p-28);
+  const double e0 = B * 0x1p-22;
+  const double Tp = 1.5 * dist2;
+  const double band = 2.0 * e0 * sqrt((double)D * Tp) + (double)D * e0 * e0 + Tp * 0x1p-20;
+  *tlo = __double2float_rd(dist2 - band);
+  *thi = __double2float_ru(dist2 + band);
+}
+
+// The pass that accumulates the bound (max |x - offset|, atomically, per
+// warp) ends with this, every thread of every block: the last block to
+// finish turns the bound into the two thresholds and resets the counter.
+template <int D>
+__device__ inline void pf_thresholds_last_block(unsigned long long* bmax, double dist2, float2* thr, unsigned* cnt) {
+  __shared__ int s_last;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    s_last = atomicAdd(cnt, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (s_last && threadIdx.x == 0) {
+    __threadfence();
+    float lo, hi;
+    pf_thresholds_from<D>(atomicAdd(bmax, 0ull), dist2, &lo, &hi);
+    *thr = make_float2(lo, hi);
+    *cnt = 0u;
+  }
+}
+
 struct CellCore {
   int D = 2;
   int64_t N = 0;
@@ -37,6 +68,7 @@ struct CellCore {
   DevBuf count, cellstart, key, slot, tmp, perm, skey, orig, orig_b, cnt_full, cnt_up, rs_full, rs_up, nbr, scratch;
   DevBuf pf[3], pfmax;  // FP32 (x - offset) copies for the prefilter, and max |x - offset|
   DevBuf pfthr;         // the prefilter's two FP32 thresholds (float2), from pfmax once per build
+  DevBuf pfcnt;         // blocks done of the pass that accumulates pfmax (its last block writes pfthr)
   DevBuf stage;         // neighbour rows staged by the count pass (fixed stride), copied by the fill
   int64_t* pin = nullptr;  // pinned host scalars
   int64_t nfull = 0, nup = 0, nbr_cap = 0;

@@ -164,6 +164,16 @@ __global__ void __launch_bounds__(STPB) k_pairB2(StepConst c, Scal* __restrict__
     double m = smax[0];
     for (int w = 1; w < STPB / 32; ++w) m = fmax(m, smax[w]);
     atomic_max_pos(&sc->maxcdx, m);
+    if (c.fold_end) {
+      // the last block to finish ends the step (k_step_end's work)
+      __threadfence();
+      if (atomicAdd(&sc->bdone, 1u) == gridDim.x - 1) {
+        __threadfence();
+        sc->maxcdx = atomicAdd(&sc->maxcdx, 0ull);  // every block's maximum, seen from here
+        step_end_body(c, sc);
+        sc->bdone = 0u;
+      }
+    }
   }
 }
 

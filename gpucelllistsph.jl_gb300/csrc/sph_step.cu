@@ -410,21 +410,7 @@ __global__ void __launch_bounds__(STPB) k_dt_reduce(StepConst c, Scal* __restric
 
 __global__ void k_step_end(StepConst c, Scal* __restrict__ sc) {
   if (threadIdx.x != 0 || blockIdx.x != 0 || sc->ovf) return;
-  double dt = sc->dt;
-  sc->etime = sc->etime + dt;  // prob.etime += prob.Δt, src/sphproblem.jl:331
-  // maximum(maximum.(abs, cΔx)) > 0.9 nui  =>  update! before the next step (:325-327)
-  const double mc = __longlong_as_double((long long)sc->maxcdx);
-  if (sc->maxcdx > sc->maxout) sc->maxout = sc->maxcdx;
-  if (c.count_reb && mc > c.reb_thr) sc->nreb += 1;
-  if (c.timestepping) {
-    double amax = __longlong_as_double((long long)sc->amax);
-    double vmax = __longlong_as_double((long long)sc->vmax);
-    double dt1 = sqrt(c.h / (3.0 * amax));
-    double dt2 = c.h / (c.c0 + vmax);
-    double nd = c.cfl * jl_min(dt1, dt2);
-    nd = jl_min(jl_max(nd, c.tmin), c.tmax);
-    sc->dt = nd;
-  }
+  step_end_body(c, sc);
 }
 
 // ---------------------------------------------------------------------------
@@ -535,6 +521,9 @@ struct PermOut {
   float* pf[3];
   unsigned long long* pfmax;
   double off[3];
+  float2* thr;     // and its two thresholds, from the last block
+  unsigned* cnt;
+  double dist2;
 };
 
 // new[k] = old[perm[k]] for the whole cell-order state; cΔx restarts at 0
@@ -554,26 +543,25 @@ __global__ void k_permute_state(StepConst c, int64_t N, const int32_t* __restric
       b = fmax(b, fabs(rel));
     }
     if (b != b) b = INFINITY;  // NaN coordinate: every candidate of the set goes to FP64
+    const int pt = S.pt[i];
+    O.pt[k] = pt;
+    const double r = S.rho[i];
+    O.rho[k] = r;
+    O.rhoh[k] = S.rhoh[i];
+    S.P1[k] = eos(r, c.gamma, c.rho0, c.P0, pt);
+    S.ir[k] = 1.0 / r;
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      O.xh[d][k] = S.xh[d][i];
+      O.v[d][k] = S.v[d][i];
+      O.vh[d][k] = S.vh[d][i];
+      O.buf2[d][k] = S.buf2[d][i];
+      S.cdx[d][k] = 0.0;
+    }
   }
   b = warp_max(b);
   if ((threadIdx.x & 31) == 0) atomic_max_pos(O.pfmax, b);
-  if (k >= N) return;
-  const int32_t i = perm[k];
-  const int pt = S.pt[i];
-  O.pt[k] = pt;
-  const double r = S.rho[i];
-  O.rho[k] = r;
-  O.rhoh[k] = S.rhoh[i];
-  S.P1[k] = eos(r, c.gamma, c.rho0, c.P0, pt);
-  S.ir[k] = 1.0 / r;
-#pragma unroll
-  for (int d = 0; d < D; ++d) {
-    O.xh[d][k] = S.xh[d][i];
-    O.v[d][k] = S.v[d][i];
-    O.vh[d][k] = S.vh[d][i];
-    O.buf2[d][k] = S.buf2[d][i];
-    S.cdx[d][k] = 0.0;
-  }
+  pf_thresholds_last_block<D>(O.pfmax, O.dist2, O.thr, O.cnt);
 }
 
 template <int D>
@@ -862,6 +850,9 @@ static int rebuild(sph_handle* h, const StepConst& c, int* ovf_dev) {
       alt.off[d] = core.g.offset[d];
     }
     alt.pfmax = core.pfmax.as<unsigned long long>();
+    alt.thr = core.pfthr.as<float2>();
+    alt.cnt = core.pfcnt.as<unsigned>();
+    alt.dist2 = core.g.dist2;
     timer_begin(T_STATE, core.st);
     k_permute_state<D><<<nblocks(h->N, 256), 256, 0, core.st>>>(c, h->N, core.perm.as<int32_t>(), make_arr<D>(h),
                                                                alt);
@@ -972,6 +963,7 @@ static int enqueue_stages(sph_handle* h, StepConst& c, Scal* dsc, int32_t& cspmc
   c.fb_eta2 = 0.01 * (c.fb_r0 * c.fb_r0);
   const int L = choose_lanes(h);
   const bool once = L > 1;  // pair-once passes; L = 1 keeps the serial gather (bit-identical to the oracle)
+  bool folded = false;  // k_step_end's work done by pass B2's last block
   // stage 1 (predictor) and stage 2 (corrector); the pair-once form times
   // pass A as the stage and the two row-sum passes together
   if (once) {
@@ -995,7 +987,12 @@ static int enqueue_stages(sph_handle* h, StepConst& c, Scal* dsc, int32_t& cspmc
     PAIRA_LAUNCH(2, c, make_arr<D>(h), make_pairbuf<D>(h));
     timer_end(T_STAGE2, st);
     timer_begin(T_ROWSUM, st);
-    PAIRB_LAUNCH(2, L, c, dsc, make_arr<D>(h), make_pairbuf<D>(h));
+    // without Δt_stepping nothing after pass B2 feeds the step's end: its
+    // last block does k_step_end's work
+    StepConst c2 = c;
+    c2.fold_end = c.timestepping ? 0 : 1;
+    PAIRB_LAUNCH(2, L, c2, dsc, make_arr<D>(h), make_pairbuf<D>(h));
+    folded = c2.fold_end != 0;
     timer_end(T_ROWSUM, st);
   } else {
     timer_begin(T_STAGE2, st);
@@ -1035,8 +1032,10 @@ static int enqueue_stages(sph_handle* h, StepConst& c, Scal* dsc, int32_t& cspmc
     GC_LAUNCHED();
     timer_end(T_DT, st);
   }
-  k_step_end<<<1, 32, 0, st>>>(c, dsc);
-  GC_LAUNCHED();
+  if (!folded) {
+    k_step_end<<<1, 32, 0, st>>>(c, dsc);
+    GC_LAUNCHED();
+  }
   return GCSPH_OK;
 }
 
@@ -1046,7 +1045,7 @@ static void init_scal(sph_handle* h, int32_t n) {
   h->pin->etime = h->prm.etime;
   h->pin->maxcdx = h->pin->amax = h->pin->vmax = 0;
   h->pin->ovf = 0;
-  h->pin->pad0 = 0;
+  h->pin->bdone = 0;
   h->pin->maxout = 0;
   h->pin->nreb = n > 0 ? 1 : 0;  // the first step always runs update!
 }

@@ -20,6 +20,7 @@ struct StepConst {
   double cfl, dt_eta2;          // Δt_stepping
   double tmin, tmax;
   int gamma, use_visc, use_pF, timestepping;
+  int fold_end;    // pass B2's last block does k_step_end's work (no Δt_stepping in this call)
   double reb_thr;  // update! is due after a step whose max |cΔx| passes this (0.9 (dist - H))
   int dt_relative; // Δt_stepping's velocity term from pair-relative Δv·Δx instead of absolute v·x
   int count_reb;   // this step's decision counts toward the call's update! total
@@ -33,7 +34,7 @@ struct Scal {
   unsigned long long amax;    // bits of max |a|
   unsigned long long vmax;    // bits of max |h v.x/(x.x+η²)|
   int ovf;                    // the neighbour CSR outgrew its buffers: this step's kernels skip
-  int pad0;
+  unsigned bdone;             // blocks of pass B2 done this step (k_step_end's work in its last block)
   unsigned long long maxout;  // bits of the largest max |cΔx| of the call (stepsolve!'s second result)
   long long nreb;             // update! calls of the call (stepsolve!'s first result)
 };
@@ -81,6 +82,26 @@ __device__ inline double dotD(const double* a, const double* b) {
 // Julia min/max propagate NaN (fmin/fmax do not)
 __device__ inline double jl_min(double a, double b) { return (a != a || b != b) ? (a + b) : fmin(a, b); }
 __device__ inline double jl_max(double a, double b) { return (a != a || b != b) ? (a + b) : fmax(a, b); }
+
+// the end of a step, one thread: etime += Δt (src/sphproblem.jl:331), the
+// update! decision from max |cΔx| (:325-327), the call's largest max |cΔx|,
+// and with Δt_stepping the next Δt from the step's maxima
+__device__ inline void step_end_body(const StepConst& c, Scal* sc) {
+  const double dt = sc->dt;
+  sc->etime = sc->etime + dt;
+  const double mc = __longlong_as_double((long long)sc->maxcdx);
+  if (sc->maxcdx > sc->maxout) sc->maxout = sc->maxcdx;
+  if (c.count_reb && mc > c.reb_thr) sc->nreb += 1;
+  if (c.timestepping) {
+    const double amax = __longlong_as_double((long long)sc->amax);
+    const double vmax = __longlong_as_double((long long)sc->vmax);
+    const double dt1 = sqrt(c.h / (3.0 * amax));
+    const double dt2 = c.h / (c.c0 + vmax);
+    double nd = c.cfl * jl_min(dt1, dt2);
+    nd = jl_min(jl_max(nd, c.tmin), c.tmax);
+    sc->dt = nd;
+  }
+}
 
 // ∂ρ∂tDDT! pair value seen from particle k (src/gpukernels_sph.jl:579-625)
 template <int D>
