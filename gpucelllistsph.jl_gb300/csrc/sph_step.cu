@@ -1223,13 +1223,11 @@ static int graph_capture(sph_handle* h, StepConst c, int32_t n, StepGraph& g) {
   timer_capture_to(&g.timers);
   int rc = GCSPH_OK;
   int32_t cspmcnt = 0;
+  // the step's maxima start at zero (the call's scalars are uploaded before
+  // each replay) and each step's end clears them for the next; the overflow
+  // flag stays set once raised
+  c.reset_max = 1;
   for (int32_t it = 0; it < n && rc == GCSPH_OK; ++it) {
-    // per-step maxima; the overflow flag stays set once raised
-    cudaError_t e = cudaMemsetAsync(&dsc->maxcdx, 0, 3 * sizeof(unsigned long long), st);
-    if (e != cudaSuccess) {
-      rc = cuda_fail(e, "cudaMemsetAsync", __FILE__, __LINE__);
-      break;
-    }
     c.count_reb = it + 1 < n;
     if ((rc = rebuild<D>(h, c, &dsc->ovf))) break;
     rc = enqueue_stages<D>(h, c, dsc, cspmcnt);

@@ -21,6 +21,7 @@ struct StepConst {
   double tmin, tmax;
   int gamma, use_visc, use_pF, timestepping;
   int fold_end;    // pass B2's last block does k_step_end's work (no Δt_stepping in this call)
+  int reset_max;   // the step's end clears the step's maxima for the next (captured calls: no memset node)
   double reb_thr;  // update! is due after a step whose max |cΔx| passes this (0.9 (dist - H))
   int dt_relative; // Δt_stepping's velocity term from pair-relative Δv·Δx instead of absolute v·x
   int count_reb;   // this step's decision counts toward the call's update! total
@@ -100,6 +101,11 @@ __device__ inline void step_end_body(const StepConst& c, Scal* sc) {
     double nd = c.cfl * jl_min(dt1, dt2);
     nd = jl_min(jl_max(nd, c.tmin), c.tmax);
     sc->dt = nd;
+  }
+  if (c.reset_max) {
+    sc->maxcdx = 0ull;
+    sc->amax = 0ull;
+    sc->vmax = 0ull;
   }
 }
 
