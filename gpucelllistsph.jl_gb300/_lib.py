@@ -113,6 +113,8 @@ _SIGS = {
     "ens_set_skin": (C.c_int, [vp, C.c_double]),
     "ens_get_skin": (C.c_int, [vp, C.POINTER(C.c_double)]),
     "ens_list_builds": (C.c_int, [vp, i32, C.POINTER(i64)]),
+    "ens_set_dpc_bound": (C.c_int, [vp, i32]),
+    "ens_get_dpc_bound": (C.c_int, [vp, C.POINTER(i32)]),
     "ens_get_list_build": (C.c_int, [vp, C.POINTER(i32), C.POINTER(i32), C.POINTER(i32), C.POINTER(i32)]),
     "srv_create": (C.c_int, [vp, i32, f64, C.c_uint32, C.POINTER(gcsph_srv_backend), C.POINTER(vp)]),
     "srv_destroy": (None, [vp]),

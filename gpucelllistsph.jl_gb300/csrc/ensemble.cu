@@ -57,6 +57,8 @@ struct EnsInst {
   int reuse;                             // the list is kept while the particles stay within the skin
   float LR2;                             // list radius², (H (1 + skin))² = cell edge²
   float dthr2;                           // rebuild when a particle has moved more than about skin/2 (squared)
+  float dpc_skip;                        // dpcreg! skips a row whose separations after the step stay above
+                                         // this (l0 with a margin for FP32 rounding)
 };
 
 struct EnsArr {
@@ -97,6 +99,11 @@ struct EnsArr {
   const int32_t* istep;      // steps done per instance (cspmcorr! schedule)
   const int* rb;             // per instance: this step rebuilds the instance's cells and list
   float* ob[3];              // offsets at the instance's last list build (same cell corner as off)
+  // dpcreg!'s row bound (null: every row is scanned): the smallest r² of each
+  // row at the step's start (stage 1) and, per instance, the largest |Δx|² of
+  // the step (after the corrector)
+  float* rmin2;
+  const unsigned* sdmax;
 };
 
 // record layouts (D = 2 | D = 3); P = the EOS of the record's density, where
@@ -664,8 +671,10 @@ __device__ __forceinline__ float lane_total(const KSum& k, unsigned gm) {
   return s - c;
 }
 
-// two blocks of 512 per SM: at most 64 registers
-template <int D, int STAGE>
+// two blocks of 512 per SM: at most 64 registers.  RM (stage 1): keep each
+// row's smallest r² for dpcreg!'s row bound (a separate instantiation, so the
+// ensembles without dpcreg! run the loop without it)
+template <int D, int STAGE, bool RM = false>
 __global__ void __launch_bounds__(ENS_MAX_TPB, 2) k_ens_stage(EnsArr A, const EnsInst* __restrict__ T) {
   if (*A.ovf) return;
   constexpr int L = stage_lanes<D>();
@@ -690,6 +699,7 @@ __global__ void __launch_bounds__(ENS_MAX_TPB, 2) k_ens_stage(EnsArr A, const En
     const float Pi = eos32(dri, pti, I);
     const int fbs = STAGE - 1;
     KSum drho, acc[D];
+    float rm2 = INFINITY;  // stage 1: the row's smallest r² (dpcreg!'s row bound)
     const int nn = A.nlc[i];
     // the next entry is loaded one iteration ahead: the list streams from
     // DRAM, and its latency then overlaps the current neighbour's arithmetic
@@ -708,6 +718,7 @@ __global__ void __launch_bounds__(ENS_MAX_TPB, 2) k_ens_stage(EnsArr A, const En
 #pragma unroll
       for (int q = 0; q < D; ++q) d[q] = (oi[q] - oj[q]) - (q == 0 ? shx : (q == 1 ? shy : shz));
       const float r2 = dot32<D>(d, d);
+      if (STAGE == 1 && RM) rm2 = fminf(rm2, r2);
       if (!(r2 < I.H2)) continue;  // in the list's skin: not a pair of this step
       // sph∇W!: W'(r)/r of WendlandC2 = -20 nDW Hinv (1-q)^3.  Reciprocals and
       // roots here are the approximate intrinsics (within 2 ulp each), far
@@ -790,7 +801,12 @@ __global__ void __launch_bounds__(ENS_MAX_TPB, 2) k_ens_stage(EnsArr A, const En
 #pragma unroll
     for (int q = 0; q < D; ++q) a[q] = lane_total<L>(acc[q], gm) - (q == 1 ? I.g : 0.f);
     const float drho_s = lane_total<L>(drho, gm);
+    if (STAGE == 1 && RM) {
+#pragma unroll
+      for (int o = L / 2; o > 0; o >>= 1) rm2 = fminf(rm2, __shfl_xor_sync(gm, rm2, o));
+    }
     if (lane != 0) continue;
+    if (STAGE == 1 && RM) A.rmin2[i] = rm2;
     const float dt = (float)I.dt;
     if (STAGE == 1) {
       // update_ρp∂ρ∂tΔt!, update_vp∂v∂tΔt!, update_xpvΔt! at Δt/2
@@ -858,10 +874,25 @@ __global__ void __launch_bounds__(ENS_MAX_TPB) k_ens_dpc(EnsArr A, const EnsInst
         ni[d] = A.offn[d][i];
         vi[d] = A.v[d][i];
       }
+      // the row bound: a pair is within l0 after the step only if its
+      // separation at the step's start, less both particles' moves, is; the
+      // row's smallest separation, its own move and the instance's largest
+      // move clear l0 for every entry, so every term would be skipped below
+      bool scan = true;
+      if (A.rmin2) {
+        float di2 = 0.f;
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+          const float dd = ni[d] - A.off[d][i];
+          di2 = fmaf(dd, dd, di2);
+        }
+        const float lo = sqrtf(A.rmin2[i]) - sqrtf(di2) - sqrtf(__uint_as_float(A.sdmax[A.inst[i]]));
+        scan = !(lo >= I.dpc_skip);
+      }
       const float dri = A.dr[i];
       const float rhoi = I.rho0 + dri, Pi = eos32(dri, pti, I);
       const float dt = (float)I.dt;
-      const int nn = A.nlc[i];
+      const int nn = scan ? A.nlc[i] : 0;
       int nxt = nn > 0 ? A.nl[i] : 0;  // entries one iteration ahead (as in the stage passes)
       for (int e = 0; e < nn; ++e) {
         const int ent = nxt;
@@ -1062,18 +1093,20 @@ __global__ void k_ens_cspm_apply(int64_t N, const int32_t* __restrict__ inst, co
 // the largest squared displacement since the last list build, per instance
 // (particles are sorted by instance: a warp's lanes of one instance reduce
 // together, one atomic per instance per warp)
-template <int D>
+// STEP: the largest move of the step (x_{n+1} - x_n, after the corrector) of
+// the instances with dpcreg!, for its row bound; NaN gives +inf (no row skips)
+template <int D, bool STEP>
 __global__ void k_ens_disp(EnsArr A, const EnsInst* __restrict__ T, unsigned* __restrict__ dmax) {
   if (*A.ovf) return;
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const bool in = i < A.N;
   const int s = in ? A.inst[i] : -1;
   unsigned bits = 0u;
-  if (in && T[s].reuse) {
+  if (in && (STEP ? T[s].use_dpc : T[s].reuse)) {
     float d2 = 0.f;
 #pragma unroll
     for (int q = 0; q < D; ++q) {
-      const float dd = A.offn[q][i] - A.ob[q][i];
+      const float dd = A.offn[q][i] - (STEP ? A.off[q][i] : A.ob[q][i]);
       d2 = fmaf(dd, dd, d2);
     }
     bits = d2 == d2 ? __float_as_uint(d2) : 0x7f800000u;  // NaN: rebuild
@@ -1104,7 +1137,7 @@ __global__ void k_ens_disp(EnsArr A, const EnsInst* __restrict__ T, unsigned* __
 // rebuilds its list at the next step (always without a skin)
 __global__ void k_ens_tick(int ninst, int32_t* __restrict__ istep, const int* __restrict__ ovf,
                            int* __restrict__ done, const EnsInst* __restrict__ T, int* __restrict__ rb,
-                           int* __restrict__ nreb, unsigned* __restrict__ dmax) {
+                           int* __restrict__ nreb, unsigned* __restrict__ dmax, unsigned* __restrict__ sdmax) {
   if (*ovf) return;
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s < ninst) {
@@ -1112,6 +1145,7 @@ __global__ void k_ens_tick(int ninst, int32_t* __restrict__ istep, const int* __
     if (rb[s]) nreb[s] += 1;
     rb[s] = T[s].reuse ? (__uint_as_float(dmax[s]) > T[s].dthr2 ? 1 : 0) : 1;
     dmax[s] = 0u;
+    sdmax[s] = 0u;
   }
   if (s == 0) *done += 1;
 }
@@ -1212,7 +1246,7 @@ struct EnsHostInst {
 
 struct EnsGraph {
   int64_t n_steps = -1, N = -1, K = -1, gen = -1;
-  int cur = -1, tpb = 0, timing = 0, nl_lanes = 0, nl_cpb = -1, nl_depth = 0, nl_cap = 0;
+  int cur = -1, tpb = 0, timing = 0, nl_lanes = 0, nl_cpb = -1, nl_depth = 0, nl_cap = 0, dpc_bound = -1;
   cudaGraphExec_t exec = nullptr;
   unsigned long long used = 0;
   long long launches = 0;
@@ -1239,6 +1273,9 @@ struct gcsph_ens {
   DevBuf R3, R4;         // packed neighbour records of the correction passes
   DevBuf OB[3];          // offsets at each instance's last list build
   DevBuf RB, NREB, DMAX; // per instance: rebuild at the next step, list builds, largest displacement²
+  DevBuf SDMAX;          // per instance: largest |Δx|² of the step (dpcreg!'s row bound)
+  DevBuf RMIN;           // per particle: smallest r² of the row at the step's start (dpcreg!'s row bound)
+  bool dpc_bound = true; // dpcreg! skips the rows the bound clears (the results are the same)
   double skin = 0.05;    // list radius H (1 + skin); 0: every step rebuilds
   bool lists_lost = false;  // the list buffer was dropped: every instance rebuilds
   int nls = 0;           // list entries per particle (grows on overflow)
@@ -1336,6 +1373,8 @@ EnsArr ens_arr(gcsph_ens* e) {
   A.r4 = (e->any_dpc || e->any_xsph || e->any_cspm) ? e->R4.as<float4>() : nullptr;
   A.istep = e->ISTEP.as<int32_t>();
   for (int d = 0; d < 3; ++d) A.ob[d] = e->OB[d < e->D ? d : 0].as<float>();
+  A.rmin2 = (e->any_dpc && e->dpc_bound) ? e->RMIN.as<float>() : nullptr;
+  A.sdmax = e->SDMAX.as<unsigned>();
   return A;
 }
 
@@ -1405,6 +1444,7 @@ int ens_reserve(gcsph_ens* e, int64_t n) {
     if ((rc = e->OFFN[d].ensure(sizeof(float) * want, e->st))) return rc;
   }
   if ((rc = e->DRH.ensure(sizeof(float) * want, e->st))) return rc;
+  if ((rc = e->RMIN.ensure(sizeof(float) * want, e->st))) return rc;
   if ((rc = e->R1.ensure(sizeof(float4) * 2 * want, e->st))) return rc;
   if ((rc = e->R2.ensure(sizeof(float4) * (e->D == 2 ? 2 : 3) * want, e->st))) return rc;
   if ((rc = e->R3.ensure(sizeof(float4) * 2 * want, e->st))) return rc;
@@ -1541,9 +1581,11 @@ int ens_relayout(gcsph_ens* e) {
     if ((rc = e->RB.ensure(sizeof(int32_t) * ni, e->st))) return rc;
     if ((rc = e->NREB.ensure(sizeof(int32_t) * ni, e->st))) return rc;
     if ((rc = e->DMAX.ensure(sizeof(unsigned) * ni, e->st, true))) return rc;
+    if ((rc = e->SDMAX.ensure(sizeof(unsigned) * ni, e->st, true))) return rc;
     GC_CUDA(cudaMemcpyAsync(e->RB.p, rb.data(), sizeof(int32_t) * ni, cudaMemcpyHostToDevice, e->st));
     GC_CUDA(cudaMemcpyAsync(e->NREB.p, nreb.data(), sizeof(int32_t) * ni, cudaMemcpyHostToDevice, e->st));
     GC_CUDA(cudaMemsetAsync(e->DMAX.p, 0, sizeof(unsigned) * ni, e->st));
+    GC_CUDA(cudaMemsetAsync(e->SDMAX.p, 0, sizeof(unsigned) * ni, e->st));
     GC_CUDA(cudaStreamSynchronize(e->st));
   }
   std::vector<int32_t> isteps(e->inst.size());
@@ -1681,7 +1723,10 @@ int ens_enqueue_step(gcsph_ens* e, cudaStream_t st, int tpb) {
   const int64_t swant = (N * stage_lanes<D>() + tpb - 1) / tpb;
   const int sgrid = (int)std::max<int64_t>(1, std::min<int64_t>(swant, (int64_t)e->sms * e->occ[t]));
   timer_begin(T_STAGE1, st);
-  k_ens_stage<D, 1><<<sgrid, tpb, 0, st>>>(A, T);
+  if (A.rmin2)
+    k_ens_stage<D, 1, true><<<sgrid, tpb, 0, st>>>(A, T);
+  else
+    k_ens_stage<D, 1, false><<<sgrid, tpb, 0, st>>>(A, T);
   GC_LAUNCHED();
   timer_end(T_STAGE1, st);
   timer_begin(T_STAGE2, st);
@@ -1691,6 +1736,10 @@ int ens_enqueue_step(gcsph_ens* e, cudaStream_t st, int tpb) {
   const int32_t ninst = (int32_t)e->inst.size();
   if (e->any_dpc) {
     timer_begin(T_DPC, st);
+    if (A.rmin2) {
+      k_ens_disp<D, true><<<nblocks(N, 256), 256, 0, st>>>(A, T, e->SDMAX.as<unsigned>());
+      GC_LAUNCHED();
+    }
     k_ens_dpc<D><<<grid, tpb, 0, st>>>(A, T);
     GC_LAUNCHED();
     k_ens_dpc_apply<D><<<nblocks(N, 256), 256, 0, st>>>(A, T);
@@ -1712,11 +1761,12 @@ int ens_enqueue_step(gcsph_ens* e, cudaStream_t st, int tpb) {
     GC_LAUNCHED();
     timer_end(T_CSPM, st);
   }
-  k_ens_disp<D><<<nblocks(N, 256), 256, 0, st>>>(A, T, e->DMAX.as<unsigned>());
+  k_ens_disp<D, false><<<nblocks(N, 256), 256, 0, st>>>(A, T, e->DMAX.as<unsigned>());
   GC_LAUNCHED();
   k_ens_tick<<<nblocks(std::max(ninst, 1), 128), 128, 0, st>>>(ninst, e->ISTEP.as<int32_t>(), A.ovf,
                                                                   A.ovf + 2, T, e->RB.as<int>(),
-                                                                  e->NREB.as<int>(), e->DMAX.as<unsigned>());
+                                                                  e->NREB.as<int>(), e->DMAX.as<unsigned>(),
+                                                                  e->SDMAX.as<unsigned>());
   GC_LAUNCHED();
   return GCSPH_OK;
 }
@@ -1827,7 +1877,7 @@ int ens_run_graph(gcsph_ens* e, int32_t n) {
   for (EnsGraph& c : e->graphs)
     if (c.exec && c.n_steps == n && c.N == e->N && c.K == e->K && c.gen == e->gen && c.cur == e->cur &&
         c.tpb == e->tpb && c.timing == timing && c.nl_lanes == e->nl_lanes && c.nl_cpb == e->nl_cpb &&
-        c.nl_depth == e->nl_depth && c.nl_cap == e->nl_cap_fix)
+        c.nl_depth == e->nl_depth && c.nl_cap == e->nl_cap_fix && c.dpc_bound == (int)e->dpc_bound)
       g = &c;
   if (!g) {
     g = &e->graphs[0];
@@ -1864,6 +1914,7 @@ int ens_run_graph(gcsph_ens* e, int32_t n) {
     g->nl_cpb = e->nl_cpb;
     g->nl_depth = e->nl_depth;
     g->nl_cap = e->nl_cap_fix;
+    g->dpc_bound = (int)e->dpc_bound;
     g->n_steps = n;
     g->N = e->N;
     g->K = e->K;
@@ -1968,7 +2019,8 @@ int ens_bytes_per_particle(int32_t D, int64_t* bytes) {
   *bytes = 2 * D * (8 + 4 + 8) + 2 * 16 + 6 * 4 + D * 16 + 4 + 8 + (D == 2 ? 64 : 256) * 4 + 4 +
            16 * (D == 2 ? 4 : 5) +  // packed records of the stages
            64 +                     // and of the correction passes
-           D * 4;                   // offsets at the last list build
+           D * 4 +                  // offsets at the last list build
+           4;                       // the row's smallest r² (dpcreg!'s row bound)
   return GCSPH_OK;
 }
 
@@ -2054,6 +2106,9 @@ int ens_add(gcsph_ens* e, int64_t n, const double* x, const double* v, const dou
     I.dpc_pmin = (float)p->dpc_pmin;
     I.dpc_pmax = (float)p->dpc_pmax;
     I.dpc_lambda = (float)p->dpc_lambda;
+    // the bound's margin: 1e-3 l0, and 1e-5 cell edges for the FP32 offsets
+    // (their rounding is a few 1e-7 cell edges)
+    I.dpc_skip = (float)(p->dpc_l0 * (1.0 + 1e-3) + 1e-5 * I.cs);
   }
   I.use_xsph = p->xsph_eps > 0;
   I.xsph_c = (float)(2.0 * p->m0 * p->xsph_eps);
@@ -2302,6 +2357,18 @@ int ens_set_skin(gcsph_ens* e, double skin) {
 int ens_get_skin(gcsph_ens* e, double* skin) {
   if (!e || !skin) return fail(GCSPH_EINVAL, "null argument");
   *skin = e->skin;
+  return GCSPH_OK;
+}
+
+int ens_set_dpc_bound(gcsph_ens* e, int32_t on) {
+  if (!e) return fail(GCSPH_EINVAL, "null handle");
+  e->dpc_bound = on != 0;
+  return GCSPH_OK;
+}
+
+int ens_get_dpc_bound(gcsph_ens* e, int32_t* on) {
+  if (!e || !on) return fail(GCSPH_EINVAL, "null argument");
+  *on = e->dpc_bound ? 1 : 0;
   return GCSPH_OK;
 }
 

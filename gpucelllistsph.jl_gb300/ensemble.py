@@ -187,6 +187,16 @@ class Ensemble:
         _lib.check(_lib.load().ens_list_builds(self._h, int(slot), C.byref(v)))
         return int(v.value)
 
+    def set_dpc_bound(self, on: bool):
+        """dpcreg!'s row bound: skip the rows that can hold no pair within l0
+        after the step (on by default).  Results are the same either way."""
+        _lib.check(_lib.load().ens_set_dpc_bound(self._h, 1 if on else 0))
+
+    def dpc_bound(self) -> bool:
+        v = C.c_int32()
+        _lib.check(_lib.load().ens_get_dpc_bound(self._h, C.byref(v)))
+        return bool(v.value)
+
     def set_list_stride(self, nls: int):
         _lib.check(_lib.load().ens_set_list_stride(self._h, int(nls)))
 

@@ -338,6 +338,14 @@ int ens_set_skin(gcsph_ens* e, double skin);
 int ens_get_skin(gcsph_ens* e, double* skin);
 /* list builds of one instance so far */
 int ens_list_builds(gcsph_ens* e, int32_t slot, int64_t* builds);
+/* dpcreg!'s row bound (on by default; no counterpart in the reference, whose
+ * dpcreg!, src/gpukernels_sph.jl:1500-1553, evaluates every pair): a row whose
+ * smallest separation at the step's start, less the particle's move and the
+ * largest move in its instance, clears l0 has no pair within l0 after the
+ * step, and its scan is skipped.  Results are the same with the bound on and
+ * off; off scans every row. */
+int ens_set_dpc_bound(gcsph_ens* e, int32_t on);
+int ens_get_dpc_bound(gcsph_ens* e, int32_t* on);
 int ens_get_list_build(gcsph_ens* e, int32_t* lanes, int32_t* cells_per_block, int32_t* depth, int32_t* cap);
 /* Entries per particle in the step's neighbour list (default 64 in 2-D, 256
  * in 3-D; it grows by itself when a row outgrows it, repeating the steps

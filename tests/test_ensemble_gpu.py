@@ -115,6 +115,51 @@ def test_fp32_full_physics_against_fp64(gpu_pkg, orc, D):
     assert err["rho"] <= TOL and err["v"] <= TOL and err["disp"] <= TOL, err
 
 
+def _min_sep(x, rows):
+    """Smallest distance from each particle in `rows` to another (brute force)."""
+    idx = np.flatnonzero(rows)
+    d2 = ((x[:, idx, None] - x[:, None, :]) ** 2).sum(axis=0)
+    d2[np.arange(idx.size), idx] = np.inf
+    return np.sqrt(d2.min(axis=1))
+
+
+@pytest.mark.parametrize("D", [2, 3])
+def test_dpc_row_bound_changes_nothing(gpu_pkg, D):
+    """dpcreg!'s row bound skips only rows with no pair within l0 after the
+    step.  Fluid jittered by up to 0.25 dx with l0 = 0.7 dx gives rows with
+    pairs within l0 and rows without; every field is bit-identical with the
+    bound on and off, and DPC does move the particles (l0 = 0 differs)."""
+    w = gpu_pkg.workloads
+    if D == 2:
+        case = w.dam_break_2d(dx=0.04, fluid=(0.6, 0.8), tank=(1.2, 1.0))
+        n = 40
+    else:
+        case = w.dam_break_3d(dx=0.05, fluid=(0.3, 0.4, 0.2), tank=(0.6, 0.6, 0.3))
+        n = 30
+    rng = np.random.default_rng(5)
+    fl = case.ptype > 1
+    case.x = case.x.copy()
+    case.x[:, fl] += rng.uniform(-0.25 * case.dx, 0.25 * case.dx, (D, int(fl.sum())))
+    l0 = 0.7 * case.dx
+    near = _min_sep(case.x, fl) < l0  # about a quarter of the fluid rows at the start
+    assert 0.05 < near.mean() < 0.9, near.mean()
+    runs = {}
+    for name, bound, dpc in (("on", True, l0), ("off", False, l0), ("nodpc", True, 0.0)):
+        spec = gpu_pkg.spec_from_case(case)
+        spec.v = _moving(case)
+        spec.dpc_l0, spec.dpc_lambda, spec.dpc_pmax = dpc, 0.005, 36000.0
+        ens = gpu_pkg.Ensemble(D)
+        ens.set_dpc_bound(bound)
+        assert ens.dpc_bound() == bound
+        slot = ens.add(spec)
+        ens.step(n)
+        runs[name] = {f: ens.get(slot, f) for f in FIELDS}
+        ens.close()
+    for f in FIELDS:
+        assert np.array_equal(runs["on"][f], runs["off"][f]), f
+    assert not np.array_equal(runs["on"]["x"], runs["nodpc"]["x"])
+
+
 def _specs(pkg):
     w = pkg.workloads
     a = pkg.spec_from_case(w.dam_break_2d(dx=0.04, fluid=(0.6, 0.8), tank=(1.2, 1.0)))
