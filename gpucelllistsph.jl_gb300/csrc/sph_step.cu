@@ -254,11 +254,14 @@ __global__ void __launch_bounds__(STPB) k_dpc(StepConst c, const Scal* __restric
 #pragma unroll
       for (int d = 0; d < D; ++d) dx[d] = xk[d] - S.x[d][m];
       const double r2 = dotD<D>(dx, dx);
-      const double r = sqrt(r2);
-      const double u = r * c.dpc_l0inv;
       // u >= 1: W = 0, so χ = 0, the factor (u >= dpckernlim) is χ and Pᵇ = 0 --
       // the pair adds an exact zero to either branch's sum, which it leaves as
-      // it is (up to the sign of a zero sum): skip it
+      // it is (up to the sign of a zero sum): skip it.  Past l0² (1 + 1e-6)
+      // the rounded u is >= 1 for certain, so most pairs skip before the root
+      // (an FP64 square root is some ten FP64-pipe instructions)
+      if (r2 > c.dpc_r2cut) continue;
+      const double r = sqrt(r2);
+      const double u = r * c.dpc_l0inv;
       if (!(u < 1.0)) continue;
 #pragma unroll
       for (int d = 0; d < D; ++d) dv[d] = vk[d] - S.v[d][m];
@@ -691,6 +694,7 @@ static StepConst make_const(const sph_handle* h) {
   c.use_pF = p.s > 0;
   if (p.dpc_l0 > 0) {
     c.dpc_l0inv = 1.0 / p.dpc_l0;
+    c.dpc_r2cut = p.dpc_l0 * p.dpc_l0 * (1.0 + 1e-6);
     c.dpc_nW = h->D == 2 ? wc2_norm_w<2>(c.dpc_l0inv) : wc2_norm_w<3>(c.dpc_l0inv);
     c.dpc_whinv = 1.0 / wc2_w(0.5, c.dpc_nW);
     c.dpc_pmin = p.dpc_pmin;

@@ -16,6 +16,7 @@ struct StepConst {
   double fb_d, fb_r0, fb_eta2;  // fbmolforce constants of the stage being run
   double twoh, pfc, hp1;        // 2h, 1.5*pi, 0.1h  (∂v∂tpF!)
   double dpc_l0inv, dpc_nW, dpc_whinv, dpc_pmin, dpc_pmax, dpc_lambda, dpc_kernlim, dpc_eta2;
+  double dpc_r2cut;  // l0² (1 + 1e-6): past it u = √r² / l0 >= 1 whatever the rounding
   double xsph_c;                // 2*m0*eps
   double cfl, dt_eta2;          // Δt_stepping
   double tmin, tmax;

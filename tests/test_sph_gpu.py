@@ -202,6 +202,23 @@ def test_full_physics_2d_split_rows(gpu_pkg, orc):
 
 
 @pytest.mark.parametrize("lanes", [1, 0])
+def test_dpc_on_jittered_fluid(gpu_pkg, orc, lanes):
+    """Fluid jittered by up to 0.25 dx and l0 = 0.7 dx: about a quarter of the
+    fluid rows hold pairs within l0, so dpcreg! acts (and the pairs past l0
+    take its r² cut before the root).  Serial rows bit-identical, split rows
+    within the contract or noise floor."""
+    case = _physics_2d(gpu_pkg)
+    rng = np.random.default_rng(5)
+    fl = case.ptype > 1
+    case.x = case.x.copy()
+    case.x[:, fl] += rng.uniform(-0.25 * case.dx, 0.25 * case.dx, (2, int(fl.sum())))
+    v = well_conditioned_v(case)
+    prob, ref = make_pair(gpu_pkg, orc, case, lanes, v=v)
+    run_both(prob, ref, 20)
+    check(orc, prob, ref, case, lanes, [(20, {})], v=v)
+
+
+@pytest.mark.parametrize("lanes", [1, 0])
 def test_full_physics_3d(gpu_pkg, orc, lanes):
     case = gpu_pkg.workloads.dam_break_3d(dx=0.05, fluid=(0.3, 0.4, 0.2), tank=(0.6, 0.6, 0.3))
     case.extra = dict(case.extra, dpc_l0=0.03)
