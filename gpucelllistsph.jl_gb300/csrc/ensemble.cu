@@ -974,9 +974,11 @@ __global__ void k_ens_dpc_apply(EnsArr A, const EnsInst* __restrict__ T) {
 
 // xsphcorr! + update_xsphcorr! (src/gpukernels_sph.jl:1745-1838): stage-1 W
 // (pairs and distances at x), v and ρ after the corrector and dpcreg!;
-// moves x only.  Reads neighbours' v, writes its own x: one pass.
+// moves x only.  Reads neighbours' v, writes its own x: one pass.  Little
+// arithmetic per neighbour and a record gather each: latency-bound, so three
+// blocks of 512 per SM (at most 42 registers) rather than the stage passes' two
 template <int D>
-__global__ void __launch_bounds__(ENS_MAX_TPB) k_ens_xsph(EnsArr A, const EnsInst* __restrict__ T) {
+__global__ void __launch_bounds__(ENS_MAX_TPB, 3) k_ens_xsph(EnsArr A, const EnsInst* __restrict__ T) {
   if (*A.ovf) return;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < A.N; i += stride) {
@@ -1283,7 +1285,7 @@ struct gcsph_ens {
   int tpb = 0;           // 0: not tuned yet
   bool tpb_fixed = false;
   int64_t tuned_n = 0;   // particle count the choice was made on
-  int sms = 0, occ[4] = {0, 0, 0, 0}, occ_nl[4] = {0, 0, 0, 0};
+  int sms = 0, occ[4] = {0, 0, 0, 0}, occ_nl[4] = {0, 0, 0, 0}, occ_x[4] = {0, 0, 0, 0};
   int nl_lanes = 4;      // lanes per particle in the list build (tuned after the block size)
   int nl_cpb = 0;        // list build: 0 = a thread group per particle, else tiles of nl_cpb cells per block
   int nl_depth = 1;      // tiles staged ahead (1 or 2)
@@ -1638,6 +1640,12 @@ int ens_occupancy(gcsph_ens* e) {
     else
       GC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b2, k_ens_nlist<3, 4>, kTpbs[t], 0));
     e->occ_nl[t] = std::max(b2, 1);
+    int b3 = 0;
+    if (e->D == 2)
+      GC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b3, k_ens_xsph<2>, kTpbs[t], 0));
+    else
+      GC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b3, k_ens_xsph<3>, kTpbs[t], 0));
+    e->occ_x[t] = std::max(b3, 1);
   }
   const int lanes[4] = {1, 2, 4, 8};
   for (int l = 0; l < 4; ++l)
@@ -1748,7 +1756,8 @@ int ens_enqueue_step(gcsph_ens* e, cudaStream_t st, int tpb) {
   }
   if (e->any_xsph) {
     timer_begin(T_XSPH, st);
-    k_ens_xsph<D><<<grid, tpb, 0, st>>>(A, T);
+    const int xgrid = (int)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)e->sms * e->occ_x[t]));
+    k_ens_xsph<D><<<xgrid, tpb, 0, st>>>(A, T);
     GC_LAUNCHED();
     timer_end(T_XSPH, st);
   }
