@@ -1667,6 +1667,16 @@ int tpb_index(int tpb) {
 }
 
 // one step of every instance: bin, re-sort, predictor pass, corrector pass
+// grid of a grid-stride pass over `want` blocks' worth of rows, with `slots`
+// blocks resident on the GPU: every block once from four waves up (the block
+// scheduler balances rows of unequal length); below that a persistent grid of
+// the resident blocks, where a partial second wave would leave SMs idle
+// (measured on GB300 for xsphcorr!: 0.95 -> 0.83 ms at 2 M 3-D particles, 8.7
+// waves; persistent 0.15 ms against 0.18 at 0.4 M, 1.7 waves)
+int wave_grid(int64_t want, int64_t slots) {
+  return (int)std::max<int64_t>(1, want >= 4 * slots ? want : std::min<int64_t>(want, slots));
+}
+
 template <int D>
 int ens_enqueue_step(gcsph_ens* e, cudaStream_t st, int tpb) {
   const int64_t N = e->N;
@@ -1700,7 +1710,7 @@ int ens_enqueue_step(gcsph_ens* e, cudaStream_t st, int tpb) {
   e->cur ^= 1;
   const int t = tpb_index(tpb);
   const int64_t want = (N + tpb - 1) / tpb;
-  const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)e->sms * e->occ[t]));
+  const int grid = wave_grid(want, (int64_t)e->sms * e->occ[t]);
   EnsArr A = ens_arr(e);
   timer_begin(T_PAIRS, st);
   if (e->nl_cpb > 0) {
@@ -1718,7 +1728,7 @@ int ens_enqueue_step(gcsph_ens* e, cudaStream_t st, int tpb) {
     // L lanes per particle in the list build (the list is the same for every L)
     const int L = e->nl_lanes;
     const int64_t gwant = (N * L + tpb - 1) / tpb;
-    const int g2 = (int)std::max<int64_t>(1, std::min<int64_t>(gwant, (int64_t)e->sms * e->occ_nl[t]));
+    const int g2 = wave_grid(gwant, (int64_t)e->sms * e->occ_nl[t]);
     switch (L) {
       case 2: k_ens_nlist<D, 2><<<g2, tpb, 0, st>>>(A, T); break;
       case 4: k_ens_nlist<D, 4><<<g2, tpb, 0, st>>>(A, T); break;
@@ -1760,13 +1770,7 @@ int ens_enqueue_step(gcsph_ens* e, cudaStream_t st, int tpb) {
   }
   if (e->any_xsph) {
     timer_begin(T_XSPH, st);
-    // a block per tpb particles once that is four waves or more (the block
-    // scheduler balances the rows); a persistent grid below, where a second
-    // partial wave would leave SMs idle (measured on GB300: 0.95 -> 0.83 ms at
-    // 2 M particles, 8.7 waves; persistent 0.15 ms against 0.18 at 0.4 M, 1.7)
-    const int64_t xslots = (int64_t)e->sms * e->occ_x[t];
-    const int xgrid = (int)std::max<int64_t>(1, want >= 4 * xslots ? want : std::min<int64_t>(want, xslots));
-    k_ens_xsph<D><<<xgrid, tpb, 0, st>>>(A, T);
+    k_ens_xsph<D><<<wave_grid(want, (int64_t)e->sms * e->occ_x[t]), tpb, 0, st>>>(A, T);
     GC_LAUNCHED();
     timer_end(T_XSPH, st);
   }
