@@ -519,45 +519,81 @@ __global__ void __launch_bounds__(TPB) k_pairs32(const double* __restrict__ x0, 
   int32_t spos = 0;  // MODE 2: staged entries so far
   const int xlo = cx > 0 ? cx - 1 : 0;
   const int xhi = cx < nx - 1 ? cx + 1 : nx - 1;
-  for (int dz = (D == 3 ? -1 : 0); dz <= (D == 3 ? 1 : 0); ++dz) {
-    const int z = cz + dz;
-    if (z < 0 || z >= nz) continue;
+  // one candidate m per lane (valid: in range and not k itself); the ballot
+  // keeps a group's hits in ascending m
+  auto visit = [&](int32_t m, bool valid) {
+    bool hit = false;
+    if (valid) {
+      const float d0 = ax - f0[m], d1 = ay - f1[m];
+      float r2f = d0 * d0 + d1 * d1;
+      if (D == 3) {
+        const float d2 = az - f2[m];
+        r2f = r2f + d2 * d2;
+      }
+      if (r2f < tlo) {
+        hit = true;
+      } else if (!(r2f > thi)) {  // inside the band (or NaN): the reference's FP64 test
+        hit = r2_ref<D>(x0[k], x1[k], D == 3 ? x2[k] : 0.0, x0[m], x1[m], D == 3 ? x2[m] : 0.0) < g.dist2;
+      }
+    }
+    if (MODE == 0) {
+      nf += hit;
+      nu += hit && (m > k);
+    } else if (MODE == 2) {
+      nf += hit;
+      nu += hit && (m > k);
+      const unsigned bal = (__ballot_sync(gm, hit) >> gbase) & (L == 32 ? 0xffffffffu : ((1u << L) - 1u));
+      const int32_t at = spos + __popc(bal & ((1u << lane) - 1u));
+      if (hit && at < S) stg[k * S + at] = m;
+      spos += __popc(bal);
+    } else {
+      const unsigned bal = (__ballot_sync(gm, hit) >> gbase) & (L == 32 ? 0xffffffffu : ((1u << L) - 1u));
+      if (hit) nbr[wpos + __popc(bal & ((1u << lane) - 1u))] = m;
+      wpos += __popc(bal);
+    }
+  };
+  if constexpr (D == 3) {
+    // The point's nine rows of three cells, in key order, are one sequence of
+    // candidates ascending in m: candidate t of it is m = t + dlt[r] for the
+    // row r with cum[r] <= t < cum[r + 1].  The lanes stride the whole
+    // sequence, so a group's trip count is ceil(candidates / L) rather than a
+    // sum over rows of a few candidates each, and the groups of a warp do not
+    // part at every row's end (measured on GB300: update! of 4M uniform 3-D
+    // points 2.43 -> 2.27 ms; in 2-D, with tens of candidates per row, the
+    // row-by-row walk below stays 4% faster)
+    constexpr int NR = 9;
+    int32_t cum[NR], dlt[NR];
+    int32_t tot = 0;
+#pragma unroll
+    for (int r = 0; r < NR; ++r) {
+      const int z = cz + (r / 3 - 1), y = cy + (r % 3 - 1);
+      int32_t m0 = 0, m1 = 0;
+      if (z >= 0 && z < nz && y >= 0 && y < ny) {
+        const int64_t base = (int64_t)nx * ((int64_t)y + (int64_t)ny * z);
+        m0 = cellstart[base + xlo];
+        m1 = cellstart[base + xhi + 1];
+      }
+      cum[r] = tot;
+      dlt[r] = m0 - tot;
+      tot += m1 - m0;
+    }
+    for (int32_t tb = 0; tb < tot; tb += L) {
+      const int32_t t = tb + lane;
+      int32_t dd = dlt[0];
+#pragma unroll
+      for (int r = 1; r < NR; ++r) dd = t >= cum[r] ? dlt[r] : dd;
+      const int32_t m = t + dd;
+      visit(m, t < tot && m != k);
+    }
+  } else {
     for (int dy = -1; dy <= 1; ++dy) {
       const int y = cy + dy;
       if (y < 0 || y >= ny) continue;
-      const int64_t base = (int64_t)nx * ((int64_t)y + (int64_t)ny * z);
+      const int64_t base = (int64_t)nx * (int64_t)y;
       const int32_t m0 = cellstart[base + xlo], m1 = cellstart[base + xhi + 1];
       for (int32_t mb = m0; mb < m1; mb += L) {
         const int32_t m = mb + lane;
-        bool hit = false;
-        if (m < m1 && m != k) {
-          const float d0 = ax - f0[m], d1 = ay - f1[m];
-          float r2f = d0 * d0 + d1 * d1;
-          if (D == 3) {
-            const float d2 = az - f2[m];
-            r2f = r2f + d2 * d2;
-          }
-          if (r2f < tlo) {
-            hit = true;
-          } else if (!(r2f > thi)) {  // inside the band (or NaN): the reference's FP64 test
-            hit = r2_ref<D>(x0[k], x1[k], D == 3 ? x2[k] : 0.0, x0[m], x1[m], D == 3 ? x2[m] : 0.0) < g.dist2;
-          }
-        }
-        if (MODE == 0) {
-          nf += hit;
-          nu += hit && (m > k);
-        } else if (MODE == 2) {
-          nf += hit;
-          nu += hit && (m > k);
-          const unsigned bal = (__ballot_sync(gm, hit) >> gbase) & (L == 32 ? 0xffffffffu : ((1u << L) - 1u));
-          const int32_t at = spos + __popc(bal & ((1u << lane) - 1u));
-          if (hit && at < S) stg[k * S + at] = m;
-          spos += __popc(bal);
-        } else {
-          const unsigned bal = (__ballot_sync(gm, hit) >> gbase) & (L == 32 ? 0xffffffffu : ((1u << L) - 1u));
-          if (hit) nbr[wpos + __popc(bal & ((1u << lane) - 1u))] = m;
-          wpos += __popc(bal);
-        }
+        visit(m, m < m1 && m != k);
       }
     }
   }
