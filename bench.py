@@ -86,6 +86,39 @@ def algorithmic_bytes_per_stage(case, npairs):
     return N * (16 * D + 28) + npairs * (16 + 2 * (16 + 16 * D))
 
 
+def algorithmic_flops_stage1(case, x, v):
+    """Algorithmic FP64 flops of one stage-1 pass A launch: every pair once,
+    the reference's per-pair expressions counted as written (add, mul, cmp,
+    div, sqrt = 1 each; the reference's own arithmetic has no FMA):
+      sphW! + sph∇W! (every pair): 7D + 16
+      ∂ρ∂tDDT! (both real): 7D + 1, and 34 per fluid side (powfancy7th 22 of it)
+      ∂v∂t! (both real): 3D + 4
+      ∂v∂t_av! (both real): 3D, and 5D + 10 more where Δv·Δx < 0
+      fbmolforce! (one side real): 3D + 1, and 3D + 14 more where r < r₀ = 2dx
+    The two data-dependent branches are counted for the pairs that take them
+    in the state (x, v) given; the pairs are those with r <= dist in x (a
+    pair exactly at dist, which the reference drops, changes the count by
+    one pair's flops)."""
+    import numpy as np
+    from scipy.spatial import cKDTree
+    D = case.D
+    pt = np.asarray(case.ptype)
+    pr = cKDTree(np.ascontiguousarray(x.T)).query_pairs(case.dist, output_type="ndarray")
+    i, j = pr[:, 0], pr[:, 1]
+    dxv = x[:, i] - x[:, j]
+    dvv = v[:, i] - v[:, j]
+    real = (pt[i] > 0) & (pt[j] > 0)
+    mixed = (pt[i] > 0) != (pt[j] > 0)
+    fluid_sides = (pt[i] > 1).astype(np.int64) + (pt[j] > 1)
+    approach = real & ((dvv * dxv).sum(axis=0) < 0)
+    inside = mixed & (np.sqrt((dxv * dxv).sum(axis=0)) < 2.0 * case.dx)
+    flops = ((7 * D + 16) * len(i) + real.sum() * ((7 * D + 1) + (3 * D + 4) + 3 * D) +
+             34 * fluid_sides[real].sum() + (5 * D + 10) * approach.sum() +
+             (3 * D + 1) * mixed.sum() + (3 * D + 14) * inside.sum())
+    return int(flops), {"pairs": int(len(i)), "real": int(real.sum()), "one_side_real": int(mixed.sum()),
+                        "approaching": int(approach.sum()), "within_r0": int(inside.sum())}
+
+
 # DRAM bytes (read + write) of one stage-1 pass A launch on this workload, from
 # the ncu capture summarised in profiles/pairA_dambreak2d_c1_fp64.md
 PAIRA_STAGE1_DRAM_BYTES = 2_100_992 + 512
@@ -634,7 +667,23 @@ def run_gb300(args):
             "fp64_pipe_frac_ncu": PAIRA_STAGE1_FP64_PIPE if top == "stage1" else None,
             "note": "pair-once pass A is FP64-pipe bound (2 FP64 instr/cycle/SM on GB300, ncu: 78% of that "
                     "peak); its working set stays in L2, so the HBM fraction against the measured copy "
-                    "bandwidth is small by construction"}
+                    "bandwidth is small by construction; 'fp64' is the algorithmic-flop side of the roofline"}
+    if top == "stage1":
+        # the compute side: the reference's per-pair flops over the measured launch time, against
+        # the FP64 peak of 2 DFMA (4 flops) per cycle per SM at the SM clock sampled under load
+        try:
+            xs = torch.stack([p_.detach() for p_ in system.points]).cpu().numpy()
+            vs = torch.stack([p_.detach() for p_ in prob.v]).cpu().numpy()
+            flops, kinds = algorithmic_flops_stage1(case, xs, vs)
+            sms = torch.cuda.get_device_properties(local).multi_processor_count
+            mhz = clk.summary().get("sm_mhz") or 2070.0
+            fp64_peak = 4.0 * sms * mhz * 1e6
+            roof["fp64"] = {"achieved": flops / avg_s / 1e12, "peak": fp64_peak / 1e12, "unit": "TFLOP/s",
+                            "frac": flops / avg_s / fp64_peak, "flops_per_launch": flops, "pairs": kinds,
+                            "peak_source": f"ncu DFMA peak_sustained 2/cycle/SM x {sms} SMs x {mhz:.0f} MHz",
+                            "state": "pairs and branches counted at the state after the timed steps"}
+        except Exception as e:  # noqa: BLE001
+            roof["fp64"] = {"unavailable": f"{type(e).__name__}: {e}"}
     cpu = None
     if not args.no_cpu_baseline:
         try:
