@@ -21,3 +21,34 @@ def test_reference_arm_prints_one_contract_line():
     assert d["impl"] == "reference" and d["value"] > 0 and d["higher_is_better"] is True
     assert d["config"]["workload"] and d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["cores"] >= 1
     assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["e2e"]["value"] == d["value"]
+
+
+def _bench_module():
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("bench_under_test", os.path.join(ROOT, "bench.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def test_pass_a_flop_count_by_hand():
+    """The roofline's flop side on a configuration counted by hand (2-D): two
+    fluid particles approaching each other, a boundary (ptype 0) particle
+    within r0 = 2dx of one of them, and a second boundary particle that pairs
+    only with the first boundary particle."""
+    import types
+    import numpy as np
+    b = _bench_module()
+    dx = 0.1
+    case = types.SimpleNamespace(D=2, dx=dx, dist=0.25, ptype=np.array([2, 2, 0, 0], dtype=np.int32))
+    x = np.array([[0.0, 0.2, -0.05, -0.05], [0.0, 0.0, -0.14, -0.37]])
+    v = np.array([[1.0, -1.0, 0.0, 0.0], [0.0, 0.0, 0.0, 0.0]])
+    flops, kinds = b.algorithmic_flops_stage1(case, x, v)
+    # pairs: (0,1) fluid-fluid at 0.2, approaching; (0,2) fluid-boundary at 0.149 < 2dx;
+    # (2,3) boundary-boundary at 0.23; (1,2) at 0.287 is past dist
+    assert kinds == {"pairs": 3, "real": 1, "one_side_real": 1, "approaching": 1, "within_r0": 1}
+    D = 2
+    geometry = 7 * D + 16                                   # every pair
+    ff = (7 * D + 1) + 2 * 34 + (3 * D + 4) + 3 * D + (5 * D + 10)
+    fb_in = (3 * D + 1) + (3 * D + 14)
+    assert flops == 3 * geometry + ff + fb_in == 236
