@@ -1141,7 +1141,7 @@ static int run(int64_t N, const double* const* x, const double* cellsize, double
   GC_LAUNCHED();
   k_apply_perm<<<nblocks(N, TPB), TPB, 0, st>>>(perm, key, nullptr, N, skey, orig);
   GC_LAUNCHED();
-  k_gather_pos<D><<<nblocks(N, TPB), TPB, 0, st>>>(perm, N, x[0], x[1], x2, xs[0], xs[1], D == 3 ? xs[2] : xs[0]);
+  k_gather_pos<D><<<nblocks(N, TPB), TPB, 0, st>>>(perm, N, x[0], x[1], x2, xs[0], xs[1], D == 3 ? xs[2] : nullptr);
   GC_LAUNCHED();
   // pair counts, offsets, then the pairs themselves
   const double cand = (double)N / (double)ncell * (D == 3 ? 27.0 : 9.0);

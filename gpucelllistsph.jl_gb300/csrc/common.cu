@@ -312,7 +312,7 @@ __global__ void __launch_bounds__(1024) k_scan_single(const TIn* __restrict__ in
 template <class TIn, class TOut>
 static int scan_impl(const TIn* in, TOut* out, int64_t n_in, int64_t m, int64_t* scratch, cudaStream_t s) {
   if (m <= 65536) {
-    k_scan_single<TIn, TOut><<<1, 1024, 0, s>>>(in, out, in, out, n_in, m);
+    k_scan_single<TIn, TOut><<<1, 1024, 0, s>>>(in, out, nullptr, nullptr, n_in, m);
     GC_LAUNCHED();
     return GCSPH_OK;
   }
