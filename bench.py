@@ -44,6 +44,9 @@ def parse():
     ap.add_argument("--no-serving", action="store_true", help="skip the serving-loop measurement")
     ap.add_argument("--serving-requests", type=int, default=40)
     ap.add_argument("--serving-horizon-scale", type=float, default=0.01)
+    ap.add_argument("--serving-policy", default="shortest", choices=["shortest", "arrival"])
+    ap.add_argument("--serving-caps", default="3000000,1000000",
+                    help="shortest-first: 2-D and 3-D particles in flight")
     ap.add_argument("--no-celllist", action="store_true", help="skip the cell-list update!/partialupdate! timing")
     ap.add_argument("--c3", action="store_true",
                     help="instead: 3-D dam break at scale, FP32 ensemble against the FP64 drop-in (one JSON line)")
@@ -359,10 +362,22 @@ def run_serving(g, args):
     import numpy as np
     S = g.serving
     raw = g.workloads.serving_requests(args.serving_requests, horizon_scale=args.serving_horizon_scale)
-    reqs = [S.Request(i, t, g.spec_from_case(c), n) for i, (t, c, n) in enumerate(raw)]
-    loop = S.ServingLoop(chunk=64)
-    stats = loop.run(reqs)
-    loop.close()
+    caps = tuple(int(c) for c in args.serving_caps.split(","))
+
+    def serve(policy):
+        reqs = [S.Request(i, t, g.spec_from_case(c), n) for i, (t, c, n) in enumerate(raw)]
+        loop = S.ServingLoop(chunk=64, policy=policy, caps=caps)
+        st = loop.run(reqs)
+        loop.close()
+        return st
+
+    stats = serve(args.serving_policy)
+    stats["policy"] = {"name": args.serving_policy, "caps_2d_3d": list(caps) if args.serving_policy == "shortest"
+                       else None}
+    other = "arrival" if args.serving_policy == "shortest" else "shortest"
+    o = serve(other)
+    stats["other_policy"] = {"name": other, "p50_s": o["p50_s"], "p99_s": o["p99_s"], "mean_s": o["mean_s"],
+                             "particle_steps_per_s": o["particle_steps_per_s"]}
     # the same solves run alone, one after another, on the plain FP64 path:
     # each one's time from its size class's measured FP64 rate
     by_d = {2: [c for _, c, _ in raw if c.D == 2], 3: [c for _, c, _ in raw if c.D == 3]}

@@ -3,9 +3,11 @@
 // call of stepsolve!/timesolve!, src/sphproblem.jl:204-345 and :420-511).
 //
 // Requests -- dam-break solves with a horizon in steps -- arrive over time.
-// Each is admitted as soon as it has arrived and the device has room for it
-// (free HBM against the ensemble's bytes per particle, twice, for buffer
-// growth, within a reserve), joins the 2-D or 3-D ensemble, and advances
+// Each is admitted once it has arrived and the device has room for it (free
+// HBM against the ensemble's bytes per particle, twice, for buffer growth,
+// within a reserve) -- in arrival order, or, under the shortest-first policy,
+// smallest work (particles x steps) first while its dimension's particles in
+// flight stay within a cap -- joins the 2-D or 3-D ensemble, and advances
 // together with every other admitted solve in chunks of at most `chunk`
 // steps, cut at the nearest horizon so that each solve stops exactly at its
 // own.  A finished solve's fields are read back and its slot is released,
@@ -57,6 +59,8 @@ struct gcsph_srv {
   cudaStream_t dim_st[2] = {nullptr, nullptr};
   int32_t chunk = 64;
   double reserve = 0.1;
+  int32_t policy = GCSPH_SRV_ARRIVAL;
+  int64_t cap[2] = {0, 0};  // shortest-first: particles in flight per dimension (0: no cap)
   uint32_t fields = 7;     // bit f: read back GCSPH_ENS field f at the horizon
   gcsph_ens* ens[2] = {nullptr, nullptr};
   std::vector<SrvReq> req;
@@ -143,18 +147,32 @@ double percentile(std::vector<double> v, double p) {
   return v[lo] + (v[hi] - v[lo]) * (pos - (double)lo);
 }
 
-// one round: admit what has arrived and fits (arrival order), then one chunk
-// of every ensemble with running solves, then release the finished ones
+// one round: admit what has arrived and fits (arrival order, or smallest
+// work first within the caps), then one chunk of every ensemble with running
+// solves, then release the finished ones
 int round(gcsph_srv* s, int* advanced) {
   *advanced = 0;
   const double now = now_of(s);
   std::vector<size_t> order;
   for (size_t i = 0; i < s->req.size(); ++i)
     if (s->req[i].state == RQ_QUEUED && s->req[i].arrival <= now) order.push_back(i);
-  std::stable_sort(order.begin(), order.end(),
-                   [&](size_t a, size_t b) { return s->req[a].arrival < s->req[b].arrival; });
+  const bool shortest = s->policy == GCSPH_SRV_SHORTEST;
+  std::stable_sort(order.begin(), order.end(), [&](size_t a, size_t b) {
+    const SrvReq &ra = s->req[a], &rb = s->req[b];
+    if (shortest) {
+      const double wa = (double)ra.n * (double)ra.steps, wb = (double)rb.n * (double)rb.steps;
+      if (wa != wb) return wa < wb;
+    }
+    return ra.arrival < rb.arrival;
+  });
+  int64_t inflight[2] = {0, 0};
+  for (const SrvReq& r : s->req)
+    if (r.state == RQ_RUNNING) inflight[r.D == 3 ? 1 : 0] += r.n;
   for (size_t i : order) {
     SrvReq& r = s->req[i];
+    const int di = r.D == 3 ? 1 : 0;
+    // within the cap, except that an idle dimension takes any solve
+    if (shortest && s->cap[di] > 0 && inflight[di] > 0 && inflight[di] + r.n > s->cap[di]) continue;
     if (!fits(s, r)) continue;
     int32_t slot = -1;
     int rc = s->be.add(s->be.ctx, r.D, (int32_t)i, &slot);
@@ -163,6 +181,7 @@ int round(gcsph_srv* s, int* advanced) {
     r.state = RQ_RUNNING;
     r.admitted = now_of(s);
     r.remaining = r.steps;
+    inflight[di] += r.n;
   }
   int64_t kd[2] = {s->chunk, s->chunk}, lived[2] = {0, 0};
   for (const SrvReq& r : s->req)
@@ -286,6 +305,25 @@ int srv_submit(gcsph_srv* s, int32_t D, int64_t n, const double* x, const double
   }
   s->req.push_back(std::move(r));
   *rid = (int32_t)(s->req.size() - 1);
+  return GCSPH_OK;
+}
+
+int srv_set_policy(gcsph_srv* s, int32_t policy, int64_t cap2d, int64_t cap3d) {
+  if (!s) return fail(GCSPH_EINVAL, "null handle");
+  if (policy != GCSPH_SRV_ARRIVAL && policy != GCSPH_SRV_SHORTEST)
+    return fail(GCSPH_EINVAL, "policy %d (GCSPH_SRV_ARRIVAL or GCSPH_SRV_SHORTEST)", (int)policy);
+  if (cap2d < 0 || cap3d < 0) return fail(GCSPH_EINVAL, "negative particle cap");
+  s->policy = policy;
+  s->cap[0] = cap2d;
+  s->cap[1] = cap3d;
+  return GCSPH_OK;
+}
+
+int srv_get_policy(gcsph_srv* s, int32_t* policy, int64_t* cap2d, int64_t* cap3d) {
+  if (!s) return fail(GCSPH_EINVAL, "null handle");
+  if (policy) *policy = s->policy;
+  if (cap2d) *cap2d = s->cap[0];
+  if (cap3d) *cap3d = s->cap[1];
   return GCSPH_OK;
 }
 

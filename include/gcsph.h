@@ -385,6 +385,10 @@ typedef struct gcsph_srv_stats {
   double p50_s, p99_s, mean_s; /* time to horizon (arrival to results on the host); NaN before any */
 } gcsph_srv_stats;
 enum { GCSPH_SRV_QUEUED = 0, GCSPH_SRV_RUNNING = 1, GCSPH_SRV_DONE = 2 };
+/* admission policies: arrival order (the default), or smallest work
+ * (particles x steps) first while a dimension's particles in flight stay
+ * within its cap (0: no cap; an idle dimension admits any solve) */
+enum { GCSPH_SRV_ARRIVAL = 0, GCSPH_SRV_SHORTEST = 1 };
 
 int srv_create(void* stream, int32_t chunk, double reserve, uint32_t fields, const gcsph_srv_backend* backend,
                gcsph_srv** out);
@@ -394,6 +398,10 @@ void srv_destroy(gcsph_srv* s);
  * (negative: now); *rid numbers the requests from 0 */
 int srv_submit(gcsph_srv* s, int32_t D, int64_t n, const double* x, const double* v, const double* rho,
                const int32_t* ptype, const gcsph_ens_params* p, int64_t steps, double arrival, int32_t* rid);
+/* the admission policy and, for GCSPH_SRV_SHORTEST, the particles in flight
+ * per dimension; set before srv_run */
+int srv_set_policy(gcsph_srv* s, int32_t policy, int64_t cap2d, int64_t cap3d);
+int srv_get_policy(gcsph_srv* s, int32_t* policy, int64_t* cap2d, int64_t* cap3d);
 /* one round (admissions, one chunk per ensemble, releases) */
 int srv_progress(gcsph_srv* s, int32_t* running, int32_t* queued);
 /* rounds until every submitted request has reached its horizon, waiting for

@@ -91,3 +91,77 @@ def test_a_request_that_can_never_fit_is_refused(pkg):
     loop = _loop(pkg, free_bytes=lambda: 10 ** 6)
     with pytest.raises(RuntimeError):
         loop.run(reqs)
+
+
+def _live(D=None):
+    """Particles in flight per the fake ensemble's log (of one dimension, or all)."""
+    n = 0
+    for t in FakeEnsemble.log:
+        if D is not None and t[1] != D:
+            continue
+        n += t[2] if t[0] == "add" else -t[2]
+    return n
+
+
+def test_shortest_first_admits_small_work_first_within_the_cap(pkg):
+    """All requests arrive at once.  Under the shortest-first policy the
+    smallest work (particles x steps) is admitted first, the 2-D particles in
+    flight never pass the cap while another solve runs, and a solve larger
+    than the cap runs alone once its dimension is idle."""
+    S = pkg.serving
+    sizes = [(4000, 10), (500, 20), (1500, 5), (9000, 3), (800, 40), (3000, 2)]  # (n, steps), all 2-D
+    reqs = [S.Request(i, 0.0, Spec(2, n), steps) for i, (n, steps) in enumerate(sizes)]
+    cap = 5000
+    peaks = []
+    orig_step = FakeEnsemble.step
+
+    def step(self, k):
+        peaks.append(_live(2))
+        orig_step(self, k)
+
+    FakeEnsemble.step = step
+    try:
+        loop = _loop(pkg, chunk=64, free_bytes=lambda: 10 ** 12, policy="shortest", caps=(cap, 0))
+        stats = loop.run(reqs)
+    finally:
+        FakeEnsemble.step = orig_step
+    assert stats["completed"] == len(reqs)
+    adds = [t[2] for t in FakeEnsemble.log if t[0] == "add"]
+    # the first admission is the smallest work, 3000 particles x 2 steps
+    works = sorted((n * st, n) for n, st in sizes)
+    assert adds[0] == works[0][1]
+    for p in peaks:
+        assert p <= cap or p == 9000, peaks  # the 9000-particle solve only alone
+    assert 9000 in peaks
+    for r in reqs:
+        assert r.result["x"][0] == r.steps
+
+
+def test_arrival_policy_admits_everything_that_fits(pkg):
+    S = pkg.serving
+    reqs = [S.Request(i, 0.0, Spec(2, 1000 * (i + 1)), 10 - i) for i in range(4)]
+    loop = _loop(pkg, chunk=64, free_bytes=lambda: 10 ** 12)
+    loop.run(reqs)
+    tags = [t[0] for t in FakeEnsemble.log]
+    assert tags[:4] == ["add"] * 4
+    assert [t[2] for t in FakeEnsemble.log[:4]] == [1000, 2000, 3000, 4000]
+
+
+def test_policy_round_trip_and_bad_policy(pkg):
+    import ctypes as C
+    import pytest
+    L = pkg._lib.load()
+    h = C.c_void_p()
+    tbl = pkg.serving._CallbackBackend(_loop(pkg), {}).table
+    pkg._lib.check(L.srv_create(None, 8, 0.1, 0, C.byref(tbl), C.byref(h)))
+    try:
+        pkg._lib.check(L.srv_set_policy(h, 1, 123, 456))
+        p, a, b = C.c_int32(), C.c_int64(), C.c_int64()
+        pkg._lib.check(L.srv_get_policy(h, C.byref(p), C.byref(a), C.byref(b)))
+        assert (p.value, a.value, b.value) == (1, 123, 456)
+        assert L.srv_set_policy(h, 7, 0, 0) != 0
+        assert L.srv_set_policy(h, 1, -1, 0) != 0
+    finally:
+        L.srv_destroy(h)
+    with pytest.raises(ValueError):
+        pkg.serving.ServingLoop(policy="fastest")
