@@ -45,7 +45,7 @@ def parse():
     ap.add_argument("--serving-requests", type=int, default=40)
     ap.add_argument("--serving-horizon-scale", type=float, default=0.01)
     ap.add_argument("--serving-policy", default="shortest", choices=["shortest", "arrival"])
-    ap.add_argument("--serving-caps", default="3000000,1000000",
+    ap.add_argument("--serving-caps", default="1500000,500000",
                     help="shortest-first: 2-D and 3-D particles in flight")
     ap.add_argument("--no-celllist", action="store_true", help="skip the cell-list update!/partialupdate! timing")
     ap.add_argument("--c3", action="store_true",
