@@ -121,8 +121,8 @@ _SIGS = {
     "srv_submit": (C.c_int, [vp, i32, i64, vp, vp, vp, vp, C.POINTER(gcsph_ens_params), i64, f64, C.POINTER(i32)]),
     "srv_progress": (C.c_int, [vp, C.POINTER(i32), C.POINTER(i32)]),
     "srv_run": (C.c_int, [vp]),
-    "srv_set_policy": (C.c_int, [vp, i32, i64, i64]),
-    "srv_get_policy": (C.c_int, [vp, C.POINTER(i32), C.POINTER(i64), C.POINTER(i64)]),
+    "srv_set_policy": (C.c_int, [vp, i32, i64, i64, f64]),
+    "srv_get_policy": (C.c_int, [vp, C.POINTER(i32), C.POINTER(i64), C.POINTER(i64), C.POINTER(f64)]),
     "srv_request": (C.c_int, [vp, i32, C.POINTER(i32), C.POINTER(f64), C.POINTER(f64), C.POINTER(f64)]),
     "srv_result": (C.c_int, [vp, i32, i32, vp]),
     "srv_stats": (C.c_int, [vp, C.POINTER(gcsph_srv_stats)]),

@@ -61,6 +61,7 @@ struct gcsph_srv {
   double reserve = 0.1;
   int32_t policy = GCSPH_SRV_ARRIVAL;
   int64_t cap[2] = {0, 0};  // shortest-first: particles in flight per dimension (0: no cap)
+  double max_wait = 0;      // shortest-first: a solve waiting this long ignores the cap (0: never)
   uint32_t fields = 7;     // bit f: read back GCSPH_ENS field f at the horizon
   gcsph_ens* ens[2] = {nullptr, nullptr};
   std::vector<SrvReq> req;
@@ -171,8 +172,10 @@ int round(gcsph_srv* s, int* advanced) {
   for (size_t i : order) {
     SrvReq& r = s->req[i];
     const int di = r.D == 3 ? 1 : 0;
-    // within the cap, except that an idle dimension takes any solve
-    if (shortest && s->cap[di] > 0 && inflight[di] > 0 && inflight[di] + r.n > s->cap[di]) continue;
+    // within the cap, except that an idle dimension takes any solve and a
+    // solve that has waited max_wait is not held back by it
+    const bool aged = s->max_wait > 0 && now - r.arrival >= s->max_wait;
+    if (shortest && !aged && s->cap[di] > 0 && inflight[di] > 0 && inflight[di] + r.n > s->cap[di]) continue;
     if (!fits(s, r)) continue;
     int32_t slot = -1;
     int rc = s->be.add(s->be.ctx, r.D, (int32_t)i, &slot);
@@ -308,22 +311,25 @@ int srv_submit(gcsph_srv* s, int32_t D, int64_t n, const double* x, const double
   return GCSPH_OK;
 }
 
-int srv_set_policy(gcsph_srv* s, int32_t policy, int64_t cap2d, int64_t cap3d) {
+int srv_set_policy(gcsph_srv* s, int32_t policy, int64_t cap2d, int64_t cap3d, double max_wait) {
   if (!s) return fail(GCSPH_EINVAL, "null handle");
   if (policy != GCSPH_SRV_ARRIVAL && policy != GCSPH_SRV_SHORTEST)
     return fail(GCSPH_EINVAL, "policy %d (GCSPH_SRV_ARRIVAL or GCSPH_SRV_SHORTEST)", (int)policy);
   if (cap2d < 0 || cap3d < 0) return fail(GCSPH_EINVAL, "negative particle cap");
+  if (!(max_wait >= 0)) return fail(GCSPH_EINVAL, "max_wait %g (0: never)", max_wait);
   s->policy = policy;
   s->cap[0] = cap2d;
   s->cap[1] = cap3d;
+  s->max_wait = max_wait;
   return GCSPH_OK;
 }
 
-int srv_get_policy(gcsph_srv* s, int32_t* policy, int64_t* cap2d, int64_t* cap3d) {
+int srv_get_policy(gcsph_srv* s, int32_t* policy, int64_t* cap2d, int64_t* cap3d, double* max_wait) {
   if (!s) return fail(GCSPH_EINVAL, "null handle");
   if (policy) *policy = s->policy;
   if (cap2d) *cap2d = s->cap[0];
   if (cap3d) *cap3d = s->cap[1];
+  if (max_wait) *max_wait = s->max_wait;
   return GCSPH_OK;
 }
 

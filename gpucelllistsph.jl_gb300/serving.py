@@ -116,11 +116,14 @@ class ServingLoop:
     back at the horizon.  policy: "arrival" admits in arrival order whatever
     fits; "shortest" admits the smallest work (particles x steps) first while
     a dimension's particles in flight stay within caps = (2-D, 3-D) (0: no
-    cap; an idle dimension admits any solve).  free_bytes /
-    ensemble_factory / bytes_per_particle replace the device's (host tests)."""
+    cap; an idle dimension admits any solve), and a solve that has waited
+    max_wait seconds is admitted as soon as it fits, cap or not (0: never).
+    free_bytes / ensemble_factory / bytes_per_particle replace the device's
+    (host tests)."""
 
     def __init__(self, chunk: int = 64, reserve: float = 0.1, fields=("x", "v", "rho"), free_bytes=None,
-                 ensemble_factory=Ensemble, bytes_per_particle=None, policy: str = "arrival", caps=(0, 0)):
+                 ensemble_factory=Ensemble, bytes_per_particle=None, policy: str = "arrival", caps=(0, 0),
+                 max_wait: float = 0.0):
         self.chunk = int(chunk)
         self.reserve = float(reserve)
         self.fields = tuple(fields)
@@ -128,6 +131,7 @@ class ServingLoop:
             raise ValueError(f"policy {policy!r} (arrival or shortest)")
         self.policy = policy
         self.caps = (int(caps[0]), int(caps[1]))
+        self.max_wait = float(max_wait)
         self.native = free_bytes is None and ensemble_factory is Ensemble and bytes_per_particle is None
         self.free_bytes = free_bytes or device_free_bytes
         self.factory = ensemble_factory
@@ -150,7 +154,7 @@ class ServingLoop:
             _lib.check(L.srv_create(None, self.chunk, self.reserve, mask, C.byref(self._backend.table),
                                     C.byref(h)))
         self._srv = h
-        _lib.check(L.srv_set_policy(h, POLICIES[self.policy], self.caps[0], self.caps[1]))
+        _lib.check(L.srv_set_policy(h, POLICIES[self.policy], self.caps[0], self.caps[1], self.max_wait))
         rid = C.c_int32()
         keep = []  # host arrays referenced until submitted (copied by the library)
         for r in reqs:

@@ -399,9 +399,11 @@ void srv_destroy(gcsph_srv* s);
 int srv_submit(gcsph_srv* s, int32_t D, int64_t n, const double* x, const double* v, const double* rho,
                const int32_t* ptype, const gcsph_ens_params* p, int64_t steps, double arrival, int32_t* rid);
 /* the admission policy and, for GCSPH_SRV_SHORTEST, the particles in flight
- * per dimension; set before srv_run */
-int srv_set_policy(gcsph_srv* s, int32_t policy, int64_t cap2d, int64_t cap3d);
-int srv_get_policy(gcsph_srv* s, int32_t* policy, int64_t* cap2d, int64_t* cap3d);
+ * per dimension and the longest wait: a solve that has waited max_wait
+ * seconds is admitted as soon as it fits, cap or not (0: never), so that a
+ * stream of small solves cannot hold a large one back for ever */
+int srv_set_policy(gcsph_srv* s, int32_t policy, int64_t cap2d, int64_t cap3d, double max_wait);
+int srv_get_policy(gcsph_srv* s, int32_t* policy, int64_t* cap2d, int64_t* cap3d, double* max_wait);
 /* one round (admissions, one chunk per ensemble, releases) */
 int srv_progress(gcsph_srv* s, int32_t* running, int32_t* queued);
 /* rounds until every submitted request has reached its horizon, waiting for

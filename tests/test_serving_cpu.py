@@ -155,13 +155,30 @@ def test_policy_round_trip_and_bad_policy(pkg):
     tbl = pkg.serving._CallbackBackend(_loop(pkg), {}).table
     pkg._lib.check(L.srv_create(None, 8, 0.1, 0, C.byref(tbl), C.byref(h)))
     try:
-        pkg._lib.check(L.srv_set_policy(h, 1, 123, 456))
-        p, a, b = C.c_int32(), C.c_int64(), C.c_int64()
-        pkg._lib.check(L.srv_get_policy(h, C.byref(p), C.byref(a), C.byref(b)))
-        assert (p.value, a.value, b.value) == (1, 123, 456)
-        assert L.srv_set_policy(h, 7, 0, 0) != 0
-        assert L.srv_set_policy(h, 1, -1, 0) != 0
+        pkg._lib.check(L.srv_set_policy(h, 1, 123, 456, 2.5))
+        p, a, b, w = C.c_int32(), C.c_int64(), C.c_int64(), C.c_double()
+        pkg._lib.check(L.srv_get_policy(h, C.byref(p), C.byref(a), C.byref(b), C.byref(w)))
+        assert (p.value, a.value, b.value, w.value) == (1, 123, 456, 2.5)
+        assert L.srv_set_policy(h, 7, 0, 0, 0.0) != 0
+        assert L.srv_set_policy(h, 1, -1, 0, 0.0) != 0
+        assert L.srv_set_policy(h, 1, 0, 0, -1.0) != 0
     finally:
         L.srv_destroy(h)
     with pytest.raises(ValueError):
         pkg.serving.ServingLoop(policy="fastest")
+
+
+def test_shortest_first_max_wait_lifts_the_cap(pkg):
+    """A solve that has waited max_wait is admitted though the cap is full:
+    with a wait limit already passed at the first round, every solve is
+    admitted at once, as under arrival order."""
+    S = pkg.serving
+    reqs = [S.Request(i, 0.0, Spec(2, 1000 * (i + 1)), 10) for i in range(4)]
+    loop = _loop(pkg, chunk=64, free_bytes=lambda: 10 ** 12, policy="shortest", caps=(1000, 0), max_wait=1e-9)
+    loop.run(reqs)
+    assert [t[0] for t in FakeEnsemble.log[:4]] == ["add"] * 4
+    # without the wait limit the 1000-particle cap admits one solve at a time
+    reqs = [S.Request(i, 0.0, Spec(2, 1000 * (i + 1)), 10) for i in range(4)]
+    loop = _loop(pkg, chunk=64, free_bytes=lambda: 10 ** 12, policy="shortest", caps=(1000, 0))
+    loop.run(reqs)
+    assert [t[0] for t in FakeEnsemble.log] == ["add", "remove"] * 4
