@@ -363,7 +363,7 @@ __device__ __forceinline__ void shift_of(int ent, const EnsInst& I, float& sx, f
   sz = (float)(((ent >> 4) & 3) - 1) * I.csf;
 }
 
-// a candidate's verdict: with L lanes on a particle, a ballot keeps the hits
+// a candidate's decision: with L lanes on a particle, a ballot keeps the hits
 // in candidate order, so the list is the same for every L
 template <int L>
 __device__ __forceinline__ void nl_emit(const EnsArr& A, int64_t i, int lane, unsigned gm, unsigned gbase, bool hit,
