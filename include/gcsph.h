@@ -358,7 +358,8 @@ int ens_get_list_stride(gcsph_ens* e, int32_t* nls);
  * counterpart in the reference, which solves one SPHProblem per call,
  * src/sphproblem.jl:204-345, :420-511).  Submitted requests are admitted
  * once they have arrived and the device has room (n x bytes per particle x 2
- * within 1 - reserve of the free memory), advance together in chunks of at
+ * within 1 - reserve of the free memory) -- in arrival order, or smallest
+ * work first within caps (srv_set_policy) -- advance together in chunks of at
  * most `chunk` steps cut at the nearest horizon, and release their slot at
  * their horizon after the fields in `fields` (bit f = GCSPH_ENS field f) are
  * read back.  Times are seconds since srv_create.
