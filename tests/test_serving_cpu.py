@@ -182,3 +182,17 @@ def test_shortest_first_max_wait_lifts_the_cap(pkg):
     loop = _loop(pkg, chunk=64, free_bytes=lambda: 10 ** 12, policy="shortest", caps=(1000, 0))
     loop.run(reqs)
     assert [t[0] for t in FakeEnsemble.log] == ["add", "remove"] * 4
+
+
+def test_latency_statistics_match_numpy(pkg):
+    """p50/p99/mean time to horizon from the native scheduler equal numpy's
+    (linear percentile) over the requests' own arrival-to-done times."""
+    S = pkg.serving
+    reqs = [S.Request(i, 0.002 * i, Spec(2 if i % 2 else 3, 100 + 37 * i), 3 + (7 * i) % 20) for i in range(13)]
+    loop = _loop(pkg, chunk=4, free_bytes=lambda: 10 ** 12, policy="shortest", caps=(600, 400))
+    stats = loop.run(reqs)
+    lat = np.array([r.done - r.arrival for r in reqs])
+    assert stats["completed"] == len(reqs)
+    assert abs(stats["p50_s"] - np.percentile(lat, 50)) <= 1e-12
+    assert abs(stats["p99_s"] - np.percentile(lat, 99)) <= 1e-12
+    assert abs(stats["mean_s"] - lat.mean()) <= 1e-12
