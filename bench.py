@@ -9,6 +9,15 @@ One bench step = stepsolve!(prob, 15): 15 SPH time steps, one CSPM period.
 Timed with CUDA events on the library's stream (the legacy default stream);
 the L2 is flushed (256 MB write) between bench steps, outside the events.
 
+Beside that headline the line carries (each skippable by a flag):
+  long_horizon  the same dam break over its full 1,000 steps: mass, energy
+                and surge front of the FP64 path, the batched FP32 path and
+                the CPU oracle (the CPU baseline's own run)
+  c3            the 3-D dam break at scale, FP32 ensemble vs FP64 drop-in
+  batched_fp32  256 independent 2-D dam breaks, 1,000 steps, FP32
+  serving       a Poisson stream of solves at their full horizons
+  celllist      update!/partialupdate! on 200k 2-D and 4M 3-D points
+
 --impl reference times the CPU restatement of the reference's algorithm (the
 reference itself is Julia + CUDA.jl and cannot run here) on all host cores.
 """
@@ -28,31 +37,38 @@ sys.path.insert(0, ROOT)
 
 SUB = 15                    # SPH steps per bench step (one CSPM period)
 WORKLOAD = "2-D dam break, plain FP64 single instance, dx=0.02, 1.0x2.0 m column in 4.0x3.0 m tank, 3 boundary rows"
+L2_NOTE = "GPU L2 flushed (256 MB write) between bench steps"
 
 
-def parse():
+def parse(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--long-horizon-steps", type=int, default=1000,
+                    help="SPH steps of the long-horizon run (the C1 configuration's 1,000)")
+    ap.add_argument("--no-long-horizon", action="store_true")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched FP32 ensemble measurement")
     ap.add_argument("--batched-instances", type=int, default=256)
-    ap.add_argument("--batched-steps", type=int, default=300, help="timed steps of the ensemble")
+    ap.add_argument("--batched-steps", type=int, default=1000, help="timed steps of the ensemble")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving-loop measurement")
-    ap.add_argument("--serving-requests", type=int, default=40)
-    ap.add_argument("--serving-horizon-scale", type=float, default=0.01)
+    ap.add_argument("--serving-requests", type=int, default=8,
+                    help="the first this many requests of the seeded stream")
+    ap.add_argument("--serving-horizon-scale", type=float, default=1.0)
     ap.add_argument("--serving-policy", default="shortest", choices=["shortest", "arrival"])
     ap.add_argument("--serving-caps", default="1500000,500000",
                     help="shortest-first: 2-D and 3-D particles in flight")
+    ap.add_argument("--serving-fp64-steps", type=int, default=20,
+                    help="steps of each request timed alone on the FP64 path")
     ap.add_argument("--no-celllist", action="store_true", help="skip the cell-list update!/partialupdate! timing")
+    ap.add_argument("--no-c3", action="store_true", help="skip the 3-D dam break at scale")
     ap.add_argument("--c3", action="store_true",
-                    help="instead: 3-D dam break at scale, FP32 ensemble against the FP64 drop-in (one JSON line)")
+                    help="instead: only the 3-D dam break at scale (one JSON line)")
     ap.add_argument("--c3-steps", type=int, default=500)
     ap.add_argument("--c3-dx", type=float, default=0.01)
-    return ap.parse_args()
+    return ap.parse_args(argv)
 
 
 def dist_env():
@@ -79,14 +95,30 @@ def make_case(pkg):
     return pkg.workloads.dam_break_2d()
 
 
-def algorithmic_bytes_per_stage(case, npairs):
-    """Algorithmic HBM bytes of one pair-once pass A (FP64), the dominant
-    kernel: N·(8D x + 8D v + 8 ρ + 8 P + 8 1/ρ + 4 ptype) of particle state
-    read once, P·16 B of pair quads read, and per pair both sides' entry
-    slots written: 2·(8 W + 8D ∇W + 8 ρ̇ + 8D a) B (stage 1; stage 2 writes
-    no W/∇W).  P = pairs with k < m."""
+def gather_stage_bytes(case, npairs):
+    """Algorithmic HBM bytes of one FP64 pair-sum stage in gather form (the
+    unit the roofline is quoted on): particle state read once, N·(8D x + 8D v
+    + 8 ρ + 8 P + 4 ptype), the sums written once, N·(8 ρ̇ + 8D a), and one
+    4-byte neighbour index per pair side, 2P·4 -- N·(24D + 28) + 8P bytes.
+    P = pairs with k < m."""
+    D, N = case.D, case.N
+    return N * (24 * D + 28) + 2 * npairs * 4
+
+
+def design_stage_bytes(case, npairs):
+    """The bytes pass A of this design moves per launch (beyond the
+    algorithmic ones: its pair quads, 16 B a pair, and both sides' entry
+    slots, 2·(8 W + 8D ∇W + 8 ρ̇ + 8D a), which pass B sums from L2):
+    N·(16D + 28) + P·(16 + 2·(16 + 16D))."""
     D, N = case.D, case.N
     return N * (16 * D + 28) + npairs * (16 + 2 * (16 + 16 * D))
+
+
+def ens_stage_bytes(D, particles, pairs):
+    """Algorithmic HBM bytes of one FP32 ensemble stage pass: the gather's
+    N·(24D + 28) with every FP64 term halved (ptype stays 4 B), N·(12D + 16),
+    plus 2P·4 of neighbour indices."""
+    return particles * (12 * D + 16) + 2 * pairs * 4
 
 
 def algorithmic_flops_stage1(case, x, v):
@@ -187,24 +219,27 @@ class Clocks:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_baseline(case, seconds, threads):
-    """The oracle (C restatement of the reference's pair loops) on host cores,
-    a bounded sample of the same workload: whole bench steps until `seconds`."""
+def _oracle_params(orc, case):
+    return orc.default_params(case.dx, case.h, case.H, case.rho0, case.m0, case.dt, case.alpha, case.c0, case.gamma,
+                              case.delta, case.CFL, case.dist)
+
+
+def cpu_baseline(g, case, steps):
+    """The oracle (C restatement of the reference's pair loops, -O3 build) on
+    one host core: stepsolve!(prob, steps) from the workload's initial state,
+    a bounded sample of the same workload.  Returns the rate, the elapsed
+    time and the flow summary of the final state (the long-horizon check's
+    CPU leg)."""
     from oracle import oracle as orc
-    orc.set_threads(threads)
-    p = orc.default_params(case.dx, case.h, case.H, case.rho0, case.m0, case.dt, case.alpha, case.c0, case.gamma,
-                           case.delta, case.CFL, case.dist)
-    s = orc.OracleSystem(case.x, case.cellsize, case.dist, case.rho, case.ptype, p)
-    s.stepsolve(1)
-    n = 0
+    orc.select_build("timed")
+    orc.set_threads(1)
+    s = orc.OracleSystem(case.x, case.cellsize, case.dist, case.rho, case.ptype, _oracle_params(orc, case))
     t0 = time.perf_counter()
-    while True:
-        s.stepsolve(SUB)
-        n += SUB
-        el = time.perf_counter() - t0
-        if el >= seconds:
-            break
-    return case.N * n / el, n, el
+    s.stepsolve(steps)
+    el = time.perf_counter() - t0
+    summ = g.diagnostics.flow_summary(s.get("x"), s.get("v"), s.get("rho"), case.ptype, case.m0, case.g,
+                                      case.interior)
+    return case.N * steps / el, el, summ, orc.loaded_build()
 
 
 def run_reference(args):
@@ -214,12 +249,11 @@ def run_reference(args):
     import __graft_entry__ as ge
     wl = ge.load_package().workloads  # importing the package needs no GPU
     from oracle import oracle as orc
+    orc.select_build("timed")
     case = wl.dam_break_2d()
     threads = orc.max_threads()
     orc.set_threads(threads)
-    p = orc.default_params(case.dx, case.h, case.H, case.rho0, case.m0, case.dt, case.alpha, case.c0, case.gamma,
-                           case.delta, case.CFL, case.dist)
-    s = orc.OracleSystem(case.x, case.cellsize, case.dist, case.rho, case.ptype, p)
+    s = orc.OracleSystem(case.x, case.cellsize, case.dist, case.rho, case.ptype, _oracle_params(orc, case))
     for _ in range(args.warmup):
         s.stepsolve(SUB)
     times = []
@@ -233,9 +267,11 @@ def run_reference(args):
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
            "data": "synthetic", "impl": "reference",
-           "config": {"workload": WORKLOAD, "particles": case.N, "sph_steps_per_bench_step": SUB},
+           "config": {"workload": WORKLOAD, "particles": case.N, "pairs": s.pairsn, "sph_steps_per_bench_step": SUB,
+                      "l2": L2_NOTE, "parallelism": f"replicas x{args.gpus}"},
            "cpu_baseline": {"value": value, "unit": "particle-steps/s", "cores": threads, "kind": "port",
-                            "sample": f"{args.steps} x stepsolve!(prob, {SUB}) on the full workload"},
+                            "sample": f"{args.steps} x stepsolve!(prob, {SUB}) on the full workload, "
+                                      f"{orc.loaded_build()} (-O3), {threads} OpenMP threads"},
            "e2e": {"value": value, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out))
     return 0
@@ -249,41 +285,46 @@ def rel_l2(a, b):
     return float(np.linalg.norm(a - b) / n) if n > 0 else float(np.linalg.norm(a - b))
 
 
-def plain_fp64_rate(g, cases, steps=30):
-    """particle-steps/s of the FP64 drop-in path (stepsolve!, captured calls)
-    on each case alone, summed over the sample."""
+def new_fp64_problem(g, case):
+    """GPUCellList + SPHProblem of a case on the FP64 drop-in path."""
+    system = g.GPUCellList(tuple(case.x), case.cellsize, case.dist)
+    prob = g.SPHProblem(system, case.dx, case.h, case.H, g.WendlandC2(dim=case.D), case.rho, case.ptype,
+                        case.rho0, case.m0, case.dt, case.alpha, case.c0, case.gamma, case.delta, case.CFL,
+                        g=case.g, s=case.s)
+    for k, val in case.extra.items():
+        setattr(prob, k, val)
+    return system, prob
+
+
+def fp64_rate_alone(g, case, steps):
+    """particle-steps/s of the FP64 drop-in (stepsolve!, captured calls) on
+    one case alone: `steps` steps timed after a sizing call and a capture."""
     import torch
-    tot_ps, tot_s = 0, 0.0
-    for case in cases:
-        system = g.GPUCellList(tuple(case.x), case.cellsize, case.dist)
-        prob = g.SPHProblem(system, case.dx, case.h, case.H, g.WendlandC2(dim=case.D), case.rho, case.ptype,
-                            case.rho0, case.m0, case.dt, case.alpha, case.c0, case.gamma, case.delta, case.CFL)
-        prob.stepsolve(steps)  # sizes the buffers (first call runs per step)
-        prob.stepsolve(steps)  # captures
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        prob.stepsolve(steps)
-        torch.cuda.synchronize()
-        tot_s += time.perf_counter() - t0
-        tot_ps += case.N * steps
-        prob.close()
-        del system
-    return tot_ps / tot_s
+    system, prob = new_fp64_problem(g, case)
+    prob.stepsolve(steps)  # sizes the buffers (the first call runs per step)
+    prob.stepsolve(steps)  # captures
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    prob.stepsolve(steps)
+    torch.cuda.synchronize()
+    el = time.perf_counter() - t0
+    prob.close()
+    system.close()
+    return case.N * steps / el
 
 
 def fp32_error_vs_fp64(g, case, alpha, delta, steps=100):
     """Relative L2 error of the FP32 ensemble against the FP64 drop-in path
     (itself bit-identical / within 1e-12 of the reference algorithm) after
     `steps` steps of one instance."""
+    import dataclasses
+    import torch
     spec = g.spec_from_case(case, alpha=alpha, delta=delta)
     ens = g.Ensemble(case.D)
     slot = ens.add(spec)
     ens.step(steps)
-    system = g.GPUCellList(tuple(case.x), case.cellsize, case.dist)
-    prob = g.SPHProblem(system, case.dx, case.h, case.H, g.WendlandC2(dim=case.D), case.rho, case.ptype,
-                        case.rho0, case.m0, case.dt, alpha, case.c0, case.gamma, delta, case.CFL)
+    system, prob = new_fp64_problem(g, dataclasses.replace(case, alpha=alpha, delta=delta))
     prob.stepsolve(steps)
-    import torch
     x64 = torch.stack(system.points).cpu().numpy()
     out = {"rho": rel_l2(ens.get(slot, "rho"), prob.rho.cpu().numpy()),
            "rho_minus_rho0": rel_l2(ens.get(slot, "rho") - case.rho0, prob.rho.cpu().numpy() - case.rho0),
@@ -292,15 +333,34 @@ def fp32_error_vs_fp64(g, case, alpha, delta, steps=100):
            "steps": steps, "particles": case.N}
     ens.close()
     prob.close()
+    system.close()
     return out
 
 
-def run_batched(g, args, plain_c1):
+def timer_families(L):
+    import ctypes as C
+    fam = {}
+    for tid in range(L.gcsph_timing_count()):
+        n_ = C.c_int64(); t_ = C.c_double()
+        L.gcsph_timing_get(tid, C.byref(n_), C.byref(t_))
+        fam[L.gcsph_timing_name(tid).decode()] = (int(n_.value), float(t_.value))
+    return fam
+
+
+def run_batched(g, args, plain_c1, hbm_peak):
     """The batched-ensemble workload: 256 independent 2-D dam breaks
     (fluid-column counts log-uniform 2k-200k, aspect 0.5-4, dx 0.005-0.02,
-    α 0.005-0.05, δ 0.05-0.2), FP32, all advanced together."""
+    α 0.005-0.05, δ 0.05-0.2), FP32, all advanced together for the
+    configured 1,000 steps."""
     import torch
     wl = g.workloads.ensemble_2d(args.batched_instances)
+    # pairs within H of every instance at its initial state (update!), for
+    # the stage passes' algorithmic bytes
+    pairs0 = 0
+    for case, _, _ in wl:
+        c = g.GPUCellList(tuple(case.x), (case.H,) * 2, case.H)
+        pairs0 += c.pairsn
+        c.close()
     ens = g.Ensemble(2)
     t0 = time.perf_counter()
     slots = [ens.add(g.spec_from_case(case, alpha=al, delta=de)) for case, al, de in wl]
@@ -324,30 +384,38 @@ def run_batched(g, args, plain_c1):
     L.gcsph_timing_enable(1)
     L.gcsph_timing_reset()
     ens.step(20)
-    import ctypes as C
-    fam = {}
-    for tid in range(L.gcsph_timing_count()):
-        n_ = C.c_int64(); t_ = C.c_double()
-        L.gcsph_timing_get(tid, C.byref(n_), C.byref(t_))
-        if n_.value:
-            fam[L.gcsph_timing_name(tid).decode()] = {"launches": int(n_.value), "total_ms": float(t_.value)}
+    fam = {k: {"launches": v[0], "total_ms": v[1]} for k, v in timer_families(L).items() if v[0]}
     L.gcsph_timing_enable(0)
     tuning = ens.tuning()
     skin = ens.skin()
     ens.close()
+    # roofline of the stage passes (FP32): algorithmic bytes over the
+    # event-timed launch of each stage
+    roof = {}
+    for st in ("stage1", "stage2"):
+        if st in fam:
+            avg_s = fam[st]["total_ms"] / 1e3 / fam[st]["launches"]
+            alg = ens_stage_bytes(2, tot["particles"], pairs0)
+            roof[st] = {"avg_launch_us": avg_s * 1e6, "alg_bytes_per_launch": alg,
+                        "achieved_gbs": alg / avg_s / 1e9, "frac_of_hbm": alg / avg_s / 1e9 / hbm_peak}
+    roof["note"] = ("bytes = N(12D+16) + 2P*4 with P the pairs within H at the instances' initial states "
+                    "(update!); the passes are bound by instruction issue (72-74% of issue slots in ncu), "
+                    "their working set per step is re-read from L2")
     sizes = sorted(wl, key=lambda t: t[0].N)
     sample = [sizes[0][0], sizes[len(sizes) // 2][0], sizes[-1][0]]
-    plain = plain_fp64_rate(g, sample)
+    plain_ps = sum(c.N * 30 for c in sample)
+    plain = plain_ps / sum(c.N * 30 / fp64_rate_alone(g, c, 30) for c in sample)
     small = sizes[0]
     err = fp32_error_vs_fp64(g, small[0], small[1], small[2])
     return {"workload": "256 independent 2-D dam breaks, fluid counts log-uniform 2k-200k, aspect 0.5-4, "
                         "dx 0.005-0.02, alpha 0.005-0.05, delta 0.05-0.2 (seeded), FP32 pair arithmetic, "
                         "FP64 positions",
             "instances": tot["instances"], "particles": tot["particles"], "cells": tot["cells"],
+            "pairs_initial": pairs0,
             "value": value, "unit": "particle-steps/s", "timed_steps": args.batched_steps,
             "ms_per_step": ms / args.batched_steps, "admission_s": t_admit, "tuning": tuning,
             "list_skin": skin, "list_builds_in_timed_steps": builds,
-            "kernel_ms_20_steps": fam,
+            "kernel_ms_20_steps": fam, "roofline_stage_passes": roof,
             "plain_fp64_same_instances": {"value": plain, "unit": "particle-steps/s",
                                           "sample": "smallest, median and largest instance, each alone, 30 steps"},
             "ratio_vs_plain_fp64_same_instances": value / plain,
@@ -358,36 +426,24 @@ def run_batched(g, args, plain_c1):
 def run_serving(g, args):
     """The serving workload: Poisson arrivals (mean 20 req/s) of dam-break
     solves, 70% 2-D / 30% 3-D, particle counts log-uniform 5k-2M, horizons
-    uniform 0.05-0.5 s scaled by --serving-horizon-scale, FP32 ensembles."""
+    uniform 0.05-0.5 s (times --serving-horizon-scale) at Δt = 1e-5, FP32
+    ensembles with FP64 positions; the first --serving-requests requests of
+    the seeded stream.  Beside it, each solve alone on the FP64 drop-in, in
+    arrival order: each one's time is its own measured FP64 rate (timed on
+    its own particle set) times its horizon."""
     import numpy as np
     S = g.serving
     raw = g.workloads.serving_requests(args.serving_requests, horizon_scale=args.serving_horizon_scale)
     caps = tuple(int(c) for c in args.serving_caps.split(","))
-
-    def serve(policy):
-        reqs = [S.Request(i, t, g.spec_from_case(c), n) for i, (t, c, n) in enumerate(raw)]
-        loop = S.ServingLoop(chunk=64, policy=policy, caps=caps)
-        st = loop.run(reqs)
-        loop.close()
-        return st
-
-    stats = serve(args.serving_policy)
-    stats["policy"] = {"name": args.serving_policy, "caps_2d_3d": list(caps) if args.serving_policy == "shortest"
-                       else None}
-    other = "arrival" if args.serving_policy == "shortest" else "shortest"
-    o = serve(other)
-    stats["other_policy"] = {"name": other, "p50_s": o["p50_s"], "p99_s": o["p99_s"], "mean_s": o["mean_s"],
-                             "particle_steps_per_s": o["particle_steps_per_s"]}
-    # the same solves run alone, one after another, on the plain FP64 path:
-    # each one's time from its size class's measured FP64 rate
-    by_d = {2: [c for _, c, _ in raw if c.D == 2], 3: [c for _, c, _ in raw if c.D == 3]}
-    rates = {}
-    for D, cs in by_d.items():
-        if cs:
-            cs = sorted(cs, key=lambda c: c.N)
-            rates[D] = plain_fp64_rate(g, [cs[len(cs) // 2]], steps=20)
-    alone = np.array([c.N * n / rates[c.D] for _, c, n in raw])
-    # sequential service in arrival order
+    reqs = [S.Request(i, t, g.spec_from_case(c), n) for i, (t, c, n) in enumerate(raw)]
+    loop = S.ServingLoop(chunk=64, policy=args.serving_policy, caps=caps)
+    stats = loop.run(reqs)
+    loop.close()
+    stats["policy"] = {"name": args.serving_policy,
+                       "caps_2d_3d": list(caps) if args.serving_policy == "shortest" else None}
+    k = args.serving_fp64_steps
+    rates = [fp64_rate_alone(g, c, k) for _, c, _ in raw]
+    alone = np.array([c.N * n / r for (_, c, n), r in zip(raw, rates)])
     t, lat = 0.0, []
     for (arr, c, n), a in zip(raw, alone):
         t = max(t, arr) + a
@@ -395,12 +451,18 @@ def run_serving(g, args):
     lat = np.array(lat)
     tot_ps = sum(c.N * n for _, c, n in raw)
     stats.update({
-        "workload": f"{len(raw)} requests, Poisson 20 req/s, 70% 2-D / 30% 3-D, particle counts log-uniform "
-                    f"5k-2M, horizons uniform 0.05-0.5 s x {args.serving_horizon_scale} (dt 1e-5)",
+        "workload": f"the first {len(raw)} requests of a seeded Poisson stream (20 req/s), 70% 2-D / 30% 3-D, "
+                    f"particle counts log-uniform 5k-2M, horizons uniform 0.05-0.5 s x "
+                    f"{args.serving_horizon_scale:g} (dt 1e-5)",
+        "horizon_scale": args.serving_horizon_scale,
+        "requests_detail": [{"D": c.D, "particles": c.N, "steps": n, "arrival_s": round(a_, 4)}
+                            for a_, c, n in raw],
         "plain_fp64_alone": {"p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
                              "particle_steps_per_s": tot_ps / alone.sum(),
-                             "how": "each solve alone, in arrival order, at the FP64 path's measured rate for "
-                                    "its dimension (median-size request of that dimension, 20 steps)"},
+                             "rates_measured": [float(r) for r in rates],
+                             "how": f"each solve alone on the FP64 drop-in, in arrival order; its time = its "
+                                    f"horizon x its own FP64 rate, measured on its own particles over {k} steps "
+                                    f"(after a sizing call and a capture)"},
     })
     stats["throughput_ratio_vs_plain_fp64"] = stats["particle_steps_per_s"] / stats["plain_fp64_alone"][
         "particle_steps_per_s"]
@@ -468,9 +530,7 @@ def run_fixture(g, reps=50):
     import torch
     fx = os.path.join(ROOT, "tests", "golden", "dambreak2d_dp002.npz")
     case = g.workloads.load_fixture(fx)
-    system = g.GPUCellList(tuple(case.x), case.cellsize, case.dist)
-    prob = g.SPHProblem(system, case.dx, case.h, case.H, g.WendlandC2(dim=2), case.rho, case.ptype, case.rho0,
-                        case.m0, case.dt, case.alpha, case.c0, case.gamma, case.delta, case.CFL)
+    system, prob = new_fp64_problem(g, case)
     for _ in range(5):
         prob.stepsolve(1)
     ts = []
@@ -498,60 +558,106 @@ def run_fixture(g, reps=50):
                     "host round trip through the public API"}
 
 
-def run_c3(args):
+def c3_measure(g, steps, dx):
     """3-D dam break at scale: fluid block 1.0 x 2.0 (vertical) x 0.5 m at
     dx = 0.01 (1.0 M fluid) in a 4.0 x 3.0 x 1.0 m tank with 3 boundary
     layers, h = √3 dx, full physics (ν = 0.2, s = 0.05, DPC l₀ = 0.005,
     λ = 0.005, pmax = 36000, XSPH ε = 0.5, CSPM every 15 steps).  The FP32
-    ensemble and the FP64 drop-in each advance it `--c3-steps` steps; the
-    per-field relative L2 error of FP32 against FP64 and both rates."""
+    ensemble and the FP64 drop-in each advance it `steps` steps from the
+    same state; the per-field relative L2 error of FP32 against FP64, the
+    flow checks of both, and both rates."""
     import torch
-    torch.cuda.set_device(0)
-    import __graft_entry__ as ge
-    g = ge.load_package()
-    case = g.workloads.dam_break_3d(dx=args.c3_dx)
-    n = args.c3_steps
+    case = g.workloads.dam_break_3d(dx=dx)
     N = case.N
-    # FP32 ensemble
+    Dg = g.diagnostics
+    # FP32 ensemble: tuned and warmed on one instance, measured on a fresh one
     ens = g.Ensemble(3)
     slot = ens.add(g.spec_from_case(case))
     ens.step(30)  # tuning (24 steps) + warm-up
     torch.cuda.synchronize()
-    # a fresh instance for the measured run, so both start from the same state
     ens.remove(slot)
     slot = ens.add(g.spec_from_case(case))
     t0 = time.perf_counter()
-    ens.step(n)
+    ens.step(steps)
     torch.cuda.synchronize()
     t32 = time.perf_counter() - t0
     f32 = {f: ens.get(slot, f) for f in ("x", "v", "rho")}
     tuning = ens.tuning()
     ens.close()
-    # FP64 drop-in
-    system = g.GPUCellList(tuple(case.x), case.cellsize, case.dist)
-    prob = g.SPHProblem(system, case.dx, case.h, case.H, g.WendlandC2(dim=3), case.rho, case.ptype, case.rho0,
-                        case.m0, case.dt, case.alpha, case.c0, case.gamma, case.delta, case.CFL, g=case.g, s=case.s)
-    for k, val in case.extra.items():
-        setattr(prob, k, val)
+    system, prob = new_fp64_problem(g, case)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    prob.stepsolve(n)
+    prob.stepsolve(steps)
     torch.cuda.synchronize()
     t64 = time.perf_counter() - t0
     x64 = torch.stack(system.points).cpu().numpy()
     v64 = torch.stack(prob.v).cpu().numpy()
     r64 = prob.rho.cpu().numpy()
+    prob.close()
+    system.close()
     err = {"rho": rel_l2(f32["rho"], r64), "rho_minus_rho0": rel_l2(f32["rho"] - case.rho0, r64 - case.rho0),
            "v": rel_l2(f32["v"], v64), "displacement": rel_l2(f32["x"] - case.x, x64 - case.x),
            "x": rel_l2(f32["x"], x64)}
-    out = {"metric": "particle-steps/s", "workload": "3-D dam break at scale, full physics, FP32 ensemble vs "
-                                                     "FP64 drop-in", "particles": N,
-           "fluid": int((case.ptype == 2).sum()), "steps": n, "dx": args.c3_dx,
-           "fp32": {"value": N * n / t32, "seconds": t32, "tuning": tuning},
-           "fp64": {"value": N * n / t64, "seconds": t64},
-           "ratio_fp32_vs_fp64": t64 / t32, "fp32_error_vs_fp64": err}
+    start = Dg.flow_summary(case.x, 0 * case.x, case.rho, case.ptype, case.m0, case.g, case.interior)
+    s64 = Dg.flow_summary(x64, v64, r64, case.ptype, case.m0, case.g, case.interior)
+    s32 = Dg.flow_summary(f32["x"], f32["v"], f32["rho"], case.ptype, case.m0, case.g, case.interior)
+    return {"workload": "3-D dam break at scale, full physics, FP32 ensemble vs FP64 drop-in", "particles": N,
+            "fluid": int((case.ptype == 2).sum()), "steps": steps, "dx": dx,
+            "fp32": {"value": N * steps / t32, "unit": "particle-steps/s", "seconds": t32, "tuning": tuning},
+            "fp64": {"value": N * steps / t64, "unit": "particle-steps/s", "seconds": t64},
+            "ratio_fp32_vs_fp64": t64 / t32, "fp32_error_vs_fp64": err,
+            "fp32_error_within_1e-4": all(err[k] <= 1e-4 for k in ("rho_minus_rho0", "v", "displacement")),
+            "flow_fp64": s64, "flow_fp32": s32, "flow_fp32_vs_fp64": Dg.compare_summaries(s32, s64, start)}
+
+
+def run_c3(args):
+    import torch
+    torch.cuda.set_device(0)
+    import __graft_entry__ as ge
+    g = ge.load_package()
+    out = dict(metric="particle-steps/s", **c3_measure(g, args.c3_steps, args.c3_dx))
     print(json.dumps(out))
     return 0
+
+
+def run_long_horizon(g, case, steps, oracle_summary=None):
+    """The dam break over its full horizon: `steps` SPH steps from the
+    initial state as one stepsolve!(prob, steps) call on the FP64 drop-in,
+    and as many steps of the same case on the batched FP32 path; the flow
+    checks of each (mass, energy, surge front), compared with each other and
+    with the CPU oracle's run of the same steps when it is given."""
+    import numpy as np
+    import torch
+    Dg = g.diagnostics
+    start = Dg.flow_summary(case.x, np.zeros_like(case.x), case.rho, case.ptype, case.m0, case.g, case.interior)
+    system, prob = new_fp64_problem(g, case)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    prob.stepsolve(steps)
+    torch.cuda.synchronize()
+    t64 = time.perf_counter() - t0
+    s64 = Dg.flow_summary(torch.stack(system.points).cpu().numpy(), torch.stack(prob.v).cpu().numpy(),
+                          prob.rho.cpu().numpy(), case.ptype, case.m0, case.g, case.interior)
+    prob.close()
+    system.close()
+    ens = g.Ensemble(case.D)
+    slot = ens.add(g.spec_from_case(case))
+    ens.step(steps)
+    s32 = Dg.flow_summary(ens.get(slot, "x"), ens.get(slot, "v"), ens.get(slot, "rho"), case.ptype, case.m0, case.g,
+                          case.interior)
+    ens.close()
+    d32 = Dg.compare_summaries(s32, s64, start)
+    out = {"steps": steps, "physical_time_s": steps * case.dt, "start": start, "fp64": s64, "fp32_ensemble": s32,
+           "fp64_seconds": t64, "fp32_vs_fp64": d32, "fp32_vs_fp64_within_tolerance": not Dg.within(d32, Dg.TOL_FP32),
+           "tolerance_fp32_vs_fp64": Dg.TOL_FP32, "tolerance_fp64_vs_oracle": Dg.TOL_FP64,
+           "checks": "mass = m0 x fluid particles inside the tank; kinetic = 0.5 m0 sum|v|^2; energy change = "
+                     "kinetic + potential since the start, relative to the potential energy released; "
+                     "front = max x of the fluid"}
+    if oracle_summary is not None:
+        d64 = Dg.compare_summaries(s64, oracle_summary, start)
+        out.update({"oracle": oracle_summary, "fp64_vs_oracle": d64,
+                    "fp64_vs_oracle_within_tolerance": not Dg.within(d64, Dg.TOL_FP64)})
+    return out
 
 
 def run_gb300(args):
@@ -569,13 +675,7 @@ def run_gb300(args):
     case = make_case(g)
     D, N = case.D, case.N
 
-    def new_problem():
-        system = g.GPUCellList(tuple(case.x), case.cellsize, case.dist)
-        prob = g.SPHProblem(system, case.dx, case.h, case.H, g.WendlandC2(dim=D), case.rho, case.ptype, case.rho0,
-                            case.m0, case.dt, case.alpha, case.c0, case.gamma, case.delta, case.CFL)
-        return system, prob
-
-    system, prob = new_problem()
+    system, prob = new_fp64_problem(g, case)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
 
     def barrier():
@@ -615,12 +715,7 @@ def run_gb300(args):
         flush.fill_(float(i))
         prob.stepsolve(SUB)
     barrier()
-    import ctypes as C
-    fam = {}
-    for tid in range(L.gcsph_timing_count()):
-        n_ = C.c_int64(); t_ = C.c_double()
-        L.gcsph_timing_get(tid, C.byref(n_), C.byref(t_))
-        fam[L.gcsph_timing_name(tid).decode()] = (int(n_.value), float(t_.value))
+    fam = timer_families(L)
     L.gcsph_timing_enable(0)
     # the roofline covers the pair-sum kernel (pass A, stage 1), the hottest single kernel; the
     # neighbour build is a family of six short kernels (its split is in kernel_ms)
@@ -631,7 +726,7 @@ def run_gb300(args):
     hv = torch.empty((D, N), dtype=torch.float64).pin_memory()
     hr = torch.empty(N, dtype=torch.float64).pin_memory()
     hx.copy_(torch.from_numpy(case.x)); hv.zero_(); hr.copy_(torch.from_numpy(case.rho))
-    system2, prob2 = new_problem()
+    system2, prob2 = new_fp64_problem(g, case)
     h2d = d2h = (2 * D + 1) * N * 8
     e_st = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     e_en = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
@@ -659,30 +754,35 @@ def run_gb300(args):
     ms_e2e = sum(e_st[i].elapsed_time(e_en[i]) for i in range(args.steps))
     ms_e2e = max_over_ranks(ms_e2e)
     e2e = ws * N * SUB * args.steps / (ms_e2e / 1e3)
+    prob2.close()
+    system2.close()
     if rank != 0:
         return 0
     # ---------------- roofline of the dominant kernel family
     peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
         peaks = json.load(open(peaks_path))
-        hbm_peak, peak_src = float(peaks["hbm_gbs"]), "measured"
+        hbm_peak, peak_src = float(peaks["hbm_gbs"]), "measured (MEASURED_PEAKS.json hbm_gbs, STREAM-style copy)"
     except Exception:
         hbm_peak, peak_src = 6800.0, "fallback"
     nl, tms = fam[top]
     avg_s = tms / 1e3 / max(nl, 1)
-    if top in ("stage1", "stage2"):
-        alg = algorithmic_bytes_per_stage(case, npairs)
-    else:
-        alg = None
+    stage = top in ("stage1", "stage2")
+    alg = gather_stage_bytes(case, npairs) if stage else None
     achieved = (alg / avg_s / 1e9) if alg else None
-    roof = {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+    roof = {"bound": "hbm", "kernel": "pass A, stage 1 (k_pairA<2,1>)" if top == "stage1" else top,
+            "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
             "frac": (achieved / hbm_peak) if achieved else None,
             "traffic": PAIRA_STAGE1_DRAM_BYTES if top == "stage1" else None, "peak_source": peak_src,
             "avg_launch_us": avg_s * 1e6, "alg_bytes_per_launch": alg,
+            "alg_bytes_rule": "gather-form pair-sum stage: N(24D+28) + 2P*4 (P = pairs k<m)",
+            "traffic_design": design_stage_bytes(case, npairs) if stage else None,
+            "traffic_design_rule": "this design's pass A: N(16D+28) + P(16 + 2(16+16D)) (pair quads read, "
+                                   "both entry slots written; pass B sums them from L2)",
             "fp64_pipe_frac_ncu": PAIRA_STAGE1_FP64_PIPE if top == "stage1" else None,
-            "note": "pair-once pass A is FP64-pipe bound (2 FP64 instr/cycle/SM on GB300, ncu: 78% of that "
-                    "peak); its working set stays in L2, so the HBM fraction against the measured copy "
-                    "bandwidth is small by construction; 'fp64' is the algorithmic-flop side of the roofline"}
+            "note": "pass A is FP64-pipe bound (GB300 issues 2 FP64 instr/cycle/SM); its working set stays in "
+                    "L2, so the HBM fraction against the measured copy bandwidth is small by construction; the "
+                    "fp64_* keys are the algorithmic-flop side of the same roofline"}
     if top == "stage1":
         # the compute side: the reference's per-pair flops over the measured launch time, against
         # the FP64 peak of 2 DFMA (4 flops) per cycle per SM at the SM clock sampled under load
@@ -693,50 +793,55 @@ def run_gb300(args):
             sms = torch.cuda.get_device_properties(local).multi_processor_count
             mhz = clk.summary().get("sm_mhz") or 2070.0
             fp64_peak = 4.0 * sms * mhz * 1e6
-            roof["fp64"] = {"achieved": flops / avg_s / 1e12, "peak": fp64_peak / 1e12, "unit": "TFLOP/s",
-                            "frac": flops / avg_s / fp64_peak, "flops_per_launch": flops, "pairs": kinds,
-                            "peak_source": f"ncu DFMA peak_sustained 2/cycle/SM x {sms} SMs x {mhz:.0f} MHz",
-                            "state": "pairs and branches counted at the state after the timed steps"}
+            roof.update({"fp64_achieved_tflops": flops / avg_s / 1e12, "fp64_peak_tflops": fp64_peak / 1e12,
+                         "fp64_frac": flops / avg_s / fp64_peak, "fp64_flops_per_launch": flops,
+                         "fp64_peak_source": f"ncu-derived: DFMA peak_sustained 2/cycle/SM x {sms} SMs x "
+                                             f"{mhz:.0f} MHz (sampled SM clock); MEASURED_PEAKS.json has no FP64 entry",
+                         "fp64_pairs_by_kind": kinds,
+                         "fp64_state": "pairs and branches counted at the state after the timed steps"})
         except Exception as e:  # noqa: BLE001
-            roof["fp64"] = {"unavailable": f"{type(e).__name__}: {e}"}
-    cpu = None
+            roof["fp64_unavailable"] = f"{type(e).__name__}: {e}"
+    graphs = dict(zip(("captured", "replayed"), prob.graph_stats()))
+    prob.close()
+    system.close()
+    cpu, oracle_summary = None, None
     if not args.no_cpu_baseline:
         try:
-            from oracle import oracle as orc
-            v, n, el = cpu_baseline(case, args.cpu_seconds, 1)
-            cpu = {"value": v, "unit": "particle-steps/s", "cores": 1, "kind": "port",
-                   "sample": f"{n} SPH steps of the same workload in {el:.1f} s, serial oracle"}
+            v_, el, oracle_summary, build = cpu_baseline(g, case, args.long_horizon_steps)
+            cpu = {"value": v_, "unit": "particle-steps/s", "cores": 1, "kind": "port",
+                   "sample": f"stepsolve!(prob, {args.long_horizon_steps}) on the full workload from its initial "
+                             f"state in {el:.1f} s, serial oracle ({build}, -O3)"}
         except Exception as e:  # noqa: BLE001
             cpu = {"value": None, "unit": "particle-steps/s", "cores": 0, "kind": "port", "sample": f"failed: {e}"}
     out = {"metric": "particle-steps/s", "value": value, "unit": "particle-steps/s", "n_gpus": ws,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
            "config": {"workload": WORKLOAD, "particles": N, "pairs": npairs, "sph_steps_per_bench_step": SUB,
-                      "l2": "flushed (256 MB write) between bench steps", "parallelism": f"replicas x{ws}"},
+                      "l2": L2_NOTE, "parallelism": f"replicas x{ws}"},
            "e2e": {"value": e2e, "unit": "particle-steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
            "gpu_launches": launches, "roofline": roof, "cpu_baseline": cpu, "clocks": clk.summary(),
            "kernel_ms": {k: {"launches": v[0], "total_ms": v[1]} for k, v in fam.items() if v[0]},
            "kernel_timing": "library event timers over a second, instrumented pass of the same K bench steps",
-           "graphs": dict(zip(("captured", "replayed"), prob.graph_stats()))}
+           "graphs": graphs}
+
+    def extra(key, fn):
+        try:
+            out[key] = fn()
+        except Exception as e:  # noqa: BLE001
+            out[key] = {"error": repr(e)}
+        torch.cuda.empty_cache()
+
+    if not args.no_long_horizon:
+        extra("long_horizon", lambda: run_long_horizon(g, case, args.long_horizon_steps, oracle_summary))
     if not args.no_celllist:
-        try:
-            out["published_fixture"] = run_fixture(g)
-        except Exception as e:  # noqa: BLE001
-            out["published_fixture"] = {"error": repr(e)}
-        try:
-            out["celllist"] = run_celllist(g)
-        except Exception as e:  # noqa: BLE001
-            out["celllist"] = {"error": repr(e)}
+        extra("published_fixture", lambda: run_fixture(g))
+        extra("celllist", lambda: run_celllist(g))
     if not args.no_batched:
-        try:
-            out["batched_fp32"] = run_batched(g, args, value / ws)
-        except Exception as e:  # noqa: BLE001
-            out["batched_fp32"] = {"error": repr(e)}
+        extra("batched_fp32", lambda: run_batched(g, args, value / ws, hbm_peak))
+    if not args.no_c3:
+        extra("c3", lambda: c3_measure(g, args.c3_steps, args.c3_dx))
     if not args.no_serving:
-        try:
-            out["serving"] = run_serving(g, args)
-        except Exception as e:  # noqa: BLE001
-            out["serving"] = {"error": repr(e)}
+        extra("serving", lambda: run_serving(g, args))
     print(json.dumps(out))
     if ws > 1:
         import torch.distributed as dist

@@ -12,7 +12,7 @@ from .celllist import GPUCellList, update, partialupdate, neighborlist, neighbor
 from .sphproblem import (SPHProblem, WendlandC2, stepsolve, timesolve, get_points, get_velocity, get_density,
                          get_pressure, get_acceleration, get_dpccorr, get_simtime, get_dt, get_sumw, get_sumgradw,
                          get_ptype)
-from . import kernels, workloads, ensemble, serving, vtkio
+from . import kernels, workloads, ensemble, serving, vtkio, diagnostics
 from .vtkio import writevtk, writecsv
 from .ensemble import Ensemble, InstanceSpec, spec_from_case
 
@@ -20,4 +20,4 @@ __all__ = ["GcsphError", "GPUCellList", "update", "partialupdate", "neighborlist
            "SPHProblem", "WendlandC2", "stepsolve", "timesolve", "get_points", "get_velocity", "get_density",
            "get_pressure", "get_acceleration", "get_dpccorr", "get_simtime", "get_dt", "get_sumw", "get_sumgradw",
            "get_ptype", "kernels", "workloads", "launch_count", "load_library", "lib_path", "ensemble", "Ensemble",
-           "InstanceSpec", "spec_from_case", "serving", "vtkio", "writevtk", "writecsv"]
+           "InstanceSpec", "spec_from_case", "serving", "vtkio", "writevtk", "writecsv", "diagnostics"]

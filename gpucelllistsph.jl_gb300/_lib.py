@@ -89,6 +89,7 @@ _SIGS = {
     "gcl_maxpairs": (C.c_int, [vp, C.POINTER(i64)]),
     "gcl_pairs_noalloc": (C.c_int, [i32, i64, PP, C.POINTER(f64), f64, C.POINTER(f64), C.POINTER(f64), vp, i64,
                                     C.c_int, C.POINTER(i64), vp]),
+    "gcl_pairs_noalloc_init": (C.c_int, []),
     "sph_create": (C.c_int, [vp, C.POINTER(gcsph_params), vp, PP, vp, C.POINTER(vp)]),
     "sph_destroy": (None, [vp]),
     "sph_set_params": (C.c_int, [vp, C.POINTER(gcsph_params)]),

@@ -25,28 +25,72 @@ namespace gcsph {
 static constexpr int TPB = 256;
 
 // ---------------------------------------------------------------------------
-// min/max reduction for the grid bounds (celllist.jl:41-43)
+// min/max reduction for the grid bounds (celllist.jl:41-43), every dimension
+// in one launch (blockIdx.y = dimension).  Julia's minimum/maximum propagate
+// NaN and the constructor's ceil(Int, NaN) then throws; a NaN coordinate
+// makes that block's minimum NaN so that the host can refuse the set.
 // ---------------------------------------------------------------------------
-__global__ void k_minmax(const double* __restrict__ x, int64_t N, double* __restrict__ part) {
+__global__ void k_minmax(const double* __restrict__ x0, const double* __restrict__ x1,
+                         const double* __restrict__ x2, int64_t N, double* __restrict__ part) {
+  const double* __restrict__ x = blockIdx.y == 0 ? x0 : (blockIdx.y == 1 ? x1 : x2);
   double mn = INFINITY, mx = -INFINITY;
+  bool nan = false;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x) {
     double v = x[i];
+    nan |= v != v;
     mn = fmin(mn, v);
     mx = fmax(mx, v);
   }
+  nan = __any_sync(0xffffffffu, nan);
   for (int o = 16; o > 0; o >>= 1) {
     mn = fmin(mn, __shfl_xor_sync(0xffffffffu, mn, o));
     mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
   }
   __shared__ double smn[TPB / 32], smx[TPB / 32];
+  __shared__ int snan[TPB / 32];
   int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  if (lane == 0) { smn[w] = mn; smx[w] = mx; }
+  if (lane == 0) { smn[w] = mn; smx[w] = mx; snan[w] = nan; }
   __syncthreads();
   if (threadIdx.x == 0) {
-    for (int k = 1; k < TPB / 32; ++k) { mn = fmin(mn, smn[k]); mx = fmax(mx, smx[k]); }
-    part[2 * blockIdx.x] = mn;
-    part[2 * blockIdx.x + 1] = mx;
+    for (int k = 1; k < TPB / 32; ++k) { mn = fmin(mn, smn[k]); mx = fmax(mx, smx[k]); nan |= snan[k] != 0; }
+    double* p = part + 2 * ((int64_t)blockIdx.y * gridDim.x + blockIdx.x);
+    p[0] = nan ? NAN : mn;
+    p[1] = mx;
   }
+}
+
+// blocks of k_minmax per dimension: four per SM of the current device, at
+// most MINMAX_MAX_BLOCKS
+int minmax_blocks() {
+  int dev = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms < 1) {
+    cudaGetLastError();
+    sms = 1;
+  }
+  return 4 * sms < MINMAX_MAX_BLOCKS ? 4 * sms : MINMAX_MAX_BLOCKS;
+}
+
+// the bounding box of the D coordinate arrays: one launch, one read-back of
+// the per-block partials (part_dev, part_host: 2 * D * nb doubles), one wait
+int bounding_box(int D, const double* const* x, int64_t N, int nb, double* part_dev, double* part_host,
+                 cudaStream_t st, double* mn, double* mx) {
+  k_minmax<<<dim3(nb, D), TPB, 0, st>>>(x[0], x[1], D == 3 ? x[2] : x[0], N, part_dev);
+  GC_LAUNCHED();
+  GC_CUDA(cudaMemcpyAsync(part_host, part_dev, sizeof(double) * 2 * D * nb, cudaMemcpyDeviceToHost, st));
+  GC_CUDA(cudaStreamSynchronize(st));
+  for (int d = 0; d < D; ++d) {
+    double a = INFINITY, b = -INFINITY;
+    for (int k = 0; k < nb; ++k) {
+      const double* p = part_host + 2 * ((int64_t)d * nb + k);
+      if (p[0] != p[0]) return fail(GCSPH_EINVAL, "NaN coordinate in dimension %d: no cell grid", d + 1);
+      a = fmin(a, p[0]);
+      b = fmax(b, p[1]);
+    }
+    mn[d] = a;
+    mx[d] = b;
+  }
+  return GCSPH_OK;
 }
 
 // ---------------------------------------------------------------------------
@@ -317,24 +361,16 @@ int CellCore::init(int D_, int64_t N_, const double* cellsize, double dist_, con
   const double seps = 1.4901161193847656e-08;  // sqrt(eps(Float64)) = 2^-26
   double mn[3], mx[3];
   if (!MIN || !MAX) {
-    const int nb = 4 * 152;
+    const int nb = minmax_blocks();
     DevBuf part;
-    int rc = part.ensure(sizeof(double) * 2 * nb, st);
+    int rc = part.ensure(sizeof(double) * 2 * D * nb, st);
     if (rc) return rc;
     double* hp = nullptr;
-    GC_CUDA(cudaMallocHost((void**)&hp, sizeof(double) * 2 * nb));
-    for (int d = 0; d < D; ++d) {
-      k_minmax<<<nb, TPB, 0, st>>>(xin[d], N, part.as<double>());
-      GC_LAUNCHED();
-      GC_CUDA(cudaMemcpyAsync(hp, part.p, sizeof(double) * 2 * nb, cudaMemcpyDeviceToHost, st));
-      GC_CUDA(cudaStreamSynchronize(st));
-      double a = INFINITY, b = -INFINITY;
-      for (int k = 0; k < nb; ++k) { a = fmin(a, hp[2 * k]); b = fmax(b, hp[2 * k + 1]); }
-      mn[d] = a;
-      mx[d] = b;
-    }
+    GC_CUDA(cudaMallocHost((void**)&hp, sizeof(double) * 2 * D * nb));
+    rc = bounding_box(D, xin, N, nb, part.as<double>(), hp, st, mn, mx);
     cudaFreeHost(hp);
     part.release();
+    if (rc) return rc;
   }
   int64_t ncell = 1;
   for (int d = 0; d < D; ++d) {
@@ -955,7 +991,10 @@ int gcl_maxpairs(gcl_handle* h, int64_t* out) {
 // __device__ arena sized for GCSPH_NOALLOC_MAX_POINTS points and
 // GCSPH_NOALLOC_MAX_CELLS grid cells; each GPU that loads this library keeps
 // that arena (24 MiB) until the process exits.  The caller passes the
-// coordinates and owns the output pair buffer.
+// coordinates and owns the output pair buffer.  CUDA reserves the arena when
+// it loads this file's module, which under lazy module loading happens at
+// the first use, so gcl_pairs_noalloc_init (or a first call) must come
+// before the caller's own pool takes the device's memory.
 // ===========================================================================
 namespace gcsph {
 namespace noalloc {
@@ -963,11 +1002,6 @@ namespace noalloc {
 constexpr int64_t MAXN = GCSPH_NOALLOC_MAX_POINTS;
 constexpr int64_t MAXC = GCSPH_NOALLOC_MAX_CELLS;
 constexpr int64_t al(int64_t b) { return (b + 255) / 256 * 256; }
-constexpr int64_t tile = 2048;  // items per block of the device scan
-constexpr int64_t scan_elems(int64_t m) {
-  return ((m + tile - 1) / tile) <= 1 ? 1 : 2 * ((m + tile - 1) / tile) + 1 + scan_elems((m + tile - 1) / tile);
-}
-constexpr int MINMAX_BLOCKS = 4 * 152;
 // arena layout, byte offsets
 constexpr int64_t O_KEY = 0;
 constexpr int64_t O_SLOT = O_KEY + al(4 * MAXN);
@@ -982,8 +1016,10 @@ constexpr int64_t O_CFULL = O_CSTART + al(4 * (MAXC + 1));
 constexpr int64_t O_CUP = O_CFULL + al(4 * MAXN);
 constexpr int64_t O_RSUP = O_CUP + al(4 * MAXN);
 constexpr int64_t O_SCAN = O_RSUP + al(8 * (MAXN + 1));
-constexpr int64_t O_MINMAX = O_SCAN + al(8 * scan_elems((MAXC > MAXN ? MAXC : MAXN) + 1));
-constexpr int64_t BYTES = O_MINMAX + al(8 * 2 * MINMAX_BLOCKS);
+// the device scan's scratch, sized by the scan's own rule for the longer of
+// the two scans (ncell + 1 and N + 1 items)
+constexpr int64_t O_MINMAX = O_SCAN + al(8 * scan_scratch_elems((MAXC > MAXN ? MAXC : MAXN) + 1));
+constexpr int64_t BYTES = O_MINMAX + al(8 * 2 * 3 * MINMAX_MAX_BLOCKS);
 
 }  // namespace noalloc
 }  // namespace gcsph
@@ -1052,9 +1088,29 @@ __global__ void __launch_bounds__(TPB) k_pairs_direct(const double* __restrict__
 
 static std::mutex g_mu;
 static void* g_arena_of[128] = {nullptr};
+static int g_minmax_blocks_of[128] = {0};
 
-// device address of the arena on the current device; set up once per device
-static int arena(unsigned char** out) {
+// every kernel a call can launch, loaded into the current context now: with
+// lazy module loading (the CUDA default) each is otherwise loaded at its
+// first launch, which takes device memory for its code
+template <int D>
+static int preload_dim() {
+  cudaFuncAttributes a;
+  const void* fns[] = {(const void*)k_cellkey<D>,           (const void*)k_gather_pos<D>,
+                       (const void*)k_pairs<D, 0, 1>,       (const void*)k_pairs<D, 0, 2>,
+                       (const void*)k_pairs<D, 0, 4>,       (const void*)k_pairs<D, 0, 8>,
+                       (const void*)k_pairs<D, 0, 16>,      (const void*)k_pairs<D, 0, 32>,
+                       (const void*)k_pairs_direct<D, 1>,   (const void*)k_pairs_direct<D, 2>,
+                       (const void*)k_pairs_direct<D, 4>,   (const void*)k_pairs_direct<D, 8>,
+                       (const void*)k_pairs_direct<D, 16>,  (const void*)k_pairs_direct<D, 32>};
+  for (const void* f : fns) GC_CUDA(cudaFuncGetAttributes(&a, f));
+  return GCSPH_OK;
+}
+
+// device address of the arena on the current device, and this device's
+// bounding-box grid; set up once per device, with the device's kernels
+// loaded at the same time
+static int arena(unsigned char** out, int* minmax_nb) {
   int dev = 0;
   GC_CUDA(cudaGetDevice(&dev));
   if (dev < 0 || dev >= 128) return fail(GCSPH_EINVAL, "device ordinal %d out of range", dev);
@@ -1063,9 +1119,19 @@ static int arena(unsigned char** out) {
     void* p = nullptr;
     cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_arena);
     if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(g_noalloc_arena)", __FILE__, __LINE__);
+    cudaFuncAttributes a;
+    const void* fns[] = {(const void*)k_minmax, (const void*)k_scatter_arrival, (const void*)k_rank_in_cell,
+                         (const void*)k_apply_perm};
+    for (const void* f : fns) GC_CUDA(cudaFuncGetAttributes(&a, f));
+    int rc = preload_dim<2>();
+    if (!rc) rc = preload_dim<3>();
+    if (!rc) rc = scan_preload();
+    if (rc) return rc;
+    g_minmax_blocks_of[dev] = minmax_blocks();
     g_arena_of[dev] = p;
   }
   *out = (unsigned char*)g_arena_of[dev];
+  if (minmax_nb) *minmax_nb = g_minmax_blocks_of[dev];
   return GCSPH_OK;
 }
 
@@ -1073,7 +1139,8 @@ template <int D>
 static int run(int64_t N, const double* const* x, const double* cellsize, double dist, const double* MIN,
                const double* MAX, int32_t* pairs, int64_t cap, int fillzero, int64_t* pairsn, cudaStream_t st) {
   unsigned char* A = nullptr;
-  int rc = arena(&A);
+  int nb = 0;
+  int rc = arena(&A, &nb);
   if (rc) return rc;
   int32_t* key = (int32_t*)(A + O_KEY);
   int32_t* slot = (int32_t*)(A + O_SLOT);
@@ -1093,23 +1160,15 @@ static int run(int64_t N, const double* const* x, const double* cellsize, double
   const double seps = 1.4901161193847656e-08;  // sqrt(eps(Float64)) = 2^-26
   Grid g{};
   int64_t ncell = 1;
+  double bmin[3] = {0, 0, 0}, bmax[3] = {0, 0, 0};
+  if (!MIN || !MAX) {
+    // pageable host copy of the per-block partials, on the stack (48 KB)
+    double host[2 * 3 * MINMAX_MAX_BLOCKS];
+    if ((rc = bounding_box(D, x, N, nb, mm, host, st, bmin, bmax))) return rc;
+  }
   for (int d = 0; d < D; ++d) {
-    double lo, hi;
-    if (!MIN || !MAX) {
-      double host[2 * MINMAX_BLOCKS];  // pageable stack copy of the per-block partials
-      k_minmax<<<MINMAX_BLOCKS, TPB, 0, st>>>(x[d], N, mm);
-      GC_LAUNCHED();
-      GC_CUDA(cudaMemcpyAsync(host, mm, sizeof(host), cudaMemcpyDeviceToHost, st));
-      GC_CUDA(cudaStreamSynchronize(st));
-      lo = INFINITY;
-      hi = -INFINITY;
-      for (int b = 0; b < MINMAX_BLOCKS; ++b) {
-        lo = fmin(lo, host[2 * b]);
-        hi = fmax(hi, host[2 * b + 1]);
-      }
-    }
-    if (MIN) lo = MIN[d];
-    if (MAX) hi = MAX[d];
+    double lo = MIN ? MIN[d] : bmin[d];
+    double hi = MAX ? MAX[d] : bmax[d];
     const double cs = cellsize[d] < dist ? dist : cellsize[d];
     lo = lo - fabs((lo + seps) * seps);
     const double c = ceil((hi - lo) / cs);
@@ -1209,4 +1268,9 @@ extern "C" int gcl_pairs_noalloc(int32_t D, int64_t N, const double* const* x_de
                                   pairsn_out, st)
                 : noalloc::run<3>(N, x_dev, cellsize, dist, MIN_or_null, MAX_or_null, pairs_dev, cap, fillzero,
                                   pairsn_out, st);
+}
+
+extern "C" int gcl_pairs_noalloc_init(void) {
+  unsigned char* A = nullptr;
+  return gcsph::noalloc::arena(&A, nullptr);
 }

@@ -58,6 +58,14 @@ __device__ inline void pf_thresholds_last_block(unsigned long long* bmax, double
   }
 }
 
+// bounding box of D coordinate arrays (celllist.jl:41-43) with one launch
+// of nb blocks per dimension and one wait; a NaN coordinate is refused with
+// GCSPH_EINVAL.  part_dev and part_host hold 2 * D * nb doubles.
+constexpr int MINMAX_MAX_BLOCKS = 1024;
+int minmax_blocks();
+int bounding_box(int D, const double* const* x, int64_t N, int nb, double* part_dev, double* part_host,
+                 cudaStream_t st, double* mn, double* mx);
+
 struct CellCore {
   int D = 2;
   int64_t N = 0;

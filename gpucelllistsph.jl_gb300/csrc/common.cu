@@ -178,9 +178,6 @@ void DevBuf::release() {
 // Exclusive scan: 256 threads x 8 items per block, block totals scanned
 // recursively, then added back.  No block ever waits on another block.
 // ---------------------------------------------------------------------------
-static constexpr int SCAN_THREADS = 256;
-static constexpr int SCAN_ITEMS = 8;
-static constexpr int64_t SCAN_TILE = (int64_t)SCAN_THREADS * SCAN_ITEMS;
 
 template <class TIn, class TOut>
 __global__ void __launch_bounds__(SCAN_THREADS) k_scan_tile(const TIn* __restrict__ in, TOut* __restrict__ out,
@@ -229,13 +226,6 @@ template <class TOut>
 __global__ void k_scan_add(TOut* __restrict__ out, int64_t m, const int64_t* __restrict__ boff) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < m) out[i] = (TOut)((long long)out[i] + boff[i / SCAN_TILE]);
-}
-
-int64_t scan_scratch_elems(int64_t m) {
-  int64_t nb = (m + SCAN_TILE - 1) / SCAN_TILE;
-  if (nb < 1) nb = 1;
-  if (nb == 1) return 1;
-  return 2 * nb + 1 + scan_scratch_elems(nb);
 }
 
 // one block walks the whole array in tiles of 1024 x 8 items, carrying the
@@ -311,7 +301,7 @@ __global__ void __launch_bounds__(1024) k_scan_single(const TIn* __restrict__ in
 
 template <class TIn, class TOut>
 static int scan_impl(const TIn* in, TOut* out, int64_t n_in, int64_t m, int64_t* scratch, cudaStream_t s) {
-  if (m <= 65536) {
+  if (m <= SCAN_SINGLE_MAX) {
     k_scan_single<TIn, TOut><<<1, 1024, 0, s>>>(in, out, nullptr, nullptr, n_in, m);
     GC_LAUNCHED();
     return GCSPH_OK;
@@ -338,7 +328,7 @@ int exclusive_scan_i32_to_i32(const int32_t* in, int32_t* out, int64_t n, int64_
 }
 int exclusive_scan2_i32_to_i64(const int32_t* in0, int64_t* out0, const int32_t* in1, int64_t* out1, int64_t n,
                                int64_t* scratch, cudaStream_t s) {
-  if (n + 1 <= 65536) {
+  if (n + 1 <= SCAN_SINGLE_MAX) {
     k_scan_single<int32_t, int64_t><<<2, 1024, 0, s>>>(in0, out0, in1, out1, n, n + 1);
     GC_LAUNCHED();
     return GCSPH_OK;
@@ -346,6 +336,17 @@ int exclusive_scan2_i32_to_i64(const int32_t* in0, int64_t* out0, const int32_t*
   int rc = scan_impl<int32_t, int64_t>(in0, out0, n, n + 1, scratch, s);
   if (rc) return rc;
   return scan_impl<int32_t, int64_t>(in1, out1, n, n + 1, scratch, s);
+}
+
+int scan_preload() {
+  cudaFuncAttributes a;
+  const void* fns[] = {
+      (const void*)k_scan_single<int32_t, int32_t>, (const void*)k_scan_single<int32_t, int64_t>,
+      (const void*)k_scan_single<int64_t, int64_t>, (const void*)k_scan_tile<int32_t, int32_t>,
+      (const void*)k_scan_tile<int32_t, int64_t>,   (const void*)k_scan_tile<int64_t, int64_t>,
+      (const void*)k_scan_add<int32_t>,             (const void*)k_scan_add<int64_t>};
+  for (const void* f : fns) GC_CUDA(cudaFuncGetAttributes(&a, f));
+  return GCSPH_OK;
 }
 
 }  // namespace gcsph

@@ -174,8 +174,23 @@ __device__ inline double warp_max(double v) {
 // device exclusive scan (3 phases, no inter-block waiting)
 // ----------------------------------------------------------------------------
 // out[i] = sum_{j<i} in[j] for i in [0, n]; out[n] = total.  scratch must
-// hold scan_scratch_elems(n) int64 values.
-int64_t scan_scratch_elems(int64_t n);
+// hold scan_scratch_elems(n + 1) int64 values.  Arrays of up to
+// SCAN_SINGLE_MAX items take one single-block launch; longer ones are
+// scanned in tiles of SCAN_TILE items, with the tile totals scanned
+// recursively in the scratch.
+constexpr int SCAN_THREADS = 256;
+constexpr int SCAN_ITEMS = 8;
+constexpr int64_t SCAN_TILE = (int64_t)SCAN_THREADS * SCAN_ITEMS;
+constexpr int64_t SCAN_SINGLE_MAX = 65536;
+constexpr int64_t scan_scratch_elems(int64_t m) {
+  return (m + SCAN_TILE - 1) / SCAN_TILE <= 1
+             ? 1
+             : 2 * ((m + SCAN_TILE - 1) / SCAN_TILE) + 1 + scan_scratch_elems((m + SCAN_TILE - 1) / SCAN_TILE);
+}
+// load every scan kernel into the current context now (a process with lazy
+// module loading otherwise loads each at its first launch, which needs
+// device memory for its code)
+int scan_preload();
 int exclusive_scan_i32_to_i64(const int32_t* in, int64_t* out, int64_t n, int64_t* scratch,
                               cudaStream_t s);
 int exclusive_scan_i32_to_i32(const int32_t* in, int32_t* out, int64_t n, int64_t* scratch,

@@ -38,6 +38,7 @@ class Case:
     g: float = 9.81
     s: float = 0.0
     extra: dict = field(default_factory=dict)   # mutable fields set after construction
+    interior: tuple = None   # per dimension (lo, hi) of the tank interior, for the flow checks
 
     @property
     def D(self):
@@ -83,7 +84,8 @@ def dam_break_2d(dx=0.02, fluid=(1.0, 2.0), tank=(4.0, 3.0), layers=3, layer_pty
     g = 9.81
     return Case(x=np.ascontiguousarray(x), rho=np.full(x.shape[1], float(rho)), ptype=ptype, dx=dx, h=h, H=H,
                 dist=dist, cellsize=(dist, dist), rho0=rho0, m0=rho0 * dx * dx, dt=1e-5, alpha=0.01,
-                c0=math.sqrt(g * 2) * 20, gamma=7, delta=0.1, CFL=0.2, g=g)
+                c0=math.sqrt(g * 2) * 20, gamma=7, delta=0.1, CFL=0.2, g=g,
+                interior=((0.0, float(tank[0])), (0.0, math.inf)))
 
 
 def dam_break_3d(dx=0.01, fluid=(1.0, 2.0, 0.5), tank=(4.0, 3.0, 1.0), layers=3, layer_ptype=None, rho=1000.0,
@@ -126,7 +128,8 @@ def dam_break_3d(dx=0.01, fluid=(1.0, 2.0, 0.5), tank=(4.0, 3.0, 1.0), layers=3,
     g = 9.81
     c = Case(x=x, rho=np.full(x.shape[1], float(rho)), ptype=ptype, dx=dx, h=h, H=H, dist=dist,
              cellsize=(dist, dist, dist), rho0=rho0, m0=rho0 * dx * dx * dx, dt=1e-5, alpha=0.01,
-             c0=math.sqrt(g * 2) * 20, gamma=7, delta=0.1, CFL=0.2, g=g)
+             c0=math.sqrt(g * 2) * 20, gamma=7, delta=0.1, CFL=0.2, g=g,
+             interior=((0.0, float(L)), (0.0, math.inf), (0.0, float(W))))
     if full_physics:
         c.s = 0.05
         c.extra = dict(nu=0.2, dpc_l0=0.005, dpc_lambda=0.005, dpc_pmax=36000.0, xsph_eps=0.5)

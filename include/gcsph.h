@@ -99,17 +99,32 @@ int gcl_maxpairs(gcl_handle* h, int64_t* out);
  * in one static device array (24 MiB, kept by every GPU that loads the
  * library until the process exits) sized for at most
  * GCSPH_NOALLOC_MAX_POINTS points and GCSPH_NOALLOC_MAX_CELLS grid cells;
- * larger inputs are rejected with GCSPH_EINVAL.  Output: the same (min,max)
- * 1-based list, in the same order, that gcl_create + gcl_emit_pairs give;
- * GCSPH_ECAPACITY and the full count when it does not fit in cap.  The first
- * call on a device looks up the array's device address (make that first call
- * before any stream capture).  Calls share the array: two calls that overlap
- * on the GPU (different streams, threads) race and corrupt each other. */
+ * larger inputs are rejected with GCSPH_EINVAL, and so is a NaN coordinate
+ * when MIN/MAX are null (the reference's grid of such a set is an error).
+ * Output: the same (min,max) 1-based list, in the same order, that
+ * gcl_create + gcl_emit_pairs give; GCSPH_ECAPACITY and the full count when
+ * it does not fit in cap.  Every call waits for `stream` before it returns:
+ * it reads the bounding box (when MIN/MAX are null) and the pair count back
+ * to the host.  Calls share the array: two calls that overlap on the GPU
+ * (different streams, threads) race and corrupt each other.
+ *
+ * CUDA reserves the static array, and loads the kernels of the call, when
+ * the library's code is first used on a device (lazy module loading, the
+ * CUDA default), and that needs free device memory.  A caller whose own
+ * pool is about to take the device's memory calls gcl_pairs_noalloc_init()
+ * first, with the device current: it looks up the array's device address
+ * and loads every kernel the call launches, once per device.  Otherwise the
+ * first gcl_pairs_noalloc call on a device does this set-up itself; make
+ * that first call (or the init) before any stream capture. */
 #define GCSPH_NOALLOC_MAX_POINTS 262144
 #define GCSPH_NOALLOC_MAX_CELLS 1048576
 int gcl_pairs_noalloc(int32_t D, int64_t N, const double* const* x_dev, const double* cellsize, double dist,
                       const double* MIN_or_null, const double* MAX_or_null, int32_t* pairs_dev, int64_t cap,
                       int fillzero, int64_t* pairsn_out, void* stream);
+/* No counterpart in the reference: the set-up of gcl_pairs_noalloc on the
+ * current device (see above); allocates nothing itself, returns 0 or
+ * GCSPH_ECUDA. */
+int gcl_pairs_noalloc_init(void);
 
 /* ---------------------------------------------------------------- SPH problem */
 

@@ -14,8 +14,27 @@ import subprocess
 import numpy as np
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
-_LIB_PATH = os.path.join(_HERE, "_build", "liboracle.so")
+# the parity build (-O2) that the tests check against, and the same source
+# at -O3 that the benchmark times as the CPU baseline (oracle/Makefile)
+_BUILDS = {"parity": os.path.join(_HERE, "_build", "liboracle.so"),
+           "timed": os.path.join(_HERE, "_build", "liboracle_timed.so")}
+_LIB_PATH = _BUILDS["parity"]
 _lib = None
+
+
+def select_build(name: str) -> None:
+    """Choose which build lib() loads: "parity" (default) or "timed".  Must
+    come before the first lib() call of the process."""
+    global _LIB_PATH
+    path = _BUILDS[name]
+    if _lib is not None and path != _LIB_PATH:
+        raise RuntimeError(f"oracle: the {_LIB_PATH} build is already loaded")
+    _LIB_PATH = path
+
+
+def loaded_build() -> str:
+    """The file name of the build lib() loads."""
+    return os.path.basename(_LIB_PATH)
 
 f64p = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
 i32p = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")

@@ -1,7 +1,7 @@
 """Generate the committed golden fixtures from the reference's test inputs.
 
-Run in a container that has the reference checkout (read-only):
-    python tests/golden/make_golden.py /root/reference
+Run where a checkout of the reference exists (read-only), with its path:
+    python tests/golden/make_golden.py <path of the reference checkout>
 Nothing at test time reads the reference; the .npz files written here are
 the fixtures.
 
@@ -145,4 +145,6 @@ def main(ref):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_golden.py <path of the reference checkout>")
+    main(sys.argv[1])

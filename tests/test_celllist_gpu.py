@@ -24,6 +24,21 @@ def _oracle_pairs(orc, x, cs, dist, MIN=None, MAX=None):
     return pairs, n, (c, off, cell, pcell, cpn)
 
 
+def _assert_maxpairs_and_capacity(c, orc, x, cs, dist, MIN=None, MAX=None):
+    """c.maxpairs() equals the oracle's мaxpairs over the oracle's cellpnum
+    (src/gpukernels_cls.jl:109-286), and the pair array's length is the
+    constructor's policy applied to it (src/celllist.jl:69-86): capacity
+    мaxpairs, shrunk to ceil(pairsn / 0.8) when less than 80% full."""
+    D = len(cs)
+    cs_, off, cell = orc.grid(x, cs, dist, MIN, MAX)
+    _, cpn = orc.cellmap(x, cs_, off, cell)
+    mp = orc.maxpairs(D, cpn, cell)
+    assert c.maxpairs() == mp
+    assert mp >= c.pairsn
+    want_cap = math.ceil(c.pairsn / 0.8) if c.pairsn < mp * 0.8 else mp
+    assert c.neighborlist().shape[0] == want_cap
+
+
 def _golden_hash(pairs):
     import importlib.util
     spec = importlib.util.spec_from_file_location("mg", os.path.join(GOLDEN, "make_golden.py"))
@@ -45,11 +60,10 @@ def test_fixture_dp002_pairs_match_golden(gpu_pkg, orc, tag):
     assert int((full[:, 0] != 0).sum()) == c.pairsn
     v = full[: c.pairsn]
     assert (v[:, 0] < v[:, 1]).all() and v.min() >= 1 and v.max() <= c.n
-    # constructor capacity policy, src/celllist.jl:80-86
-    mp = c.maxpairs()
-    assert mp >= c.pairsn
-    want_cap = math.ceil(c.pairsn / 0.8) if c.pairsn < mp * 0.8 else mp
-    assert full.shape[0] == want_cap
+    # мaxpairs (src/gpukernels_cls.jl:109-286) against the oracle's count of
+    # the same cells, and the constructor's capacity policy built on it
+    # (src/celllist.jl:69-86): the list length follows from that count alone
+    _assert_maxpairs_and_capacity(c, orc, z["x"], (dist, dist), dist)
 
 
 def test_fixture_dp004_full_set(gpu_pkg, orc):
@@ -57,6 +71,7 @@ def test_fixture_dp004_full_set(gpu_pkg, orc):
     dist = float(z["pairs_H_dist"])
     c = gpu_pkg.GPUCellList(tuple(z["x"]), (dist, dist), dist)
     assert np.array_equal(_set(orc, c.neighborlistview()), orc.pair_set(z["pairs_H"]))
+    _assert_maxpairs_and_capacity(c, orc, z["x"], (dist, dist), dist)
 
 
 def test_fixture_3d_boundary_hash(gpu_pkg, orc):
@@ -78,6 +93,8 @@ def test_random_sets_match_oracle(gpu_pkg, orc, D, N, dist, seed):
     assert c.grid == tuple(int(v) for v in cell)
     assert np.allclose(c.offset, off, rtol=0, atol=0)
     assert np.array_equal(c.cellpnum.cpu().numpy(), cpn)
+    assert c.maxpairs() == orc.maxpairs(D, cpn, cell)
+    _assert_maxpairs_and_capacity(c, orc, x, (dist,) * D, dist)
 
 
 def test_adversarial_points(gpu_pkg, orc):
@@ -99,6 +116,7 @@ def test_clamped_cells_with_given_box(gpu_pkg, orc):
     pairs, n, _ = _oracle_pairs(orc, x, (dist,) * 3, dist, MIN=(0, 0, 0), MAX=(1, 1, 1))
     assert c.pairsn == n
     assert np.array_equal(_set(orc, c.neighborlistview()), orc.pair_set(pairs))
+    _assert_maxpairs_and_capacity(c, orc, x, (dist,) * 3, dist, MIN=(0, 0, 0), MAX=(1, 1, 1))
 
 
 def test_single_overfull_cell(gpu_pkg, orc):
@@ -170,19 +188,37 @@ def test_emit_into_a_buffer_not_8_byte_aligned(gpu_pkg):
 @pytest.mark.parametrize("D,N,dist", [(2, 200_000, 0.016), (3, 4_000_000, 0.008)])
 def test_full_size_pair_sets(gpu_pkg, orc, D, N, dist):
     """The cell-list configuration at full size: 200k 2-D / 4M 3-D uniform
-    points, pair sets compared with the oracle, then a jittered
+    points, pair sets and мaxpairs compared with the oracle, then a jittered
     partialupdate! compared by count and set."""
     x = gpu_pkg.workloads.uniform_points(N, D)
     c = gpu_pkg.GPUCellList(tuple(x), (dist,) * D, dist)
-    pairs, n, _ = _oracle_pairs(orc, x, (dist,) * D, dist)
+    pairs, n, (_, _, cell, pcell, cpn) = _oracle_pairs(orc, x, (dist,) * D, dist)
     assert c.pairsn == n
-    got = c.neighborlistview().cpu().numpy().astype(np.int64)
-    assert (got[:, 0] < got[:, 1]).all()
-    want = pairs.astype(np.int64)
-    kg = np.sort(got[:, 0] * (1 << 32) + got[:, 1])
-    kw = np.sort(want[:, 0] * (1 << 32) + want[:, 1])
-    assert np.array_equal(kg, kw)
-    assert np.unique(kg).size == kg.size
+    assert c.maxpairs() == orc.maxpairs(D, cpn, cell)
+
+    def same_set(got, want):
+        got = got.astype(np.int64)
+        assert (got[:, 0] < got[:, 1]).all()
+        want = want.astype(np.int64)
+        kg = np.sort(got[:, 0] * (1 << 32) + got[:, 1])
+        kw = np.sort(want[:, 0] * (1 << 32) + want[:, 1])
+        assert np.array_equal(kg, kw)
+        assert np.unique(kg).size == kg.size
+
+    same_set(c.neighborlistview().cpu().numpy(), pairs)
+    del pairs
+    # partialupdate! (src/celllist.jl:141-145): every point jittered by
+    # U(-0.1, 0.1)·dist per coordinate, the pair search re-run with the cell
+    # membership of the build above (stale cells) and the new coordinates;
+    # the oracle does the same with its own stale pcell
+    rng = np.random.default_rng(7)
+    xj = np.ascontiguousarray(x + rng.uniform(-0.1, 0.1, x.shape) * dist)
+    for d in range(D):
+        c.points[d].copy_(torch.from_numpy(xj[d]))
+    c.partialupdate()
+    pj, nj = orc.neib_search(xj, pcell, cell, dist)
+    assert c.pairsn == nj
+    same_set(c.neighborlistview().cpu().numpy(), pj)
 
 
 @pytest.mark.parametrize("D", [2, 3])
@@ -190,7 +226,8 @@ def test_tiny_and_degenerate_sets(gpu_pkg, orc, D):
     """One point (no pairs); two coincident points (r² = 0 < dist²: one pair);
     two points exactly dist apart (the reference's test is strict: no pair);
     every case against the oracle.  An empty set is refused, as the
-    reference's bounding box of no points is an error."""
+    reference's bounding box of no points is an error, and so is a set with
+    a NaN coordinate."""
     dist = 0.1
     cases = {
         "one": np.full((D, 1), 0.5),
@@ -211,3 +248,9 @@ def test_tiny_and_degenerate_sets(gpu_pkg, orc, D):
         assert c.pairsn == want[name], name
     with pytest.raises(RuntimeError):
         gpu_pkg.GPUCellList(tuple(np.zeros((D, 0))), (dist,) * D, dist)
+    # a NaN coordinate: Julia's minimum is NaN and ceil(Int, NaN) throws in
+    # the constructor (src/celllist.jl:41-46); refused here as well
+    bad = np.full((D, 4), 0.5)
+    bad[D - 1, 2] = np.nan
+    with pytest.raises(RuntimeError, match="NaN"):
+        gpu_pkg.GPUCellList(tuple(bad), (dist,) * D, dist)

@@ -126,6 +126,9 @@ def compare(prob, ref, case, fields=FIELDS, rtol=RTOL, exact=True, floor=None):
         lip = case.gamma * P0 * float(np.max(rho_ref / case.rho0)) ** (case.gamma - 1) / case.rho0
         bound = lip * drho + 8 * np.finfo(np.float64).eps * P0 * np.sqrt(rho_ref.size)
         tol["P"] = max(tol["P"], bound / max(np.linalg.norm(P_ref), 1e-300))
+    widened = {k: f"{errs[k]:.2e} <= {tol[k]:.2e}" for k in fields if tol[k] > rtol}
+    print(f"\n[tolerance] normwise errors; fields whose tolerance the noise floor widened past {rtol:g}: "
+          f"{widened or 'none'}; all errors: { {k: float(f'{v:.3e}') for k, v in errs.items()} }")
     bad = {k: (v, tol[k]) for k, v in errs.items() if not v <= tol[k]}
     assert not bad, f"fields over tolerance (err, tol): {bad}"
     if exact:
@@ -153,15 +156,53 @@ def run_both(prob, ref, n, **kw):
     return a
 
 
+def per_element_relerr(got, want):
+    """max_i |got_i - want_i| / |want_i| per particle i, for a vector field
+    with the Euclidean norm of particle i's vector, over the particles whose
+    value is nonzero; a particle whose value is zero must be zero in got as
+    well (inf otherwise)."""
+    got = np.asarray(got, dtype=np.float64)
+    want = np.asarray(want, dtype=np.float64)
+    if want.ndim == 2:
+        dn = np.linalg.norm(got - want, axis=0)
+        wn = np.linalg.norm(want, axis=0)
+    else:
+        dn, wn = np.abs(got - want), np.abs(want)
+    nz = wn != 0
+    if np.any(dn[~nz] != 0):
+        return math.inf
+    return float(np.max(dn[nz] / wn[nz])) if nz.any() else 0.0
+
+
+# per-particle relative bounds of the C1 100-step run on split rows (measured
+# 1.1e-15 for ρ, 2.1e-15 for x); a particle's velocity is compared as a
+# vector, since one component of it can sit near zero
+ELEMENT_BOUNDS = {"rho": 1e-13, "x": 1e-13, "v": 1e-10}
+
+
 @pytest.mark.parametrize("lanes", [1, 0])
 def test_dam_break_2d_c1_100_steps(gpu_pkg, orc, lanes):
     """The plain FP64 configuration: 2-D dam break, dx=0.02, boundary ptype 0,
-    cell list rebuilt every step, 100 steps (CSPM fires at 15, 30, ...)."""
+    cell list rebuilt every step, 100 steps (CSPM fires at 15, 30, ...).
+    Serial rows are bit-identical to the oracle.  The default split rows
+    meet the FP64 contract itself on every field -- 1e-12 normwise, with no
+    noise-floor widening -- and the per-element relative errors of ρ, x and
+    v are reported and bounded."""
     case = gpu_pkg.workloads.dam_break_2d()
     prob, ref = make_pair(gpu_pkg, orc, case, lanes)
     un, _ = run_both(prob, ref, 100)
     assert un == 100
-    check(orc, prob, ref, case, lanes, [(100, {})])
+    if lanes == 1:
+        compare(prob, ref, case, exact=True)
+        return
+    # no floor and no EOS allowance: every field within RTOL as it stands
+    errs = {f: relerr(gpu_field(prob, f), ref.get(f)) for f in FIELDS}
+    over = {f: e for f, e in errs.items() if not e <= RTOL}
+    assert not over, f"fields over {RTOL:g} normwise: {over}"
+    elem = {f: per_element_relerr(gpu_field(prob, f), ref.get(f)) for f in ELEMENT_BOUNDS}
+    print(f"\n[C1 split rows, 100 steps] normwise {errs}\n  per-element relative {elem}")
+    bad = {f: (elem[f], b) for f, b in ELEMENT_BOUNDS.items() if not elem[f] <= b}
+    assert not bad, f"per-element relative errors over their bounds: {bad}"
 
 
 @pytest.mark.parametrize("lanes", [1, 0])
