@@ -105,6 +105,7 @@ _SIGS = {
     "ens_add": (C.c_int, [vp, i64, vp, vp, vp, vp, C.POINTER(gcsph_ens_params), C.POINTER(i32)]),
     "ens_remove": (C.c_int, [vp, i32]),
     "ens_step": (C.c_int, [vp, i32]),
+    "ens_set_stream": (C.c_int, [vp, vp]),
     "ens_get": (C.c_int, [vp, i32, i32, vp]),
     "ens_info": (C.c_int, [vp, i32, C.POINTER(i64), C.POINTER(i64), C.POINTER(f64)]),
     "ens_totals": (C.c_int, [vp, C.POINTER(i32), C.POINTER(i64), C.POINTER(i64)]),

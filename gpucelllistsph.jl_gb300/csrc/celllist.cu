@@ -96,24 +96,28 @@ int bounding_box(int D, const double* const* x, int64_t N, int nb, double* part_
 // ---------------------------------------------------------------------------
 // binning: key, arrival slot, per-cell count (kernel_cellmap!)
 // ---------------------------------------------------------------------------
+// With fold_cnt the last block to finish also scans the counts into
+// cellstart (grids of at most SCAN_FOLD_MAX - 1 cells): no separate scan.
 template <int D>
 __global__ void k_cellkey(const double* __restrict__ x0, const double* __restrict__ x1, const double* __restrict__ x2,
                           int64_t N, Grid g, int32_t* __restrict__ key, int32_t* __restrict__ slot,
-                          int32_t* __restrict__ count) {
+                          int32_t* __restrict__ count, int32_t* __restrict__ cellstart, unsigned* fold_cnt) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= N) return;
-  const double* xs[3] = {x0, x1, x2};
-  int64_t lin = 0, stride = 1;
+  if (i < N) {
+    const double* xs[3] = {x0, x1, x2};
+    int64_t lin = 0, stride = 1;
 #pragma unroll
-  for (int d = 0; d < D; ++d) {
-    double p = (xs[d][i] - g.offset[d]) * g.hinv[d];
-    double c = fmin(fmax(p, 1.0), (double)g.nc[d]);
-    int ci = (int)ceil(c);
-    lin += (int64_t)(ci - 1) * stride;
-    stride *= g.nc[d];
+    for (int d = 0; d < D; ++d) {
+      double p = (xs[d][i] - g.offset[d]) * g.hinv[d];
+      double c = fmin(fmax(p, 1.0), (double)g.nc[d]);
+      int ci = (int)ceil(c);
+      lin += (int64_t)(ci - 1) * stride;
+      stride *= g.nc[d];
+    }
+    key[i] = (int32_t)lin;
+    slot[i] = atomicAdd(&count[lin], 1);
   }
-  key[i] = (int32_t)lin;
-  slot[i] = atomicAdd(&count[lin], 1);
+  if (fold_cnt && last_block_of_grid(fold_cnt)) block_exclusive_scan<int32_t>(count, cellstart, g.ncell);
 }
 
 __global__ void k_scatter_arrival(const int32_t* __restrict__ key, const int32_t* __restrict__ slot,
@@ -175,6 +179,87 @@ __global__ void k_apply_perm(const int32_t* __restrict__ perm, const int32_t* __
   int32_t i = perm[k];
   skey[k] = key[i];
   orig[k] = ord ? ord[i] : i;
+}
+
+// ---------------------------------------------------------------------------
+// Stable LSD radix sort of the cell keys (8-bit digits), the O(N) ordering of
+// large sets.  Its input is the particles in original order (keys[o] is the
+// key of the particle whose original index is o, vals[o] that particle), so
+// sorting by key alone, stably, orders each cell by original index: the
+// order the counting sort's in-cell rank gives, with no term in the square
+// of a cell's population.  A tile is RADIX_TPB threads x RADIX_ITEMS keys.
+// ---------------------------------------------------------------------------
+constexpr int RADIX_TPB = 256;
+constexpr int RADIX_ITEMS = 8;
+constexpr int64_t RADIX_TILE = (int64_t)RADIX_TPB * RADIX_ITEMS;
+
+// keys and values in original order: keys[ord[i]] = key[i], vals[ord[i]] = i
+__global__ void k_radix_prep(const int32_t* __restrict__ key, const int32_t* __restrict__ ord, int64_t N,
+                             int32_t* __restrict__ keys, int32_t* __restrict__ vals) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  const int32_t o = ord[i];
+  keys[o] = key[i];
+  vals[o] = (int32_t)i;
+}
+
+// digit histogram of each tile, digit-major: hist[d * ntiles + tile]
+__global__ void __launch_bounds__(RADIX_TPB) k_radix_up(const int32_t* __restrict__ keys, int64_t N, int shift,
+                                                        int32_t* __restrict__ hist, int64_t ntiles) {
+  __shared__ int h[256];
+  h[threadIdx.x] = 0;
+  __syncthreads();
+  const int64_t base = (int64_t)blockIdx.x * RADIX_TILE;
+#pragma unroll
+  for (int j = 0; j < RADIX_ITEMS; ++j) {
+    const int64_t idx = base + (int64_t)j * RADIX_TPB + threadIdx.x;
+    if (idx < N) atomicAdd(&h[(keys[idx] >> shift) & 255], 1);
+  }
+  __syncthreads();
+  hist[(int64_t)threadIdx.x * ntiles + blockIdx.x] = h[threadIdx.x];
+}
+
+// scatter of each tile's keys and values to their digit's scanned offset,
+// stable: the tile's keys go in index order, RADIX_TPB at a time; lanes of a
+// warp with equal digits rank by lane (match_any), warps by a prefix over
+// the warps' counts, rounds by a running count per digit.  vals == nullptr:
+// the value of key idx is idx.
+__global__ void __launch_bounds__(RADIX_TPB) k_radix_down(const int32_t* __restrict__ keys,
+                                                          const int32_t* __restrict__ vals, int64_t N, int shift,
+                                                          const int32_t* __restrict__ offs, int64_t ntiles,
+                                                          int32_t* __restrict__ keys_out,
+                                                          int32_t* __restrict__ vals_out) {
+  constexpr int NW = RADIX_TPB / 32;
+  __shared__ int run[256];
+  __shared__ int wcnt[NW][256];
+  const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+  run[tid] = offs[(int64_t)tid * ntiles + blockIdx.x];
+  const int64_t base = (int64_t)blockIdx.x * RADIX_TILE;
+  const unsigned lt = (1u << lane) - 1u;
+  for (int j = 0; j < RADIX_ITEMS; ++j) {
+#pragma unroll
+    for (int q = 0; q < NW; ++q) wcnt[q][tid] = 0;
+    __syncthreads();
+    const int64_t idx = base + (int64_t)j * RADIX_TPB + tid;
+    const bool valid = idx < N;
+    const int32_t kv = valid ? keys[idx] : 0;
+    const int dg = valid ? ((kv >> shift) & 255) : 256;
+    const unsigned peers = __match_any_sync(0xffffffffu, dg);
+    const int rank = __popc(peers & lt);
+    if (valid && rank == 0) wcnt[w][dg] = __popc(peers);
+    __syncthreads();
+    if (valid) {
+      int pos = run[dg] + rank;
+      for (int q = 0; q < w; ++q) pos += wcnt[q][dg];
+      keys_out[pos] = kv;
+      vals_out[pos] = vals ? vals[idx] : (int32_t)idx;
+    }
+    __syncthreads();
+    int add = 0;
+#pragma unroll
+    for (int q = 0; q < NW; ++q) add += wcnt[q][tid];
+    run[tid] += add;
+  }
 }
 
 template <int D>
@@ -405,12 +490,25 @@ int CellCore::init(int D_, int64_t N_, const double* cellsize, double dist_, con
   if ((rc = rs_up.ensure(sizeof(int64_t) * (N + 1), st))) return rc;
   int64_t sc = scan_scratch_elems((ncell > N ? ncell : N) + 1);
   if ((rc = scratch.ensure(sizeof(int64_t) * (sc + 16), st))) return rc;
+  // zeroed once: each pass that folds a scan resets its counter itself
+  if ((rc = foldcnt.ensure(sizeof(unsigned) * 2, st, true))) return rc;
+  if (N > RADIX_MIN_N) {
+    const int64_t ntiles = (N + RADIX_TILE - 1) / RADIX_TILE;
+    for (int b = 0; b < 2; ++b) {
+      if ((rc = rkey[b].ensure(sizeof(int32_t) * N, st))) return rc;
+      if ((rc = rval[b].ensure(sizeof(int32_t) * N, st))) return rc;
+    }
+    if ((rc = rhist.ensure(sizeof(int32_t) * 256 * ntiles, st))) return rc;
+    if ((rc = rhoff.ensure(sizeof(int32_t) * (256 * ntiles + 1), st))) return rc;
+    if (scan_scratch_elems(256 * ntiles + 1) > sc) return fail(GCSPH_EINVAL, "radix scan scratch");
+  }
   return GCSPH_OK;
 }
 
 void CellCore::release() {
   DevBuf* all[] = {&count, &cellstart, &key, &slot, &tmp, &perm, &skey, &orig, &cnt_full, &cnt_up, &rs_full,
-                   &rs_up, &nbr, &scratch, &pf[0], &pf[1], &pf[2], &pfmax, &pfthr, &pfcnt, &orig_b, &stage};
+                   &rs_up, &nbr, &scratch, &pf[0], &pf[1], &pf[2], &pfmax, &pfthr, &pfcnt, &orig_b, &stage,
+                   &foldcnt, &rkey[0], &rkey[1], &rval[0], &rval[1], &rhist, &rhoff};
   for (DevBuf* b : all) b->release();
   if (pin) cudaFreeHost(pin);
   pin = nullptr;
@@ -420,25 +518,68 @@ int CellCore::sort(const double* const* xin, const int32_t* ord) {
   timer_begin(T_SORT, st);
   GC_CUDA(cudaMemsetAsync(count.p, 0, sizeof(int32_t) * g.ncell, st));
   const double* x2 = D == 3 ? xin[2] : xin[0];
+  int rc;
+  const bool fold = g.ncell + 1 <= SCAN_FOLD_MAX;
+  unsigned* fc = fold ? foldcnt.as<unsigned>() : nullptr;
   if (D == 2)
     k_cellkey<2><<<nblocks(N, TPB), TPB, 0, st>>>(xin[0], xin[1], x2, N, g, key.as<int32_t>(), slot.as<int32_t>(),
-                                                   count.as<int32_t>());
+                                                   count.as<int32_t>(), cellstart.as<int32_t>(), fc);
   else
     k_cellkey<3><<<nblocks(N, TPB), TPB, 0, st>>>(xin[0], xin[1], x2, N, g, key.as<int32_t>(), slot.as<int32_t>(),
-                                                   count.as<int32_t>());
+                                                   count.as<int32_t>(), cellstart.as<int32_t>(), fc);
   GC_LAUNCHED();
-  int rc = exclusive_scan_i32_to_i32(count.as<int32_t>(), cellstart.as<int32_t>(), g.ncell, scratch.as<int64_t>(), st);
-  if (rc) return rc;
-  k_scatter_arrival<<<nblocks(N, TPB), TPB, 0, st>>>(key.as<int32_t>(), slot.as<int32_t>(), cellstart.as<int32_t>(), N,
-                                                      tmp.as<int32_t>());
-  GC_LAUNCHED();
+  if (!fold) {
+    rc = exclusive_scan_i32_to_i32(count.as<int32_t>(), cellstart.as<int32_t>(), g.ncell, scratch.as<int64_t>(), st);
+    if (rc) return rc;
+  }
   // ord may be `orig` itself (re-sorting particles already in cell order), so
   // the new map is written to the spare buffer and the two are swapped
   int rc2 = orig_b.ensure(sizeof(int32_t) * N, st);
   if (rc2) return rc2;
-  k_rank_apply<<<nblocks(N, TPB), TPB, 0, st>>>(tmp.as<int32_t>(), key.as<int32_t>(), cellstart.as<int32_t>(), ord, N,
-                                                 perm.as<int32_t>(), skey.as<int32_t>(), orig_b.as<int32_t>());
-  GC_LAUNCHED();
+  if (N > RADIX_MIN_N) {
+    // large sets: the stable radix sort of the keys in original order
+    const int64_t ntiles = (N + RADIX_TILE - 1) / RADIX_TILE;
+    int bits = 1;
+    while (bits < 31 && (1LL << bits) < g.ncell) ++bits;
+    const int npass = (bits + 7) / 8;
+    const int32_t* kin = key.as<int32_t>();
+    const int32_t* vin = nullptr;
+    int nxt = 0;
+    if (ord) {
+      k_radix_prep<<<nblocks(N, TPB), TPB, 0, st>>>(key.as<int32_t>(), ord, N, rkey[0].as<int32_t>(),
+                                                     rval[0].as<int32_t>());
+      GC_LAUNCHED();
+      kin = rkey[0].as<int32_t>();
+      vin = rval[0].as<int32_t>();
+      nxt = 1;
+    }
+    for (int p = 0; p < npass; ++p) {
+      k_radix_up<<<(unsigned)ntiles, RADIX_TPB, 0, st>>>(kin, N, 8 * p, rhist.as<int32_t>(), ntiles);
+      GC_LAUNCHED();
+      if ((rc = exclusive_scan_i32_to_i32(rhist.as<int32_t>(), rhoff.as<int32_t>(), 256 * ntiles,
+                                          scratch.as<int64_t>(), st)))
+        return rc;
+      const bool last = p == npass - 1;
+      int32_t* kout = last ? skey.as<int32_t>() : rkey[nxt].as<int32_t>();
+      int32_t* vout = last ? perm.as<int32_t>() : rval[nxt].as<int32_t>();
+      k_radix_down<<<(unsigned)ntiles, RADIX_TPB, 0, st>>>(kin, vin, N, 8 * p, rhoff.as<int32_t>(), ntiles, kout,
+                                                            vout);
+      GC_LAUNCHED();
+      kin = kout;
+      vin = vout;
+      nxt ^= 1;
+    }
+    k_apply_perm<<<nblocks(N, TPB), TPB, 0, st>>>(perm.as<int32_t>(), key.as<int32_t>(), ord, N, skey.as<int32_t>(),
+                                                   orig_b.as<int32_t>());
+    GC_LAUNCHED();
+  } else {
+    k_scatter_arrival<<<nblocks(N, TPB), TPB, 0, st>>>(key.as<int32_t>(), slot.as<int32_t>(),
+                                                        cellstart.as<int32_t>(), N, tmp.as<int32_t>());
+    GC_LAUNCHED();
+    k_rank_apply<<<nblocks(N, TPB), TPB, 0, st>>>(tmp.as<int32_t>(), key.as<int32_t>(), cellstart.as<int32_t>(), ord,
+                                                   N, perm.as<int32_t>(), skey.as<int32_t>(), orig_b.as<int32_t>());
+    GC_LAUNCHED();
+  }
   std::swap(orig.p, orig_b.p);
   std::swap(orig.bytes, orig_b.bytes);
   timer_end(T_SORT, st);
@@ -507,9 +648,9 @@ __global__ void k_make_pf(const double* __restrict__ x0, const double* __restric
 }
 
 
-// k_pairs with the FP32 prefilter; same output, same order
+// one point's row of the pair search with the FP32 prefilter (k_pairs32)
 template <int D, int MODE, int L>
-__global__ void __launch_bounds__(TPB) k_pairs32(const double* __restrict__ x0, const double* __restrict__ x1,
+__device__ __forceinline__ void pairs32_row(const double* __restrict__ x0, const double* __restrict__ x1,
                                                  const double* __restrict__ x2, const float* __restrict__ f0,
                                                  const float* __restrict__ f1, const float* __restrict__ f2,
                                                  const float2* __restrict__ thr,
@@ -646,6 +787,189 @@ __global__ void __launch_bounds__(TPB) k_pairs32(const double* __restrict__ x0, 
   }
 }
 
+// ---------------------------------------------------------------------------
+// 3-D count (and stage) pass with a warp per cell, for sparse grids (a few
+// points per cell, as 4M uniform points in 125^3 cells).  The per-point pass
+// above strides each point's 27-cell neighbourhood as one candidate sequence
+// and pays, for every point and every candidate, the lookup of the candidate's
+// row.  Here a warp takes one cell: it finds the neighbourhood's nine rows
+// once, loads the candidates' FP32 offsets into registers once (CELL_SLOTS per
+// lane, so up to 32 CELL_SLOTS candidates), and every point of the cell
+// tests them from there.  Same test (FP32 prefilter, the reference's FP64
+// expression in the rounding band), same counts, rows staged ascending in m
+// (slot j, lane l holds candidate 32 j + l of the ascending sequence).  A cell
+// whose neighbourhood holds more candidates walks it in windows of that many.
+// ---------------------------------------------------------------------------
+constexpr int CELL_SLOTS = 4;
+
+__global__ void __launch_bounds__(TPB) k_pairs_cell3(const double* __restrict__ x0, const double* __restrict__ x1,
+                                                     const double* __restrict__ x2, const float* __restrict__ f0,
+                                                     const float* __restrict__ f1, const float* __restrict__ f2,
+                                                     const float2* __restrict__ thr,
+                                                     const int32_t* __restrict__ cellstart, Grid g,
+                                                     int32_t* __restrict__ cnt_full, int32_t* __restrict__ cnt_up,
+                                                     int32_t* __restrict__ stg, int S) {
+  const int64_t c = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (c >= g.ncell) return;  // whole warp
+  const int32_t ks = cellstart[c], ke = cellstart[c + 1];
+  if (ks == ke) return;
+  const int nx = g.nc[0], ny = g.nc[1], nz = g.nc[2];
+  const int cx = (int)(c % nx);
+  const int64_t t0 = c / nx;
+  const int cy = (int)(t0 % ny);
+  const int cz = (int)(t0 / ny);
+  const int xlo = cx > 0 ? cx - 1 : 0;
+  const int xhi = cx < nx - 1 ? cx + 1 : nx - 1;
+  // the nine rows (z, y) of the neighbourhood, each a contiguous range of the
+  // sorted points: lane r < 9 finds row r, a shuffle scan gives the starts
+  int32_t m0 = 0, len = 0;
+  if (lane < 9) {
+    const int z = cz + (lane / 3 - 1), y = cy + (lane % 3 - 1);
+    if (z >= 0 && z < nz && y >= 0 && y < ny) {
+      const int64_t base = (int64_t)nx * ((int64_t)y + (int64_t)ny * z);
+      m0 = cellstart[base + xlo];
+      len = cellstart[base + xhi + 1] - m0;
+    }
+  }
+  int32_t cum = len;
+#pragma unroll
+  for (int o = 1; o < 16; o <<= 1) {
+    const int32_t y = __shfl_up_sync(0xffffffffu, cum, o);
+    if (lane >= o) cum += y;
+  }
+  const int32_t tot = __shfl_sync(0xffffffffu, cum, 8);
+  int32_t rstart[9], rdelta[9];  // start of row r in the sequence, and m - t within it
+#pragma unroll
+  for (int r = 0; r < 9; ++r) {
+    const int32_t cr = __shfl_sync(0xffffffffu, cum, r), lr = __shfl_sync(0xffffffffu, len, r);
+    rstart[r] = cr - lr;
+    rdelta[r] = __shfl_sync(0xffffffffu, m0, r) - rstart[r];
+  }
+  const float2 tt = *thr;
+  const float tlo = tt.x, thi = tt.y;
+  const unsigned lt = (1u << lane) - 1u;
+  constexpr int WIN = 32 * CELL_SLOTS;
+  for (int32_t w0 = 0; w0 < tot; w0 += WIN) {
+    int32_t sm[CELL_SLOTS];
+    float sx[CELL_SLOTS], sy[CELL_SLOTS], sz[CELL_SLOTS];
+#pragma unroll
+    for (int j = 0; j < CELL_SLOTS; ++j) {
+      const int32_t t = w0 + 32 * j + lane;
+      int32_t dd = rdelta[0];
+#pragma unroll
+      for (int r = 1; r < 9; ++r) dd = t >= rstart[r] ? rdelta[r] : dd;
+      sm[j] = t < tot ? t + dd : -1;
+      sx[j] = sm[j] >= 0 ? f0[sm[j]] : 0.0f;
+      sy[j] = sm[j] >= 0 ? f1[sm[j]] : 0.0f;
+      sz[j] = sm[j] >= 0 ? f2[sm[j]] : 0.0f;
+    }
+    for (int32_t k = ks; k < ke; ++k) {
+      const float ax = f0[k], ay = f1[k], az = f2[k];
+      int32_t nf = w0 > 0 ? cnt_full[k] : 0, nu = w0 > 0 ? cnt_up[k] : 0;
+      int32_t spos = nf;
+#pragma unroll
+      for (int j = 0; j < CELL_SLOTS; ++j) {
+        const int32_t m = sm[j];
+        bool hit = false;
+        if (m >= 0 && m != k) {
+          const float d0 = ax - sx[j], d1 = ay - sy[j], d2 = az - sz[j];
+          const float r2f = (d0 * d0 + d1 * d1) + d2 * d2;
+          if (r2f < tlo) {
+            hit = true;
+          } else if (!(r2f > thi)) {  // inside the band (or NaN): the reference's FP64 test
+            hit = r2_ref<3>(x0[k], x1[k], x2[k], x0[m], x1[m], x2[m]) < g.dist2;
+          }
+        }
+        const unsigned bal = __ballot_sync(0xffffffffu, hit);
+        if (stg && hit) {
+          const int32_t at = spos + __popc(bal & lt);
+          if (at < S) stg[(int64_t)k * S + at] = m;
+        }
+        spos += __popc(bal);
+        nf += __popc(bal);
+        nu += __popc(__ballot_sync(0xffffffffu, hit && m > k));
+      }
+      if (lane == 0) {
+        cnt_full[k] = nf;
+        cnt_up[k] = nu;
+      }
+      __syncwarp();
+    }
+  }
+}
+
+// MODE 3 (fill and pair list): the MODE 1 fill, then for each entry e of k's
+// row whose neighbour m is above k the flat pair (k, m, e, mirror(e)), with
+// mirror(e) the position of k in m's row, found by binary search in m's
+// staged row (m's smaller-index part, ascending); a row too long to be staged
+// gives mirror -1, which pass A resolves from the finished neighbour list.
+template <int D, int L>
+__device__ __forceinline__ void pairs32_quads(int64_t N, const int32_t* __restrict__ cnt_full,
+                                              const int32_t* __restrict__ cnt_up, const int64_t* __restrict__ rs_full,
+                                              const int64_t* __restrict__ rs_up, const int32_t* __restrict__ nbr,
+                                              int64_t cap, const int32_t* __restrict__ stg, int S,
+                                              int4* __restrict__ pq) {
+  const int64_t gt = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t k = gt / L;
+  const int lane = (int)(gt % L);
+  if (k >= N) return;
+  // past the capacity the fill raised the overflow flag and the step is
+  // repeated; the pair list holds cap / 2 + 1 pairs, enough when it fits
+  if (rs_full[N] > cap) return;
+  const int64_t r0 = rs_full[k], r1 = rs_full[k + 1];
+  const int32_t n = (int32_t)(r1 - r0);
+  const int32_t nu = cnt_up[k];
+  const int64_t u0 = rs_up[k];
+  const bool staged = n <= S;
+  for (int32_t q = n - nu + lane; q < n; q += L) {
+    const int32_t m = staged ? stg[k * S + q] : nbr[r0 + q];
+    const int32_t nm = cnt_full[m];
+    int32_t mir = -1;
+    if (nm <= S) {
+      int32_t lo = 0, hi = nm - cnt_up[m];
+      const int32_t* row = stg + (int64_t)m * S;
+      while (lo < hi) {
+        const int32_t mid = (lo + hi) >> 1;
+        if (row[mid] < k) lo = mid + 1;
+        else hi = mid;
+      }
+      mir = (int32_t)(rs_full[m] + lo);
+    }
+    pq[u0 + (q - (n - nu))] = make_int4((int)k, (int)m, (int)(r0 + q), mir);
+  }
+}
+
+// the pair search with the FP32 prefilter (same output, same order as
+// k_pairs).  MODE 4: MODE 2, then the last block to finish scans the row
+// counts into rs_full / rs_up (N + 1 <= SCAN_FOLD_MAX; a separate mode, so
+// that the scan's registers do not weigh on MODE 2 at large N).  MODE 3: the
+// fill, then the flat pair list of the pair-once passes (pairs32_quads).
+template <int D, int MODE, int L>
+__global__ void __launch_bounds__(TPB) k_pairs32(const double* __restrict__ x0, const double* __restrict__ x1,
+                                                 const double* __restrict__ x2, const float* __restrict__ f0,
+                                                 const float* __restrict__ f1, const float* __restrict__ f2,
+                                                 const float2* __restrict__ thr,
+                                                 const int32_t* __restrict__ skey,
+                                                 const int32_t* __restrict__ cellstart, int64_t N, Grid g,
+                                                 int32_t* __restrict__ cnt_full, int32_t* __restrict__ cnt_up,
+                                                 const int64_t* __restrict__ rs_full, int32_t* __restrict__ nbr,
+                                                 int64_t cap, int* __restrict__ ovf, int32_t* __restrict__ stg,
+                                                 int S, int64_t* fold_rs_full, int64_t* fold_rs_up,
+                                                 unsigned* fold_cnt, const int64_t* __restrict__ rs_up,
+                                                 int4* __restrict__ pq) {
+  pairs32_row<D, MODE == 3 ? 1 : (MODE == 4 ? 2 : MODE), L>(x0, x1, x2, f0, f1, f2, thr, skey, cellstart, N, g,
+                                                             cnt_full, cnt_up, rs_full, nbr, cap, ovf, stg, S);
+  if (MODE == 4 && last_block_of_grid(fold_cnt)) {
+    block_exclusive_scan<int64_t>(cnt_full, fold_rs_full, N);
+    block_exclusive_scan<int64_t>(cnt_up, fold_rs_up, N);
+  }
+  if (MODE == 3) {
+    __syncwarp();  // a recomputed row's entries, written by the group's lanes, are read back
+    pairs32_quads<D, L>(N, cnt_full, cnt_up, rs_full, rs_up, nbr, cap, stg, S, pq);
+  }
+}
+
 // lanes per particle in the pair search: about 8 candidates per lane
 // Lanes per point of the pair passes.  A point walks 3^(D-1) rows of three
 // cells each, and the lanes share a row's candidates, so the lanes follow the
@@ -656,17 +980,19 @@ __global__ void __launch_bounds__(TPB) k_pairs32(const double* __restrict__ x0, 
 // volume over the dist-ball's (9/π in 2-D, 81/(4π) in 3-D, times
 // (cellsize/dist)^D), which weights cells by the points in them; the first
 // build takes the grid-wide mean N / ncell (which also counts empty cells).
-int CellCore::pair_lanes() const {
-  if (lanes > 0) return lanes;
-  double cand;
+double CellCore::candidates_per_point() const {
   if (nfull_est > 0 && N > 0) {
     double vol = D == 3 ? 81.0 / (4.0 * GCSPH_PI64) : 9.0 / GCSPH_PI64;
     for (int d = 0; d < D; ++d) vol *= cs[d] / dist;
-    cand = (double)nfull_est / (double)N * vol;
-  } else {
-    const double per_cell = (double)N / (double)g.ncell;
-    cand = per_cell * (D == 3 ? 27.0 : 9.0);
+    return (double)nfull_est / (double)N * vol;
   }
+  const double per_cell = (double)N / (double)g.ncell;
+  return per_cell * (D == 3 ? 27.0 : 9.0);
+}
+
+int CellCore::pair_lanes() const {
+  if (lanes > 0) return lanes;
+  const double cand = candidates_per_point();
   const double per_row = cand / (D == 3 ? 9.0 : 3.0);
   int L = 1;
   while (L < 32 && (double)(2 * L) <= per_row) L <<= 1;
@@ -730,7 +1056,9 @@ int CellCore::ensure_pf() {
   return pfmax.ensure(sizeof(unsigned long long), st, true);
 }
 
-int CellCore::build_pairs(const double* const* xs, int* ovf_dev, bool scan_up, bool pf_ready) {
+int CellCore::build_pairs(const double* const* xs, int* ovf_dev, bool scan_up, bool pf_ready, int4* pq,
+                          bool* pq_done) {
+  if (pq_done) *pq_done = false;
   if (!sorted) return fail(GCSPH_ESTATE, "pair build before binning");
   const double* x2 = D == 3 ? xs[2] : xs[0];
   timer_begin(T_PAIRS, st);
@@ -757,20 +1085,35 @@ int CellCore::build_pairs(const double* const* xs, int* ovf_dev, bool scan_up, b
   int32_t* sp = nullptr;
   if (mean > 0 && (rc0 = stage.ensure(sizeof(int32_t) * (size_t)N * (size_t)S, st)) == GCSPH_OK) sp = stage.as<int32_t>();
   if (rc0) return rc0;
-  if (sp)
+  // sparse 3-D grids: a warp per cell (k_pairs_cell3)
+  const bool cell3 = D == 3 && cell_warps && candidates_per_point() <= CELL3_MAX_CAND;
+  // small sets: the count pass's last block scans the row counts (both
+  // arrays), so no scan launch follows
+  const bool fold = sp && !cell3 && N + 1 <= SCAN_FOLD_MAX;
+  unsigned* fc = fold ? foldcnt.as<unsigned>() + 1 : nullptr;
+  if (cell3)
+    k_pairs_cell3<<<nblocks(g.ncell * 32, TPB), TPB, 0, st>>>(xs[0], xs[1], x2, pf[0].as<float>(),
+                                                               pf[1].as<float>(), f2, thr, cellstart.as<int32_t>(), g,
+                                                               cnt_full.as<int32_t>(), cnt_up.as<int32_t>(), sp, S);
+  else if (fold)
+    PAIRS32_LAUNCH(4, L, xs[0], xs[1], x2, pf[0].as<float>(), pf[1].as<float>(), f2, thr, skey.as<int32_t>(),
+                   cellstart.as<int32_t>(), N, g, cnt_full.as<int32_t>(), cnt_up.as<int32_t>(), nullptr, nullptr, 0,
+                   nullptr, sp, S, rs_full.as<int64_t>(), rs_up.as<int64_t>(), fc, nullptr, nullptr);
+  else if (sp)
     PAIRS32_LAUNCH(2, L, xs[0], xs[1], x2, pf[0].as<float>(), pf[1].as<float>(), f2, thr, skey.as<int32_t>(),
                    cellstart.as<int32_t>(), N, g, cnt_full.as<int32_t>(), cnt_up.as<int32_t>(), nullptr, nullptr, 0,
-                   nullptr, sp, S);
+                   nullptr, sp, S, nullptr, nullptr, nullptr, nullptr, nullptr);
   else
     PAIRS32_LAUNCH(0, L, xs[0], xs[1], x2, pf[0].as<float>(), pf[1].as<float>(), f2, thr, skey.as<int32_t>(),
                    cellstart.as<int32_t>(), N, g, cnt_full.as<int32_t>(), cnt_up.as<int32_t>(), nullptr, nullptr, 0,
-                   nullptr, nullptr, 0);
+                   nullptr, nullptr, 0, nullptr, nullptr, nullptr, nullptr, nullptr);
   GC_LAUNCHED();
-  int rc = scan_up ? exclusive_scan2_i32_to_i64(cnt_full.as<int32_t>(), rs_full.as<int64_t>(),
-                                                cnt_up.as<int32_t>(), rs_up.as<int64_t>(), N,
-                                                scratch.as<int64_t>(), st)
-                  : exclusive_scan_i32_to_i64(cnt_full.as<int32_t>(), rs_full.as<int64_t>(), N,
-                                              scratch.as<int64_t>(), st);
+  int rc = GCSPH_OK;
+  if (!fold)
+    rc = scan_up ? exclusive_scan2_i32_to_i64(cnt_full.as<int32_t>(), rs_full.as<int64_t>(), cnt_up.as<int32_t>(),
+                                              rs_up.as<int64_t>(), N, scratch.as<int64_t>(), st)
+                 : exclusive_scan_i32_to_i64(cnt_full.as<int32_t>(), rs_full.as<int64_t>(), N,
+                                             scratch.as<int64_t>(), st);
   if (rc) return rc;
   timer_end(T_PAIRS, st);
   if (ovf_dev && nbr_cap > 0) {
@@ -787,9 +1130,20 @@ int CellCore::build_pairs(const double* const* xs, int* ovf_dev, bool scan_up, b
     if (nfull > nbr_cap && (rc = grow_nbr(nfull))) return rc;
   }
   timer_begin(T_PAIRS, st);
-  PAIRS32_LAUNCH(1, L, xs[0], xs[1], x2, pf[0].as<float>(), pf[1].as<float>(), f2, thr, skey.as<int32_t>(),
-                 cellstart.as<int32_t>(), N, g, nullptr, nullptr, rs_full.as<int64_t>(), nbr.as<int32_t>(), nbr_cap,
-                 ovf_dev, sp, S);
+  if (pq && sp && scan_up && nfull < 0) {
+    // the fill and the flat pair list of the pair-once passes in one launch
+    // (only where the capacity did not change in this build: the caller sized
+    // its pair list for it)
+    PAIRS32_LAUNCH(3, L, xs[0], xs[1], x2, pf[0].as<float>(), pf[1].as<float>(), f2, thr, skey.as<int32_t>(),
+                   cellstart.as<int32_t>(), N, g, cnt_full.as<int32_t>(), cnt_up.as<int32_t>(),
+                   rs_full.as<int64_t>(), nbr.as<int32_t>(), nbr_cap, ovf_dev, sp, S, nullptr, nullptr, nullptr,
+                   rs_up.as<int64_t>(), pq);
+    if (pq_done) *pq_done = true;
+  } else {
+    PAIRS32_LAUNCH(1, L, xs[0], xs[1], x2, pf[0].as<float>(), pf[1].as<float>(), f2, thr, skey.as<int32_t>(),
+                   cellstart.as<int32_t>(), N, g, nullptr, nullptr, rs_full.as<int64_t>(), nbr.as<int32_t>(), nbr_cap,
+                   ovf_dev, sp, S, nullptr, nullptr, nullptr, nullptr, nullptr);
+  }
   GC_LAUNCHED();
   timer_end(T_PAIRS, st);
   built = true;
@@ -1191,7 +1545,7 @@ static int run(int64_t N, const double* const* x, const double* cellsize, double
   // so the per-cell counters are cleared first
   GC_CUDA(cudaMemsetAsync(count, 0, sizeof(int32_t) * ncell, st));
   const double* x2 = D == 3 ? x[2] : x[0];
-  k_cellkey<D><<<nblocks(N, TPB), TPB, 0, st>>>(x[0], x[1], x2, N, g, key, slot, count);
+  k_cellkey<D><<<nblocks(N, TPB), TPB, 0, st>>>(x[0], x[1], x2, N, g, key, slot, count, nullptr, nullptr);
   GC_LAUNCHED();
   if ((rc = exclusive_scan_i32_to_i32(count, cstart, ncell, scan, st))) return rc;
   k_scatter_arrival<<<nblocks(N, TPB), TPB, 0, st>>>(key, slot, cstart, N, tmpv);

@@ -66,6 +66,13 @@ int minmax_blocks();
 int bounding_box(int D, const double* const* x, int64_t N, int nb, double* part_dev, double* part_host,
                  cudaStream_t st, double* mn, double* mx);
 
+// sets of more points than this are ordered by the stable radix sort (O(N));
+// smaller ones by the counting sort's in-cell rank (fewer launches)
+constexpr int64_t RADIX_MIN_N = 65536;
+// the 3-D count pass takes a warp per cell where a point has at most this
+// many candidates (the warp's registers hold 128 of them at a time)
+constexpr double CELL3_MAX_CAND = 96.0;
+
 struct CellCore {
   int D = 2;
   int64_t N = 0;
@@ -78,13 +85,19 @@ struct CellCore {
   DevBuf pfthr;         // the prefilter's two FP32 thresholds (float2), from pfmax once per build
   DevBuf pfcnt;         // blocks done of the pass that accumulates pfmax (its last block writes pfthr)
   DevBuf stage;         // neighbour rows staged by the count pass (fixed stride), copied by the fill
+  DevBuf foldcnt;       // finished-block counters of the passes whose last block runs a scan (2 unsigned)
+  DevBuf rkey[2], rval[2], rhist, rhoff;  // radix sort of large sets: ping-pong keys/values, tile histograms
   int64_t* pin = nullptr;  // pinned host scalars
   int64_t nfull = 0, nup = 0, nbr_cap = 0;
   int64_t nfull_est = 0;  // last neighbour-entry count read back (lane choice); nfull is -1 while unknown
   int64_t gen = 0;        // bumped whenever a buffer a captured step graph points into is reallocated
   bool sorted = false, built = false, up_valid = false;
   int lanes = 0;  // lanes per particle in the pair search; 0 = by mean candidate count
+  bool cell_warps = true;  // sparse 3-D grids: the count pass with a warp per cell (k_pairs_cell3)
   int pair_lanes() const;
+  // candidates (points in the 3^D stencil) per point: from the last build's
+  // neighbour count, else from the grid-wide mean per cell
+  double candidates_per_point() const;
 
   int init(int D_, int64_t N_, const double* cellsize, double dist_, const double* MIN, const double* MAX,
            const double* const* xin, cudaStream_t s);
@@ -101,8 +114,13 @@ struct CellCore {
   // count: rows past nbr_cap raise *ovf_dev instead (see grow_nbr).  scan_up
   // also scans the larger-index counts into rs_up (device only) in the same
   // launch as the row offsets.
-  // pf_ready: the FP32 prefilter copy of xs (pf, pfmax) was written by the caller's permute
-  int build_pairs(const double* const* xs, int* ovf_dev = nullptr, bool scan_up = false, bool pf_ready = false);
+  // pf_ready: the FP32 prefilter copy of xs (pf, pfmax) was written by the caller's permute.
+  // pq (with scan_up): the fill also writes the flat pair list (k, m, e, mirror(e)) of the
+  // pair-once passes when the count pass staged the rows and the fill runs without a host
+  // round trip (the capacity unchanged: pq must hold nbr_cap / 2 + 1 pairs); *pq_done says
+  // whether it did
+  int build_pairs(const double* const* xs, int* ovf_dev = nullptr, bool scan_up = false, bool pf_ready = false,
+                  int4* pq = nullptr, bool* pq_done = nullptr);
   int ensure_pf();
   int grow_nbr(int64_t need);
   int read_nfull();

@@ -2242,6 +2242,14 @@ int ens_remove(gcsph_ens* e, int32_t slot) {
   return GCSPH_OK;
 }
 
+int ens_set_stream(gcsph_ens* e, void* stream) {
+  if (!e) return fail(GCSPH_EINVAL, "null handle");
+  if ((cudaStream_t)stream == e->st) return GCSPH_OK;
+  GC_CUDA(cudaStreamSynchronize(e->st));  // the old stream's work is done before the next call's starts
+  e->st = (cudaStream_t)stream;
+  return GCSPH_OK;
+}
+
 int ens_step(gcsph_ens* e, int32_t n) {
   if (!e) return fail(GCSPH_EINVAL, "null handle");
   if (n < 0) return fail(GCSPH_EINVAL, "n must be >= 0");

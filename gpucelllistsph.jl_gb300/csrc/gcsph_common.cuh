@@ -191,6 +191,87 @@ constexpr int64_t scan_scratch_elems(int64_t m) {
 // module loading otherwise loads each at its first launch, which needs
 // device memory for its code)
 int scan_preload();
+
+// Arrays of up to SCAN_FOLD_MAX items are scanned by the last block of the
+// kernel that produced them (block_exclusive_scan), which saves the scan's
+// own launch: a step at small N is bound by its chain of short launches.
+constexpr int64_t SCAN_FOLD_MAX = 16384;
+
+// true in every thread of the block that finishes last among gridDim.x
+// blocks; each thread's earlier global writes are visible to that block.
+// *cnt counts finished blocks and is reset to 0 by the last one.
+__device__ inline bool last_block_of_grid(unsigned* cnt) {
+  __shared__ int s_last;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) s_last = atomicAdd(cnt, 1u) == gridDim.x - 1;
+  __syncthreads();
+  const bool last = s_last != 0;
+  if (last) {
+    __threadfence();
+    if (threadIdx.x == 0) *cnt = 0u;
+  }
+  return last;
+}
+
+// out[i] = sum_{j<i} in[j] for i in [0, n] (out[n] = total), by one block
+// (blockDim.x a multiple of 32), 16 items per thread per tile, read as four
+// 16-byte vectors (in 16-byte aligned).  Reads go to L2 (ld.global.cg): the
+// inputs were written by other blocks of the grid.
+template <class TOut>
+__device__ void block_exclusive_scan(const int32_t* in, TOut* out, int64_t n) {
+  constexpr int IT = 16;
+  __shared__ long long wsum[32];
+  const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5, nw = blockDim.x >> 5;
+  long long carry = 0;
+  for (int64_t base = 0; base <= n; base += (int64_t)blockDim.x * IT) {
+    const int64_t i0 = base + (int64_t)tid * IT;
+    int v[IT];
+    if (i0 + IT <= n) {
+#pragma unroll
+      for (int q = 0; q < IT / 4; ++q) {
+        const int4 t = __ldcg(reinterpret_cast<const int4*>(in + i0) + q);
+        v[4 * q] = t.x;
+        v[4 * q + 1] = t.y;
+        v[4 * q + 2] = t.z;
+        v[4 * q + 3] = t.w;
+      }
+    } else {
+#pragma unroll
+      for (int j = 0; j < IT; ++j) v[j] = i0 + j < n ? __ldcg(in + i0 + j) : 0;
+    }
+    long long s = 0;
+#pragma unroll
+    for (int j = 0; j < IT; ++j) s += v[j];
+    long long inc = s;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const long long y = __shfl_up_sync(0xffffffffu, inc, o);
+      if (lane >= o) inc += y;
+    }
+    if (lane == 31) wsum[w] = inc;
+    __syncthreads();
+    if (w == 0) {
+      long long t = lane < nw ? wsum[lane] : 0;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const long long y = __shfl_up_sync(0xffffffffu, t, o);
+        if (lane >= o) t += y;
+      }
+      if (lane < nw) wsum[lane] = t;
+    }
+    __syncthreads();
+    long long run = carry + (w > 0 ? wsum[w - 1] : 0) + inc - s;
+#pragma unroll
+    for (int j = 0; j < IT; ++j) {
+      if (i0 + j <= n) out[i0 + j] = (TOut)run;
+      run += v[j];
+    }
+    carry += wsum[nw - 1];
+    __syncthreads();
+  }
+}
+
 int exclusive_scan_i32_to_i64(const int32_t* in, int64_t* out, int64_t n, int64_t* scratch,
                               cudaStream_t s);
 int exclusive_scan_i32_to_i32(const int32_t* in, int32_t* out, int64_t n, int64_t* scratch,

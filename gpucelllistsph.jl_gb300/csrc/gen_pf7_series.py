@@ -18,6 +18,7 @@ import struct
 
 K = 10            # highest power kept in the exact series
 EPS_MAX = F(1, 128)
+EPS_SHORT = F(1, 1024)  # a shorter head of the same series serves |eps| <= EPS_SHORT
 TOL = 2.0 ** -64  # dropped tail, relative to 1
 
 
@@ -109,16 +110,35 @@ def horner(c, e):
     return r
 
 
-def main():
-    up, lo = series(True), series(False)
+def short_terms(c):
+    """Terms of series c that matter for |eps| <= EPS_SHORT (the dropped
+    tail stays below TOL relative to 1)."""
+    n = len(c) - 1
+    while n > 1 and abs(c[n]) * float(EPS_SHORT) ** n < TOL:
+        n -= 1
+    return n + 1
+
+
+def sweep(up, lo, eps_max, n):
+    """Largest gap to the iteration's own output over a sweep of |eps| <=
+    eps_max, with the first n terms of each series."""
     worst = 0.0
     for i in range(-2000, 2001):
-        e = float(EPS_MAX) * i / 2000.0
+        e = float(eps_max) * i / 2000.0
         x = 1.0 + e
         e = x - 1.0
-        s = horner(up if e >= 0 else lo, e)
+        s = horner((up if e >= 0 else lo)[:n], e)
         worst = max(worst, abs((1.0 + s) - ref_pf7(x)))
+    return worst
+
+
+def main():
+    up, lo = series(True), series(False)
+    worst = sweep(up, lo, EPS_MAX, max(len(up), len(lo)))
     assert worst <= 4.5e-16, worst
+    nshort = max(short_terms(up), short_terms(lo))
+    worst_short = sweep(up, lo, EPS_SHORT, nshort)
+    assert worst_short <= 4.5e-16, worst_short
     here = os.path.dirname(os.path.abspath(__file__))
     with open(os.path.join(here, "pf7_series.cuh"), "w") as f:
         f.write("// Generated by gen_pf7_series.py -- do not edit.\n")
@@ -126,10 +146,14 @@ def main():
         f.write("// (src/gpukernels_sph.jl:499-515; worst gap to the iteration over a sweep: %.3g)\n" % worst)
         f.write("#pragma once\n")
         f.write("#define PF7_EPS_MAX %r\n" % float(EPS_MAX))
+        f.write("// |eps| <= PF7_EPS_SHORT needs only the first PF7_SHORT_N terms (worst gap %.3g)\n" % worst_short)
+        f.write("#define PF7_EPS_SHORT %r\n" % float(EPS_SHORT))
+        f.write("#define PF7_SHORT_N %d\n" % nshort)
         for name, c in (("PF7_UP", up), ("PF7_LO", lo)):
             f.write("#define %s_N %d\n" % (name, len(c)))
             f.write("#define %s_C {%s}\n" % (name, ", ".join(repr(v) for v in c)))
-    print("pf7 series:", len(up), len(lo), "terms; worst gap", worst)
+    print("pf7 series:", len(up), len(lo), "terms; worst gap", worst, "; short head", nshort, "terms, gap",
+          worst_short)
 
 
 if __name__ == "__main__":

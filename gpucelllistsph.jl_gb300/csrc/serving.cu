@@ -54,9 +54,15 @@ struct gcsph_srv {
   gcsph_srv_backend be{};
   bool own = false;        // the library's backend
   void* stream = nullptr;
-  // the library's backend, no stream given: one stream per dimension, so the
-  // 2-D and 3-D ensembles' chunks run side by side
-  cudaStream_t dim_st[2] = {nullptr, nullptr};
+  // the library's backend, no stream given: streams per dimension, so the
+  // 2-D and 3-D ensembles' chunks run side by side -- [d][0] at the lowest
+  // priority, [d][1] at the highest (shortest first: the dimension holding
+  // the solve with the least work left runs on its high-priority stream)
+  cudaStream_t dim_st[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
+  // wall seconds per step of each dimension's last chunk (library backend):
+  // the faster dimension takes more steps per round, so that a round's two
+  // chunks take about the same time and neither dimension waits on the other
+  double spp[2] = {0.0, 0.0};
   int32_t chunk = 64;
   double reserve = 0.1;
   int32_t policy = GCSPH_SRV_ARRIVAL;
@@ -79,7 +85,7 @@ int own_add(void* ctx, int32_t D, int32_t rid, int32_t* slot) {
   gcsph_srv* s = (gcsph_srv*)ctx;
   gcsph_ens*& e = ens_of(s, D);
   int rc;
-  void* st = s->dim_st[D == 3 ? 1 : 0] ? (void*)s->dim_st[D == 3 ? 1 : 0] : s->stream;
+  void* st = s->dim_st[D == 3 ? 1 : 0][0] ? (void*)s->dim_st[D == 3 ? 1 : 0][0] : s->stream;
   if (!e && (rc = ens_create(D, st, &e))) return rc;
   SrvReq& r = s->req[rid];
   rc = ens_add(e, r.n, r.x.data(), r.has_v ? r.v.data() : nullptr, r.rho.data(), r.ptype.data(), &r.prm, slot);
@@ -186,30 +192,58 @@ int round(gcsph_srv* s, int* advanced) {
     r.remaining = r.steps;
     inflight[di] += r.n;
   }
-  int64_t kd[2] = {s->chunk, s->chunk}, lived[2] = {0, 0};
+  int64_t kd[2] = {s->chunk, s->chunk}, lived[2] = {0, 0}, left[2] = {INT64_MAX, INT64_MAX};
+  double least[2] = {INFINITY, INFINITY};  // least work (particles x steps) left of a running solve
   for (const SrvReq& r : s->req)
     if (r.state == RQ_RUNNING) {
       const int di = r.D == 3 ? 1 : 0;
-      kd[di] = std::min(kd[di], r.remaining);
+      left[di] = std::min(left[di], r.remaining);
       lived[di] += r.n;
+      least[di] = std::min(least[di], (double)r.n * (double)r.remaining);
     }
+  const bool both = s->dim_st[0][0] && s->dim_st[1][0] && lived[0] > 0 && lived[1] > 0;
+  if (both && s->spp[0] > 0 && s->spp[1] > 0) {
+    // the dimension that is faster per step takes a power-of-two multiple of
+    // the chunk (at most 16), so that both chunks take about the same time
+    const int slow = s->spp[0] >= s->spp[1] ? 0 : 1, fast = 1 - slow;
+    const double ratio = s->spp[slow] / s->spp[fast];
+    int64_t k = s->chunk;
+    while (k < 16 * (int64_t)s->chunk && (double)(2 * k) <= (double)s->chunk * ratio) k *= 2;
+    kd[fast] = k;
+  }
+  for (int di = 0; di < 2; ++di) kd[di] = std::min(kd[di], left[di]);
+  if (both) {
+    // shortest first: the solve with the least work left gets the GPU first
+    const int hi = s->policy == GCSPH_SRV_SHORTEST ? (least[0] <= least[1] ? 0 : 1) : -1;
+    for (int di = 0; di < 2; ++di) {
+      int rc = ens_set_stream(s->ens[di], s->dim_st[di][di == hi ? 1 : 0]);
+      if (rc) return rc;
+    }
+  }
+  auto timed_step = [&](int di) {
+    const auto t0 = std::chrono::steady_clock::now();
+    const int rc = s->be.step(s->be.ctx, 2 + di, (int32_t)kd[di]);
+    const double sec = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    if (rc == GCSPH_OK && kd[di] > 0) s->spp[di] = sec / (double)kd[di];
+    return rc;
+  };
   int rcd[2] = {GCSPH_OK, GCSPH_OK};
-  if (s->dim_st[0] && s->dim_st[1] && lived[0] > 0 && lived[1] > 0) {
+  if (both) {
     // both ensembles run: the 3-D chunk from a second host thread, on its own
     // stream, while this thread runs the 2-D one (an error's message is
     // carried back: the library keeps it per thread)
     std::string msg3;
     std::thread t([&] {
-      rcd[1] = s->be.step(s->be.ctx, 3, (int32_t)kd[1]);
+      rcd[1] = timed_step(1);
       if (rcd[1]) msg3 = gcsph_last_error();
     });
-    rcd[0] = s->be.step(s->be.ctx, 2, (int32_t)kd[0]);
+    rcd[0] = timed_step(0);
     t.join();
     if (rcd[0]) return rcd[0];
     if (rcd[1]) return fail(rcd[1], "%s", msg3.c_str());
   } else {
     for (int di = 0; di < 2; ++di)
-      if (lived[di] > 0 && (rcd[di] = s->be.step(s->be.ctx, 2 + di, (int32_t)kd[di]))) return rcd[di];
+      if (lived[di] > 0 && (rcd[di] = timed_step(di))) return rcd[di];
   }
   for (int32_t D = 2; D <= 3; ++D) {
     const int di = D == 3 ? 1 : 0;
@@ -257,12 +291,25 @@ int srv_create(void* stream, int32_t chunk, double reserve, uint32_t fields, con
     s->be = *backend;
   } else {
     s->own = true;
-    if (!stream)
-      for (cudaStream_t& st : s->dim_st)
-        if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) {
-          cudaGetLastError();
-          st = nullptr;
+    int lo = 0, hi = 0;
+    if (!stream && cudaDeviceGetStreamPriorityRange(&lo, &hi) == cudaSuccess) {
+      for (auto& pair : s->dim_st)
+        for (int k = 0; k < 2; ++k)
+          if (cudaStreamCreateWithPriority(&pair[k], cudaStreamNonBlocking, k ? hi : lo) != cudaSuccess) {
+            cudaGetLastError();
+            pair[k] = nullptr;
+          }
+      for (auto& pair : s->dim_st)
+        if (!pair[0] || !pair[1]) {
+          for (auto& q : s->dim_st)
+            for (cudaStream_t& st : q) {
+              if (st) cudaStreamDestroy(st);
+              st = nullptr;
+            }
+          break;
         }
+    }
+    cudaGetLastError();
     s->be.ctx = s;
     s->be.add = own_add;
     s->be.remove = own_remove;
@@ -280,8 +327,9 @@ void srv_destroy(gcsph_srv* s) {
   if (!s) return;
   for (gcsph_ens* e : s->ens)
     if (e) ens_destroy(e);
-  for (cudaStream_t st : s->dim_st)
-    if (st) cudaStreamDestroy(st);
+  for (auto& pair : s->dim_st)
+    for (cudaStream_t st : pair)
+      if (st) cudaStreamDestroy(st);
   delete s;
 }
 

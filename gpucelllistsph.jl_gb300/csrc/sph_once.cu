@@ -8,14 +8,44 @@
 
 namespace gcsph {
 
+// fbmolforce!, :1891-1901, for a pair with exactly one real side, at
+// separation dx (r2 = |dx|², r = |dx|): adds Δx Fc to f
+template <int D>
+__device__ inline void fb_pair(const StepConst& c, const double* dx, double r2, double r, double* f) {
+  if (dbits(r) < dbits(c.fb_r0)) {
+    const double q = c.fb_r0 * rcp_nr(r + c.fb_eta2);
+    const double q2 = q * q, q4 = q2 * q2, q8 = q4 * q4, q12 = q8 * q4;
+    const double Fc = c.fb_d * (q12 - q4) * rcp_nr(r2 + c.fb_eta2);
+#pragma unroll
+    for (int d = 0; d < D; ++d) f[d] += dx[d] * Fc;
+  }
+}
+
+// Pass A: one thread per pair (k, m), k < m in cell order.  Stage 1 at
+// (x, ρ, v, P(ρ)) also writes W and ∇W; stage 2 at (xΔt½, ρΔt½, vΔt½,
+// P(ρΔt½)) with the stage-1 ∇W and fbmolforce! at x.  The reference's terms,
+// src/gpukernels_sph.jl, in their algebraically equal pair-once forms:
+//  * ∇W = Δx d𝒲/r with d𝒲/r = dWr (1 - u)^3 -- no division by r;
+//  * ∂ρ∂tDDT! (:542-631): both sides share DDTkh m₀ (-Δx·∇W)/(r² + η²);
+//  * ∂v∂t! (:740-776) and ∂v∂t_av! (:852-901) as one factor of ∇W,
+//    -m₀ (Pk + Pm)/(ρk ρm) + 2 α c₀ h m₀ (Δv·Δx)/((r² + η²)(ρk + ρm)).
 template <int D, int STAGE>
-__global__ void __launch_bounds__(STPB) k_pairA(StepConst c, SArr<D> S, PairBuf B) {
-  if (*S.ovf) return;
-  const int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (u >= *B.npair) return;
+__device__ __forceinline__ void pairA_one(const StepConst& c, const SArr<D>& S, const PairBuf& B, int64_t u) {
   const int4 q = B.pq[u];
-  const int k = q.x, m = q.y, e = q.z, me = q.w;
-  // stage 1 at (x, ρ, v, P(ρ)); stage 2 at (xΔt½, ρΔt½, vΔt½, P(ρΔt½)) with stage-1 ∇W, fb at x
+  const int k = q.x, m = q.y, e = q.z;
+  int me = q.w;
+  if (STAGE == 1 && me < 0) {
+    // the partner's row was not staged when the pair list was written: k's
+    // position in m's (ascending) row of the finished neighbour list
+    int64_t lo = S.rs[m], hi = S.rs[m + 1];
+    while (lo < hi) {
+      const int64_t mid = (lo + hi) >> 1;
+      if (S.nbr[mid] < k) lo = mid + 1;
+      else hi = mid;
+    }
+    me = (int)lo;
+    B.pq[u] = make_int4(k, m, e, me);
+  }
   const double* const* XP = STAGE == 1 ? S.x : S.xh;
   const double* const* VP = STAGE == 1 ? S.v : S.vh;
   const double* RP = STAGE == 1 ? S.rho : S.rhoh;
@@ -28,53 +58,86 @@ __global__ void __launch_bounds__(STPB) k_pairA(StepConst c, SArr<D> S, PairBuf 
     dv[d] = VP[d][k] - VP[d][m];
   }
   const double r2 = dotD<D>(dx, dx);
-  double r;
+  const bool r2pos = dbits(r2) != 0;  // r2 is +0 or positive
+  const int ptk = S.pt[k], ptm = S.pt[m];
+  const bool mixed = (ptk > 0) != (ptm > 0);
+  double r = 0.0;
   if (STAGE == 1) {
-    const double ri = rsqrt(r2);
-    r = r2 > 0.0 ? r2 * ri : 0.0;
-    const double u1 = r * c.Hinv;
-    const double w = wc2_w(u1, c.nW);
-    const double dwk_r = wc2_dw(u1, c.nDW) * ri;
+    if (r2pos) r = sqrt_nr(r2);
+    const double uu = r * c.Hinv;
+    double w = 0.0, dwr = 0.0;
+    if (dbits(uu) < ONE_BITS) {
+      const double t = 1.0 - uu;
+      const double t2 = t * t;
+      w = ((1.0 + 4.0 * uu) * (t2 * t2)) * c.nW;
+      dwr = (t2 * t) * c.dWr;
+    }
+    if (!r2pos) dwr = NAN;  // the reference's d𝒲(0)/0
     S.We[e] = w;
     S.We[me] = w;
 #pragma unroll
     for (int d = 0; d < D; ++d) {
-      gw[d] = dx[d] * dwk_r;
+      gw[d] = dx[d] * dwr;
       S.gWe[d][e] = gw[d];
       S.gWe[d][me] = -gw[d];
     }
   } else {
-    r = c.use_pF ? (r2 > 0.0 ? r2 * rsqrt(r2) : 0.0) : 0.0;
+    if (c.use_pF && r2pos) r = sqrt_nr(r2);
 #pragma unroll
     for (int d = 0; d < D; ++d) gw[d] = S.gWe[d][e];
   }
-  const int ptk = S.pt[k], ptm = S.pt[m];
   const double rk = RP[k], rm = RP[m], irk = IP[k], irm = IP[m];
   const bool both = ptk > 0 && ptm > 0;
   double dk = 0.0, dm = 0.0;
-  const double inv_r2eta = both ? 1.0 / (r2 + c.eta2) : 0.0;
+  double sg = ptk * ptm > 0 ? -c.m0 * ((PP[k] + PP[m]) * (irk * irm)) : 0.0;
+  double visc = 0.0;
   if (both) {
-    // ∂ρ∂tDDT!, src/gpukernels_sph.jl:520-575, both sides of the pair
-    const double dot3 = -dotD<D>(dx, gw);
+    const double inv = rcp_nr(r2 + c.eta2);
     const double m0dot = c.m0 * dotD<D>(dv, gw);
     dk = m0dot;
     dm = m0dot;
-    const double ez = c.DDTgz * dx[1];
-    if (ptk > 1) {
-      const double dp = c.rho0 * (1.0 + pf7m1_fast(ez, c.ginv, c.gamma)) - c.rho0;
-      dk += c.DDTkh * ((rm - rk) - dp) * inv_r2eta * dot3 * c.m0 * irm;
+    if (ptk > 1 || ptm > 1) {
+      const double com = c.DDTkhm0 * (-dotD<D>(dx, gw)) * inv;
+      const double ez = c.DDTgz * dx[1];
+      const double drr = rm - rk;
+      if (ptk > 1) {
+        const double dp = c.rho0 * (1.0 + pf7m1_fast(ez, c.ginv, c.gamma)) - c.rho0;
+        dk += (drr - dp) * com * irm;
+      }
+      if (ptm > 1) {
+        const double dn = c.rho0 * (1.0 + pf7m1_fast(-ez, c.ginv, c.gamma)) - c.rho0;
+        dm += (-drr - dn) * com * irk;
+      }
     }
-    if (ptm > 1) {
-      const double dn = c.rho0 * (1.0 + pf7m1_fast(-ez, c.ginv, c.gamma)) - c.rho0;
-      dm += c.DDTkh * ((rk - rm) - dn) * inv_r2eta * dot3 * c.m0 * irk;
+    const double cond = dotD<D>(dv, dx);
+    const bool av = neg_int(cond);
+    if (av || c.use_visc) {
+      const double isum = rcp_nr(rk + rm);
+      if (av) sg += c.avK * cond * inv * isum;
+      if (c.use_visc) visc = 4.0 * c.nu * c.m0 * dotD<D>(dx, gw) * isum * inv;
     }
   }
   double f[D];
-  pair_force_fast<D>(c, ptk, ptm, dx, r2, inv_r2eta, gw, dv, rk, rm, irk, irm, PP[k], PP[m], f);
-  double dxf[D];
 #pragma unroll
-  for (int d = 0; d < D; ++d) dxf[d] = STAGE == 1 ? dx[d] : S.x[d][k] - S.x[d][m];
-  pair_tail_terms<D, STAGE>(c, ptk, ptm, dxf, dx, r, f);
+  for (int d = 0; d < D; ++d) f[d] = c.use_visc ? fma(visc, dv[d], sg * gw[d]) : sg * gw[d];
+  if (mixed) {
+    if (STAGE == 1) {
+      fb_pair<D>(c, dx, r2, r, f);
+    } else {
+      double dxf[D];
+#pragma unroll
+      for (int d = 0; d < D; ++d) dxf[d] = S.x[d][k] - S.x[d][m];
+      const double r2f = dotD<D>(dxf, dxf);
+      fb_pair<D>(c, dxf, r2f, dbits(r2f) != 0 ? sqrt_nr(r2f) : 0.0, f);
+    }
+  }
+  if (c.use_pF) {
+    Acc<D> A;
+    A.zero();
+    pf_term<D>(c, A, ptk, ptm, dx, r);
+#pragma unroll
+    for (int d = 0; d < D; ++d) f[d] += A.pf[d];
+  }
   B.cd[e] = dk;
   B.cd[me] = dm;
 #pragma unroll
@@ -82,6 +145,28 @@ __global__ void __launch_bounds__(STPB) k_pairA(StepConst c, SArr<D> S, PairBuf 
     B.ca[d][e] = f[d];
     B.ca[d][me] = -f[d];
   }
+}
+
+// Pass A over all pairs.  The grid holds at most the SMs' resident blocks,
+// and each warp claims 32 consecutive pairs at a time from a counter, until
+// none is left: an SM whose pairs were cheap (boundary rows) takes more,
+// where a grid of one thread per pair ends on its slowest SM.  The last
+// block to finish resets the counter for the next pass.
+template <int D, int STAGE>
+__global__ void __launch_bounds__(STPB) k_pairA(StepConst c, SArr<D> S, PairBuf B) {
+  if (!*S.ovf) {
+    const int64_t np = *B.npair;
+    const int lane = threadIdx.x & 31;
+    for (;;) {
+      unsigned long long base = 0;
+      if (lane == 0) base = atomicAdd(B.next, 32ull);
+      base = __shfl_sync(0xffffffffu, base, 0);
+      if ((int64_t)base >= np) break;
+      const int64_t u = (int64_t)base + lane;
+      if (u < np) pairA_one<D, STAGE>(c, S, B, u);
+    }
+  }
+  if (last_block_of_grid(B.done) && threadIdx.x == 0) *B.next = 0ull;
 }
 
 // pass B, stage 1: row sums + the three half-step predictors
@@ -179,9 +264,10 @@ __global__ void __launch_bounds__(STPB) k_pairB2(StepConst c, Scal* __restrict__
 
 
 template <int D>
-int launch_pairA(int stage, int64_t threads, cudaStream_t st, const StepConst& c, const SArr<D>& S,
+int launch_pairA(int stage, int64_t threads, int blocks_max, cudaStream_t st, const StepConst& c, const SArr<D>& S,
                  const PairBuf& B) {
-  const int g = nblocks(threads, STPB);
+  int g = nblocks(threads, STPB);
+  if (g > blocks_max) g = blocks_max;
   if (stage == 1)
     k_pairA<D, 1><<<g, STPB, 0, st>>>(c, S, B);
   else
@@ -211,8 +297,8 @@ int launch_pairB(int stage, int L, int64_t N, cudaStream_t st, const StepConst& 
   return GCSPH_OK;
 }
 
-template int launch_pairA<2>(int, int64_t, cudaStream_t, const StepConst&, const SArr<2>&, const PairBuf&);
-template int launch_pairA<3>(int, int64_t, cudaStream_t, const StepConst&, const SArr<3>&, const PairBuf&);
+template int launch_pairA<2>(int, int64_t, int, cudaStream_t, const StepConst&, const SArr<2>&, const PairBuf&);
+template int launch_pairA<3>(int, int64_t, int, cudaStream_t, const StepConst&, const SArr<3>&, const PairBuf&);
 template int launch_pairB<2>(int, int, int64_t, cudaStream_t, const StepConst&, Scal*, const SArr<2>&,
                              const PairBuf&);
 template int launch_pairB<3>(int, int, int64_t, cudaStream_t, const StepConst&, Scal*, const SArr<3>&,

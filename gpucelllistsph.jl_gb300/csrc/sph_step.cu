@@ -647,6 +647,8 @@ struct sph_handle {
       GWe[3], IR, IRH;
   DevBuf PT_b, BUF2_b[3];  // spares for the in-loop re-sort
   DevBuf CD, CA[3], PQ;     // pair-once passes: per-entry contributions, flat pair list
+  DevBuf PAWORK;            // pass A's work counters (next pair; finished blocks), zeroed once
+  int pa_blocks = 1024;     // pass A's grid: the SMs' resident blocks
   int ix = 0, ixh = 0, iv = 0, ivh = 0, irho = 0, irhoh = 0;
   int64_t we_cap = 0;
   int lanes = 0;  // lanes per particle in the pair passes; 0 = by mean row length
@@ -687,6 +689,9 @@ static StepConst make_const(const sph_handle* h) {
     c.nW = wc2_norm_w<3>(c.Hinv);
     c.nDW = wc2_norm_dw<3>(c.Hinv);
   }
+  c.dWr = -20.0 * c.nDW * c.Hinv;
+  c.DDTkhm0 = c.DDTkh * p.m0;
+  c.avK = 2.0 * p.alpha * p.c0 * p.h * p.m0;
   c.twoh = 2.0 * p.h;
   c.pfc = 1.5 * GCSPH_PI64;
   c.hp1 = 0.1 * p.h;
@@ -788,6 +793,8 @@ static PairBuf make_pairbuf(sph_handle* h) {
   for (int d = 0; d < D; ++d) B.ca[d] = h->CA[d].as<double>();
   B.pq = h->PQ.as<int4>();
   B.npair = h->cl->core.rs_up.as<int64_t>() + h->N;
+  B.next = h->PAWORK.as<unsigned long long>();
+  B.done = (unsigned*)(h->PAWORK.as<unsigned long long>() + 1);
   return B;
 }
 
@@ -878,15 +885,21 @@ static int rebuild(sph_handle* h, const StepConst& c, int* ovf_dev) {
   }
   const double* xs[3] = {h->X[h->ix][0].as<double>(), h->X[h->ix][1].as<double>(),
                          D == 3 ? h->X[h->ix][2].as<double>() : nullptr};
-  if ((rc = core.build_pairs(xs, ovf_dev, true, pf_ready))) return rc;
+  // the flat pair list comes with the fill when the capacity stays (pass A
+  // resolves the mirror of a pair whose partner's row was too long to stage)
+  bool pq_done = false;
+  int4* pq = h->we_cap >= core.nbr_cap && core.nbr_cap > 0 ? h->PQ.as<int4>() : nullptr;
+  if ((rc = core.build_pairs(xs, ovf_dev, true, pf_ready, pq, &pq_done))) return rc;
   if ((rc = grow_entry_arrays<D>(h))) return rc;
-  // flat pair list: offsets scanned with the row offsets (no read-back), then the quads
-  timer_begin(T_PAIRS, core.st);
-  k_pair_quads<<<nblocks(h->N * QL, 256), 256, 0, core.st>>>(h->N, core.rs_full.as<int64_t>(), core.nbr.as<int32_t>(),
-                                                         core.cnt_full.as<int32_t>(), core.cnt_up.as<int32_t>(),
-                                                         core.rs_up.as<int64_t>(), ovf_dev, h->PQ.as<int4>());
-  GC_LAUNCHED();
-  timer_end(T_PAIRS, core.st);
+  if (!pq_done) {
+    // flat pair list: offsets scanned with the row offsets (no read-back), then the quads
+    timer_begin(T_PAIRS, core.st);
+    k_pair_quads<<<nblocks(h->N * QL, 256), 256, 0, core.st>>>(
+        h->N, core.rs_full.as<int64_t>(), core.nbr.as<int32_t>(), core.cnt_full.as<int32_t>(),
+        core.cnt_up.as<int32_t>(), core.rs_up.as<int64_t>(), ovf_dev, h->PQ.as<int4>());
+    GC_LAUNCHED();
+    timer_end(T_PAIRS, core.st);
+  }
   return GCSPH_OK;
 }
 
@@ -910,7 +923,7 @@ static int rebuild(sph_handle* h, const StepConst& c, int* ovf_dev) {
 // pair count itself stays on the device); pass B: L lanes per row
 #define PAIRA_LAUNCH(STAGE, ...)                                                              \
   do {                                                                                        \
-    const int _rc = launch_pairA<D>(STAGE, h->cl->core.nbr_cap / 2 + 1, st, __VA_ARGS__);     \
+    const int _rc = launch_pairA<D>(STAGE, h->cl->core.nbr_cap / 2 + 1, h->pa_blocks, st, __VA_ARGS__); \
     if (_rc) return _rc;                                                                      \
   } while (0)
 
@@ -1397,6 +1410,16 @@ int sph_create(gcl_handle* cl, const gcsph_params* prm, double* rho_dev, double*
   E(h->DRHO, nb, true);
   E(h->PLAST, nb, true);
   E(h->scal, sizeof(Scal), true);
+  E(h->PAWORK, 2 * sizeof(unsigned long long), true);
+  if (!rc) {
+    // pass A's grid: eight blocks per SM at most (the registers of its
+    // STPB-thread blocks allow seven or eight), all resident at once
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) == cudaSuccess && cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) ==
+                                                   cudaSuccess && sms > 0)
+      h->pa_blocks = 8 * sms;
+    cudaGetLastError();
+  }
   if (!rc) {
     cudaError_t e = cudaMallocHost((void**)&h->pin, sizeof(Scal));
     if (e != cudaSuccess) rc = cuda_fail(e, "cudaMallocHost", __FILE__, __LINE__);
@@ -1431,6 +1454,7 @@ void sph_destroy(sph_handle* h) {
   for (DevBuf* b : one) b->release();
   h->CD.release();
   h->PQ.release();
+  h->PAWORK.release();
   for (int d = 0; d < 3; ++d) {
     h->CA[d].release();
     h->BUF2_b[d].release();

@@ -14,6 +14,9 @@ static constexpr int STPB = 128;
 struct StepConst {
   double h, eta2, m0, rho0, ginv, DDTkh, DDTgz, P0, alpha, c0, nu, g, s, Hinv, nW, nDW;
   double fb_d, fb_r0, fb_eta2;  // fbmolforce constants of the stage being run
+  // pair-once products of the constants: d𝒲/r = dWr (1 - u)^3 (u / r = H⁻¹),
+  // δ-SPH's DDTkh m₀, and ∂v∂t_av!'s 2 α c₀ h m₀
+  double dWr, DDTkhm0, avK;
   double twoh, pfc, hp1;        // 2h, 1.5*pi, 0.1h  (∂v∂tpF!)
   double dpc_l0inv, dpc_nW, dpc_whinv, dpc_pmin, dpc_pmax, dpc_lambda, dpc_kernlim, dpc_eta2;
   double dpc_r2cut;  // l0² (1 + 1e-6): past it u = √r² / l0 >= 1 whatever the rounding
@@ -327,27 +330,80 @@ __device__ inline void group_sum_acc(Acc<D>& A, const StepConst& c, unsigned gm)
 struct PairBuf {
   double* cd;             // ∂ρ/∂t contribution per neighbour entry
   double* ca[3];          // ∂v/∂t contribution per neighbour entry (gravity not included)
-  const int4* pq;         // (k, m, e, mirror(e)) of every pair, k < m
+  int4* pq;               // (k, m, e, mirror(e)) of every pair, k < m (mirror -1: stage 1 finds it)
   const int64_t* npair;   // number of pairs (device scalar)
+  // pass A's work distribution: [0] the next unclaimed pair, reset by the
+  // pass's last block; done counts the finished blocks (last_block_of_grid)
+  unsigned long long* next;
+  unsigned* done;
 };
+
+// ---------------------------------------------------------------------------
+// Pair-once arithmetic.  The FP64 pipe is the bound of pass A (2 FP64
+// thread-instructions per cycle per SM on GB300), so its compares run on the
+// integer pipe over the bit patterns, and its reciprocals and its root are
+// Newton-Raphson iterations from the hardware's approximate reciprocal and
+// reciprocal square root (rcp.approx / rsqrt.approx .f64, about 2^-22
+// relative): two steps each, quadratic convergence, a result within a few
+// ulp -- fewer FP64 instructions than the IEEE-rounded sequences, inside the
+// FP64 contract this path is held to.
+// ---------------------------------------------------------------------------
+__device__ inline long long dbits(double x) { return __double_as_longlong(x); }
+constexpr long long ONE_BITS = 0x3FF0000000000000LL;  // bits of 1.0
+// x < 0.0 exactly as the FP compare (-0.0 and NaN are not), on the integer pipe
+__device__ inline bool neg_int(double x) {
+  return (unsigned long long)dbits(x) - 0x8000000000000001ull < 0x7FF0000000000000ull;
+}
+
+// 1/x, x normal (Newton-Raphson: y <- y + y (1 - x y))
+__device__ inline double rcp_nr(double x) {
+  double y;
+  asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
+  double e = fma(-x, y, 1.0);
+  y = fma(y, e, y);
+  e = fma(-x, y, 1.0);
+  return fma(y, e, y);
+}
+
+// sqrt(x), x normal and positive (Newton-Raphson on 1/sqrt(x):
+// y <- y + y (1/2 - (x/2) y^2), then x y)
+__device__ inline double sqrt_nr(double x) {
+  double y;
+  asm("rsqrt.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
+  const double hx = 0.5 * x;
+  double e = fma(-hx, y * y, 0.5);
+  y = fma(y, e, y);
+  e = fma(-hx, y * y, 0.5);
+  y = fma(y, e, y);
+  return x * y;
+}
 
 // powfancy7th(x) - 1 for x = 1 + eps, src/gpukernels_sph.jl:499-515.  Where
 // |eps| <= PF7_EPS_MAX the exact Taylor series of that iteration's output
-// (gen_pf7_series.py, bias included) replaces its two divisions; elsewhere
-// the iteration itself runs.  eps is taken as (1 + eps) - 1, the argument the
+// (gen_pf7_series.py, bias included) replaces its two divisions, and where
+// |eps| <= PF7_EPS_SHORT its first PF7_SHORT_N terms do; elsewhere the
+// iteration itself runs.  eps is taken as (1 + eps) - 1, the argument the
 // reference's rounded x carries.  Callers form ρ0 (1 + r) - ρ0 as the
 // reference forms ρ0 t - ρ0: 1 + r rounds to the t the iteration returns.
 __device__ inline double pf7m1_fast(double eps_in, double ginv, int gamma) {
   const double x = 1.0 + eps_in;
   const double e = x - 1.0;  // exact for x in [0.5, 2]
-  if (gamma == 7 && fabs(e) <= PF7_EPS_MAX) {
+  const long long ae = dbits(e) & 0x7FFFFFFFFFFFFFFFLL;
+  static_assert(PF7_UP_N == PF7_LO_N, "series lengths");
+  if (gamma == 7 && ae <= dbits(PF7_EPS_MAX)) {
     const double cu[PF7_UP_N] = PF7_UP_C;
     const double cl[PF7_LO_N] = PF7_LO_C;
-    static_assert(PF7_UP_N == PF7_LO_N, "series lengths");
-    const bool up = e >= 0.0;
-    double r = up ? cu[PF7_UP_N - 1] : cl[PF7_UP_N - 1];
+    const bool up = dbits(e) >= 0;
+    double r;
+    if (ae <= dbits(PF7_EPS_SHORT)) {
+      r = up ? cu[PF7_SHORT_N - 1] : cl[PF7_SHORT_N - 1];
 #pragma unroll
-    for (int i = PF7_UP_N - 2; i >= 0; --i) r = fma(r, e, up ? cu[i] : cl[i]);
+      for (int i = PF7_SHORT_N - 2; i >= 0; --i) r = fma(r, e, up ? cu[i] : cl[i]);
+    } else {
+      r = up ? cu[PF7_UP_N - 1] : cl[PF7_UP_N - 1];
+#pragma unroll
+      for (int i = PF7_UP_N - 2; i >= 0; --i) r = fma(r, e, up ? cu[i] : cl[i]);
+    }
     return r;
   }
   return powfancy7th_1div(x, ginv, gamma) - 1.0;
@@ -398,7 +454,7 @@ __device__ inline void row_sums(const SArr<D>& S, const PairBuf& B, int64_t k, i
 // pair-once passes (sph_once.cu): pass A over `threads` pair slots, pass B
 // (row sums + predictor / corrector) with L lanes per particle
 template <int D>
-int launch_pairA(int stage, int64_t threads, cudaStream_t st, const StepConst& c, const SArr<D>& S,
+int launch_pairA(int stage, int64_t threads, int blocks_max, cudaStream_t st, const StepConst& c, const SArr<D>& S,
                  const PairBuf& B);
 template <int D>
 int launch_pairB(int stage, int L, int64_t N, cudaStream_t st, const StepConst& c, Scal* sc, const SArr<D>& S,

@@ -322,6 +322,9 @@ int ens_remove(gcsph_ens* e, int32_t slot);
 /* n steps of every instance (a captured graph per n; the first steps after a
  * layout change may time three block sizes -- ordinary steps all the same) */
 int ens_step(gcsph_ens* e, int32_t n);
+/* the stream of the ensemble's later calls (NULL: the legacy default
+ * stream); waits for the work of the current one first */
+int ens_set_stream(gcsph_ens* e, void* stream);
 /* one field of one instance, in its original particle order, as double */
 int ens_get(gcsph_ens* e, int32_t slot, int32_t field, double* out_host);
 int ens_info(gcsph_ens* e, int32_t slot, int64_t* n, int64_t* steps, double* etime);

@@ -254,3 +254,37 @@ def test_tiny_and_degenerate_sets(gpu_pkg, orc, D):
     bad[D - 1, 2] = np.nan
     with pytest.raises(RuntimeError, match="NaN"):
         gpu_pkg.GPUCellList(tuple(bad), (dist,) * D, dist)
+
+
+def test_one_crowded_cell(gpu_pkg):
+    """10^5 points in one cell (cellsize 1 over the unit square, dist 0.002):
+    sets of this size take the stable radix sort, whose cost has no term in
+    the square of a cell's population, and update! (binning + pair search)
+    completes in under 50 ms after a warm-up.  The pair set equals the
+    reference's test r² < dist² (every pair of this grid is a candidate),
+    evaluated here from scipy cKDTree candidates."""
+    import time
+    from scipy.spatial import cKDTree
+    N, dist = 100_000, 0.002
+    x = gpu_pkg.workloads.uniform_points(N, 2, seed=31)
+    c = gpu_pkg.GPUCellList(tuple(x), (1.0, 1.0), dist)
+    assert int(c.cellpnum.max().item()) > N // 4
+    c.update()
+    ts = []
+    for _ in range(3):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        c.update()
+        torch.cuda.synchronize()
+        ts.append(time.perf_counter() - t0)
+    print(f"\n[crowded cell] update! of {N} points in {len(c.grid)}-D grid {c.grid}: {min(ts) * 1e3:.2f} ms")
+    assert min(ts) < 0.050
+    cand = cKDTree(x.T).query_pairs(dist * (1 + 1e-7), output_type="ndarray")
+    i, j = cand[:, 0], cand[:, 1]
+    d0 = x[0, i] - x[0, j]
+    d1 = x[1, i] - x[1, j]
+    keep = (d0 * d0 + d1 * d1) < dist * dist
+    want = np.sort((np.minimum(i, j)[keep] + 1) * (1 << 32) + np.maximum(i, j)[keep] + 1)
+    got = c.neighborlistview().cpu().numpy().astype(np.int64)
+    assert c.pairsn == want.size
+    assert np.array_equal(np.sort(got[:, 0] * (1 << 32) + got[:, 1]), want)

@@ -205,6 +205,18 @@ def test_dam_break_2d_c1_100_steps(gpu_pkg, orc, lanes):
     assert not bad, f"per-element relative errors over their bounds: {bad}"
 
 
+def test_large_set_radix_order_serial_rows(gpu_pkg, orc):
+    """A 2-D dam break of 82k particles (dx = 0.005): sets above 65,536
+    points are ordered by the stable radix sort, the re-sort inside the step
+    included, and the serial rows stay bit-identical to the oracle -- the
+    radix order is the counting sort's (cell, original index) order."""
+    case = gpu_pkg.workloads.dam_break_2d(dx=0.005)
+    assert case.N > 65536
+    prob, ref = make_pair(gpu_pkg, orc, case, lanes=1)
+    run_both(prob, ref, 3)
+    compare(prob, ref, case, exact=True)
+
+
 @pytest.mark.parametrize("lanes", [1, 0])
 def test_fixture_dp002_readme_parameters(gpu_pkg, orc, lanes):
     """The reference's own 2-D fixture (ptype 2 / 1 / 0, hydrostatic ρ) with
