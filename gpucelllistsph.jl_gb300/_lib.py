@@ -87,6 +87,7 @@ _SIGS = {
     "gcl_emit_pairs": (C.c_int, [vp, vp, i64, C.c_int, C.POINTER(i64)]),
     "gcl_cellpnum": (C.c_int, [vp, vp]),
     "gcl_maxpairs": (C.c_int, [vp, C.POINTER(i64)]),
+    "gcl_set_sort": (C.c_int, [vp, i32]),
     "gcl_pairs_noalloc": (C.c_int, [i32, i64, PP, C.POINTER(f64), f64, C.POINTER(f64), C.POINTER(f64), vp, i64,
                                     C.c_int, C.POINTER(i64), vp]),
     "gcl_pairs_noalloc_init": (C.c_int, []),

@@ -143,6 +143,13 @@ class GPUCellList:
         _lib.check(_lib.load().gcl_maxpairs(self._h, C.byref(mp)))
         return int(mp.value)
 
+    def set_sort(self, mode: int):
+        """The order inside a cell of the binning (no reference counterpart):
+        0 = chosen by the most crowded cell (default), 1 = the counting sort's
+        in-cell rank, 2 = the stable radix sort (sets above 65,536 points).
+        The pair list and every result are the same for each choice."""
+        _lib.check(_lib.load().gcl_set_sort(self._h, int(mode)))
+
     def close(self):
         h = getattr(self, "_h", None)
         if h:

@@ -98,11 +98,15 @@ int bounding_box(int D, const double* const* x, int64_t N, int nb, double* part_
 // ---------------------------------------------------------------------------
 // With fold_cnt the last block to finish also scans the counts into
 // cellstart (grids of at most SCAN_FOLD_MAX - 1 cells): no separate scan.
+// With popmax the largest population of a cell goes to *popmax (which the
+// caller zeroed): one atomic per warp.
 template <int D>
 __global__ void k_cellkey(const double* __restrict__ x0, const double* __restrict__ x1, const double* __restrict__ x2,
                           int64_t N, Grid g, int32_t* __restrict__ key, int32_t* __restrict__ slot,
-                          int32_t* __restrict__ count, int32_t* __restrict__ cellstart, unsigned* fold_cnt) {
+                          int32_t* __restrict__ count, int32_t* __restrict__ cellstart, unsigned* fold_cnt,
+                          int* popmax) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int pop = 0;
   if (i < N) {
     const double* xs[3] = {x0, x1, x2};
     int64_t lin = 0, stride = 1;
@@ -115,7 +119,13 @@ __global__ void k_cellkey(const double* __restrict__ x0, const double* __restric
       stride *= g.nc[d];
     }
     key[i] = (int32_t)lin;
-    slot[i] = atomicAdd(&count[lin], 1);
+    slot[i] = pop = atomicAdd(&count[lin], 1);
+    ++pop;
+  }
+  if (popmax) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) pop = max(pop, __shfl_xor_sync(0xffffffffu, pop, o));
+    if ((threadIdx.x & 31) == 0 && pop > 0) atomicMax(popmax, pop);
   }
   if (fold_cnt && last_block_of_grid(fold_cnt)) block_exclusive_scan<int32_t>(count, cellstart, g.ncell);
 }
@@ -500,6 +510,7 @@ int CellCore::init(int D_, int64_t N_, const double* cellsize, double dist_, con
     }
     if ((rc = rhist.ensure(sizeof(int32_t) * 256 * ntiles, st))) return rc;
     if ((rc = rhoff.ensure(sizeof(int32_t) * (256 * ntiles + 1), st))) return rc;
+    if ((rc = popmax.ensure(sizeof(int), st, true))) return rc;
     if (scan_scratch_elems(256 * ntiles + 1) > sc) return fail(GCSPH_EINVAL, "radix scan scratch");
   }
   return GCSPH_OK;
@@ -508,36 +519,43 @@ int CellCore::init(int D_, int64_t N_, const double* cellsize, double dist_, con
 void CellCore::release() {
   DevBuf* all[] = {&count, &cellstart, &key, &slot, &tmp, &perm, &skey, &orig, &cnt_full, &cnt_up, &rs_full,
                    &rs_up, &nbr, &scratch, &pf[0], &pf[1], &pf[2], &pfmax, &pfthr, &pfcnt, &orig_b, &stage,
-                   &foldcnt, &rkey[0], &rkey[1], &rval[0], &rval[1], &rhist, &rhoff};
+                   &foldcnt, &rkey[0], &rkey[1], &rval[0], &rval[1], &rhist, &rhoff, &popmax};
   for (DevBuf* b : all) b->release();
   if (pin) cudaFreeHost(pin);
   pin = nullptr;
 }
 
-int CellCore::sort(const double* const* xin, const int32_t* ord) {
+int CellCore::sort(const double* const* xin, const int32_t* ord, bool may_sync) {
   timer_begin(T_SORT, st);
   GC_CUDA(cudaMemsetAsync(count.p, 0, sizeof(int32_t) * g.ncell, st));
   const double* x2 = D == 3 ? xin[2] : xin[0];
   int rc;
   const bool fold = g.ncell + 1 <= SCAN_FOLD_MAX;
   unsigned* fc = fold ? foldcnt.as<unsigned>() : nullptr;
+  // large sets track the most crowded cell, which picks the in-cell ordering
+  int* pm = N > RADIX_MIN_N ? popmax.as<int>() : nullptr;
+  if (pm) GC_CUDA(cudaMemsetAsync(pm, 0, sizeof(int), st));
   if (D == 2)
     k_cellkey<2><<<nblocks(N, TPB), TPB, 0, st>>>(xin[0], xin[1], x2, N, g, key.as<int32_t>(), slot.as<int32_t>(),
-                                                   count.as<int32_t>(), cellstart.as<int32_t>(), fc);
+                                                   count.as<int32_t>(), cellstart.as<int32_t>(), fc, pm);
   else
     k_cellkey<3><<<nblocks(N, TPB), TPB, 0, st>>>(xin[0], xin[1], x2, N, g, key.as<int32_t>(), slot.as<int32_t>(),
-                                                   count.as<int32_t>(), cellstart.as<int32_t>(), fc);
+                                                   count.as<int32_t>(), cellstart.as<int32_t>(), fc, pm);
   GC_LAUNCHED();
   if (!fold) {
     rc = exclusive_scan_i32_to_i32(count.as<int32_t>(), cellstart.as<int32_t>(), g.ncell, scratch.as<int64_t>(), st);
     if (rc) return rc;
   }
+  if (pm && may_sync && sort_mode == 0 && (rc = read_popmax())) return rc;
+  // the in-cell order: the counting sort's rank costs the square of a cell's
+  // population per cell, the radix sort a fixed few passes over the set
+  const bool radix = N > RADIX_MIN_N && (sort_mode == 2 || (sort_mode == 0 && last_popmax > RADIX_MIN_POP));
   // ord may be `orig` itself (re-sorting particles already in cell order), so
   // the new map is written to the spare buffer and the two are swapped
   int rc2 = orig_b.ensure(sizeof(int32_t) * N, st);
   if (rc2) return rc2;
-  if (N > RADIX_MIN_N) {
-    // large sets: the stable radix sort of the keys in original order
+  if (radix) {
+    // crowded cells of a large set: the stable radix sort of the keys in original order
     const int64_t ntiles = (N + RADIX_TILE - 1) / RADIX_TILE;
     int bits = 1;
     while (bits < 31 && (1LL << bits) < g.ncell) ++bits;
@@ -573,11 +591,13 @@ int CellCore::sort(const double* const* xin, const int32_t* ord) {
                                                    orig_b.as<int32_t>());
     GC_LAUNCHED();
   } else {
-    k_scatter_arrival<<<nblocks(N, TPB), TPB, 0, st>>>(key.as<int32_t>(), slot.as<int32_t>(),
-                                                        cellstart.as<int32_t>(), N, tmp.as<int32_t>());
+    // small sets: 64-thread blocks, so these latency-bound passes spread over more SMs
+    const int tb = N <= RADIX_MIN_N ? 64 : TPB;
+    k_scatter_arrival<<<nblocks(N, tb), tb, 0, st>>>(key.as<int32_t>(), slot.as<int32_t>(), cellstart.as<int32_t>(),
+                                                      N, tmp.as<int32_t>());
     GC_LAUNCHED();
-    k_rank_apply<<<nblocks(N, TPB), TPB, 0, st>>>(tmp.as<int32_t>(), key.as<int32_t>(), cellstart.as<int32_t>(), ord,
-                                                   N, perm.as<int32_t>(), skey.as<int32_t>(), orig_b.as<int32_t>());
+    k_rank_apply<<<nblocks(N, tb), tb, 0, st>>>(tmp.as<int32_t>(), key.as<int32_t>(), cellstart.as<int32_t>(), ord, N,
+                                                 perm.as<int32_t>(), skey.as<int32_t>(), orig_b.as<int32_t>());
     GC_LAUNCHED();
   }
   std::swap(orig.p, orig_b.p);
@@ -586,6 +606,18 @@ int CellCore::sort(const double* const* xin, const int32_t* ord) {
   sorted = true;
   built = false;
   up_valid = false;
+  return GCSPH_OK;
+}
+
+int CellCore::read_popmax() {
+  if (N <= RADIX_MIN_N || !popmax.p) return GCSPH_OK;
+  GC_CUDA(cudaMemcpyAsync(pin + 7, popmax.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+  GC_CUDA(cudaStreamSynchronize(st));
+  const bool before = last_popmax > RADIX_MIN_POP;
+  last_popmax = *(const int*)(pin + 7);
+  // a captured step graph holds the ordering it was captured with: a change
+  // of the choice retires the captured graphs
+  if ((last_popmax > RADIX_MIN_POP) != before) ++gen;
   return GCSPH_OK;
 }
 
@@ -738,27 +770,41 @@ __device__ __forceinline__ void pairs32_row(const double* __restrict__ x0, const
     // part at every row's end (measured on GB300: update! of 4M uniform 3-D
     // points 2.43 -> 2.27 ms; in 2-D, with tens of candidates per row, the
     // row-by-row walk below stays 4% faster)
+    // The group's row table sits in shared memory; each lane keeps the row of
+    // its candidate and moves on only where its candidate passes a row's end,
+    // instead of locating every candidate among the nine rows (measured on
+    // GB300: update! of 4M uniform 3-D points 2.28 -> 2.00 ms).
     constexpr int NR = 9;
-    int32_t cum[NR], dlt[NR];
+    __shared__ int32_t s_rows[TPB / L][2 * NR + 1];  // starts (+ end sentinel), then m - t per row
+    int32_t* rows = s_rows[threadIdx.x / L];
     int32_t tot = 0;
+    if (lane == 0) {
 #pragma unroll
-    for (int r = 0; r < NR; ++r) {
-      const int z = cz + (r / 3 - 1), y = cy + (r % 3 - 1);
-      int32_t m0 = 0, m1 = 0;
-      if (z >= 0 && z < nz && y >= 0 && y < ny) {
-        const int64_t base = (int64_t)nx * ((int64_t)y + (int64_t)ny * z);
-        m0 = cellstart[base + xlo];
-        m1 = cellstart[base + xhi + 1];
+      for (int r = 0; r < NR; ++r) {
+        const int z = cz + (r / 3 - 1), y = cy + (r % 3 - 1);
+        int32_t m0 = 0, m1 = 0;
+        if (z >= 0 && z < nz && y >= 0 && y < ny) {
+          const int64_t base = (int64_t)nx * ((int64_t)y + (int64_t)ny * z);
+          m0 = cellstart[base + xlo];
+          m1 = cellstart[base + xhi + 1];
+        }
+        rows[r] = tot;
+        rows[NR + 1 + r] = m0 - tot;
+        tot += m1 - m0;
       }
-      cum[r] = tot;
-      dlt[r] = m0 - tot;
-      tot += m1 - m0;
+      rows[NR] = 0x7fffffff;
     }
+    tot = __shfl_sync(gm, tot, gbase);
+    __syncwarp(gm);
+    int r = 0;
+    int32_t next = rows[1], dd = rows[NR + 1];
     for (int32_t tb = 0; tb < tot; tb += L) {
       const int32_t t = tb + lane;
-      int32_t dd = dlt[0];
-#pragma unroll
-      for (int r = 1; r < NR; ++r) dd = t >= cum[r] ? dlt[r] : dd;
+      while (t >= next) {  // r stops at the last row: its end is the sentinel
+        ++r;
+        next = rows[r + 1];
+        dd = rows[NR + 1 + r];
+      }
       const int32_t m = t + dd;
       visit(m, t < tot && m != k);
     }
@@ -783,118 +829,6 @@ __device__ __forceinline__ void pairs32_row(const double* __restrict__ x0, const
     if (lane == 0) {
       cnt_full[k] = nf;
       cnt_up[k] = nu;
-    }
-  }
-}
-
-// ---------------------------------------------------------------------------
-// 3-D count (and stage) pass with a warp per cell, for sparse grids (a few
-// points per cell, as 4M uniform points in 125^3 cells).  The per-point pass
-// above strides each point's 27-cell neighbourhood as one candidate sequence
-// and pays, for every point and every candidate, the lookup of the candidate's
-// row.  Here a warp takes one cell: it finds the neighbourhood's nine rows
-// once, loads the candidates' FP32 offsets into registers once (CELL_SLOTS per
-// lane, so up to 32 CELL_SLOTS candidates), and every point of the cell
-// tests them from there.  Same test (FP32 prefilter, the reference's FP64
-// expression in the rounding band), same counts, rows staged ascending in m
-// (slot j, lane l holds candidate 32 j + l of the ascending sequence).  A cell
-// whose neighbourhood holds more candidates walks it in windows of that many.
-// ---------------------------------------------------------------------------
-constexpr int CELL_SLOTS = 4;
-
-__global__ void __launch_bounds__(TPB) k_pairs_cell3(const double* __restrict__ x0, const double* __restrict__ x1,
-                                                     const double* __restrict__ x2, const float* __restrict__ f0,
-                                                     const float* __restrict__ f1, const float* __restrict__ f2,
-                                                     const float2* __restrict__ thr,
-                                                     const int32_t* __restrict__ cellstart, Grid g,
-                                                     int32_t* __restrict__ cnt_full, int32_t* __restrict__ cnt_up,
-                                                     int32_t* __restrict__ stg, int S) {
-  const int64_t c = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int lane = threadIdx.x & 31;
-  if (c >= g.ncell) return;  // whole warp
-  const int32_t ks = cellstart[c], ke = cellstart[c + 1];
-  if (ks == ke) return;
-  const int nx = g.nc[0], ny = g.nc[1], nz = g.nc[2];
-  const int cx = (int)(c % nx);
-  const int64_t t0 = c / nx;
-  const int cy = (int)(t0 % ny);
-  const int cz = (int)(t0 / ny);
-  const int xlo = cx > 0 ? cx - 1 : 0;
-  const int xhi = cx < nx - 1 ? cx + 1 : nx - 1;
-  // the nine rows (z, y) of the neighbourhood, each a contiguous range of the
-  // sorted points: lane r < 9 finds row r, a shuffle scan gives the starts
-  int32_t m0 = 0, len = 0;
-  if (lane < 9) {
-    const int z = cz + (lane / 3 - 1), y = cy + (lane % 3 - 1);
-    if (z >= 0 && z < nz && y >= 0 && y < ny) {
-      const int64_t base = (int64_t)nx * ((int64_t)y + (int64_t)ny * z);
-      m0 = cellstart[base + xlo];
-      len = cellstart[base + xhi + 1] - m0;
-    }
-  }
-  int32_t cum = len;
-#pragma unroll
-  for (int o = 1; o < 16; o <<= 1) {
-    const int32_t y = __shfl_up_sync(0xffffffffu, cum, o);
-    if (lane >= o) cum += y;
-  }
-  const int32_t tot = __shfl_sync(0xffffffffu, cum, 8);
-  int32_t rstart[9], rdelta[9];  // start of row r in the sequence, and m - t within it
-#pragma unroll
-  for (int r = 0; r < 9; ++r) {
-    const int32_t cr = __shfl_sync(0xffffffffu, cum, r), lr = __shfl_sync(0xffffffffu, len, r);
-    rstart[r] = cr - lr;
-    rdelta[r] = __shfl_sync(0xffffffffu, m0, r) - rstart[r];
-  }
-  const float2 tt = *thr;
-  const float tlo = tt.x, thi = tt.y;
-  const unsigned lt = (1u << lane) - 1u;
-  constexpr int WIN = 32 * CELL_SLOTS;
-  for (int32_t w0 = 0; w0 < tot; w0 += WIN) {
-    int32_t sm[CELL_SLOTS];
-    float sx[CELL_SLOTS], sy[CELL_SLOTS], sz[CELL_SLOTS];
-#pragma unroll
-    for (int j = 0; j < CELL_SLOTS; ++j) {
-      const int32_t t = w0 + 32 * j + lane;
-      int32_t dd = rdelta[0];
-#pragma unroll
-      for (int r = 1; r < 9; ++r) dd = t >= rstart[r] ? rdelta[r] : dd;
-      sm[j] = t < tot ? t + dd : -1;
-      sx[j] = sm[j] >= 0 ? f0[sm[j]] : 0.0f;
-      sy[j] = sm[j] >= 0 ? f1[sm[j]] : 0.0f;
-      sz[j] = sm[j] >= 0 ? f2[sm[j]] : 0.0f;
-    }
-    for (int32_t k = ks; k < ke; ++k) {
-      const float ax = f0[k], ay = f1[k], az = f2[k];
-      int32_t nf = w0 > 0 ? cnt_full[k] : 0, nu = w0 > 0 ? cnt_up[k] : 0;
-      int32_t spos = nf;
-#pragma unroll
-      for (int j = 0; j < CELL_SLOTS; ++j) {
-        const int32_t m = sm[j];
-        bool hit = false;
-        if (m >= 0 && m != k) {
-          const float d0 = ax - sx[j], d1 = ay - sy[j], d2 = az - sz[j];
-          const float r2f = (d0 * d0 + d1 * d1) + d2 * d2;
-          if (r2f < tlo) {
-            hit = true;
-          } else if (!(r2f > thi)) {  // inside the band (or NaN): the reference's FP64 test
-            hit = r2_ref<3>(x0[k], x1[k], x2[k], x0[m], x1[m], x2[m]) < g.dist2;
-          }
-        }
-        const unsigned bal = __ballot_sync(0xffffffffu, hit);
-        if (stg && hit) {
-          const int32_t at = spos + __popc(bal & lt);
-          if (at < S) stg[(int64_t)k * S + at] = m;
-        }
-        spos += __popc(bal);
-        nf += __popc(bal);
-        nu += __popc(__ballot_sync(0xffffffffu, hit && m > k));
-      }
-      if (lane == 0) {
-        cnt_full[k] = nf;
-        cnt_up[k] = nu;
-      }
-      __syncwarp();
     }
   }
 }
@@ -960,10 +894,8 @@ __global__ void __launch_bounds__(TPB) k_pairs32(const double* __restrict__ x0, 
                                                  int4* __restrict__ pq) {
   pairs32_row<D, MODE == 3 ? 1 : (MODE == 4 ? 2 : MODE), L>(x0, x1, x2, f0, f1, f2, thr, skey, cellstart, N, g,
                                                              cnt_full, cnt_up, rs_full, nbr, cap, ovf, stg, S);
-  if (MODE == 4 && last_block_of_grid(fold_cnt)) {
-    block_exclusive_scan<int64_t>(cnt_full, fold_rs_full, N);
-    block_exclusive_scan<int64_t>(cnt_up, fold_rs_up, N);
-  }
+  if (MODE == 4 && last_block_of_grid(fold_cnt))
+    block_exclusive_scan2_i64(cnt_full, fold_rs_full, cnt_up, fold_rs_up, N);
   if (MODE == 3) {
     __syncwarp();  // a recomputed row's entries, written by the group's lanes, are read back
     pairs32_quads<D, L>(N, cnt_full, cnt_up, rs_full, rs_up, nbr, cap, stg, S, pq);
@@ -1085,17 +1017,11 @@ int CellCore::build_pairs(const double* const* xs, int* ovf_dev, bool scan_up, b
   int32_t* sp = nullptr;
   if (mean > 0 && (rc0 = stage.ensure(sizeof(int32_t) * (size_t)N * (size_t)S, st)) == GCSPH_OK) sp = stage.as<int32_t>();
   if (rc0) return rc0;
-  // sparse 3-D grids: a warp per cell (k_pairs_cell3)
-  const bool cell3 = D == 3 && cell_warps && candidates_per_point() <= CELL3_MAX_CAND;
   // small sets: the count pass's last block scans the row counts (both
   // arrays), so no scan launch follows
-  const bool fold = sp && !cell3 && N + 1 <= SCAN_FOLD_MAX;
+  const bool fold = sp && N + 1 <= SCAN_FOLD_MAX;
   unsigned* fc = fold ? foldcnt.as<unsigned>() + 1 : nullptr;
-  if (cell3)
-    k_pairs_cell3<<<nblocks(g.ncell * 32, TPB), TPB, 0, st>>>(xs[0], xs[1], x2, pf[0].as<float>(),
-                                                               pf[1].as<float>(), f2, thr, cellstart.as<int32_t>(), g,
-                                                               cnt_full.as<int32_t>(), cnt_up.as<int32_t>(), sp, S);
-  else if (fold)
+  if (fold)
     PAIRS32_LAUNCH(4, L, xs[0], xs[1], x2, pf[0].as<float>(), pf[1].as<float>(), f2, thr, skey.as<int32_t>(),
                    cellstart.as<int32_t>(), N, g, cnt_full.as<int32_t>(), cnt_up.as<int32_t>(), nullptr, nullptr, 0,
                    nullptr, sp, S, rs_full.as<int64_t>(), rs_up.as<int64_t>(), fc, nullptr, nullptr);
@@ -1240,7 +1166,7 @@ int CellCore::maxpairs(int64_t* out) {
 using namespace gcsph;
 
 static int gcl_full_update(gcl_handle* h) {
-  int rc = h->core.sort(h->xuser, nullptr);
+  int rc = h->core.sort(h->xuser, nullptr, true);
   if (rc) return rc;
   double* xs[3] = {h->xs[0].as<double>(), h->xs[1].as<double>(), h->core.D == 3 ? h->xs[2].as<double>() : nullptr};
   if ((rc = h->core.gather_positions(h->xuser, xs))) return rc;
@@ -1331,6 +1257,13 @@ int gcl_cellpnum(gcl_handle* h, int32_t* cellpnum_dev) {
 int gcl_maxpairs(gcl_handle* h, int64_t* out) {
   if (!h || !out) return fail(GCSPH_EINVAL, "null argument");
   return h->core.maxpairs(out);
+}
+
+int gcl_set_sort(gcl_handle* h, int32_t mode) {
+  if (!h) return fail(GCSPH_EINVAL, "null handle");
+  if (mode < 0 || mode > 2) return fail(GCSPH_EINVAL, "sort mode %d (0, 1 or 2)", (int)mode);
+  h->core.sort_mode = mode;
+  return GCSPH_OK;
 }
 
 }  // extern "C"
@@ -1545,7 +1478,7 @@ static int run(int64_t N, const double* const* x, const double* cellsize, double
   // so the per-cell counters are cleared first
   GC_CUDA(cudaMemsetAsync(count, 0, sizeof(int32_t) * ncell, st));
   const double* x2 = D == 3 ? x[2] : x[0];
-  k_cellkey<D><<<nblocks(N, TPB), TPB, 0, st>>>(x[0], x[1], x2, N, g, key, slot, count, nullptr, nullptr);
+  k_cellkey<D><<<nblocks(N, TPB), TPB, 0, st>>>(x[0], x[1], x2, N, g, key, slot, count, nullptr, nullptr, nullptr);
   GC_LAUNCHED();
   if ((rc = exclusive_scan_i32_to_i32(count, cstart, ncell, scan, st))) return rc;
   k_scatter_arrival<<<nblocks(N, TPB), TPB, 0, st>>>(key, slot, cstart, N, tmpv);

@@ -69,9 +69,9 @@ int bounding_box(int D, const double* const* x, int64_t N, int nb, double* part_
 // sets of more points than this are ordered by the stable radix sort (O(N));
 // smaller ones by the counting sort's in-cell rank (fewer launches)
 constexpr int64_t RADIX_MIN_N = 65536;
-// the 3-D count pass takes a warp per cell where a point has at most this
-// many candidates (the warp's registers hold 128 of them at a time)
-constexpr double CELL3_MAX_CAND = 96.0;
+// ... and then only where a cell holds more than this many points (below it
+// the rank's cost is a few loads per point and takes fewer launches)
+constexpr int RADIX_MIN_POP = 128;
 
 struct CellCore {
   int D = 2;
@@ -93,7 +93,9 @@ struct CellCore {
   int64_t gen = 0;        // bumped whenever a buffer a captured step graph points into is reallocated
   bool sorted = false, built = false, up_valid = false;
   int lanes = 0;  // lanes per particle in the pair search; 0 = by mean candidate count
-  bool cell_warps = true;  // sparse 3-D grids: the count pass with a warp per cell (k_pairs_cell3)
+  int sort_mode = 0;    // in-cell order: 0 by the population, 1 counting sort's rank, 2 radix sort
+  int last_popmax = 0;  // largest cell population seen (large sets; read where the host waits anyway)
+  DevBuf popmax;
   int pair_lanes() const;
   // candidates (points in the 3^D stencil) per point: from the last build's
   // neighbour count, else from the grid-wide mean per cell
@@ -104,7 +106,10 @@ struct CellCore {
   void release();
   // bin xin (input order) into the frozen grid and sort by (cell, ord[i]);
   // ord == nullptr means the input order is the original order.
-  int sort(const double* const* xin, const int32_t* ord);
+  // may_sync: the caller waits anyway, so the most crowded cell of this very
+  // binning is read back to pick the ordering (else the last one read)
+  int sort(const double* const* xin, const int32_t* ord, bool may_sync = false);
+  int read_popmax();
   // gather xs[d][k] = xin[d][perm[k]] (and orig[k] = ord[perm[k]] is done by sort)
   int gather_positions(const double* const* xin, double* const* xs);
   // gather xs[d][k] = xorig[d][orig[k]] for partial updates

@@ -147,26 +147,19 @@ __device__ __forceinline__ void pairA_one(const StepConst& c, const SArr<D>& S, 
   }
 }
 
-// Pass A over all pairs.  The grid holds at most the SMs' resident blocks,
-// and each warp claims 32 consecutive pairs at a time from a counter, until
-// none is left: an SM whose pairs were cheap (boundary rows) takes more,
-// where a grid of one thread per pair ends on its slowest SM.  The last
-// block to finish resets the counter for the next pass.
+// Pass A over all pairs, 32 consecutive pairs per warp.  The pairs come in
+// cell order, so the costly fluid pairs and the cheap boundary pairs sit in
+// runs; a grid that took its warps' chunks in that order would end on the
+// SMs that drew fluid runs.  Warp w takes chunk (w * spread) mod W instead
+// (W warps in the grid, spread coprime to W: a permutation of the chunks),
+// which gives every block chunks from all over the list.
 template <int D, int STAGE>
-__global__ void __launch_bounds__(STPB) k_pairA(StepConst c, SArr<D> S, PairBuf B) {
-  if (!*S.ovf) {
-    const int64_t np = *B.npair;
-    const int lane = threadIdx.x & 31;
-    for (;;) {
-      unsigned long long base = 0;
-      if (lane == 0) base = atomicAdd(B.next, 32ull);
-      base = __shfl_sync(0xffffffffu, base, 0);
-      if ((int64_t)base >= np) break;
-      const int64_t u = (int64_t)base + lane;
-      if (u < np) pairA_one<D, STAGE>(c, S, B, u);
-    }
-  }
-  if (last_block_of_grid(B.done) && threadIdx.x == 0) *B.next = 0ull;
+__global__ void __launch_bounds__(STPB) k_pairA(StepConst c, SArr<D> S, PairBuf B, int64_t spread) {
+  if (*S.ovf) return;
+  const int64_t W = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t u = ((w * spread) % W) * 32 + (threadIdx.x & 31);
+  if (u < *B.npair) pairA_one<D, STAGE>(c, S, B, u);
 }
 
 // pass B, stage 1: row sums + the three half-step predictors
@@ -263,15 +256,28 @@ __global__ void __launch_bounds__(STPB) k_pairB2(StepConst c, Scal* __restrict__
 }
 
 
+static int64_t gcd64(int64_t a, int64_t b) {
+  while (b) {
+    const int64_t t = a % b;
+    a = b;
+    b = t;
+  }
+  return a;
+}
+
 template <int D>
-int launch_pairA(int stage, int64_t threads, int blocks_max, cudaStream_t st, const StepConst& c, const SArr<D>& S,
+int launch_pairA(int stage, int64_t threads, cudaStream_t st, const StepConst& c, const SArr<D>& S,
                  const PairBuf& B) {
-  int g = nblocks(threads, STPB);
-  if (g > blocks_max) g = blocks_max;
+  const int g = nblocks(threads, STPB);
+  // a stride near W / golden ratio, coprime to the grid's W warps
+  const int64_t W = (int64_t)g * (STPB / 32);
+  int64_t spread = (int64_t)(0.6180339887 * (double)W) | 1;
+  while (spread > 1 && gcd64(spread, W) != 1) spread += 2;
+  if (spread < 1 || spread >= W) spread = 1;
   if (stage == 1)
-    k_pairA<D, 1><<<g, STPB, 0, st>>>(c, S, B);
+    k_pairA<D, 1><<<g, STPB, 0, st>>>(c, S, B, spread);
   else
-    k_pairA<D, 2><<<g, STPB, 0, st>>>(c, S, B);
+    k_pairA<D, 2><<<g, STPB, 0, st>>>(c, S, B, spread);
   GC_LAUNCHED();
   return GCSPH_OK;
 }
@@ -297,8 +303,8 @@ int launch_pairB(int stage, int L, int64_t N, cudaStream_t st, const StepConst& 
   return GCSPH_OK;
 }
 
-template int launch_pairA<2>(int, int64_t, int, cudaStream_t, const StepConst&, const SArr<2>&, const PairBuf&);
-template int launch_pairA<3>(int, int64_t, int, cudaStream_t, const StepConst&, const SArr<3>&, const PairBuf&);
+template int launch_pairA<2>(int, int64_t, cudaStream_t, const StepConst&, const SArr<2>&, const PairBuf&);
+template int launch_pairA<3>(int, int64_t, cudaStream_t, const StepConst&, const SArr<3>&, const PairBuf&);
 template int launch_pairB<2>(int, int, int64_t, cudaStream_t, const StepConst&, Scal*, const SArr<2>&,
                              const PairBuf&);
 template int launch_pairB<3>(int, int, int64_t, cudaStream_t, const StepConst&, Scal*, const SArr<3>&,

@@ -647,8 +647,6 @@ struct sph_handle {
       GWe[3], IR, IRH;
   DevBuf PT_b, BUF2_b[3];  // spares for the in-loop re-sort
   DevBuf CD, CA[3], PQ;     // pair-once passes: per-entry contributions, flat pair list
-  DevBuf PAWORK;            // pass A's work counters (next pair; finished blocks), zeroed once
-  int pa_blocks = 1024;     // pass A's grid: the SMs' resident blocks
   int ix = 0, ixh = 0, iv = 0, ivh = 0, irho = 0, irhoh = 0;
   int64_t we_cap = 0;
   int lanes = 0;  // lanes per particle in the pair passes; 0 = by mean row length
@@ -793,8 +791,6 @@ static PairBuf make_pairbuf(sph_handle* h) {
   for (int d = 0; d < D; ++d) B.ca[d] = h->CA[d].as<double>();
   B.pq = h->PQ.as<int4>();
   B.npair = h->cl->core.rs_up.as<int64_t>() + h->N;
-  B.next = h->PAWORK.as<unsigned long long>();
-  B.done = (unsigned*)(h->PAWORK.as<unsigned long long>() + 1);
   return B;
 }
 
@@ -865,7 +861,9 @@ static int rebuild(sph_handle* h, const StepConst& c, int* ovf_dev) {
     alt.cnt = core.pfcnt.as<unsigned>();
     alt.dist2 = core.g.dist2;
     timer_begin(T_STATE, core.st);
-    k_permute_state<D><<<nblocks(h->N, 256), 256, 0, core.st>>>(c, h->N, core.perm.as<int32_t>(), make_arr<D>(h),
+    // small sets: 64-thread blocks, so the latency-bound gather spreads over more SMs
+    const int ptb = h->N <= RADIX_MIN_N ? 64 : 256;
+    k_permute_state<D><<<nblocks(h->N, ptb), ptb, 0, core.st>>>(c, h->N, core.perm.as<int32_t>(), make_arr<D>(h),
                                                                alt);
     pf_ready = true;
     GC_LAUNCHED();
@@ -923,7 +921,7 @@ static int rebuild(sph_handle* h, const StepConst& c, int* ovf_dev) {
 // pair count itself stays on the device); pass B: L lanes per row
 #define PAIRA_LAUNCH(STAGE, ...)                                                              \
   do {                                                                                        \
-    const int _rc = launch_pairA<D>(STAGE, h->cl->core.nbr_cap / 2 + 1, h->pa_blocks, st, __VA_ARGS__); \
+    const int _rc = launch_pairA<D>(STAGE, h->cl->core.nbr_cap / 2 + 1, st, __VA_ARGS__);     \
     if (_rc) return _rc;                                                                      \
   } while (0)
 
@@ -1344,8 +1342,11 @@ static int step_impl(sph_handle* h, int32_t n, int timestepping, double tmin, do
   c.dt_relative = h->dt_relative;
   bool done = false;
   int rc = step_graph<D>(h, c, n, timestepping, tmin, tmax, updaten_out, maxcdx_out, &done);
-  if (rc || done) return rc;
-  return step_eager<D>(h, c, n, updaten_out, maxcdx_out);
+  if (!rc && !done) rc = step_eager<D>(h, c, n, updaten_out, maxcdx_out);
+  // the call has finished on the device: the most crowded cell it binned
+  // picks the in-cell ordering of the next call (large sets)
+  if (!rc) rc = h->cl->core.read_popmax();
+  return rc;
 }
 
 extern "C" {
@@ -1410,16 +1411,6 @@ int sph_create(gcl_handle* cl, const gcsph_params* prm, double* rho_dev, double*
   E(h->DRHO, nb, true);
   E(h->PLAST, nb, true);
   E(h->scal, sizeof(Scal), true);
-  E(h->PAWORK, 2 * sizeof(unsigned long long), true);
-  if (!rc) {
-    // pass A's grid: eight blocks per SM at most (the registers of its
-    // STPB-thread blocks allow seven or eight), all resident at once
-    int dev = 0, sms = 0;
-    if (cudaGetDevice(&dev) == cudaSuccess && cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) ==
-                                                   cudaSuccess && sms > 0)
-      h->pa_blocks = 8 * sms;
-    cudaGetLastError();
-  }
   if (!rc) {
     cudaError_t e = cudaMallocHost((void**)&h->pin, sizeof(Scal));
     if (e != cudaSuccess) rc = cuda_fail(e, "cudaMallocHost", __FILE__, __LINE__);
@@ -1454,7 +1445,6 @@ void sph_destroy(sph_handle* h) {
   for (DevBuf* b : one) b->release();
   h->CD.release();
   h->PQ.release();
-  h->PAWORK.release();
   for (int d = 0; d < 3; ++d) {
     h->CA[d].release();
     h->BUF2_b[d].release();

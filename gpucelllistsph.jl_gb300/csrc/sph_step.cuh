@@ -332,10 +332,6 @@ struct PairBuf {
   double* ca[3];          // ∂v/∂t contribution per neighbour entry (gravity not included)
   int4* pq;               // (k, m, e, mirror(e)) of every pair, k < m (mirror -1: stage 1 finds it)
   const int64_t* npair;   // number of pairs (device scalar)
-  // pass A's work distribution: [0] the next unclaimed pair, reset by the
-  // pass's last block; done counts the finished blocks (last_block_of_grid)
-  unsigned long long* next;
-  unsigned* done;
 };
 
 // ---------------------------------------------------------------------------
@@ -454,7 +450,7 @@ __device__ inline void row_sums(const SArr<D>& S, const PairBuf& B, int64_t k, i
 // pair-once passes (sph_once.cu): pass A over `threads` pair slots, pass B
 // (row sums + predictor / corrector) with L lanes per particle
 template <int D>
-int launch_pairA(int stage, int64_t threads, int blocks_max, cudaStream_t st, const StepConst& c, const SArr<D>& S,
+int launch_pairA(int stage, int64_t threads, cudaStream_t st, const StepConst& c, const SArr<D>& S,
                  const PairBuf& B);
 template <int D>
 int launch_pairB(int stage, int L, int64_t N, cudaStream_t st, const StepConst& c, Scal* sc, const SArr<D>& S,

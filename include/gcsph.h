@@ -90,6 +90,14 @@ int gcl_cellpnum(gcl_handle* h, int32_t* cellpnum_dev);
 /* мaxpairs(c.cellpnum) -- src/gpukernels_cls.jl:109-286 */
 int gcl_maxpairs(gcl_handle* h, int64_t* out);
 
+/* The order inside a cell (by original index) of the binning (no reference
+ * counterpart; a tuning knob -- the pair list, its order and every result
+ * are the same for every choice).  0 = chosen by the most crowded cell (the
+ * default), 1 = the counting sort's in-cell rank (cost: the square of a
+ * cell's population), 2 = a stable radix sort (a few passes over the set;
+ * sets of more than 65,536 points only). */
+int gcl_set_sort(gcl_handle* h, int32_t mode);
+
 /* No counterpart in the reference.  The pair list of GPUCellList(points,
  * cellsize, dist; MIN, MAX) in a single call that allocates no memory, for
  * callers that must not allocate device memory while they run: a host whose

@@ -288,3 +288,30 @@ def test_one_crowded_cell(gpu_pkg):
     got = c.neighborlistview().cpu().numpy().astype(np.int64)
     assert c.pairsn == want.size
     assert np.array_equal(np.sort(got[:, 0] * (1 << 32) + got[:, 1]), want)
+
+
+@pytest.mark.parametrize("D,N", [(2, 200_000), (3, 300_000)])
+def test_sort_choices_same_pair_list(gpu_pkg, D, N):
+    """The three in-cell orderings of a large set (by the most crowded cell,
+    the counting sort's rank, the stable radix sort) give the same pair list
+    in the same order, for update! and partialupdate! alike."""
+    x = gpu_pkg.workloads.uniform_points(N, D, seed=7 + D)
+    dist = 0.006 if D == 2 else 0.02
+    lists = []
+    for mode in (0, 1, 2):
+        c = gpu_pkg.GPUCellList(tuple(x), (dist,) * D, dist)
+        c.set_sort(mode)
+        c.update()
+        c.partialupdate()
+        lists.append(c.neighborlistview().clone())
+        c.close()
+    assert lists[0].shape[0] > N
+    assert torch.equal(lists[0], lists[1]) and torch.equal(lists[1], lists[2])
+
+
+def test_set_sort_rejects_unknown_mode(gpu_pkg):
+    x = gpu_pkg.workloads.uniform_points(1000, 2, seed=3)
+    c = gpu_pkg.GPUCellList(tuple(x), (0.05, 0.05), 0.05)
+    with pytest.raises(RuntimeError):
+        c.set_sort(3)
+    c.close()
