@@ -502,6 +502,9 @@ int CellCore::init(int D_, int64_t N_, const double* cellsize, double dist_, con
   if ((rc = scratch.ensure(sizeof(int64_t) * (sc + 16), st))) return rc;
   // zeroed once: each pass that folds a scan resets its counter itself
   if ((rc = foldcnt.ensure(sizeof(unsigned) * 2, st, true))) return rc;
+  if (N + 1 <= SCAN_FOLD_MAX &&
+      (rc = foldsum.ensure(sizeof(int32_t) * (2 * N + 4 * ROWS_FOLD_MAX_BLOCKS + 2), st)))
+    return rc;
   if (N > RADIX_MIN_N) {
     const int64_t ntiles = (N + RADIX_TILE - 1) / RADIX_TILE;
     for (int b = 0; b < 2; ++b) {
@@ -519,7 +522,7 @@ int CellCore::init(int D_, int64_t N_, const double* cellsize, double dist_, con
 void CellCore::release() {
   DevBuf* all[] = {&count, &cellstart, &key, &slot, &tmp, &perm, &skey, &orig, &cnt_full, &cnt_up, &rs_full,
                    &rs_up, &nbr, &scratch, &pf[0], &pf[1], &pf[2], &pfmax, &pfthr, &pfcnt, &orig_b, &stage,
-                   &foldcnt, &rkey[0], &rkey[1], &rval[0], &rval[1], &rhist, &rhoff, &popmax};
+                   &foldcnt, &foldsum, &rkey[0], &rkey[1], &rval[0], &rval[1], &rhist, &rhoff, &popmax};
   for (DevBuf* b : all) b->release();
   if (pin) cudaFreeHost(pin);
   pin = nullptr;
@@ -680,6 +683,19 @@ __global__ void k_make_pf(const double* __restrict__ x0, const double* __restric
 }
 
 
+// Row starts of a small set as the count pass folds them (rows_fold, below)
+struct FoldRows {
+  // fb: local offsets [2N] (full, up), block totals [2G], block bases [2G],
+  // the two totals [2]
+  __device__ static int32_t* totals(int32_t* fb, int64_t N) { return fb + 2 * N; }
+  __device__ static int32_t* bases(int32_t* fb, int64_t N, int G) { return fb + 2 * N + 2 * G; }
+  // start of row i of array a (0 full, 1 up) as the fill pass reads it
+  __device__ static int64_t start(const int32_t* fb, int a, int64_t i, int64_t N, int P, int G) {
+    if (i >= N) return fb[2 * N + 4 * G + a];
+    return (int64_t)fb[a * N + i] + fb[2 * N + 2 * G + a * G + i / P];
+  }
+};
+
 // one point's row of the pair search with the FP32 prefilter (k_pairs32)
 template <int D, int MODE, int L>
 __device__ __forceinline__ void pairs32_row(const double* __restrict__ x0, const double* __restrict__ x1,
@@ -691,21 +707,31 @@ __device__ __forceinline__ void pairs32_row(const double* __restrict__ x0, const
                                                  int32_t* __restrict__ cnt_full, int32_t* __restrict__ cnt_up,
                                                  const int64_t* __restrict__ rs_full, int32_t* __restrict__ nbr,
                                                  int64_t cap, int* __restrict__ ovf, int32_t* __restrict__ stg,
-                                                 int S) {
+                                                 int S, const int32_t* fold_buf) {
   // MODE 0: count; MODE 2: count and stage the row (ascending) in stg[k*S ..]
   // when it fits; MODE 1: fill the CSR row -- a copy of the staged row when
-  // the count pass staged it, else the search again
+  // the count pass staged it, else the search again.  MODE 1 reads the row
+  // starts from the count pass's fold buffer where it folded (FoldRows)
   const int64_t gt = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int64_t k = gt / L;
   const int lane = (int)(gt % L);
   if (k >= N) return;
-  if (MODE == 1 && rs_full[k + 1] > cap) {  // the row does not fit: report, write nothing
+  int64_t r0 = 0, r1 = 0;
+  if (MODE == 1) {
+    if (fold_buf) {
+      r0 = FoldRows::start(fold_buf, 0, k, N, TPB / L, gridDim.x);
+      r1 = FoldRows::start(fold_buf, 0, k + 1, N, TPB / L, gridDim.x);
+    } else {
+      r0 = rs_full[k];
+      r1 = rs_full[k + 1];
+    }
+  }
+  if (MODE == 1 && r1 > cap) {  // the row does not fit: report, write nothing
     if (ovf && lane == 0) atomicExch(ovf, 1);
     return;
   }
   if (MODE == 1 && stg) {
-    const int64_t r0 = rs_full[k];
-    const int32_t n = (int32_t)(rs_full[k + 1] - r0);
+    const int32_t n = (int32_t)(r1 - r0);
     if (n <= S) {
       for (int32_t q = lane; q < n; q += L) nbr[r0 + q] = stg[k * S + q];
       return;
@@ -724,7 +750,7 @@ __device__ __forceinline__ void pairs32_row(const double* __restrict__ x0, const
   const int cz = t / ny;
   const float ax = f0[k], ay = f1[k], az = D == 3 ? f2[k] : 0.0f;
   int32_t nf = 0, nu = 0;
-  int64_t wpos = MODE == 1 ? rs_full[k] : 0;
+  int64_t wpos = r0;
   int32_t spos = 0;  // MODE 2: staged entries so far
   const int xlo = cx > 0 ? cx - 1 : 0;
   const int xhi = cx < nx - 1 ? cx + 1 : nx - 1;
@@ -843,18 +869,23 @@ __device__ __forceinline__ void pairs32_quads(int64_t N, const int32_t* __restri
                                               const int32_t* __restrict__ cnt_up, const int64_t* __restrict__ rs_full,
                                               const int64_t* __restrict__ rs_up, const int32_t* __restrict__ nbr,
                                               int64_t cap, const int32_t* __restrict__ stg, int S,
-                                              int4* __restrict__ pq) {
+                                              int4* __restrict__ pq, const int32_t* fold_buf) {
   const int64_t gt = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int64_t k = gt / L;
   const int lane = (int)(gt % L);
   if (k >= N) return;
+  // row starts as the fill read them (where the count pass folded them, the
+  // final arrays are being written by this very pass)
+  auto start = [&](int a, int64_t i) -> int64_t {
+    return fold_buf ? FoldRows::start(fold_buf, a, i, N, TPB / L, gridDim.x) : (a ? rs_up : rs_full)[i];
+  };
   // past the capacity the fill raised the overflow flag and the step is
   // repeated; the pair list holds cap / 2 + 1 pairs, enough when it fits
-  if (rs_full[N] > cap) return;
-  const int64_t r0 = rs_full[k], r1 = rs_full[k + 1];
+  if (start(0, N) > cap) return;
+  const int64_t r0 = start(0, k), r1 = start(0, k + 1);
   const int32_t n = (int32_t)(r1 - r0);
   const int32_t nu = cnt_up[k];
-  const int64_t u0 = rs_up[k];
+  const int64_t u0 = start(1, k);
   const bool staged = n <= S;
   for (int32_t q = n - nu + lane; q < n; q += L) {
     const int32_t m = staged ? stg[k * S + q] : nbr[r0 + q];
@@ -868,17 +899,108 @@ __device__ __forceinline__ void pairs32_quads(int64_t N, const int32_t* __restri
         if (row[mid] < k) lo = mid + 1;
         else hi = mid;
       }
-      mir = (int32_t)(rs_full[m] + lo);
+      mir = (int32_t)(start(0, m) + lo);
     }
     pq[u0 + (q - (n - nu))] = make_int4((int)k, (int)m, (int)(r0 + q), mir);
   }
 }
 
+// The row starts of small sets (N + 1 <= SCAN_FOLD_MAX), in two levels, in
+// the int32 buffer fb (FoldRows below).  MODE 4's block b holds the points
+// [b P, (b + 1) P), P = TPB / L: it scans their two counts into block-local
+// offsets and stores its two totals; the last block to finish scans the G
+// block totals into block bases.  The fill pass (MODE 1 / 3: same N and L,
+// so the same G) reads a start as local offset + its block's base and writes
+// the final rs_full / rs_up.  A single-block scan of all N counts walks them
+// tile after tile, one load round trip each; this way the last block has one
+// scan of G entries.  Sums fit in int32: N + 1 <= SCAN_FOLD_MAX points have
+// fewer than 2^28 neighbour entries.
+
+template <int L>
+__device__ __forceinline__ void rows_fold(const int32_t* cnt_full, const int32_t* cnt_up, int64_t N,
+                                          int64_t* rs_full, int64_t* rs_up, int32_t* fb, unsigned* fold_cnt) {
+  constexpr int P = TPB / L, NW = TPB / 32, IT = ROWS_FOLD_MAX_BLOCKS / TPB;
+  __shared__ int32_t s_w[2][NW];
+  const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+  const int G = gridDim.x;
+  __syncthreads();  // the block's counts are written
+  const int64_t i = (int64_t)blockIdx.x * P + tid;
+  const bool mine = tid < P && i < N;
+  const int32_t c0 = mine ? cnt_full[i] : 0, c1 = mine ? cnt_up[i] : 0;
+  int32_t s0 = c0, s1 = c1;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int32_t y0 = __shfl_up_sync(0xffffffffu, s0, o), y1 = __shfl_up_sync(0xffffffffu, s1, o);
+    if (lane >= o) {
+      s0 += y0;
+      s1 += y1;
+    }
+  }
+  if (lane == 31) {
+    s_w[0][w] = s0;
+    s_w[1][w] = s1;
+  }
+  __syncthreads();
+  int32_t b0 = 0, b1 = 0, t0 = 0, t1 = 0;
+#pragma unroll
+  for (int v = 0; v < NW; ++v) {
+    if (v < w) {
+      b0 += s_w[0][v];
+      b1 += s_w[1][v];
+    }
+    t0 += s_w[0][v];
+    t1 += s_w[1][v];
+  }
+  if (mine) {
+    fb[i] = b0 + s0 - c0;
+    fb[N + i] = b1 + s1 - c1;
+  }
+  int32_t* tots = FoldRows::totals(fb, N);
+  if (tid == 0) {
+    tots[blockIdx.x] = t0;
+    tots[G + blockIdx.x] = t1;
+  }
+  if (!last_block_of_grid(fold_cnt)) return;
+  // the block totals' exclusive scan into the block bases (G <= ROWS_FOLD_MAX_BLOCKS)
+  int32_t* bases = FoldRows::bases(fb, N, G);
+#pragma unroll
+  for (int a = 0; a < 2; ++a) {
+    int32_t v[IT], run = 0;
+#pragma unroll
+    for (int j = 0; j < IT; ++j) {
+      const int idx = tid * IT + j;
+      v[j] = idx < G ? __ldcg(tots + a * G + idx) : 0;
+      run += v[j];
+    }
+    int32_t inc = run;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int32_t y = __shfl_up_sync(0xffffffffu, inc, o);
+      if (lane >= o) inc += y;
+    }
+    __syncthreads();  // s_w of the pass before has been read
+    if (lane == 31) s_w[a][w] = inc;
+    __syncthreads();
+    int32_t base = inc - run;
+    for (int u = 0; u < w; ++u) base += s_w[a][u];
+#pragma unroll
+    for (int j = 0; j < IT; ++j) {
+      const int idx = tid * IT + j;
+      if (idx < G) bases[a * G + idx] = base;
+      base += v[j];
+    }
+    if (tid == TPB - 1) {
+      fb[2 * N + 4 * G + a] = base;
+      (a ? rs_up : rs_full)[N] = base;
+    }
+  }
+}
+
 // the pair search with the FP32 prefilter (same output, same order as
-// k_pairs).  MODE 4: MODE 2, then the last block to finish scans the row
-// counts into rs_full / rs_up (N + 1 <= SCAN_FOLD_MAX; a separate mode, so
-// that the scan's registers do not weigh on MODE 2 at large N).  MODE 3: the
-// fill, then the flat pair list of the pair-once passes (pairs32_quads).
+// k_pairs).  MODE 4: MODE 2, then the row starts rs_full / rs_up by
+// rows_fold (N + 1 <= SCAN_FOLD_MAX; a separate mode, so that the fold's
+// shared memory does not weigh on MODE 2 at large N).  MODE 3: the fill, then
+// the flat pair list of the pair-once passes (pairs32_quads).
 template <int D, int MODE, int L>
 __global__ void __launch_bounds__(TPB) k_pairs32(const double* __restrict__ x0, const double* __restrict__ x1,
                                                  const double* __restrict__ x2, const float* __restrict__ f0,
@@ -891,14 +1013,23 @@ __global__ void __launch_bounds__(TPB) k_pairs32(const double* __restrict__ x0, 
                                                  int64_t cap, int* __restrict__ ovf, int32_t* __restrict__ stg,
                                                  int S, int64_t* fold_rs_full, int64_t* fold_rs_up,
                                                  unsigned* fold_cnt, const int64_t* __restrict__ rs_up,
-                                                 int4* __restrict__ pq) {
+                                                 int4* __restrict__ pq, int32_t* fold_buf) {
+  if ((MODE == 1 || MODE == 3) && fold_buf) {
+    // small sets: the final row starts, from the count pass's two levels
+    const int64_t gt = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t k = gt / L;
+    if (k < N && gt % L == 0) {
+      fold_rs_full[k] = FoldRows::start(fold_buf, 0, k, N, TPB / L, gridDim.x);
+      fold_rs_up[k] = FoldRows::start(fold_buf, 1, k, N, TPB / L, gridDim.x);
+    }
+  }
   pairs32_row<D, MODE == 3 ? 1 : (MODE == 4 ? 2 : MODE), L>(x0, x1, x2, f0, f1, f2, thr, skey, cellstart, N, g,
-                                                             cnt_full, cnt_up, rs_full, nbr, cap, ovf, stg, S);
-  if (MODE == 4 && last_block_of_grid(fold_cnt))
-    block_exclusive_scan2_i64(cnt_full, fold_rs_full, cnt_up, fold_rs_up, N);
+                                                             cnt_full, cnt_up, rs_full, nbr, cap, ovf, stg, S,
+                                                             fold_buf);
+  if (MODE == 4) rows_fold<L>(cnt_full, cnt_up, N, fold_rs_full, fold_rs_up, fold_buf, fold_cnt);
   if (MODE == 3) {
     __syncwarp();  // a recomputed row's entries, written by the group's lanes, are read back
-    pairs32_quads<D, L>(N, cnt_full, cnt_up, rs_full, rs_up, nbr, cap, stg, S, pq);
+    pairs32_quads<D, L>(N, cnt_full, cnt_up, rs_full, rs_up, nbr, cap, stg, S, pq, fold_buf);
   }
 }
 
@@ -1019,20 +1150,24 @@ int CellCore::build_pairs(const double* const* xs, int* ovf_dev, bool scan_up, b
   if (rc0) return rc0;
   // small sets: the count pass's last block scans the row counts (both
   // arrays), so no scan launch follows
-  const bool fold = sp && N + 1 <= SCAN_FOLD_MAX;
+  const bool fold = sp && foldsum.p && N + 1 <= SCAN_FOLD_MAX && nblocks(N * (int64_t)L, TPB) <= ROWS_FOLD_MAX_BLOCKS;
   unsigned* fc = fold ? foldcnt.as<unsigned>() + 1 : nullptr;
+  int32_t* fbuf = fold ? foldsum.as<int32_t>() : nullptr;
+  int64_t* frs_full = fold ? rs_full.as<int64_t>() : nullptr;
+  int64_t* frs_up = fold ? rs_up.as<int64_t>() : nullptr;
   if (fold)
     PAIRS32_LAUNCH(4, L, xs[0], xs[1], x2, pf[0].as<float>(), pf[1].as<float>(), f2, thr, skey.as<int32_t>(),
                    cellstart.as<int32_t>(), N, g, cnt_full.as<int32_t>(), cnt_up.as<int32_t>(), nullptr, nullptr, 0,
-                   nullptr, sp, S, rs_full.as<int64_t>(), rs_up.as<int64_t>(), fc, nullptr, nullptr);
+                   nullptr, sp, S, rs_full.as<int64_t>(), rs_up.as<int64_t>(), fc, nullptr, nullptr,
+                   foldsum.as<int32_t>());
   else if (sp)
     PAIRS32_LAUNCH(2, L, xs[0], xs[1], x2, pf[0].as<float>(), pf[1].as<float>(), f2, thr, skey.as<int32_t>(),
                    cellstart.as<int32_t>(), N, g, cnt_full.as<int32_t>(), cnt_up.as<int32_t>(), nullptr, nullptr, 0,
-                   nullptr, sp, S, nullptr, nullptr, nullptr, nullptr, nullptr);
+                   nullptr, sp, S, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr);
   else
     PAIRS32_LAUNCH(0, L, xs[0], xs[1], x2, pf[0].as<float>(), pf[1].as<float>(), f2, thr, skey.as<int32_t>(),
                    cellstart.as<int32_t>(), N, g, cnt_full.as<int32_t>(), cnt_up.as<int32_t>(), nullptr, nullptr, 0,
-                   nullptr, nullptr, 0, nullptr, nullptr, nullptr, nullptr, nullptr);
+                   nullptr, nullptr, 0, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr);
   GC_LAUNCHED();
   int rc = GCSPH_OK;
   if (!fold)
@@ -1062,13 +1197,13 @@ int CellCore::build_pairs(const double* const* xs, int* ovf_dev, bool scan_up, b
     // its pair list for it)
     PAIRS32_LAUNCH(3, L, xs[0], xs[1], x2, pf[0].as<float>(), pf[1].as<float>(), f2, thr, skey.as<int32_t>(),
                    cellstart.as<int32_t>(), N, g, cnt_full.as<int32_t>(), cnt_up.as<int32_t>(),
-                   rs_full.as<int64_t>(), nbr.as<int32_t>(), nbr_cap, ovf_dev, sp, S, nullptr, nullptr, nullptr,
-                   rs_up.as<int64_t>(), pq);
+                   rs_full.as<int64_t>(), nbr.as<int32_t>(), nbr_cap, ovf_dev, sp, S, frs_full, frs_up, nullptr,
+                   rs_up.as<int64_t>(), pq, fbuf);
     if (pq_done) *pq_done = true;
   } else {
     PAIRS32_LAUNCH(1, L, xs[0], xs[1], x2, pf[0].as<float>(), pf[1].as<float>(), f2, thr, skey.as<int32_t>(),
                    cellstart.as<int32_t>(), N, g, nullptr, nullptr, rs_full.as<int64_t>(), nbr.as<int32_t>(), nbr_cap,
-                   ovf_dev, sp, S, nullptr, nullptr, nullptr, nullptr, nullptr);
+                   ovf_dev, sp, S, frs_full, frs_up, nullptr, nullptr, nullptr, fbuf);
   }
   GC_LAUNCHED();
   timer_end(T_PAIRS, st);

@@ -72,6 +72,8 @@ constexpr int64_t RADIX_MIN_N = 65536;
 // ... and then only where a cell holds more than this many points (below it
 // the rank's cost is a few loads per point and takes fewer launches)
 constexpr int RADIX_MIN_POP = 128;
+// blocks of the count pass whose row-start scan it folds (rows_fold)
+constexpr int ROWS_FOLD_MAX_BLOCKS = 2048;
 
 struct CellCore {
   int D = 2;
@@ -86,6 +88,7 @@ struct CellCore {
   DevBuf pfcnt;         // blocks done of the pass that accumulates pfmax (its last block writes pfthr)
   DevBuf stage;         // neighbour rows staged by the count pass (fixed stride), copied by the fill
   DevBuf foldcnt;       // finished-block counters of the passes whose last block runs a scan (2 unsigned)
+  DevBuf foldsum;       // block totals of the folded row-start scan (small sets)
   DevBuf rkey[2], rval[2], rhist, rhoff;  // radix sort of large sets: ping-pong keys/values, tile histograms
   int64_t* pin = nullptr;  // pinned host scalars
   int64_t nfull = 0, nup = 0, nbr_cap = 0;

@@ -218,78 +218,6 @@ __device__ inline bool last_block_of_grid(unsigned* cnt) {
   return s_last != 0;
 }
 
-// Two exclusive scans of n items each (in0 -> out0, in1 -> out1, out[n] =
-// total) by one block of exactly SCAN2_THREADS threads, both arrays in the
-// same tiles: each thread reads 8 consecutive items of each array as two
-// 16-byte vectors (in0, in1 16-byte aligned); the results go out through one
-// shared tile, array by array, so that the stores are coalesced.
-constexpr int SCAN2_THREADS = 256;
-__device__ inline void block_exclusive_scan2_i64(const int32_t* in0, int64_t* out0, const int32_t* in1,
-                                                 int64_t* out1, int64_t n) {
-  constexpr int IT = 8, TILE = SCAN2_THREADS * IT, NW = SCAN2_THREADS / 32;
-  __shared__ long long tile[TILE];
-  __shared__ long long wsum[2][NW];
-  const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
-  long long carry[2] = {0, 0};
-  for (int64_t base = 0; base <= n; base += TILE) {
-    const int64_t i0 = base + (int64_t)tid * IT;
-    int v[2][IT];
-    long long s[2], inc[2];
-#pragma unroll
-    for (int a = 0; a < 2; ++a) {
-      const int32_t* in = a ? in1 : in0;
-      if (i0 + IT <= n) {
-        const int4 t0 = __ldcg(reinterpret_cast<const int4*>(in + i0));
-        const int4 t1 = __ldcg(reinterpret_cast<const int4*>(in + i0) + 1);
-        v[a][0] = t0.x; v[a][1] = t0.y; v[a][2] = t0.z; v[a][3] = t0.w;
-        v[a][4] = t1.x; v[a][5] = t1.y; v[a][6] = t1.z; v[a][7] = t1.w;
-      } else {
-#pragma unroll
-        for (int j = 0; j < IT; ++j) v[a][j] = i0 + j < n ? __ldcg(in + i0 + j) : 0;
-      }
-      s[a] = 0;
-#pragma unroll
-      for (int j = 0; j < IT; ++j) s[a] += v[a][j];
-      inc[a] = s[a];
-#pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        const long long y = __shfl_up_sync(0xffffffffu, inc[a], o);
-        if (lane >= o) inc[a] += y;
-      }
-      if (lane == 31) wsum[a][w] = inc[a];
-    }
-    __syncthreads();
-    if (w < 2) {
-      long long t = lane < NW ? wsum[w][lane] : 0;
-#pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        const long long y = __shfl_up_sync(0xffffffffu, t, o);
-        if (lane >= o) t += y;
-      }
-      if (lane < NW) wsum[w][lane] = t;
-    }
-    __syncthreads();
-#pragma unroll
-    for (int a = 0; a < 2; ++a) {
-      long long run = carry[a] + (w > 0 ? wsum[a][w - 1] : 0) + inc[a] - s[a];
-#pragma unroll
-      for (int j = 0; j < IT; ++j) {
-        tile[tid * IT + j] = run;
-        run += v[a][j];
-      }
-      __syncthreads();
-      int64_t* out = a ? out1 : out0;
-#pragma unroll
-      for (int j = 0; j < IT; ++j) {
-        const int64_t idx = base + (int64_t)j * SCAN2_THREADS + tid;
-        if (idx <= n) out[idx] = tile[j * SCAN2_THREADS + tid];
-      }
-      carry[a] += wsum[a][NW - 1];
-      __syncthreads();
-    }
-  }
-}
-
 // out[i] = sum_{j<i} in[j] for i in [0, n] (out[n] = total), by one block
 // (blockDim.x a multiple of 32), 16 items per thread per tile, read as four
 // 16-byte vectors (in 16-byte aligned).  Reads go to L2 (ld.global.cg): the

@@ -147,33 +147,71 @@ __device__ __forceinline__ void pairA_one(const StepConst& c, const SArr<D>& S, 
   }
 }
 
-// Pass A over all pairs, 32 consecutive pairs per warp.  The pairs come in
-// cell order, so the costly fluid pairs and the cheap boundary pairs sit in
-// runs; a grid that took its warps' chunks in that order would end on the
-// SMs that drew fluid runs.  Warp w takes chunk (w * spread) mod W instead
-// (W warps in the grid, spread coprime to W: a permutation of the chunks),
-// which gives every block chunks from all over the list.
+// Pass A over all pairs in chunks of 32 consecutive pairs, one chunk per warp
+// at a time, with one block per SM: PA_TPB threads of about 70 registers
+// leave no room for a second block, and the grid is the SM count.  Block b
+// takes chunks b, b + G, b + 2G, ... (G blocks) and its warp w every NW-th
+// of those, so every SM gets the same number of chunks (to one) -- a grid of
+// many small blocks leaves some SMs one block more than others -- and
+// consecutive chunks of the cell-ordered list, runs of costly fluid pairs or
+// of cheap boundary pairs, go to different SMs.
+constexpr int PA_TPB = 768;
 template <int D, int STAGE>
-__global__ void __launch_bounds__(STPB) k_pairA(StepConst c, SArr<D> S, PairBuf B, int64_t spread) {
+__global__ void __launch_bounds__(PA_TPB, 1) k_pairA(StepConst c, SArr<D> S, PairBuf B) {
   if (*S.ovf) return;
-  const int64_t W = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int64_t u = ((w * spread) % W) * 32 + (threadIdx.x & 31);
-  if (u < *B.npair) pairA_one<D, STAGE>(c, S, B, u);
+  const int64_t np = *B.npair;
+  const int64_t G = gridDim.x;
+  constexpr int NW = PA_TPB / 32;
+  const int lane = threadIdx.x & 31;
+  for (int64_t t = threadIdx.x >> 5;; t += NW) {
+    const int64_t u0 = ((int64_t)blockIdx.x + G * t) * 32;
+    if (u0 >= np) break;
+    if (u0 + lane < np) pairA_one<D, STAGE>(c, S, B, u0 + lane);
+  }
+}
+
+// Pass B: a block of 32 L threads holds 32 particles, L lanes summing each
+// row; the sums go through shared memory to warp 0, which runs the
+// per-particle update for all 32 at once.  (Run by each group's lane 0, the
+// update's divisions and EOS power would issue on the FP64 pipe with 32 / L
+// lanes of a warp active: GB300 issues 2 FP64 thread-instructions per cycle
+// per SM, so that costs the full warp's time for a few lanes' work.)
+template <int D>
+struct RowSums {
+  double drho[32];
+  double a[D][32];
+};
+
+template <int D, int L>
+__device__ __forceinline__ void pairB_sums(const SArr<D>& S, const PairBuf& B, int64_t N, RowSums<D>& R) {
+  const int g = threadIdx.x / L, lane = threadIdx.x % L;
+  const int64_t k = (int64_t)blockIdx.x * 32 + g;
+  double drho = 0.0, a[D];
+#pragma unroll
+  for (int d = 0; d < D; ++d) a[d] = 0.0;
+  if (k < N) row_sums<D, L>(S, B, k, lane, group_mask<L>(), drho, a);  // whole groups take part
+  if (lane == 0) {
+    R.drho[g] = drho;
+#pragma unroll
+    for (int d = 0; d < D; ++d) R.a[d][g] = a[d];
+  }
+  __syncthreads();
 }
 
 // pass B, stage 1: row sums + the three half-step predictors
 template <int D, int L>
-__global__ void __launch_bounds__(STPB) k_pairB1(StepConst c, const Scal* __restrict__ sc, int64_t N, SArr<D> S,
-                                                 PairBuf B) {
+__global__ void __launch_bounds__(32 * L) k_pairB1(StepConst c, const Scal* __restrict__ sc, int64_t N, SArr<D> S,
+                                                   PairBuf B) {
   if (*S.ovf) return;
-  const int64_t gt = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const int64_t k = gt / L;
-  const int lane = (int)(gt % L);
-  if (k >= N) return;  // whole sub-group leaves together
-  double drho, a[D];
-  row_sums<D, L>(S, B, k, lane, group_mask<L>(), drho, a);
-  if (lane != 0) return;
+  __shared__ RowSums<D> R;
+  pairB_sums<D, L>(S, B, N, R);
+  if (threadIdx.x >= 32) return;
+  const int64_t k = (int64_t)blockIdx.x * 32 + threadIdx.x;
+  if (k >= N) return;
+  double a[D];
+#pragma unroll
+  for (int d = 0; d < D; ++d) a[d] = R.a[d][threadIdx.x];
+  const double drho = R.drho[threadIdx.x];
   a[1] = a[1] - c.g;
   const int ptk = S.pt[k];
   const double hdt = sc->dt * 0.5;
@@ -193,57 +231,55 @@ __global__ void __launch_bounds__(STPB) k_pairB1(StepConst c, const Scal* __rest
 
 // pass B, stage 2: row sums + symplectic_update! + max |cΔx|
 template <int D, int L>
-__global__ void __launch_bounds__(STPB) k_pairB2(StepConst c, Scal* __restrict__ sc, int64_t N, SArr<D> S,
-                                                 PairBuf B) {
-  if (*S.ovf) return;  // uniform over the grid, before the block reduction below
-  const int64_t gt = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const int64_t k = gt / L;
-  const int lane = (int)(gt % L);
+__global__ void __launch_bounds__(32 * L) k_pairB2(StepConst c, Scal* __restrict__ sc, int64_t N, SArr<D> S,
+                                                   PairBuf B) {
+  if (*S.ovf) return;  // uniform over the grid, before the barrier below
+  __shared__ RowSums<D> R;
+  pairB_sums<D, L>(S, B, N, R);
+  if (threadIdx.x >= 32) return;
+  const int64_t k = (int64_t)blockIdx.x * 32 + threadIdx.x;
   double mc = 0.0;
   if (k < N) {
-    double drho, a[D];
-    row_sums<D, L>(S, B, k, lane, group_mask<L>(), drho, a);
-    if (lane == 0) {
-      const double dt = sc->dt;
-      a[1] = a[1] - c.g;
-      const int ptk = S.pt[k];
-      S.drho[k] = drho;
-      S.Plast[k] = S.P2[k];
-      const double epsi = -(drho / S.rhoh[k]) * dt;
-      double rv = S.rho[k] * (2.0 - epsi) / (2.0 + epsi);
-      if (rv < c.rho0 && ptk <= 1) rv = c.rho0;
-      S.rho[k] = rv;
-      S.rhoho[k] = rv;
-      S.P1[k] = eos(rv, c.gamma, c.rho0, c.P0, ptk);
-      S.ir[k] = 1.0 / rv;
-      const double ml = ptk > 1 ? 1.0 : 0.0;
+    double a[D];
 #pragma unroll
-      for (int d = 0; d < D; ++d) {
-        S.a[d][k] = a[d];
-        const double vv = S.v[d][k];
-        const double nv = vv + a[d] * dt * ml;
-        S.vho[d][k] = nv;
-        S.v[d][k] = nv;
-        const double ddx = (vv + nv) * 0.5 * dt;
-        const double cd = S.cdx[d][k] + ddx;
-        S.cdx[d][k] = cd;
-        mc = fmax(mc, fabs(cd));
-        const double xv = S.x[d][k] + ddx;
-        S.xho[d][k] = xv;
-        S.xo[d][k] = xv;
-      }
+    for (int d = 0; d < D; ++d) a[d] = R.a[d][threadIdx.x];
+    const double drho = R.drho[threadIdx.x];
+    const double dt = sc->dt;
+    a[1] = a[1] - c.g;
+    const int ptk = S.pt[k];
+    S.drho[k] = drho;
+    S.Plast[k] = S.P2[k];
+    const double epsi = -(drho / S.rhoh[k]) * dt;
+    double rv = S.rho[k] * (2.0 - epsi) / (2.0 + epsi);
+    if (rv < c.rho0 && ptk <= 1) rv = c.rho0;
+    S.rho[k] = rv;
+    S.rhoho[k] = rv;
+    S.P1[k] = eos(rv, c.gamma, c.rho0, c.P0, ptk);
+    S.ir[k] = 1.0 / rv;
+    const double ml = ptk > 1 ? 1.0 : 0.0;
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      S.a[d][k] = a[d];
+      const double vv = S.v[d][k];
+      const double nv = vv + a[d] * dt * ml;
+      S.vho[d][k] = nv;
+      S.v[d][k] = nv;
+      const double ddx = (vv + nv) * 0.5 * dt;
+      const double cd = S.cdx[d][k] + ddx;
+      S.cdx[d][k] = cd;
+      mc = fmax(mc, fabs(cd));
+      const double xv = S.x[d][k] + ddx;
+      S.xho[d][k] = xv;
+      S.xo[d][k] = xv;
     }
   }
   mc = warp_max(mc);
-  __shared__ double smax[STPB / 32];
-  if ((threadIdx.x & 31) == 0) smax[threadIdx.x >> 5] = mc;
-  __syncthreads();
+  __syncwarp();
   if (threadIdx.x == 0) {
-    double m = smax[0];
-    for (int w = 1; w < STPB / 32; ++w) m = fmax(m, smax[w]);
-    atomic_max_pos(&sc->maxcdx, m);
+    atomic_max_pos(&sc->maxcdx, mc);
     if (c.fold_end) {
-      // the last block to finish ends the step (k_step_end's work)
+      // the last block to finish ends the step (k_step_end's work); only
+      // warp 0 of each block writes step state, and its lane 0 signals here
       __threadfence();
       if (atomicAdd(&sc->bdone, 1u) == gridDim.x - 1) {
         __threadfence();
@@ -256,28 +292,26 @@ __global__ void __launch_bounds__(STPB) k_pairB2(StepConst c, Scal* __restrict__
 }
 
 
-static int64_t gcd64(int64_t a, int64_t b) {
-  while (b) {
-    const int64_t t = a % b;
-    a = b;
-    b = t;
-  }
-  return a;
-}
-
 template <int D>
-int launch_pairA(int stage, int64_t threads, cudaStream_t st, const StepConst& c, const SArr<D>& S,
-                 const PairBuf& B) {
-  const int g = nblocks(threads, STPB);
-  // a stride near W / golden ratio, coprime to the grid's W warps
-  const int64_t W = (int64_t)g * (STPB / 32);
-  int64_t spread = (int64_t)(0.6180339887 * (double)W) | 1;
-  while (spread > 1 && gcd64(spread, W) != 1) spread += 2;
-  if (spread < 1 || spread >= W) spread = 1;
+int launch_pairA(int stage, cudaStream_t st, const StepConst& c, const SArr<D>& S, const PairBuf& B) {
+  // one block per SM (the kernel's registers and PA_TPB leave room for one);
+  // the occupancy query covers a build where two would fit
+  static int grid[2] = {0, 0};
+  int& g = grid[stage - 1];
+  if (g == 0) {
+    int dev = 0, sms = 0, per = 0;
+    GC_CUDA(cudaGetDevice(&dev));
+    GC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    if (stage == 1)
+      GC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_pairA<D, 1>, PA_TPB, 0));
+    else
+      GC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_pairA<D, 2>, PA_TPB, 0));
+    g = sms * (per > 0 ? per : 1);
+  }
   if (stage == 1)
-    k_pairA<D, 1><<<g, STPB, 0, st>>>(c, S, B, spread);
+    k_pairA<D, 1><<<g, PA_TPB, 0, st>>>(c, S, B);
   else
-    k_pairA<D, 2><<<g, STPB, 0, st>>>(c, S, B, spread);
+    k_pairA<D, 2><<<g, PA_TPB, 0, st>>>(c, S, B);
   GC_LAUNCHED();
   return GCSPH_OK;
 }
@@ -285,12 +319,12 @@ int launch_pairA(int stage, int64_t threads, cudaStream_t st, const StepConst& c
 template <int D>
 int launch_pairB(int stage, int L, int64_t N, cudaStream_t st, const StepConst& c, Scal* sc, const SArr<D>& S,
                  const PairBuf& B) {
-  const int g = nblocks(N * (int64_t)L, STPB);
+  const int g = nblocks(N, 32);  // 32 particles per block, 32 L threads
 #define GC_PAIRB(LL)                                                        \
   if (stage == 1)                                                          \
-    k_pairB1<D, LL><<<g, STPB, 0, st>>>(c, sc, N, S, B);                   \
+    k_pairB1<D, LL><<<g, 32 * LL, 0, st>>>(c, sc, N, S, B);                \
   else                                                                     \
-    k_pairB2<D, LL><<<g, STPB, 0, st>>>(c, sc, N, S, B);
+    k_pairB2<D, LL><<<g, 32 * LL, 0, st>>>(c, sc, N, S, B);
   switch (L) {
     case 2: GC_PAIRB(2) break;
     case 4: GC_PAIRB(4) break;
@@ -303,8 +337,8 @@ int launch_pairB(int stage, int L, int64_t N, cudaStream_t st, const StepConst& 
   return GCSPH_OK;
 }
 
-template int launch_pairA<2>(int, int64_t, cudaStream_t, const StepConst&, const SArr<2>&, const PairBuf&);
-template int launch_pairA<3>(int, int64_t, cudaStream_t, const StepConst&, const SArr<3>&, const PairBuf&);
+template int launch_pairA<2>(int, cudaStream_t, const StepConst&, const SArr<2>&, const PairBuf&);
+template int launch_pairA<3>(int, cudaStream_t, const StepConst&, const SArr<3>&, const PairBuf&);
 template int launch_pairB<2>(int, int, int64_t, cudaStream_t, const StepConst&, Scal*, const SArr<2>&,
                              const PairBuf&);
 template int launch_pairB<3>(int, int, int64_t, cudaStream_t, const StepConst&, Scal*, const SArr<3>&,

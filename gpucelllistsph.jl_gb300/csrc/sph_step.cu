@@ -915,13 +915,11 @@ static int rebuild(sph_handle* h, const StepConst& c, int* ovf_dev) {
     }                                                                                         \
   } while (0)
 
-// pass A: one thread per pair, the grid sized by the entry capacity (the
-// pair count itself stays on the device)
-// pass A: one thread per pair, the grid sized by the entry capacity (the
-// pair count itself stays on the device); pass B: L lanes per row
+// pass A: one thread per pair, one block per SM (the pair count itself
+// stays on the device); pass B: L lanes per row
 #define PAIRA_LAUNCH(STAGE, ...)                                                              \
   do {                                                                                        \
-    const int _rc = launch_pairA<D>(STAGE, h->cl->core.nbr_cap / 2 + 1, st, __VA_ARGS__);     \
+    const int _rc = launch_pairA<D>(STAGE, st, __VA_ARGS__);                                  \
     if (_rc) return _rc;                                                                      \
   } while (0)
 

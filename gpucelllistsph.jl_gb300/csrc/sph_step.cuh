@@ -436,7 +436,25 @@ __device__ inline void row_sums(const SArr<D>& S, const PairBuf& B, int64_t k, i
 #pragma unroll
   for (int d = 0; d < D; ++d) a[d] = 0.0;
   const int64_t e0 = S.rs[k], e1 = S.rs[k + 1];
-  for (int64_t e = e0 + lane; e < e1; e += L) {
+  int64_t e = e0 + lane;
+  // four entries' loads in flight at a time; each sum still adds its
+  // entries in row order
+  for (; e + 3 * L < e1; e += 4 * L) {
+    double cv[4], av[4][D];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      cv[j] = B.cd[e + j * L];
+#pragma unroll
+      for (int d = 0; d < D; ++d) av[j][d] = B.ca[d][e + j * L];
+    }
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      drho += cv[j];
+#pragma unroll
+      for (int d = 0; d < D; ++d) a[d] += av[j][d];
+    }
+  }
+  for (; e < e1; e += L) {
     drho += B.cd[e];
 #pragma unroll
     for (int d = 0; d < D; ++d) a[d] += B.ca[d][e];
@@ -447,11 +465,11 @@ __device__ inline void row_sums(const SArr<D>& S, const PairBuf& B, int64_t k, i
 }
 
 
-// pair-once passes (sph_once.cu): pass A over `threads` pair slots, pass B
-// (row sums + predictor / corrector) with L lanes per particle
+// pair-once passes (sph_once.cu): pass A over the device-side pair count,
+// one block per SM; pass B (row sums + predictor / corrector) with L lanes
+// per particle, 32 particles per block
 template <int D>
-int launch_pairA(int stage, int64_t threads, cudaStream_t st, const StepConst& c, const SArr<D>& S,
-                 const PairBuf& B);
+int launch_pairA(int stage, cudaStream_t st, const StepConst& c, const SArr<D>& S, const PairBuf& B);
 template <int D>
 int launch_pairB(int stage, int L, int64_t N, cudaStream_t st, const StepConst& c, Scal* sc, const SArr<D>& S,
                  const PairBuf& B);
