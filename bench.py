@@ -154,10 +154,11 @@ def algorithmic_flops_stage1(case, x, v):
                         "approaching": int(approach.sum()), "within_r0": int(inside.sum())}
 
 
-# DRAM bytes (read + write) of one stage-1 pass A launch on this workload, from
-# the ncu capture summarised in profiles/pairA_dambreak2d_c1_fp64.md
-PAIRA_STAGE1_DRAM_BYTES = 2_100_992 + 512
-PAIRA_STAGE1_FP64_PIPE = 0.777
+# DRAM bytes (read + write) of one stage-1 pass A launch on this workload and
+# its FP64 pipe's busy fraction (of active cycles), from one ncu --set full
+# capture of that launch (one block per SM, 103,881 pairs)
+PAIRA_STAGE1_DRAM_BYTES = 2_089_728 + 768
+PAIRA_STAGE1_FP64_PIPE = 0.771
 
 
 class Clocks:

@@ -108,17 +108,8 @@ __global__ void k_cellkey(const double* __restrict__ x0, const double* __restric
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   int pop = 0;
   if (i < N) {
-    const double* xs[3] = {x0, x1, x2};
-    int64_t lin = 0, stride = 1;
-#pragma unroll
-    for (int d = 0; d < D; ++d) {
-      double p = (xs[d][i] - g.offset[d]) * g.hinv[d];
-      double c = fmin(fmax(p, 1.0), (double)g.nc[d]);
-      int ci = (int)ceil(c);
-      lin += (int64_t)(ci - 1) * stride;
-      stride *= g.nc[d];
-    }
-    key[i] = (int32_t)lin;
+    const int32_t lin = cell_key<D>(x0, x1, x2, i, g);
+    key[i] = lin;
     slot[i] = pop = atomicAdd(&count[lin], 1);
     ++pop;
   }
@@ -166,19 +157,7 @@ __global__ void k_rank_apply(const int32_t* __restrict__ tmp, const int32_t* __r
                              int32_t* __restrict__ perm, int32_t* __restrict__ skey, int32_t* __restrict__ orig) {
   int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= N) return;
-  int32_t i = tmp[q];
-  int32_t c = key[i];
-  int32_t s = cellstart[c], e = cellstart[c + 1];
-  int32_t oi = ord ? ord[i] : i;
-  int32_t r = 0;
-  for (int32_t t = s; t < e; ++t) {
-    int32_t j = tmp[t];
-    int32_t oj = ord ? ord[j] : j;
-    r += (oj < oi);
-  }
-  perm[s + r] = i;
-  skey[s + r] = c;
-  orig[s + r] = oi;
+  rank_in_cell(tmp, key, cellstart, ord, q, perm, skey, orig);
 }
 
 __global__ void k_apply_perm(const int32_t* __restrict__ perm, const int32_t* __restrict__ key,
@@ -493,6 +472,8 @@ int CellCore::init(int D_, int64_t N_, const double* cellsize, double dist_, con
   if ((rc = tmp.ensure(sizeof(int32_t) * N, st))) return rc;
   if ((rc = perm.ensure(sizeof(int32_t) * N, st))) return rc;
   if ((rc = skey.ensure(sizeof(int32_t) * N, st))) return rc;
+  // the spare original-index map every binning writes into (then swapped in)
+  if ((rc = orig_b.ensure(sizeof(int32_t) * N, st))) return rc;
   if ((rc = orig.ensure(sizeof(int32_t) * N, st))) return rc;
   if ((rc = cnt_full.ensure(sizeof(int32_t) * N, st))) return rc;
   if ((rc = cnt_up.ensure(sizeof(int32_t) * N, st))) return rc;
@@ -528,8 +509,9 @@ void CellCore::release() {
   pin = nullptr;
 }
 
-int CellCore::sort(const double* const* xin, const int32_t* ord, bool may_sync) {
+int CellCore::sort(const double* const* xin, const int32_t* ord, bool may_sync, bool* rank_deferred) {
   timer_begin(T_SORT, st);
+  if (rank_deferred) *rank_deferred = false;
   GC_CUDA(cudaMemsetAsync(count.p, 0, sizeof(int32_t) * g.ncell, st));
   const double* x2 = D == 3 ? xin[2] : xin[0];
   int rc;
@@ -599,17 +581,27 @@ int CellCore::sort(const double* const* xin, const int32_t* ord, bool may_sync) 
     k_scatter_arrival<<<nblocks(N, tb), tb, 0, st>>>(key.as<int32_t>(), slot.as<int32_t>(), cellstart.as<int32_t>(),
                                                       N, tmp.as<int32_t>());
     GC_LAUNCHED();
+    if (rank_deferred) {
+      // the caller ranks (rank_in_cell) and applies the order in its own pass
+      *rank_deferred = true;
+      timer_end(T_SORT, st);
+      return GCSPH_OK;
+    }
     k_rank_apply<<<nblocks(N, tb), tb, 0, st>>>(tmp.as<int32_t>(), key.as<int32_t>(), cellstart.as<int32_t>(), ord, N,
                                                  perm.as<int32_t>(), skey.as<int32_t>(), orig_b.as<int32_t>());
     GC_LAUNCHED();
   }
+  sort_done();
+  timer_end(T_SORT, st);
+  return GCSPH_OK;
+}
+
+void CellCore::sort_done() {
   std::swap(orig.p, orig_b.p);
   std::swap(orig.bytes, orig_b.bytes);
-  timer_end(T_SORT, st);
   sorted = true;
   built = false;
   up_valid = false;
-  return GCSPH_OK;
 }
 
 int CellCore::read_popmax() {
@@ -707,11 +699,15 @@ __device__ __forceinline__ void pairs32_row(const double* __restrict__ x0, const
                                                  int32_t* __restrict__ cnt_full, int32_t* __restrict__ cnt_up,
                                                  const int64_t* __restrict__ rs_full, int32_t* __restrict__ nbr,
                                                  int64_t cap, int* __restrict__ ovf, int32_t* __restrict__ stg,
-                                                 int S, const int32_t* fold_buf) {
+                                                 int S, const int32_t* fold_buf, bool up) {
   // MODE 0: count; MODE 2: count and stage the row (ascending) in stg[k*S ..]
   // when it fits; MODE 1: fill the CSR row -- a copy of the staged row when
   // the count pass staged it, else the search again.  MODE 1 reads the row
-  // starts from the count pass's fold buffer where it folded (FoldRows)
+  // starts from the count pass's fold buffer where it folded (FoldRows).
+  // up: the half stencil, candidates m > k only (the cell list's own
+  // (min, max) list): the rows whose cells all come before k's in key order
+  // are skipped and k's own row starts at k + 1, so a row holds exactly the
+  // larger-index part of the full row, in the same order
   const int64_t gt = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int64_t k = gt / L;
   const int lane = (int)(gt % L);
@@ -809,10 +805,11 @@ __device__ __forceinline__ void pairs32_row(const double* __restrict__ x0, const
       for (int r = 0; r < NR; ++r) {
         const int z = cz + (r / 3 - 1), y = cy + (r % 3 - 1);
         int32_t m0 = 0, m1 = 0;
-        if (z >= 0 && z < nz && y >= 0 && y < ny) {
+        if (z >= 0 && z < nz && y >= 0 && y < ny && !(up && r < NR / 2)) {
           const int64_t base = (int64_t)nx * ((int64_t)y + (int64_t)ny * z);
           m0 = cellstart[base + xlo];
           m1 = cellstart[base + xhi + 1];
+          if (up && r == NR / 2) m0 = (int32_t)(k + 1);  // k's own row: k lies in it
         }
         rows[r] = tot;
         rows[NR + 1 + r] = m0 - tot;
@@ -835,11 +832,13 @@ __device__ __forceinline__ void pairs32_row(const double* __restrict__ x0, const
       visit(m, t < tot && m != k);
     }
   } else {
-    for (int dy = -1; dy <= 1; ++dy) {
+    for (int dy = up ? 0 : -1; dy <= 1; ++dy) {
       const int y = cy + dy;
       if (y < 0 || y >= ny) continue;
       const int64_t base = (int64_t)nx * (int64_t)y;
-      const int32_t m0 = cellstart[base + xlo], m1 = cellstart[base + xhi + 1];
+      int32_t m0 = cellstart[base + xlo];
+      const int32_t m1 = cellstart[base + xhi + 1];
+      if (up && dy == 0) m0 = (int32_t)(k + 1);  // k's own row: k lies in it
       for (int32_t mb = m0; mb < m1; mb += L) {
         const int32_t m = mb + lane;
         visit(m, m < m1 && m != k);
@@ -1013,7 +1012,7 @@ __global__ void __launch_bounds__(TPB) k_pairs32(const double* __restrict__ x0, 
                                                  int64_t cap, int* __restrict__ ovf, int32_t* __restrict__ stg,
                                                  int S, int64_t* fold_rs_full, int64_t* fold_rs_up,
                                                  unsigned* fold_cnt, const int64_t* __restrict__ rs_up,
-                                                 int4* __restrict__ pq, int32_t* fold_buf) {
+                                                 int4* __restrict__ pq, int32_t* fold_buf, bool up) {
   if ((MODE == 1 || MODE == 3) && fold_buf) {
     // small sets: the final row starts, from the count pass's two levels
     const int64_t gt = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -1025,7 +1024,7 @@ __global__ void __launch_bounds__(TPB) k_pairs32(const double* __restrict__ x0, 
   }
   pairs32_row<D, MODE == 3 ? 1 : (MODE == 4 ? 2 : MODE), L>(x0, x1, x2, f0, f1, f2, thr, skey, cellstart, N, g,
                                                              cnt_full, cnt_up, rs_full, nbr, cap, ovf, stg, S,
-                                                             fold_buf);
+                                                             fold_buf, up);
   if (MODE == 4) rows_fold<L>(cnt_full, cnt_up, N, fold_rs_full, fold_rs_up, fold_buf, fold_cnt);
   if (MODE == 3) {
     __syncwarp();  // a recomputed row's entries, written by the group's lanes, are read back
@@ -1120,8 +1119,14 @@ int CellCore::ensure_pf() {
 }
 
 int CellCore::build_pairs(const double* const* xs, int* ovf_dev, bool scan_up, bool pf_ready, int4* pq,
-                          bool* pq_done) {
+                          bool* pq_done, bool up) {
   if (pq_done) *pq_done = false;
+  if (up) {
+    // the half stencil: every row is its larger-index part, so both counts
+    // and both row-start scans are the same; no pair list for the step
+    scan_up = true;
+    pq = nullptr;
+  }
   if (!sorted) return fail(GCSPH_ESTATE, "pair build before binning");
   const double* x2 = D == 3 ? xs[2] : xs[0];
   timer_begin(T_PAIRS, st);
@@ -1142,7 +1147,8 @@ int CellCore::build_pairs(const double* const* xs, int* ovf_dev, bool scan_up, b
     GC_LAUNCHED();
   }
   // rows of up to S neighbours are staged by the count pass and copied by the fill
-  const double mean = N > 0 && nfull_est > 0 ? (double)nfull_est / (double)N : 0.0;
+  // nfull_est counts full rows (a half-stencil build records twice its count)
+  const double mean = N > 0 && nfull_est > 0 ? (up ? 0.5 : 1.0) * (double)nfull_est / (double)N : 0.0;
   int S = 16;
   while (S < 256 && (double)S < 1.5 * mean + 8.0) S <<= 1;
   int32_t* sp = nullptr;
@@ -1159,15 +1165,15 @@ int CellCore::build_pairs(const double* const* xs, int* ovf_dev, bool scan_up, b
     PAIRS32_LAUNCH(4, L, xs[0], xs[1], x2, pf[0].as<float>(), pf[1].as<float>(), f2, thr, skey.as<int32_t>(),
                    cellstart.as<int32_t>(), N, g, cnt_full.as<int32_t>(), cnt_up.as<int32_t>(), nullptr, nullptr, 0,
                    nullptr, sp, S, rs_full.as<int64_t>(), rs_up.as<int64_t>(), fc, nullptr, nullptr,
-                   foldsum.as<int32_t>());
+                   foldsum.as<int32_t>(), up);
   else if (sp)
     PAIRS32_LAUNCH(2, L, xs[0], xs[1], x2, pf[0].as<float>(), pf[1].as<float>(), f2, thr, skey.as<int32_t>(),
                    cellstart.as<int32_t>(), N, g, cnt_full.as<int32_t>(), cnt_up.as<int32_t>(), nullptr, nullptr, 0,
-                   nullptr, sp, S, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr);
+                   nullptr, sp, S, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, up);
   else
     PAIRS32_LAUNCH(0, L, xs[0], xs[1], x2, pf[0].as<float>(), pf[1].as<float>(), f2, thr, skey.as<int32_t>(),
                    cellstart.as<int32_t>(), N, g, cnt_full.as<int32_t>(), cnt_up.as<int32_t>(), nullptr, nullptr, 0,
-                   nullptr, nullptr, 0, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr);
+                   nullptr, nullptr, 0, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, up);
   GC_LAUNCHED();
   int rc = GCSPH_OK;
   if (!fold)
@@ -1187,7 +1193,7 @@ int CellCore::build_pairs(const double* const* xs, int* ovf_dev, bool scan_up, b
     GC_CUDA(cudaStreamSynchronize(st));
     timer_collect();
     nfull = pin[0];
-    nfull_est = nfull;
+    nfull_est = up ? 2 * nfull : nfull;
     if (nfull > nbr_cap && (rc = grow_nbr(nfull))) return rc;
   }
   timer_begin(T_PAIRS, st);
@@ -1198,17 +1204,18 @@ int CellCore::build_pairs(const double* const* xs, int* ovf_dev, bool scan_up, b
     PAIRS32_LAUNCH(3, L, xs[0], xs[1], x2, pf[0].as<float>(), pf[1].as<float>(), f2, thr, skey.as<int32_t>(),
                    cellstart.as<int32_t>(), N, g, cnt_full.as<int32_t>(), cnt_up.as<int32_t>(),
                    rs_full.as<int64_t>(), nbr.as<int32_t>(), nbr_cap, ovf_dev, sp, S, frs_full, frs_up, nullptr,
-                   rs_up.as<int64_t>(), pq, fbuf);
+                   rs_up.as<int64_t>(), pq, fbuf, false);
     if (pq_done) *pq_done = true;
   } else {
     PAIRS32_LAUNCH(1, L, xs[0], xs[1], x2, pf[0].as<float>(), pf[1].as<float>(), f2, thr, skey.as<int32_t>(),
                    cellstart.as<int32_t>(), N, g, nullptr, nullptr, rs_full.as<int64_t>(), nbr.as<int32_t>(), nbr_cap,
-                   ovf_dev, sp, S, frs_full, frs_up, nullptr, nullptr, nullptr, fbuf);
+                   ovf_dev, sp, S, frs_full, frs_up, nullptr, nullptr, nullptr, fbuf, up);
   }
   GC_LAUNCHED();
   timer_end(T_PAIRS, st);
   built = true;
   up_valid = false;
+  rows_upper = up;
   return GCSPH_OK;
 }
 
@@ -1225,7 +1232,7 @@ int CellCore::read_nfull() {
   GC_CUDA(cudaMemcpyAsync(pin, rs_full.as<int64_t>() + N, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
   GC_CUDA(cudaStreamSynchronize(st));
   nfull = pin[0];
-  nfull_est = nfull;
+  nfull_est = rows_upper ? 2 * nfull : nfull;
   return GCSPH_OK;
 }
 
@@ -1300,12 +1307,14 @@ int CellCore::maxpairs(int64_t* out) {
 // ---------------------------------------------------------------------------
 using namespace gcsph;
 
+// update! and partialupdate! return the pairs k < m only: their builds take
+// the half stencil
 static int gcl_full_update(gcl_handle* h) {
   int rc = h->core.sort(h->xuser, nullptr, true);
   if (rc) return rc;
   double* xs[3] = {h->xs[0].as<double>(), h->xs[1].as<double>(), h->core.D == 3 ? h->xs[2].as<double>() : nullptr};
   if ((rc = h->core.gather_positions(h->xuser, xs))) return rc;
-  return h->core.build_pairs((const double* const*)xs);
+  return h->core.build_pairs((const double* const*)xs, nullptr, false, false, nullptr, nullptr, true);
 }
 
 extern "C" {
@@ -1369,7 +1378,7 @@ int gcl_partialupdate(gcl_handle* h, int64_t* pairsn_out) {
   double* xs[3] = {h->xs[0].as<double>(), h->xs[1].as<double>(), h->core.D == 3 ? h->xs[2].as<double>() : nullptr};
   int rc = h->core.gather_positions_by_orig(h->xuser, xs);
   if (rc) return rc;
-  if ((rc = h->core.build_pairs((const double* const*)xs))) return rc;
+  if ((rc = h->core.build_pairs((const double* const*)xs, nullptr, false, false, nullptr, nullptr, true))) return rc;
   if ((rc = h->core.ensure_up())) return rc;
   if (pairsn_out) *pairsn_out = h->core.nup;
   GC_CUDA(cudaStreamSynchronize(h->core.st));

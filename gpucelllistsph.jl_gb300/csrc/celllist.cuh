@@ -27,6 +27,48 @@ struct Grid {
   double dist2;
 };
 
+// the cell of point i (0-based linear key, x fastest): kernel_cellmap!'s
+// clamped ceil((x - offset) / cellsize), src/gpukernels_cls.jl:28-60
+template <int D>
+__device__ inline int32_t cell_key(const double* x0, const double* x1, const double* x2, int64_t i, const Grid& g) {
+  const double* xs[3] = {x0, x1, x2};
+  int64_t lin = 0, stride = 1;
+#pragma unroll
+  for (int d = 0; d < D; ++d) {
+    const double p = (xs[d][i] - g.offset[d]) * g.hinv[d];
+    const double c = fmin(fmax(p, 1.0), (double)g.nc[d]);
+    const int ci = (int)ceil(c);
+    lin += (int64_t)(ci - 1) * stride;
+    stride *= g.nc[d];
+  }
+  return (int32_t)lin;
+}
+
+// The counting sort's last step for the point in arrival position q: its
+// rank among its cell's points by original index (a stable, history-free
+// order; cost: the cell's population), and so its slot k in cell order,
+// where the map entries go.  Returns k; *i_out is the point's input index.
+__device__ inline int64_t rank_in_cell(const int32_t* __restrict__ tmp, const int32_t* __restrict__ key,
+                                       const int32_t* __restrict__ cellstart, const int32_t* __restrict__ ord,
+                                       int64_t q, int32_t* __restrict__ perm, int32_t* __restrict__ skey,
+                                       int32_t* __restrict__ orig, int32_t* i_out = nullptr) {
+  const int32_t i = tmp[q];
+  const int32_t c = key[i];
+  const int32_t s = cellstart[c], e = cellstart[c + 1];
+  const int32_t oi = ord ? ord[i] : i;
+  int32_t r = 0;
+  for (int32_t t = s; t < e; ++t) {
+    const int32_t j = tmp[t];
+    const int32_t oj = ord ? ord[j] : j;
+    r += (oj < oi);
+  }
+  perm[s + r] = i;
+  skey[s + r] = c;
+  orig[s + r] = oi;
+  if (i_out) *i_out = i;
+  return s + r;
+}
+
 template <int D>
 __device__ inline void pf_thresholds_from(unsigned long long bits, double dist2, float* tlo, float* thi) {
   const double B = __longlong_as_double((long long)bits) * (1.0 + 0x1p-28);
@@ -95,6 +137,7 @@ struct CellCore {
   int64_t nfull_est = 0;  // last neighbour-entry count read back (lane choice); nfull is -1 while unknown
   int64_t gen = 0;        // bumped whenever a buffer a captured step graph points into is reallocated
   bool sorted = false, built = false, up_valid = false;
+  bool rows_upper = false;  // the last build stored the larger-index part of each row only
   int lanes = 0;  // lanes per particle in the pair search; 0 = by mean candidate count
   int sort_mode = 0;    // in-cell order: 0 by the population, 1 counting sort's rank, 2 radix sort
   int last_popmax = 0;  // largest cell population seen (large sets; read where the host waits anyway)
@@ -111,7 +154,12 @@ struct CellCore {
   // ord == nullptr means the input order is the original order.
   // may_sync: the caller waits anyway, so the most crowded cell of this very
   // binning is read back to pick the ordering (else the last one read)
-  int sort(const double* const* xin, const int32_t* ord, bool may_sync = false);
+  // rank_deferred (the counting sort's path only, where it is set true):
+  // stop after the arrival lists; the caller ranks each point with
+  // rank_in_cell in a pass of its own and then calls sort_done
+  int sort(const double* const* xin, const int32_t* ord, bool may_sync = false, bool* rank_deferred = nullptr);
+  // the bookkeeping after a binning into perm / skey / orig_b (orig_b becomes orig)
+  void sort_done();
   int read_popmax();
   // gather xs[d][k] = xin[d][perm[k]] (and orig[k] = ord[perm[k]] is done by sort)
   int gather_positions(const double* const* xin, double* const* xs);
@@ -127,8 +175,10 @@ struct CellCore {
   // pair-once passes when the count pass staged the rows and the fill runs without a host
   // round trip (the capacity unchanged: pq must hold nbr_cap / 2 + 1 pairs); *pq_done says
   // whether it did
+  // up: the half stencil (only the m > k part of each row is searched and
+  // stored: rs_full == rs_up), for callers that need the pairs k < m alone
   int build_pairs(const double* const* xs, int* ovf_dev = nullptr, bool scan_up = false, bool pf_ready = false,
-                  int4* pq = nullptr, bool* pq_done = nullptr);
+                  int4* pq = nullptr, bool* pq_done = nullptr, bool up = false);
   int ensure_pf();
   int grow_nbr(int64_t need);
   int read_nfull();

@@ -529,38 +529,66 @@ struct PermOut {
   double dist2;
 };
 
-// new[k] = old[perm[k]] for the whole cell-order state; cΔx restarts at 0
-// (src/sphproblem.jl:229), P(ρ) and 1/ρ are recomputed for stage 1
+// new[k] = old[i] for the whole cell-order state of one particle; cΔx
+// restarts at 0 (src/sphproblem.jl:229), P(ρ) and 1/ρ are recomputed for
+// stage 1; b takes the max |x - offset| of the FP32 prefilter copy
+template <int D>
+__device__ __forceinline__ void permute_one(const StepConst& c, const SArr<D>& S, const PermOut<D>& O, int64_t i,
+                                            int64_t k, double& b) {
+  double bk = 0.0;
+#pragma unroll
+  for (int d = 0; d < D; ++d) {
+    const double xv = S.x[d][i];
+    O.x[d][k] = xv;
+    const double rel = xv - O.off[d];
+    O.pf[d][k] = (float)rel;
+    bk = fmax(bk, fabs(rel));
+  }
+  if (bk != bk) bk = INFINITY;  // NaN coordinate: every candidate of the set goes to FP64
+  b = fmax(b, bk);
+  const int pt = S.pt[i];
+  O.pt[k] = pt;
+  const double r = S.rho[i];
+  O.rho[k] = r;
+  O.rhoh[k] = S.rhoh[i];
+  S.P1[k] = eos(r, c.gamma, c.rho0, c.P0, pt);
+  S.ir[k] = 1.0 / r;
+#pragma unroll
+  for (int d = 0; d < D; ++d) {
+    O.xh[d][k] = S.xh[d][i];
+    O.v[d][k] = S.v[d][i];
+    O.vh[d][k] = S.vh[d][i];
+    O.buf2[d][k] = S.buf2[d][i];
+    S.cdx[d][k] = 0.0;
+  }
+}
+
+// new[k] = old[perm[k]] for the whole cell-order state
 template <int D>
 __global__ void k_permute_state(StepConst c, int64_t N, const int32_t* __restrict__ perm, SArr<D> S, PermOut<D> O) {
   int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   double b = 0.0;
-  if (k < N) {
-    const int32_t i = perm[k];
-#pragma unroll
-    for (int d = 0; d < D; ++d) {
-      const double xv = S.x[d][i];
-      O.x[d][k] = xv;
-      const double rel = xv - O.off[d];
-      O.pf[d][k] = (float)rel;
-      b = fmax(b, fabs(rel));
-    }
-    if (b != b) b = INFINITY;  // NaN coordinate: every candidate of the set goes to FP64
-    const int pt = S.pt[i];
-    O.pt[k] = pt;
-    const double r = S.rho[i];
-    O.rho[k] = r;
-    O.rhoh[k] = S.rhoh[i];
-    S.P1[k] = eos(r, c.gamma, c.rho0, c.P0, pt);
-    S.ir[k] = 1.0 / r;
-#pragma unroll
-    for (int d = 0; d < D; ++d) {
-      O.xh[d][k] = S.xh[d][i];
-      O.v[d][k] = S.v[d][i];
-      O.vh[d][k] = S.vh[d][i];
-      O.buf2[d][k] = S.buf2[d][i];
-      S.cdx[d][k] = 0.0;
-    }
+  if (k < N) permute_one<D>(c, S, O, perm[k], k, b);
+  b = warp_max(b);
+  if ((threadIdx.x & 31) == 0) atomic_max_pos(O.pfmax, b);
+  pf_thresholds_last_block<D>(O.pfmax, O.dist2, O.thr, O.cnt);
+}
+
+// The counting sort's rank and the state permute in one pass (sets the
+// counting sort orders): the point in arrival position q finds its slot k in
+// the new cell order and moves its state there at once -- one launch and one
+// read of the map fewer than k_rank_apply followed by k_permute_state.
+template <int D>
+__global__ void k_rank_permute(StepConst c, int64_t N, const int32_t* __restrict__ tmp,
+                               const int32_t* __restrict__ key, const int32_t* __restrict__ cellstart,
+                               const int32_t* __restrict__ ord, int32_t* __restrict__ perm,
+                               int32_t* __restrict__ skey, int32_t* __restrict__ orig, SArr<D> S, PermOut<D> O) {
+  const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  double b = 0.0;
+  if (q < N) {
+    int32_t i = 0;
+    const int64_t k = rank_in_cell(tmp, key, cellstart, ord, q, perm, skey, orig, &i);
+    permute_one<D>(c, S, O, i, k, b);
   }
   b = warp_max(b);
   if ((threadIdx.x & 31) == 0) atomic_max_pos(O.pfmax, b);
@@ -602,7 +630,7 @@ struct HostSide {
   void* pt[2];
   void* buf2[3][2];
   void* orig[2];
-  bool sorted, built, up_valid, in_cell_order;
+  bool sorted, built, up_valid, in_cell_order, rows_upper;
   int64_t nfull;
 };
 
@@ -849,7 +877,8 @@ static int rebuild(sph_handle* h, const StepConst& c, int* ovf_dev) {
     // the old cell order straight into the new one
     const double* xc[3] = {h->X[h->ix][0].as<double>(), h->X[h->ix][1].as<double>(),
                            D == 3 ? h->X[h->ix][2].as<double>() : nullptr};
-    if ((rc = core.sort(xc, core.orig.as<int32_t>()))) return rc;
+    bool rank_deferred = false;
+    if ((rc = core.sort(xc, core.orig.as<int32_t>(), false, &rank_deferred))) return rc;
     if ((rc = core.ensure_pf())) return rc;
     PermOut<D> alt = make_alt<D>(h);
     for (int d = 0; d < D; ++d) {
@@ -860,14 +889,25 @@ static int rebuild(sph_handle* h, const StepConst& c, int* ovf_dev) {
     alt.thr = core.pfthr.as<float2>();
     alt.cnt = core.pfcnt.as<unsigned>();
     alt.dist2 = core.g.dist2;
-    timer_begin(T_STATE, core.st);
-    // small sets: 64-thread blocks, so the latency-bound gather spreads over more SMs
+    // small sets: 64-thread blocks, so the latency-bound passes spread over more SMs
     const int ptb = h->N <= RADIX_MIN_N ? 64 : 256;
-    k_permute_state<D><<<nblocks(h->N, ptb), ptb, 0, core.st>>>(c, h->N, core.perm.as<int32_t>(), make_arr<D>(h),
-                                                               alt);
+    if (rank_deferred) {
+      timer_begin(T_STATE, core.st);
+      k_rank_permute<D><<<nblocks(h->N, ptb), ptb, 0, core.st>>>(
+          c, h->N, core.tmp.as<int32_t>(), core.key.as<int32_t>(), core.cellstart.as<int32_t>(),
+          core.orig.as<int32_t>(), core.perm.as<int32_t>(), core.skey.as<int32_t>(), core.orig_b.as<int32_t>(),
+          make_arr<D>(h), alt);
+      GC_LAUNCHED();
+      timer_end(T_STATE, core.st);
+      core.sort_done();
+    } else {
+      timer_begin(T_STATE, core.st);
+      k_permute_state<D><<<nblocks(h->N, ptb), ptb, 0, core.st>>>(c, h->N, core.perm.as<int32_t>(), make_arr<D>(h),
+                                                                 alt);
+      GC_LAUNCHED();
+      timer_end(T_STATE, core.st);
+    }
     pf_ready = true;
-    GC_LAUNCHED();
-    timer_end(T_STATE, core.st);
     h->ix ^= 1;
     h->ixh ^= 1;
     h->iv ^= 1;
@@ -945,6 +985,14 @@ static int finish_call(sph_handle* h, const StepConst& c, Scal* dsc) {
   cudaStream_t st = core.st;
   int rc;
   if (h->in_cell_order && (rc = scatter_state<D>(h))) return rc;
+  if (core.built && core.rows_upper) {
+    // no update! ran in this call (n = 0) and the last pair set is the cell
+    // list's own update!, which stores the larger-index half of each row:
+    // the same set again with full rows, on the points it was binned from
+    const double* xs[3] = {h->cl->xs[0].as<double>(), h->cl->xs[1].as<double>(),
+                           D == 3 ? h->cl->xs[2].as<double>() : nullptr};
+    if ((rc = core.build_pairs(xs, nullptr, true))) return rc;
+  }
   // post-batch ∑W, ∑∇W on the last pair set and the final points
   if (core.built) {
     const double* x2 = D == 3 ? h->cl->xuser[2] : h->cl->xuser[0];
@@ -1161,6 +1209,7 @@ static HostSide host_side(const sph_handle* h) {
   s.sorted = core.sorted;
   s.built = core.built;
   s.up_valid = core.up_valid;
+  s.rows_upper = core.rows_upper;
   s.in_cell_order = h->in_cell_order;
   s.nfull = core.nfull;
   return s;
@@ -1186,6 +1235,7 @@ static void set_host_side(sph_handle* h, const HostSide& s) {
   core.sorted = s.sorted;
   core.built = s.built;
   core.up_valid = s.up_valid;
+  core.rows_upper = s.rows_upper;
   h->in_cell_order = s.in_cell_order;
   core.nfull = s.nfull;
 }
@@ -1209,7 +1259,7 @@ static GraphKey graph_key(const sph_handle* h, int32_t n, int timestepping, doub
   k.at = host_side(h);
   // flags and counts the capture does not depend on (it always starts by
   // binning the caller's points) stay out of the key
-  k.at.sorted = k.at.built = k.at.up_valid = k.at.in_cell_order = false;
+  k.at.sorted = k.at.built = k.at.up_valid = k.at.in_cell_order = k.at.rows_upper = false;
   k.at.nfull = 0;
   for (int d = 0; d < 3; ++d) {
     k.user[d] = h->cl->xuser[d];
