@@ -118,7 +118,13 @@ __global__ void k_cellkey(const double* __restrict__ x0, const double* __restric
     for (int o = 16; o > 0; o >>= 1) pop = max(pop, __shfl_xor_sync(0xffffffffu, pop, o));
     if ((threadIdx.x & 31) == 0 && pop > 0) atomicMax(popmax, pop);
   }
-  if (fold_cnt && last_block_of_grid(fold_cnt)) block_exclusive_scan<int32_t>(count, cellstart, g.ncell);
+  if (fold_cnt && last_block_of_grid(fold_cnt)) {
+    block_exclusive_scan<int32_t>(count, cellstart, g.ncell);
+    // the counts are spent: zero again for the next binning (a cell's
+    // population is cellstart[c + 1] - cellstart[c] from here on)
+    __syncthreads();
+    for (int64_t c = threadIdx.x; c < g.ncell; c += blockDim.x) count[c] = 0;
+  }
 }
 
 __global__ void k_scatter_arrival(const int32_t* __restrict__ key, const int32_t* __restrict__ slot,
@@ -384,14 +390,21 @@ __global__ void k_emit_pairs_l(const int64_t* __restrict__ rs_full, const int64_
   }
 }
 
+// points per cell (cellpnum), from the cell starts
+__global__ void k_cell_pop(const int32_t* __restrict__ cellstart, int64_t ncell, int32_t* __restrict__ pop) {
+  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c < ncell) pop[c] = cellstart[c + 1] - cellstart[c];
+}
+
 // мaxpairs: n(n-1)/2 + n * (half-stencil neighbour counts), gpukernels_cls.jl:130-286
 template <int D>
-__global__ void k_maxpairs(const int32_t* __restrict__ count, Grid g, unsigned long long* __restrict__ out) {
+__global__ void k_maxpairs(const int32_t* __restrict__ cellstart, Grid g, unsigned long long* __restrict__ out) {
   int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   unsigned long long v = 0;
+  auto count = [&](int64_t cell) -> int64_t { return cellstart[cell + 1] - cellstart[cell]; };
   if (c < g.ncell) {
     const int nx = g.nc[0], ny = g.nc[1], nz = D == 3 ? g.nc[2] : 1;
-    int64_t n = count[c];
+    int64_t n = count(c);
     if (n > 0) {
       int cx = (int)(c % nx);
       int64_t t = c / nx;
@@ -403,7 +416,7 @@ __global__ void k_maxpairs(const int32_t* __restrict__ count, Grid g, unsigned l
       for (int o = 0; o < no; ++o) {
         int a = cx + off[o][0], b = cy + off[o][1], z = cz + (D == 3 ? off[o][2] : 0);
         if (a >= 0 && a < nx && b >= 0 && b < ny && z >= 0 && z < nz)
-          m += count[a + (int64_t)nx * (b + (int64_t)ny * z)];
+          m += count(a + (int64_t)nx * (b + (int64_t)ny * z));
       }
       v = (unsigned long long)((int64_t)((double)(n * (n - 1)) * 0.5) + m * n);
     }
@@ -465,7 +478,7 @@ int CellCore::init(int D_, int64_t N_, const double* cellsize, double dist_, con
   g.ncell = ncell;
   g.dist2 = dist * dist;
   int rc;
-  if ((rc = count.ensure(sizeof(int32_t) * ncell, st))) return rc;
+  if ((rc = count.ensure(sizeof(int32_t) * ncell, st, true))) return rc;  // zero at rest
   if ((rc = cellstart.ensure(sizeof(int32_t) * (ncell + 1), st))) return rc;
   if ((rc = key.ensure(sizeof(int32_t) * N, st))) return rc;
   if ((rc = slot.ensure(sizeof(int32_t) * N, st))) return rc;
@@ -509,10 +522,13 @@ void CellCore::release() {
   pin = nullptr;
 }
 
-int CellCore::sort(const double* const* xin, const int32_t* ord, bool may_sync, bool* rank_deferred) {
+int CellCore::sort(const double* const* xin, const int32_t* ord, bool may_sync, bool* rank_deferred,
+                   bool keys_ready) {
   timer_begin(T_SORT, st);
   if (rank_deferred) *rank_deferred = false;
-  GC_CUDA(cudaMemsetAsync(count.p, 0, sizeof(int32_t) * g.ncell, st));
+  if (keys_ready && !keys_in_step())
+    return fail(GCSPH_ESTATE, "cell keys from the step for a set that does not take them");
+  // count is zero at rest: every binning zeroes it again once scanned
   const double* x2 = D == 3 ? xin[2] : xin[0];
   int rc;
   const bool fold = g.ncell + 1 <= SCAN_FOLD_MAX;
@@ -520,16 +536,20 @@ int CellCore::sort(const double* const* xin, const int32_t* ord, bool may_sync, 
   // large sets track the most crowded cell, which picks the in-cell ordering
   int* pm = N > RADIX_MIN_N ? popmax.as<int>() : nullptr;
   if (pm) GC_CUDA(cudaMemsetAsync(pm, 0, sizeof(int), st));
-  if (D == 2)
-    k_cellkey<2><<<nblocks(N, TPB), TPB, 0, st>>>(xin[0], xin[1], x2, N, g, key.as<int32_t>(), slot.as<int32_t>(),
-                                                   count.as<int32_t>(), cellstart.as<int32_t>(), fc, pm);
-  else
-    k_cellkey<3><<<nblocks(N, TPB), TPB, 0, st>>>(xin[0], xin[1], x2, N, g, key.as<int32_t>(), slot.as<int32_t>(),
-                                                   count.as<int32_t>(), cellstart.as<int32_t>(), fc, pm);
-  GC_LAUNCHED();
+  // with keys_ready, key, slot and cellstart are written and count is zero again
+  if (!keys_ready) {
+    if (D == 2)
+      k_cellkey<2><<<nblocks(N, TPB), TPB, 0, st>>>(xin[0], xin[1], x2, N, g, key.as<int32_t>(), slot.as<int32_t>(),
+                                                     count.as<int32_t>(), cellstart.as<int32_t>(), fc, pm);
+    else
+      k_cellkey<3><<<nblocks(N, TPB), TPB, 0, st>>>(xin[0], xin[1], x2, N, g, key.as<int32_t>(), slot.as<int32_t>(),
+                                                     count.as<int32_t>(), cellstart.as<int32_t>(), fc, pm);
+    GC_LAUNCHED();
+  }
   if (!fold) {
     rc = exclusive_scan_i32_to_i32(count.as<int32_t>(), cellstart.as<int32_t>(), g.ncell, scratch.as<int64_t>(), st);
     if (rc) return rc;
+    GC_CUDA(cudaMemsetAsync(count.p, 0, sizeof(int32_t) * g.ncell, st));
   }
   if (pm && may_sync && sort_mode == 0 && (rc = read_popmax())) return rc;
   // the in-cell order: the counting sort's rank costs the square of a cell's
@@ -1293,9 +1313,9 @@ int CellCore::maxpairs(int64_t* out) {
   int64_t* d = scratch.as<int64_t>();
   GC_CUDA(cudaMemsetAsync(d, 0, sizeof(int64_t), st));
   if (D == 2)
-    k_maxpairs<2><<<nblocks(g.ncell, TPB), TPB, 0, st>>>(count.as<int32_t>(), g, (unsigned long long*)d);
+    k_maxpairs<2><<<nblocks(g.ncell, TPB), TPB, 0, st>>>(cellstart.as<int32_t>(), g, (unsigned long long*)d);
   else
-    k_maxpairs<3><<<nblocks(g.ncell, TPB), TPB, 0, st>>>(count.as<int32_t>(), g, (unsigned long long*)d);
+    k_maxpairs<3><<<nblocks(g.ncell, TPB), TPB, 0, st>>>(cellstart.as<int32_t>(), g, (unsigned long long*)d);
   GC_LAUNCHED();
   return read_scalar(d, out);
 }
@@ -1392,8 +1412,9 @@ int gcl_emit_pairs(gcl_handle* h, int32_t* pairs_dev, int64_t cap, int fillzero,
 
 int gcl_cellpnum(gcl_handle* h, int32_t* cellpnum_dev) {
   if (!h || !cellpnum_dev) return fail(GCSPH_EINVAL, "null argument");
-  GC_CUDA(cudaMemcpyAsync(cellpnum_dev, h->core.count.p, sizeof(int32_t) * h->core.g.ncell, cudaMemcpyDeviceToDevice,
-                          h->core.st));
+  const int64_t nc = h->core.g.ncell;
+  k_cell_pop<<<nblocks(nc, TPB), TPB, 0, h->core.st>>>(h->core.cellstart.as<int32_t>(), nc, cellpnum_dev);
+  GC_LAUNCHED();
   GC_CUDA(cudaStreamSynchronize(h->core.st));
   return GCSPH_OK;
 }

@@ -30,18 +30,22 @@ struct Grid {
 // the cell of point i (0-based linear key, x fastest): kernel_cellmap!'s
 // clamped ceil((x - offset) / cellsize), src/gpukernels_cls.jl:28-60
 template <int D>
-__device__ inline int32_t cell_key(const double* x0, const double* x1, const double* x2, int64_t i, const Grid& g) {
-  const double* xs[3] = {x0, x1, x2};
+__device__ inline int32_t cell_key_v(const double* xv, const Grid& g) {
   int64_t lin = 0, stride = 1;
 #pragma unroll
   for (int d = 0; d < D; ++d) {
-    const double p = (xs[d][i] - g.offset[d]) * g.hinv[d];
+    const double p = (xv[d] - g.offset[d]) * g.hinv[d];
     const double c = fmin(fmax(p, 1.0), (double)g.nc[d]);
     const int ci = (int)ceil(c);
     lin += (int64_t)(ci - 1) * stride;
     stride *= g.nc[d];
   }
   return (int32_t)lin;
+}
+template <int D>
+__device__ inline int32_t cell_key(const double* x0, const double* x1, const double* x2, int64_t i, const Grid& g) {
+  double xv[3] = {x0[i], x1[i], D == 3 ? x2[i] : 0.0};
+  return cell_key_v<D>(xv, g);
 }
 
 // The counting sort's last step for the point in arrival position q: its
@@ -124,6 +128,9 @@ struct CellCore {
   Grid g{};
   cudaStream_t st = 0;
 
+  // count (points per cell) is a binning's scratch and zero at rest: each
+  // binning zeroes it again once scanned; a cell's population is
+  // cellstart[c + 1] - cellstart[c]
   DevBuf count, cellstart, key, slot, tmp, perm, skey, orig, orig_b, cnt_full, cnt_up, rs_full, rs_up, nbr, scratch;
   DevBuf pf[3], pfmax;  // FP32 (x - offset) copies for the prefilter, and max |x - offset|
   DevBuf pfthr;         // the prefilter's two FP32 thresholds (float2), from pfmax once per build
@@ -157,7 +164,14 @@ struct CellCore {
   // rank_deferred (the counting sort's path only, where it is set true):
   // stop after the arrival lists; the caller ranks each point with
   // rank_in_cell in a pass of its own and then calls sort_done
-  int sort(const double* const* xin, const int32_t* ord, bool may_sync = false, bool* rank_deferred = nullptr);
+  // keys_ready: the cell keys, arrival slots and cell starts of xin were
+  // written by the step's last pass (small sets whose cell starts that pass
+  // scans, see keys_in_step), so the binning starts at the arrival lists
+  int sort(const double* const* xin, const int32_t* ord, bool may_sync = false, bool* rank_deferred = nullptr,
+           bool keys_ready = false);
+  // whether the next binning's keys may come from the step's last pass: a
+  // grid whose cell starts one block scans, and the counting sort's order
+  bool keys_in_step() const { return g.ncell + 1 <= SCAN_FOLD_MAX && N <= RADIX_MIN_N && sort_mode != 2; }
   // the bookkeeping after a binning into perm / skey / orig_b (orig_b becomes orig)
   void sort_done();
   int read_popmax();

@@ -229,18 +229,20 @@ __global__ void __launch_bounds__(32 * L) k_pairB1(StepConst c, const Scal* __re
   S.irh[k] = 1.0 / rv;
 }
 
-// pass B, stage 2: row sums + symplectic_update! + max |cΔx|
+// pass B, stage 2: row sums + symplectic_update! + max |cΔx|; with nb.key
+// also the next binning's keys, slots and (last block) cell starts
 template <int D, int L>
 __global__ void __launch_bounds__(32 * L) k_pairB2(StepConst c, Scal* __restrict__ sc, int64_t N, SArr<D> S,
-                                                   PairBuf B) {
-  if (*S.ovf) return;  // uniform over the grid, before the barrier below
+                                                   PairBuf B, NextBin nb) {
+  if (*S.ovf) return;  // uniform over the grid, before the barriers below
   __shared__ RowSums<D> R;
   pairB_sums<D, L>(S, B, N, R);
-  if (threadIdx.x >= 32) return;
+  const bool w0 = threadIdx.x < 32;
   const int64_t k = (int64_t)blockIdx.x * 32 + threadIdx.x;
+  if (!w0 && !nb.key) return;
   double mc = 0.0;
-  if (k < N) {
-    double a[D];
+  if (w0 && k < N) {
+    double a[D], xn[D];
 #pragma unroll
     for (int d = 0; d < D; ++d) a[d] = R.a[d][threadIdx.x];
     const double drho = R.drho[threadIdx.x];
@@ -271,22 +273,42 @@ __global__ void __launch_bounds__(32 * L) k_pairB2(StepConst c, Scal* __restrict
       const double xv = S.x[d][k] + ddx;
       S.xho[d][k] = xv;
       S.xo[d][k] = xv;
+      xn[d] = xv;
+    }
+    if (nb.key) {
+      const int32_t ck = cell_key_v<D>(xn, nb.g);
+      nb.key[k] = ck;
+      nb.slot[k] = atomicAdd(&nb.count[ck], 1);
     }
   }
-  mc = warp_max(mc);
-  __syncwarp();
-  if (threadIdx.x == 0) {
-    atomic_max_pos(&sc->maxcdx, mc);
-    if (c.fold_end) {
-      // the last block to finish ends the step (k_step_end's work); only
-      // warp 0 of each block writes step state, and its lane 0 signals here
-      __threadfence();
-      if (atomicAdd(&sc->bdone, 1u) == gridDim.x - 1) {
-        __threadfence();
+  if (w0) {
+    mc = warp_max(mc);
+    __syncwarp();
+    if (threadIdx.x == 0) atomic_max_pos(&sc->maxcdx, mc);
+  }
+  if (nb.key) {
+    // the whole block takes part: the last one ends the step (k_step_end's
+    // work) and scans the next binning's cell starts, then zeroes the counts
+    if (last_block_of_grid(&sc->bdone)) {
+      if (threadIdx.x == 0) {
         sc->maxcdx = atomicAdd(&sc->maxcdx, 0ull);  // every block's maximum, seen from here
         step_end_body(c, sc);
-        sc->bdone = 0u;
       }
+      block_exclusive_scan<int32_t>(nb.count, nb.cellstart, nb.g.ncell);
+      __syncthreads();
+      for (int64_t cc = threadIdx.x; cc < nb.g.ncell; cc += blockDim.x) nb.count[cc] = 0;
+    }
+    return;
+  }
+  if (threadIdx.x == 0 && c.fold_end) {
+    // the last block to finish ends the step (k_step_end's work); only warp
+    // 0 of each block writes step state, and its lane 0 signals here
+    __threadfence();
+    if (atomicAdd(&sc->bdone, 1u) == gridDim.x - 1) {
+      __threadfence();
+      sc->maxcdx = atomicAdd(&sc->maxcdx, 0ull);  // every block's maximum, seen from here
+      step_end_body(c, sc);
+      sc->bdone = 0u;
     }
   }
 }
@@ -318,13 +340,15 @@ int launch_pairA(int stage, cudaStream_t st, const StepConst& c, const SArr<D>& 
 
 template <int D>
 int launch_pairB(int stage, int L, int64_t N, cudaStream_t st, const StepConst& c, Scal* sc, const SArr<D>& S,
-                 const PairBuf& B) {
+                 const PairBuf& B, const NextBin* nb) {
   const int g = nblocks(N, 32);  // 32 particles per block, 32 L threads
+  NextBin none{};
+  const NextBin& nbv = nb ? *nb : none;
 #define GC_PAIRB(LL)                                                        \
   if (stage == 1)                                                          \
     k_pairB1<D, LL><<<g, 32 * LL, 0, st>>>(c, sc, N, S, B);                \
   else                                                                     \
-    k_pairB2<D, LL><<<g, 32 * LL, 0, st>>>(c, sc, N, S, B);
+    k_pairB2<D, LL><<<g, 32 * LL, 0, st>>>(c, sc, N, S, B, nbv);
   switch (L) {
     case 2: GC_PAIRB(2) break;
     case 4: GC_PAIRB(4) break;
@@ -340,8 +364,8 @@ int launch_pairB(int stage, int L, int64_t N, cudaStream_t st, const StepConst& 
 template int launch_pairA<2>(int, cudaStream_t, const StepConst&, const SArr<2>&, const PairBuf&);
 template int launch_pairA<3>(int, cudaStream_t, const StepConst&, const SArr<3>&, const PairBuf&);
 template int launch_pairB<2>(int, int, int64_t, cudaStream_t, const StepConst&, Scal*, const SArr<2>&,
-                             const PairBuf&);
+                             const PairBuf&, const NextBin*);
 template int launch_pairB<3>(int, int, int64_t, cudaStream_t, const StepConst&, Scal*, const SArr<3>&,
-                             const PairBuf&);
+                             const PairBuf&, const NextBin*);
 
 }  // namespace gcsph

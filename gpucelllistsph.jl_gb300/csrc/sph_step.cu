@@ -681,6 +681,7 @@ struct sph_handle {
   DevBuf scal;
   Scal* pin = nullptr;
   bool in_cell_order = false;
+  bool keys_ready = false;  // pass B2 wrote the next binning's keys (captured calls)
   bool use_graphs = true;
   int dt_relative = 0;
   StepGraph graphs[4];
@@ -878,7 +879,9 @@ static int rebuild(sph_handle* h, const StepConst& c, int* ovf_dev) {
     const double* xc[3] = {h->X[h->ix][0].as<double>(), h->X[h->ix][1].as<double>(),
                            D == 3 ? h->X[h->ix][2].as<double>() : nullptr};
     bool rank_deferred = false;
-    if ((rc = core.sort(xc, core.orig.as<int32_t>(), false, &rank_deferred))) return rc;
+    const bool keys_ready = h->keys_ready;
+    h->keys_ready = false;
+    if ((rc = core.sort(xc, core.orig.as<int32_t>(), false, &rank_deferred, keys_ready))) return rc;
     if ((rc = core.ensure_pf())) return rc;
     PermOut<D> alt = make_alt<D>(h);
     for (int d = 0; d < D; ++d) {
@@ -1013,7 +1016,9 @@ static int finish_call(sph_handle* h, const StepConst& c, Scal* dsc) {
 // Shared by the eager loop and the graph capture; only the host-side buffer
 // indices change here, in an order fixed by the parameters.
 template <int D>
-static int enqueue_stages(sph_handle* h, StepConst& c, Scal* dsc, int32_t& cspmcnt) {
+// next_bins: update! starts the next step (captured calls): pass B2 may
+// start its binning (NextBin)
+static int enqueue_stages(sph_handle* h, StepConst& c, Scal* dsc, int32_t& cspmcnt, bool next_bins) {
   CellCore& core = h->cl->core;
   cudaStream_t st = core.st;
   const gcsph_params& p = h->prm;
@@ -1052,7 +1057,18 @@ static int enqueue_stages(sph_handle* h, StepConst& c, Scal* dsc, int32_t& cspmc
     // last block does k_step_end's work
     StepConst c2 = c;
     c2.fold_end = c.timestepping ? 0 : 1;
-    PAIRB_LAUNCH(2, L, c2, dsc, make_arr<D>(h), make_pairbuf<D>(h));
+    // the next binning's keys from the new positions, where nothing after
+    // pass B2 moves the particles (no DPC, no XSPH) and its last block ends the step
+    NextBin nb{};
+    if (next_bins && c2.fold_end && !(p.dpc_l0 > 0) && !(p.xsph_eps > 0) && core.keys_in_step()) {
+      nb.key = core.key.as<int32_t>();
+      nb.slot = core.slot.as<int32_t>();
+      nb.count = core.count.as<int32_t>();
+      nb.cellstart = core.cellstart.as<int32_t>();
+      nb.g = core.g;
+      h->keys_ready = true;
+    }
+    PAIRB_LAUNCH(2, L, c2, dsc, make_arr<D>(h), make_pairbuf<D>(h), &nb);
     folded = c2.fold_end != 0;
     timer_end(T_ROWSUM, st);
   } else {
@@ -1126,6 +1142,7 @@ static int step_eager(sph_handle* h, StepConst c, int32_t n, int64_t* updaten_ou
   int32_t cspmcnt = 0;
   int rc;
   c.count_reb = 0;
+  h->keys_ready = false;  // the eager loop bins every step itself
   for (int32_t it = 0; it < n; ++it) {
     const int32_t cspm_before = cspmcnt;
     // per-step device scalars: max|cΔx|, the Δt maxima and the overflow flag
@@ -1136,7 +1153,7 @@ static int step_eager(sph_handle* h, StepConst c, int32_t n, int64_t* updaten_ou
       updaten += 1;
     }
     const int saved[6] = {h->ix, h->ixh, h->iv, h->ivh, h->irho, h->irhoh};
-    if ((rc = enqueue_stages<D>(h, c, dsc, cspmcnt))) return rc;
+    if ((rc = enqueue_stages<D>(h, c, dsc, cspmcnt, false))) return rc;
     GC_CUDA(cudaMemcpyAsync(h->pin, dsc, sizeof(Scal), cudaMemcpyDeviceToHost, st));
     GC_CUDA(cudaStreamSynchronize(st));
     timer_collect();
@@ -1290,12 +1307,14 @@ static int graph_capture(sph_handle* h, StepConst c, int32_t n, StepGraph& g) {
   // each replay) and each step's end clears them for the next; the overflow
   // flag stays set once raised
   c.reset_max = 1;
+  h->keys_ready = false;
   for (int32_t it = 0; it < n && rc == GCSPH_OK; ++it) {
     c.count_reb = it + 1 < n;
     if ((rc = rebuild<D>(h, c, &dsc->ovf))) break;
-    rc = enqueue_stages<D>(h, c, dsc, cspmcnt);
+    rc = enqueue_stages<D>(h, c, dsc, cspmcnt, it + 1 < n);
   }
   if (rc == GCSPH_OK) rc = finish_call<D>(h, c, dsc);
+  h->keys_ready = false;
   timer_capture_to(nullptr);
   core.st = run_st;
   cudaGraph_t graph = nullptr;

@@ -470,8 +470,19 @@ __device__ inline void row_sums(const SArr<D>& S, const PairBuf& B, int64_t k, i
 // per particle, 32 particles per block
 template <int D>
 int launch_pairA(int stage, cudaStream_t st, const StepConst& c, const SArr<D>& S, const PairBuf& B);
+// The next step's binning started by pass B2 (update! every step): each
+// particle's cell key and arrival slot from its new position, and, in the
+// last block, the cell starts (CellCore::sort with keys_ready goes on from
+// there).  key == nullptr: none.
+struct NextBin {
+  int32_t* key;
+  int32_t* slot;
+  int32_t* count;      // zero on entry, zero again on exit
+  int32_t* cellstart;
+  Grid g;
+};
 template <int D>
 int launch_pairB(int stage, int L, int64_t N, cudaStream_t st, const StepConst& c, Scal* sc, const SArr<D>& S,
-                 const PairBuf& B);
+                 const PairBuf& B, const NextBin* nb = nullptr);
 
 }  // namespace gcsph
