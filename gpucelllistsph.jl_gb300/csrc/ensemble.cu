@@ -35,6 +35,14 @@ constexpr int ENS_MAX_TPB = 512;
 
 // per-instance constants (device table, indexed by packing position)
 struct EnsInst {
+  // the stage passes' per-entry constants in 16-byte groups, so that a
+  // branch loads the group it needs with one vector load
+  float4 kA;      // H², 1/H, dwc, cell edge
+  float4 kB;      // ρ₀, η², m₀, DDTgz
+  float4 kC;      // kddt, kav, kvisc, P₀
+  float4 kD;      // pfcr, hp1, 2h, kpf
+  float4 kE;      // pc[0..3]
+  float4 kFB[2];  // fb_d, fb_r0, fb_eta2, 1/ρ₀ of stage 1 and stage 2
   double origin[3];
   double csinv;  // 1 / cell edge
   double cs;
@@ -53,6 +61,11 @@ struct EnsInst {
   float rho0inv, m0inv;                  // 1/ρ₀, 1/m₀
   float dwc;                             // -20 nDW / H: W'(r)/r = dwc (1 - r/H)^3
   float pfcr;                            // 1.5π / 2h: the cosine's argument per unit r in ∂v∂tpF!
+  // products of the above that the stage passes use as one factor
+  float kddt;                            // DDTkh m₀ (∂ρ∂tDDT!)
+  float kav;                             // 2 α c₀ h m₀ (∂v∂t_av!: -Π m₀ / ((Δv·Δx) / ((r² + η²)(ρi + ρj))))
+  float kvisc;                           // 4 ν m₀ (∂v∂t_visc!)
+  float kpf;                             // s / m₀ (∂v∂tpF!)
   int p_off;                             // first particle of the instance (list entries are instance-local)
   int reuse;                             // the list is kept while the particles stay within the skin
   float LR2;                             // list radius², (H (1 + skin))² = cell edge²
@@ -194,6 +207,27 @@ struct KSum {
   }
 };
 
+// Kahan sums of the x and y components in packed FP32 pairs (sm_100's
+// two-wide FADD/FFMA): the compensation is kept negated, nc = -c, so that
+// every step is an add or a fused multiply-add by -1 -- y = x + nc,
+// t = s + y, nc = (s - t) + y -- bit for bit the scalar KSum on each lane
+struct KSum2 {
+  float2 s = make_float2(0.f, 0.f), nc = make_float2(0.f, 0.f);
+  __device__ __forceinline__ void add(float2 x) {
+    const float2 m1 = make_float2(-1.f, -1.f);
+    const float2 y = __fadd2_rn(x, nc);
+    const float2 t = __fadd2_rn(s, y);
+    nc = __fadd2_rn(__ffma2_rn(t, m1, s), y);
+    s = t;
+  }
+  __device__ __forceinline__ KSum part(int q) const {
+    KSum k;
+    k.s = q == 0 ? s.x : s.y;
+    k.c = q == 0 ? -nc.x : -nc.y;
+    return k;
+  }
+};
+
 // √x for x >= 0 by the approximate reciprocal root (within a few ulp); 0 at 0
 __device__ __forceinline__ float sqrt_fast(float x) { return x > 0.f ? x * rsqrtf(x) : 0.f; }
 
@@ -206,21 +240,26 @@ __device__ __forceinline__ float dot32(const float* a, const float* b) {
 }
 
 // P0 ((1+e)^γ - 1), e = δρ/ρ₀, without cancellation (pressure(), src/gpukernels_sph.jl:691-697)
-__device__ __forceinline__ float eos32(float dr, int pt, const EnsInst& I) {
+__device__ __forceinline__ float eos32g(float dr, int pt, float rho0inv, float P0, int gamma) {
   if (pt <= 1 && dr < 0.f) return 0.f;
-  const float e = dr * I.rho0inv;
+  const float e = dr * rho0inv;
   float p;
-  if (I.gamma == 7)
+  if (gamma == 7)
     p = e * (7.f + e * (21.f + e * (35.f + e * (35.f + e * (21.f + e * (7.f + e))))));
   else
-    p = expm1f((float)I.gamma * log1pf(e));
-  return I.P0 * p;
+    p = expm1f((float)gamma * log1pf(e));
+  return P0 * p;
+}
+__device__ __forceinline__ float eos32(float dr, int pt, const EnsInst& I) {
+  return eos32g(dr, pt, I.rho0inv, I.P0, I.gamma);
 }
 
-// (1+ε)^(1/γ) - 1 (powfancy7th(1+ε) - 1, src/gpukernels_sph.jl:499-515)
-__device__ __forceinline__ float root_m1(float eps, const EnsInst& I) {
-  if (fabsf(eps) < 0.01f) return eps * (I.pc[0] + eps * (I.pc[1] + eps * (I.pc[2] + eps * I.pc[3])));
-  return powf(1.f + eps, 1.f / (float)I.gamma) - 1.f;
+
+// (1+ε)^(1/γ) - 1 (powfancy7th(1+ε) - 1, src/gpukernels_sph.jl:499-515), from
+// the series coefficients pc
+__device__ __forceinline__ float root_m1g(float eps, const float4& pc, int gamma) {
+  if (fabsf(eps) < 0.01f) return eps * (pc.x + eps * (pc.y + eps * (pc.z + eps * pc.w)));
+  return powf(1.f + eps, 1.f / (float)gamma) - 1.f;
 }
 
 __device__ __forceinline__ void cell_of(int key, const EnsInst& I, int& c0, int& c1, int& c2) {
@@ -357,10 +396,17 @@ __device__ __forceinline__ int ent_code(int dxc, int dy, int dz) {
 __device__ __forceinline__ int ent_make(int j_local, int code) { return (int)(((unsigned)j_local << 6) | code); }
 __device__ __forceinline__ int ent_index(int ent) { return (int)((unsigned)ent >> 6); }
 
-__device__ __forceinline__ void shift_of(int ent, const EnsInst& I, float& sx, float& sy, float& sz) {
-  sx = (float)((ent & 3) - 1) * I.csf;
-  sy = (float)(((ent >> 2) & 3) - 1) * I.csf;
-  sz = (float)(((ent >> 4) & 3) - 1) * I.csf;
+// An entry's cell shift per axis, field - 1 in {-1, 0, 1}, as floats.  Each
+// 2-bit field is OR-ed into the low mantissa bits of 1.5 * 2^23
+// (0x4B400000), where it reads as 12582912 + field exactly, and one
+// subtraction leaves field - 1; the separation then takes the shift times
+// the cell edge in one fused multiply-add.
+template <int D>
+__device__ __forceinline__ void ent_shift(int ent, float* s) {
+  const unsigned u = (unsigned)ent;
+  s[0] = __uint_as_float((u & 3u) | 0x4B400000u) - 12582913.f;
+  s[1] = __uint_as_float(((u >> 2) & 3u) | 0x4B400000u) - 12582913.f;
+  if (D == 3) s[D - 1] = __uint_as_float(((u >> 4) & 3u) | 0x4B400000u) - 12582913.f;
 }
 
 // a candidate's decision: with L lanes on a particle, a ballot keeps the hits
@@ -698,7 +744,9 @@ __global__ void __launch_bounds__(ENS_MAX_TPB, 2) k_ens_stage(EnsArr A, const En
     const float irhoi = __fdividef(1.f, rhoi);
     const float Pi = eos32(dri, pti, I);
     const int fbs = STAGE - 1;
-    KSum drho, acc[D];
+    KSum drho;
+    KSum2 accxy;  // the x and y components of the acceleration, packed
+    KSum accz;
     float rm2 = INFINITY;  // stage 1: the row's smallest r² (dpcreg!'s row bound)
     const int nn = A.nlc[i];
     // the next entry is loaded one iteration ahead: the list streams from
@@ -708,95 +756,101 @@ __global__ void __launch_bounds__(ENS_MAX_TPB, 2) k_ens_stage(EnsArr A, const En
       const int ent = nxt;
       if (e + L < nn) nxt = A.nl[(int64_t)(e + L) * A.ncap + i];
       const Rec<D, STAGE> rec = load_rec<D, STAGE>(A.r1, A.r2, I.p_off + ent_index(ent));
-      float shx, shy, shz;
-      shift_of(ent, I, shx, shy, shz);
+      float sh[D];
+      ent_shift<D>(ent, sh);
       // the neighbour's record: offsets (at x, and at xΔt½ in stage 2), velocity, δρ, ptype
       float oj[D], hj[D], vj[D], drj, Prec = 0.f;
       int ptj;
       decode_rec<D, STAGE>(rec, oj, hj, vj, drj, ptj, Prec);
+      const float4 kA = I.kA;  // H², 1/H, dwc, cell edge
       float d[D];
 #pragma unroll
-      for (int q = 0; q < D; ++q) d[q] = (oi[q] - oj[q]) - (q == 0 ? shx : (q == 1 ? shy : shz));
+      for (int q = 0; q < D; ++q) d[q] = fmaf(-sh[q], kA.w, oi[q] - oj[q]);
       const float r2 = dot32<D>(d, d);
       if (STAGE == 1 && RM) rm2 = fminf(rm2, r2);
-      if (!(r2 < I.H2)) continue;  // in the list's skin: not a pair of this step
+      if (!(r2 < kA.x)) continue;  // in the list's skin: not a pair of this step
       // sph∇W!: W'(r)/r of WendlandC2 = -20 nDW Hinv (1-q)^3.  Reciprocals and
       // roots here are the approximate intrinsics (within 2 ulp each), far
       // inside the FP32 path's error against FP64.
       const float r = r2 > 0.f ? r2 * rsqrtf(r2) : 0.f;
-      const float u = r * I.Hinv;
+      const float u = r * kA.y;
       const float t = u < 1.f ? 1.f - u : 0.f;
-      const float dwr = I.dwc * (t * t * t);
+      const float dwr = kA.z * (t * t * t);
       float gw[D], dd[D], dv[D];
 #pragma unroll
       for (int q = 0; q < D; ++q) {
         gw[q] = d[q] * dwr;
-        dd[q] = STAGE == 1 ? d[q] : (ohi[q] - hj[q]) - (q == 0 ? shx : (q == 1 ? shy : shz));
+        dd[q] = STAGE == 1 ? d[q] : fmaf(-sh[q], kA.w, ohi[q] - hj[q]);
         dv[q] = vi[q] - vj[q];
       }
+      const float4 kB = I.kB;  // ρ₀, η², m₀, DDTgz
       const float r2d = STAGE == 1 ? r2 : dot32<D>(dd, dd);
-      const float rhoj = I.rho0 + drj;
+      const float rhoj = kB.x + drj;
       const float irhoj = __fdividef(1.f, rhoj);
       const bool both = pti > 0 && ptj > 0;
-      const float inv = __fdividef(1.f, r2d + I.eta2);
-      float f[D];
+      const float inv = __fdividef(1.f, r2d + kB.y);
+      // gsc: the factor of ∇W of ∂v∂t! and ∂v∂t_av! together; f: the
+      // viscous, surface-tension and boundary terms
+      float gsc = 0.f, f[D];
 #pragma unroll
       for (int q = 0; q < D; ++q) f[q] = 0.f;
-      if (both) {
-        // ∂ρ∂tDDT!
-        float term = I.m0 * dot32<D>(dv, gw);
-        if (pti > 1) {
-          const float dp = I.rho0 * root_m1(I.DDTgz * dd[1], I);
-          term += I.DDTkh * ((drj - dri) - dp) * inv * (-dot32<D>(dd, gw)) * I.m0 * irhoj;
-        }
-        drho.add(term);
-      }
       if (pti * ptj > 0) {
         // ∂v∂t!
-        const float Pj = rec_has_p<D, STAGE>() ? Prec : eos32(drj, ptj, I);
-        const float sc = -I.m0 * (Pi + Pj) * (irhoi * irhoj);
-#pragma unroll
-        for (int q = 0; q < D; ++q) f[q] = sc * gw[q];
+        float Pj = Prec;
+        if (!rec_has_p<D, STAGE>()) Pj = eos32g(drj, ptj, I.kFB[0].w, I.kC.w, I.gamma);
+        gsc = -kB.z * (Pi + Pj) * (irhoi * irhoj);
       }
       if (both) {
+        const float4 kC = I.kC;  // kddt, kav, kvisc
+        const float ddgw = dot32<D>(dd, gw);
+        // ∂ρ∂tDDT!
+        float term = kB.z * dot32<D>(dv, gw);
+        if (pti > 1) {
+          const float dp = kB.x * root_m1g(kB.w * dd[1], I.kE, I.gamma);
+          term += kC.x * ((drj - dri) - dp) * inv * (-ddgw) * irhoj;
+        }
+        drho.add(term);
         const float cond = dot32<D>(dv, dd);
         if (cond < 0.f || I.use_visc) {
-          const float isum = __fdividef(1.f, rhoi + rhoj);
-          if (cond < 0.f) {
-            // ∂v∂t_av!
-            const float dmu = I.h * cond * inv;
-            const float dPi = (-I.alpha * I.c0 * dmu) * (2.f * isum);
-#pragma unroll
-            for (int q = 0; q < D; ++q) f[q] += -dPi * I.m0 * gw[q];
-          }
+          const float ii = __fdividef(1.f, rhoi + rhoj) * inv;
+          // ∂v∂t_av!: -Π m₀ = 2 α c₀ h m₀ (Δv·Δx) / ((r² + η²)(ρi + ρj))
+          if (cond < 0.f) gsc += kC.y * cond * ii;
           if (I.use_visc) {
             // ∂v∂t_visc!
-            const float nt = 4.f * I.nu * I.m0 * dot32<D>(dd, gw) * isum * inv;
+            const float nt = kC.z * ddgw * ii;
 #pragma unroll
-            for (int q = 0; q < D; ++q) f[q] += nt * dv[q];
+            for (int q = 0; q < D; ++q) f[q] = nt * dv[q];
           }
         }
         if (I.use_pF) {
-          // ∂v∂tpF!
-          const float rd = r2d > 0.f ? r2d * rsqrtf(r2d) : 0.f;
-          if (rd < I.twoh) {
-            const float scos = I.s * __cosf(I.pfcr * rd) * __fdividef(1.f, rd + I.hp1);  // argument in [0, 1.5π)
+          // ∂v∂tpF! (in stage 1 the separation is r itself)
+          const float4 kD = I.kD;  // pfcr, hp1, 2h, kpf
+          const float rd = STAGE == 1 ? r : (r2d > 0.f ? r2d * rsqrtf(r2d) : 0.f);
+          if (rd < kD.z) {
+            const float scos = kD.w * __cosf(kD.x * rd) * __fdividef(1.f, rd + kD.y);  // argument in [0, 1.5π)
 #pragma unroll
-            for (int q = 0; q < D; ++q) f[q] += scos * dd[q] * I.m0inv;
+            for (int q = 0; q < D; ++q) f[q] = fmaf(scos, dd[q], f[q]);
           }
         }
       }
-      if ((pti > 0) != (ptj > 0) && r < I.fb_r0[fbs]) {
-        // fbmolforce! at x
-        const float qq = I.fb_r0[fbs] * __fdividef(1.f, r + I.fb_eta2[fbs]);
-        const float q2 = qq * qq, q4 = q2 * q2, q8 = q4 * q4;
-        const float Fc = I.fb_d[fbs] * (q8 * q4 - q4) * __fdividef(1.f, r2 + I.fb_eta2[fbs]);
+      if ((pti > 0) != (ptj > 0)) {
+        const float4 kF = I.kFB[fbs];  // fb_d, fb_r0, fb_eta2
+        if (r < kF.y) {
+          // fbmolforce! at x
+          const float qq = kF.y * __fdividef(1.f, r + kF.z);
+          const float q2 = qq * qq, q4 = q2 * q2, q8 = q4 * q4;
+          const float Fc = kF.x * (q8 * q4 - q4) * __fdividef(1.f, r2 + kF.z);
 #pragma unroll
-        for (int q = 0; q < D; ++q) f[q] += d[q] * Fc;
+          for (int q = 0; q < D; ++q) f[q] += d[q] * Fc;
+        }
       }
-#pragma unroll
-      for (int q = 0; q < D; ++q) acc[q].add(f[q]);
+      accxy.add(make_float2(fmaf(gsc, gw[0], f[0]), fmaf(gsc, gw[1], f[1])));
+      if (D == 3) accz.add(fmaf(gsc, gw[D - 1], f[D - 1]));
     }
+    KSum acc[D];
+    acc[0] = accxy.part(0);
+    acc[1] = accxy.part(1);
+    if (D == 3) acc[D - 1] = accz;
     float a[D];
 #pragma unroll
     for (int q = 0; q < D; ++q) a[q] = lane_total<L>(acc[q], gm) - (q == 1 ? I.g : 0.f);
@@ -902,12 +956,12 @@ __global__ void __launch_bounds__(ENS_MAX_TPB) k_ens_dpc(EnsArr A, const EnsInst
         // the offsets; beyond l0 (u >= 1) W, χ and Pᵇ vanish and so does the
         // pair's dpcreg! term, so the rest is read only within l0
         const float4 ra = __ldg(A.r3 + 2 * (int64_t)j);
-        float shx, shy, shz;
-        shift_of(ent, I, shx, shy, shz);
+        float sh[D];
+        ent_shift<D>(ent, sh);
         const float onj[3] = {ra.x, ra.y, D == 3 ? ra.z : 0.f};
         float dx[D];
 #pragma unroll
-        for (int q = 0; q < D; ++q) dx[q] = (ni[q] - onj[q]) - (q == 0 ? shx : (q == 1 ? shy : shz));
+        for (int q = 0; q < D; ++q) dx[q] = fmaf(-sh[q], I.csf, ni[q] - onj[q]);
         const float r2 = dot32<D>(dx, dx);
         const float u = sqrt_fast(r2) * I.dpc_l0inv;
         if (!(u < 1.f)) continue;
@@ -922,7 +976,7 @@ __global__ void __launch_bounds__(ENS_MAX_TPB) k_ens_dpc(EnsArr A, const EnsInst
           const float oj[3] = {sj.x, sj.y, sj.z};
           float dm[D];
 #pragma unroll
-          for (int q = 0; q < D; ++q) dm[q] = (A.off[q][i] - oj[q]) - (q == 0 ? shx : (q == 1 ? shy : shz));
+          for (int q = 0; q < D; ++q) dm[q] = fmaf(-sh[q], I.csf, A.off[q][i] - oj[q]);
           if (!(dot32<D>(dm, dm) < I.H2)) continue;
         }
         float dv[D];
@@ -1002,11 +1056,11 @@ __global__ void __launch_bounds__(ENS_MAX_TPB, 3) k_ens_xsph(EnsArr A, const Ens
       int ptj;
       decode_rec<D, 1>(load_rec<D, 1>(A.r4, nullptr, j), oj, hj, vj, drj, ptj, pu);
       if (!(ptj > 1)) continue;
-      float shx, shy, shz;
-      shift_of(ent, I, shx, shy, shz);
+      float sh[D];
+      ent_shift<D>(ent, sh);
       float d[D];
 #pragma unroll
-      for (int q = 0; q < D; ++q) d[q] = (oi[q] - oj[q]) - (q == 0 ? shx : (q == 1 ? shy : shz));
+      for (int q = 0; q < D; ++q) d[q] = fmaf(-sh[q], I.csf, oi[q] - oj[q]);
       const float r2 = dot32<D>(d, d);
       if (!(r2 < I.H2)) continue;  // in the list's skin
       const float u = sqrt_fast(r2) * I.Hinv;
@@ -1062,11 +1116,11 @@ __global__ void __launch_bounds__(ENS_MAX_TPB) k_ens_cspm(EnsArr A, const EnsIns
       int ptj;
       decode_rec<D, 1>(load_rec<D, 1>(A.r4, nullptr, j), oj, hj, vj, drj, ptj, pu);
       if (!(ptj > 0)) continue;
-      float shx, shy, shz;
-      shift_of(ent, I, shx, shy, shz);
+      float sh[D];
+      ent_shift<D>(ent, sh);
       float d[D];
 #pragma unroll
-      for (int q = 0; q < D; ++q) d[q] = (oi[q] - oj[q]) - (q == 0 ? shx : (q == 1 ? shy : shz));
+      for (int q = 0; q < D; ++q) d[q] = fmaf(-sh[q], I.csf, oi[q] - oj[q]);
       const float r2 = dot32<D>(d, d);
       if (!(r2 < I.H2)) continue;  // in the list's skin
       const float u = sqrt_fast(r2) * I.Hinv;
@@ -2144,6 +2198,16 @@ int ens_add(gcsph_ens* e, int64_t n, const double* x, const double* v, const dou
   I.m0inv = (float)(1.0 / p->m0);
   I.dwc = (float)(-20.0 * (D == 2 ? wc2_norm_dw<2>(1.0 / p->H) : wc2_norm_dw<3>(1.0 / p->H)) / p->H);
   I.pfcr = (float)(1.5 * GCSPH_PI64 / (2.0 * p->h));
+  I.kddt = (float)(2.0 * p->h * p->delta * p->c0 * p->m0);
+  I.kav = (float)(2.0 * p->alpha * p->c0 * p->h * p->m0);
+  I.kvisc = (float)(4.0 * p->nu * p->m0);
+  I.kpf = (float)(p->s / p->m0);
+  I.kA = make_float4(I.H2, I.Hinv, I.dwc, I.csf);
+  I.kB = make_float4(I.rho0, I.eta2, I.m0, I.DDTgz);
+  I.kC = make_float4(I.kddt, I.kav, I.kvisc, I.P0);
+  I.kD = make_float4(I.pfcr, I.hp1, I.twoh, I.kpf);
+  I.kE = make_float4(I.pc[0], I.pc[1], I.pc[2], I.pc[3]);
+  for (int st = 0; st < 2; ++st) I.kFB[st] = make_float4(I.fb_d[st], I.fb_r0[st], I.fb_eta2[st], I.rho0inv);
   // host staging in the engine's types
   std::vector<float> vf((size_t)D * n, 0.f), drf((size_t)n);
   std::vector<int32_t> ids((size_t)n);
