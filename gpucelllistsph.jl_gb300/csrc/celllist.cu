@@ -127,11 +127,16 @@ __global__ void k_cellkey(const double* __restrict__ x0, const double* __restric
   }
 }
 
+// the arrival lists: point i at its cell's start plus its arrival slot; with
+// tord also its order value (ord[i], or i), for rank_in_cell
 __global__ void k_scatter_arrival(const int32_t* __restrict__ key, const int32_t* __restrict__ slot,
-                                  const int32_t* __restrict__ cellstart, int64_t N, int32_t* __restrict__ tmp) {
+                                  const int32_t* __restrict__ cellstart, int64_t N, int32_t* __restrict__ tmp,
+                                  const int32_t* __restrict__ ord = nullptr, int32_t* __restrict__ tord = nullptr) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= N) return;
-  tmp[cellstart[key[i]] + slot[i]] = (int32_t)i;
+  const int32_t pos = cellstart[key[i]] + slot[i];
+  tmp[pos] = (int32_t)i;
+  if (tord) tord[pos] = ord ? ord[i] : (int32_t)i;
 }
 
 // rank of each cell member by original index: stable, history-free order.
@@ -160,10 +165,11 @@ __global__ void k_rank_in_cell(const int32_t* __restrict__ tmp, const int32_t* _
 // k_apply_perm, without the second launch)
 __global__ void k_rank_apply(const int32_t* __restrict__ tmp, const int32_t* __restrict__ key,
                              const int32_t* __restrict__ cellstart, const int32_t* __restrict__ ord, int64_t N,
-                             int32_t* __restrict__ perm, int32_t* __restrict__ skey, int32_t* __restrict__ orig) {
+                             int32_t* __restrict__ perm, int32_t* __restrict__ skey, int32_t* __restrict__ orig,
+                             const int32_t* __restrict__ tord) {
   int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= N) return;
-  rank_in_cell(tmp, key, cellstart, ord, q, perm, skey, orig);
+  rank_in_cell(tmp, key, cellstart, ord, q, perm, skey, orig, nullptr, tord);
 }
 
 __global__ void k_apply_perm(const int32_t* __restrict__ perm, const int32_t* __restrict__ key,
@@ -483,6 +489,7 @@ int CellCore::init(int D_, int64_t N_, const double* cellsize, double dist_, con
   if ((rc = key.ensure(sizeof(int32_t) * N, st))) return rc;
   if ((rc = slot.ensure(sizeof(int32_t) * N, st))) return rc;
   if ((rc = tmp.ensure(sizeof(int32_t) * N, st))) return rc;
+  if ((rc = tord.ensure(sizeof(int32_t) * N, st))) return rc;
   if ((rc = perm.ensure(sizeof(int32_t) * N, st))) return rc;
   if ((rc = skey.ensure(sizeof(int32_t) * N, st))) return rc;
   // the spare original-index map every binning writes into (then swapped in)
@@ -514,7 +521,7 @@ int CellCore::init(int D_, int64_t N_, const double* cellsize, double dist_, con
 }
 
 void CellCore::release() {
-  DevBuf* all[] = {&count, &cellstart, &key, &slot, &tmp, &perm, &skey, &orig, &cnt_full, &cnt_up, &rs_full,
+  DevBuf* all[] = {&count, &cellstart, &key, &slot, &tmp, &tord, &perm, &skey, &orig, &cnt_full, &cnt_up, &rs_full,
                    &rs_up, &nbr, &scratch, &pf[0], &pf[1], &pf[2], &pfmax, &pfthr, &pfcnt, &orig_b, &stage,
                    &foldcnt, &foldsum, &rkey[0], &rkey[1], &rval[0], &rval[1], &rhist, &rhoff, &popmax};
   for (DevBuf* b : all) b->release();
@@ -599,7 +606,7 @@ int CellCore::sort(const double* const* xin, const int32_t* ord, bool may_sync, 
     // small sets: 64-thread blocks, so these latency-bound passes spread over more SMs
     const int tb = N <= RADIX_MIN_N ? 64 : TPB;
     k_scatter_arrival<<<nblocks(N, tb), tb, 0, st>>>(key.as<int32_t>(), slot.as<int32_t>(), cellstart.as<int32_t>(),
-                                                      N, tmp.as<int32_t>());
+                                                      N, tmp.as<int32_t>(), ord, tord.as<int32_t>());
     GC_LAUNCHED();
     if (rank_deferred) {
       // the caller ranks (rank_in_cell) and applies the order in its own pass
@@ -608,7 +615,8 @@ int CellCore::sort(const double* const* xin, const int32_t* ord, bool may_sync, 
       return GCSPH_OK;
     }
     k_rank_apply<<<nblocks(N, tb), tb, 0, st>>>(tmp.as<int32_t>(), key.as<int32_t>(), cellstart.as<int32_t>(), ord, N,
-                                                 perm.as<int32_t>(), skey.as<int32_t>(), orig_b.as<int32_t>());
+                                                 perm.as<int32_t>(), skey.as<int32_t>(), orig_b.as<int32_t>(),
+                                                 tord.as<int32_t>());
     GC_LAUNCHED();
   }
   sort_done();

@@ -52,19 +52,30 @@ __device__ inline int32_t cell_key(const double* x0, const double* x1, const dou
 // rank among its cell's points by original index (a stable, history-free
 // order; cost: the cell's population), and so its slot k in cell order,
 // where the map entries go.  Returns k; *i_out is the point's input index.
+// With tord (the order value of each arrival-list entry, written beside tmp)
+// the cell's values are one contiguous run, read without a second, dependent
+// load per member.
 __device__ inline int64_t rank_in_cell(const int32_t* __restrict__ tmp, const int32_t* __restrict__ key,
                                        const int32_t* __restrict__ cellstart, const int32_t* __restrict__ ord,
                                        int64_t q, int32_t* __restrict__ perm, int32_t* __restrict__ skey,
-                                       int32_t* __restrict__ orig, int32_t* i_out = nullptr) {
+                                       int32_t* __restrict__ orig, int32_t* i_out = nullptr,
+                                       const int32_t* __restrict__ tord = nullptr) {
   const int32_t i = tmp[q];
   const int32_t c = key[i];
   const int32_t s = cellstart[c], e = cellstart[c + 1];
-  const int32_t oi = ord ? ord[i] : i;
   int32_t r = 0;
-  for (int32_t t = s; t < e; ++t) {
-    const int32_t j = tmp[t];
-    const int32_t oj = ord ? ord[j] : j;
-    r += (oj < oi);
+  int32_t oi;
+  if (tord) {
+    oi = tord[q];
+#pragma unroll 4
+    for (int32_t t = s; t < e; ++t) r += (tord[t] < oi);
+  } else {
+    oi = ord ? ord[i] : i;
+    for (int32_t t = s; t < e; ++t) {
+      const int32_t j = tmp[t];
+      const int32_t oj = ord ? ord[j] : j;
+      r += (oj < oi);
+    }
   }
   perm[s + r] = i;
   skey[s + r] = c;
@@ -132,6 +143,7 @@ struct CellCore {
   // binning zeroes it again once scanned; a cell's population is
   // cellstart[c + 1] - cellstart[c]
   DevBuf count, cellstart, key, slot, tmp, perm, skey, orig, orig_b, cnt_full, cnt_up, rs_full, rs_up, nbr, scratch;
+  DevBuf tord;          // the arrival lists' order values (ord of each tmp entry): the rank reads one array
   DevBuf pf[3], pfmax;  // FP32 (x - offset) copies for the prefilter, and max |x - offset|
   DevBuf pfthr;         // the prefilter's two FP32 thresholds (float2), from pfmax once per build
   DevBuf pfcnt;         // blocks done of the pass that accumulates pfmax (its last block writes pfthr)

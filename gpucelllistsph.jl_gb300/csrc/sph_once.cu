@@ -22,7 +22,7 @@ __device__ inline void fb_pair(const StepConst& c, const double* dx, double r2, 
 }
 
 // Pass A: one thread per pair (k, m), k < m in cell order.  Stage 1 at
-// (x, ρ, v, P(ρ)) also writes W and ∇W; stage 2 at (xΔt½, ρΔt½, vΔt½,
+// (x, ρ, v, P(ρ)) also writes ∇W, and W in the steps that read it; stage 2 at (xΔt½, ρΔt½, vΔt½,
 // P(ρΔt½)) with the stage-1 ∇W and fbmolforce! at x.  The reference's terms,
 // src/gpukernels_sph.jl, in their algebraically equal pair-once forms:
 //  * ∇W = Δx d𝒲/r with d𝒲/r = dWr (1 - u)^3 -- no division by r;
@@ -69,17 +69,21 @@ __device__ __forceinline__ void pairA_one(const StepConst& c, const SArr<D>& S, 
     if (dbits(uu) < ONE_BITS) {
       const double t = 1.0 - uu;
       const double t2 = t * t;
-      w = ((1.0 + 4.0 * uu) * (t2 * t2)) * c.nW;
+      if (c.need_w) w = ((1.0 + 4.0 * uu) * (t2 * t2)) * c.nW;
       dwr = (t2 * t) * c.dWr;
     }
     if (!r2pos) dwr = NAN;  // the reference's d𝒲(0)/0
-    S.We[e] = w;
-    S.We[me] = w;
+    if (c.need_w) {
+      // both rows' slots: xsphcorr! and cspmcorr! walk every row
+      S.We[e] = w;
+      S.We[me] = w;
+    }
+    // stage 2 reads ∇W from the pair's k-side slot only (the call's ∑∇W is
+    // recomputed from the positions at its end)
 #pragma unroll
     for (int d = 0; d < D; ++d) {
       gw[d] = dx[d] * dwr;
       S.gWe[d][e] = gw[d];
-      S.gWe[d][me] = -gw[d];
     }
   } else {
     if (c.use_pF && r2pos) r = sqrt_nr(r2);

@@ -529,38 +529,63 @@ struct PermOut {
   double dist2;
 };
 
-// new[k] = old[i] for the whole cell-order state of one particle; cΔx
-// restarts at 0 (src/sphproblem.jl:229), P(ρ) and 1/ρ are recomputed for
-// stage 1; b takes the max |x - offset| of the FP32 prefilter copy
+// the cell-order state of one particle that a re-sort moves
 template <int D>
-__device__ __forceinline__ void permute_one(const StepConst& c, const SArr<D>& S, const PermOut<D>& O, int64_t i,
-                                            int64_t k, double& b) {
+struct PermVals {
+  double x[D], xh[D], v[D], vh[D], buf2[D], rho, rhoh;
+  int pt;
+};
+template <int D>
+__device__ __forceinline__ PermVals<D> perm_load(const SArr<D>& S, int64_t i) {
+  PermVals<D> p;
+#pragma unroll
+  for (int d = 0; d < D; ++d) {
+    p.x[d] = S.x[d][i];
+    p.xh[d] = S.xh[d][i];
+    p.v[d] = S.v[d][i];
+    p.vh[d] = S.vh[d][i];
+    p.buf2[d] = S.buf2[d][i];
+  }
+  p.rho = S.rho[i];
+  p.rhoh = S.rhoh[i];
+  p.pt = S.pt[i];
+  return p;
+}
+// new[k] = the state p of one particle; cΔx restarts at 0
+// (src/sphproblem.jl:229), P(ρ) and 1/ρ are recomputed for stage 1; b takes
+// the max |x - offset| of the FP32 prefilter copy
+template <int D>
+__device__ __forceinline__ void perm_store(const StepConst& c, const SArr<D>& S, const PermOut<D>& O,
+                                           const PermVals<D>& p, int64_t k, double& b) {
   double bk = 0.0;
 #pragma unroll
   for (int d = 0; d < D; ++d) {
-    const double xv = S.x[d][i];
-    O.x[d][k] = xv;
-    const double rel = xv - O.off[d];
+    O.x[d][k] = p.x[d];
+    const double rel = p.x[d] - O.off[d];
     O.pf[d][k] = (float)rel;
     bk = fmax(bk, fabs(rel));
   }
   if (bk != bk) bk = INFINITY;  // NaN coordinate: every candidate of the set goes to FP64
   b = fmax(b, bk);
-  const int pt = S.pt[i];
-  O.pt[k] = pt;
-  const double r = S.rho[i];
-  O.rho[k] = r;
-  O.rhoh[k] = S.rhoh[i];
-  S.P1[k] = eos(r, c.gamma, c.rho0, c.P0, pt);
-  S.ir[k] = 1.0 / r;
+  O.pt[k] = p.pt;
+  O.rho[k] = p.rho;
+  O.rhoh[k] = p.rhoh;
+  S.P1[k] = eos(p.rho, c.gamma, c.rho0, c.P0, p.pt);
+  S.ir[k] = 1.0 / p.rho;
 #pragma unroll
   for (int d = 0; d < D; ++d) {
-    O.xh[d][k] = S.xh[d][i];
-    O.v[d][k] = S.v[d][i];
-    O.vh[d][k] = S.vh[d][i];
-    O.buf2[d][k] = S.buf2[d][i];
+    O.xh[d][k] = p.xh[d];
+    O.v[d][k] = p.v[d];
+    O.vh[d][k] = p.vh[d];
+    O.buf2[d][k] = p.buf2[d];
     S.cdx[d][k] = 0.0;
   }
+}
+// new[k] = old[i] for the whole cell-order state of one particle
+template <int D>
+__device__ __forceinline__ void permute_one(const StepConst& c, const SArr<D>& S, const PermOut<D>& O, int64_t i,
+                                            int64_t k, double& b) {
+  perm_store<D>(c, S, O, perm_load<D>(S, i), k, b);
 }
 
 // new[k] = old[perm[k]] for the whole cell-order state
@@ -582,13 +607,17 @@ template <int D>
 __global__ void k_rank_permute(StepConst c, int64_t N, const int32_t* __restrict__ tmp,
                                const int32_t* __restrict__ key, const int32_t* __restrict__ cellstart,
                                const int32_t* __restrict__ ord, int32_t* __restrict__ perm,
-                               int32_t* __restrict__ skey, int32_t* __restrict__ orig, SArr<D> S, PermOut<D> O) {
+                               int32_t* __restrict__ skey, int32_t* __restrict__ orig, SArr<D> S, PermOut<D> O,
+                               const int32_t* __restrict__ tord) {
   const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   double b = 0.0;
   if (q < N) {
-    int32_t i = 0;
-    const int64_t k = rank_in_cell(tmp, key, cellstart, ord, q, perm, skey, orig, &i);
-    permute_one<D>(c, S, O, i, k, b);
+    // the particle's state is loaded as soon as its index is known, so that
+    // these loads overlap the rank's (the rank's stores could alias them)
+    const int32_t i = tmp[q];
+    const PermVals<D> pv = perm_load<D>(S, i);
+    const int64_t k = rank_in_cell(tmp, key, cellstart, ord, q, perm, skey, orig, nullptr, tord);
+    perm_store<D>(c, S, O, pv, k, b);
   }
   b = warp_max(b);
   if ((threadIdx.x & 31) == 0) atomic_max_pos(O.pfmax, b);
@@ -899,7 +928,7 @@ static int rebuild(sph_handle* h, const StepConst& c, int* ovf_dev) {
       k_rank_permute<D><<<nblocks(h->N, ptb), ptb, 0, core.st>>>(
           c, h->N, core.tmp.as<int32_t>(), core.key.as<int32_t>(), core.cellstart.as<int32_t>(),
           core.orig.as<int32_t>(), core.perm.as<int32_t>(), core.skey.as<int32_t>(), core.orig_b.as<int32_t>(),
-          make_arr<D>(h), alt);
+          make_arr<D>(h), alt, core.tord.as<int32_t>());
       GC_LAUNCHED();
       timer_end(T_STATE, core.st);
       core.sort_done();
@@ -1029,6 +1058,9 @@ static int enqueue_stages(sph_handle* h, StepConst& c, Scal* dsc, int32_t& cspmc
   c.fb_eta2 = 0.01 * (c.fb_r0 * c.fb_r0);
   const int L = choose_lanes(h);
   const bool once = L > 1;  // pair-once passes; L = 1 keeps the serial gather (bit-identical to the oracle)
+  // W of the pairs is read by xsphcorr! and by a CSPM step's cspmcorr! only
+  // (the call's ∑W is recomputed from the positions at its end)
+  c.need_w = (p.xsph_eps > 0) || (p.cspmn > 0 && cspmcnt == p.cspmn);
   bool folded = false;  // k_step_end's work done by pass B2's last block
   // stage 1 (predictor) and stage 2 (corrector); the pair-once form times
   // pass A as the stage and the two row-sum passes together

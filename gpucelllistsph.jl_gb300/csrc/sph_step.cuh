@@ -29,6 +29,7 @@ struct StepConst {
   double reb_thr;  // update! is due after a step whose max |cΔx| passes this (0.9 (dist - H))
   int dt_relative; // Δt_stepping's velocity term from pair-relative Δv·Δx instead of absolute v·x
   int count_reb;   // this step's decision counts toward the call's update! total
+  int need_w;      // pass A stage 1 writes W: xsphcorr! or this step's cspmcorr! reads it
 };
 
 // device scalars of a running solve
