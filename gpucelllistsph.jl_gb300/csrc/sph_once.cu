@@ -208,26 +208,39 @@ __global__ void __launch_bounds__(32 * L) k_pairB1(StepConst c, const Scal* __re
                                                    PairBuf B) {
   if (*S.ovf) return;
   __shared__ RowSums<D> R;
-  pairB_sums<D, L>(S, B, N, R);
-  if (threadIdx.x >= 32) return;
+  // warp 0 updates the block's 32 particles: their state is loaded before the
+  // row sums, so that these loads overlap them (the row sums read only the
+  // entry slots)
   const int64_t k = (int64_t)blockIdx.x * 32 + threadIdx.x;
-  if (k >= N) return;
+  const bool mine = threadIdx.x < 32 && k < N;
+  int ptk = 0;
+  double hdt = 0.0, rh0 = 0.0, vh0[D], xh0[D];
+  if (mine) {
+    ptk = S.pt[k];
+    hdt = sc->dt * 0.5;
+    rh0 = S.rhoh[k];
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      vh0[d] = S.vh[d][k];
+      xh0[d] = S.xh[d][k];
+    }
+  }
+  pairB_sums<D, L>(S, B, N, R);
+  if (!mine) return;
   double a[D];
 #pragma unroll
   for (int d = 0; d < D; ++d) a[d] = R.a[d][threadIdx.x];
   const double drho = R.drho[threadIdx.x];
   a[1] = a[1] - c.g;
-  const int ptk = S.pt[k];
-  const double hdt = sc->dt * 0.5;
-  double rv = S.rhoh[k] + drho * hdt;
+  double rv = rh0 + drho * hdt;
   if (rv < c.rho0 && ptk < 0) rv = c.rho0;
   S.rhoh[k] = rv;
 #pragma unroll
   for (int d = 0; d < D; ++d) {
-    double vh = S.vh[d][k];
+    double vh = vh0[d];
     if (ptk > 1) vh = vh + a[d] * hdt;
     S.vh[d][k] = vh;
-    S.xh[d][k] = S.xh[d][k] + vh * hdt;
+    S.xh[d][k] = xh0[d] + vh * hdt;
   }
   S.P2[k] = eos(rv, c.gamma, c.rho0, c.P0, ptk);
   S.irh[k] = 1.0 / rv;
@@ -240,23 +253,39 @@ __global__ void __launch_bounds__(32 * L) k_pairB2(StepConst c, Scal* __restrict
                                                    PairBuf B, NextBin nb) {
   if (*S.ovf) return;  // uniform over the grid, before the barriers below
   __shared__ RowSums<D> R;
-  pairB_sums<D, L>(S, B, N, R);
   const bool w0 = threadIdx.x < 32;
   const int64_t k = (int64_t)blockIdx.x * 32 + threadIdx.x;
+  // warp 0's particles' state, loaded before the row sums so that these
+  // loads overlap them (the row sums read only the entry slots)
+  const bool mine = w0 && k < N;
+  int ptk = 0;
+  double dt = 0.0, p2 = 0.0, rh = 0.0, r0 = 0.0, v0[D], cd0[D], x0[D];
+  if (mine) {
+    ptk = S.pt[k];
+    dt = sc->dt;
+    p2 = S.P2[k];
+    rh = S.rhoh[k];
+    r0 = S.rho[k];
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      v0[d] = S.v[d][k];
+      cd0[d] = S.cdx[d][k];
+      x0[d] = S.x[d][k];
+    }
+  }
+  pairB_sums<D, L>(S, B, N, R);
   if (!w0 && !nb.key) return;
   double mc = 0.0;
-  if (w0 && k < N) {
+  if (mine) {
     double a[D], xn[D];
 #pragma unroll
     for (int d = 0; d < D; ++d) a[d] = R.a[d][threadIdx.x];
     const double drho = R.drho[threadIdx.x];
-    const double dt = sc->dt;
     a[1] = a[1] - c.g;
-    const int ptk = S.pt[k];
     S.drho[k] = drho;
-    S.Plast[k] = S.P2[k];
-    const double epsi = -(drho / S.rhoh[k]) * dt;
-    double rv = S.rho[k] * (2.0 - epsi) / (2.0 + epsi);
+    S.Plast[k] = p2;
+    const double epsi = -(drho / rh) * dt;
+    double rv = r0 * (2.0 - epsi) / (2.0 + epsi);
     if (rv < c.rho0 && ptk <= 1) rv = c.rho0;
     S.rho[k] = rv;
     S.rhoho[k] = rv;
@@ -266,15 +295,15 @@ __global__ void __launch_bounds__(32 * L) k_pairB2(StepConst c, Scal* __restrict
 #pragma unroll
     for (int d = 0; d < D; ++d) {
       S.a[d][k] = a[d];
-      const double vv = S.v[d][k];
+      const double vv = v0[d];
       const double nv = vv + a[d] * dt * ml;
       S.vho[d][k] = nv;
       S.v[d][k] = nv;
       const double ddx = (vv + nv) * 0.5 * dt;
-      const double cd = S.cdx[d][k] + ddx;
+      const double cd = cd0[d] + ddx;
       S.cdx[d][k] = cd;
       mc = fmax(mc, fabs(cd));
-      const double xv = S.x[d][k] + ddx;
+      const double xv = x0[d] + ddx;
       S.xho[d][k] = xv;
       S.xo[d][k] = xv;
       xn[d] = xv;
