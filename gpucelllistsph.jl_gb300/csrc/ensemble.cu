@@ -39,10 +39,10 @@ struct EnsInst {
   // branch loads the group it needs with one vector load
   float4 kA;      // H², 1/H, dwc, cell edge
   float4 kB;      // ρ₀, η², m₀, DDTgz
-  float4 kC;      // kddt, kav, kvisc, P₀
+  float4 kC;      // kddt, kav, kvisc, (unused)
   float4 kD;      // pfcr, hp1, 2h, kpf
   float4 kE;      // pc[0..3]
-  float4 kFB[2];  // fb_d, fb_r0, fb_eta2, 1/ρ₀ of stage 1 and stage 2
+  float4 kFB[2];  // fb_d, fb_r0, fb_eta2, (unused) of stage 1 and stage 2
   double origin[3];
   double csinv;  // 1 / cell edge
   double cs;
@@ -240,18 +240,15 @@ __device__ __forceinline__ float dot32(const float* a, const float* b) {
 }
 
 // P0 ((1+e)^γ - 1), e = δρ/ρ₀, without cancellation (pressure(), src/gpukernels_sph.jl:691-697)
-__device__ __forceinline__ float eos32g(float dr, int pt, float rho0inv, float P0, int gamma) {
+__device__ __forceinline__ float eos32(float dr, int pt, const EnsInst& I) {
   if (pt <= 1 && dr < 0.f) return 0.f;
-  const float e = dr * rho0inv;
+  const float e = dr * I.rho0inv;
   float p;
-  if (gamma == 7)
+  if (I.gamma == 7)
     p = e * (7.f + e * (21.f + e * (35.f + e * (35.f + e * (21.f + e * (7.f + e))))));
   else
-    p = expm1f((float)gamma * log1pf(e));
-  return P0 * p;
-}
-__device__ __forceinline__ float eos32(float dr, int pt, const EnsInst& I) {
-  return eos32g(dr, pt, I.rho0inv, I.P0, I.gamma);
+    p = expm1f((float)I.gamma * log1pf(e));
+  return I.P0 * p;
 }
 
 
@@ -797,7 +794,7 @@ __global__ void __launch_bounds__(ENS_MAX_TPB, 2) k_ens_stage(EnsArr A, const En
       if (pti * ptj > 0) {
         // ∂v∂t!
         float Pj = Prec;
-        if (!rec_has_p<D, STAGE>()) Pj = eos32g(drj, ptj, I.kFB[0].w, I.kC.w, I.gamma);
+        if (!rec_has_p<D, STAGE>()) Pj = eos32(drj, ptj, I);
         gsc = -kB.z * (Pi + Pj) * (irhoi * irhoj);
       }
       if (both) {
@@ -2204,10 +2201,10 @@ int ens_add(gcsph_ens* e, int64_t n, const double* x, const double* v, const dou
   I.kpf = (float)(p->s / p->m0);
   I.kA = make_float4(I.H2, I.Hinv, I.dwc, I.csf);
   I.kB = make_float4(I.rho0, I.eta2, I.m0, I.DDTgz);
-  I.kC = make_float4(I.kddt, I.kav, I.kvisc, I.P0);
+  I.kC = make_float4(I.kddt, I.kav, I.kvisc, 0.f);
   I.kD = make_float4(I.pfcr, I.hp1, I.twoh, I.kpf);
   I.kE = make_float4(I.pc[0], I.pc[1], I.pc[2], I.pc[3]);
-  for (int st = 0; st < 2; ++st) I.kFB[st] = make_float4(I.fb_d[st], I.fb_r0[st], I.fb_eta2[st], I.rho0inv);
+  for (int st = 0; st < 2; ++st) I.kFB[st] = make_float4(I.fb_d[st], I.fb_r0[st], I.fb_eta2[st], 0.f);
   // host staging in the engine's types
   std::vector<float> vf((size_t)D * n, 0.f), drf((size_t)n);
   std::vector<int32_t> ids((size_t)n);
