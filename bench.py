@@ -157,8 +157,8 @@ def algorithmic_flops_stage1(case, x, v):
 # DRAM bytes (read + write) of one stage-1 pass A launch on this workload and
 # its FP64 pipe's busy fraction (of active cycles), from one ncu --set full
 # capture of that launch (one block per SM, 103,881 pairs)
-PAIRA_STAGE1_DRAM_BYTES = 2_089_728 + 768
-PAIRA_STAGE1_FP64_PIPE = 0.771
+PAIRA_STAGE1_DRAM_BYTES = 2_215_168 + 124_672
+PAIRA_STAGE1_FP64_PIPE = 0.764
 
 
 class Clocks:
