@@ -63,7 +63,7 @@ struct EnsInst {
   float pfcr;                            // 1.5π / 2h: the cosine's argument per unit r in ∂v∂tpF!
   // products of the above that the stage passes use as one factor
   float kddt;                            // DDTkh m₀ (∂ρ∂tDDT!)
-  float kav;                             // 2 α c₀ h m₀ (∂v∂t_av!: -Π m₀ / ((Δv·Δx) / ((r² + η²)(ρi + ρj))))
+  float kav;                             // 2 α c₀ h m₀: ∂v∂t_av!'s -Π m₀ over (Δv·Δx) / ((r² + η²)(ρi + ρj))
   float kvisc;                           // 4 ν m₀ (∂v∂t_visc!)
   float kpf;                             // s / m₀ (∂v∂tpF!)
   int p_off;                             // first particle of the instance (list entries are instance-local)

@@ -22,8 +22,9 @@ __device__ inline void fb_pair(const StepConst& c, const double* dx, double r2, 
 }
 
 // Pass A: one thread per pair (k, m), k < m in cell order.  Stage 1 at
-// (x, ρ, v, P(ρ)) also writes ∇W, and W in the steps that read it; stage 2 at (xΔt½, ρΔt½, vΔt½,
-// P(ρΔt½)) with the stage-1 ∇W and fbmolforce! at x.  The reference's terms,
+// (x, ρ, v, P(ρ)) also writes ∇W, and W in the steps that read it; stage 2
+// at (xΔt½, ρΔt½, vΔt½, P(ρΔt½)) with the stage-1 ∇W and fbmolforce! at x.
+// The reference's terms,
 // src/gpukernels_sph.jl, in their algebraically equal pair-once forms:
 //  * ∇W = Δx d𝒲/r with d𝒲/r = dWr (1 - u)^3 -- no division by r;
 //  * ∂ρ∂tDDT! (:542-631): both sides share DDTkh m₀ (-Δx·∇W)/(r² + η²);
