@@ -402,14 +402,20 @@ def run_batched(g, args, plain_c1, hbm_peak):
             roof[st] = {"avg_launch_us": avg_s * 1e6, "alg_bytes_per_launch": alg,
                         "achieved_gbs": alg / avg_s / 1e9, "frac_of_hbm": alg / avg_s / 1e9 / hbm_peak}
     roof["note"] = ("bytes = N(12D+16) + 2P*4 with P the pairs within H at the instances' initial states "
-                    "(update!); the passes are bound by instruction issue (72-74% of issue slots in ncu), "
-                    "their working set per step is re-read from L2")
+                    "(update!); the passes are bound by instruction issue (63-67% of issue slots in ncu, with "
+                    "long-scoreboard waits on the neighbour records), their working set per step is re-read "
+                    "from L2")
     sizes = sorted(wl, key=lambda t: t[0].N)
     sample = [sizes[0][0], sizes[len(sizes) // 2][0], sizes[-1][0]]
     plain_ps = sum(c.N * 30 for c in sample)
     plain = plain_ps / sum(c.N * 30 / fp64_rate_alone(g, c, 30) for c in sample)
-    small = sizes[0]
-    err = fp32_error_vs_fp64(g, small[0], small[1], small[2])
+    # the FP32 error after 100 steps on the same three instances; the line's
+    # error_vs_fp64 is the largest of the three per field
+    picks = [sizes[0], sizes[len(sizes) // 2], sizes[-1]]
+    errs = [fp32_error_vs_fp64(g, c, al, de) for c, al, de in picks]
+    err = {k: max(e[k] for e in errs) for k in ("rho", "rho_minus_rho0", "v", "displacement")}
+    err.update({"steps": 100, "of": "the largest of the smallest, median and largest instance",
+                "by_instance": errs})
     return {"workload": "256 independent 2-D dam breaks, fluid counts log-uniform 2k-200k, aspect 0.5-4, "
                         "dx 0.005-0.02, alpha 0.005-0.05, delta 0.05-0.2 (seeded), FP32 pair arithmetic, "
                         "FP64 positions",
