@@ -159,6 +159,10 @@ def algorithmic_flops_stage1(case, x, v):
 # capture of that launch (one block per SM, 103,881 pairs)
 PAIRA_STAGE1_DRAM_BYTES = 2_215_168 + 124_672
 PAIRA_STAGE1_FP64_PIPE = 0.764
+# the FP32 ensemble's stage passes are bound by instruction issue: their busy
+# fraction of the issue slots (of active SMs) in one ncu --set full capture of
+# the 64-instance 2-D ensemble (one launch of each stage)
+ENS_STAGE_ISSUE_FRAC = {"stage1": 0.628, "stage2": 0.673}
 
 
 class Clocks:
@@ -400,7 +404,8 @@ def run_batched(g, args, plain_c1, hbm_peak):
             avg_s = fam[st]["total_ms"] / 1e3 / fam[st]["launches"]
             alg = ens_stage_bytes(2, tot["particles"], pairs0)
             roof[st] = {"avg_launch_us": avg_s * 1e6, "alg_bytes_per_launch": alg,
-                        "achieved_gbs": alg / avg_s / 1e9, "frac_of_hbm": alg / avg_s / 1e9 / hbm_peak}
+                        "achieved_gbs": alg / avg_s / 1e9, "frac_of_hbm": alg / avg_s / 1e9 / hbm_peak,
+                        "issue_slots_busy_ncu": ENS_STAGE_ISSUE_FRAC[st]}
     roof["note"] = ("bytes = N(12D+16) + 2P*4 with P the pairs within H at the instances' initial states "
                     "(update!); the passes are bound by instruction issue (63-67% of issue slots in ncu, with "
                     "long-scoreboard waits on the neighbour records), their working set per step is re-read "
