@@ -52,3 +52,25 @@ def test_pass_a_flop_count_by_hand():
     ff = (7 * D + 1) + 2 * 34 + (3 * D + 4) + 3 * D + (5 * D + 10)
     fb_in = (3 * D + 1) + (3 * D + 14)
     assert flops == 3 * geometry + ff + fb_in == 236
+
+
+def test_clock_record_reads_the_sampler_output(tmp_path):
+    """The bench's clock record from the nvidia-smi sampler's CSV (no GPU): the
+    median SM clock, the maximum, the number of samples and every throttle
+    reason seen active in any sample."""
+    bench = _bench_module()
+    clk = bench.Clocks(0)
+    clk.path = str(tmp_path / "clocks.csv")
+    rows = [
+        "0, 2070, 2070, 612.3, 0x0000000000000000, Not Active, Not Active, Not Active, Not Active",
+        "0, 2055, 2070, 640.1, 0x0000000000000004, Not Active, Not Active, Not Active, Active",
+        "0, 2070, 2070, 655.0, 0x0000000000000000, Not Active, Not Active, Not Active, Not Active",
+        "garbage line",
+    ]
+    open(clk.path, "w").write("\n".join(rows) + "\n")
+    s = clk.summary()
+    assert s["sm_mhz"] == 2070.0 and s["sm_max_mhz"] == 2070.0
+    assert s["samples"] == 3
+    assert s["reasons"] == ["sw_power_cap"]
+    clk.path = str(tmp_path / "missing.csv")
+    assert clk.summary()["reasons"] == ["unsampled"]
