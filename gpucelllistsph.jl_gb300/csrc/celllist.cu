@@ -860,14 +860,24 @@ __device__ __forceinline__ void pairs32_row(const double* __restrict__ x0, const
       visit(m, t < tot && m != k);
     }
   } else {
-    for (int dy = up ? 0 : -1; dy <= 1; ++dy) {
-      const int y = cy + dy;
-      if (y < 0 || y >= ny) continue;
-      const int64_t base = (int64_t)nx * (int64_t)y;
-      int32_t m0 = cellstart[base + xlo];
-      const int32_t m1 = cellstart[base + xhi + 1];
-      if (up && dy == 0) m0 = (int32_t)(k + 1);  // k's own row: k lies in it
-      for (int32_t mb = m0; mb < m1; mb += L) {
+    // the three rows' candidate ranges first, so that their six loads go out
+    // together rather than one row's after the previous row's candidates
+    int32_t rm0[3], rm1[3];
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+      const int dy = r - 1, y = cy + dy;
+      rm0[r] = rm1[r] = 0;
+      if (!(up && dy < 0) && y >= 0 && y < ny) {
+        const int64_t base = (int64_t)nx * (int64_t)y;
+        rm0[r] = cellstart[base + xlo];
+        rm1[r] = cellstart[base + xhi + 1];
+        if (up && dy == 0) rm0[r] = (int32_t)(k + 1);  // k's own row: k lies in it
+      }
+    }
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+      const int32_t m1 = rm1[r];
+      for (int32_t mb = rm0[r]; mb < m1; mb += L) {
         const int32_t m = mb + lane;
         visit(m, m < m1 && m != k);
       }
